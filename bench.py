@@ -1,0 +1,316 @@
+#!/usr/bin/env python
+"""Benchmark of the ray-cast hot path: batched TriMesh::cast_ray_and_get_normal on the
+65,536-triangle terrain (256 x 128 height field) with 1,048,576 rays, max_toi = 100, solid.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+A step is one pass of the path over the whole ray batch (Morton sort of the rays + LBVH traversal
++ ray/triangle tests + result write), through the library's C ABI on device-resident buffers.
+`e2e` is the same call with pinned host buffers (host->device rays and device->host hits inside
+the timed region). L2 is flushed (256 MiB write) before every timed step, outside the step's
+events. Under torchrun each rank runs its own replica of the workload on its GPU (no collective in
+the data path); value = rays of all ranks / the slowest rank's time.
+
+--impl reference times the oracle (the C++ restatement of parry3d's f32 path, the only CPU
+implementation of the reference that builds here: no Rust toolchain) on all host threads, on the
+same workload, metric and unit; under torchrun only rank 0 runs it.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+N_RAYS = 1 << 20
+MAX_TOI = 100.0
+METRIC = "Mrays/s"
+WORKLOAD = "terrain_trimesh_rays"
+
+
+def config(world: int, n_rays: int) -> dict:
+    return {"workload": WORKLOAD, "triangles": 65536, "grid": "256x128", "rays": n_rays, "max_toi": MAX_TOI,
+            "solid": True, "ray_dirs": "uniform downward hemisphere", "l2": "flushed before each step (256 MiB write)",
+            "parallelism": f"replicas{world}"}
+
+
+def dist_info():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+class ClockSampler:
+    """Samples nvidia-smi clocks / throttle reasons during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                         stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self) -> dict | None:
+        if self.proc is None:
+            return None
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.close()
+        sm, smax, reasons = [], [], set()
+        names = ["active", "hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in Path(self.path).read_text().splitlines():
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, val in zip(names[1:], parts[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(nm)
+        os.unlink(self.path)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peak_hbm() -> tuple[float, str]:
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        try:
+            return float(json.loads(p.read_text())["hbm_gbs"]), "measured"
+        except Exception:
+            pass
+    return 6800.0, "fallback"
+
+
+def profiled_traffic(name: str) -> float | None:
+    """dram read+write bytes per launch recorded from an ncu capture (profiles/<name>.txt)."""
+    p = ROOT / "profiles" / f"{name}.txt"
+    if not p.exists():
+        return None
+    for line in p.read_text().splitlines():
+        if line.startswith("dram_bytes_per_launch_full_size:"):
+            try:
+                return float(line.split(":", 1)[1].split()[0])
+            except ValueError:
+                return None
+    return None
+
+
+def cpu_oracle_rays(v, i, rays, reps: int):
+    """Times the oracle (f32 restatement of parry3d) over all host threads; returns (Mrays/s, stats, threads)."""
+    from oracle import build as ob
+    ob.build()
+    from oracle import oracle as O
+    threads = os.cpu_count() or 1
+    m = O.TriMesh(v, i, "f32")
+    _, _, _, stats = m.cast_rays_and_get_normal(rays, MAX_TOI, threads=threads, want_stats=True)
+    times = []
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        m.cast_rays_and_get_normal(rays, MAX_TOI, threads=threads)
+        times.append(time.perf_counter() - t0)
+    return len(rays) / statistics.median(times) / 1e6, stats, threads
+
+
+def run_reference(args) -> int:
+    world, rank, local = dist_info()
+    if rank != 0:
+        return 0
+    from parry_gb300 import workloads as W
+    from oracle import build as ob
+    ob.build()
+    from oracle import oracle as O
+    v, i = W.terrain_mesh()
+    rays = W.terrain_rays(args.n_rays)
+    threads = os.cpu_count() or 1
+    m = O.TriMesh(v, i, "f32")
+    for _ in range(args.warmup):
+        m.cast_rays_and_get_normal(rays, MAX_TOI, threads=threads)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        m.cast_rays_and_get_normal(rays, MAX_TOI, threads=threads)
+    dt = time.perf_counter() - t0
+    ms = dt / args.steps * 1e3
+    value = args.n_rays / (ms / 1e3) / 1e6
+    line = {"impl": "reference", "metric": METRIC, "value": round(value, 3), "unit": "Mrays/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 3), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": config(1, args.n_rays),
+            "cpu_baseline": {"value": round(value, 3), "unit": "Mrays/s", "cores": threads, "kind": "port",
+                             "sample": f"the full workload ({args.n_rays} rays) per step; C++ restatement of parry3d "
+                                       f"0.25 f32 (binned BVH, find_best), std::thread over {threads} threads"},
+            "e2e": {"value": round(value, 3), "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "note": "parry3d itself is Rust and cannot be built here (no cargo/rustc); the oracle port stands in"}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_gb300(args) -> int:
+    import numpy as np
+    import torch
+
+    world, rank, local = dist_info()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    from parry_gb300 import _build
+    _build.build()
+    import parry_gb300 as pg
+    from parry_gb300 import workloads as W
+
+    n = args.n_rays
+    v, i = W.terrain_mesh()
+    rays_h = W.terrain_rays(n)
+    ctx = pg.Context(device=local)
+    stream = torch.cuda.current_stream()
+    ctx.set_stream(stream.cuda_stream)
+    mesh = pg.TriMesh(ctx, v, i)
+    rays_d = torch.from_numpy(rays_h).cuda()
+    feat = torch.empty(n, dtype=torch.int32, device="cuda")
+    toi = torch.empty(n, dtype=torch.float32, device="cuda")
+    nrm = torch.empty((n, 3), dtype=torch.float32, device="cuda")
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+
+    def step():
+        mesh.cast_rays_and_get_normal(rays_d, MAX_TOI, out=(feat, toi, nrm))
+
+    for _ in range(max(args.warmup, 3) if args.warmup >= 3 else args.warmup):
+        step()
+    torch.cuda.synchronize()
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    ctx.enable_kernel_timing(True)
+    ctx.reset_kernel_timing()
+    launches0 = ctx.kernel_launches
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    sampler = ClockSampler(local)
+    barrier()
+    torch.cuda.synchronize()
+    sampler.start()
+    for k in range(args.steps):
+        flush.zero_()
+        starts[k].record(stream)
+        step()
+        ends[k].record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    clocks = sampler.stop()
+    launches = ctx.kernel_launches - launches0
+    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    ms = sum(step_ms) / len(step_ms)
+    k_ms, k_n = ctx.kernel_time("trimesh_rays")
+    s_ms, s_n = ctx.kernel_time("ray_sort")
+    ctx.enable_kernel_timing(False)
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * n / (ms / 1e3) / 1e6
+
+    # e2e: the same public call with pinned host buffers (H2D rays, D2H results inside the region)
+    rays_p = torch.from_numpy(rays_h).pin_memory()
+    feat_p = torch.empty(n, dtype=torch.int32, pin_memory=True)
+    toi_p = torch.empty(n, dtype=torch.float32, pin_memory=True)
+    nrm_p = torch.empty((n, 3), dtype=torch.float32, pin_memory=True)
+    for _ in range(2):
+        mesh.cast_rays_and_get_normal(rays_p, MAX_TOI, out=(feat_p, toi_p, nrm_p))
+    e2e_ms = []
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        mesh.cast_rays_and_get_normal(rays_p, MAX_TOI, out=(feat_p, toi_p, nrm_p))
+        e2e_ms.append((time.perf_counter() - t0) * 1e3)
+    e2e = statistics.mean(e2e_ms)
+    if world > 1:
+        t = torch.tensor([e2e], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e = float(t.item())
+    e2e_value = world * n / (e2e / 1e3) / 1e6
+    same = bool(np.array_equal(feat_p.numpy(), feat.cpu().numpy()))
+
+    if rank == 0:
+        cpu_value, stats, threads = cpu_oracle_rays(v, i, rays_h, reps=3)
+        wide = stats["wide_visits"] / n
+        leaves = stats["leaf_tests"] / n
+        bytes_per_ray = 24 + 20 + 64 * wide + 36 * leaves
+        k_avg = k_ms / max(k_n, 1)
+        achieved = bytes_per_ray * n / (k_avg / 1e3) / 1e9
+        peak, peak_kind = measured_peak_hbm()
+        traffic = profiled_traffic("trimesh_rays_terrain")
+        line = {
+            "metric": METRIC, "value": round(value, 2), "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(ms, 4), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": config(world, n),
+            "e2e": {"value": round(e2e_value, 2), "unit": "Mrays/s", "h2d_bytes_per_step": n * 24,
+                    "d2h_bytes_per_step": n * 20, "ms_per_step": round(e2e, 4), "matches_device_path": same},
+            "roofline": {"bound": "hbm", "kernel": "k_trimesh_rays", "achieved": round(achieved, 1), "peak": peak,
+                         "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": traffic,
+                         "peak_source": peak_kind,
+                         "bytes_per_ray": round(bytes_per_ray, 1),
+                         "bytes_model": "24 B ray + 20 B hit + 64 B x wide-node visits + 36 B x triangle tests, visit "
+                                        "counts of the f32 oracle's parry binned BVH on the same rays",
+                         "oracle_wide_visits_per_ray": round(wide, 3), "oracle_tri_tests_per_ray": round(leaves, 3),
+                         "kernel_ms": round(k_avg, 4), "sort_ms": round(s_ms / max(s_n, 1), 4)},
+            "cpu_baseline": {"value": round(cpu_value, 3), "unit": "Mrays/s", "cores": threads, "kind": "port",
+                             "sample": f"the full workload ({n} rays), median of 3; C++ restatement of parry3d f32"},
+            "gpu_launches": launches,
+            "clocks": clocks,
+        }
+        print(json.dumps(line), flush=True)
+    ctx.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+def main() -> int:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--n-rays", type=int, default=N_RAYS)
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gb300(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,130 @@
+/*
+ * libparrygpu — GB300 (sm_103a) batched implementation of parry3d's data-parallel query path,
+ * exported as a plain C ABI.
+ *
+ * Every entry point replaces a CPU loop over one parry3d call; the reference interface each one
+ * replaces is cited (paths relative to the parry repository).
+ *
+ * Conventions
+ *  - Pointers may be device pointers or host pointers (pageable or pinned); the library checks
+ *    each with cudaPointerGetAttributes. Host inputs are staged through library-owned device
+ *    buffers. A call whose outputs are all device pointers is asynchronous on the context's
+ *    stream; a call with any host output synchronises that stream before returning.
+ *  - Layouts follow parry3d's #[repr(C)] types: Aabb = {mins xyz, maxs xyz} (6 floats),
+ *    Ray = {origin xyz, dir xyz} (6 floats), Isometry = pose7 {qi, qj, qk, qw, tx, ty, tz}.
+ *  - The library owns the device memory behind each handle; the caller owns every output buffer.
+ *  - One stream per context. A context is not thread-safe; distinct contexts are.
+ *  - Errors: every function returns a parrygpu_status. Query results that parry expresses as
+ *    Option::None (no hit, no contact) are reported in the output arrays, not as errors.
+ */
+#ifndef PARRY_GPU_H
+#define PARRY_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum parrygpu_status {
+  PARRYGPU_OK = 0,
+  PARRYGPU_INVALID_ARG = 1,
+  /* parry: Err(Unsupported) for a shape pair without an implementation (src/query/error.rs:146-147). */
+  PARRYGPU_UNSUPPORTED_PAIR = 2,
+  /* The caller's pair buffer is too small; *n_out still holds the full pair count. */
+  PARRYGPU_CAPACITY_EXCEEDED = 3,
+  PARRYGPU_TIMEOUT = 5,
+  PARRYGPU_CUDA_ERROR = 6,
+  /* A traversal stack overflowed its fixed depth (the affected queries report no result). */
+  PARRYGPU_STACK_OVERFLOW = 7,
+  PARRYGPU_NO_DEVICE = 8
+} parrygpu_status;
+
+typedef struct parrygpu_ctx parrygpu_ctx;
+typedef struct parrygpu_bvh parrygpu_bvh;
+typedef struct parrygpu_trimesh parrygpu_trimesh;
+
+typedef struct parrygpu_config {
+  int device;              /* CUDA device ordinal */
+  uint32_t ray_block;      /* threads per block for ray traversal (0 = library default) */
+  uint32_t sort_rays;      /* 1 = Morton-sort rays before traversal (default), 0 = input order */
+  uint32_t reserved[5];
+} parrygpu_config;
+
+/* ---- context ---------------------------------------------------------------------------- */
+
+/* Fills *cfg with the library defaults. */
+void parrygpu_default_config(parrygpu_config* cfg);
+/* Creates a context on cfg->device (cfg may be NULL for defaults) with its own stream. */
+parrygpu_status parrygpu_create(parrygpu_ctx** out, const parrygpu_config* cfg);
+void parrygpu_destroy(parrygpu_ctx* ctx);
+/* Makes the context launch on `stream` (a cudaStream_t; NULL = the context's own stream). */
+parrygpu_status parrygpu_set_stream(parrygpu_ctx* ctx, void* stream);
+/* Waits for the context's stream; reports device-side error flags raised since the last sync. */
+parrygpu_status parrygpu_sync(parrygpu_ctx* ctx);
+const char* parrygpu_last_error(const parrygpu_ctx* ctx);
+const char* parrygpu_status_string(parrygpu_status s);
+/* Number of kernels this context has launched since creation. */
+uint64_t parrygpu_kernel_launches(const parrygpu_ctx* ctx);
+/* Per-kernel timing: when enabled, the main kernel of each call is bracketed with CUDA events on
+ * the context stream. parrygpu_kernel_time synchronises and returns the total milliseconds and
+ * launch count recorded for `kernel` (e.g. "trimesh_rays", "ray_sort", "lbvh_build") since the
+ * last reset. No reference counterpart (parry has no device timing). */
+parrygpu_status parrygpu_enable_kernel_timing(parrygpu_ctx* ctx, int enable);
+parrygpu_status parrygpu_kernel_time(parrygpu_ctx* ctx, const char* kernel, double* total_ms, uint64_t* launches);
+parrygpu_status parrygpu_reset_kernel_timing(parrygpu_ctx* ctx);
+
+/* ---- partitioning::Bvh -------------------------------------------------------------------- */
+
+/* Replaces Bvh::from_leaves(strategy, &[Aabb]) (src/partitioning/bvh/bvh_tree.rs:1835-1837).
+ * Builds an LBVH (30-bit Morton codes, device radix sort, Karras hierarchy, atomic bottom-up fit)
+ * over `n` AABBs (n x 6 floats). Leaf data = the AABB's index, as in from_leaves. The tree is
+ * stored in the reference's 64-byte BvhNodeWide layout with the root in wide node 0. */
+parrygpu_status parrygpu_bvh_build(parrygpu_ctx* ctx, const float* aabbs, uint32_t n, parrygpu_bvh** out);
+void parrygpu_bvh_destroy(parrygpu_bvh* bvh);
+/* Replaces Bvh::insert_or_update_partially for every leaf followed by Bvh::refit
+ * (src/partitioning/bvh/bvh_insert.rs:209-231, src/partitioning/bvh/bvh_refit.rs:170-180):
+ * leaf i takes aabbs[i] and every internal AABB is recomputed bottom-up; topology is kept. */
+parrygpu_status parrygpu_bvh_refit(parrygpu_ctx* ctx, parrygpu_bvh* bvh, const float* aabbs);
+/* Replaces Bvh::traverse_bvtt_single_tree::<false> (src/partitioning/bvh/bvh_traverse_bvtt.rs:19-31):
+ * every unordered pair of leaves whose AABBs intersect (inclusive), written as (min, max) pairs
+ * (2 x u32 each) into pairs[0 .. 2*cap). *n_out (host) receives the total pair count. With
+ * sorted != 0 the pairs are in ascending lexicographic order. */
+parrygpu_status parrygpu_bvh_self_pairs(parrygpu_ctx* ctx, const parrygpu_bvh* bvh, uint32_t* pairs, uint64_t cap,
+                                        uint64_t* n_out, int sorted);
+/* Replaces Bvh::leaf_pairs(&other, |a, b| a.intersects(b)) (src/partitioning/bvh/bvh_traverse_bvtt.rs:210-316):
+ * (leaf of a, leaf of b) pairs. As in the reference iterator, the pairs formed by the two roots'
+ * direct children are taken without an AABB check. */
+parrygpu_status parrygpu_bvh_leaf_pairs(parrygpu_ctx* ctx, const parrygpu_bvh* a, const parrygpu_bvh* b, uint32_t* pairs,
+                                        uint64_t cap, uint64_t* n_out, int sorted);
+/* Leaf count (Bvh::leaf_count, bvh_tree.rs:2295-2301) and wide-node count of the tree. */
+parrygpu_status parrygpu_bvh_info(const parrygpu_bvh* bvh, uint32_t* leaf_count, uint32_t* wide_node_count);
+/* Copies the tree's wide nodes (wide_node_count x 64 bytes, BvhNodeWide layout) into `out`. */
+parrygpu_status parrygpu_bvh_copy_nodes(parrygpu_ctx* ctx, const parrygpu_bvh* bvh, void* out);
+
+/* ---- TriMesh ray casts ------------------------------------------------------------------- */
+
+/* Replaces TriMesh::new(vertices, indices) (src/shape/trimesh.rs:607, BVH :1159-1171). */
+parrygpu_status parrygpu_trimesh_create(parrygpu_ctx* ctx, const float* vertices, uint32_t n_vertices,
+                                        const uint32_t* indices, uint32_t n_triangles, parrygpu_trimesh** out);
+void parrygpu_trimesh_destroy(parrygpu_trimesh* mesh);
+/* Replaces a loop of RayCast::cast_ray_and_get_normal(m, ray, max_toi, solid) on a TriMesh
+ * (src/query/ray/ray.rs:393-403 -> src/query/ray/ray_trimesh.rs:17-35). pose7 = the mesh pose m
+ * (NULL = identity). rays: n x 6 floats. Outputs per ray:
+ *   feature[i] = hit triangle t for a front-face hit, t + n_triangles for a back-face hit
+ *                (FeatureId::Face), UINT32_MAX for no hit;
+ *   toi[i]     = time of impact (0 on a miss);
+ *   normal     = n x 3 floats, world-space normal facing the ray origin (may be NULL: then this
+ *                is RayCast::cast_ray, which returns the toi only).
+ * Exact toi ties resolve to the lowest triangle index. `solid` has no effect on triangles in 3-D,
+ * as in the reference. */
+parrygpu_status parrygpu_trimesh_cast_rays(parrygpu_ctx* ctx, const parrygpu_trimesh* mesh, const float* pose7,
+                                           const float* rays, uint32_t n, float max_toi, int solid, uint32_t* feature,
+                                           float* toi, float* normal);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PARRY_GPU_H */

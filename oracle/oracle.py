@@ -1,0 +1,163 @@
+"""Oracle (test infrastructure only): ctypes wrapper over liboracle.so, the C++ restatement of
+parry3d's query path (f32 = parry3d, f64 = parry3d-f64).
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline / reference legs import this, as
+the checker or the timed CPU baseline. The product (parry_gb300, libparrygpu.so) never does.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from pathlib import Path
+
+import numpy as np
+
+_HERE = Path(__file__).resolve().parent
+_lib = None
+
+P = C.c_void_p
+U32 = C.c_uint32
+U64 = C.c_uint64
+I32 = C.c_int
+F32 = C.c_float
+
+_SIGS = {
+    "oracle_trimesh_new_f32": (P, [P, U32, P, U32]),
+    "oracle_trimesh_new_f64": (P, [P, U32, P, U32]),
+    "oracle_trimesh_free_f32": (None, [P]),
+    "oracle_trimesh_free_f64": (None, [P]),
+    "oracle_trimesh_cast_rays_f32": (None, [P, P, P, U64, F32, I32, I32, P, P, P, P]),
+    "oracle_trimesh_cast_rays_f64": (None, [P, P, P, U64, F32, I32, I32, P, P, P, P]),
+    "oracle_trimesh_bvh_nodes_f32": (U32, [P, P, U32]),
+    "oracle_bvh_new_f32": (P, [P, U32]),
+    "oracle_bvh_free_f32": (None, [P]),
+    "oracle_bvh_nodes_f32": (U32, [P, P, U32]),
+    "oracle_bvh_refit_f32": (None, [P, P, U32]),
+    "oracle_bvh_self_pairs_f32": (P, [P]),
+    "oracle_bvh_leaf_pairs_f32": (P, [P, P]),
+    "oracle_pairs_count": (U64, [P]),
+    "oracle_pairs_copy": (None, [P, P]),
+    "oracle_pairs_free": (None, [P]),
+}
+
+
+def lib() -> C.CDLL:
+    global _lib
+    if _lib is None:
+        path = _HERE / "liboracle.so"
+        if not path.exists():
+            from . import build as _b  # type: ignore
+            _b.build()
+        l = C.CDLL(str(path))
+        for name, (res, args) in _SIGS.items():
+            f = getattr(l, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = l
+    return _lib
+
+
+def _p(a: np.ndarray | None):
+    return None if a is None else C.c_void_p(a.ctypes.data)
+
+
+def default_threads() -> int:
+    return os.cpu_count() or 1
+
+
+class TriMesh:
+    """Reference TriMesh (binned BVH) with cast_ray_and_get_normal in f32 or f64."""
+
+    def __init__(self, vertices: np.ndarray, indices: np.ndarray, precision: str = "f32"):
+        self.v = np.ascontiguousarray(vertices, dtype=np.float32)
+        self.i = np.ascontiguousarray(indices, dtype=np.uint32)
+        self.prec = precision
+        self.n_triangles = self.i.shape[0]
+        self._h = getattr(lib(), f"oracle_trimesh_new_{precision}")(_p(self.v), self.v.shape[0], _p(self.i), self.i.shape[0])
+
+    def cast_rays_and_get_normal(self, rays: np.ndarray, max_toi: float, pose: np.ndarray | None = None,
+                                 lowest_index: bool = True, threads: int | None = None, want_stats: bool = False):
+        rays = np.ascontiguousarray(rays, dtype=np.float32)
+        n = rays.shape[0]
+        dt = np.float32 if self.prec == "f32" else np.float64
+        feat = np.empty(n, dtype=np.uint32)
+        toi = np.empty(n, dtype=dt)
+        nrm = np.empty((n, 3), dtype=dt)
+        stats = np.zeros(2, dtype=np.uint64)
+        pz = None if pose is None else np.ascontiguousarray(pose, dtype=np.float32)
+        getattr(lib(), f"oracle_trimesh_cast_rays_{self.prec}")(
+            self._h, _p(pz), _p(rays), n, float(max_toi), 1 if lowest_index else 0,
+            threads if threads is not None else default_threads(), _p(feat), _p(toi), _p(nrm),
+            _p(stats) if want_stats else None)
+        if want_stats:
+            return feat, toi, nrm, {"wide_visits": int(stats[0]), "leaf_tests": int(stats[1])}
+        return feat, toi, nrm
+
+    def bvh_nodes(self) -> np.ndarray:
+        n = lib().oracle_trimesh_bvh_nodes_f32(self._h, None, 0)
+        raw = np.empty(n * 16, dtype=np.float32)
+        lib().oracle_trimesh_bvh_nodes_f32(self._h, _p(raw), n)
+        return raw.reshape(n, 16)
+
+    def __del__(self):
+        try:
+            getattr(lib(), f"oracle_trimesh_free_{self.prec}")(self._h)
+        except Exception:
+            pass
+
+
+def _take_pairs(h) -> np.ndarray:
+    n = lib().oracle_pairs_count(h)
+    out = np.empty((n, 2), dtype=np.uint32)
+    if n:
+        lib().oracle_pairs_copy(h, _p(out))
+    lib().oracle_pairs_free(h)
+    return out
+
+
+class Bvh:
+    """Reference Bvh built with BvhBuildStrategy::Binned (f32)."""
+
+    def __init__(self, aabbs: np.ndarray):
+        self.a = np.ascontiguousarray(aabbs, dtype=np.float32)
+        self._h = lib().oracle_bvh_new_f32(_p(self.a), self.a.shape[0])
+
+    def refit(self, aabbs: np.ndarray) -> None:
+        a = np.ascontiguousarray(aabbs, dtype=np.float32)
+        lib().oracle_bvh_refit_f32(self._h, _p(a), a.shape[0])
+
+    def nodes(self) -> np.ndarray:
+        n = lib().oracle_bvh_nodes_f32(self._h, None, 0)
+        raw = np.empty(n * 16, dtype=np.float32)
+        lib().oracle_bvh_nodes_f32(self._h, _p(raw), n)
+        return raw.reshape(n, 16)
+
+    def traverse_bvtt_single_tree(self) -> np.ndarray:
+        """Pairs in the reference's callback order (not canonicalised)."""
+        return _take_pairs(lib().oracle_bvh_self_pairs_f32(self._h))
+
+    def leaf_pairs(self, other: "Bvh") -> np.ndarray:
+        return _take_pairs(lib().oracle_bvh_leaf_pairs_f32(self._h, other._h))
+
+    def __del__(self):
+        try:
+            lib().oracle_bvh_free_f32(self._h)
+        except Exception:
+            pass
+
+
+def canonical_sorted_pairs(pairs: np.ndarray) -> np.ndarray:
+    """(min, max) per row, rows sorted lexicographically."""
+    if len(pairs) == 0:
+        return pairs.reshape(0, 2)
+    a = np.minimum(pairs[:, 0], pairs[:, 1])
+    b = np.maximum(pairs[:, 0], pairs[:, 1])
+    order = np.lexsort((b, a))
+    return np.stack([a[order], b[order]], axis=1)
+
+
+def sorted_pairs(pairs: np.ndarray) -> np.ndarray:
+    if len(pairs) == 0:
+        return pairs.reshape(0, 2)
+    order = np.lexsort((pairs[:, 1], pairs[:, 0]))
+    return pairs[order]

@@ -1,0 +1,246 @@
+"""parry_gb300 — GB300-native batched replacement for parry3d's data-parallel query path.
+
+The Python surface mirrors the reference API names so that a CPU loop over parry calls maps onto
+one batched call here:
+
+    parry3d                                            parry_gb300
+    -------------------------------------------------  ------------------------------------------------
+    Bvh::from_leaves(strategy, &aabbs)                 Bvh.from_leaves(ctx, aabbs)
+    Bvh::refit(&mut ws) (+ insert_or_update_partially) Bvh.refit(aabbs)
+    Bvh::traverse_bvtt_single_tree(&mut ws, &mut f)    Bvh.traverse_bvtt_single_tree() -> (k, 2) pairs
+    Bvh::leaf_pairs(&other, check)                     Bvh.leaf_pairs(other) -> (k, 2) pairs
+    TriMesh::new(vertices, indices)                    TriMesh(ctx, vertices, indices)
+    TriMesh::cast_ray_and_get_normal(m, ray, t, solid) TriMesh.cast_rays_and_get_normal(rays, t, solid, pose)
+    TriMesh::cast_ray(m, ray, t, solid)                TriMesh.cast_rays(rays, t, solid, pose)
+
+Arrays may be numpy arrays (host memory, staged by the library) or torch tensors (CUDA tensors are
+used in place; outputs are then allocated on the same device). Every call goes through the C ABI
+of libparrygpu.so (include/parry_gpu.h); there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _capi
+from ._capi import ParryGpuError, lib, check
+
+__all__ = ["Context", "Bvh", "TriMesh", "ParryGpuError", "NO_HIT", "lib"]
+
+NO_HIT = 0xFFFFFFFF
+
+try:  # torch is optional plumbing (device memory, streams); numpy inputs work without it.
+    import torch
+except Exception:  # pragma: no cover
+    torch = None
+
+
+def _is_torch(x) -> bool:
+    return torch is not None and isinstance(x, torch.Tensor)
+
+
+def _as_input(x, dtype):
+    """Returns (keepalive, pointer) for an input array (numpy or torch), C-contiguous."""
+    if x is None:
+        return None, None
+    if _is_torch(x):
+        tdt = {np.float32: torch.float32, np.uint32: torch.int32}[dtype]
+        if x.dtype != tdt and not (dtype is np.uint32 and x.dtype in (torch.int32, torch.uint32)):
+            x = x.to(tdt)
+        x = x.contiguous()
+        return x, C.c_void_p(x.data_ptr())
+    a = np.ascontiguousarray(x, dtype=dtype)
+    return a, C.c_void_p(a.ctypes.data)
+
+
+def _alloc_like(ref, shape, dtype):
+    """Allocates an output on the same side (numpy / torch CPU / torch CUDA) as `ref`."""
+    if _is_torch(ref):
+        tdt = {np.float32: torch.float32, np.uint32: torch.int32}[dtype]
+        pin = ref.device.type == "cpu" and ref.is_pinned()
+        t = torch.empty(shape, dtype=tdt, device=ref.device, pin_memory=pin)
+        return t, C.c_void_p(t.data_ptr())
+    a = np.empty(shape, dtype=dtype)
+    return a, C.c_void_p(a.ctypes.data)
+
+
+class Context:
+    """A device context (one CUDA stream). Mirrors nothing in parry, which is single-threaded CPU."""
+
+    def __init__(self, device: int = 0, ray_block: int = 0, sort_rays: bool = True):
+        cfg = _capi.ParryGpuConfig()
+        lib().parrygpu_default_config(C.byref(cfg))
+        cfg.device = device
+        cfg.ray_block = ray_block
+        cfg.sort_rays = 1 if sort_rays else 0
+        h = C.c_void_p()
+        check(lib().parrygpu_create(C.byref(h), C.byref(cfg)))
+        self._h = h
+        self.device = device
+
+    @property
+    def handle(self):
+        return self._h
+
+    def set_stream(self, stream_ptr: int | None) -> None:
+        check(lib().parrygpu_set_stream(self._h, C.c_void_p(stream_ptr or 0)), self._h)
+
+    def sync(self) -> None:
+        check(lib().parrygpu_sync(self._h), self._h)
+
+    @property
+    def kernel_launches(self) -> int:
+        return int(lib().parrygpu_kernel_launches(self._h))
+
+    def enable_kernel_timing(self, on: bool = True) -> None:
+        check(lib().parrygpu_enable_kernel_timing(self._h, 1 if on else 0), self._h)
+
+    def reset_kernel_timing(self) -> None:
+        check(lib().parrygpu_reset_kernel_timing(self._h), self._h)
+
+    def kernel_time(self, kernel: str) -> tuple[float, int]:
+        """(total ms, launches) of the event-timed launches of `kernel` since the last reset."""
+        ms, n = C.c_double(0.0), C.c_uint64(0)
+        check(lib().parrygpu_kernel_time(self._h, kernel.encode(), C.byref(ms), C.byref(n)), self._h)
+        return ms.value, n.value
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            lib().parrygpu_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def _pairs_call(ctx: Context, fn, args, sorted_: bool, cap_hint: int):
+    cap = max(int(cap_hint), 1024)
+    while True:
+        out = np.empty((cap, 2), dtype=np.uint32)
+        n = C.c_uint64(0)
+        st = fn(ctx.handle, *args, C.c_void_p(out.ctypes.data), C.c_uint64(cap), C.byref(n), 1 if sorted_ else 0)
+        if st == 3 and n.value > cap:  # capacity exceeded: retry with the exact count
+            cap = int(n.value)
+            continue
+        check(st, ctx.handle)
+        return out[: n.value]
+
+
+class Bvh:
+    """partitioning::Bvh on the GPU: LBVH built from 30-bit Morton codes (see include/parry_gpu.h)."""
+
+    def __init__(self, ctx: Context, handle):
+        self.ctx = ctx
+        self._h = handle
+
+    @classmethod
+    def from_leaves(cls, ctx: Context, aabbs) -> "Bvh":
+        """Bvh::from_leaves: `aabbs` is (n, 6) = mins xyz, maxs xyz; leaf data = row index."""
+        keep, p = _as_input(aabbs, np.float32)
+        n = int(keep.shape[0]) if keep is not None else 0
+        h = C.c_void_p()
+        check(lib().parrygpu_bvh_build(ctx.handle, p, n, C.byref(h)), ctx.handle)
+        return cls(ctx, h)
+
+    def refit(self, aabbs) -> None:
+        """insert_or_update_partially for every leaf, then Bvh::refit (topology kept)."""
+        keep, p = _as_input(aabbs, np.float32)
+        check(lib().parrygpu_bvh_refit(self.ctx.handle, self._h, p), self.ctx.handle)
+
+    def info(self) -> tuple[int, int]:
+        lc, wc = C.c_uint32(0), C.c_uint32(0)
+        check(lib().parrygpu_bvh_info(self._h, C.byref(lc), C.byref(wc)))
+        return lc.value, wc.value
+
+    def leaf_count(self) -> int:
+        return self.info()[0]
+
+    def nodes(self) -> np.ndarray:
+        """Wide nodes as a structured array in the reference's BvhNodeWide layout."""
+        _, wc = self.info()
+        raw = np.empty(wc * 16, dtype=np.float32)
+        if wc:
+            check(lib().parrygpu_bvh_copy_nodes(self.ctx.handle, self._h, C.c_void_p(raw.ctypes.data)), self.ctx.handle)
+        return raw.reshape(wc, 16)
+
+    def traverse_bvtt_single_tree(self, sorted: bool = True, cap_hint: int | None = None) -> np.ndarray:
+        """All intersecting leaf pairs (each unordered pair once) as canonical (min, max) rows."""
+        hint = cap_hint if cap_hint is not None else 4 * self.leaf_count()
+        return _pairs_call(self.ctx, lib().parrygpu_bvh_self_pairs, (self._h,), sorted, hint)
+
+    def leaf_pairs(self, other: "Bvh", sorted: bool = True, cap_hint: int | None = None) -> np.ndarray:
+        """Bvh::leaf_pairs(&other, aabb-intersection check) as (leaf of self, leaf of other) rows."""
+        hint = cap_hint if cap_hint is not None else 4 * max(self.leaf_count(), other.leaf_count())
+        return _pairs_call(self.ctx, lib().parrygpu_bvh_leaf_pairs, (self._h, other._h), sorted, hint)
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            lib().parrygpu_bvh_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class TriMesh:
+    """shape::TriMesh for ray casts: vertices (n_v, 3) f32, indices (n_t, 3) u32."""
+
+    def __init__(self, ctx: Context, vertices, indices):
+        kv, pv = _as_input(vertices, np.float32)
+        ki, pi = _as_input(indices, np.uint32)
+        self.ctx = ctx
+        self.n_vertices = int(kv.shape[0])
+        self.n_triangles = int(ki.shape[0])
+        h = C.c_void_p()
+        check(lib().parrygpu_trimesh_create(ctx.handle, pv, self.n_vertices, pi, self.n_triangles, C.byref(h)), ctx.handle)
+        self._h = h
+
+    def _cast(self, rays, max_toi, solid, pose, want_normal, out=None):
+        kr, pr = _as_input(rays, np.float32)
+        n = int(kr.shape[0])
+        kp, pp = _as_input(pose, np.float32) if pose is not None else (None, None)
+        if out is None:
+            feat, pf = _alloc_like(kr, (n,), np.uint32)
+            toi, pt = _alloc_like(kr, (n,), np.float32)
+            nrm, pn = _alloc_like(kr, (n, 3), np.float32) if want_normal else (None, None)
+        else:
+            feat, toi, nrm = out
+            pf, pt = C.c_void_p(_dptr(feat)), C.c_void_p(_dptr(toi))
+            pn = C.c_void_p(_dptr(nrm)) if (want_normal and nrm is not None) else None
+        check(lib().parrygpu_trimesh_cast_rays(self.ctx.handle, self._h, pp, pr, n, float(max_toi), 1 if solid else 0,
+                                               pf, pt, pn), self.ctx.handle)
+        return feat, toi, nrm
+
+    def cast_rays_and_get_normal(self, rays, max_toi: float, solid: bool = True, pose=None, out=None):
+        """Batched RayCast::cast_ray_and_get_normal. Returns (feature, toi, normal):
+        feature = triangle (front face), triangle + n_triangles (back face) or NO_HIT."""
+        return self._cast(rays, max_toi, solid, pose, True, out)
+
+    def cast_rays(self, rays, max_toi: float, solid: bool = True, pose=None, out=None):
+        """Batched RayCast::cast_ray (toi only). Returns (feature, toi)."""
+        f, t, _ = self._cast(rays, max_toi, solid, pose, False, out)
+        return f, t
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            lib().parrygpu_trimesh_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def _dptr(x) -> int:
+    if _is_torch(x):
+        return x.data_ptr()
+    return x.ctypes.data

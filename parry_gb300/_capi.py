@@ -1,0 +1,93 @@
+"""ctypes binding of libparrygpu's C ABI (include/parry_gpu.h).
+
+This is the same binding a Python user of the C library would write; the Rust/C bindings a
+maintainer of the reference would add are shown in INTEGRATION.md. Loading fails loudly when the
+compiled library is missing: there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+_LIB_PATH = Path(__file__).resolve().parent / "libparrygpu.so"
+
+P = C.c_void_p
+U32 = C.c_uint32
+U64 = C.c_uint64
+I32 = C.c_int
+F32 = C.c_float
+PU64 = C.POINTER(C.c_uint64)
+PU32 = C.POINTER(C.c_uint32)
+
+STATUS = {
+    0: "ok",
+    1: "invalid argument",
+    2: "unsupported shape pair",
+    3: "capacity exceeded",
+    5: "device wait timed out",
+    6: "CUDA error",
+    7: "traversal stack overflow",
+    8: "no CUDA device",
+}
+
+# name -> (restype, argtypes); every symbol declared in include/parry_gpu.h.
+SIGNATURES: dict[str, tuple] = {
+    "parrygpu_default_config": (None, [P]),
+    "parrygpu_create": (I32, [C.POINTER(P), P]),
+    "parrygpu_destroy": (None, [P]),
+    "parrygpu_set_stream": (I32, [P, P]),
+    "parrygpu_sync": (I32, [P]),
+    "parrygpu_last_error": (C.c_char_p, [P]),
+    "parrygpu_status_string": (C.c_char_p, [I32]),
+    "parrygpu_kernel_launches": (U64, [P]),
+    "parrygpu_enable_kernel_timing": (I32, [P, I32]),
+    "parrygpu_kernel_time": (I32, [P, C.c_char_p, C.POINTER(C.c_double), PU64]),
+    "parrygpu_reset_kernel_timing": (I32, [P]),
+    "parrygpu_bvh_build": (I32, [P, P, U32, C.POINTER(P)]),
+    "parrygpu_bvh_destroy": (None, [P]),
+    "parrygpu_bvh_refit": (I32, [P, P, P]),
+    "parrygpu_bvh_self_pairs": (I32, [P, P, P, U64, PU64, I32]),
+    "parrygpu_bvh_leaf_pairs": (I32, [P, P, P, P, U64, PU64, I32]),
+    "parrygpu_bvh_info": (I32, [P, PU32, PU32]),
+    "parrygpu_bvh_copy_nodes": (I32, [P, P, P]),
+    "parrygpu_trimesh_create": (I32, [P, P, U32, P, U32, C.POINTER(P)]),
+    "parrygpu_trimesh_destroy": (None, [P]),
+    "parrygpu_trimesh_cast_rays": (I32, [P, P, P, P, U32, F32, I32, P, P, P]),
+}
+
+
+class ParryGpuError(RuntimeError):
+    def __init__(self, status: int, msg: str = ""):
+        self.status = status
+        super().__init__(f"{STATUS.get(status, 'unknown status')} ({status}){': ' + msg if msg else ''}")
+
+
+class ParryGpuConfig(C.Structure):
+    _fields_ = [("device", C.c_int), ("ray_block", C.c_uint32), ("sort_rays", C.c_uint32), ("reserved", C.c_uint32 * 5)]
+
+
+_lib = None
+
+
+def lib() -> C.CDLL:
+    """Loads libparrygpu.so (built by parry_gb300._build / __graft_entry__.build())."""
+    global _lib
+    if _lib is None:
+        if not _LIB_PATH.exists():
+            raise ImportError(f"{_LIB_PATH} is missing: build it with `python -c 'import __graft_entry__ as g; g.build()'`")
+        l = C.CDLL(str(_LIB_PATH))
+        for name, (res, args) in SIGNATURES.items():
+            f = getattr(l, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = l
+    return _lib
+
+
+def check(status: int, ctx=None) -> None:
+    if status != 0:
+        msg = ""
+        if ctx is not None:
+            raw = lib().parrygpu_last_error(ctx)
+            msg = raw.decode() if raw else ""
+        raise ParryGpuError(status, msg)

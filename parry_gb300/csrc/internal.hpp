@@ -1,0 +1,125 @@
+// Internal declarations shared by the translation units of libparrygpu.
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <cstdio>
+#include <string>
+#include <vector>
+#include <map>
+#include <utility>
+#include "../../include/parry_gpu.h"
+
+// Device-side error word bits (set by kernels, read and cleared by parrygpu_sync).
+enum : uint32_t {
+  ERR_STACK_OVERFLOW = 1u << 0,
+  ERR_CAPACITY = 1u << 1,
+  ERR_TIMEOUT = 1u << 2,
+  ERR_POLYTOPE_FULL = 1u << 3,
+};
+
+// A grow-only device buffer owned by a context or a handle.
+struct DevBuf {
+  void* ptr = nullptr;
+  size_t bytes = 0;
+  cudaError_t reserve(size_t need) {
+    if (need <= bytes) return cudaSuccess;
+    if (ptr) { cudaError_t e = cudaFree(ptr); if (e != cudaSuccess) return e; ptr = nullptr; bytes = 0; }
+    size_t cap = need < 256 ? 256 : need;
+    cudaError_t e = cudaMalloc(&ptr, cap);
+    if (e == cudaSuccess) bytes = cap;
+    return e;
+  }
+  void release() { if (ptr) cudaFree(ptr); ptr = nullptr; bytes = 0; }
+  template <class T> T* as() const { return (T*)ptr; }
+};
+
+struct parrygpu_ctx {
+  int device = 0;
+  cudaStream_t own_stream = nullptr;
+  cudaStream_t stream = nullptr;
+  parrygpu_config cfg{};
+  std::string last_error;
+  uint64_t launches = 0;
+  uint32_t* d_err = nullptr;    // device error word
+  uint32_t* h_err = nullptr;    // pinned mirror
+  // Scratch reused across calls (sort buffers, staging of host inputs/outputs, counters).
+  DevBuf sort_k[2], sort_v[2], sort_hist, stage_in[4], stage_out[4], misc, counters;
+  DevBuf ray_keys, ray_order;
+  // Optional per-kernel event timing (parrygpu_enable_kernel_timing).
+  bool timing = false;
+  std::map<std::string, std::vector<std::pair<cudaEvent_t, cudaEvent_t>>> pending;
+  std::map<std::string, std::pair<double, uint64_t>> timed;
+};
+
+// Brackets one kernel launch with CUDA events when the context has timing enabled.
+struct KernelTimer {
+  parrygpu_ctx* ctx;
+  const char* name;
+  cudaEvent_t a = nullptr, b = nullptr;
+  KernelTimer(parrygpu_ctx* c, const char* n) : ctx(c), name(n) {
+    if (ctx->timing && cudaEventCreate(&a) == cudaSuccess && cudaEventCreate(&b) == cudaSuccess) cudaEventRecord(a, ctx->stream);
+    else { a = b = nullptr; cudaGetLastError(); }
+  }
+  void stop() {
+    if (!a) return;
+    cudaEventRecord(b, ctx->stream);
+    ctx->pending[name].push_back({a, b});
+    a = b = nullptr;
+  }
+};
+
+struct parrygpu_bvh {
+  uint32_t n_leaves = 0;
+  uint32_t n_wide = 0;
+  DevBuf wide;          // n_wide x 64 B  (BvhNodeWide layout)
+  DevBuf leaf_parent;   // per sorted leaf: (wide << 1) | side
+  DevBuf node_parent;   // per internal node: (wide << 1) | side, root = UINT32_MAX
+  DevBuf leaf_index;    // sorted position -> leaf data (user index)
+  DevBuf flags;         // per internal node arrival counters for the bottom-up fit
+  DevBuf info;          // per internal node: (split position gamma, last sorted leaf of its range)
+  DevBuf root_aabb;     // 6 floats
+  bool leaf_data_is_position = false;
+};
+
+struct parrygpu_trimesh {
+  uint32_t n_vertices = 0, n_triangles = 0;
+  parrygpu_bvh bvh;     // leaves store the sorted position of the triangle in `soup`
+  DevBuf soup;          // per sorted position: a.xyz b.x | b.yz c.xy | c.z orig 0 0  (3 x float4)
+};
+
+// ---- status helpers ----
+parrygpu_status set_error(parrygpu_ctx* ctx, parrygpu_status s, const char* fmt, ...);
+parrygpu_status check_cuda(parrygpu_ctx* ctx, cudaError_t e, const char* what);
+#define PG_CUDA(ctx, call)                                                   \
+  do {                                                                       \
+    cudaError_t _e = (call);                                                 \
+    if (_e != cudaSuccess) return check_cuda((ctx), _e, #call);              \
+  } while (0)
+#define PG_LAUNCHED(ctx)                                                     \
+  do {                                                                       \
+    (ctx)->launches++;                                                       \
+    cudaError_t _e = cudaGetLastError();                                     \
+    if (_e != cudaSuccess) return check_cuda((ctx), _e, "kernel launch");    \
+  } while (0)
+
+// ---- host/device pointer staging ----
+bool is_device_ptr(const void* p);
+// Returns a device pointer holding `bytes` of `src` (src itself when already on the device).
+parrygpu_status stage_input(parrygpu_ctx* ctx, DevBuf& buf, const void* src, size_t bytes, const void** dptr);
+// Returns a device pointer for an output of `bytes`; *needs_copy tells whether `dst` is host memory.
+parrygpu_status stage_output(parrygpu_ctx* ctx, DevBuf& buf, void* dst, size_t bytes, void** dptr, bool* needs_copy);
+
+// ---- radix sort (sort.cu) ----
+// Stable LSD sort of (keys, values) by the low `key_bits` bits. In/out in ctx scratch; returns the
+// buffer index (0/1) holding the result in ctx->sort_k / ctx->sort_v.
+parrygpu_status radix_sort_pairs(parrygpu_ctx* ctx, uint32_t n, int key_bits, int* result_buf);
+parrygpu_status radix_sort_reserve(parrygpu_ctx* ctx, uint32_t n);
+
+// ---- LBVH (lbvh.cu) ----
+// Builds `bvh` from `n` device AABBs (n x 6 floats). When leaf_data_is_position, leaf nodes store
+// their sorted position instead of the AABB index.
+parrygpu_status lbvh_build(parrygpu_ctx* ctx, parrygpu_bvh* bvh, const float* d_aabbs, uint32_t n, bool leaf_data_is_position);
+parrygpu_status lbvh_refit(parrygpu_ctx* ctx, parrygpu_bvh* bvh, const float* d_aabbs);
+
+// Launch configuration helpers.
+static inline uint32_t div_up(uint64_t a, uint64_t b) { return (uint32_t)((a + b - 1) / b); }

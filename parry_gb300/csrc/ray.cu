@@ -1,0 +1,411 @@
+// Batched ray casts against a triangle mesh (TriMesh + RayCast replacement).
+//
+// Mesh layout in HBM (all L2-resident for meshes of ~10^5 triangles):
+//   wide : LBVH in BvhNodeWide layout; leaf `children` = sorted position of the triangle
+//   soup : per sorted position, the triangle's three vertices + original index in 3 x float4
+//          (48 B), so a leaf test is three 16-byte loads from the cache line next to its
+//          neighbours in Morton order.
+// Rays are optionally Morton-sorted by origin first (coherent traversal); results are written to
+// the ray's original slot.
+//
+// Per-ray algorithm: best-first descent of the reference's Bvh::find_best
+// (src/partitioning/bvh/bvh_traverse.rs:335-417) with the node cost of BvhNode::cast_ray
+// (src/partitioning/bvh/bvh_tree.rs:1177-1181 -> src/query/ray/ray_aabb.rs:12-49) and the leaf
+// cost of Triangle::cast_local_ray_and_get_normal (src/query/ray/ray_triangle.rs:49-152). Exact toi
+// ties go to the lowest triangle index: nodes whose entry time equals the best toi are still
+// visited, and an equal toi replaces the best only with a smaller triangle index.
+#include "internal.hpp"
+#include "common.cuh"
+#include "lbvh_device.cuh"
+
+using namespace pg;
+
+namespace {
+
+constexpr int RAY_STACK = 64;
+
+struct TriHit {
+  float toi;
+  uint32_t fid;
+};
+
+// src/query/ray/ray_triangle.rs:70-152, toi and face id only (normal recomputed for the winner).
+__device__ __forceinline__ bool ray_triangle_toi(V3 a, V3 b, V3 c, V3 o, V3 dir, TriHit* h) {
+  V3 ab = b - a;
+  V3 ac = c - a;
+  V3 n = cross(ab, ac);
+  float d = dot(n, dir);
+  if (d == 0.0f) return false;
+  V3 ap = o - a;
+  float t = dot(ap, n);
+  if ((t < 0.0f && d < 0.0f) || (t > 0.0f && d > 0.0f)) return false;
+  uint32_t fid = d < 0.0f ? 0u : 1u;
+  d = fabsf(d);
+  V3 e = -cross(dir, ap);
+  float v, w;
+  if (t < 0.0f) {
+    v = -dot(ac, e);
+    if (v < 0.0f || v > d) return false;
+    w = dot(ab, e);
+    if (w < 0.0f || v + w > d) return false;
+    float invd = 1.0f / d;
+    h->toi = -t * invd;
+  } else {
+    v = dot(ac, e);
+    if (v < 0.0f || v > d) return false;
+    w = -dot(ab, e);
+    if (w < 0.0f || v + w > d) return false;
+    float invd = 1.0f / d;
+    h->toi = t * invd;
+  }
+  h->fid = fid;
+  return true;
+}
+
+// Normal of the winning triangle, as ray_triangle.rs computes it (faces the ray origin).
+__device__ __forceinline__ V3 ray_triangle_normal(V3 a, V3 b, V3 c, V3 o) {
+  V3 ab = b - a;
+  V3 ac = c - a;
+  V3 n = cross(ab, ac);
+  V3 ap = o - a;
+  float t = dot(ap, n);
+  return t < 0.0f ? -normalize(n) : normalize(n);
+}
+
+// src/query/ray/ray_aabb.rs:12-49 with solid = true; FLT_MAX on a miss.
+__device__ __forceinline__ float slab(float3 mn, float3 mx, V3 o, V3 inv, uint32_t zmask, float max_toi) {
+  float tmin = 0.0f, tmax = max_toi;
+  bool miss = false;
+  if (zmask & 1u) {
+    miss |= (o.x < mn.x) | (o.x > mx.x);
+  } else {
+    float n = (mn.x - o.x) * inv.x, f = (mx.x - o.x) * inv.x;
+    if (n > f) { float s = n; n = f; f = s; }
+    tmin = fmaxf(tmin, n); tmax = fminf(tmax, f);
+  }
+  if (zmask & 2u) {
+    miss |= (o.y < mn.y) | (o.y > mx.y);
+  } else {
+    float n = (mn.y - o.y) * inv.y, f = (mx.y - o.y) * inv.y;
+    if (n > f) { float s = n; n = f; f = s; }
+    tmin = fmaxf(tmin, n); tmax = fminf(tmax, f);
+  }
+  if (zmask & 4u) {
+    miss |= (o.z < mn.z) | (o.z > mx.z);
+  } else {
+    float n = (mn.z - o.z) * inv.z, f = (mx.z - o.z) * inv.z;
+    if (n > f) { float s = n; n = f; f = s; }
+    tmin = fmaxf(tmin, n); tmax = fminf(tmax, f);
+  }
+  return (!miss && tmin <= tmax) ? tmin : FLT_MAX;
+}
+
+__device__ __forceinline__ void load_tri(const float4* __restrict__ soup, uint32_t p, V3* a, V3* b, V3* c, uint32_t* orig) {
+  const float4* s = soup + 3 * (size_t)p;
+  float4 x = __ldg(s), y = __ldg(s + 1), z = __ldg(s + 2);
+  *a = v3(x.x, x.y, x.z);
+  *b = v3(x.w, y.x, y.y);
+  *c = v3(y.z, y.w, z.x);
+  *orig = __float_as_uint(z.y);
+}
+
+template <bool HAS_POSE, bool WANT_NORMAL>
+__global__ void k_trimesh_rays(const WideNode* __restrict__ wide, const float4* __restrict__ soup, uint32_t n_tris,
+                               const float* __restrict__ rays, const uint32_t* __restrict__ order, uint32_t n, float max_toi,
+                               Pose pose, uint32_t* __restrict__ feat, float* __restrict__ toi_out, float* __restrict__ normal_out,
+                               uint32_t* __restrict__ err) {
+  uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  uint32_t r = order ? order[k] : k;
+  const float* rp = rays + 6 * (size_t)r;
+  V3 o = v3(rp[0], rp[1], rp[2]);
+  V3 dir = v3(rp[3], rp[4], rp[5]);
+  if (HAS_POSE) {
+    o = pose_inv_point(pose, o);
+    dir = pose_inv_rotate(pose, dir);
+  }
+  uint32_t zmask = (dir.x == 0.0f ? 1u : 0u) | (dir.y == 0.0f ? 2u : 0u) | (dir.z == 0.0f ? 4u : 0u);
+  V3 inv = v3(dir.x != 0.0f ? 1.0f / dir.x : 0.0f, dir.y != 0.0f ? 1.0f / dir.y : 0.0f, dir.z != 0.0f ? 1.0f / dir.z : 0.0f);
+
+  float best = max_toi;
+  uint32_t best_orig = 0xffffffffu, best_pos = 0xffffffffu;
+  bool have = false;
+
+  auto try_leaf = [&](uint32_t pos) {
+    V3 a, b, c;
+    uint32_t orig;
+    load_tri(soup, pos, &a, &b, &c, &orig);
+    TriHit h;
+    if (!ray_triangle_toi(a, b, c, o, dir, &h)) return;
+    if (!(h.toi <= best)) return;  // Triangle::cast_local_ray_and_get_normal: toi <= max_toi
+    if (h.toi < best || (have && h.toi == best && orig < best_orig)) {
+      best = h.toi; best_orig = orig; best_pos = pos; have = true;
+    }
+  };
+
+  WideNode root;
+  load_wide(wide, 0, &root);
+  if ((root.r.data & 0x3fffffffu) == 0u) {
+    // Partial root (single triangle), bvh_traverse.rs:354-362.
+    float s = slab(root.l.mins, root.l.maxs, o, inv, zmask, max_toi);
+    if (s < max_toi) try_leaf(root.l.children);
+  } else {
+    uint32_t stack[RAY_STACK];
+    int sp = 0;
+    WideNode w = root;
+    for (;;) {
+      float ls = slab(w.l.mins, w.l.maxs, o, inv, zmask, best);
+      float rs = slab(w.r.mins, w.r.maxs, o, inv, zmask, best);
+      const BvhNodeDev* nearn = &w.l;
+      const BvhNodeDev* farn = &w.r;
+      if (ls > rs) { float t = ls; ls = rs; rs = t; nearn = &w.r; farn = &w.l; }
+      uint32_t next = 0xffffffffu;
+      if (ls != FLT_MAX && (ls < best || (have && ls == best))) {
+        if ((nearn->data & 0x3fffffffu) == 1u) try_leaf(nearn->children);
+        else next = nearn->children;
+      }
+      if (rs != FLT_MAX && (rs < best || (have && rs == best))) {
+        if ((farn->data & 0x3fffffffu) == 1u) {
+          try_leaf(farn->children);
+        } else if (next != 0xffffffffu) {
+          if (sp >= RAY_STACK) { atomicOr(err, ERR_STACK_OVERFLOW); break; }
+          stack[sp++] = farn->children;
+        } else {
+          next = farn->children;
+        }
+      }
+      if (next == 0xffffffffu) {
+        if (sp == 0) break;
+        next = stack[--sp];
+      }
+      load_wide(wide, next, &w);
+    }
+  }
+
+  if (have) {
+    V3 a, b, c;
+    uint32_t orig;
+    load_tri(soup, best_pos, &a, &b, &c, &orig);
+    TriHit h;
+    ray_triangle_toi(a, b, c, o, dir, &h);
+    feat[r] = h.fid == 1u ? best_orig + n_tris : best_orig;
+    toi_out[r] = best;
+    if (WANT_NORMAL) {
+      V3 nrm = ray_triangle_normal(a, b, c, o);
+      if (HAS_POSE) nrm = pose_rotate(pose, nrm);
+      normal_out[3 * (size_t)r + 0] = nrm.x;
+      normal_out[3 * (size_t)r + 1] = nrm.y;
+      normal_out[3 * (size_t)r + 2] = nrm.z;
+    }
+  } else {
+    feat[r] = 0xffffffffu;
+    toi_out[r] = 0.0f;
+    if (WANT_NORMAL) {
+      normal_out[3 * (size_t)r + 0] = 0.0f;
+      normal_out[3 * (size_t)r + 1] = 0.0f;
+      normal_out[3 * (size_t)r + 2] = 0.0f;
+    }
+  }
+}
+
+__global__ void k_tri_aabbs(const float* __restrict__ verts, const uint32_t* __restrict__ idx, uint32_t nt, uint32_t nv,
+                            float* __restrict__ aabbs, uint32_t* __restrict__ err) {
+  uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nt) return;
+  uint32_t i0 = idx[3 * (size_t)t], i1 = idx[3 * (size_t)t + 1], i2 = idx[3 * (size_t)t + 2];
+  if (i0 >= nv || i1 >= nv || i2 >= nv) { atomicOr(err, ERR_CAPACITY); i0 = i1 = i2 = 0; }
+  float* out = aabbs + 6 * (size_t)t;
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    float a = verts[3 * (size_t)i0 + d], b = verts[3 * (size_t)i1 + d], c = verts[3 * (size_t)i2 + d];
+    // aabb_triangle.rs:25-27: a.min(b).min(c), a.max(b).max(c)
+    out[d] = fminf(fminf(a, b), c);
+    out[3 + d] = fmaxf(fmaxf(a, b), c);
+  }
+}
+
+__global__ void k_tri_soup(const float* __restrict__ verts, const uint32_t* __restrict__ idx, const uint32_t* __restrict__ leaf_index,
+                           uint32_t nt, uint32_t nv, float4* __restrict__ soup) {
+  uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= nt) return;
+  uint32_t t = leaf_index[p];
+  uint32_t i0 = idx[3 * (size_t)t], i1 = idx[3 * (size_t)t + 1], i2 = idx[3 * (size_t)t + 2];
+  if (i0 >= nv || i1 >= nv || i2 >= nv) i0 = i1 = i2 = 0;
+  const float* a = verts + 3 * (size_t)i0;
+  const float* b = verts + 3 * (size_t)i1;
+  const float* c = verts + 3 * (size_t)i2;
+  soup[3 * (size_t)p + 0] = make_float4(a[0], a[1], a[2], b[0]);
+  soup[3 * (size_t)p + 1] = make_float4(b[1], b[2], c[0], c[1]);
+  soup[3 * (size_t)p + 2] = make_float4(c[2], __uint_as_float(t), 0.0f, 0.0f);
+}
+
+__global__ void k_ray_bounds(const float* __restrict__ rays, uint32_t n, uint32_t* __restrict__ bounds) {
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  float mn[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, mx[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+  if (i < n) {
+#pragma unroll
+    for (int d = 0; d < 3; ++d) { mn[d] = rays[6 * (size_t)i + d]; mx[d] = mn[d]; }
+  }
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      mn[d] = fminf(mn[d], __shfl_xor_sync(0xffffffffu, mn[d], o));
+      mx[d] = fmaxf(mx[d], __shfl_xor_sync(0xffffffffu, mx[d], o));
+    }
+  }
+  if ((threadIdx.x & 31) == 0) {
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      atomicMin(&bounds[d], float_flip(mn[d]));
+      atomicMax(&bounds[3 + d], float_flip(mx[d]));
+    }
+  }
+}
+
+__global__ void k_ray_keys(const float* __restrict__ rays, uint32_t n, const uint32_t* __restrict__ bounds, uint32_t* __restrict__ keys,
+                           uint32_t* __restrict__ vals) {
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  float u[3];
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    float lo = float_unflip(bounds[d]), hi = float_unflip(bounds[3 + d]);
+    float ext = hi - lo;
+    u[d] = ext > 0.0f ? (rays[6 * (size_t)i + d] - lo) / ext : 0.5f;
+  }
+  keys[i] = morton30(u[0], u[1], u[2]);
+  vals[i] = i;
+}
+
+}  // namespace
+
+extern "C" {
+
+parrygpu_status parrygpu_trimesh_create(parrygpu_ctx* ctx, const float* vertices, uint32_t n_vertices, const uint32_t* indices,
+                                        uint32_t n_triangles, parrygpu_trimesh** out) {
+  if (!ctx || !out) return PARRYGPU_INVALID_ARG;
+  *out = nullptr;
+  if (n_triangles > 0 && (!vertices || !indices || n_vertices == 0))
+    return set_error(ctx, PARRYGPU_INVALID_ARG, "trimesh needs vertices and indices");
+  PG_CUDA(ctx, cudaSetDevice(ctx->device));
+  const void* dv = nullptr;
+  const void* di = nullptr;
+  parrygpu_status s = stage_input(ctx, ctx->stage_in[0], vertices, (size_t)n_vertices * 12, &dv);
+  if (s != PARRYGPU_OK) return s;
+  s = stage_input(ctx, ctx->stage_in[1], indices, (size_t)n_triangles * 12, &di);
+  if (s != PARRYGPU_OK) return s;
+  parrygpu_trimesh* m = new parrygpu_trimesh();
+  m->n_vertices = n_vertices;
+  m->n_triangles = n_triangles;
+  if (n_triangles > 0) {
+    DevBuf aabbs;
+    cudaError_t e = aabbs.reserve((size_t)n_triangles * 24);
+    if (e == cudaSuccess) e = m->soup.reserve((size_t)n_triangles * 48);
+    if (e != cudaSuccess) { aabbs.release(); parrygpu_trimesh_destroy(m); return check_cuda(ctx, e, "trimesh alloc"); }
+    k_tri_aabbs<<<div_up(n_triangles, 256), 256, 0, ctx->stream>>>((const float*)dv, (const uint32_t*)di, n_triangles, n_vertices,
+                                                                   aabbs.as<float>(), ctx->d_err);
+    ctx->launches++;
+    s = lbvh_build(ctx, &m->bvh, aabbs.as<float>(), n_triangles, true);
+    if (s == PARRYGPU_OK) {
+      k_tri_soup<<<div_up(n_triangles, 256), 256, 0, ctx->stream>>>((const float*)dv, (const uint32_t*)di, m->bvh.leaf_index.as<uint32_t>(),
+                                                                     n_triangles, n_vertices, m->soup.as<float4>());
+      ctx->launches++;
+    }
+    cudaError_t se = cudaStreamSynchronize(ctx->stream);
+    aabbs.release();
+    if (s != PARRYGPU_OK) { parrygpu_trimesh_destroy(m); return s; }
+    if (se != cudaSuccess) { parrygpu_trimesh_destroy(m); return check_cuda(ctx, se, "trimesh build"); }
+    s = parrygpu_sync(ctx);
+    if (s != PARRYGPU_OK) {
+      parrygpu_trimesh_destroy(m);
+      return set_error(ctx, PARRYGPU_INVALID_ARG, "triangle index out of range of the vertex buffer");
+    }
+  }
+  *out = m;
+  return PARRYGPU_OK;
+}
+
+void parrygpu_trimesh_destroy(parrygpu_trimesh* m) {
+  if (!m) return;
+  for (DevBuf* d : {&m->bvh.wide, &m->bvh.leaf_parent, &m->bvh.node_parent, &m->bvh.leaf_index, &m->bvh.flags, &m->bvh.root_aabb,
+                    &m->bvh.info, &m->soup})
+    d->release();
+  delete m;
+}
+
+parrygpu_status parrygpu_trimesh_cast_rays(parrygpu_ctx* ctx, const parrygpu_trimesh* mesh, const float* pose7, const float* rays,
+                                           uint32_t n, float max_toi, int solid, uint32_t* feature, float* toi, float* normal) {
+  (void)solid;
+  if (!ctx || !mesh) return PARRYGPU_INVALID_ARG;
+  if (n == 0) return PARRYGPU_OK;
+  if (!rays || !feature || !toi) return set_error(ctx, PARRYGPU_INVALID_ARG, "rays, feature and toi are required");
+  PG_CUDA(ctx, cudaSetDevice(ctx->device));
+  Pose pose{0.f, 0.f, 0.f, 1.f, v3(0.f, 0.f, 0.f)};
+  bool has_pose = pose7 != nullptr;
+  if (has_pose) {
+    float p[7];
+    if (is_device_ptr(pose7)) {
+      PG_CUDA(ctx, cudaMemcpyAsync(p, pose7, 28, cudaMemcpyDeviceToHost, ctx->stream));
+      PG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    } else {
+      for (int i = 0; i < 7; ++i) p[i] = pose7[i];
+    }
+    pose = Pose{p[0], p[1], p[2], p[3], v3(p[4], p[5], p[6])};
+  }
+  const void* d_rays = nullptr;
+  parrygpu_status s = stage_input(ctx, ctx->stage_in[2], rays, (size_t)n * 24, &d_rays);
+  if (s != PARRYGPU_OK) return s;
+  void *d_feat, *d_toi, *d_nrm;
+  bool c_feat, c_toi, c_nrm;
+  if ((s = stage_output(ctx, ctx->stage_out[1], feature, (size_t)n * 4, &d_feat, &c_feat)) != PARRYGPU_OK) return s;
+  if ((s = stage_output(ctx, ctx->stage_out[2], toi, (size_t)n * 4, &d_toi, &c_toi)) != PARRYGPU_OK) return s;
+  if ((s = stage_output(ctx, ctx->stage_out[3], normal, (size_t)n * 12, &d_nrm, &c_nrm)) != PARRYGPU_OK) return s;
+
+  if (mesh->n_triangles == 0) {
+    PG_CUDA(ctx, cudaMemsetAsync(d_feat, 0xff, (size_t)n * 4, ctx->stream));
+    PG_CUDA(ctx, cudaMemsetAsync(d_toi, 0, (size_t)n * 4, ctx->stream));
+    if (d_nrm) PG_CUDA(ctx, cudaMemsetAsync(d_nrm, 0, (size_t)n * 12, ctx->stream));
+  } else {
+    const uint32_t* order = nullptr;
+    if (ctx->cfg.sort_rays && n > 4096) {
+      s = radix_sort_reserve(ctx, n);
+      if (s != PARRYGPU_OK) return s;
+      PG_CUDA(ctx, ctx->misc.reserve(64));
+      uint32_t* bounds = ctx->misc.as<uint32_t>() + 8;
+      PG_CUDA(ctx, cudaMemsetAsync(bounds, 0xff, 12, ctx->stream));
+      PG_CUDA(ctx, cudaMemsetAsync(bounds + 3, 0x00, 12, ctx->stream));
+      k_ray_bounds<<<div_up(n, 256), 256, 0, ctx->stream>>>((const float*)d_rays, n, bounds);
+      PG_LAUNCHED(ctx);
+      k_ray_keys<<<div_up(n, 256), 256, 0, ctx->stream>>>((const float*)d_rays, n, bounds, ctx->sort_k[0].as<uint32_t>(),
+                                                          ctx->sort_v[0].as<uint32_t>());
+      PG_LAUNCHED(ctx);
+      int rb;
+      KernelTimer kt(ctx, "ray_sort");
+      s = radix_sort_pairs(ctx, n, 30, &rb);
+      kt.stop();
+      if (s != PARRYGPU_OK) return s;
+      order = ctx->sort_v[rb].as<uint32_t>();
+    }
+    uint32_t bs = ctx->cfg.ray_block ? ctx->cfg.ray_block : 128;
+    const WideNode* w = mesh->bvh.wide.as<WideNode>();
+    const float4* soup = mesh->soup.as<float4>();
+#define PG_RAY_LAUNCH(P, N)                                                                                               \
+  k_trimesh_rays<P, N><<<div_up(n, bs), bs, 0, ctx->stream>>>(w, soup, mesh->n_triangles, (const float*)d_rays, order, n, \
+                                                              max_toi, pose, (uint32_t*)d_feat, (float*)d_toi,            \
+                                                              (float*)d_nrm, ctx->d_err)
+    KernelTimer kt(ctx, "trimesh_rays");
+    if (has_pose) { if (d_nrm) PG_RAY_LAUNCH(true, true); else PG_RAY_LAUNCH(true, false); }
+    else { if (d_nrm) PG_RAY_LAUNCH(false, true); else PG_RAY_LAUNCH(false, false); }
+#undef PG_RAY_LAUNCH
+    kt.stop();
+    PG_LAUNCHED(ctx);
+  }
+  if (c_feat) PG_CUDA(ctx, cudaMemcpyAsync(feature, d_feat, (size_t)n * 4, cudaMemcpyDeviceToHost, ctx->stream));
+  if (c_toi) PG_CUDA(ctx, cudaMemcpyAsync(toi, d_toi, (size_t)n * 4, cudaMemcpyDeviceToHost, ctx->stream));
+  if (c_nrm) PG_CUDA(ctx, cudaMemcpyAsync(normal, d_nrm, (size_t)n * 12, cudaMemcpyDeviceToHost, ctx->stream));
+  if (c_feat || c_toi || c_nrm || d_rays != rays) return parrygpu_sync(ctx);
+  return PARRYGPU_OK;
+}
+
+}  // extern "C"

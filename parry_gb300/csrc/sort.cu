@@ -1,0 +1,142 @@
+// Stable LSD radix sort of (u32 key, u32 value) pairs, written for the LBVH build (30-bit Morton
+// keys) and for ray / pair ordering. 8-bit digits, 4096-key tiles:
+//   1. per-tile digit histogram (shared-memory atomics), stored digit-major: hist[d * tiles + t]
+//   2. one exclusive scan over the digit-major array -> global offset of (digit, tile)
+//   3. per-tile stable scatter: each 256-key round ranks keys within a warp with __match_any_sync,
+//      warps are ordered by a shared-memory prefix over per-warp digit counts.
+#include "internal.hpp"
+
+namespace {
+
+constexpr int RS_BINS = 256;
+constexpr int RS_THREADS = 256;
+constexpr int RS_ITEMS = 16;
+constexpr int RS_TILE = RS_THREADS * RS_ITEMS;
+constexpr int RS_WARPS = RS_THREADS / 32;
+constexpr int SCAN_THREADS = 1024;
+
+__global__ void __launch_bounds__(RS_THREADS) k_rs_hist(const uint32_t* __restrict__ keys, uint32_t n, int shift,
+                                                        uint32_t* __restrict__ hist, uint32_t tiles) {
+  __shared__ uint32_t h[RS_BINS];
+  h[threadIdx.x] = 0;
+  __syncthreads();
+  uint32_t base = blockIdx.x * (uint32_t)RS_TILE;
+#pragma unroll 4
+  for (int r = 0; r < RS_ITEMS; ++r) {
+    uint32_t i = base + r * RS_THREADS + threadIdx.x;
+    if (i < n) atomicAdd(&h[(keys[i] >> shift) & 0xffu], 1u);
+  }
+  __syncthreads();
+  hist[threadIdx.x * tiles + blockIdx.x] = h[threadIdx.x];
+}
+
+__global__ void __launch_bounds__(SCAN_THREADS) k_rs_scan(uint32_t* __restrict__ data, uint32_t m) {
+  __shared__ uint32_t sums[SCAN_THREADS];
+  uint32_t tid = threadIdx.x;
+  uint32_t per = (m + SCAN_THREADS - 1) / SCAN_THREADS;
+  uint32_t begin = tid * per;
+  uint32_t end = begin + per < m ? begin + per : m;
+  uint32_t s = 0;
+  for (uint32_t i = begin; i < end; ++i) s += data[i];
+  sums[tid] = s;
+  __syncthreads();
+  for (uint32_t off = 1; off < SCAN_THREADS; off <<= 1) {
+    uint32_t v = tid >= off ? sums[tid - off] : 0u;
+    __syncthreads();
+    sums[tid] += v;
+    __syncthreads();
+  }
+  uint32_t run = tid ? sums[tid - 1] : 0u;
+  for (uint32_t i = begin; i < end; ++i) {
+    uint32_t v = data[i];
+    data[i] = run;
+    run += v;
+  }
+}
+
+__global__ void __launch_bounds__(RS_THREADS) k_rs_scatter(const uint32_t* __restrict__ kin, const uint32_t* __restrict__ vin,
+                                                           uint32_t* __restrict__ kout, uint32_t* __restrict__ vout, uint32_t n,
+                                                           int shift, const uint32_t* __restrict__ hist, uint32_t tiles) {
+  __shared__ uint32_t digit_base[RS_BINS];
+  __shared__ uint32_t round_total[RS_BINS];
+  __shared__ uint32_t warp_cnt[RS_WARPS][RS_BINS];
+  __shared__ uint32_t warp_off[RS_WARPS][RS_BINS];
+  const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+  digit_base[tid] = hist[tid * tiles + blockIdx.x];
+#pragma unroll
+  for (int ww = 0; ww < RS_WARPS; ++ww) warp_cnt[ww][tid] = 0;
+  __syncthreads();
+  const uint32_t base = blockIdx.x * (uint32_t)RS_TILE;
+  const unsigned lt_mask = (1u << lane) - 1u;
+  for (int r = 0; r < RS_ITEMS; ++r) {
+    if (base + r * RS_THREADS >= n) break;  // uniform across the block
+    uint32_t i = base + r * RS_THREADS + tid;
+    bool valid = i < n;
+    uint32_t k = valid ? kin[i] : 0u;
+    uint32_t v = valid ? vin[i] : 0u;
+    uint32_t d = valid ? ((k >> shift) & 0xffu) : (256u + lane);
+    unsigned peers = __match_any_sync(0xffffffffu, d);
+    uint32_t rank = __popc(peers & lt_mask);
+    if (valid && rank == 0) warp_cnt[w][d] = __popc(peers);
+    __syncthreads();
+    {
+      uint32_t off = 0;
+#pragma unroll
+      for (int ww = 0; ww < RS_WARPS; ++ww) {
+        uint32_t c = warp_cnt[ww][tid];
+        warp_off[ww][tid] = off;
+        off += c;
+      }
+      round_total[tid] = off;
+    }
+    __syncthreads();
+    if (valid) {
+      uint32_t pos = digit_base[d] + warp_off[w][d] + rank;
+      kout[pos] = k;
+      vout[pos] = v;
+    }
+    __syncthreads();
+    digit_base[tid] += round_total[tid];
+#pragma unroll
+    for (int ww = 0; ww < RS_WARPS; ++ww) warp_cnt[ww][tid] = 0;
+    __syncthreads();
+  }
+}
+
+}  // namespace
+
+parrygpu_status radix_sort_reserve(parrygpu_ctx* ctx, uint32_t n) {
+  size_t bytes = (size_t)(n ? n : 1) * 4;
+  for (int i = 0; i < 2; ++i) {
+    PG_CUDA(ctx, ctx->sort_k[i].reserve(bytes));
+    PG_CUDA(ctx, ctx->sort_v[i].reserve(bytes));
+  }
+  uint32_t tiles = div_up(n ? n : 1, RS_TILE);
+  PG_CUDA(ctx, ctx->sort_hist.reserve((size_t)tiles * RS_BINS * 4));
+  return PARRYGPU_OK;
+}
+
+parrygpu_status radix_sort_pairs(parrygpu_ctx* ctx, uint32_t n, int key_bits, int* result_buf) {
+  *result_buf = 0;
+  if (n <= 1) return PARRYGPU_OK;
+  parrygpu_status s = radix_sort_reserve(ctx, n);
+  if (s != PARRYGPU_OK) return s;
+  uint32_t tiles = div_up(n, RS_TILE);
+  uint32_t* hist = ctx->sort_hist.as<uint32_t>();
+  int cur = 0;
+  for (int shift = 0; shift < key_bits; shift += 8) {
+    const uint32_t* kin = ctx->sort_k[cur].as<uint32_t>();
+    const uint32_t* vin = ctx->sort_v[cur].as<uint32_t>();
+    uint32_t* kout = ctx->sort_k[cur ^ 1].as<uint32_t>();
+    uint32_t* vout = ctx->sort_v[cur ^ 1].as<uint32_t>();
+    k_rs_hist<<<tiles, RS_THREADS, 0, ctx->stream>>>(kin, n, shift, hist, tiles);
+    PG_LAUNCHED(ctx);
+    k_rs_scan<<<1, SCAN_THREADS, 0, ctx->stream>>>(hist, tiles * RS_BINS);
+    PG_LAUNCHED(ctx);
+    k_rs_scatter<<<tiles, RS_THREADS, 0, ctx->stream>>>(kin, vin, kout, vout, n, shift, hist, tiles);
+    PG_LAUNCHED(ctx);
+    cur ^= 1;
+  }
+  *result_buf = cur;
+  return PARRYGPU_OK;
+}

@@ -1,0 +1,117 @@
+"""Parity of the CUDA ray-cast path (through the C ABI) with the oracle's f32 restatement of
+parry3d: hit triangle / face ids identical, toi and normals within 1e-5 relative (f32 rounding of
+the same arithmetic; observed differences are 0), and the error against the f64 oracle stated."""
+import json
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import parry_gb300 as pg
+from parry_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+REL = 1e-5
+KA = json.loads((Path(__file__).parent / "golden" / "known_answers.json").read_text())
+
+
+def _compare(f, t, n, fo, to, no):
+    np.testing.assert_array_equal(f, fo)
+    hit = fo != pg.NO_HIT
+    np.testing.assert_allclose(t[hit], to[hit], rtol=REL, atol=0)
+    np.testing.assert_allclose(n[hit], no[hit], rtol=REL, atol=REL)
+
+
+def test_known_answers(gpu_ctx):
+    case = KA["trimesh_culling_triangle"]
+    m = pg.TriMesh(gpu_ctx, np.array(case["vertices"], np.float32), np.array(case["indices"], np.uint32))
+    rays = np.array([r["origin"] + r["dir"] for r in case["rays"]], np.float32)
+    f, t, n = m.cast_rays_and_get_normal(rays, case["max_toi"])
+    for k, r in enumerate(case["rays"]):
+        assert f[k] == r["expect_feature"]
+        assert t[k] == pytest.approx(r["expect_toi"], rel=1e-6)
+        np.testing.assert_allclose(n[k], r["expect_normal"], atol=1e-6)
+
+
+def test_golden_fixture(gpu_ctx):
+    g = np.load(Path(__file__).parent / "golden" / "terrain_small.npz")
+    m = pg.TriMesh(gpu_ctx, g["vertices"], g["indices"])
+    f, t, n = m.cast_rays_and_get_normal(g["rays"], float(g["max_toi"]))
+    _compare(f, t, n, g["feature_f32"], g["toi_f32"], g["normal_f32"])
+
+
+@pytest.mark.parametrize("sort_rays", [True, False])
+def test_medium_terrain_vs_oracle(oracle_lib, sort_rays):
+    ctx = pg.Context(0, sort_rays=sort_rays)
+    v, i = W.terrain_mesh(64, 32, seed=21)
+    rays = W.terrain_rays(200_000, 64, 32, seed=21)
+    m = pg.TriMesh(ctx, v, i)
+    f, t, n = m.cast_rays_and_get_normal(rays, 100.0)
+    fo, to, no = oracle_lib.TriMesh(v, i).cast_rays_and_get_normal(rays, 100.0)
+    _compare(f, t, n, fo, to, no)
+    ctx.close()
+
+
+def test_full_size_terrain_vs_oracle(gpu_ctx, oracle_lib):
+    """The 65,536-triangle terrain and 1,048,576 rays: identical hit sets; error vs f64 stated."""
+    v, i = W.terrain_mesh()
+    rays = W.terrain_rays(1 << 20)
+    m = pg.TriMesh(gpu_ctx, v, i)
+    f, t, n = m.cast_rays_and_get_normal(rays, 100.0)
+    om = oracle_lib.TriMesh(v, i)
+    fo, to, no = om.cast_rays_and_get_normal(rays, 100.0)
+    _compare(f, t, n, fo, to, no)
+    f64, t64, _ = oracle_lib.TriMesh(v, i, "f64").cast_rays_and_get_normal(rays, 100.0)
+    hit = (fo != pg.NO_HIT) & (f64 == fo)
+    err = np.abs(t[hit].astype(np.float64) - t64[hit]) / np.abs(t64[hit])
+    print(f"\ntoi rel err vs f64 oracle: max {err.max():.3e} p99 {np.quantile(err, 0.99):.3e}; "
+          f"feature mismatches vs f64: {(f64 != fo).sum()}")
+    assert err.max() < 1e-4
+
+
+def test_pose_and_cast_ray_variant(gpu_ctx, oracle_lib):
+    v, i = W.terrain_mesh(32, 16, seed=4)
+    rays = W.terrain_rays(50_000, 32, 16, seed=4)
+    q = np.array([0.1, 0.2, -0.3, 0.9], np.float64)
+    q /= np.linalg.norm(q)
+    pose = np.array(list(q) + [3.0, -2.0, 1.5], np.float32)
+    # move rays into the posed frame roughly: rotate is irrelevant for parity; just use them
+    m = pg.TriMesh(gpu_ctx, v, i)
+    f, t, n = m.cast_rays_and_get_normal(rays, 100.0, pose=pose)
+    fo, to, no = oracle_lib.TriMesh(v, i).cast_rays_and_get_normal(rays, 100.0, pose=pose)
+    _compare(f, t, n, fo, to, no)
+    f2, t2 = m.cast_rays(rays, 100.0, pose=pose)
+    np.testing.assert_array_equal(f2, f)
+    np.testing.assert_array_equal(t2, t)
+
+
+def test_device_and_pinned_buffers(gpu_ctx, oracle_lib):
+    import torch
+    v, i = W.terrain_mesh(32, 16, seed=8)
+    rays = W.terrain_rays(100_000, 32, 16, seed=8)
+    m = pg.TriMesh(gpu_ctx, torch.from_numpy(v).cuda(), torch.from_numpy(i.view(np.int32)).cuda())
+    fd, td, nd = m.cast_rays_and_get_normal(torch.from_numpy(rays).cuda(), 100.0)
+    gpu_ctx.sync()
+    fp, tp, np_ = m.cast_rays_and_get_normal(torch.from_numpy(rays).pin_memory(), 100.0)
+    fo, to, no = oracle_lib.TriMesh(v, i).cast_rays_and_get_normal(rays, 100.0)
+    _compare(fd.cpu().numpy().view(np.uint32), td.cpu().numpy(), nd.cpu().numpy(), fo, to, no)
+    _compare(fp.numpy().view(np.uint32), tp.numpy(), np_.numpy(), fo, to, no)
+
+
+def test_edge_cases(gpu_ctx):
+    # empty mesh: every ray misses
+    m0 = pg.TriMesh(gpu_ctx, np.zeros((0, 3), np.float32), np.zeros((0, 3), np.uint32))
+    f, t, n = m0.cast_rays_and_get_normal(np.array([[0, 1, 0, 0, -1, 0]], np.float32), 10.0)
+    assert f[0] == pg.NO_HIT
+    # zero rays
+    m1 = pg.TriMesh(gpu_ctx, np.array([[0, 0, 0], [1, 0, 0], [0, 0, 1]], np.float32), np.array([[0, 2, 1]], np.uint32))
+    f, t, n = m1.cast_rays_and_get_normal(np.zeros((0, 6), np.float32), 10.0)
+    assert len(f) == 0
+    # single triangle (partial root), hit exactly at max_toi is rejected (strict <)
+    r = np.array([[0.2, 1, 0.2, 0, -1, 0], [0.2, 2, 0.2, 0, -1, 0]], np.float32)
+    f, t, n = m1.cast_rays_and_get_normal(r, 2.0)
+    assert f[0] == 0 and t[0] == pytest.approx(1.0)
+    assert f[1] == pg.NO_HIT
+    # out-of-range index is rejected
+    with pytest.raises(pg.ParryGpuError):
+        pg.TriMesh(gpu_ctx, np.zeros((3, 3), np.float32), np.array([[0, 1, 5]], np.uint32))
