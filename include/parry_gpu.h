@@ -49,7 +49,9 @@ typedef struct parrygpu_config {
   int device;              /* CUDA device ordinal */
   uint32_t ray_block;      /* threads per block for ray traversal (0 = library default) */
   uint32_t sort_rays;      /* 1 = Morton-sort rays before traversal (default), 0 = input order */
-  uint32_t reserved[5];
+  uint32_t ray_sort_key;   /* 0 = 30-bit Morton code of the origin; 1 = direction octant (3 bits)
+                              above a 27-bit Morton code of the origin */
+  uint32_t reserved[4];
 } parrygpu_config;
 
 /* ---- context ---------------------------------------------------------------------------- */

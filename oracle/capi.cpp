@@ -5,7 +5,7 @@
 // Each function comes in an f32 flavour (parry3d) and an f64 flavour (parry3d-f64); f64 inputs
 // are the f32 inputs widened, so the f64 result measures the f32 path's rounding error.
 #include "ray.hpp"
-#include "query.hpp"
+#include "contact.hpp"
 #include <thread>
 #include <vector>
 #include <algorithm>
@@ -83,6 +83,66 @@ struct PairBuf {
   std::vector<uint32_t> v;
 };
 
+// A shape set in the C-ABI layout: types[n], params[n x 4], poses[n x 7], convex vertex pool.
+template <class R> struct ShapeSet {
+  std::vector<Shape<R>> shapes;
+  std::vector<Iso<R>> poses;
+  std::vector<Vec3<R>> pool;
+  ShapeSet(const uint32_t* types, const float* params, const float* poses7, const float* hullv, uint32_t nhv, uint64_t n) {
+    pool.resize(nhv);
+    for (uint32_t i = 0; i < nhv; ++i) pool[i] = Vec3<R>(R(hullv[3 * i]), R(hullv[3 * i + 1]), R(hullv[3 * i + 2]));
+    shapes.resize(n);
+    poses.resize(n);
+    for (uint64_t i = 0; i < n; ++i) {
+      Shape<R>& s = shapes[i];
+      const float* p = params + 4 * i;
+      s.type = types[i];
+      if (s.type == SHAPE_BALL) s.radius = R(p[0]);
+      else if (s.type == SHAPE_CUBOID) s.half = Vec3<R>(R(p[0]), R(p[1]), R(p[2]));
+      else if (s.type == SHAPE_CAPSULE) { s.half_height = R(p[0]); s.radius = R(p[1]); }
+      else {
+        uint32_t first, count;
+        std::memcpy(&first, p, 4);
+        std::memcpy(&count, p + 1, 4);
+        s.pts = pool.data() + first;
+        s.npts = count;
+      }
+      poses[i] = Iso<R>::from_pose7(poses7 + 7 * i);
+    }
+  }
+};
+
+template <class R, class O>
+void contacts(const uint32_t* types, const float* params, const float* poses, const float* hullv, uint32_t nhv, uint64_t nshapes,
+              const uint32_t* pairs, uint64_t npairs, float prediction, const float* init_dirs, int threads, O* out, uint8_t* has,
+              uint64_t* stats) {
+  ShapeSet<R> set(types, params, poses, hullv, nhv, nshapes);
+  std::atomic<uint64_t> gi{0}, ei{0}, ec{0};
+  parallel_for(npairs, threads, [&](uint64_t k) {
+    uint32_t a = pairs[2 * k], b = pairs[2 * k + 1];
+    Contact<R> c;
+    GjkStats st;
+    Vec3<R> idir;
+    const Vec3<R>* ip = nullptr;
+    if (init_dirs) {
+      idir = Vec3<R>(R(init_dirs[3 * k]), R(init_dirs[3 * k + 1]), R(init_dirs[3 * k + 2]));
+      ip = &idir;
+    }
+    bool ok = contact_world(set.poses[a], set.shapes[a], set.poses[b], set.shapes[b], R(prediction), &c, &st, ip);
+    gi += st.gjk_iters; ei += st.epa_iters; ec += st.epa_calls;
+    has[k] = ok ? 1 : 0;
+    O* o = out + 13 * k;
+    if (ok) {
+      const Vec3<R>* v[4] = {&c.point1, &c.point2, &c.normal1, &c.normal2};
+      for (int j = 0; j < 4; ++j) { o[3 * j] = O(v[j]->x); o[3 * j + 1] = O(v[j]->y); o[3 * j + 2] = O(v[j]->z); }
+      o[12] = O(c.dist);
+    } else {
+      for (int j = 0; j < 13; ++j) o[j] = O(0);
+    }
+  });
+  if (stats) { stats[0] = gi.load(); stats[1] = ei.load(); stats[2] = ec.load(); }
+}
+
 }  // namespace
 
 extern "C" {
@@ -137,6 +197,28 @@ void* oracle_bvh_leaf_pairs_f32(void* a, void* b) {
   ((Bvh<float>*)a)->leaf_pairs(*(Bvh<float>*)b, [&](uint32_t x, uint32_t y) { pb->v.push_back(x); pb->v.push_back(y); });
   return pb;
 }
+// ---------------- convex shapes: AABBs and query::contact ----------------
+void oracle_shape_aabbs_f32(const uint32_t* types, const float* params, const float* poses, const float* hullv, uint32_t nhv,
+                            uint64_t n, float margin, float* out) {
+  ShapeSet<float> set(types, params, poses, hullv, nhv, n);
+  for (uint64_t i = 0; i < n; ++i) {
+    Aabb<float> a = shape_aabb(set.shapes[i], set.poses[i]);
+    if (margin > 0.0f) a = a.loosened(margin);
+    out[6 * i + 0] = a.mins.x; out[6 * i + 1] = a.mins.y; out[6 * i + 2] = a.mins.z;
+    out[6 * i + 3] = a.maxs.x; out[6 * i + 4] = a.maxs.y; out[6 * i + 5] = a.maxs.z;
+  }
+}
+void oracle_contacts_f32(const uint32_t* types, const float* params, const float* poses, const float* hullv, uint32_t nhv,
+                         uint64_t nshapes, const uint32_t* pairs, uint64_t npairs, float prediction, const float* init_dirs,
+                         int threads, float* out, uint8_t* has, uint64_t* stats) {
+  contacts<float, float>(types, params, poses, hullv, nhv, nshapes, pairs, npairs, prediction, init_dirs, threads, out, has, stats);
+}
+void oracle_contacts_f64(const uint32_t* types, const float* params, const float* poses, const float* hullv, uint32_t nhv,
+                         uint64_t nshapes, const uint32_t* pairs, uint64_t npairs, float prediction, const float* init_dirs,
+                         int threads, double* out, uint8_t* has, uint64_t* stats) {
+  contacts<double, double>(types, params, poses, hullv, nhv, nshapes, pairs, npairs, prediction, init_dirs, threads, out, has, stats);
+}
+
 uint64_t oracle_pairs_count(void* p) { return ((PairBuf*)p)->v.size() / 2; }
 void oracle_pairs_copy(void* p, uint32_t* out) { std::memcpy(out, ((PairBuf*)p)->v.data(), ((PairBuf*)p)->v.size() * 4); }
 void oracle_pairs_free(void* p) { delete (PairBuf*)p; }

@@ -63,7 +63,8 @@ class ParryGpuError(RuntimeError):
 
 
 class ParryGpuConfig(C.Structure):
-    _fields_ = [("device", C.c_int), ("ray_block", C.c_uint32), ("sort_rays", C.c_uint32), ("reserved", C.c_uint32 * 5)]
+    _fields_ = [("device", C.c_int), ("ray_block", C.c_uint32), ("sort_rays", C.c_uint32), ("ray_sort_key", C.c_uint32),
+                ("reserved", C.c_uint32 * 4)]
 
 
 _lib = None

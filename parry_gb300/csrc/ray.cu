@@ -239,12 +239,18 @@ __global__ void k_tri_soup(const float* __restrict__ verts, const uint32_t* __re
   soup[3 * (size_t)p + 2] = make_float4(c[2], __uint_as_float(t), 0.0f, 0.0f);
 }
 
-__global__ void k_ray_bounds(const float* __restrict__ rays, uint32_t n, uint32_t* __restrict__ bounds) {
-  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+// Bounds of the ray origins: warp shuffles, then a shared-memory reduction, then one atomic per
+// block and component (order-preserving float encoding).
+__global__ void __launch_bounds__(256) k_ray_bounds(const float* __restrict__ rays, uint32_t n, uint32_t* __restrict__ bounds) {
+  __shared__ float smn[3][8], smx[3][8];
   float mn[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, mx[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
-  if (i < n) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
 #pragma unroll
-    for (int d = 0; d < 3; ++d) { mn[d] = rays[6 * (size_t)i + d]; mx[d] = mn[d]; }
+    for (int d = 0; d < 3; ++d) {
+      float v = rays[6 * (size_t)i + d];
+      mn[d] = fminf(mn[d], v);
+      mx[d] = fmaxf(mx[d], v);
+    }
   }
 #pragma unroll
   for (int d = 0; d < 3; ++d) {
@@ -254,17 +260,23 @@ __global__ void k_ray_bounds(const float* __restrict__ rays, uint32_t n, uint32_
       mx[d] = fmaxf(mx[d], __shfl_xor_sync(0xffffffffu, mx[d], o));
     }
   }
-  if ((threadIdx.x & 31) == 0) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (lane == 0) {
 #pragma unroll
-    for (int d = 0; d < 3; ++d) {
-      atomicMin(&bounds[d], float_flip(mn[d]));
-      atomicMax(&bounds[3 + d], float_flip(mx[d]));
-    }
+    for (int d = 0; d < 3; ++d) { smn[d][w] = mn[d]; smx[d][w] = mx[d]; }
+  }
+  __syncthreads();
+  if (threadIdx.x < 3) {
+    int d = threadIdx.x;
+    float a = smn[d][0], b = smx[d][0];
+    for (int k = 1; k < (int)(blockDim.x >> 5); ++k) { a = fminf(a, smn[d][k]); b = fmaxf(b, smx[d][k]); }
+    atomicMin(&bounds[d], float_flip(a));
+    atomicMax(&bounds[3 + d], float_flip(b));
   }
 }
 
 __global__ void k_ray_keys(const float* __restrict__ rays, uint32_t n, const uint32_t* __restrict__ bounds, uint32_t* __restrict__ keys,
-                           uint32_t* __restrict__ vals) {
+                           uint32_t* __restrict__ vals, uint32_t key_mode) {
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   float u[3];
@@ -274,7 +286,13 @@ __global__ void k_ray_keys(const float* __restrict__ rays, uint32_t n, const uin
     float ext = hi - lo;
     u[d] = ext > 0.0f ? (rays[6 * (size_t)i + d] - lo) / ext : 0.5f;
   }
-  keys[i] = morton30(u[0], u[1], u[2]);
+  uint32_t key = morton30(u[0], u[1], u[2]);
+  if (key_mode == 1) {
+    const float* d = rays + 6 * (size_t)i + 3;
+    uint32_t oct = (d[0] < 0.0f ? 4u : 0u) | (d[1] < 0.0f ? 2u : 0u) | (d[2] < 0.0f ? 1u : 0u);
+    key = (oct << 27) | (key >> 3);
+  }
+  keys[i] = key;
   vals[i] = i;
 }
 
@@ -375,10 +393,10 @@ parrygpu_status parrygpu_trimesh_cast_rays(parrygpu_ctx* ctx, const parrygpu_tri
       uint32_t* bounds = ctx->misc.as<uint32_t>() + 8;
       PG_CUDA(ctx, cudaMemsetAsync(bounds, 0xff, 12, ctx->stream));
       PG_CUDA(ctx, cudaMemsetAsync(bounds + 3, 0x00, 12, ctx->stream));
-      k_ray_bounds<<<div_up(n, 256), 256, 0, ctx->stream>>>((const float*)d_rays, n, bounds);
+      k_ray_bounds<<<div_up(n, 256 * 8), 256, 0, ctx->stream>>>((const float*)d_rays, n, bounds);
       PG_LAUNCHED(ctx);
       k_ray_keys<<<div_up(n, 256), 256, 0, ctx->stream>>>((const float*)d_rays, n, bounds, ctx->sort_k[0].as<uint32_t>(),
-                                                          ctx->sort_v[0].as<uint32_t>());
+                                                          ctx->sort_v[0].as<uint32_t>(), ctx->cfg.ray_sort_key);
       PG_LAUNCHED(ctx);
       int rb;
       KernelTimer kt(ctx, "ray_sort");

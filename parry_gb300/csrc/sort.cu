@@ -1,5 +1,5 @@
 // Stable LSD radix sort of (u32 key, u32 value) pairs, written for the LBVH build (30-bit Morton
-// keys) and for ray / pair ordering. 8-bit digits, 4096-key tiles:
+// keys) and for ray / pair ordering. 8-bit digits, 2048-key tiles:
 //   1. per-tile digit histogram (shared-memory atomics), stored digit-major: hist[d * tiles + t]
 //   2. one exclusive scan over the digit-major array -> global offset of (digit, tile)
 //   3. per-tile stable scatter: each 256-key round ranks keys within a warp with __match_any_sync,
@@ -10,7 +10,7 @@ namespace {
 
 constexpr int RS_BINS = 256;
 constexpr int RS_THREADS = 256;
-constexpr int RS_ITEMS = 16;
+constexpr int RS_ITEMS = 8;
 constexpr int RS_TILE = RS_THREADS * RS_ITEMS;
 constexpr int RS_WARPS = RS_THREADS / 32;
 constexpr int SCAN_THREADS = 1024;
@@ -30,27 +30,50 @@ __global__ void __launch_bounds__(RS_THREADS) k_rs_hist(const uint32_t* __restri
   hist[threadIdx.x * tiles + blockIdx.x] = h[threadIdx.x];
 }
 
+// Exclusive scan of the digit-major histogram (m = tiles * 256 entries, a multiple of 4) in one
+// block: 4096-entry chunks, 4 consecutive entries per thread (one 16-byte load), warp-shuffle scans,
+// a running carry between chunks.
 __global__ void __launch_bounds__(SCAN_THREADS) k_rs_scan(uint32_t* __restrict__ data, uint32_t m) {
-  __shared__ uint32_t sums[SCAN_THREADS];
-  uint32_t tid = threadIdx.x;
-  uint32_t per = (m + SCAN_THREADS - 1) / SCAN_THREADS;
-  uint32_t begin = tid * per;
-  uint32_t end = begin + per < m ? begin + per : m;
-  uint32_t s = 0;
-  for (uint32_t i = begin; i < end; ++i) s += data[i];
-  sums[tid] = s;
+  __shared__ uint32_t warp_sums[SCAN_THREADS / 32];
+  __shared__ uint32_t carry;
+  const uint32_t tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+  if (tid == 0) carry = 0;
   __syncthreads();
-  for (uint32_t off = 1; off < SCAN_THREADS; off <<= 1) {
-    uint32_t v = tid >= off ? sums[tid - off] : 0u;
+  for (uint32_t base = 0; base < m; base += SCAN_THREADS * 4) {
+    uint32_t idx = base + tid * 4;
+    uint4 v = make_uint4(0, 0, 0, 0);
+    if (idx < m) v = *reinterpret_cast<const uint4*>(data + idx);
+    uint32_t t = v.x + v.y + v.z + v.w;
+    uint32_t incl = t;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= (uint32_t)o) incl += y;
+    }
+    if (lane == 31) warp_sums[w] = incl;
     __syncthreads();
-    sums[tid] += v;
+    if (w == 0) {
+      uint32_t ws = warp_sums[lane];
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        uint32_t y = __shfl_up_sync(0xffffffffu, ws, o);
+        if (lane >= (uint32_t)o) ws += y;
+      }
+      warp_sums[lane] = ws;  // inclusive over warps
+    }
     __syncthreads();
-  }
-  uint32_t run = tid ? sums[tid - 1] : 0u;
-  for (uint32_t i = begin; i < end; ++i) {
-    uint32_t v = data[i];
-    data[i] = run;
-    run += v;
+    uint32_t excl = carry + (w ? warp_sums[w - 1] : 0u) + (incl - t);
+    if (idx < m) {
+      uint4 o;
+      o.x = excl;
+      o.y = excl + v.x;
+      o.z = o.y + v.y;
+      o.w = o.z + v.z;
+      *reinterpret_cast<uint4*>(data + idx) = o;
+    }
+    __syncthreads();
+    if (tid == 0) carry += warp_sums[SCAN_THREADS / 32 - 1];
+    __syncthreads();
   }
 }
 
