@@ -125,6 +125,57 @@ parrygpu_status parrygpu_trimesh_cast_rays(parrygpu_ctx* ctx, const parrygpu_tri
                                            const float* rays, uint32_t n, float max_toi, int solid, uint32_t* feature,
                                            float* toi, float* normal);
 
+/* ---- convex shapes and query::contact ------------------------------------------------------ */
+
+typedef enum parrygpu_shape_type {
+  PARRYGPU_BALL = 0,     /* Ball::new(r)                        params {r, 0, 0, 0} */
+  PARRYGPU_CUBOID = 1,   /* Cuboid::new(half_extents)           params {hx, hy, hz, 0} */
+  PARRYGPU_CAPSULE = 2,  /* Capsule::new_y(half_height, radius) params {half_height, radius, 0, 0} */
+  PARRYGPU_CONVEX = 3,   /* ConvexPolyhedron vertex cloud       params {first vertex, vertex count (u32 bits), 0, 0} */
+  PARRYGPU_TRIANGLE = 4  /* Triangle::new(a, b, c)              params {first vertex (u32 bits), 3, 0, 0} */
+} parrygpu_shape_type;
+
+/* A set of shapes with their poses (SoA). Convex and triangle vertices live in one pool. */
+typedef struct parrygpu_shapes {
+  uint64_t n;
+  const uint32_t* types;   /* n */
+  const float* params;     /* n x 4 */
+  const float* poses;      /* n x 7 (pose7) */
+  const float* vertices;   /* n_vertices x 3 */
+  uint64_t n_vertices;
+} parrygpu_shapes;
+
+/* Same layout as the reference's Contact (src/query/contact/contact.rs:71-105), world space. */
+typedef struct parrygpu_contact {
+  float point1[3];
+  float point2[3];
+  float normal1[3];
+  float normal2[3];
+  float dist;
+} parrygpu_contact;
+
+typedef struct parrygpu_gjk_stats {
+  uint64_t gjk_iterations;  /* support evaluations inside GJK loops */
+  uint64_t epa_iterations;  /* support evaluations inside EPA loops */
+  uint64_t epa_calls;
+  uint64_t reserved;
+} parrygpu_gjk_stats;
+
+/* Replaces Shape::compute_aabb(pos) (src/bounding_volume/aabb_ball.rs:25-27, aabb_cuboid.rs:9-14,
+ * aabb_capsule.rs:8-10, aabb_convex_polyhedron.rs:8-10) followed by Aabb::loosened(margin)
+ * (src/bounding_volume/aabb.rs:982) when margin > 0. aabbs: n x 6 floats. */
+parrygpu_status parrygpu_shapes_aabbs(parrygpu_ctx* ctx, const parrygpu_shapes* shapes, float margin, float* aabbs);
+/* Replaces a loop of query::contact(pos_a, a, pos_b, b, prediction) over the (a, b) rows of `pairs`
+ * (src/query/contact/contact_shape_shape.rs:123-138 -> DefaultQueryDispatcher::contact,
+ * src/query/default_query_dispatcher.rs:302-356). out[k] is written and has_contact[k] = 1 for
+ * Some(contact); has_contact[k] = 0 for None. init_dirs (n_pairs x 3, may be NULL) is the
+ * init_dir warm start of contact_support_map_support_map_with_params
+ * (src/query/contact/contact_support_map_support_map.rs:40-62), used by pairs that take the
+ * GJK/EPA path; NULL gives the reference default. stats may be NULL (else the call synchronises). */
+parrygpu_status parrygpu_contacts(parrygpu_ctx* ctx, const parrygpu_shapes* shapes, const uint32_t* pairs, uint64_t n_pairs,
+                                  float prediction, const float* init_dirs, parrygpu_contact* out, uint8_t* has_contact,
+                                  parrygpu_gjk_stats* stats);
+
 #ifdef __cplusplus
 }
 #endif

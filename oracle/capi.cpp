@@ -117,7 +117,11 @@ void contacts(const uint32_t* types, const float* params, const float* poses, co
               const uint32_t* pairs, uint64_t npairs, float prediction, const float* init_dirs, int threads, O* out, uint8_t* has,
               uint64_t* stats) {
   ShapeSet<R> set(types, params, poses, hullv, nhv, nshapes);
-  std::atomic<uint64_t> gi{0}, ei{0}, ec{0};
+  std::atomic<uint64_t> gi{0}, ei{0}, ec{0}, mf{0}, mv{0}, ms{0};
+  auto amax = [](std::atomic<uint64_t>& a, uint64_t v) {
+    uint64_t cur = a.load();
+    while (v > cur && !a.compare_exchange_weak(cur, v)) {}
+  };
   parallel_for(npairs, threads, [&](uint64_t k) {
     uint32_t a = pairs[2 * k], b = pairs[2 * k + 1];
     Contact<R> c;
@@ -130,6 +134,7 @@ void contacts(const uint32_t* types, const float* params, const float* poses, co
     }
     bool ok = contact_world(set.poses[a], set.shapes[a], set.poses[b], set.shapes[b], R(prediction), &c, &st, ip);
     gi += st.gjk_iters; ei += st.epa_iters; ec += st.epa_calls;
+    amax(mf, st.epa_max_faces); amax(mv, st.epa_max_verts); amax(ms, st.epa_max_sil);
     has[k] = ok ? 1 : 0;
     O* o = out + 13 * k;
     if (ok) {
@@ -140,7 +145,10 @@ void contacts(const uint32_t* types, const float* params, const float* poses, co
       for (int j = 0; j < 13; ++j) o[j] = O(0);
     }
   });
-  if (stats) { stats[0] = gi.load(); stats[1] = ei.load(); stats[2] = ec.load(); }
+  if (stats) {
+    stats[0] = gi.load(); stats[1] = ei.load(); stats[2] = ec.load();
+    stats[3] = mf.load(); stats[4] = mv.load(); stats[5] = ms.load();
+  }
 }
 
 }  // namespace

@@ -255,6 +255,11 @@ template <class R> struct Epa {
       compute_silhouette(support_point_id, face.adj[1], o2);
       compute_silhouette(support_point_id, face.adj[2], o3);
       size_t first_new_face_id = faces.size();
+      if (st) {
+        st->epa_max_sil = std::max<uint64_t>(st->epa_max_sil, silhouette.size());
+        st->epa_max_faces = std::max<uint64_t>(st->epa_max_faces, faces.size() + silhouette.size());
+        st->epa_max_verts = std::max<uint64_t>(st->epa_max_verts, vertices.size());
+      }
       if (silhouette.empty()) return false;
       for (size_t e = 0; e < silhouette.size(); ++e) {
         size_t fid = silhouette[e].first, opp = silhouette[e].second;

@@ -136,6 +136,9 @@ struct GjkStats {
   uint64_t gjk_iters = 0;  // support evaluations in the GJK loop
   uint64_t epa_iters = 0;  // support evaluations in the EPA loop
   uint64_t epa_calls = 0;
+  uint64_t epa_max_faces = 0;   // largest polytope face array in one EPA call
+  uint64_t epa_max_verts = 0;
+  uint64_t epa_max_sil = 0;     // largest silhouette
 };
 
 // gjk.rs:353-453 with exact_dist = true.

@@ -138,10 +138,10 @@ template <class R> struct Iso {
   Vec3<R> transform_vector(const Vec3<R>& v) const { return rot.rotate(v); }
   Vec3<R> inverse_transform_point(const Vec3<R>& p) const { return rot.inv_rotate(p - tra); }
   Vec3<R> inverse_transform_vector(const Vec3<R>& v) const { return rot.inv_rotate(v); }
-  // nalgebra Isometry::inverse: rotation conj, translation -(conj * t).
+  // nalgebra Isometry::inverse_mut: rotation conj, translation conj * (-t).
   Iso inverse() const {
     Quat<R> ci = rot.conj();
-    return Iso(ci, -ci.rotate(tra));
+    return Iso(ci, ci.rotate(-tra));
   }
   // self * o
   Iso operator*(const Iso& o) const {

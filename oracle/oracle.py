@@ -35,6 +35,9 @@ _SIGS = {
     "oracle_bvh_refit_f32": (None, [P, P, U32]),
     "oracle_bvh_self_pairs_f32": (P, [P]),
     "oracle_bvh_leaf_pairs_f32": (P, [P, P]),
+    "oracle_shape_aabbs_f32": (None, [P, P, P, P, U32, U64, F32, P]),
+    "oracle_contacts_f32": (None, [P, P, P, P, U32, U64, P, U64, F32, P, I32, P, P, P]),
+    "oracle_contacts_f64": (None, [P, P, P, P, U32, U64, P, U64, F32, P, I32, P, P, P]),
     "oracle_pairs_count": (U64, [P]),
     "oracle_pairs_copy": (None, [P, P]),
     "oracle_pairs_free": (None, [P]),
@@ -161,3 +164,37 @@ def sorted_pairs(pairs: np.ndarray) -> np.ndarray:
         return pairs.reshape(0, 2)
     order = np.lexsort((pairs[:, 1], pairs[:, 0]))
     return pairs[order]
+
+
+def _shape_arrays(shapes):
+    t, prm, pos, pool = shapes.arrays()
+    return (np.ascontiguousarray(t, np.uint32), np.ascontiguousarray(prm, np.float32),
+            np.ascontiguousarray(pos, np.float32), np.ascontiguousarray(pool, np.float32))
+
+
+def shape_aabbs(shapes, margin: float = 0.0) -> np.ndarray:
+    """Shape::compute_aabb(pos).loosened(margin) for every shape of a parry_gb300.shapes.ShapeSet."""
+    t, prm, pos, pool = _shape_arrays(shapes)
+    out = np.empty((len(t), 6), np.float32)
+    lib().oracle_shape_aabbs_f32(_p(t), _p(prm), _p(pos), _p(pool), len(pool), len(t), float(margin), _p(out))
+    return out
+
+
+def contacts(shapes, pairs: np.ndarray, prediction: float, init_dirs: np.ndarray | None = None, precision: str = "f32",
+             threads: int | None = None):
+    """query::contact(pos_a, a, pos_b, b, prediction) per (a, b) row of `pairs`.
+
+    Returns (has_contact u8 (k,), out (k, 13) = point1, point2, normal1, normal2, dist, stats dict)."""
+    t, prm, pos, pool = _shape_arrays(shapes)
+    pairs = np.ascontiguousarray(pairs, np.uint32).reshape(-1, 2)
+    k = len(pairs)
+    dt = np.float32 if precision == "f32" else np.float64
+    out = np.empty((k, 13), dt)
+    has = np.empty(k, np.uint8)
+    st = np.zeros(6, np.uint64)
+    idir = None if init_dirs is None else np.ascontiguousarray(init_dirs, np.float32).reshape(-1, 3)
+    getattr(lib(), f"oracle_contacts_{precision}")(_p(t), _p(prm), _p(pos), _p(pool), len(pool), len(t), _p(pairs), k,
+                                                   float(prediction), _p(idir), threads if threads is not None else default_threads(),
+                                                   _p(out), _p(has), _p(st))
+    return has, out, {"gjk_iters": int(st[0]), "epa_iters": int(st[1]), "epa_calls": int(st[2]),
+                      "epa_max_faces": int(st[3]), "epa_max_verts": int(st[4]), "epa_max_silhouette": int(st[5])}

@@ -12,6 +12,8 @@ one batched call here:
     TriMesh::new(vertices, indices)                    TriMesh(ctx, vertices, indices)
     TriMesh::cast_ray_and_get_normal(m, ray, t, solid) TriMesh.cast_rays_and_get_normal(rays, t, solid, pose)
     TriMesh::cast_ray(m, ray, t, solid)                TriMesh.cast_rays(rays, t, solid, pose)
+    Shape::compute_aabb(pos).loosened(m)               shape_aabbs(ctx, shapes, margin)
+    query::contact(pos1, g1, pos2, g2, prediction)     contacts(ctx, shapes, pairs, prediction, init_dirs)
 
 Arrays may be numpy arrays (host memory, staged by the library) or torch tensors (CUDA tensors are
 used in place; outputs are then allocated on the same device). Every call goes through the C ABI
@@ -26,7 +28,9 @@ import numpy as np
 from . import _capi
 from ._capi import ParryGpuError, lib, check
 
-__all__ = ["Context", "Bvh", "TriMesh", "ParryGpuError", "NO_HIT", "lib"]
+__all__ = ["Context", "Bvh", "TriMesh", "ShapeSet", "shape_aabbs", "contacts", "ParryGpuError", "NO_HIT", "lib"]
+
+from .shapes import ShapeSet  # noqa: E402
 
 NO_HIT = 0xFFFFFFFF
 
@@ -245,3 +249,59 @@ def _dptr(x) -> int:
     if _is_torch(x):
         return x.data_ptr()
     return x.ctypes.data
+
+
+class _StagedShapes:
+    """Keeps the arrays of a ShapeSet (or of device tensors) alive behind a parrygpu_shapes struct."""
+
+    def __init__(self, shapes):
+        if isinstance(shapes, ShapeSet):
+            t, prm, pos, pool = shapes.arrays()
+        else:
+            t, prm, pos, pool = shapes
+        kt, pt = _as_input(t, np.uint32)
+        kp, pp = _as_input(prm, np.float32)
+        kq, pq = _as_input(pos, np.float32)
+        kv, pv = _as_input(pool, np.float32)
+        self.keep = (kt, kp, kq, kv)
+        self.n = int(kt.shape[0])
+        self.struct = _capi.ParryGpuShapes(self.n, pt.value if pt else None, pp.value if pp else None,
+                                           pq.value if pq else None, pv.value if (pv and kv.shape[0]) else None,
+                                           int(kv.shape[0]) if kv is not None else 0)
+        self.ref = kq
+
+
+def shape_aabbs(ctx: Context, shapes, margin: float = 0.0):
+    """Shape::compute_aabb(pos).loosened(margin) for every shape: (n, 6) = mins, maxs."""
+    st = _StagedShapes(shapes)
+    out, po = _alloc_like(st.ref, (st.n, 6), np.float32)
+    check(lib().parrygpu_shapes_aabbs(ctx.handle, C.byref(st.struct), float(margin), po), ctx.handle)
+    return out
+
+
+def contacts(ctx: Context, shapes, pairs, prediction: float, init_dirs=None, want_stats: bool = False, out=None):
+    """Batched query::contact over the (a, b) rows of `pairs`.
+
+    Returns (has_contact u8 (k,), contacts f32 (k, 13) = point1, point2, normal1, normal2, dist)
+    [, stats dict]."""
+    st = _StagedShapes(shapes)
+    kp, pp = _as_input(pairs, np.uint32)
+    k = int(kp.shape[0]) if kp is not None else 0
+    ki, pi = _as_input(init_dirs, np.float32) if init_dirs is not None else (None, None)
+    if out is None:
+        res, pr = _alloc_like(kp, (k, 13), np.float32)
+        if _is_torch(kp):
+            has = torch.empty(k, dtype=torch.uint8, device=kp.device, pin_memory=kp.device.type == "cpu" and kp.is_pinned())
+            ph = C.c_void_p(has.data_ptr())
+        else:
+            has = np.empty(k, np.uint8)
+            ph = C.c_void_p(has.ctypes.data)
+    else:
+        has, res = out
+        ph, pr = C.c_void_p(_dptr(has)), C.c_void_p(_dptr(res))
+    stats = _capi.ParryGpuGjkStats()
+    check(lib().parrygpu_contacts(ctx.handle, C.byref(st.struct), pp, k, float(prediction), pi, pr, ph,
+                                  C.byref(stats) if want_stats else None), ctx.handle)
+    if want_stats:
+        return has, res, {"gjk_iters": stats.gjk_iterations, "epa_iters": stats.epa_iterations, "epa_calls": stats.epa_calls}
+    return has, res

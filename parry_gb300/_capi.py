@@ -53,7 +53,19 @@ SIGNATURES: dict[str, tuple] = {
     "parrygpu_trimesh_create": (I32, [P, P, U32, P, U32, C.POINTER(P)]),
     "parrygpu_trimesh_destroy": (None, [P]),
     "parrygpu_trimesh_cast_rays": (I32, [P, P, P, P, U32, F32, I32, P, P, P]),
+    "parrygpu_shapes_aabbs": (I32, [P, P, F32, P]),
+    "parrygpu_contacts": (I32, [P, P, P, U64, F32, P, P, P, P]),
 }
+
+
+class ParryGpuShapes(C.Structure):
+    _fields_ = [("n", C.c_uint64), ("types", C.c_void_p), ("params", C.c_void_p), ("poses", C.c_void_p),
+                ("vertices", C.c_void_p), ("n_vertices", C.c_uint64)]
+
+
+class ParryGpuGjkStats(C.Structure):
+    _fields_ = [("gjk_iterations", C.c_uint64), ("epa_iterations", C.c_uint64), ("epa_calls", C.c_uint64),
+                ("reserved", C.c_uint64)]
 
 
 class ParryGpuError(RuntimeError):

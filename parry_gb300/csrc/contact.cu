@@ -1,0 +1,528 @@
+// Batched query::contact for convex shapes (balls, cuboids, capsules, convex polyhedra, triangles)
+// and per-shape AABBs.
+//
+// Pipeline (one stream, no host round trip):
+//   k_contacts_main  one thread per pair: dispatch of DefaultQueryDispatcher::contact
+//                    (src/query/default_query_dispatcher.rs:302-356): ball-ball analytic, ball-convex
+//                    by point projection, otherwise GJK (gjk_device.cuh). Pairs whose GJK ends inside
+//                    the Minkowski difference append (pair, final simplex) to an EPA queue.
+//   k_contacts_epa   persistent grid-stride loop over the EPA queue, one polytope workspace slot per
+//                    thread (epa_device.cuh), finishing those pairs exactly as the reference does.
+// Results are written in world space (contact_shape_shape.rs:123-138).
+#include "internal.hpp"
+#include "epa_device.cuh"
+#include <cstring>
+
+using namespace pg;
+
+namespace {
+
+constexpr int CT_THREADS = 128;
+constexpr int EPA_THREADS = 64;
+constexpr int QUEUE_WORDS = 40;  // pair, dim, 4 x CSO (9 words), pad
+
+struct ContactOut {
+  V3 p1, p2, n1, n2;
+  float dist;
+};
+
+struct ShapeArrays {
+  const uint32_t* types;
+  const float4* params;
+  const float* poses;
+  const float* pool;
+  uint64_t n_shapes;
+  uint64_t n_vertices;
+};
+
+// Rejects out-of-range pair indices and vertex ranges (reported as a capacity / argument error
+// through the context's error word; the pair reports no contact).
+__device__ __forceinline__ bool valid_pair(const ShapeArrays& sh, uint32_t a, uint32_t b) {
+  if (a >= sh.n_shapes || b >= sh.n_shapes) return false;
+  uint32_t ids[2] = {a, b};
+#pragma unroll
+  for (int k = 0; k < 2; ++k) {
+    uint32_t t = sh.types[ids[k]];
+    if (t > SH_TRIANGLE) return false;
+    if (t == SH_CONVEX || t == SH_TRIANGLE) {
+      float4 p = sh.params[ids[k]];
+      uint64_t first = __float_as_uint(p.x), cnt = __float_as_uint(p.y);
+      if (cnt == 0 || first + cnt > sh.n_vertices || (t == SH_TRIANGLE && cnt != 3)) return false;
+    }
+  }
+  return true;
+}
+
+// contact_ball_ball.rs:9-42
+__device__ __forceinline__ bool contact_ball_ball(const Pose& pos12, float r1, float r2, float prediction, ContactOut* c) {
+  V3 center = pos12.t;
+  float d2 = dot(center, center);
+  float sum = r1 + r2;
+  float sum_err = sum + prediction;
+  if (!(d2 < sum_err * sum_err)) return false;
+  V3 n1 = d2 != 0.0f ? normalize(center) : v3(1.f, 0.f, 0.f);
+  V3 n2 = -pose_inv_rotate(pos12, n1);
+  c->p1 = n1 * r1;
+  c->p2 = n2 * r2;
+  c->n1 = n1;
+  c->n2 = n2;
+  c->dist = sqrtf(d2) - sum;
+  return true;
+}
+
+struct PointProj {
+  bool inside;
+  V3 point;
+  int face;
+};
+
+// point_aabb.rs:9-132 on [-h, h] with solid = false.
+__device__ __forceinline__ PointProj project_cuboid(V3 h, V3 pt) {
+  V3 mins = -h, maxs = h;
+  V3 mins_pt = mins - pt, pt_maxs = pt - maxs;
+  V3 z = v3(0.f, 0.f, 0.f);
+  V3 shift = vmax(mins_pt, z) - vmax(pt_maxs, z);
+  bool inside = shift.x == 0.0f && shift.y == 0.0f && shift.z == 0.0f;
+  PointProj out;
+  V3 ls;
+  if (!inside) {
+    ls = pt + shift;
+    out.inside = false;
+  } else {
+    float best = -FLT_MAX;
+    bool is_mins = false;
+    int best_id = 0;
+    float mp[3] = {mins_pt.x, mins_pt.y, mins_pt.z}, pm[3] = {pt_maxs.x, pt_maxs.y, pt_maxs.z};
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      if (mp[i] < pm[i]) {
+        if (pm[i] > best) { best_id = i; is_mins = false; best = pm[i]; }
+      } else if (mp[i] > best) { best_id = i; is_mins = true; best = mp[i]; }
+    }
+    float s[3] = {0.f, 0.f, 0.f};
+    s[best_id] = is_mins ? best : -best;
+    shift = v3(s[0], s[1], s[2]);
+    ls = pt + shift;
+    out.inside = true;
+  }
+  out.point = ls;
+  out.face = -1;
+  float sh[3] = {shift.x, shift.y, shift.z}, l[3] = {ls.x, ls.y, ls.z}, mn[3] = {mins.x, mins.y, mins.z}, mx[3] = {maxs.x, maxs.y, maxs.z};
+  int nz = 0, last_nz = 0;
+#pragma unroll
+  for (int i = 0; i < 3; ++i) { if (sh[i] == 0.0f) nz++; else last_nz = i; }
+  if (nz == 3) {
+    for (int i = 0; i < 3; ++i) {
+      if (l[i] > mx[i] - EPS) { out.face = i; break; }
+      if (l[i] <= mn[i] + EPS) { out.face = i + 3; break; }
+    }
+  } else if (nz == 2) {
+    float center = (mn[last_nz] + mx[last_nz]) * 0.5f;
+    out.face = l[last_nz] < center ? last_nz + 3 : last_nz;
+  }
+  return out;
+}
+
+// point_capsule.rs:7-51 with solid = false.
+__device__ __forceinline__ PointProj project_capsule(float hh, float radius, V3 pt) {
+  Loc loc;
+  V3 a = v3(0.f, -hh, 0.f), b = v3(0.f, hh, 0.f);
+  V3 proj = project_segment(a, b, pt, &loc);
+  V3 dir;
+  float dist;
+  PointProj out;
+  out.face = -1;
+  if (try_normalize(pt - proj, EPS, &dir, &dist)) {
+    out.inside = dist <= radius;
+    out.point = proj + dir * radius;
+    return out;
+  }
+  V3 sd;
+  out.inside = true;
+  if (try_normalize(b - a, EPS, &sd)) {
+    float sign = copysignf(1.0f, sd.z);
+    float aa = -1.0f / (sign + sd.z);
+    float bb = sd.x * sd.y * aa;
+    V3 t = v3(1.0f + sign * sd.x * sd.x * aa, sign * bb, -sign * sd.x);
+    out.point = proj + t * radius;
+  } else {
+    out.point = proj + v3(0.f, radius, 0.f);
+  }
+  return out;
+}
+
+// Finishes contact_convex_polyhedron_ball (contact_ball_convex_polyhedron.rs:26-63) from a projection.
+__device__ __forceinline__ bool finish_convex_ball(const Pose& pos12, const ShapeDev& s1, const PointProj& proj, float r2, float prediction,
+                                                   ContactOut* c) {
+  V3 center = pos12.t;
+  float dist;
+  V3 n1, dir1;
+  float len;
+  if (try_normalize(proj.point - center, EPS, &dir1, &len)) {
+    if (proj.inside) { dist = -len - r2; n1 = dir1; }
+    else { dist = len - r2; n1 = -dir1; }
+  } else {
+    dist = -r2;
+    if (s1.type == SH_CUBOID && proj.face >= 0) {
+      float d[3] = {0.f, 0.f, 0.f};
+      if (proj.face < 3) d[proj.face] = 1.0f; else d[proj.face - 3] = -1.0f;
+      n1 = v3(d[0], d[1], d[2]);
+    } else if (!try_normalize(proj.point, EPS, &n1)) {
+      n1 = v3(0.f, 1.f, 0.f);
+    }
+  }
+  if (!(dist <= prediction)) return false;
+  V3 n2 = pose_inv_rotate(pos12, -n1);
+  c->p1 = proj.point;
+  c->p2 = n2 * r2;
+  c->n1 = n1;
+  c->n2 = n2;
+  c->dist = dist;
+  return true;
+}
+
+// contact_support_map_support_map: ClosestPoints -> Contact
+__device__ __forceinline__ void finish_support_pair(const Pose& pos12, V3 p1, V3 p2, V3 n1, ContactOut* c) {
+  c->dist = dot(p2 - p1, n1);
+  c->p1 = p1;
+  c->p2 = pose_inv_point(pos12, p2);
+  c->n1 = n1;
+  c->n2 = pose_inv_rotate(pos12, -n1);
+}
+
+__device__ __forceinline__ void write_out(float* __restrict__ out, uint8_t* __restrict__ has, uint64_t k, bool ok, const ContactOut& c,
+                                          const Pose& pa, const Pose& pb) {
+  float* o = out + 13 * k;
+  if (ok) {
+    V3 p1 = pose_point(pa, c.p1), p2 = pose_point(pb, c.p2), n1 = pose_rotate(pa, c.n1), n2 = pose_rotate(pb, c.n2);
+    o[0] = p1.x; o[1] = p1.y; o[2] = p1.z;
+    o[3] = p2.x; o[4] = p2.y; o[5] = p2.z;
+    o[6] = n1.x; o[7] = n1.y; o[8] = n1.z;
+    o[9] = n2.x; o[10] = n2.y; o[11] = n2.z;
+    o[12] = c.dist;
+  } else {
+#pragma unroll
+    for (int j = 0; j < 13; ++j) o[j] = 0.0f;
+  }
+  has[k] = ok ? 1 : 0;
+}
+
+__device__ __forceinline__ void enqueue(uint32_t* __restrict__ queue, unsigned long long* __restrict__ qcount, uint64_t k, const Simplex& s) {
+  unsigned long long slot = atomicAdd(qcount, 1ull);
+  uint32_t* e = queue + (size_t)slot * QUEUE_WORDS;
+  e[0] = (uint32_t)k;
+  e[1] = (uint32_t)s.dim;
+  for (int i = 0; i <= s.dim; ++i) {
+    float* f = reinterpret_cast<float*>(e + 2 + 9 * i);
+    f[0] = s.v[i].p.x; f[1] = s.v[i].p.y; f[2] = s.v[i].p.z;
+    f[3] = s.v[i].o1.x; f[4] = s.v[i].o1.y; f[5] = s.v[i].o1.z;
+    f[6] = s.v[i].o2.x; f[7] = s.v[i].o2.y; f[8] = s.v[i].o2.z;
+  }
+}
+
+// Which path a pair takes in DefaultQueryDispatcher::contact.
+enum : int { PATH_BALL_BALL = 0, PATH_BALL_FIRST = 1, PATH_BALL_SECOND = 2, PATH_SUPPORT = 3 };
+
+struct PairSetup {
+  ShapeDev s1, s2;
+  Pose pa, pb, pos12;
+  int path;
+  // for the ball paths: the convex shape, the pose used for the projection and the ball radius
+  Pose cpos;
+  const ShapeDev* convex;
+  float radius;
+};
+
+__device__ __forceinline__ void setup_pair(const ShapeArrays& sh, uint32_t a, uint32_t b, PairSetup* ps) {
+  ps->s1 = load_shape(sh.types, sh.params, sh.pool, a);
+  ps->s2 = load_shape(sh.types, sh.params, sh.pool, b);
+  ps->pa = load_pose(sh.poses, a);
+  ps->pb = load_pose(sh.poses, b);
+  ps->pos12 = pose_inv_mul(ps->pa, ps->pb);
+  bool b1 = ps->s1.type == SH_BALL, b2 = ps->s2.type == SH_BALL;
+  if (b1 && b2) ps->path = PATH_BALL_BALL;
+  else if (b1) { ps->path = PATH_BALL_FIRST; ps->cpos = pose_inverse(ps->pos12); ps->convex = &ps->s2; ps->radius = ps->s1.a; }
+  else if (b2) { ps->path = PATH_BALL_SECOND; ps->cpos = ps->pos12; ps->convex = &ps->s1; ps->radius = ps->s2.a; }
+  else ps->path = PATH_SUPPORT;
+}
+
+__device__ __forceinline__ void flip(ContactOut* c) {
+  V3 t = c->p1; c->p1 = c->p2; c->p2 = t;
+  t = c->n1; c->n1 = c->n2; c->n2 = t;
+}
+
+__global__ void __launch_bounds__(CT_THREADS) k_contacts_main(ShapeArrays sh, const uint32_t* __restrict__ pairs, uint64_t n,
+                                                              float prediction, const float* __restrict__ init_dirs,
+                                                              float* __restrict__ out, uint8_t* __restrict__ has,
+                                                              uint32_t* __restrict__ queue, unsigned long long* __restrict__ qcount,
+                                                              unsigned long long* __restrict__ stats, uint32_t* __restrict__ err) {
+  uint64_t k = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+  uint32_t iters = 0;
+  if (k < n && !valid_pair(sh, pairs[2 * k], pairs[2 * k + 1])) {
+    atomicOr(err, ERR_CAPACITY);
+    float* o = out + 13 * k;
+    for (int j = 0; j < 13; ++j) o[j] = 0.0f;
+    has[k] = 0;
+  } else if (k < n) {
+    PairSetup ps;
+    setup_pair(sh, pairs[2 * k], pairs[2 * k + 1], &ps);
+    ContactOut c;
+    bool ok = false, done = true;
+    if (ps.path == PATH_BALL_BALL) {
+      ok = contact_ball_ball(ps.pos12, ps.s1.a, ps.s2.a, prediction, &c);
+    } else if (ps.path != PATH_SUPPORT) {
+      const ShapeDev& cs = *ps.convex;
+      PointProj proj;
+      V3 center = ps.cpos.t;
+      if (cs.type == SH_CUBOID) proj = project_cuboid(v3(cs.a, cs.b, cs.c), center);
+      else if (cs.type == SH_CAPSULE) proj = project_capsule(cs.a, cs.b, center);
+      else {
+        // point_support_map.rs:17-57: GJK projection of the origin onto shape - center
+        Pose m{0.f, 0.f, 0.f, 1.f, -center};
+        Pose minv = pose_inverse(m);
+        Pose m_inv{0.f, 0.f, 0.f, 1.f, center};
+        ShapeDev origin;
+        origin.type = SH_ORIGIN;
+        V3 dir;
+        if (!try_normalize(-m.t, EPS, &dir)) dir = v3(1.f, 0.f, 0.f);
+        Simplex s;
+        simplex_reset(s, cso_from_shapes(m_inv, cs, origin, dir));
+        GjkOut g = gjk_closest_points(minv, cs, origin, FLT_MAX, s, &iters);
+        if (g.kind == GJK_CLOSEST) {
+          proj.inside = false;
+          proj.point = g.p1;
+          proj.face = -1;
+        } else {
+          enqueue(queue, qcount, k, s);
+          done = false;
+        }
+      }
+      if (done) {
+        ok = finish_convex_ball(ps.cpos, cs, proj, ps.radius, prediction, &c);
+        if (ok && ps.path == PATH_BALL_FIRST) flip(&c);
+      }
+    } else {
+      V3 dir;
+      if (init_dirs) dir = v3(init_dirs[3 * k], init_dirs[3 * k + 1], init_dirs[3 * k + 2]);
+      else if (!try_normalize(ps.pos12.t, EPS, &dir)) dir = v3(1.f, 0.f, 0.f);
+      Simplex s;
+      simplex_reset(s, cso_from_shapes(ps.pos12, ps.s1, ps.s2, dir));
+      GjkOut g = gjk_closest_points(ps.pos12, ps.s1, ps.s2, prediction, s, &iters);
+      if (g.kind == GJK_CLOSEST) {
+        ok = true;
+        finish_support_pair(ps.pos12, g.p1, g.p2, g.dir, &c);
+      } else if (g.kind == GJK_INTERSECTION) {
+        enqueue(queue, qcount, k, s);
+        done = false;
+      }
+    }
+    if (done) write_out(out, has, k, ok, c, ps.pa, ps.pb);
+  }
+  if (stats) {
+    uint32_t w = __reduce_add_sync(0xffffffffu, iters);
+    if ((threadIdx.x & 31) == 0 && w) atomicAdd(&stats[0], (unsigned long long)w);
+  }
+}
+
+__global__ void __launch_bounds__(EPA_THREADS) k_contacts_epa(ShapeArrays sh, const uint32_t* __restrict__ pairs, float prediction,
+                                                              float* __restrict__ out, uint8_t* __restrict__ has,
+                                                              const uint32_t* __restrict__ queue, const unsigned long long* __restrict__ qcount,
+                                                              uint32_t* __restrict__ ws_pool, unsigned long long* __restrict__ stats,
+                                                              uint32_t* __restrict__ err) {
+  const uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x;
+  EpaWs ws{ws_pool + (size_t)(slot >> 5) * (EPA_WORDS * 32) + (slot & 31)};
+  const unsigned long long total = *qcount;
+  uint32_t iters = 0, calls = 0;
+  for (unsigned long long e = slot; e < total; e += (unsigned long long)gridDim.x * blockDim.x) {
+    const uint32_t* q = queue + (size_t)e * QUEUE_WORDS;
+    uint64_t k = q[0];
+    Simplex s;
+    simplex_reset(s, CSO{});
+    s.dim = (int)q[1];
+    for (int i = 0; i <= s.dim; ++i) {
+      const float* f = reinterpret_cast<const float*>(q + 2 + 9 * i);
+      s.v[i] = CSO{v3(f[0], f[1], f[2]), v3(f[3], f[4], f[5]), v3(f[6], f[7], f[8])};
+    }
+    PairSetup ps;
+    setup_pair(sh, pairs[2 * k], pairs[2 * k + 1], &ps);
+    ContactOut c;
+    bool ok = false;
+    V3 p1, p2, nn;
+    calls++;
+    if (ps.path == PATH_SUPPORT) {
+      int r = epa_closest_points(ws, ps.pos12, ps.s1, ps.s2, s, &p1, &p2, &nn, &iters);
+      if (r == EPA_OVERFLOW) atomicOr(err, ERR_POLYTOPE_FULL);
+      if (r == EPA_OK) { ok = true; finish_support_pair(ps.pos12, p1, p2, nn, &c); }
+    } else {
+      const ShapeDev& cs = *ps.convex;
+      V3 center = ps.cpos.t;
+      Pose m{0.f, 0.f, 0.f, 1.f, -center};
+      Pose minv = pose_inverse(m);
+      ShapeDev origin;
+      origin.type = SH_ORIGIN;
+      PointProj proj;
+      proj.face = -1;
+      proj.inside = true;
+      int r = epa_closest_points(ws, minv, cs, origin, s, &p1, &p2, &nn, &iters);
+      if (r == EPA_OVERFLOW) atomicOr(err, ERR_POLYTOPE_FULL);
+      proj.point = r == EPA_OK ? p1 : center;
+      ok = finish_convex_ball(ps.cpos, cs, proj, ps.radius, prediction, &c);
+      if (ok && ps.path == PATH_BALL_FIRST) flip(&c);
+    }
+    write_out(out, has, k, ok, c, ps.pa, ps.pb);
+  }
+  if (stats) {
+    uint32_t w = __reduce_add_sync(0xffffffffu, iters);
+    uint32_t cw = __reduce_add_sync(0xffffffffu, calls);
+    if ((threadIdx.x & 31) == 0) {
+      if (w) atomicAdd(&stats[1], (unsigned long long)w);
+      if (cw) atomicAdd(&stats[2], (unsigned long long)cw);
+    }
+  }
+}
+
+// Shape::compute_aabb(pos).loosened(margin)
+__global__ void k_shape_aabbs(ShapeArrays sh, uint64_t n, float margin, float* __restrict__ out, uint32_t* __restrict__ err) {
+  uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  if (!valid_pair(sh, (uint32_t)i, (uint32_t)i)) {
+    atomicOr(err, ERR_CAPACITY);
+    for (int j = 0; j < 6; ++j) out[6 * i + j] = 0.0f;
+    return;
+  }
+  ShapeDev s = load_shape(sh.types, sh.params, sh.pool, (uint32_t)i);
+  Pose p = load_pose(sh.poses, (uint32_t)i);
+  V3 mn, mx;
+  if (s.type == SH_BALL) {
+    mn = p.t + v3(-s.a, -s.a, -s.a);
+    mx = p.t + v3(s.a, s.a, s.a);
+  } else if (s.type == SH_CUBOID) {
+    // |R| h with R = to_rotation_matrix (isometry_ops.rs:14-19), row r = (|m_r0| hx + |m_r1| hy) + |m_r2| hz
+    float ww = p.qw * p.qw, ii = p.qi * p.qi, jj = p.qj * p.qj, kk = p.qk * p.qk;
+    float ij = p.qi * p.qj * 2.0f, wk = p.qw * p.qk * 2.0f, wj = p.qw * p.qj * 2.0f;
+    float ik = p.qi * p.qk * 2.0f, jk = p.qj * p.qk * 2.0f, wi = p.qw * p.qi * 2.0f;
+    float m00 = ww + ii - jj - kk, m01 = ij - wk, m02 = wj + ik;
+    float m10 = wk + ij, m11 = ww - ii + jj - kk, m12 = jk - wi;
+    float m20 = ik - wj, m21 = wi + jk, m22 = ww - ii - jj + kk;
+    V3 he = v3((fabsf(m00) * s.a + fabsf(m01) * s.b) + fabsf(m02) * s.c, (fabsf(m10) * s.a + fabsf(m11) * s.b) + fabsf(m12) * s.c,
+               (fabsf(m20) * s.a + fabsf(m21) * s.b) + fabsf(m22) * s.c);
+    mn = p.t - he;
+    mx = p.t + he;
+  } else if (s.type == SH_CAPSULE) {
+    V3 a = pose_point(p, v3(0.f, -s.a, 0.f)), b = pose_point(p, v3(0.f, s.a, 0.f));
+    mn = vmin(a, b) - v3(s.b, s.b, s.b);
+    mx = vmax(a, b) + v3(s.b, s.b, s.b);
+  } else {
+    mn = pose_point(p, ldv(s.pts));
+    mx = mn;
+    for (uint32_t j = 1; j < s.npts; ++j) {
+      V3 q = pose_point(p, ldv(s.pts + 3 * j));
+      mn = vmin(mn, q);
+      mx = vmax(mx, q);
+    }
+  }
+  if (margin > 0.0f) {
+    mn = mn + v3(-margin, -margin, -margin);
+    mx = mx + v3(margin, margin, margin);
+  }
+  float* o = out + 6 * i;
+  o[0] = mn.x; o[1] = mn.y; o[2] = mn.z; o[3] = mx.x; o[4] = mx.y; o[5] = mx.z;
+}
+
+}  // namespace
+
+static parrygpu_status stage_shapes(parrygpu_ctx* ctx, const parrygpu_shapes* s, ShapeArrays* out) {
+  if (!s) return set_error(ctx, PARRYGPU_INVALID_ARG, "shapes is null");
+  const void *t, *p, *q, *v;
+  parrygpu_status st;
+  if ((st = stage_input(ctx, ctx->stage_in[0], s->types, (size_t)s->n * 4, &t)) != PARRYGPU_OK) return st;
+  if ((st = stage_input(ctx, ctx->stage_in[1], s->params, (size_t)s->n * 16, &p)) != PARRYGPU_OK) return st;
+  if ((st = stage_input(ctx, ctx->stage_in[2], s->poses, (size_t)s->n * 28, &q)) != PARRYGPU_OK) return st;
+  if ((st = stage_input(ctx, ctx->stage_in[3], s->vertices, (size_t)s->n_vertices * 12, &v)) != PARRYGPU_OK) return st;
+  if (((uintptr_t)p & 15) != 0) return set_error(ctx, PARRYGPU_INVALID_ARG, "shape params must be 16-byte aligned");
+  *out = ShapeArrays{(const uint32_t*)t, (const float4*)p, (const float*)q, (const float*)v, s->n, s->n_vertices};
+  return PARRYGPU_OK;
+}
+
+extern "C" {
+
+parrygpu_status parrygpu_shapes_aabbs(parrygpu_ctx* ctx, const parrygpu_shapes* shapes, float margin, float* aabbs) {
+  if (!ctx || !shapes) return PARRYGPU_INVALID_ARG;
+  if (shapes->n == 0) return PARRYGPU_OK;
+  if (!aabbs) return set_error(ctx, PARRYGPU_INVALID_ARG, "aabbs is null");
+  PG_CUDA(ctx, cudaSetDevice(ctx->device));
+  ShapeArrays sh;
+  parrygpu_status s = stage_shapes(ctx, shapes, &sh);
+  if (s != PARRYGPU_OK) return s;
+  void* d_out;
+  bool copy;
+  if ((s = stage_output(ctx, ctx->stage_out[0], aabbs, (size_t)shapes->n * 24, &d_out, &copy)) != PARRYGPU_OK) return s;
+  KernelTimer kt(ctx, "shape_aabbs");
+  k_shape_aabbs<<<div_up(shapes->n, 256), 256, 0, ctx->stream>>>(sh, shapes->n, margin, (float*)d_out, ctx->d_err);
+  kt.stop();
+  PG_LAUNCHED(ctx);
+  if (copy) {
+    PG_CUDA(ctx, cudaMemcpyAsync(aabbs, d_out, (size_t)shapes->n * 24, cudaMemcpyDeviceToHost, ctx->stream));
+  }
+  if (copy || sh.types != shapes->types || sh.poses != shapes->poses) return parrygpu_sync(ctx);
+  return PARRYGPU_OK;
+}
+
+parrygpu_status parrygpu_contacts(parrygpu_ctx* ctx, const parrygpu_shapes* shapes, const uint32_t* pairs, uint64_t n_pairs,
+                                  float prediction, const float* init_dirs, parrygpu_contact* out, uint8_t* has_contact,
+                                  parrygpu_gjk_stats* stats) {
+  if (!ctx || !shapes) return PARRYGPU_INVALID_ARG;
+  if (stats) std::memset(stats, 0, sizeof(*stats));
+  if (n_pairs == 0) return PARRYGPU_OK;
+  if (!pairs || !out || !has_contact) return set_error(ctx, PARRYGPU_INVALID_ARG, "pairs, out and has_contact are required");
+  PG_CUDA(ctx, cudaSetDevice(ctx->device));
+  ShapeArrays sh;
+  parrygpu_status s = stage_shapes(ctx, shapes, &sh);
+  if (s != PARRYGPU_OK) return s;
+  const void *dp, *di = nullptr;
+  if ((s = stage_input(ctx, ctx->stage_in[4], pairs, (size_t)n_pairs * 8, &dp)) != PARRYGPU_OK) return s;
+  if (init_dirs && (s = stage_input(ctx, ctx->stage_in[5], init_dirs, (size_t)n_pairs * 12, &di)) != PARRYGPU_OK) return s;
+  void *d_out, *d_has;
+  bool c_out, c_has;
+  if ((s = stage_output(ctx, ctx->stage_out[0], out, (size_t)n_pairs * 52, &d_out, &c_out)) != PARRYGPU_OK) return s;
+  if ((s = stage_output(ctx, ctx->stage_out[1], has_contact, (size_t)n_pairs, &d_has, &c_has)) != PARRYGPU_OK) return s;
+  PG_CUDA(ctx, ctx->ct_queue.reserve((size_t)n_pairs * QUEUE_WORDS * 4));
+  PG_CUDA(ctx, ctx->ct_counters.reserve(64));
+  uint32_t epa_blocks = (uint32_t)(ctx->sm_count > 0 ? ctx->sm_count : 152) * 4;
+  uint32_t slots = epa_blocks * EPA_THREADS;
+  PG_CUDA(ctx, ctx->epa_ws.reserve((size_t)(slots / 32) * EPA_SLOT_GROUP_BYTES));
+  unsigned long long* ctr = ctx->ct_counters.as<unsigned long long>();  // [0] queue count, [1..3] stats
+  PG_CUDA(ctx, cudaMemsetAsync(ctr, 0, 64, ctx->stream));
+  {
+    KernelTimer kt(ctx, "contacts_gjk");
+    k_contacts_main<<<div_up(n_pairs, CT_THREADS), CT_THREADS, 0, ctx->stream>>>(
+        sh, (const uint32_t*)dp, n_pairs, prediction, (const float*)di, (float*)d_out, (uint8_t*)d_has, ctx->ct_queue.as<uint32_t>(),
+        ctr, ctr + 1, ctx->d_err);
+    kt.stop();
+    PG_LAUNCHED(ctx);
+  }
+  {
+    KernelTimer kt(ctx, "contacts_epa");
+    k_contacts_epa<<<epa_blocks, EPA_THREADS, 0, ctx->stream>>>(sh, (const uint32_t*)dp, prediction, (float*)d_out, (uint8_t*)d_has,
+                                                                ctx->ct_queue.as<uint32_t>(), ctr, ctx->epa_ws.as<uint32_t>(), ctr + 1,
+                                                                ctx->d_err);
+    kt.stop();
+    PG_LAUNCHED(ctx);
+  }
+  if (c_out) PG_CUDA(ctx, cudaMemcpyAsync(out, d_out, (size_t)n_pairs * 52, cudaMemcpyDeviceToHost, ctx->stream));
+  if (c_has) PG_CUDA(ctx, cudaMemcpyAsync(has_contact, d_has, (size_t)n_pairs, cudaMemcpyDeviceToHost, ctx->stream));
+  if (stats) {
+    unsigned long long h[4];
+    PG_CUDA(ctx, cudaMemcpyAsync(h, ctr, 32, cudaMemcpyDeviceToHost, ctx->stream));
+    PG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    stats->gjk_iterations = h[1];
+    stats->epa_iterations = h[2];
+    stats->epa_calls = h[3];
+  }
+  bool staged_in = sh.types != shapes->types || sh.params != (const float4*)shapes->params || sh.poses != shapes->poses ||
+                   dp != pairs || (init_dirs && di != init_dirs) || (shapes->n_vertices && sh.pool != shapes->vertices);
+  if (c_out || c_has || stats || staged_in) return parrygpu_sync(ctx);
+  return PARRYGPU_OK;
+}
+
+}  // extern "C"

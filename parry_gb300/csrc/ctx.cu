@@ -78,6 +78,7 @@ parrygpu_status parrygpu_create(parrygpu_ctx** out, const parrygpu_config* cfg) 
   if (e == cudaSuccess) e = cudaMalloc(&ctx->d_err, sizeof(uint32_t));
   if (e == cudaSuccess) e = cudaMemset(ctx->d_err, 0, sizeof(uint32_t));
   if (e == cudaSuccess) e = cudaMallocHost(&ctx->h_err, sizeof(uint32_t));
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, ctx->device);
   if (e != cudaSuccess) { delete ctx; return PARRYGPU_CUDA_ERROR; }
   ctx->stream = ctx->own_stream;
   *out = ctx;
@@ -91,7 +92,11 @@ void parrygpu_destroy(parrygpu_ctx* ctx) {
   for (auto* b : {&ctx->sort_k[0], &ctx->sort_k[1], &ctx->sort_v[0], &ctx->sort_v[1], &ctx->sort_hist, &ctx->misc,
                   &ctx->counters, &ctx->ray_keys, &ctx->ray_order})
     b->release();
-  for (int i = 0; i < 4; ++i) { ctx->stage_in[i].release(); ctx->stage_out[i].release(); }
+  for (int i = 0; i < 8; ++i) ctx->stage_in[i].release();
+  for (int i = 0; i < 4; ++i) ctx->stage_out[i].release();
+  ctx->ct_queue.release();
+  ctx->ct_counters.release();
+  ctx->epa_ws.release();
   if (ctx->d_err) cudaFree(ctx->d_err);
   if (ctx->h_err) cudaFreeHost(ctx->h_err);
   drop_pending(ctx);

@@ -1,0 +1,322 @@
+// Device-side EPA (src/query/epa/epa3.rs:17-675, path relative to the parry repository).
+//
+// The polytope lives in a per-thread workspace slot in global memory, interleaved across the 32
+// slots of a warp (word w of slot s at base[w * 32 + s % 32]) so that lanes touching the same
+// element index coalesce. Fixed capacities replace the reference's Vecs; exceeding one aborts the
+// pair and raises a capacity error (observed maxima on 8-256-vertex hull pairs: 239 faces,
+// 55 vertices, silhouettes of 10 edges). The reference's recursive silhouette walk becomes an
+// explicit stack visiting faces in the same order, and its BinaryHeap is restated with the same
+// sift operations so that ties between face distances pop in the same order.
+#pragma once
+#include "gjk_device.cuh"
+
+namespace pg {
+
+constexpr int EPA_MAX_VERTS = 128;
+constexpr int EPA_MAX_FACES = 512;
+constexpr int EPA_MAX_SIL = 64;
+constexpr int EPA_STACK = 256;
+constexpr int EPA_W_VERTS = 0;                                   // 9 words per vertex
+constexpr int EPA_W_FACES = EPA_W_VERTS + 9 * EPA_MAX_VERTS;     // 9 words per face
+constexpr int EPA_W_HEAP = EPA_W_FACES + 9 * EPA_MAX_FACES;      // 2 words per heap entry
+constexpr int EPA_W_SIL = EPA_W_HEAP + 2 * EPA_MAX_FACES;        // 1 word per silhouette edge
+constexpr int EPA_W_STACK = EPA_W_SIL + EPA_MAX_SIL;             // 1 word per stack entry
+constexpr int EPA_WORDS = EPA_W_STACK + EPA_STACK;               // words per slot
+constexpr size_t EPA_SLOT_GROUP_BYTES = (size_t)EPA_WORDS * 32 * 4;  // one warp's 32 slots
+
+struct EpaWs {
+  uint32_t* base;  // slot's first word (lane-interleaved, stride 32)
+  __device__ __forceinline__ uint32_t& w(int i) const { return base[(size_t)i * 32]; }
+  __device__ __forceinline__ float& f(int i) const { return reinterpret_cast<float&>(base[(size_t)i * 32]); }
+  // vertices
+  __device__ __forceinline__ void set_vert(int v, const CSO& c) const {
+    int o = EPA_W_VERTS + 9 * v;
+    f(o) = c.p.x; f(o + 1) = c.p.y; f(o + 2) = c.p.z;
+    f(o + 3) = c.o1.x; f(o + 4) = c.o1.y; f(o + 5) = c.o1.z;
+    f(o + 6) = c.o2.x; f(o + 7) = c.o2.y; f(o + 8) = c.o2.z;
+  }
+  __device__ __forceinline__ V3 vp(int v) const { int o = EPA_W_VERTS + 9 * v; return v3(f(o), f(o + 1), f(o + 2)); }
+  __device__ __forceinline__ V3 vo1(int v) const { int o = EPA_W_VERTS + 9 * v + 3; return v3(f(o), f(o + 1), f(o + 2)); }
+  __device__ __forceinline__ V3 vo2(int v) const { int o = EPA_W_VERTS + 9 * v + 6; return v3(f(o), f(o + 1), f(o + 2)); }
+  // faces: word0 = pts (3 x u8) | deleted << 24; word1 = adj0 | adj1 << 16; word2 = adj2; 3-5 normal; 6-8 bcoords
+  __device__ __forceinline__ int fo(int fid) const { return EPA_W_FACES + 9 * fid; }
+  __device__ __forceinline__ int pt(int fid, int k) const { return (w(fo(fid)) >> (8 * k)) & 0xff; }
+  __device__ __forceinline__ bool deleted(int fid) const { return (w(fo(fid)) >> 24) != 0; }
+  __device__ __forceinline__ void set_deleted(int fid) const { w(fo(fid)) |= 0x01000000u; }
+  __device__ __forceinline__ int adj(int fid, int k) const {
+    return k == 0 ? (int)(w(fo(fid) + 1) & 0xffff) : (k == 1 ? (int)(w(fo(fid) + 1) >> 16) : (int)w(fo(fid) + 2));
+  }
+  __device__ __forceinline__ void set_adj(int fid, int k, int v) const {
+    if (k == 0) w(fo(fid) + 1) = (w(fo(fid) + 1) & 0xffff0000u) | (uint32_t)v;
+    else if (k == 1) w(fo(fid) + 1) = (w(fo(fid) + 1) & 0xffffu) | ((uint32_t)v << 16);
+    else w(fo(fid) + 2) = (uint32_t)v;
+  }
+  __device__ __forceinline__ V3 normal(int fid) const { int o = fo(fid) + 3; return v3(f(o), f(o + 1), f(o + 2)); }
+  __device__ __forceinline__ float bc(int fid, int k) const { return f(fo(fid) + 6 + k); }
+};
+
+struct EpaHeap {
+  const EpaWs* ws;
+  int len;
+  __device__ __forceinline__ uint32_t id(int i) const { return ws->w(EPA_W_HEAP + 2 * i); }
+  __device__ __forceinline__ float nd(int i) const { return ws->f(EPA_W_HEAP + 2 * i + 1); }
+  __device__ __forceinline__ void put(int i, uint32_t fid, float d) const { ws->w(EPA_W_HEAP + 2 * i) = fid; ws->f(EPA_W_HEAP + 2 * i + 1) = d; }
+  // FaceId::cmp: -1 / 0 / 1 (NaN -> 0)
+  static __device__ __forceinline__ int cmp(float a, float b) { return a < b ? -1 : (a > b ? 1 : 0); }
+  __device__ int sift_up(int start, int pos) {
+    uint32_t eid = id(pos);
+    float ed = nd(pos);
+    while (pos > start) {
+      int parent = (pos - 1) / 2;
+      if (cmp(ed, nd(parent)) <= 0) break;
+      put(pos, id(parent), nd(parent));
+      pos = parent;
+    }
+    put(pos, eid, ed);
+    return pos;
+  }
+  __device__ void push(uint32_t fid, float d) {
+    put(len, fid, d);
+    int old = len;
+    len += 1;
+    sift_up(0, old);
+  }
+  __device__ void sift_down_to_bottom(int pos) {
+    int end = len, start = pos;
+    uint32_t eid = id(pos);
+    float ed = nd(pos);
+    int child = 2 * pos + 1;
+    while (end >= 2 && child <= end - 2) {
+      child += (cmp(nd(child), nd(child + 1)) <= 0) ? 1 : 0;
+      put(pos, id(child), nd(child));
+      pos = child;
+      child = 2 * pos + 1;
+    }
+    if (child == end - 1) {
+      put(pos, id(child), nd(child));
+      pos = child;
+    }
+    put(pos, eid, ed);
+    sift_up(start, pos);
+  }
+  __device__ bool pop(uint32_t* fid, float* d) {
+    if (len == 0) return false;
+    len -= 1;
+    uint32_t iid = id(len);
+    float idd = nd(len);
+    if (len > 0) {
+      uint32_t rid = id(0);
+      float rd = nd(0);
+      put(0, iid, idd);
+      iid = rid;
+      idd = rd;
+      sift_down_to_bottom(0);
+    }
+    *fid = iid;
+    *d = idd;
+    return true;
+  }
+};
+
+// Face::new (epa3.rs:90-118): writes face `fid`, returns whether the origin projects inside it.
+__device__ __noinline__ bool epa_new_face(const EpaWs& ws, int fid, int p0, int p1, int p2, int a0, int a1, int a2) {
+  V3 A = ws.vp(p0), B = ws.vp(p1), C = ws.vp(p2);
+  Loc loc;
+  V3 proj = project_triangle(A, B, C, v3(0.f, 0.f, 0.f), &loc);
+  float bc[3] = {0.f, 0.f, 0.f};
+  bool inside;
+  if (loc.kind == LOC_VERTEX || loc.kind == LOC_EDGE) {
+    if (loc.kind == LOC_VERTEX) bc[loc.id] = 1.0f;
+    else {
+      int i0 = loc.id == 1 ? 1 : 0;
+      int i1 = loc.id == 0 ? 1 : 2;
+      bc[i0] = loc.bc[0];
+      bc[i1] = loc.bc[1];
+    }
+    bool is_inside = fabsf(proj.x) <= EPS && fabsf(proj.y) <= EPS && fabsf(proj.z) <= EPS;
+    float tol = EPS * 100.0f;
+    inside = is_inside || dot(proj, proj) < tol * tol;
+  } else if (loc.kind == LOC_FACE) {
+    bc[0] = loc.bc[0]; bc[1] = loc.bc[1]; bc[2] = loc.bc[2];
+    inside = true;
+  } else {
+    inside = false;
+  }
+  V3 n;
+  if (!try_normalize(cross(B - A, C - A), EPS, &n)) n = v3(0.f, 0.f, 0.f);
+  int o = ws.fo(fid);
+  ws.w(o) = (uint32_t)p0 | ((uint32_t)p1 << 8) | ((uint32_t)p2 << 16);
+  ws.w(o + 1) = (uint32_t)a0 | ((uint32_t)a1 << 16);
+  ws.w(o + 2) = (uint32_t)a2;
+  ws.f(o + 3) = n.x; ws.f(o + 4) = n.y; ws.f(o + 5) = n.z;
+  ws.f(o + 6) = bc[0]; ws.f(o + 7) = bc[1]; ws.f(o + 8) = bc[2];
+  return inside;
+}
+
+__device__ __forceinline__ void epa_face_closest_points(const EpaWs& ws, int fid, V3* p1, V3* p2) {
+  int a = ws.pt(fid, 0), b = ws.pt(fid, 1), c = ws.pt(fid, 2);
+  float b0 = ws.bc(fid, 0), b1 = ws.bc(fid, 1), b2 = ws.bc(fid, 2);
+  *p1 = (ws.vo1(a) * b0 + ws.vo1(b) * b1) + ws.vo1(c) * b2;
+  *p2 = (ws.vo2(a) * b0 + ws.vo2(b) * b1) + ws.vo2(c) * b2;
+}
+
+__device__ __forceinline__ int epa_next_ccw(const EpaWs& ws, int fid, int id) {
+  if (ws.pt(fid, 0) == id) return 1;
+  if (ws.pt(fid, 1) == id) return 2;
+  return 0;
+}
+
+__device__ __forceinline__ bool epa_can_be_seen_by(const EpaWs& ws, int fid, int point, int opp) {
+  V3 p0 = ws.vp(ws.pt(fid, opp));
+  V3 p1 = ws.vp(ws.pt(fid, (opp + 1) % 3));
+  V3 p2 = ws.vp(ws.pt(fid, (opp + 2) % 3));
+  V3 pt = ws.vp(point);
+  if (dot(pt - p0, ws.normal(fid)) >= -GJK_EPS_TOL) return true;
+  float e = EPS * 100.0f;
+  V3 c = cross(p2 - p1, pt - p1);
+  return fabsf(dot(c, c)) <= e * e;
+}
+
+enum : int { EPA_NONE = 0, EPA_OK = 1, EPA_OVERFLOW = 2 };
+
+// EPA::closest_points. `iters` counts support evaluations. Returns EPA_OK with (p1, p2, n),
+// EPA_NONE for the reference's None, EPA_OVERFLOW when a fixed capacity was exceeded.
+__device__ __noinline__ int epa_closest_points(const EpaWs& ws, const Pose& pos12, const ShapeDev& g1, const ShapeDev& g2,
+                                               const Simplex& simplex, V3* p1, V3* p2, V3* n, uint32_t* iters) {
+  const float eps_tol = EPS * 100.0f;
+  int nverts = simplex.dim + 1;
+  for (int i = 0; i < nverts; ++i) ws.set_vert(i, simplex.v[i]);
+  int nfaces = 0;
+  EpaHeap heap{&ws, 0};
+  if (simplex.dim == 0) {
+    *p1 = v3(0.f, 0.f, 0.f); *p2 = v3(0.f, 0.f, 0.f); *n = v3(0.f, 1.f, 0.f);
+    return EPA_OK;
+  } else if (simplex.dim == 3) {
+    V3 dp1 = ws.vp(1) - ws.vp(0), dp2 = ws.vp(2) - ws.vp(0), dp3 = ws.vp(3) - ws.vp(0);
+    if (dot(cross(dp1, dp2), dp3) > 0.0f) {
+      CSO t1 = simplex.v[1], t2 = simplex.v[2];
+      ws.set_vert(1, t2);
+      ws.set_vert(2, t1);
+    }
+    bool in0 = epa_new_face(ws, 0, 0, 1, 2, 3, 1, 2);
+    bool in1 = epa_new_face(ws, 1, 1, 3, 2, 3, 2, 0);
+    bool in2 = epa_new_face(ws, 2, 0, 2, 3, 0, 1, 3);
+    bool in3 = epa_new_face(ws, 3, 0, 3, 1, 2, 1, 0);
+    nfaces = 4;
+    bool ins[4] = {in0, in1, in2, in3};
+    for (int k = 0; k < 4; ++k) {
+      if (ins[k]) {
+        float dist = dot(ws.normal(k), ws.vp(k));
+        if (-dist > GJK_EPS_TOL) return EPA_NONE;
+        heap.push((uint32_t)k, -dist);
+      }
+    }
+    if (!(in0 || in1 || in2 || in3)) return EPA_NONE;
+  } else {
+    if (simplex.dim == 1) {
+      V3 v = ws.vp(1) - ws.vp(0);
+      V3 a = fabsf(v.x) > fabsf(v.y) ? v3(v.z, 0.0f, -v.x) : v3(0.0f, -v.z, v.y);
+      a = normalize(a);
+      ws.set_vert(2, cso_from_shapes(pos12, g1, g2, cross(a, v)));
+      nverts = 3;
+    }
+    epa_new_face(ws, 0, 0, 1, 2, 1, 1, 1);
+    epa_new_face(ws, 1, 0, 2, 1, 0, 0, 0);
+    nfaces = 2;
+    heap.push(0u, 0.0f);
+    heap.push(1u, 0.0f);
+  }
+  int niter = 0;
+  float max_dist = FLT_MAX;
+  uint32_t best_id = heap.id(0);
+  float old_dist = 0.0f;
+  uint32_t fid_u;
+  float neg;
+  while (heap.pop(&fid_u, &neg)) {
+    int fid = (int)fid_u;
+    if (ws.deleted(fid)) continue;
+    (*iters)++;
+    // copy of the popped face (its fields are modified below)
+    int fpts[3] = {ws.pt(fid, 0), ws.pt(fid, 1), ws.pt(fid, 2)};
+    int fadj[3] = {ws.adj(fid, 0), ws.adj(fid, 1), ws.adj(fid, 2)};
+    V3 fnormal = ws.normal(fid);
+    float fbc[3] = {ws.bc(fid, 0), ws.bc(fid, 1), ws.bc(fid, 2)};
+    if (nverts >= EPA_MAX_VERTS) return EPA_OVERFLOW;
+    CSO cso = cso_from_shapes(pos12, g1, g2, fnormal);
+    int support_id = nverts;
+    ws.set_vert(nverts++, cso);
+    float candidate = dot(cso.p, fnormal);
+    if (candidate < max_dist) { best_id = fid_u; max_dist = candidate; }
+    float curr_dist = -neg;
+    if (max_dist - curr_dist < eps_tol || (fabsf(curr_dist - old_dist) < EPS && candidate < max_dist)) {
+      epa_face_closest_points(ws, (int)best_id, p1, p2);
+      *n = ws.normal((int)best_id);
+      return EPA_OK;
+    }
+    old_dist = curr_dist;
+    ws.set_deleted(fid);
+    // silhouette: depth-first walk restated with an explicit stack (same visiting order)
+    int nsil = 0;
+    int sp = 0;
+    for (int k = 2; k >= 0; --k) {
+      int a = fadj[k];
+      int o = epa_next_ccw(ws, a, fpts[k]);
+      ws.w(EPA_W_STACK + sp++) = (uint32_t)a | ((uint32_t)o << 16);
+    }
+    while (sp > 0) {
+      uint32_t e = ws.w(EPA_W_STACK + --sp);
+      int id = (int)(e & 0xffff), opp = (int)(e >> 16);
+      if (ws.deleted(id)) continue;
+      if (!epa_can_be_seen_by(ws, id, support_id, opp)) {
+        if (nsil >= EPA_MAX_SIL) return EPA_OVERFLOW;
+        ws.w(EPA_W_SIL + nsil++) = (uint32_t)id | ((uint32_t)opp << 16);
+      } else {
+        ws.set_deleted(id);
+        int a1 = (opp + 2) % 3, a2 = opp;
+        int adj1 = ws.adj(id, a1), adj2 = ws.adj(id, a2);
+        int o1 = epa_next_ccw(ws, adj1, ws.pt(id, a1));
+        int o2 = epa_next_ccw(ws, adj2, ws.pt(id, a2));
+        if (sp + 2 > EPA_STACK) return EPA_OVERFLOW;
+        ws.w(EPA_W_STACK + sp++) = (uint32_t)adj2 | ((uint32_t)o2 << 16);
+        ws.w(EPA_W_STACK + sp++) = (uint32_t)adj1 | ((uint32_t)o1 << 16);
+      }
+    }
+    int first_new = nfaces;
+    if (nsil == 0) return EPA_NONE;
+    for (int s = 0; s < nsil; ++s) {
+      uint32_t e = ws.w(EPA_W_SIL + s);
+      int sfid = (int)(e & 0xffff), opp = (int)(e >> 16);
+      if (ws.deleted(sfid)) continue;
+      if (nfaces >= EPA_MAX_FACES || heap.len >= EPA_MAX_FACES) return EPA_OVERFLOW;
+      int new_id = nfaces;
+      int pt1 = ws.pt(sfid, (opp + 2) % 3);
+      int pt2 = ws.pt(sfid, (opp + 1) % 3);
+      bool inside = epa_new_face(ws, new_id, pt1, pt2, support_id, sfid, new_id + 1, new_id - 1);
+      ws.set_adj(sfid, (opp + 1) % 3, new_id);
+      nfaces++;
+      if (inside) {
+        float dist = dot(ws.normal(new_id), ws.vp(ws.pt(new_id, 0)));
+        if (dist < curr_dist) {
+          V3 a0 = ws.vo1(fpts[0]), a1 = ws.vo1(fpts[1]), a2 = ws.vo1(fpts[2]);
+          V3 b0 = ws.vo2(fpts[0]), b1 = ws.vo2(fpts[1]), b2 = ws.vo2(fpts[2]);
+          *p1 = (a0 * fbc[0] + a1 * fbc[1]) + a2 * fbc[2];
+          *p2 = (b0 * fbc[0] + b1 * fbc[1]) + b2 * fbc[2];
+          *n = fnormal;
+          return EPA_OK;
+        }
+        if (-dist > GJK_EPS_TOL) return EPA_NONE;
+        heap.push((uint32_t)new_id, -dist);
+      }
+    }
+    if (first_new == nfaces) return EPA_NONE;
+    ws.set_adj(first_new, 2, nfaces - 1);
+    ws.set_adj(nfaces - 1, 1, first_new);
+    niter += 1;
+    if (niter > 100) break;
+  }
+  epa_face_closest_points(ws, (int)best_id, p1, p2);
+  *n = ws.normal((int)best_id);
+  return EPA_OK;
+}
+
+}  // namespace pg

@@ -61,3 +61,82 @@ def terrain_rays(n: int, nx: int = 256, nz: int = 128, seed: int = 0x9A77E0) -> 
     r = np.sqrt(np.maximum(0.0, 1.0 - dy * dy))
     rays = np.stack([ox, oy, oz, r * np.cos(phi), dy, r * np.sin(phi)], axis=-1)
     return rays.astype(np.float32)
+
+
+def _log_uniform(seed: int, stream: int, n: int, lo: float, hi: float) -> np.ndarray:
+    return np.exp(uniform(seed, stream, n, np.log(lo), np.log(hi)))
+
+
+def _unit_quats(seed: int, stream: int, n: int) -> np.ndarray:
+    """Uniform random unit quaternions (i, j, k, w) by Shoemake's subgroup method, float64."""
+    u1 = uniform(seed, stream, n)
+    u2 = uniform(seed, stream + 1, n, 0.0, 2.0 * np.pi)
+    u3 = uniform(seed, stream + 2, n, 0.0, 2.0 * np.pi)
+    a, b = np.sqrt(1.0 - u1), np.sqrt(u1)
+    q = np.stack([a * np.sin(u2), a * np.cos(u2), b * np.sin(u3), b * np.cos(u3)], axis=-1)
+    return q / np.linalg.norm(q, axis=-1, keepdims=True)
+
+
+def _sphere_dirs(seed: int, stream: int, n: int) -> np.ndarray:
+    z = uniform(seed, stream, n, -1.0, 1.0)
+    phi = uniform(seed, stream + 1, n, 0.0, 2.0 * np.pi)
+    r = np.sqrt(np.maximum(0.0, 1.0 - z * z))
+    return np.stack([r * np.cos(phi), r * np.sin(phi), z], axis=-1)
+
+
+def ellipsoid_hulls(n_hulls: int, seed: int, stream: int, nmin: int = 8, nmax: int = 256):
+    """Vertex clouds of `n_hulls` hulls: N ~ round(log-uniform[nmin, nmax]) points uniform on the unit
+    sphere, scaled per axis by U[0.5, 2]. Points on an ellipsoid are all extreme points, so the
+    cloud is the hull's vertex set. Returns (pool (sum N, 3) f32, first (n,), count (n,))."""
+    counts = np.rint(_log_uniform(seed, stream, n_hulls, nmin, nmax)).astype(np.int64)
+    counts = np.clip(counts, nmin, nmax)
+    first = np.concatenate([[0], np.cumsum(counts)[:-1]]).astype(np.int64)
+    total = int(counts.sum())
+    dirs = _sphere_dirs(seed, stream + 1, total)
+    scale = uniform(seed, stream + 3, 3 * n_hulls, 0.5, 2.0).reshape(n_hulls, 3)
+    owner = np.repeat(np.arange(n_hulls), counts)
+    pool = (dirs * scale[owner]).astype(np.float32)
+    return pool, first.astype(np.uint32), counts.astype(np.uint32)
+
+
+def hull_pairs(n_pairs: int, seed: int = 0x9A77E2, nmin: int = 8, nmax: int = 256):
+    """Batched uneven GJK/EPA workload: pair k = (hull 2k at the identity, hull 2k+1 at a random
+    relative pose: uniform rotation, translation = unit direction x U[0.5, 3]).
+    Returns (ShapeSet, pairs (n, 2) u32)."""
+    from .shapes import ShapeSet, CONVEX
+    n = 2 * n_pairs
+    pool, first, count = ellipsoid_hulls(n, seed, 10, nmin, nmax)
+    types = np.full(n, CONVEX, np.uint32)
+    params = np.zeros((n, 4), np.float32)
+    pu = params.view(np.uint32)
+    pu[:, 0] = first
+    pu[:, 1] = count
+    poses = np.zeros((n, 7), np.float64)
+    poses[:, 3] = 1.0
+    q = _unit_quats(seed, 20, n_pairs)
+    t = _sphere_dirs(seed, 30, n_pairs) * uniform(seed, 32, n_pairs, 0.5, 3.0)[:, None]
+    poses[1::2, 0:4] = q
+    poses[1::2, 4:7] = t
+    pairs = np.stack([np.arange(0, n, 2), np.arange(1, n, 2)], axis=1).astype(np.uint32)
+    return ShapeSet.from_arrays(types, params, poses.astype(np.float32), pool), pairs
+
+
+def broadphase_shapes(n: int = 131072, extent: float = 200.0, seed: int = 0x9A77E1):
+    """Broadphase workload: n shapes, even indices balls (radius log-uniform [0.25, 4]), odd indices
+    cuboids (half extents log-uniform [0.25, 4], uniform rotation), centres U([-extent, extent)^3)."""
+    from .shapes import ShapeSet, BALL, CUBOID
+    types = np.where(np.arange(n) % 2 == 0, BALL, CUBOID).astype(np.uint32)
+    params = np.zeros((n, 4), np.float64)
+    params[:, 0] = _log_uniform(seed, 1, n, 0.25, 4.0)
+    params[:, 1] = _log_uniform(seed, 2, n, 0.25, 4.0)
+    params[:, 2] = _log_uniform(seed, 3, n, 0.25, 4.0)
+    params[types == BALL, 1:] = 0.0
+    poses = np.zeros((n, 7), np.float64)
+    poses[:, 3] = 1.0
+    q = _unit_quats(seed, 4, n)
+    cub = types == CUBOID
+    poses[cub, 0:4] = q[cub]
+    poses[:, 4] = uniform(seed, 8, n, -extent, extent)
+    poses[:, 5] = uniform(seed, 9, n, -extent, extent)
+    poses[:, 6] = uniform(seed, 10, n, -extent, extent)
+    return ShapeSet.from_arrays(types, params.astype(np.float32), poses.astype(np.float32))

@@ -1,0 +1,110 @@
+"""Parity of the CUDA query::contact path (through the C ABI) with the oracle's f32 restatement:
+has-contact decisions identical; points, normals and depth within 1e-5 (relative, with an absolute
+floor of 1e-5 for values near zero); error against the f64 oracle stated."""
+import numpy as np
+import pytest
+
+import parry_gb300 as pg
+from parry_gb300 import workloads as W
+from tests import _contact_cases as CC
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-5
+
+
+def _compare(has, out, ho, oo, what=""):
+    np.testing.assert_array_equal(has, ho, err_msg=f"has_contact differs {what}")
+    m = ho == 1
+    np.testing.assert_allclose(out[m], oo[m], rtol=TOL, atol=TOL, err_msg=what)
+
+
+def test_known_answers(gpu_ctx, oracle_lib):
+    s, pairs, c = CC.cuboid_epa()
+    has, out = pg.contacts(gpu_ctx, s, pairs, c["prediction"])
+    assert has.all()
+    for k, case in enumerate(c["cases"]):
+        assert out[k, 12] == np.float32(case["expect_dist"])
+        np.testing.assert_array_equal(out[k, 6:9], np.array(case["expect_normal1"], np.float32))
+    s, pairs, c = CC.triangle_touch()
+    has, out = pg.contacts(gpu_ctx, s, pairs, c["prediction"])
+    assert has[0] == 1 and abs(out[0, 1] - c["expect_point1_y"]) <= c["tolerance"]
+    assert abs(out[0, 0] - c["expect_point1_x"]) <= c["tolerance"]
+    s, pairs, c = CC.ball_ball()
+    for case in c["cases"]:
+        has, out = pg.contacts(gpu_ctx, s, pairs, case["prediction"])
+        assert (has[0] == 0) if case["expect"] is None else (has[0] == 1 and 0 < out[0, 12] <= case["prediction"])
+    s, pairs, c = CC.ball_cuboid()
+    has, out = pg.contacts(gpu_ctx, s, pairs, c["prediction"])
+    assert has[0] == 1 and out[0, 12] <= 0 and has[1] == 1 and out[1, 12] >= 0 and has[2] == 0
+
+
+def test_hull_pairs_vs_oracle(gpu_ctx, oracle_lib):
+    s, pairs = W.hull_pairs(50_000, seed=11)
+    has, out, st = pg.contacts(gpu_ctx, s, pairs, 0.0, want_stats=True)
+    ho, oo, sto = oracle_lib.contacts(s, pairs, 0.0)
+    _compare(has, out, ho, oo, "hull pairs")
+    assert st["gjk_iters"] == sto["gjk_iters"] and st["epa_iters"] == sto["epa_iters"]
+    h64, o64, _ = oracle_lib.contacts(s, pairs, 0.0, precision="f64")
+    m = (ho == 1) & (h64 == 1)
+    err = np.abs(out[m, 12].astype(np.float64) - o64[m, 12])
+    print(f"\ndepth abs err vs f64 oracle: max {err.max():.3e} p99 {np.quantile(err, 0.99):.3e}")
+
+
+def test_mixed_shapes_vs_oracle(gpu_ctx, oracle_lib):
+    """Balls, cuboids, capsules, hulls and triangles in every combination, with prediction."""
+    rng = np.random.default_rng(7)
+    s = pg.ShapeSet()
+    pool, first, count = W.ellipsoid_hulls(64, seed=5, stream=1, nmin=8, nmax=64)
+    n = 400
+    for i in range(n):
+        q = rng.normal(size=4)
+        q /= np.linalg.norm(q)
+        pose = pg.shapes.pose7(rng.uniform(-3, 3, 3), q)
+        t = i % 5
+        if t == 0:
+            s.add_ball(rng.uniform(0.3, 2.0), pose)
+        elif t == 1:
+            s.add_cuboid(rng.uniform(0.3, 2.0, 3), pose)
+        elif t == 2:
+            s.add_capsule(rng.uniform(0.2, 1.5), rng.uniform(0.2, 1.0), pose)
+        elif t == 3:
+            h = i % 64
+            s.add_convex(pool[first[h]:first[h] + count[h]], pose)
+        else:
+            s.add_triangle(*rng.uniform(-1.5, 1.5, (3, 3)), pose)
+    pairs = np.array([(a, b) for a in range(0, n, 3) for b in range(1, n, 7) if a != b], np.uint32)
+    for pred in (0.0, 0.25):
+        has, out = pg.contacts(gpu_ctx, s, pairs, pred)
+        ho, oo, _ = oracle_lib.contacts(s, pairs, pred)
+        _compare(has, out, ho, oo, f"mixed shapes prediction {pred}")
+        assert ho.sum() > 100
+
+
+def test_init_dir_warm_start(gpu_ctx, oracle_lib):
+    s, pairs = W.hull_pairs(20_000, seed=12)
+    rng = np.random.default_rng(1)
+    d = rng.normal(size=(len(pairs), 3)).astype(np.float32)
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    has, out = pg.contacts(gpu_ctx, s, pairs, 0.0, init_dirs=d)
+    ho, oo, _ = oracle_lib.contacts(s, pairs, 0.0, init_dirs=d)
+    _compare(has, out, ho, oo, "init_dir")
+
+
+def test_shape_aabbs(gpu_ctx, oracle_lib):
+    s = W.broadphase_shapes(20_000, seed=3)
+    for margin in (0.0, 0.05):
+        np.testing.assert_array_equal(pg.shape_aabbs(gpu_ctx, s, margin), oracle_lib.shape_aabbs(s, margin))
+
+
+def test_broadphase_pipeline(gpu_ctx, oracle_lib):
+    """Shape AABBs loosened by prediction/2 -> LBVH -> all overlapping pairs -> query::contact."""
+    s = W.broadphase_shapes(131072)
+    a = pg.shape_aabbs(gpu_ctx, s, 0.05)
+    bvh = pg.Bvh.from_leaves(gpu_ctx, a)
+    pairs = bvh.traverse_bvtt_single_tree()
+    want = oracle_lib.canonical_sorted_pairs(oracle_lib.Bvh(oracle_lib.shape_aabbs(s, 0.05)).traverse_bvtt_single_tree())
+    np.testing.assert_array_equal(pairs, want)
+    has, out = pg.contacts(gpu_ctx, s, pairs, 0.1)
+    ho, oo, _ = oracle_lib.contacts(s, pairs, 0.1)
+    _compare(has, out, ho, oo, "broadphase contacts")
+    print(f"\n{len(pairs)} candidate pairs, {int(ho.sum())} contacts")
