@@ -125,6 +125,24 @@ parrygpu_status parrygpu_trimesh_cast_rays(parrygpu_ctx* ctx, const parrygpu_tri
                                            const float* rays, uint32_t n, float max_toi, int solid, uint32_t* feature,
                                            float* toi, float* normal);
 
+/* Largest batch parrygpu_trimesh_cast_rays_noalloc accepts. */
+#define PARRYGPU_NOALLOC_MAX_RAYS 262144u
+
+/* No counterpart in the reference (parry allocates nothing on a device): the same ray cast as
+ * parrygpu_trimesh_cast_rays, for callers that may not allocate device memory while they run (an
+ * engine that owns the whole device budget, a frame loop that must never block on cudaMalloc or on
+ * cudaFree's device-wide wait). It allocates nothing: the ray-ordering scratch is a fixed array
+ * inside the library, sized for PARRYGPU_NOALLOC_MAX_RAYS rays (about 4.3 MB, held on every GPU
+ * that loads the library until exit). Larger batches are rejected with PARRYGPU_INVALID_ARG; split
+ * them. rays, feature, toi and normal must be device pointers (host buffers would need staging);
+ * pose7 may be host or device memory. The first call on a device looks up the array's device
+ * address; make that first call before any stream capture. Every call shares the one array and it
+ * keeps the last call's contents, so calls that overlap on the GPU race: keep them on one stream
+ * or synchronise between them. Results match parrygpu_trimesh_cast_rays. */
+parrygpu_status parrygpu_trimesh_cast_rays_noalloc(parrygpu_ctx* ctx, const parrygpu_trimesh* mesh, const float* pose7,
+                                                   const float* rays, uint32_t n, float max_toi, int solid, uint32_t* feature,
+                                                   float* toi, float* normal);
+
 /* ---- convex shapes and query::contact ------------------------------------------------------ */
 
 typedef enum parrygpu_shape_type {

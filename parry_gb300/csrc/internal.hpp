@@ -117,6 +117,16 @@ parrygpu_status stage_output(parrygpu_ctx* ctx, DevBuf& buf, void* dst, size_t b
 // buffer index (0/1) holding the result in ctx->sort_k / ctx->sort_v.
 parrygpu_status radix_sort_pairs(parrygpu_ctx* ctx, uint32_t n, int key_bits, int* result_buf);
 parrygpu_status radix_sort_reserve(parrygpu_ctx* ctx, uint32_t n);
+// The same sort on caller-provided device buffers (no allocation); hist needs
+// radix_sort_hist_entries(n) words.
+parrygpu_status radix_sort_pairs_in(parrygpu_ctx* ctx, uint32_t n, int key_bits, uint32_t* k0, uint32_t* v0, uint32_t* k1,
+                                    uint32_t* v1, uint32_t* hist, int* result_buf);
+uint32_t radix_sort_hist_entries(uint32_t n);
+
+// ---- ray casts (ray.cu): launch helpers on caller-provided device buffers (no allocation) ----
+parrygpu_status launch_ray_keys(parrygpu_ctx* ctx, const float* d_rays, uint32_t n, uint32_t* bounds, uint32_t* keys, uint32_t* vals);
+parrygpu_status launch_trimesh_rays(parrygpu_ctx* ctx, const parrygpu_trimesh* mesh, const float* pose7_host, const float* d_rays,
+                                    const uint32_t* order, uint32_t n, float max_toi, uint32_t* d_feat, float* d_toi, float* d_nrm);
 
 // ---- LBVH (lbvh.cu) ----
 // Builds `bvh` from `n` device AABBs (n x 6 floats). When leaf_data_is_position, leaf nodes store

@@ -427,3 +427,34 @@ parrygpu_status parrygpu_trimesh_cast_rays(parrygpu_ctx* ctx, const parrygpu_tri
 }
 
 }  // extern "C"
+
+// Launches the ray-ordering keys (origin bounds into `bounds`, 6 words, then Morton keys) on
+// caller-provided device buffers. Allocates nothing.
+parrygpu_status launch_ray_keys(parrygpu_ctx* ctx, const float* d_rays, uint32_t n, uint32_t* bounds, uint32_t* keys, uint32_t* vals) {
+  PG_CUDA(ctx, cudaMemsetAsync(bounds, 0xff, 12, ctx->stream));
+  PG_CUDA(ctx, cudaMemsetAsync(bounds + 3, 0x00, 12, ctx->stream));
+  k_ray_bounds<<<div_up(n, 256 * 8), 256, 0, ctx->stream>>>(d_rays, n, bounds);
+  PG_LAUNCHED(ctx);
+  k_ray_keys<<<div_up(n, 256), 256, 0, ctx->stream>>>(d_rays, n, bounds, keys, vals, ctx->cfg.ray_sort_key);
+  PG_LAUNCHED(ctx);
+  return PARRYGPU_OK;
+}
+
+// Launches the traversal kernel on device buffers (order may be NULL). Allocates nothing.
+parrygpu_status launch_trimesh_rays(parrygpu_ctx* ctx, const parrygpu_trimesh* mesh, const float* pose7_host, const float* d_rays,
+                                    const uint32_t* order, uint32_t n, float max_toi, uint32_t* d_feat, float* d_toi, float* d_nrm) {
+  Pose pose{0.f, 0.f, 0.f, 1.f, v3(0.f, 0.f, 0.f)};
+  bool has_pose = pose7_host != nullptr;
+  if (has_pose) pose = Pose{pose7_host[0], pose7_host[1], pose7_host[2], pose7_host[3], v3(pose7_host[4], pose7_host[5], pose7_host[6])};
+  uint32_t bs = ctx->cfg.ray_block ? ctx->cfg.ray_block : 128;
+  const WideNode* w = mesh->bvh.wide.as<WideNode>();
+  const float4* soup = mesh->soup.as<float4>();
+#define PG_RAY_LAUNCH2(P, N)                                                                                                   \
+  k_trimesh_rays<P, N><<<div_up(n, bs), bs, 0, ctx->stream>>>(w, soup, mesh->n_triangles, d_rays, order, n, max_toi, pose, d_feat, \
+                                                              d_toi, d_nrm, ctx->d_err)
+  if (has_pose) { if (d_nrm) PG_RAY_LAUNCH2(true, true); else PG_RAY_LAUNCH2(true, false); }
+  else { if (d_nrm) PG_RAY_LAUNCH2(false, true); else PG_RAY_LAUNCH2(false, false); }
+#undef PG_RAY_LAUNCH2
+  PG_LAUNCHED(ctx);
+  return PARRYGPU_OK;
+}

@@ -163,3 +163,28 @@ parrygpu_status radix_sort_pairs(parrygpu_ctx* ctx, uint32_t n, int key_bits, in
   *result_buf = cur;
   return PARRYGPU_OK;
 }
+
+// Same sort on caller-provided buffers (k0/v0 hold the input; k1/v1 and hist are scratch of at least
+// n and 256 * ceil(n / 2048) entries). Allocates nothing.
+parrygpu_status radix_sort_pairs_in(parrygpu_ctx* ctx, uint32_t n, int key_bits, uint32_t* k0, uint32_t* v0, uint32_t* k1,
+                                    uint32_t* v1, uint32_t* hist, int* result_buf) {
+  *result_buf = 0;
+  if (n <= 1) return PARRYGPU_OK;
+  uint32_t tiles = div_up(n, RS_TILE);
+  uint32_t* ks[2] = {k0, k1};
+  uint32_t* vs[2] = {v0, v1};
+  int cur = 0;
+  for (int shift = 0; shift < key_bits; shift += 8) {
+    k_rs_hist<<<tiles, RS_THREADS, 0, ctx->stream>>>(ks[cur], n, shift, hist, tiles);
+    PG_LAUNCHED(ctx);
+    k_rs_scan<<<1, SCAN_THREADS, 0, ctx->stream>>>(hist, tiles * RS_BINS);
+    PG_LAUNCHED(ctx);
+    k_rs_scatter<<<tiles, RS_THREADS, 0, ctx->stream>>>(ks[cur], vs[cur], ks[cur ^ 1], vs[cur ^ 1], n, shift, hist, tiles);
+    PG_LAUNCHED(ctx);
+    cur ^= 1;
+  }
+  *result_buf = cur;
+  return PARRYGPU_OK;
+}
+
+uint32_t radix_sort_hist_entries(uint32_t n) { return div_up(n ? n : 1, RS_TILE) * RS_BINS; }
