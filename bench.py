@@ -142,6 +142,98 @@ def cpu_oracle_rays(v, i, rays, reps: int):
     return len(rays) / statistics.median(times) / 1e6, stats, threads
 
 
+def contacts_section(ctx, stream, steps: int, warmup: int, n_pairs: int, flush) -> dict:
+    """Batched query::contact on uneven convex-hull pairs (8-256 vertices, log-uniform), the
+    GJK/EPA workload: device-resident pairs/s, end-to-end pairs/s through host buffers, kernel
+    split, FP32 roofline from the oracle's support-scan count, and the oracle CPU baseline."""
+    import numpy as np
+    import torch
+    import parry_gb300 as pg
+    from parry_gb300 import workloads as W
+    from oracle import build as ob
+    ob.build()
+    from oracle import oracle as O
+
+    s, pairs = W.hull_pairs(n_pairs)
+    t, prm, pos, pool = s.arrays()
+    dev = tuple(torch.from_numpy(np.ascontiguousarray(a)).cuda() for a in (t.view(np.int32), prm, pos, pool))
+    dpairs = torch.from_numpy(pairs.view(np.int32)).cuda()
+    has = torch.empty(n_pairs, dtype=torch.uint8, device="cuda")
+    res = torch.empty((n_pairs, 13), dtype=torch.float32, device="cuda")
+    for _ in range(max(1, warmup)):
+        pg.contacts(ctx, dev, dpairs, 0.0, out=(has, res))
+    torch.cuda.synchronize()
+    ctx.enable_kernel_timing(True)
+    ctx.reset_kernel_timing()
+    st_ev = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    en_ev = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    l0 = ctx.kernel_launches
+    for k in range(steps):
+        flush.zero_()
+        st_ev[k].record(stream)
+        pg.contacts(ctx, dev, dpairs, 0.0, out=(has, res))
+        en_ev[k].record(stream)
+    torch.cuda.synchronize()
+    ms = sum(a.elapsed_time(b) for a, b in zip(st_ev, en_ev)) / steps
+    g_ms, g_n = ctx.kernel_time("contacts_gjk")
+    e_ms, e_n = ctx.kernel_time("contacts_epa")
+    ctx.enable_kernel_timing(False)
+    launches = ctx.kernel_launches - l0
+    _, _, gst = pg.contacts(ctx, dev, dpairs, 0.0, out=(has, res), want_stats=True)
+    # end to end from pinned host buffers
+    host = tuple(torch.from_numpy(np.ascontiguousarray(a)).pin_memory() for a in (t.view(np.int32), prm, pos, pool))
+    hpairs = torch.from_numpy(pairs.view(np.int32)).pin_memory()
+    hhas = torch.empty(n_pairs, dtype=torch.uint8, pin_memory=True)
+    hres = torch.empty((n_pairs, 13), dtype=torch.float32, pin_memory=True)
+    pg.contacts(ctx, host, hpairs, 0.0, out=(hhas, hres))
+    e2e = []
+    for _ in range(steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        pg.contacts(ctx, host, hpairs, 0.0, out=(hhas, hres))
+        e2e.append((time.perf_counter() - t0) * 1e3)
+    e2e_ms = statistics.mean(e2e)
+    h2d = sum(a.numel() * a.element_size() for a in host) + hpairs.numel() * 4
+    d2h = n_pairs * (13 * 4 + 1)
+    # oracle on a bounded sample: CPU baseline and the support-scan count of the flop model
+    sample = min(n_pairs, 131072)
+    threads = os.cpu_count() or 1
+    O.contacts(s, pairs[:2048], 0.0, threads=threads)
+    t0 = time.perf_counter()
+    oh, oo, ost = O.contacts(s, pairs[:sample], 0.0, threads=threads)
+    cpu_s = time.perf_counter() - t0
+    same = bool(np.array_equal(oh, has[:sample].cpu().numpy()))
+    flops_per_pair = 5.0 * ost["support_vertices"] / sample
+    kernel_ms = g_ms / max(g_n, 1) + e_ms / max(e_n, 1)
+    sm_mhz = 2070.0
+    try:
+        sm_mhz = float(json.loads((ROOT / "MEASURED_PEAKS.json").read_text())["sm_max_mhz"])
+    except Exception:
+        pass
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    fp32_peak = sms * 128 * 2 * sm_mhz * 1e6 / 1e12
+    achieved = flops_per_pair * n_pairs / (kernel_ms / 1e3) / 1e12
+    return {
+        "workload": "convex hull pairs, 8-256 vertices log-uniform on ellipsoids, random relative pose, prediction 0",
+        "pairs": n_pairs, "metric": "contact pairs/s", "value": round(n_pairs / (ms / 1e3), 1), "unit": "pairs/s",
+        "ms_per_step": round(ms, 4), "kernel_ms": {"gjk": round(g_ms / max(g_n, 1), 4), "epa": round(e_ms / max(e_n, 1), 4)},
+        "gpu_launches": launches,
+        "e2e": {"value": round(n_pairs / (e2e_ms / 1e3), 1), "unit": "pairs/s", "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h), "ms_per_step": round(e2e_ms, 3)},
+        "mean_iterations": {"gjk": round(gst["gjk_iters"] / n_pairs, 4), "epa": round(gst["epa_iters"] / n_pairs, 4),
+                            "epa_calls": gst["epa_calls"]},
+        "contact_fraction": round(float(has.float().mean().item()), 4),
+        "roofline": {"bound": "fp32", "achieved": round(achieved, 4), "peak": round(fp32_peak, 1), "unit": "TFLOP/s",
+                     "frac": round(achieved / fp32_peak, 6), "peak_source": "nominal: SMs x 128 lanes x 2 (FMA) x max SM clock",
+                     "flops_per_pair": round(flops_per_pair, 1),
+                     "flops_model": "5 flops per vertex dot x vertices scanned by the f32 oracle's support calls on a sample"},
+        "cpu_baseline": {"value": round(sample / cpu_s, 1), "unit": "pairs/s", "cores": threads, "kind": "port",
+                         "sample": f"first {sample} pairs; C++ restatement of parry3d f32 query::contact"},
+        "matches_oracle_on_sample": same,
+    }
+
+
 def run_reference(args) -> int:
     world, rank, local = dist_info()
     if rank != 0:
@@ -266,6 +358,9 @@ def run_gb300(args) -> int:
         e2e = float(t.item())
     e2e_value = world * n / (e2e / 1e3) / 1e6
     same = bool(np.array_equal(feat_p.numpy(), feat.cpu().numpy()))
+    contacts = None
+    if args.contact_pairs > 0:
+        contacts = contacts_section(ctx, stream, args.steps, args.warmup, args.contact_pairs, flush)
 
     if rank == 0:
         cpu_value, stats, threads = cpu_oracle_rays(v, i, rays_h, reps=3)
@@ -294,6 +389,7 @@ def run_gb300(args) -> int:
                              "sample": f"the full workload ({n} rays), median of 3; C++ restatement of parry3d f32"},
             "gpu_launches": launches,
             "clocks": clocks,
+            "contacts": contacts,
         }
         print(json.dumps(line), flush=True)
     ctx.close()
@@ -309,6 +405,8 @@ def main() -> int:
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--n-rays", type=int, default=N_RAYS)
+    ap.add_argument("--contact-pairs", type=int, default=1 << 20,
+                    help="hull pairs of the GJK/EPA section (0 skips it)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

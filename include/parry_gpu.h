@@ -44,6 +44,7 @@ typedef enum parrygpu_status {
 typedef struct parrygpu_ctx parrygpu_ctx;
 typedef struct parrygpu_bvh parrygpu_bvh;
 typedef struct parrygpu_trimesh parrygpu_trimesh;
+typedef struct parrygpu_compound parrygpu_compound;
 
 typedef struct parrygpu_config {
   int device;              /* CUDA device ordinal */
@@ -193,6 +194,21 @@ parrygpu_status parrygpu_shapes_aabbs(parrygpu_ctx* ctx, const parrygpu_shapes* 
 parrygpu_status parrygpu_contacts(parrygpu_ctx* ctx, const parrygpu_shapes* shapes, const uint32_t* pairs, uint64_t n_pairs,
                                   float prediction, const float* init_dirs, parrygpu_contact* out, uint8_t* has_contact,
                                   parrygpu_gjk_stats* stats);
+
+/* ---- Compound (shape set) ray casts ------------------------------------------------------- */
+
+/* Replaces Compound::new(shapes) (src/shape/compound.rs:113-144): copies the parts (with their poses)
+ * to the device and builds an LBVH over their world AABBs. Leaf data = part index. */
+parrygpu_status parrygpu_compound_create(parrygpu_ctx* ctx, const parrygpu_shapes* shapes, parrygpu_compound** out);
+void parrygpu_compound_destroy(parrygpu_compound* compound);
+/* Moves the parts (n x 7 poses) and refits the compound's BVH (topology kept). */
+parrygpu_status parrygpu_compound_set_poses(parrygpu_ctx* ctx, parrygpu_compound* compound, const float* poses);
+/* Replaces a loop of RayCast::cast_ray_and_get_normal(m, ray, max_toi, solid) on a Compound
+ * (src/query/ray/ray.rs:393-403 -> src/query/ray/ray_composite_shape.rs:95-104). pose7 = the
+ * compound's pose (NULL = identity). Outputs per ray: part index (UINT32_MAX on a miss), toi and
+ * world-space normal (normal may be NULL). Exact toi ties resolve to the lowest part index. */
+parrygpu_status parrygpu_compound_cast_rays(parrygpu_ctx* ctx, const parrygpu_compound* compound, const float* pose7, const float* rays,
+                                            uint32_t n, float max_toi, int solid, uint32_t* part, float* toi, float* normal);
 
 #ifdef __cplusplus
 }

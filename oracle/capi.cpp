@@ -6,6 +6,7 @@
 // are the f32 inputs widened, so the f64 result measures the f32 path's rounding error.
 #include "ray.hpp"
 #include "contact.hpp"
+#include "shape_ray.hpp"
 #include <thread>
 #include <vector>
 #include <algorithm>
@@ -117,7 +118,7 @@ void contacts(const uint32_t* types, const float* params, const float* poses, co
               const uint32_t* pairs, uint64_t npairs, float prediction, const float* init_dirs, int threads, O* out, uint8_t* has,
               uint64_t* stats) {
   ShapeSet<R> set(types, params, poses, hullv, nhv, nshapes);
-  std::atomic<uint64_t> gi{0}, ei{0}, ec{0}, mf{0}, mv{0}, ms{0};
+  std::atomic<uint64_t> gi{0}, ei{0}, ec{0}, mf{0}, mv{0}, ms{0}, sv{0};
   auto amax = [](std::atomic<uint64_t>& a, uint64_t v) {
     uint64_t cur = a.load();
     while (v > cur && !a.compare_exchange_weak(cur, v)) {}
@@ -132,7 +133,9 @@ void contacts(const uint32_t* types, const float* params, const float* poses, co
       idir = Vec3<R>(R(init_dirs[3 * k]), R(init_dirs[3 * k + 1]), R(init_dirs[3 * k + 2]));
       ip = &idir;
     }
+    g_support_vertices = 0;
     bool ok = contact_world(set.poses[a], set.shapes[a], set.poses[b], set.shapes[b], R(prediction), &c, &st, ip);
+    sv += g_support_vertices;
     gi += st.gjk_iters; ei += st.epa_iters; ec += st.epa_calls;
     amax(mf, st.epa_max_faces); amax(mv, st.epa_max_verts); amax(ms, st.epa_max_sil);
     has[k] = ok ? 1 : 0;
@@ -147,8 +150,45 @@ void contacts(const uint32_t* types, const float* params, const float* poses, co
   });
   if (stats) {
     stats[0] = gi.load(); stats[1] = ei.load(); stats[2] = ec.load();
-    stats[3] = mf.load(); stats[4] = mv.load(); stats[5] = ms.load();
+    stats[3] = mf.load(); stats[4] = mv.load(); stats[5] = ms.load(); stats[6] = sv.load();
   }
+}
+
+template <class R> Compound<R>* make_compound(const uint32_t* types, const float* params, const float* poses, const float* hullv,
+                                              uint32_t nhv, uint64_t n) {
+  Compound<R>* c = new Compound<R>();
+  ShapeSet<R> set(types, params, poses, hullv, nhv, n);
+  c->shapes = set.shapes;
+  c->poses = set.poses;
+  c->pool = std::move(set.pool);  // the buffer moves with the vector: shape pointers stay valid
+  c->build();
+  return c;
+}
+
+template <class R, class O>
+void compound_cast(const Compound<R>* c, const float* pose7, const float* rays, uint64_t n, float max_toi, int solid, int lowest,
+                   int threads, uint32_t* part, O* toi, O* normal, uint64_t* stats) {
+  Iso<R> iso = pose7 ? Iso<R>::from_pose7(pose7) : Iso<R>::identity();
+  std::atomic<uint64_t> wide{0}, leaves{0};
+  parallel_for(n, threads, [&](uint64_t i) {
+    Ray<R> r;
+    r.origin = Vec3<R>(R(rays[6 * i]), R(rays[6 * i + 1]), R(rays[6 * i + 2]));
+    r.dir = Vec3<R>(R(rays[6 * i + 3]), R(rays[6 * i + 4]), R(rays[6 * i + 5]));
+    if (pose7) r = Ray<R>{iso.inverse_transform_point(r.origin), iso.inverse_transform_vector(r.dir)};
+    uint32_t p;
+    R t;
+    Vec3<R> nn;
+    VisitStats st;
+    bool ok = c->cast_local_ray_and_get_normal(r, R(max_toi), solid != 0, lowest != 0, &p, &t, &nn, stats ? &st : nullptr);
+    if (stats) { wide += st.wide_visits; leaves += st.leaf_tests; }
+    if (ok && pose7) nn = iso.transform_vector(nn);
+    part[i] = ok ? p : UINT32_MAX;
+    toi[i] = ok ? O(t) : O(0);
+    normal[3 * i] = ok ? O(nn.x) : O(0);
+    normal[3 * i + 1] = ok ? O(nn.y) : O(0);
+    normal[3 * i + 2] = ok ? O(nn.z) : O(0);
+  });
+  if (stats) { stats[0] = wide.load(); stats[1] = leaves.load(); }
 }
 
 }  // namespace
@@ -225,6 +265,24 @@ void oracle_contacts_f64(const uint32_t* types, const float* params, const float
                          uint64_t nshapes, const uint32_t* pairs, uint64_t npairs, float prediction, const float* init_dirs,
                          int threads, double* out, uint8_t* has, uint64_t* stats) {
   contacts<double, double>(types, params, poses, hullv, nhv, nshapes, pairs, npairs, prediction, init_dirs, threads, out, has, stats);
+}
+
+// ---------------- Compound (shape set) ray casts ----------------
+void* oracle_compound_new_f32(const uint32_t* t, const float* p, const float* q, const float* v, uint32_t nv, uint64_t n) {
+  return make_compound<float>(t, p, q, v, nv, n);
+}
+void* oracle_compound_new_f64(const uint32_t* t, const float* p, const float* q, const float* v, uint32_t nv, uint64_t n) {
+  return make_compound<double>(t, p, q, v, nv, n);
+}
+void oracle_compound_free_f32(void* c) { delete (Compound<float>*)c; }
+void oracle_compound_free_f64(void* c) { delete (Compound<double>*)c; }
+void oracle_compound_cast_rays_f32(void* c, const float* pose7, const float* rays, uint64_t n, float max_toi, int solid, int lowest,
+                                   int threads, uint32_t* part, float* toi, float* normal, uint64_t* stats) {
+  compound_cast<float, float>((Compound<float>*)c, pose7, rays, n, max_toi, solid, lowest, threads, part, toi, normal, stats);
+}
+void oracle_compound_cast_rays_f64(void* c, const float* pose7, const float* rays, uint64_t n, float max_toi, int solid, int lowest,
+                                   int threads, uint32_t* part, double* toi, double* normal, uint64_t* stats) {
+  compound_cast<double, double>((Compound<double>*)c, pose7, rays, n, max_toi, solid, lowest, threads, part, toi, normal, stats);
 }
 
 uint64_t oracle_pairs_count(void* p) { return ((PairBuf*)p)->v.size() / 2; }

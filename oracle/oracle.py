@@ -38,6 +38,12 @@ _SIGS = {
     "oracle_shape_aabbs_f32": (None, [P, P, P, P, U32, U64, F32, P]),
     "oracle_contacts_f32": (None, [P, P, P, P, U32, U64, P, U64, F32, P, I32, P, P, P]),
     "oracle_contacts_f64": (None, [P, P, P, P, U32, U64, P, U64, F32, P, I32, P, P, P]),
+    "oracle_compound_new_f32": (P, [P, P, P, P, U32, U64]),
+    "oracle_compound_new_f64": (P, [P, P, P, P, U32, U64]),
+    "oracle_compound_free_f32": (None, [P]),
+    "oracle_compound_free_f64": (None, [P]),
+    "oracle_compound_cast_rays_f32": (None, [P, P, P, U64, F32, I32, I32, I32, P, P, P, P]),
+    "oracle_compound_cast_rays_f64": (None, [P, P, P, U64, F32, I32, I32, I32, P, P, P, P]),
     "oracle_pairs_count": (U64, [P]),
     "oracle_pairs_copy": (None, [P, P]),
     "oracle_pairs_free": (None, [P]),
@@ -191,10 +197,45 @@ def contacts(shapes, pairs: np.ndarray, prediction: float, init_dirs: np.ndarray
     dt = np.float32 if precision == "f32" else np.float64
     out = np.empty((k, 13), dt)
     has = np.empty(k, np.uint8)
-    st = np.zeros(6, np.uint64)
+    st = np.zeros(7, np.uint64)
     idir = None if init_dirs is None else np.ascontiguousarray(init_dirs, np.float32).reshape(-1, 3)
     getattr(lib(), f"oracle_contacts_{precision}")(_p(t), _p(prm), _p(pos), _p(pool), len(pool), len(t), _p(pairs), k,
                                                    float(prediction), _p(idir), threads if threads is not None else default_threads(),
                                                    _p(out), _p(has), _p(st))
     return has, out, {"gjk_iters": int(st[0]), "epa_iters": int(st[1]), "epa_calls": int(st[2]),
-                      "epa_max_faces": int(st[3]), "epa_max_verts": int(st[4]), "epa_max_silhouette": int(st[5])}
+                      "epa_max_faces": int(st[3]), "epa_max_verts": int(st[4]), "epa_max_silhouette": int(st[5]),
+                      "support_vertices": int(st[6])}
+
+
+class Compound:
+    """Reference Compound (shape set): binned BVH over part AABBs, RayCast with part poses."""
+
+    def __init__(self, shapes, precision: str = "f32"):
+        self.arr = _shape_arrays(shapes)
+        t, prm, pos, pool = self.arr
+        self.prec = precision
+        self._h = getattr(lib(), f"oracle_compound_new_{precision}")(_p(t), _p(prm), _p(pos), _p(pool), len(pool), len(t))
+
+    def cast_rays_and_get_normal(self, rays: np.ndarray, max_toi: float, solid: bool = True, pose=None, lowest_index: bool = True,
+                                 threads: int | None = None, want_stats: bool = False):
+        rays = np.ascontiguousarray(rays, dtype=np.float32)
+        n = rays.shape[0]
+        dt = np.float32 if self.prec == "f32" else np.float64
+        part = np.empty(n, np.uint32)
+        toi = np.empty(n, dt)
+        nrm = np.empty((n, 3), dt)
+        st = np.zeros(2, np.uint64)
+        pz = None if pose is None else np.ascontiguousarray(pose, np.float32)
+        getattr(lib(), f"oracle_compound_cast_rays_{self.prec}")(self._h, _p(pz), _p(rays), n, float(max_toi), 1 if solid else 0,
+                                                                 1 if lowest_index else 0,
+                                                                 threads if threads is not None else default_threads(),
+                                                                 _p(part), _p(toi), _p(nrm), _p(st) if want_stats else None)
+        if want_stats:
+            return part, toi, nrm, {"wide_visits": int(st[0]), "leaf_tests": int(st[1])}
+        return part, toi, nrm
+
+    def __del__(self):
+        try:
+            getattr(lib(), f"oracle_compound_free_{self.prec}")(self._h)
+        except Exception:
+            pass

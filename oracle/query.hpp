@@ -91,10 +91,16 @@ template <class R> struct CSOPoint {
 };
 
 // Support provider: either a shape or the constant origin (for point projections).
+// Counts the vertices scanned by support calls (the dominant FP32 work: 5 flops per vertex dot).
+inline thread_local uint64_t g_support_vertices = 0;
+
 template <class R> struct Support {
   const Shape<R>* shape;  // nullptr = ConstantOrigin
-  Vec3<R> local(const Vec3<R>& d) const { return shape ? shape->local_support(d) : Vec3<R>(); }
-  Vec3<R> world(const Iso<R>& m, const Vec3<R>& d) const { return shape ? shape->support(m, d) : m.tra; }
+  static void count(const Shape<R>* s) {
+    if (s && (s->type == SHAPE_CONVEX || s->type == SHAPE_TRIANGLE)) g_support_vertices += s->npts;
+  }
+  Vec3<R> local(const Vec3<R>& d) const { count(shape); return shape ? shape->local_support(d) : Vec3<R>(); }
+  Vec3<R> world(const Iso<R>& m, const Vec3<R>& d) const { count(shape); return shape ? shape->support(m, d) : m.tra; }
 };
 
 template <class R>

@@ -14,6 +14,8 @@ one batched call here:
     TriMesh::cast_ray(m, ray, t, solid)                TriMesh.cast_rays(rays, t, solid, pose)
     Shape::compute_aabb(pos).loosened(m)               shape_aabbs(ctx, shapes, margin)
     query::contact(pos1, g1, pos2, g2, prediction)     contacts(ctx, shapes, pairs, prediction, init_dirs)
+    Compound::new(shapes)                              Compound(ctx, shapes)
+    Compound::cast_ray_and_get_normal(m, ray, t, s)    Compound.cast_rays_and_get_normal(rays, t, solid, pose)
 
 Arrays may be numpy arrays (host memory, staged by the library) or torch tensors (CUDA tensors are
 used in place; outputs are then allocated on the same device). Every call goes through the C ABI
@@ -28,7 +30,7 @@ import numpy as np
 from . import _capi
 from ._capi import ParryGpuError, lib, check
 
-__all__ = ["Context", "Bvh", "TriMesh", "ShapeSet", "shape_aabbs", "contacts", "ParryGpuError", "NO_HIT", "lib"]
+__all__ = ["Context", "Bvh", "TriMesh", "Compound", "ShapeSet", "shape_aabbs", "contacts", "ParryGpuError", "NO_HIT", "lib"]
 
 from .shapes import ShapeSet  # noqa: E402
 
@@ -305,3 +307,47 @@ def contacts(ctx: Context, shapes, pairs, prediction: float, init_dirs=None, wan
     if want_stats:
         return has, res, {"gjk_iters": stats.gjk_iterations, "epa_iters": stats.epa_iterations, "epa_calls": stats.epa_calls}
     return has, res
+
+
+class Compound:
+    """shape::Compound on the GPU: parts with poses under one LBVH, for batched ray casts."""
+
+    def __init__(self, ctx: Context, shapes):
+        self.ctx = ctx
+        st = _StagedShapes(shapes)
+        self.n = st.n
+        h = C.c_void_p()
+        check(lib().parrygpu_compound_create(ctx.handle, C.byref(st.struct), C.byref(h)), ctx.handle)
+        self._h = h
+
+    def set_poses(self, poses) -> None:
+        """Moves the parts ((n, 7) poses) and refits the BVH."""
+        kp, pp = _as_input(poses, np.float32)
+        check(lib().parrygpu_compound_set_poses(self.ctx.handle, self._h, pp), self.ctx.handle)
+
+    def cast_rays_and_get_normal(self, rays, max_toi: float, solid: bool = True, pose=None, out=None):
+        """Batched Compound::cast_ray_and_get_normal: (part, toi, normal); part = NO_HIT on a miss."""
+        kr, pr = _as_input(rays, np.float32)
+        n = int(kr.shape[0])
+        kq, pq = _as_input(pose, np.float32) if pose is not None else (None, None)
+        if out is None:
+            part, pp = _alloc_like(kr, (n,), np.uint32)
+            toi, pt = _alloc_like(kr, (n,), np.float32)
+            nrm, pn = _alloc_like(kr, (n, 3), np.float32)
+        else:
+            part, toi, nrm = out
+            pp, pt, pn = C.c_void_p(_dptr(part)), C.c_void_p(_dptr(toi)), C.c_void_p(_dptr(nrm)) if nrm is not None else None
+        check(lib().parrygpu_compound_cast_rays(self.ctx.handle, self._h, pq, pr, n, float(max_toi), 1 if solid else 0, pp, pt, pn),
+              self.ctx.handle)
+        return part, toi, nrm
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            lib().parrygpu_compound_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

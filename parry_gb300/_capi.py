@@ -56,6 +56,10 @@ SIGNATURES: dict[str, tuple] = {
     "parrygpu_trimesh_cast_rays_noalloc": (I32, [P, P, P, P, U32, F32, I32, P, P, P]),
     "parrygpu_shapes_aabbs": (I32, [P, P, F32, P]),
     "parrygpu_contacts": (I32, [P, P, P, U64, F32, P, P, P, P]),
+    "parrygpu_compound_create": (I32, [P, P, C.POINTER(P)]),
+    "parrygpu_compound_destroy": (None, [P]),
+    "parrygpu_compound_set_poses": (I32, [P, P, P]),
+    "parrygpu_compound_cast_rays": (I32, [P, P, P, P, U32, F32, I32, P, P, P]),
 }
 
 

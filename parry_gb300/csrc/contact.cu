@@ -444,6 +444,13 @@ static parrygpu_status stage_shapes(parrygpu_ctx* ctx, const parrygpu_shapes* s,
   return PARRYGPU_OK;
 }
 
+parrygpu_status compound_part_aabbs(parrygpu_ctx* ctx, const parrygpu_compound* c, float* d_out) {
+  ShapeArrays sh{c->types.as<uint32_t>(), c->params.as<float4>(), c->poses.as<float>(), c->pool.as<float>(), c->n, c->n_vertices};
+  k_shape_aabbs<<<div_up(c->n, 256), 256, 0, ctx->stream>>>(sh, c->n, 0.0f, d_out, ctx->d_err);
+  PG_LAUNCHED(ctx);
+  return PARRYGPU_OK;
+}
+
 extern "C" {
 
 parrygpu_status parrygpu_shapes_aabbs(parrygpu_ctx* ctx, const parrygpu_shapes* shapes, float margin, float* aabbs) {
@@ -488,7 +495,7 @@ parrygpu_status parrygpu_contacts(parrygpu_ctx* ctx, const parrygpu_shapes* shap
   if ((s = stage_output(ctx, ctx->stage_out[1], has_contact, (size_t)n_pairs, &d_has, &c_has)) != PARRYGPU_OK) return s;
   PG_CUDA(ctx, ctx->ct_queue.reserve((size_t)n_pairs * QUEUE_WORDS * 4));
   PG_CUDA(ctx, ctx->ct_counters.reserve(64));
-  uint32_t epa_blocks = (uint32_t)(ctx->sm_count > 0 ? ctx->sm_count : 152) * 4;
+  uint32_t epa_blocks = (uint32_t)(ctx->sm_count > 0 ? ctx->sm_count : 152) * 8;
   uint32_t slots = epa_blocks * EPA_THREADS;
   PG_CUDA(ctx, ctx->epa_ws.reserve((size_t)(slots / 32) * EPA_SLOT_GROUP_BYTES));
   unsigned long long* ctr = ctx->ct_counters.as<unsigned long long>();  // [0] queue count, [1..3] stats

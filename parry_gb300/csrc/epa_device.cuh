@@ -119,7 +119,7 @@ struct EpaHeap {
 };
 
 // Face::new (epa3.rs:90-118): writes face `fid`, returns whether the origin projects inside it.
-__device__ __noinline__ bool epa_new_face(const EpaWs& ws, int fid, int p0, int p1, int p2, int a0, int a1, int a2) {
+static __device__ __noinline__ bool epa_new_face(const EpaWs& ws, int fid, int p0, int p1, int p2, int a0, int a1, int a2) {
   V3 A = ws.vp(p0), B = ws.vp(p1), C = ws.vp(p2);
   Loc loc;
   V3 proj = project_triangle(A, B, C, v3(0.f, 0.f, 0.f), &loc);
@@ -181,7 +181,7 @@ enum : int { EPA_NONE = 0, EPA_OK = 1, EPA_OVERFLOW = 2 };
 
 // EPA::closest_points. `iters` counts support evaluations. Returns EPA_OK with (p1, p2, n),
 // EPA_NONE for the reference's None, EPA_OVERFLOW when a fixed capacity was exceeded.
-__device__ __noinline__ int epa_closest_points(const EpaWs& ws, const Pose& pos12, const ShapeDev& g1, const ShapeDev& g2,
+static __device__ __noinline__ int epa_closest_points(const EpaWs& ws, const Pose& pos12, const ShapeDev& g1, const ShapeDev& g2,
                                                const Simplex& simplex, V3* p1, V3* p2, V3* n, uint32_t* iters) {
   const float eps_tol = EPS * 100.0f;
   int nverts = simplex.dim + 1;

@@ -102,11 +102,32 @@ __device__ __forceinline__ V3 local_support(const ShapeDev& s, V3 dir) {
       return d2 > d3 ? p1 : p2;
     }
     case SH_CONVEX: {
-      uint32_t best = 0;
-      float bd = dot(ldv(s.pts), dir);
-      for (uint32_t i = 1; i < s.npts; ++i) {
+      // First index of the maximum dot product (point_cloud_support_point: best = 0, then strict
+      // `>`). Four interleaved partial scans over indices >= 1, each seeded with vertex 0, keep four
+      // independent load/compare chains in flight; each keeps the first index of its own maximum,
+      // and the merge prefers the larger value, then the smaller index - the sequential answer
+      // (NaN dot products never replace, as in the sequential scan).
+      const uint32_t n = s.npts;
+      const float d0 = dot(ldv(s.pts), dir);
+      uint32_t bi[4] = {0u, 0u, 0u, 0u};
+      float bd[4] = {d0, d0, d0, d0};
+      uint32_t i = 1;
+      for (; i + 4 <= n; i += 4) {
+#pragma unroll
+        for (int l = 0; l < 4; ++l) {
+          float d = dot(ldv(s.pts + 3 * (i + l)), dir);
+          if (d > bd[l]) { bd[l] = d; bi[l] = i + l; }
+        }
+      }
+      for (int l = 0; i < n; ++i, ++l) {
         float d = dot(ldv(s.pts + 3 * i), dir);
-        if (d > bd) { bd = d; best = i; }
+        if (d > bd[l]) { bd[l] = d; bi[l] = i; }
+      }
+      uint32_t best = bi[0];
+      float bv = bd[0];
+#pragma unroll
+      for (int l = 1; l < 4; ++l) {
+        if (bd[l] > bv || (bd[l] == bv && bi[l] < best)) { bv = bd[l]; best = bi[l]; }
       }
       return ldv(s.pts + 3 * best);
     }
@@ -148,7 +169,7 @@ __device__ __forceinline__ V3 project_segment(V3 a, V3 b, V3 pt, Loc* loc) {
   return a + ab * u;
 }
 
-__device__ __noinline__ V3 project_triangle(V3 a, V3 b, V3 c, V3 pt, Loc* loc) {
+static __device__ __noinline__ V3 project_triangle(V3 a, V3 b, V3 c, V3 pt, Loc* loc) {
   V3 ab = b - a, ac = c - a, ap = pt - a;
   float ab_ap = dot(ab, ap), ac_ap = dot(ac, ap);
   if (ab_ap <= 0.0f && ac_ap <= 0.0f) { *loc = Loc{LOC_VERTEX, 0, {1.f, 0.f, 0.f}}; return a; }
@@ -226,7 +247,7 @@ __device__ __forceinline__ bool tet_face(int i, V3 a, V3 b, V3 c, V3 ap, V3 bp, 
   return false;
 }
 
-__device__ __noinline__ V3 project_tetrahedron(V3 a, V3 b, V3 c, V3 d, V3 pt, Loc* loc) {
+static __device__ __noinline__ V3 project_tetrahedron(V3 a, V3 b, V3 c, V3 d, V3 pt, Loc* loc) {
   V3 ab = b - a, ac = c - a, ad = d - a, ap = pt - a;
   float ap_ab = dot(ap, ab), ap_ac = dot(ap, ac), ap_ad = dot(ap, ad);
   if (ap_ab <= 0.0f && ap_ac <= 0.0f && ap_ad <= 0.0f) { *loc = Loc{LOC_VERTEX, 0, {1.f, 0.f, 0.f}}; return a; }
@@ -301,7 +322,7 @@ __device__ __forceinline__ bool simplex_add(Simplex& s, const CSO& pt) {
   return true;
 }
 
-__device__ __noinline__ V3 simplex_project_origin_and_reduce(Simplex& s) {
+static __device__ __noinline__ V3 simplex_project_origin_and_reduce(Simplex& s) {
   const V3 o = v3(0.f, 0.f, 0.f);
   Loc loc;
   if (s.dim == 0) {
@@ -379,7 +400,7 @@ __device__ __forceinline__ void gjk_result(const Simplex& s, bool prev, V3* p1, 
 }
 
 // gjk::closest_points with exact_dist = true (gjk.rs:353-453). `iters` counts support evaluations.
-__device__ __noinline__ GjkOut gjk_closest_points(const Pose& pos12, const ShapeDev& g1, const ShapeDev& g2, float max_dist, Simplex& s,
+static __device__ __noinline__ GjkOut gjk_closest_points(const Pose& pos12, const ShapeDev& g1, const ShapeDev& g2, float max_dist, Simplex& s,
                                                   uint32_t* iters) {
   const float eps_tol = GJK_EPS_TOL;
   const float eps_rel = sqrtf(eps_tol);

@@ -90,6 +90,13 @@ struct parrygpu_trimesh {
   DevBuf soup;          // per sorted position: a.xyz b.x | b.yz c.xy | c.z orig 0 0  (3 x float4)
 };
 
+// A shape set under one BVH (the reference's Compound), with device copies of the shape arrays.
+struct parrygpu_compound {
+  uint64_t n = 0, n_vertices = 0;
+  DevBuf types, params, poses, pool, aabbs;
+  parrygpu_bvh bvh;
+};
+
 // ---- status helpers ----
 parrygpu_status set_error(parrygpu_ctx* ctx, parrygpu_status s, const char* fmt, ...);
 parrygpu_status check_cuda(parrygpu_ctx* ctx, cudaError_t e, const char* what);
@@ -133,6 +140,10 @@ parrygpu_status launch_trimesh_rays(parrygpu_ctx* ctx, const parrygpu_trimesh* m
 // their sorted position instead of the AABB index.
 parrygpu_status lbvh_build(parrygpu_ctx* ctx, parrygpu_bvh* bvh, const float* d_aabbs, uint32_t n, bool leaf_data_is_position);
 parrygpu_status lbvh_refit(parrygpu_ctx* ctx, parrygpu_bvh* bvh, const float* d_aabbs);
+
+// ---- shapes (contact.cu) ----
+// World AABBs of a compound's parts (Shape::compute_aabb(pos)) into d_out (n x 6 floats).
+parrygpu_status compound_part_aabbs(parrygpu_ctx* ctx, const parrygpu_compound* c, float* d_out);
 
 // Launch configuration helpers.
 static inline uint32_t div_up(uint64_t a, uint64_t b) { return (uint32_t)((a + b - 1) / b); }

@@ -1,0 +1,446 @@
+// Batched ray casts against a shape set (the reference's Compound: parts with poses under one BVH).
+//
+// Per ray: best-first descent of Bvh::find_best (src/partitioning/bvh/bvh_traverse.rs:335-417)
+// over the LBVH of the parts' world AABBs, leaf cost = the part's RayCast::cast_ray_and_get_normal
+// (ray moved into the part frame, src/query/ray/ray.rs:393-403) with max_toi = best so far:
+//   ball      src/query/ray/ray_ball.rs:33-98
+//   cuboid    src/query/ray/ray_cuboid.rs:6-25 -> ray_aabb.rs:51-92 -> clip/clip_aabb_line.rs:79-185
+//   capsule, convex polyhedron
+//             src/query/ray/ray_support_map.rs:19-71 -> gjk.rs:519-534, 660-795 (GJK ray cast)
+//   triangle  src/query/ray/ray_triangle.rs:49-152
+// Compound semantics: src/query/ray/ray_composite_shape.rs:86-105, src/shape/compound.rs:113-144.
+// Exact toi ties resolve to the lowest part index (as for triangle meshes).
+#include "internal.hpp"
+#include "gjk_device.cuh"
+#include "lbvh_device.cuh"
+
+using namespace pg;
+
+namespace {
+
+constexpr int CRAY_STACK = 64;
+
+__device__ __forceinline__ bool ray_ball(float r, V3 o, V3 d, bool solid, float max_toi, float* toi, V3* n) {
+  float a = dot(d, d), b = dot(o, d), c = dot(o, o) - r * r;
+  bool inside;
+  float t;
+  if (a == 0.0f) {
+    if (c > 0.0f) return false;
+    inside = true; t = 0.0f;
+  } else {
+    if (c > 0.0f && b > 0.0f) return false;
+    float delta = b * b - a * c;
+    if (delta < 0.0f) return false;
+    t = (-b - sqrtf(delta)) / a;
+    if (t <= 0.0f) { inside = true; t = solid ? 0.0f : (-b + sqrtf(delta)) / a; }
+    else inside = false;
+  }
+  V3 nn = normalize(o + d * t);
+  if (!(t <= max_toi)) return false;
+  *toi = t;
+  *n = inside ? -nn : nn;
+  return true;
+}
+
+__device__ __forceinline__ float cmp3(V3 v, int i) { return i == 0 ? v.x : (i == 1 ? v.y : v.z); }
+
+// clip_aabb_line + ray_aabb on [-h, h]
+__device__ __forceinline__ bool ray_cuboid(V3 h, V3 o, V3 d, bool solid, float max_toi, float* toi, V3* n) {
+  float tmax = FLT_MAX, tmin = -FLT_MAX;
+  int near_side = 0, far_side = 0;
+  bool near_diag = false, far_diag = false;
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    float di = cmp3(d, i), oi = cmp3(o, i), hi = cmp3(h, i);
+    if (di == 0.0f) {
+      if (oi < -hi || oi > hi) return false;
+    } else {
+      float denom = 1.0f / di;
+      float a = (-hi - oi) * denom, b = (hi - oi) * denom;
+      bool flip = a > b;
+      if (flip) { float s = a; a = b; b = s; }
+      if (a > tmin) { tmin = a; near_side = flip ? -(i + 1) : (i + 1); near_diag = false; }
+      else if (a == tmin) near_diag = true;
+      if (b < tmax) { tmax = b; far_side = !flip ? -(i + 1) : (i + 1); far_diag = false; }
+      else if (b == tmax) far_diag = true;
+      if (tmax < 0.0f || tmin > tmax) return false;
+    }
+  }
+  float tn, tf;
+  V3 nn, nf;
+  bool contains = !(o.x < -h.x || o.x > h.x || o.y < -h.y || o.y > h.y || o.z < -h.z || o.z > h.z);
+  bool degenerate = false;
+  if (near_diag) { tn = tmin; nn = -normalize(d); }
+  else if (near_side == 0) { degenerate = true; }
+  else {
+    float c[3] = {0.f, 0.f, 0.f};
+    if (near_side < 0) c[-near_side - 1] = 1.0f; else c[near_side - 1] = -1.0f;
+    tn = tmin; nn = v3(c[0], c[1], c[2]);
+  }
+  if (!degenerate) {
+    if (far_diag) { tf = tmax; nf = -normalize(d); }
+    else if (far_side == 0) { degenerate = true; }
+    else {
+      float c[3] = {0.f, 0.f, 0.f};
+      if (far_side < 0) c[-far_side - 1] = -1.0f; else c[far_side - 1] = 1.0f;
+      tf = tmax; nf = v3(c[0], c[1], c[2]);
+    }
+  }
+  if (degenerate) {
+    if (!contains) return false;
+    tn = 0.0f; nn = v3(0.f, 0.f, 0.f); tf = 0.0f; nf = nn;
+  }
+  if (tn < 0.0f) {
+    if (solid) { *toi = 0.0f; *n = v3(0.f, 0.f, 0.f); return true; }
+    if (tf <= max_toi) { *toi = tf; *n = nf; return true; }
+    return false;
+  }
+  if (tn <= max_toi) { *toi = tn; *n = nn; return true; }
+  return false;
+}
+
+__device__ __forceinline__ bool ray_halfspace(V3 center, V3 normal, V3 o, V3 d, float* t) {
+  V3 dpos = center - o;
+  float denom = dot(normal, d);
+  if (fabsf(denom) <= EPS) return false;
+  float tt = dot(normal, dpos) / denom;
+  if (tt >= 0.0f) { *t = tt; return true; }
+  return false;
+}
+
+// gjk.rs:660-795 minkowski_ray_cast with the identity pose and the constant origin.
+__device__ __noinline__ bool gjk_cast_local_ray(const ShapeDev& shape, V3 ro, V3 rd, float max_toi, float* toi_out, V3* n_out) {
+  const float eps_tol = GJK_EPS_TOL;
+  const float eps_rel = sqrtf(eps_tol);
+  float ray_length = norm(rd);
+  if (fabsf(ray_length) <= EPS) return false;
+  float ltoi = 0.0f;
+  V3 co = ro, cd = rd / ray_length;
+  V3 dir = -cd;
+  V3 ldir = dir;
+  Pose id{0.f, 0.f, 0.f, 1.f, v3(0.f, 0.f, 0.f)};
+  ShapeDev origin;
+  origin.type = SH_ORIGIN;
+  Simplex s;
+  CSO sp = cso_from_shapes(id, shape, origin, dir);
+  simplex_reset(s, CSO{sp.p - co, sp.o1, sp.o2});
+  V3 proj = simplex_project_origin_and_reduce(s);
+  float max_bound = FLT_MAX;
+  int niter = 0;
+  bool last_chance = false;
+  for (;;) {
+    float old_max_bound = max_bound;
+    float nb;
+    V3 u;
+    if (try_normalize(-proj, eps_tol, &u, &nb)) { dir = u; max_bound = nb; }
+    else { *toi_out = ltoi / ray_length; *n_out = ldir; return true; }
+    CSO support;
+    if (max_bound >= old_max_bound) {
+      last_chance = true;
+      V3 p = proj + co;
+      support = CSO{p, p, v3(0.f, 0.f, 0.f)};
+    } else {
+      support = cso_from_shapes(id, shape, origin, dir);
+    }
+    if (last_chance && ltoi > 0.0f) { *toi_out = ltoi / ray_length; *n_out = ldir; return true; }
+    float t;
+    if (ray_halfspace(support.p, dir, co, cd, &t)) {
+      if (dot(dir, cd) < 0.0f && t > 0.0f) {
+        ldir = dir;
+        ltoi += t;
+        if (ltoi / ray_length > max_toi) return false;
+        V3 shift = cd * t;
+        co = co + shift;
+        max_bound = FLT_MAX;
+        for (int i = 0; i <= s.dim; ++i) s.v[i].p = s.v[i].p + (-shift);
+        last_chance = false;
+      }
+    } else {
+      if (dot(dir, cd) > eps_tol) return false;
+    }
+    if (last_chance) return false;
+    float min_bound = -dot(dir, support.p - co);
+    if (max_bound - min_bound <= eps_rel * max_bound) return false;
+    simplex_add(s, CSO{support.p - co, support.o1, support.o2});
+    proj = simplex_project_origin_and_reduce(s);
+    if (s.dim == 3) {
+      if (min_bound >= eps_tol) return false;
+      *toi_out = ltoi / ray_length; *n_out = ldir; return true;
+    }
+    niter += 1;
+    if (niter == 100) return false;
+  }
+}
+
+// ray_support_map.rs:19-71
+__device__ __forceinline__ bool ray_support_map(const ShapeDev& shape, V3 o, V3 d, bool solid, float max_toi, float* toi, V3* n) {
+  float t;
+  V3 nn;
+  if (!gjk_cast_local_ray(shape, o, d, max_toi, &t, &nn)) return false;
+  if (solid || t != 0.0f) { *toi = t; *n = nn; return true; }
+  V3 ndir = normalize(d);
+  V3 supp = local_support(shape, ndir);
+  float eps = 0.001f;
+  float shift = dot(supp - o, ndir) + eps;
+  float t2;
+  V3 n2;
+  if (!gjk_cast_local_ray(shape, o + ndir * shift, -d, shift + eps, &t2, &n2)) return false;
+  float tt = shift - t2;
+  if (!(tt <= max_toi)) return false;
+  *toi = tt;
+  *n = -n2;
+  return true;
+}
+
+// ray_triangle.rs:49-152 (toi <= max_toi filter), normal facing the ray origin
+__device__ __forceinline__ bool ray_triangle(V3 a, V3 b, V3 c, V3 o, V3 dir, float max_toi, float* toi, V3* nrm) {
+  V3 ab = b - a, ac = c - a;
+  V3 n = cross(ab, ac);
+  float d = dot(n, dir);
+  if (d == 0.0f) return false;
+  V3 ap = o - a;
+  float t = dot(ap, n);
+  if ((t < 0.0f && d < 0.0f) || (t > 0.0f && d > 0.0f)) return false;
+  d = fabsf(d);
+  V3 e = -cross(dir, ap);
+  float v, w, tt;
+  V3 normal;
+  if (t < 0.0f) {
+    v = -dot(ac, e);
+    if (v < 0.0f || v > d) return false;
+    w = dot(ab, e);
+    if (w < 0.0f || v + w > d) return false;
+    float invd = 1.0f / d;
+    tt = -t * invd;
+    normal = -normalize(n);
+  } else {
+    v = dot(ac, e);
+    if (v < 0.0f || v > d) return false;
+    w = -dot(ab, e);
+    if (w < 0.0f || v + w > d) return false;
+    float invd = 1.0f / d;
+    tt = t * invd;
+    normal = normalize(n);
+  }
+  if (!(tt <= max_toi)) return false;
+  *toi = tt;
+  *nrm = normal;
+  return true;
+}
+
+// RayCast::cast_ray_and_get_normal(pose, ray, max_toi, solid) for one part.
+__device__ __noinline__ bool part_cast_ray(const ShapeDev& s, const Pose& pose, V3 wo, V3 wd, float max_toi, bool solid, float* toi, V3* n) {
+  V3 o = pose_inv_point(pose, wo), d = pose_inv_rotate(pose, wd);
+  V3 ln;
+  bool ok;
+  switch (s.type) {
+    case SH_BALL: ok = ray_ball(s.a, o, d, solid, max_toi, toi, &ln); break;
+    case SH_CUBOID: ok = ray_cuboid(v3(s.a, s.b, s.c), o, d, solid, max_toi, toi, &ln); break;
+    case SH_TRIANGLE: ok = ray_triangle(ldv(s.pts), ldv(s.pts + 3), ldv(s.pts + 6), o, d, max_toi, toi, &ln); break;
+    default: ok = ray_support_map(s, o, d, solid, max_toi, toi, &ln); break;
+  }
+  if (ok) *n = pose_rotate(pose, ln);
+  return ok;
+}
+
+// Ray vs AABB slab (ray_aabb.rs:12-49, solid), FLT_MAX on a miss.
+__device__ __forceinline__ float slab(float3 mn, float3 mx, V3 o, V3 inv, uint32_t zmask, float max_toi) {
+  float tmin = 0.0f, tmax = max_toi;
+  bool miss = false;
+  float oo[3] = {o.x, o.y, o.z}, iv[3] = {inv.x, inv.y, inv.z}, lo[3] = {mn.x, mn.y, mn.z}, hi[3] = {mx.x, mx.y, mx.z};
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    if (zmask & (1u << i)) {
+      miss |= (oo[i] < lo[i]) | (oo[i] > hi[i]);
+    } else {
+      float a = (lo[i] - oo[i]) * iv[i], b = (hi[i] - oo[i]) * iv[i];
+      if (a > b) { float t = a; a = b; b = t; }
+      tmin = fmaxf(tmin, a);
+      tmax = fminf(tmax, b);
+    }
+  }
+  return (!miss && tmin <= tmax) ? tmin : FLT_MAX;
+}
+
+struct CompoundDev {
+  const uint32_t* types;
+  const float4* params;
+  const float* poses;
+  const float* pool;
+};
+
+__global__ void __launch_bounds__(128) k_compound_rays(const WideNode* __restrict__ wide, CompoundDev cd, const float* __restrict__ rays,
+                                                       uint32_t n, float max_toi, int solid, int has_pose, Pose cpose,
+                                                       uint32_t* __restrict__ part_out, float* __restrict__ toi_out,
+                                                       float* __restrict__ normal_out, uint32_t* __restrict__ err) {
+  uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= n) return;
+  const float* rp = rays + 6 * (size_t)r;
+  V3 o = v3(rp[0], rp[1], rp[2]), dir = v3(rp[3], rp[4], rp[5]);
+  if (has_pose) { o = pose_inv_point(cpose, o); dir = pose_inv_rotate(cpose, dir); }
+  uint32_t zmask = (dir.x == 0.0f ? 1u : 0u) | (dir.y == 0.0f ? 2u : 0u) | (dir.z == 0.0f ? 4u : 0u);
+  V3 inv = v3(dir.x != 0.0f ? 1.0f / dir.x : 0.0f, dir.y != 0.0f ? 1.0f / dir.y : 0.0f, dir.z != 0.0f ? 1.0f / dir.z : 0.0f);
+  float best = max_toi;
+  uint32_t best_part = 0xffffffffu;
+  V3 best_n = v3(0.f, 0.f, 0.f);
+  bool have = false;
+  auto try_leaf = [&](uint32_t part) {
+    ShapeDev s = load_shape(cd.types, cd.params, cd.pool, part);
+    Pose p = load_pose(cd.poses, part);
+    float t;
+    V3 nn;
+    if (!part_cast_ray(s, p, o, dir, best, solid != 0, &t, &nn)) return;
+    if (t < best || (have && t == best && part < best_part)) { best = t; best_part = part; best_n = nn; have = true; }
+  };
+  WideNode w;
+  load_wide(wide, 0, &w);
+  if ((w.r.data & 0x3fffffffu) == 0u) {
+    float s = slab(w.l.mins, w.l.maxs, o, inv, zmask, max_toi);
+    if (s < max_toi) try_leaf(w.l.children);
+  } else {
+    uint32_t stack[CRAY_STACK];
+    int sp = 0;
+    for (;;) {
+      float ls = slab(w.l.mins, w.l.maxs, o, inv, zmask, best);
+      float rs = slab(w.r.mins, w.r.maxs, o, inv, zmask, best);
+      const BvhNodeDev* nearn = &w.l;
+      const BvhNodeDev* farn = &w.r;
+      if (ls > rs) { float t = ls; ls = rs; rs = t; nearn = &w.r; farn = &w.l; }
+      uint32_t next = 0xffffffffu;
+      uint32_t far_child = farn->children, far_data = farn->data;
+      if (ls != FLT_MAX && (ls < best || (have && ls == best))) {
+        if ((nearn->data & 0x3fffffffu) == 1u) try_leaf(nearn->children);
+        else next = nearn->children;
+      }
+      if (rs != FLT_MAX && (rs < best || (have && rs == best))) {
+        if ((far_data & 0x3fffffffu) == 1u) try_leaf(far_child);
+        else if (next != 0xffffffffu) {
+          if (sp >= CRAY_STACK) { atomicOr(err, ERR_STACK_OVERFLOW); break; }
+          stack[sp++] = far_child;
+        } else next = far_child;
+      }
+      if (next == 0xffffffffu) {
+        if (sp == 0) break;
+        next = stack[--sp];
+      }
+      load_wide(wide, next, &w);
+    }
+  }
+  if (has_pose && have) best_n = pose_rotate(cpose, best_n);
+  part_out[r] = have ? best_part : 0xffffffffu;
+  toi_out[r] = have ? best : 0.0f;
+  if (normal_out) {
+    normal_out[3 * (size_t)r] = best_n.x;
+    normal_out[3 * (size_t)r + 1] = best_n.y;
+    normal_out[3 * (size_t)r + 2] = best_n.z;
+  }
+}
+
+}  // namespace
+
+static parrygpu_status compound_copy_in(parrygpu_ctx* ctx, DevBuf& dst, const void* src, size_t bytes) {
+  PG_CUDA(ctx, dst.reserve(bytes ? bytes : 16));
+  if (bytes) PG_CUDA(ctx, cudaMemcpyAsync(dst.ptr, src, bytes, cudaMemcpyDefault, ctx->stream));
+  return PARRYGPU_OK;
+}
+
+extern "C" {
+
+parrygpu_status parrygpu_compound_create(parrygpu_ctx* ctx, const parrygpu_shapes* shapes, parrygpu_compound** out) {
+  if (!ctx || !shapes || !out) return PARRYGPU_INVALID_ARG;
+  *out = nullptr;
+  if (shapes->n > 0xffffffffull) return set_error(ctx, PARRYGPU_INVALID_ARG, "too many parts");
+  PG_CUDA(ctx, cudaSetDevice(ctx->device));
+  parrygpu_compound* c = new parrygpu_compound();
+  c->n = shapes->n;
+  c->n_vertices = shapes->n_vertices;
+  parrygpu_status s;
+  if ((s = compound_copy_in(ctx, c->types, shapes->types, c->n * 4)) != PARRYGPU_OK ||
+      (s = compound_copy_in(ctx, c->params, shapes->params, c->n * 16)) != PARRYGPU_OK ||
+      (s = compound_copy_in(ctx, c->poses, shapes->poses, c->n * 28)) != PARRYGPU_OK ||
+      (s = compound_copy_in(ctx, c->pool, shapes->vertices, c->n_vertices * 12)) != PARRYGPU_OK ||
+      (s = compound_copy_in(ctx, c->aabbs, nullptr, 0)) != PARRYGPU_OK) {
+    parrygpu_compound_destroy(c);
+    return s;
+  }
+  if (c->n > 0) {
+    if ((s = check_cuda(ctx, c->aabbs.reserve(c->n * 24), "compound aabbs")) != PARRYGPU_OK ||
+        (s = compound_part_aabbs(ctx, c, c->aabbs.as<float>())) != PARRYGPU_OK ||
+        (s = lbvh_build(ctx, &c->bvh, c->aabbs.as<float>(), (uint32_t)c->n, false)) != PARRYGPU_OK) {
+      parrygpu_compound_destroy(c);
+      return s;
+    }
+  }
+  PG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  if ((s = parrygpu_sync(ctx)) != PARRYGPU_OK) {
+    parrygpu_compound_destroy(c);
+    return set_error(ctx, PARRYGPU_INVALID_ARG, "invalid shape description (type or vertex range)");
+  }
+  *out = c;
+  return PARRYGPU_OK;
+}
+
+void parrygpu_compound_destroy(parrygpu_compound* c) {
+  if (!c) return;
+  for (DevBuf* d : {&c->types, &c->params, &c->poses, &c->pool, &c->aabbs, &c->bvh.wide, &c->bvh.leaf_parent, &c->bvh.node_parent,
+                    &c->bvh.leaf_index, &c->bvh.flags, &c->bvh.root_aabb, &c->bvh.info})
+    d->release();
+  delete c;
+}
+
+parrygpu_status parrygpu_compound_set_poses(parrygpu_ctx* ctx, parrygpu_compound* c, const float* poses) {
+  if (!ctx || !c) return PARRYGPU_INVALID_ARG;
+  if (c->n == 0) return PARRYGPU_OK;
+  if (!poses) return set_error(ctx, PARRYGPU_INVALID_ARG, "poses is null");
+  PG_CUDA(ctx, cudaSetDevice(ctx->device));
+  PG_CUDA(ctx, cudaMemcpyAsync(c->poses.ptr, poses, c->n * 28, cudaMemcpyDefault, ctx->stream));
+  parrygpu_status s = compound_part_aabbs(ctx, c, c->aabbs.as<float>());
+  if (s != PARRYGPU_OK) return s;
+  s = lbvh_refit(ctx, &c->bvh, c->aabbs.as<float>());
+  if (s != PARRYGPU_OK) return s;
+  if (!is_device_ptr(poses)) PG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return PARRYGPU_OK;
+}
+
+parrygpu_status parrygpu_compound_cast_rays(parrygpu_ctx* ctx, const parrygpu_compound* c, const float* pose7, const float* rays, uint32_t n,
+                                            float max_toi, int solid, uint32_t* part, float* toi, float* normal) {
+  if (!ctx || !c) return PARRYGPU_INVALID_ARG;
+  if (n == 0) return PARRYGPU_OK;
+  if (!rays || !part || !toi) return set_error(ctx, PARRYGPU_INVALID_ARG, "rays, part and toi are required");
+  PG_CUDA(ctx, cudaSetDevice(ctx->device));
+  Pose pose{0.f, 0.f, 0.f, 1.f, v3(0.f, 0.f, 0.f)};
+  if (pose7) {
+    float p[7];
+    PG_CUDA(ctx, cudaMemcpyAsync(p, pose7, 28, cudaMemcpyDefault, ctx->stream));
+    PG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    pose = Pose{p[0], p[1], p[2], p[3], v3(p[4], p[5], p[6])};
+  }
+  const void* d_rays;
+  parrygpu_status s = stage_input(ctx, ctx->stage_in[6], rays, (size_t)n * 24, &d_rays);
+  if (s != PARRYGPU_OK) return s;
+  void *d_part, *d_toi, *d_nrm;
+  bool c1, c2, c3;
+  if ((s = stage_output(ctx, ctx->stage_out[1], part, (size_t)n * 4, &d_part, &c1)) != PARRYGPU_OK) return s;
+  if ((s = stage_output(ctx, ctx->stage_out[2], toi, (size_t)n * 4, &d_toi, &c2)) != PARRYGPU_OK) return s;
+  if ((s = stage_output(ctx, ctx->stage_out[3], normal, (size_t)n * 12, &d_nrm, &c3)) != PARRYGPU_OK) return s;
+  if (c->n == 0) {
+    PG_CUDA(ctx, cudaMemsetAsync(d_part, 0xff, (size_t)n * 4, ctx->stream));
+    PG_CUDA(ctx, cudaMemsetAsync(d_toi, 0, (size_t)n * 4, ctx->stream));
+    if (d_nrm) PG_CUDA(ctx, cudaMemsetAsync(d_nrm, 0, (size_t)n * 12, ctx->stream));
+  } else {
+    CompoundDev cd{c->types.as<uint32_t>(), c->params.as<float4>(), c->poses.as<float>(), c->pool.as<float>()};
+    KernelTimer kt(ctx, "compound_rays");
+    k_compound_rays<<<div_up(n, 128), 128, 0, ctx->stream>>>(c->bvh.wide.as<WideNode>(), cd, (const float*)d_rays, n, max_toi, solid,
+                                                             pose7 ? 1 : 0, pose, (uint32_t*)d_part, (float*)d_toi, (float*)d_nrm,
+                                                             ctx->d_err);
+    kt.stop();
+    PG_LAUNCHED(ctx);
+  }
+  if (c1) PG_CUDA(ctx, cudaMemcpyAsync(part, d_part, (size_t)n * 4, cudaMemcpyDeviceToHost, ctx->stream));
+  if (c2) PG_CUDA(ctx, cudaMemcpyAsync(toi, d_toi, (size_t)n * 4, cudaMemcpyDeviceToHost, ctx->stream));
+  if (c3) PG_CUDA(ctx, cudaMemcpyAsync(normal, d_nrm, (size_t)n * 12, cudaMemcpyDeviceToHost, ctx->stream));
+  if (c1 || c2 || c3 || d_rays != rays) return parrygpu_sync(ctx);
+  return PARRYGPU_OK;
+}
+
+}  // extern "C"

@@ -46,3 +46,42 @@ def ball_cuboid():
         b = s.add_ball(c["ball_radius"], pose7(case["ball_pos"]))
         pairs.append((b, cub))
     return s, np.array(pairs, np.uint32), c
+
+
+def cuboid_ray():
+    c = KA["cuboid_ray_doc_test"]
+    s = ShapeSet()
+    s.add_cuboid(c["half_extents"])
+    return s, np.array([c["ray"]], np.float32), c
+
+
+def solid_ray_cast():
+    c = KA["solid_ray_cast3d"]
+    s = ShapeSet()
+    s.add_cuboid(c["half_extents"])
+    return s, c
+
+
+def mixed_scene(n: int, seed: int, extent: float = 6.0):
+    """Balls, cuboids, capsules, convex hulls and triangles at random poses in a cube."""
+    from parry_gb300 import workloads as W
+    rng = np.random.default_rng(seed)
+    s = ShapeSet()
+    pool, first, count = W.ellipsoid_hulls(32, seed=seed, stream=1, nmin=8, nmax=64)
+    for i in range(n):
+        q = rng.normal(size=4)
+        q /= np.linalg.norm(q)
+        pose = pose7(rng.uniform(-extent, extent, 3), q)
+        t = i % 5
+        if t == 0:
+            s.add_ball(rng.uniform(0.3, 1.5), pose)
+        elif t == 1:
+            s.add_cuboid(rng.uniform(0.3, 1.5, 3), pose)
+        elif t == 2:
+            s.add_capsule(rng.uniform(0.2, 1.2), rng.uniform(0.2, 0.8), pose)
+        elif t == 3:
+            h = i % 32
+            s.add_convex(pool[first[h]:first[h] + count[h]], pose)
+        else:
+            s.add_triangle(*rng.uniform(-1.2, 1.2, (3, 3)), pose)
+    return s
