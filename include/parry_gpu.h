@@ -195,6 +195,47 @@ parrygpu_status parrygpu_contacts(parrygpu_ctx* ctx, const parrygpu_shapes* shap
                                   float prediction, const float* init_dirs, parrygpu_contact* out, uint8_t* has_contact,
                                   parrygpu_gjk_stats* stats);
 
+/* Same as parrygpu_contacts, and also writes final_dirs[k] (n_pairs x 3, may be NULL): the
+ * direction the reference's GJK/EPA ends with, in the first shape's local frame - the contact
+ * normal1 for ClosestPoints (closest points or EPA), the separating direction for NoIntersection,
+ * zero for pairs that take the ball paths. These are the labels of the learned warm start. */
+parrygpu_status parrygpu_contacts_with_dirs(parrygpu_ctx* ctx, const parrygpu_shapes* shapes, const uint32_t* pairs, uint64_t n_pairs,
+                                            float prediction, const float* init_dirs, parrygpu_contact* out, uint8_t* has_contact,
+                                            parrygpu_gjk_stats* stats, float* final_dirs);
+
+/* ---- learned GJK warm start (no reference counterpart: parry's init_dir hook is its only tie) ----
+ * A 39 -> 128 -> 128 -> 128 -> 128 -> 3 MLP (GELU, BF16 weights and activations, FP32 accumulation
+ * on the tensor cores) predicts contact_support_map_support_map_with_params's init_dir from the
+ * relative pose (7) and a 16-float descriptor per shape. Inputs are padded to 48 features. */
+typedef struct parrygpu_mlp parrygpu_mlp;
+
+#define PARRYGPU_MLP_IN 48
+#define PARRYGPU_MLP_HIDDEN 128
+#define PARRYGPU_MLP_LAYERS 5
+
+/* Xavier-uniform initialisation from `seed`. */
+parrygpu_status parrygpu_mlp_create(parrygpu_ctx* ctx, uint64_t seed, parrygpu_mlp** out);
+void parrygpu_mlp_destroy(parrygpu_mlp* mlp);
+/* Pair features (n_pairs x 48 floats: relative pose of b in a's frame, descriptors of a and b). */
+parrygpu_status parrygpu_mlp_features(parrygpu_ctx* ctx, const parrygpu_shapes* shapes, const uint32_t* pairs, uint64_t n_pairs,
+                                      float* features);
+/* Trains on (features, unit target directions) with Adam for `epochs` passes in minibatches of
+ * `batch` pairs (loss = mean(1 - cos(prediction, target))). loss_per_epoch (epochs floats) may be NULL. */
+parrygpu_status parrygpu_mlp_train(parrygpu_ctx* ctx, parrygpu_mlp* mlp, const float* features, const float* targets, uint64_t n,
+                                   uint32_t epochs, uint32_t batch, float lr, float* loss_per_epoch);
+/* Predicted unit init directions (n x 3). Degenerate outputs fall back to the reference default
+ * (the relative translation, else +x), which the caller passes as is. */
+parrygpu_status parrygpu_mlp_predict(parrygpu_ctx* ctx, const parrygpu_mlp* mlp, const float* features, uint64_t n, float* dirs);
+/* Loss and gradients of one batch without updating (gradient checks): grads receives the
+ * parameters' gradients in the layout of parrygpu_mlp_get_params. */
+parrygpu_status parrygpu_mlp_loss_and_grads(parrygpu_ctx* ctx, const parrygpu_mlp* mlp, const float* features, const float* targets,
+                                            uint64_t n, float* loss, float* grads);
+/* Number of parameters (float32 master weights and biases, layer by layer: W [out x in] then b). */
+uint64_t parrygpu_mlp_param_count(void);
+/* Copies the FP32 master parameters out / in (checkpoint and resume; the BF16 copies follow). */
+parrygpu_status parrygpu_mlp_get_params(parrygpu_ctx* ctx, const parrygpu_mlp* mlp, float* params);
+parrygpu_status parrygpu_mlp_set_params(parrygpu_ctx* ctx, parrygpu_mlp* mlp, const float* params);
+
 /* ---- Compound (shape set) ray casts ------------------------------------------------------- */
 
 /* Replaces Compound::new(shapes) (src/shape/compound.rs:113-144): copies the parts (with their poses)

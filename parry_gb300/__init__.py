@@ -30,7 +30,8 @@ import numpy as np
 from . import _capi
 from ._capi import ParryGpuError, lib, check
 
-__all__ = ["Context", "Bvh", "TriMesh", "Compound", "ShapeSet", "shape_aabbs", "contacts", "ParryGpuError", "NO_HIT", "lib"]
+__all__ = ["Context", "Bvh", "TriMesh", "Compound", "ShapeSet", "WarmStartMLP", "shape_aabbs", "contacts", "ParryGpuError",
+           "NO_HIT", "lib"]
 
 from .shapes import ShapeSet  # noqa: E402
 
@@ -281,11 +282,12 @@ def shape_aabbs(ctx: Context, shapes, margin: float = 0.0):
     return out
 
 
-def contacts(ctx: Context, shapes, pairs, prediction: float, init_dirs=None, want_stats: bool = False, out=None):
+def contacts(ctx: Context, shapes, pairs, prediction: float, init_dirs=None, want_stats: bool = False, out=None,
+             final_dirs=None):
     """Batched query::contact over the (a, b) rows of `pairs`.
 
     Returns (has_contact u8 (k,), contacts f32 (k, 13) = point1, point2, normal1, normal2, dist)
-    [, stats dict]."""
+    [, stats dict]. `final_dirs` (k x 3 buffer) receives the direction GJK/EPA ended with."""
     st = _StagedShapes(shapes)
     kp, pp = _as_input(pairs, np.uint32)
     k = int(kp.shape[0]) if kp is not None else 0
@@ -302,8 +304,9 @@ def contacts(ctx: Context, shapes, pairs, prediction: float, init_dirs=None, wan
         has, res = out
         ph, pr = C.c_void_p(_dptr(has)), C.c_void_p(_dptr(res))
     stats = _capi.ParryGpuGjkStats()
-    check(lib().parrygpu_contacts(ctx.handle, C.byref(st.struct), pp, k, float(prediction), pi, pr, ph,
-                                  C.byref(stats) if want_stats else None), ctx.handle)
+    pd = C.c_void_p(_dptr(final_dirs)) if final_dirs is not None else None
+    check(lib().parrygpu_contacts_with_dirs(ctx.handle, C.byref(st.struct), pp, k, float(prediction), pi, pr, ph,
+                                            C.byref(stats) if want_stats else None, pd), ctx.handle)
     if want_stats:
         return has, res, {"gjk_iters": stats.gjk_iterations, "epa_iters": stats.epa_iterations, "epa_calls": stats.epa_calls}
     return has, res
@@ -344,6 +347,92 @@ class Compound:
     def close(self) -> None:
         if getattr(self, "_h", None):
             lib().parrygpu_compound_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class WarmStartMLP:
+    """Learned GJK initial direction (BF16 tensor-core MLP, see include/parry_gpu.h)."""
+
+    IN = 48
+
+    def __init__(self, ctx: Context, seed: int = 0):
+        self.ctx = ctx
+        h = C.c_void_p()
+        check(lib().parrygpu_mlp_create(ctx.handle, C.c_uint64(seed), C.byref(h)), ctx.handle)
+        self._h = h
+
+    @staticmethod
+    def param_count() -> int:
+        return int(lib().parrygpu_mlp_param_count())
+
+    def features(self, shapes, pairs):
+        st = _StagedShapes(shapes)
+        kp, pp = _as_input(pairs, np.uint32)
+        k = int(kp.shape[0])
+        out, po = _alloc_like(kp, (k, self.IN), np.float32)
+        check(lib().parrygpu_mlp_features(self.ctx.handle, C.byref(st.struct), pp, k, po), self.ctx.handle)
+        return out
+
+    def train(self, features, targets, epochs: int = 1, batch: int = 8192, lr: float = 1e-3):
+        """Adam on mean(1 - cos(prediction, target)); features and targets must be CUDA tensors."""
+        kf, pf = _as_input(features, np.float32)
+        kt, pt = _as_input(targets, np.float32)
+        losses = np.zeros(max(1, epochs), np.float32)
+        check(lib().parrygpu_mlp_train(self.ctx.handle, self._h, pf, pt, int(kf.shape[0]), int(epochs), int(batch), float(lr),
+                                       C.c_void_p(losses.ctypes.data)), self.ctx.handle)
+        return losses[:epochs]
+
+    def predict(self, features):
+        kf, pf = _as_input(features, np.float32)
+        n = int(kf.shape[0])
+        out, po = _alloc_like(kf, (n, 3), np.float32)
+        check(lib().parrygpu_mlp_predict(self.ctx.handle, self._h, pf, n, po), self.ctx.handle)
+        return out
+
+    def loss_and_grads(self, features, targets):
+        kf, pf = _as_input(features, np.float32)
+        kt, pt = _as_input(targets, np.float32)
+        loss = C.c_float(0.0)
+        grads = np.zeros(self.param_count(), np.float32)
+        check(lib().parrygpu_mlp_loss_and_grads(self.ctx.handle, self._h, pf, pt, int(kf.shape[0]), C.byref(loss),
+                                                C.c_void_p(grads.ctypes.data)), self.ctx.handle)
+        return float(loss.value), grads
+
+    def get_params(self) -> np.ndarray:
+        p = np.zeros(self.param_count(), np.float32)
+        check(lib().parrygpu_mlp_get_params(self.ctx.handle, self._h, C.c_void_p(p.ctypes.data)), self.ctx.handle)
+        return p
+
+    def set_params(self, params) -> None:
+        p = np.ascontiguousarray(params, np.float32)
+        assert p.size == self.param_count()
+        check(lib().parrygpu_mlp_set_params(self.ctx.handle, self._h, C.c_void_p(p.ctypes.data)), self.ctx.handle)
+
+    def save(self, path) -> None:
+        """Checkpoint: a JSON header line then the raw float32 parameters."""
+        import json
+        p = self.get_params()
+        with open(path, "wb") as f:
+            f.write((json.dumps({"format": "parry_gb300.warm_start_mlp", "version": 1, "params": int(p.size)}) + "\n").encode())
+            f.write(p.tobytes())
+
+    def load(self, path) -> None:
+        import json
+        with open(path, "rb") as f:
+            hdr = json.loads(f.readline().decode())
+            if hdr.get("format") != "parry_gb300.warm_start_mlp" or hdr.get("params") != self.param_count():
+                raise ValueError(f"not a compatible warm-start checkpoint: {hdr}")
+            self.set_params(np.frombuffer(f.read(), np.float32))
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            lib().parrygpu_mlp_destroy(self._h)
             self._h = None
 
     def __del__(self):

@@ -56,6 +56,16 @@ SIGNATURES: dict[str, tuple] = {
     "parrygpu_trimesh_cast_rays_noalloc": (I32, [P, P, P, P, U32, F32, I32, P, P, P]),
     "parrygpu_shapes_aabbs": (I32, [P, P, F32, P]),
     "parrygpu_contacts": (I32, [P, P, P, U64, F32, P, P, P, P]),
+    "parrygpu_contacts_with_dirs": (I32, [P, P, P, U64, F32, P, P, P, P, P]),
+    "parrygpu_mlp_create": (I32, [P, U64, C.POINTER(P)]),
+    "parrygpu_mlp_destroy": (None, [P]),
+    "parrygpu_mlp_features": (I32, [P, P, P, U64, P]),
+    "parrygpu_mlp_train": (I32, [P, P, P, P, U64, U32, U32, F32, P]),
+    "parrygpu_mlp_predict": (I32, [P, P, P, U64, P]),
+    "parrygpu_mlp_loss_and_grads": (I32, [P, P, P, P, U64, P, P]),
+    "parrygpu_mlp_param_count": (U64, []),
+    "parrygpu_mlp_get_params": (I32, [P, P, P]),
+    "parrygpu_mlp_set_params": (I32, [P, P, P]),
     "parrygpu_compound_create": (I32, [P, P, C.POINTER(P)]),
     "parrygpu_compound_destroy": (None, [P]),
     "parrygpu_compound_set_poses": (I32, [P, P, P]),

@@ -255,7 +255,8 @@ __global__ void __launch_bounds__(CT_THREADS) k_contacts_main(ShapeArrays sh, co
                                                               float prediction, const float* __restrict__ init_dirs,
                                                               float* __restrict__ out, uint8_t* __restrict__ has,
                                                               uint32_t* __restrict__ queue, unsigned long long* __restrict__ qcount,
-                                                              unsigned long long* __restrict__ stats, uint32_t* __restrict__ err) {
+                                                              unsigned long long* __restrict__ stats, uint32_t* __restrict__ err,
+                                                              float* __restrict__ final_dirs) {
   uint64_t k = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
   uint32_t iters = 0;
   if (k < n && !valid_pair(sh, pairs[2 * k], pairs[2 * k + 1])) {
@@ -315,6 +316,12 @@ __global__ void __launch_bounds__(CT_THREADS) k_contacts_main(ShapeArrays sh, co
         enqueue(queue, qcount, k, s);
         done = false;
       }
+      if (final_dirs && g.kind != GJK_INTERSECTION) {
+        final_dirs[3 * k] = g.dir.x; final_dirs[3 * k + 1] = g.dir.y; final_dirs[3 * k + 2] = g.dir.z;
+      }
+    }
+    if (final_dirs && ps.path != PATH_SUPPORT) {
+      final_dirs[3 * k] = 0.0f; final_dirs[3 * k + 1] = 0.0f; final_dirs[3 * k + 2] = 0.0f;
     }
     if (done) write_out(out, has, k, ok, c, ps.pa, ps.pb);
   }
@@ -328,7 +335,7 @@ __global__ void __launch_bounds__(EPA_THREADS) k_contacts_epa(ShapeArrays sh, co
                                                               float* __restrict__ out, uint8_t* __restrict__ has,
                                                               const uint32_t* __restrict__ queue, const unsigned long long* __restrict__ qcount,
                                                               uint32_t* __restrict__ ws_pool, unsigned long long* __restrict__ stats,
-                                                              uint32_t* __restrict__ err) {
+                                                              uint32_t* __restrict__ err, float* __restrict__ final_dirs) {
   const uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x;
   EpaWs ws{ws_pool + (size_t)(slot >> 5) * (EPA_WORDS * 32) + (slot & 31)};
   const unsigned long long total = *qcount;
@@ -353,6 +360,10 @@ __global__ void __launch_bounds__(EPA_THREADS) k_contacts_epa(ShapeArrays sh, co
       int r = epa_closest_points(ws, ps.pos12, ps.s1, ps.s2, s, &p1, &p2, &nn, &iters);
       if (r == EPA_OVERFLOW) atomicOr(err, ERR_POLYTOPE_FULL);
       if (r == EPA_OK) { ok = true; finish_support_pair(ps.pos12, p1, p2, nn, &c); }
+      if (final_dirs) {
+        V3 fd = r == EPA_OK ? nn : v3(1.f, 0.f, 0.f);  // GJKResult::NoIntersection(x) when EPA fails
+        final_dirs[3 * k] = fd.x; final_dirs[3 * k + 1] = fd.y; final_dirs[3 * k + 2] = fd.z;
+      }
     } else {
       const ShapeDev& cs = *ps.convex;
       V3 center = ps.cpos.t;
@@ -478,6 +489,12 @@ parrygpu_status parrygpu_shapes_aabbs(parrygpu_ctx* ctx, const parrygpu_shapes* 
 parrygpu_status parrygpu_contacts(parrygpu_ctx* ctx, const parrygpu_shapes* shapes, const uint32_t* pairs, uint64_t n_pairs,
                                   float prediction, const float* init_dirs, parrygpu_contact* out, uint8_t* has_contact,
                                   parrygpu_gjk_stats* stats) {
+  return parrygpu_contacts_with_dirs(ctx, shapes, pairs, n_pairs, prediction, init_dirs, out, has_contact, stats, nullptr);
+}
+
+parrygpu_status parrygpu_contacts_with_dirs(parrygpu_ctx* ctx, const parrygpu_shapes* shapes, const uint32_t* pairs, uint64_t n_pairs,
+                                            float prediction, const float* init_dirs, parrygpu_contact* out, uint8_t* has_contact,
+                                            parrygpu_gjk_stats* stats, float* final_dirs) {
   if (!ctx || !shapes) return PARRYGPU_INVALID_ARG;
   if (stats) std::memset(stats, 0, sizeof(*stats));
   if (n_pairs == 0) return PARRYGPU_OK;
@@ -493,6 +510,9 @@ parrygpu_status parrygpu_contacts(parrygpu_ctx* ctx, const parrygpu_shapes* shap
   bool c_out, c_has;
   if ((s = stage_output(ctx, ctx->stage_out[0], out, (size_t)n_pairs * 52, &d_out, &c_out)) != PARRYGPU_OK) return s;
   if ((s = stage_output(ctx, ctx->stage_out[1], has_contact, (size_t)n_pairs, &d_has, &c_has)) != PARRYGPU_OK) return s;
+  void* d_dirs = nullptr;
+  bool c_dirs = false;
+  if ((s = stage_output(ctx, ctx->stage_out[2], final_dirs, (size_t)n_pairs * 12, &d_dirs, &c_dirs)) != PARRYGPU_OK) return s;
   PG_CUDA(ctx, ctx->ct_queue.reserve((size_t)n_pairs * QUEUE_WORDS * 4));
   PG_CUDA(ctx, ctx->ct_counters.reserve(64));
   uint32_t epa_blocks = (uint32_t)(ctx->sm_count > 0 ? ctx->sm_count : 152) * 8;
@@ -504,7 +524,7 @@ parrygpu_status parrygpu_contacts(parrygpu_ctx* ctx, const parrygpu_shapes* shap
     KernelTimer kt(ctx, "contacts_gjk");
     k_contacts_main<<<div_up(n_pairs, CT_THREADS), CT_THREADS, 0, ctx->stream>>>(
         sh, (const uint32_t*)dp, n_pairs, prediction, (const float*)di, (float*)d_out, (uint8_t*)d_has, ctx->ct_queue.as<uint32_t>(),
-        ctr, ctr + 1, ctx->d_err);
+        ctr, ctr + 1, ctx->d_err, (float*)d_dirs);
     kt.stop();
     PG_LAUNCHED(ctx);
   }
@@ -512,12 +532,13 @@ parrygpu_status parrygpu_contacts(parrygpu_ctx* ctx, const parrygpu_shapes* shap
     KernelTimer kt(ctx, "contacts_epa");
     k_contacts_epa<<<epa_blocks, EPA_THREADS, 0, ctx->stream>>>(sh, (const uint32_t*)dp, prediction, (float*)d_out, (uint8_t*)d_has,
                                                                 ctx->ct_queue.as<uint32_t>(), ctr, ctx->epa_ws.as<uint32_t>(), ctr + 1,
-                                                                ctx->d_err);
+                                                                ctx->d_err, (float*)d_dirs);
     kt.stop();
     PG_LAUNCHED(ctx);
   }
   if (c_out) PG_CUDA(ctx, cudaMemcpyAsync(out, d_out, (size_t)n_pairs * 52, cudaMemcpyDeviceToHost, ctx->stream));
   if (c_has) PG_CUDA(ctx, cudaMemcpyAsync(has_contact, d_has, (size_t)n_pairs, cudaMemcpyDeviceToHost, ctx->stream));
+  if (c_dirs) PG_CUDA(ctx, cudaMemcpyAsync(final_dirs, d_dirs, (size_t)n_pairs * 12, cudaMemcpyDeviceToHost, ctx->stream));
   if (stats) {
     unsigned long long h[4];
     PG_CUDA(ctx, cudaMemcpyAsync(h, ctr, 32, cudaMemcpyDeviceToHost, ctx->stream));
@@ -528,7 +549,7 @@ parrygpu_status parrygpu_contacts(parrygpu_ctx* ctx, const parrygpu_shapes* shap
   }
   bool staged_in = sh.types != shapes->types || sh.params != (const float4*)shapes->params || sh.poses != shapes->poses ||
                    dp != pairs || (init_dirs && di != init_dirs) || (shapes->n_vertices && sh.pool != shapes->vertices);
-  if (c_out || c_has || stats || staged_in) return parrygpu_sync(ctx);
+  if (c_out || c_has || c_dirs || stats || staged_in) return parrygpu_sync(ctx);
   return PARRYGPU_OK;
 }
 

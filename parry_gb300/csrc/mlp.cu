@@ -1,0 +1,657 @@
+// Learned GJK warm start: a small MLP trained and evaluated with hand-written BF16 tensor-core
+// kernels (mma.sync m16n8k16, FP32 accumulation). No reference counterpart: its only link to the
+// reference is the init_dir parameter of contact_support_map_support_map_with_params
+// (src/query/contact/contact_support_map_support_map.rs:40-62), and the plain GJK result remains
+// the judge of the answer - a poor guess only costs iterations.
+//
+// Network: 48 (39 features + zero padding) -> 128 -> 128 -> 128 -> 128 -> 3, GELU (erf form) after
+// each hidden layer, output normalised to a unit direction in the first shape's frame.
+// Parameters: FP32 masters + Adam moments; BF16 copies feed the tensor cores. Activations between
+// layers are BF16; pre-activations are kept in FP32 for the backward pass.
+// Layout of the parameter vector (parrygpu_mlp_get_params): per layer W [out x in] then b [out].
+#include "internal.hpp"
+#include "common.cuh"
+#include <cuda_bf16.h>
+#include <vector>
+#include <cmath>
+
+using namespace pg;
+
+namespace {
+
+constexpr int IN = PARRYGPU_MLP_IN;
+constexpr int HID = PARRYGPU_MLP_HIDDEN;
+constexpr int NL = PARRYGPU_MLP_LAYERS;
+constexpr int OUT = 3;
+constexpr int DIN[NL] = {IN, HID, HID, HID, HID};
+constexpr int DOUT[NL] = {HID, HID, HID, HID, OUT};
+constexpr int DESC = 16;
+
+constexpr uint64_t w_off(int l) {
+  uint64_t o = 0;
+  for (int i = 0; i < l; ++i) o += (uint64_t)DOUT[i] * DIN[i] + DOUT[i];
+  return o;
+}
+constexpr uint64_t b_off(int l) { return w_off(l) + (uint64_t)DOUT[l] * DIN[l]; }
+constexpr uint64_t N_PARAMS = w_off(NL);
+
+typedef __nv_bfloat16 bf16;
+
+// ---------------------------------------------------------------- tensor-core GEMM
+// C[M x N] (fp32, ldc) = sum_k A(m, k) B(k, n), A(m,k) = A_COL ? A[k*lda + m] : A[m*lda + k],
+// B(k,n) = B_KN ? B[k*ldb + n] : B[n*ldb + k]. 64x64 CTA tile, 32-deep K steps, 4 warps of 32x32,
+// operands staged K-contiguous in shared memory, mma.sync.m16n8k16 bf16 -> fp32. Split-K over
+// gridDim.z writes partial tiles to C + z * M * ldc (reduced afterwards in a fixed order).
+constexpr int GBM = 64, GBN = 64, GBK = 32, GPAD = 8;
+
+__device__ __forceinline__ void mma_bf16(float* d, const uint32_t* a, const uint32_t* b) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, {%0,%1,%2,%3};\n"
+      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
+
+template <bool A_COL, bool B_KN>
+__global__ void __launch_bounds__(128) k_gemm(const bf16* __restrict__ A, int lda, const bf16* __restrict__ B, int ldb,
+                                              float* __restrict__ C, int ldc, int M, int N, int K, int k_per_split) {
+  __shared__ __align__(16) bf16 As[GBM][GBK + GPAD];
+  __shared__ __align__(16) bf16 Bs[GBN][GBK + GPAD];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int wm = warp >> 1, wn = warp & 1;
+  const int m0 = blockIdx.y * GBM, n0 = blockIdx.x * GBN;
+  const int kbeg = blockIdx.z * k_per_split;
+  const int kend = min(K, kbeg + k_per_split);
+  float acc[2][4][4];
+#pragma unroll
+  for (int i = 0; i < 2; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+#pragma unroll
+      for (int q = 0; q < 4; ++q) acc[i][j][q] = 0.0f;
+  const bf16 zero = __float2bfloat16(0.0f);
+  for (int k0 = kbeg; k0 < kend; k0 += GBK) {
+    // stage A tile (64 x 32) as As[m][k]
+#pragma unroll
+    for (int e = 0; e < (GBM * GBK) / 128; ++e) {
+      int idx = e * 128 + tid;
+      int m, k;
+      if (A_COL) { m = idx % GBM; k = idx / GBM; } else { k = idx % GBK; m = idx / GBK; }
+      int gm = m0 + m, gk = k0 + k;
+      bf16 v = zero;
+      if (gm < M && gk < kend) v = A_COL ? A[(size_t)gk * lda + gm] : A[(size_t)gm * lda + gk];
+      As[m][k] = v;
+    }
+    // stage B tile (32 x 64) as Bs[n][k]
+#pragma unroll
+    for (int e = 0; e < (GBN * GBK) / 128; ++e) {
+      int idx = e * 128 + tid;
+      int n, k;
+      if (B_KN) { n = idx % GBN; k = idx / GBN; } else { k = idx % GBK; n = idx / GBK; }
+      int gn = n0 + n, gk = k0 + k;
+      bf16 v = zero;
+      if (gn < N && gk < kend) v = B_KN ? B[(size_t)gk * ldb + gn] : B[(size_t)gn * ldb + gk];
+      Bs[n][k] = v;
+    }
+    __syncthreads();
+    const int g = lane >> 2, t = lane & 3;
+#pragma unroll
+    for (int ks = 0; ks < GBK; ks += 16) {
+      uint32_t af[2][4], bfr[4][2];
+#pragma unroll
+      for (int mi = 0; mi < 2; ++mi) {
+        int r = wm * 32 + mi * 16 + g;
+        af[mi][0] = *reinterpret_cast<const uint32_t*>(&As[r][ks + 2 * t]);
+        af[mi][1] = *reinterpret_cast<const uint32_t*>(&As[r + 8][ks + 2 * t]);
+        af[mi][2] = *reinterpret_cast<const uint32_t*>(&As[r][ks + 8 + 2 * t]);
+        af[mi][3] = *reinterpret_cast<const uint32_t*>(&As[r + 8][ks + 8 + 2 * t]);
+      }
+#pragma unroll
+      for (int ni = 0; ni < 4; ++ni) {
+        int c = wn * 32 + ni * 8 + g;
+        bfr[ni][0] = *reinterpret_cast<const uint32_t*>(&Bs[c][ks + 2 * t]);
+        bfr[ni][1] = *reinterpret_cast<const uint32_t*>(&Bs[c][ks + 8 + 2 * t]);
+      }
+#pragma unroll
+      for (int mi = 0; mi < 2; ++mi)
+#pragma unroll
+        for (int ni = 0; ni < 4; ++ni) mma_bf16(acc[mi][ni], af[mi], bfr[ni]);
+    }
+    __syncthreads();
+  }
+  float* Cz = C + (size_t)blockIdx.z * M * ldc;
+  const int g = lane >> 2, t = lane & 3;
+#pragma unroll
+  for (int mi = 0; mi < 2; ++mi)
+#pragma unroll
+    for (int ni = 0; ni < 4; ++ni) {
+      int r = m0 + wm * 32 + mi * 16 + g;
+      int c = n0 + wn * 32 + ni * 8 + 2 * t;
+      if (r < M && c < N) Cz[(size_t)r * ldc + c] = acc[mi][ni][0];
+      if (r < M && c + 1 < N) Cz[(size_t)r * ldc + c + 1] = acc[mi][ni][1];
+      if (r + 8 < M && c < N) Cz[(size_t)(r + 8) * ldc + c] = acc[mi][ni][2];
+      if (r + 8 < M && c + 1 < N) Cz[(size_t)(r + 8) * ldc + c + 1] = acc[mi][ni][3];
+    }
+}
+
+// Sum of `splits` partial [n] arrays in a fixed order.
+__global__ void k_reduce_splits(const float* __restrict__ part, int splits, size_t n, float* __restrict__ out) {
+  size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  float s = 0.0f;
+  for (int z = 0; z < splits; ++z) s += part[(size_t)z * n + i];
+  out[i] = s;
+}
+
+// ---------------------------------------------------------------- elementwise kernels
+__device__ __forceinline__ float gelu(float x) { return 0.5f * x * (1.0f + erff(x * 0.70710678118654752f)); }
+__device__ __forceinline__ float gelu_grad(float x) {
+  float cdf = 0.5f * (1.0f + erff(x * 0.70710678118654752f));
+  float pdf = 0.3989422804014327f * expf(-0.5f * x * x);
+  return cdf + x * pdf;
+}
+
+// Z += b; A = bf16(gelu(Z)) (hidden layers) or Z += b only (output layer, A = nullptr).
+__global__ void k_bias_act(float* __restrict__ Z, const float* __restrict__ b, int rows, int cols, bf16* __restrict__ A) {
+  size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i >= (size_t)rows * cols) return;
+  float z = Z[i] + b[i % cols];
+  Z[i] = z;
+  if (A) A[i] = __float2bfloat16(gelu(z));
+}
+
+// loss_b = 1 - cos(y, t); dY = d(mean loss)/dy (bf16). Block-reduced loss sum.
+__global__ void k_cos_loss(const float* __restrict__ Y, const float* __restrict__ T, int rows, float inv_batch, bf16* __restrict__ dY,
+                           float* __restrict__ loss_sum) {
+  __shared__ float red[8];
+  int b = blockIdx.x * blockDim.x + threadIdx.x;
+  float l = 0.0f;
+  if (b < rows) {
+    V3 y = v3(Y[3 * b], Y[3 * b + 1], Y[3 * b + 2]);
+    V3 t = v3(T[3 * b], T[3 * b + 1], T[3 * b + 2]);
+    float yy = y.x * y.x + y.y * y.y + y.z * y.z;
+    V3 g;
+    if (yy < 1e-20f) {
+      l = 1.0f;
+      g = t * (-inv_batch);
+    } else {
+      float ny = sqrtf(yy);
+      float c = (y.x * t.x + y.y * t.y + y.z * t.z) / ny;
+      l = 1.0f - c;
+      g = (t / ny - y * (c / yy)) * (-inv_batch);
+    }
+    dY[3 * b] = __float2bfloat16(g.x);
+    dY[3 * b + 1] = __float2bfloat16(g.y);
+    dY[3 * b + 2] = __float2bfloat16(g.z);
+  }
+  for (int o = 16; o > 0; o >>= 1) l += __shfl_xor_sync(0xffffffffu, l, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = l;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    float s = 0.0f;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += red[w];
+    atomicAdd(loss_sum, s);
+  }
+}
+
+// Output layer gradient as fp32 too (for its bias): dYf = dY (already scaled).
+__global__ void k_bf16_to_f32(const bf16* __restrict__ x, size_t n, float* __restrict__ y) {
+  size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i < n) y[i] = __bfloat162float(x[i]);
+}
+
+// dZ = dA * gelu'(Z): fp32 (bias gradient) and bf16 (GEMM operand)
+__global__ void k_gelu_back(const float* __restrict__ dA, const float* __restrict__ Z, size_t n, float* __restrict__ dZf,
+                            bf16* __restrict__ dZ) {
+  size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  float g = dA[i] * gelu_grad(Z[i]);
+  dZf[i] = g;
+  dZ[i] = __float2bfloat16(g);
+}
+
+// db[c] = sum over rows of dZ[r][c], fixed order
+__global__ void k_colsum(const float* __restrict__ dZ, int rows, int cols, float* __restrict__ db) {
+  int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= cols) return;
+  float s = 0.0f;
+  for (int r = 0; r < rows; ++r) s += dZ[(size_t)r * cols + c];
+  db[c] = s;
+}
+
+__global__ void k_adam(float* __restrict__ w, const float* __restrict__ g, float* __restrict__ m, float* __restrict__ v, size_t n, float lr,
+                       float b1, float b2, float eps, float c1, float c2) {
+  size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  float gi = g[i];
+  float mi = b1 * m[i] + (1.0f - b1) * gi;
+  float vi = b2 * v[i] + (1.0f - b2) * gi * gi;
+  m[i] = mi;
+  v[i] = vi;
+  w[i] -= lr * (mi / c1) / (sqrtf(vi / c2) + eps);
+}
+
+__global__ void k_f32_to_bf16(const float* __restrict__ x, size_t n, bf16* __restrict__ y) {
+  size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i < n) y[i] = __float2bfloat16(x[i]);
+}
+
+// Unit direction from the network output; falls back to the reference default (the relative
+// translation in the features, else +x) for degenerate outputs.
+__global__ void k_normalize_dirs(const float* __restrict__ Y, const float* __restrict__ feat, size_t n, float* __restrict__ dirs) {
+  size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  V3 y = v3(Y[3 * k], Y[3 * k + 1], Y[3 * k + 2]);
+  float yy = dot(y, y);
+  V3 d;
+  if (yy > 1e-12f && isfinite(yy)) d = y / sqrtf(yy);
+  else {
+    V3 t = v3(feat[k * IN + 4], feat[k * IN + 5], feat[k * IN + 6]);
+    float tt = dot(t, t);
+    d = tt > 1.1920929e-7f * 1.1920929e-7f ? t / sqrtf(tt) : v3(1.f, 0.f, 0.f);
+  }
+  dirs[3 * k] = d.x;
+  dirs[3 * k + 1] = d.y;
+  dirs[3 * k + 2] = d.z;
+}
+
+__global__ void k_features_to_bf16(const float* __restrict__ f, size_t n, bf16* __restrict__ x) {
+  size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i < n * IN) x[i] = __float2bfloat16(f[i]);
+}
+
+// ---------------------------------------------------------------- features
+// Principal moments: eigenvalues of a symmetric 3x3 matrix (closed form), descending.
+__device__ void sym_eig3(float a00, float a01, float a02, float a11, float a12, float a22, float* e) {
+  float p1 = a01 * a01 + a02 * a02 + a12 * a12;
+  if (p1 <= 1e-30f) {
+    float d[3] = {a00, a11, a22};
+    for (int i = 0; i < 2; ++i)
+      for (int j = 0; j < 2 - i; ++j)
+        if (d[j] < d[j + 1]) { float t = d[j]; d[j] = d[j + 1]; d[j + 1] = t; }
+    e[0] = d[0]; e[1] = d[1]; e[2] = d[2];
+    return;
+  }
+  float q = (a00 + a11 + a22) / 3.0f;
+  float p2 = (a00 - q) * (a00 - q) + (a11 - q) * (a11 - q) + (a22 - q) * (a22 - q) + 2.0f * p1;
+  float p = sqrtf(p2 / 6.0f);
+  float b00 = (a00 - q) / p, b11 = (a11 - q) / p, b22 = (a22 - q) / p, b01 = a01 / p, b02 = a02 / p, b12 = a12 / p;
+  float det = b00 * (b11 * b22 - b12 * b12) - b01 * (b01 * b22 - b12 * b02) + b02 * (b01 * b12 - b11 * b02);
+  float r = fminf(fmaxf(det * 0.5f, -1.0f), 1.0f);
+  float phi = acosf(r) / 3.0f;
+  e[0] = q + 2.0f * p * cosf(phi);
+  e[2] = q + 2.0f * p * cosf(phi + 2.0943951023931953f);
+  e[1] = 3.0f * q - e[0] - e[2];
+}
+
+// 16-float shape descriptor: AABB half extents (3), principal second moments of the shape's
+// points (3), vertex count / 256, bounding radius, type one-hot (ball, cuboid, capsule, polyhedron),
+// AABB volume, log(vertex count) / log(256), 2 zeros.
+__global__ void k_shape_desc(const uint32_t* __restrict__ types, const float4* __restrict__ params, const float* __restrict__ pool, uint64_t n,
+                             uint64_t n_vertices, float* __restrict__ desc) {
+  uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  uint32_t t = types[i];
+  float4 p = params[i];
+  float he[3] = {0, 0, 0}, mom[3] = {0, 0, 0}, cnt = 1.0f, rad = 0.0f;
+  if (t == 0) {
+    he[0] = he[1] = he[2] = p.x;
+    mom[0] = mom[1] = mom[2] = 0.2f * p.x * p.x;
+    rad = p.x;
+  } else if (t == 1) {
+    he[0] = p.x; he[1] = p.y; he[2] = p.z;
+    float d[3] = {p.x * p.x / 3.0f, p.y * p.y / 3.0f, p.z * p.z / 3.0f};
+    sym_eig3(d[0], 0.f, 0.f, d[1], 0.f, d[2], mom);
+    cnt = 8.0f;
+    rad = sqrtf(p.x * p.x + p.y * p.y + p.z * p.z);
+  } else if (t == 2) {
+    he[0] = p.y; he[1] = p.x + p.y; he[2] = p.y;
+    sym_eig3(0.25f * p.y * p.y, 0.f, 0.f, p.x * p.x / 3.0f + 0.25f * p.y * p.y, 0.f, 0.25f * p.y * p.y, mom);
+    cnt = 2.0f;
+    rad = p.x + p.y;
+  } else {
+    uint64_t first = __float_as_uint(p.x), c = __float_as_uint(p.y);
+    if (c == 0 || first + c > n_vertices) c = 0;
+    const float* v = pool + 3 * first;
+    float mn[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, mx[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX}, s[3] = {0, 0, 0};
+    for (uint64_t j = 0; j < c; ++j) {
+      for (int d = 0; d < 3; ++d) {
+        float x = v[3 * j + d];
+        mn[d] = fminf(mn[d], x); mx[d] = fmaxf(mx[d], x); s[d] += x;
+      }
+      float r2 = v[3 * j] * v[3 * j] + v[3 * j + 1] * v[3 * j + 1] + v[3 * j + 2] * v[3 * j + 2];
+      rad = fmaxf(rad, sqrtf(r2));
+    }
+    float inv = c ? 1.0f / (float)c : 0.0f;
+    float m[3] = {s[0] * inv, s[1] * inv, s[2] * inv};
+    float cxx = 0, cxy = 0, cxz = 0, cyy = 0, cyz = 0, czz = 0;
+    for (uint64_t j = 0; j < c; ++j) {
+      float x = v[3 * j] - m[0], y = v[3 * j + 1] - m[1], z = v[3 * j + 2] - m[2];
+      cxx += x * x; cxy += x * y; cxz += x * z; cyy += y * y; cyz += y * z; czz += z * z;
+    }
+    sym_eig3(cxx * inv, cxy * inv, cxz * inv, cyy * inv, cyz * inv, czz * inv, mom);
+    for (int d = 0; d < 3; ++d) he[d] = c ? 0.5f * (mx[d] - mn[d]) : 0.0f;
+    cnt = (float)c;
+    t = 3;
+  }
+  float* o = desc + 16 * i;
+  o[0] = he[0]; o[1] = he[1]; o[2] = he[2];
+  o[3] = mom[0]; o[4] = mom[1]; o[5] = mom[2];
+  o[6] = cnt / 256.0f;
+  o[7] = rad;
+  for (int k = 0; k < 4; ++k) o[8 + k] = (t == (uint32_t)k) ? 1.0f : 0.0f;
+  o[12] = 8.0f * he[0] * he[1] * he[2];
+  o[13] = cnt > 0.0f ? logf(cnt) / logf(256.0f) : 0.0f;
+  o[14] = 0.0f;
+  o[15] = 0.0f;
+}
+
+// Pair features: relative pose of b in a's frame (quaternion with w >= 0, translation), desc(a), desc(b), zeros.
+__global__ void k_pair_features(const float* __restrict__ poses, const float* __restrict__ desc, const uint32_t* __restrict__ pairs, uint64_t n,
+                                uint64_t n_shapes, float* __restrict__ f) {
+  uint64_t k = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  uint32_t a = pairs[2 * k], b = pairs[2 * k + 1];
+  float* o = f + k * IN;
+  for (int j = 0; j < IN; ++j) o[j] = 0.0f;
+  if (a >= n_shapes || b >= n_shapes) return;
+  const float* pa = poses + 7 * (size_t)a;
+  const float* pb = poses + 7 * (size_t)b;
+  // q = conj(qa) * qb ; t = conj(qa) (tb - ta)
+  float ai = -pa[0], aj = -pa[1], ak = -pa[2], aw = pa[3];
+  float bi = pb[0], bj = pb[1], bk = pb[2], bw = pb[3];
+  float qi = aw * bi + ai * bw + aj * bk - ak * bj;
+  float qj = aw * bj - ai * bk + aj * bw + ak * bi;
+  float qk = aw * bk + ai * bj - aj * bi + ak * bw;
+  float qw = aw * bw - ai * bi - aj * bj - ak * bk;
+  float sgn = qw < 0.0f ? -1.0f : 1.0f;
+  V3 t = quat_rotate(ai, aj, ak, aw, v3(pb[4] - pa[4], pb[5] - pa[5], pb[6] - pa[6]));
+  o[0] = sgn * qi; o[1] = sgn * qj; o[2] = sgn * qk; o[3] = sgn * qw;
+  o[4] = t.x; o[5] = t.y; o[6] = t.z;
+  for (int j = 0; j < DESC; ++j) { o[7 + j] = desc[16 * (size_t)a + j]; o[7 + DESC + j] = desc[16 * (size_t)b + j]; }
+}
+
+uint64_t splitmix(uint64_t& s) {
+  uint64_t z = (s += 0x9E3779B97F4A7C15ull);
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+
+}  // namespace
+
+struct parrygpu_mlp {
+  DevBuf w, g, m, v, wb;  // fp32 masters, grads, Adam moments; bf16 weights
+  DevBuf gpart;           // split-K partial gradients
+  DevBuf x, z[NL], a[NL - 1], dy, df, dz, dzf, dxa, loss;  // activations / gradients of one batch
+  uint64_t cap = 0;       // batch capacity of the activation buffers
+  uint64_t step = 0;      // Adam step
+};
+
+namespace {
+
+template <bool AC, bool BK>
+parrygpu_status gemm(parrygpu_ctx* ctx, const bf16* A, int lda, const bf16* B, int ldb, float* C, int ldc, int M, int N, int K, int splits = 1) {
+  int kps = ((K + splits - 1) / splits + GBK - 1) / GBK * GBK;
+  splits = (K + kps - 1) / kps;
+  dim3 grid(div_up(N, GBN), div_up(M, GBM), splits);
+  k_gemm<AC, BK><<<grid, 128, 0, ctx->stream>>>(A, lda, B, ldb, C, ldc, M, N, K, kps);
+  PG_LAUNCHED(ctx);
+  return PARRYGPU_OK;
+}
+
+parrygpu_status ensure_cap(parrygpu_ctx* ctx, parrygpu_mlp* mlp, uint64_t n) {
+  if (n <= mlp->cap) return PARRYGPU_OK;
+  PG_CUDA(ctx, mlp->x.reserve(n * IN * 2));
+  for (int l = 0; l < NL; ++l) PG_CUDA(ctx, mlp->z[l].reserve(n * DOUT[l] * 4));
+  for (int l = 0; l < NL - 1; ++l) PG_CUDA(ctx, mlp->a[l].reserve(n * HID * 2));
+  PG_CUDA(ctx, mlp->dy.reserve(n * OUT * 2));
+  PG_CUDA(ctx, mlp->df.reserve(n * HID * 4));
+  PG_CUDA(ctx, mlp->dz.reserve(n * HID * 2));
+  PG_CUDA(ctx, mlp->dzf.reserve(n * HID * 4));
+  PG_CUDA(ctx, mlp->dxa.reserve(n * HID * 4));
+  PG_CUDA(ctx, mlp->loss.reserve(16));
+  uint64_t splits = (n + 511) / 512;
+  PG_CUDA(ctx, mlp->gpart.reserve(splits * HID * HID * 4));
+  mlp->cap = n;
+  return PARRYGPU_OK;
+}
+
+inline const bf16* wbf(const parrygpu_mlp* m, int l) { return m->wb.as<bf16>() + w_off(l); }
+
+// Forward of `n` samples whose bf16 features are in mlp->x; output in z[NL-1] (n x 3).
+parrygpu_status forward(parrygpu_ctx* ctx, parrygpu_mlp* mlp, uint64_t n) {
+  const bf16* in = mlp->x.as<bf16>();
+  for (int l = 0; l < NL; ++l) {
+    float* Z = mlp->z[l].as<float>();
+    parrygpu_status s = gemm<false, false>(ctx, in, DIN[l], wbf(mlp, l), DIN[l], Z, DOUT[l], (int)n, DOUT[l], DIN[l]);
+    if (s != PARRYGPU_OK) return s;
+    bf16* A = l < NL - 1 ? mlp->a[l].as<bf16>() : nullptr;
+    k_bias_act<<<div_up(n * DOUT[l], 256), 256, 0, ctx->stream>>>(Z, mlp->w.as<float>() + b_off(l), (int)n, DOUT[l], A);
+    PG_LAUNCHED(ctx);
+    in = A;
+  }
+  return PARRYGPU_OK;
+}
+
+// Backward for the batch in the activation buffers (targets t, n samples); gradients -> mlp->g.
+parrygpu_status backward(parrygpu_ctx* ctx, parrygpu_mlp* mlp, const float* t, uint64_t n, uint64_t denom) {
+  k_cos_loss<<<div_up(n, 256), 256, 0, ctx->stream>>>(mlp->z[NL - 1].as<float>(), t, (int)n, 1.0f / (float)denom, mlp->dy.as<bf16>(),
+                                                      mlp->loss.as<float>());
+  PG_LAUNCHED(ctx);
+  // output layer: dZ = dY
+  const bf16* dZ = mlp->dy.as<bf16>();
+  k_bf16_to_f32<<<div_up(n * OUT, 256), 256, 0, ctx->stream>>>(dZ, n * OUT, mlp->dzf.as<float>());
+  PG_LAUNCHED(ctx);
+  for (int l = NL - 1; l >= 0; --l) {
+    int o = DOUT[l], i = DIN[l];
+    const bf16* Ain = l > 0 ? mlp->a[l - 1].as<bf16>() : mlp->x.as<bf16>();
+    // dW = dZ^T . A_in  (K = batch, split for parallelism; fixed-order reduction)
+    int splits = (int)((n + 511) / 512);
+    parrygpu_status s = gemm<true, true>(ctx, dZ, o, Ain, i, mlp->gpart.as<float>(), i, o, i, (int)n, splits);
+    if (s != PARRYGPU_OK) return s;
+    int kps = (((int)n + splits - 1) / splits + GBK - 1) / GBK * GBK;
+    int used = ((int)n + kps - 1) / kps;
+    k_reduce_splits<<<div_up((size_t)o * i, 256), 256, 0, ctx->stream>>>(mlp->gpart.as<float>(), used, (size_t)o * i,
+                                                                         mlp->g.as<float>() + w_off(l));
+    PG_LAUNCHED(ctx);
+    k_colsum<<<div_up(o, 128), 128, 0, ctx->stream>>>(mlp->dzf.as<float>(), (int)n, o, mlp->g.as<float>() + b_off(l));
+    PG_LAUNCHED(ctx);
+    if (l == 0) break;
+    // dA_in = dZ . W ; dZ_in = dA_in * gelu'(Z_in)
+    s = gemm<false, true>(ctx, dZ, o, wbf(mlp, l), i, mlp->df.as<float>(), i, (int)n, i, o);
+    if (s != PARRYGPU_OK) return s;
+    k_gelu_back<<<div_up(n * i, 256), 256, 0, ctx->stream>>>(mlp->df.as<float>(), mlp->z[l - 1].as<float>(), n * i, mlp->dzf.as<float>(),
+                                                            mlp->dz.as<bf16>());
+    PG_LAUNCHED(ctx);
+    dZ = mlp->dz.as<bf16>();
+  }
+  return PARRYGPU_OK;
+}
+
+parrygpu_status refresh_bf16(parrygpu_ctx* ctx, parrygpu_mlp* mlp) {
+  k_f32_to_bf16<<<div_up(N_PARAMS, 256), 256, 0, ctx->stream>>>(mlp->w.as<float>(), N_PARAMS, mlp->wb.as<bf16>());
+  PG_LAUNCHED(ctx);
+  return PARRYGPU_OK;
+}
+
+parrygpu_status load_features(parrygpu_ctx* ctx, parrygpu_mlp* mlp, const float* d_feat, uint64_t n) {
+  k_features_to_bf16<<<div_up(n * IN, 256), 256, 0, ctx->stream>>>(d_feat, n, mlp->x.as<bf16>());
+  PG_LAUNCHED(ctx);
+  return PARRYGPU_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+uint64_t parrygpu_mlp_param_count(void) { return N_PARAMS; }
+
+parrygpu_status parrygpu_mlp_create(parrygpu_ctx* ctx, uint64_t seed, parrygpu_mlp** out) {
+  if (!ctx || !out) return PARRYGPU_INVALID_ARG;
+  PG_CUDA(ctx, cudaSetDevice(ctx->device));
+  parrygpu_mlp* m = new parrygpu_mlp();
+  std::vector<float> host(N_PARAMS, 0.0f);
+  uint64_t s = seed;
+  for (int l = 0; l < NL; ++l) {
+    float a = std::sqrt(6.0f / (float)(DIN[l] + DOUT[l]));
+    for (uint64_t i = 0; i < (uint64_t)DOUT[l] * DIN[l]; ++i) {
+      double u = (double)(splitmix(s) >> 11) * (1.0 / 9007199254740992.0);
+      host[w_off(l) + i] = (float)((2.0 * u - 1.0) * a);
+    }
+  }
+  cudaError_t e = m->w.reserve(N_PARAMS * 4);
+  if (e == cudaSuccess) e = m->g.reserve(N_PARAMS * 4);
+  if (e == cudaSuccess) e = m->m.reserve(N_PARAMS * 4);
+  if (e == cudaSuccess) e = m->v.reserve(N_PARAMS * 4);
+  if (e == cudaSuccess) e = m->wb.reserve(N_PARAMS * 2);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(m->w.ptr, host.data(), N_PARAMS * 4, cudaMemcpyHostToDevice, ctx->stream);
+  if (e == cudaSuccess) e = cudaMemsetAsync(m->m.ptr, 0, N_PARAMS * 4, ctx->stream);
+  if (e == cudaSuccess) e = cudaMemsetAsync(m->v.ptr, 0, N_PARAMS * 4, ctx->stream);
+  if (e != cudaSuccess) { parrygpu_mlp_destroy(m); return check_cuda(ctx, e, "mlp create"); }
+  parrygpu_status st = refresh_bf16(ctx, m);
+  if (st == PARRYGPU_OK) st = check_cuda(ctx, cudaStreamSynchronize(ctx->stream), "mlp create");
+  if (st != PARRYGPU_OK) { parrygpu_mlp_destroy(m); return st; }
+  *out = m;
+  return PARRYGPU_OK;
+}
+
+void parrygpu_mlp_destroy(parrygpu_mlp* m) {
+  if (!m) return;
+  for (DevBuf* d : {&m->w, &m->g, &m->m, &m->v, &m->wb, &m->gpart, &m->x, &m->dy, &m->df, &m->dz, &m->dzf, &m->dxa, &m->loss}) d->release();
+  for (int l = 0; l < NL; ++l) m->z[l].release();
+  for (int l = 0; l < NL - 1; ++l) m->a[l].release();
+  delete m;
+}
+
+parrygpu_status parrygpu_mlp_features(parrygpu_ctx* ctx, const parrygpu_shapes* shapes, const uint32_t* pairs, uint64_t n_pairs, float* features) {
+  if (!ctx || !shapes) return PARRYGPU_INVALID_ARG;
+  if (n_pairs == 0) return PARRYGPU_OK;
+  if (!pairs || !features) return set_error(ctx, PARRYGPU_INVALID_ARG, "pairs and features are required");
+  PG_CUDA(ctx, cudaSetDevice(ctx->device));
+  const void *t, *p, *q, *v, *dp;
+  parrygpu_status s;
+  if ((s = stage_input(ctx, ctx->stage_in[0], shapes->types, shapes->n * 4, &t)) != PARRYGPU_OK) return s;
+  if ((s = stage_input(ctx, ctx->stage_in[1], shapes->params, shapes->n * 16, &p)) != PARRYGPU_OK) return s;
+  if ((s = stage_input(ctx, ctx->stage_in[2], shapes->poses, shapes->n * 28, &q)) != PARRYGPU_OK) return s;
+  if ((s = stage_input(ctx, ctx->stage_in[3], shapes->vertices, shapes->n_vertices * 12, &v)) != PARRYGPU_OK) return s;
+  if ((s = stage_input(ctx, ctx->stage_in[4], pairs, n_pairs * 8, &dp)) != PARRYGPU_OK) return s;
+  void* d_f;
+  bool copy;
+  if ((s = stage_output(ctx, ctx->stage_out[0], features, n_pairs * IN * 4, &d_f, &copy)) != PARRYGPU_OK) return s;
+  PG_CUDA(ctx, ctx->misc.reserve(64));
+  DevBuf& desc = ctx->stage_out[3];
+  PG_CUDA(ctx, desc.reserve(shapes->n * 16 * 4));
+  k_shape_desc<<<div_up(shapes->n, 128), 128, 0, ctx->stream>>>((const uint32_t*)t, (const float4*)p, (const float*)v, shapes->n, shapes->n_vertices,
+                                                                 desc.as<float>());
+  PG_LAUNCHED(ctx);
+  k_pair_features<<<div_up(n_pairs, 128), 128, 0, ctx->stream>>>((const float*)q, desc.as<float>(), (const uint32_t*)dp, n_pairs, shapes->n,
+                                                                 (float*)d_f);
+  PG_LAUNCHED(ctx);
+  if (copy) PG_CUDA(ctx, cudaMemcpyAsync(features, d_f, n_pairs * IN * 4, cudaMemcpyDeviceToHost, ctx->stream));
+  return parrygpu_sync(ctx);
+}
+
+parrygpu_status parrygpu_mlp_train(parrygpu_ctx* ctx, parrygpu_mlp* mlp, const float* features, const float* targets, uint64_t n, uint32_t epochs,
+                                   uint32_t batch, float lr, float* loss_per_epoch) {
+  if (!ctx || !mlp || !features || !targets || n == 0 || batch == 0) return PARRYGPU_INVALID_ARG;
+  PG_CUDA(ctx, cudaSetDevice(ctx->device));
+  if (!is_device_ptr(features) || !is_device_ptr(targets))
+    return set_error(ctx, PARRYGPU_INVALID_ARG, "parrygpu_mlp_train needs device-resident features and targets");
+  parrygpu_status s = ensure_cap(ctx, mlp, batch);
+  if (s != PARRYGPU_OK) return s;
+  const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
+  KernelTimer kt(ctx, "mlp_train");
+  for (uint32_t ep = 0; ep < epochs; ++ep) {
+    PG_CUDA(ctx, cudaMemsetAsync(mlp->loss.ptr, 0, 4, ctx->stream));
+    for (uint64_t b0 = 0; b0 < n; b0 += batch) {
+      uint64_t nb = n - b0 < batch ? n - b0 : batch;
+      if ((s = load_features(ctx, mlp, features + b0 * IN, nb)) != PARRYGPU_OK) return s;
+      if ((s = forward(ctx, mlp, nb)) != PARRYGPU_OK) return s;
+      if ((s = backward(ctx, mlp, targets + b0 * 3, nb, nb)) != PARRYGPU_OK) return s;
+      mlp->step += 1;
+      float c1 = 1.0f - std::pow(b1, (float)mlp->step), c2 = 1.0f - std::pow(b2, (float)mlp->step);
+      k_adam<<<div_up(N_PARAMS, 256), 256, 0, ctx->stream>>>(mlp->w.as<float>(), mlp->g.as<float>(), mlp->m.as<float>(), mlp->v.as<float>(),
+                                                            N_PARAMS, lr, b1, b2, eps, c1, c2);
+      PG_LAUNCHED(ctx);
+      if ((s = refresh_bf16(ctx, mlp)) != PARRYGPU_OK) return s;
+    }
+    if (loss_per_epoch) {
+      float l;
+      PG_CUDA(ctx, cudaMemcpyAsync(&l, mlp->loss.ptr, 4, cudaMemcpyDeviceToHost, ctx->stream));
+      PG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+      loss_per_epoch[ep] = l / (float)n;
+    }
+  }
+  kt.stop();
+  return parrygpu_sync(ctx);
+}
+
+parrygpu_status parrygpu_mlp_predict(parrygpu_ctx* ctx, const parrygpu_mlp* cmlp, const float* features, uint64_t n, float* dirs) {
+  if (!ctx || !cmlp || !features || !dirs) return PARRYGPU_INVALID_ARG;
+  if (n == 0) return PARRYGPU_OK;
+  parrygpu_mlp* mlp = const_cast<parrygpu_mlp*>(cmlp);
+  PG_CUDA(ctx, cudaSetDevice(ctx->device));
+  const uint64_t chunk = 1 << 18;
+  parrygpu_status s = ensure_cap(ctx, mlp, n < chunk ? n : chunk);
+  if (s != PARRYGPU_OK) return s;
+  const void* d_f;
+  if ((s = stage_input(ctx, ctx->stage_in[7], features, n * IN * 4, &d_f)) != PARRYGPU_OK) return s;
+  void* d_dirs;
+  bool copy;
+  if ((s = stage_output(ctx, ctx->stage_out[2], dirs, n * 12, &d_dirs, &copy)) != PARRYGPU_OK) return s;
+  KernelTimer kt(ctx, "mlp_predict");
+  for (uint64_t b0 = 0; b0 < n; b0 += chunk) {
+    uint64_t nb = n - b0 < chunk ? n - b0 : chunk;
+    if ((s = load_features(ctx, mlp, (const float*)d_f + b0 * IN, nb)) != PARRYGPU_OK) return s;
+    if ((s = forward(ctx, mlp, nb)) != PARRYGPU_OK) return s;
+    k_normalize_dirs<<<div_up(nb, 256), 256, 0, ctx->stream>>>(mlp->z[NL - 1].as<float>(), (const float*)d_f + b0 * IN, nb,
+                                                              (float*)d_dirs + b0 * 3);
+    PG_LAUNCHED(ctx);
+  }
+  kt.stop();
+  if (copy) PG_CUDA(ctx, cudaMemcpyAsync(dirs, d_dirs, n * 12, cudaMemcpyDeviceToHost, ctx->stream));
+  if (copy || d_f != features) return parrygpu_sync(ctx);
+  return PARRYGPU_OK;
+}
+
+parrygpu_status parrygpu_mlp_loss_and_grads(parrygpu_ctx* ctx, const parrygpu_mlp* cmlp, const float* features, const float* targets, uint64_t n,
+                                            float* loss, float* grads) {
+  if (!ctx || !cmlp || !features || !targets || n == 0) return PARRYGPU_INVALID_ARG;
+  parrygpu_mlp* mlp = const_cast<parrygpu_mlp*>(cmlp);
+  PG_CUDA(ctx, cudaSetDevice(ctx->device));
+  parrygpu_status s = ensure_cap(ctx, mlp, n);
+  if (s != PARRYGPU_OK) return s;
+  const void *d_f, *d_t;
+  if ((s = stage_input(ctx, ctx->stage_in[6], features, n * IN * 4, &d_f)) != PARRYGPU_OK) return s;
+  if ((s = stage_input(ctx, ctx->stage_in[7], targets, n * 12, &d_t)) != PARRYGPU_OK) return s;
+  PG_CUDA(ctx, cudaMemsetAsync(mlp->loss.ptr, 0, 4, ctx->stream));
+  if ((s = load_features(ctx, mlp, (const float*)d_f, n)) != PARRYGPU_OK) return s;
+  if ((s = forward(ctx, mlp, n)) != PARRYGPU_OK) return s;
+  if ((s = backward(ctx, mlp, (const float*)d_t, n, n)) != PARRYGPU_OK) return s;
+  float l = 0.0f;
+  PG_CUDA(ctx, cudaMemcpyAsync(&l, mlp->loss.ptr, 4, cudaMemcpyDeviceToHost, ctx->stream));
+  if (grads) PG_CUDA(ctx, cudaMemcpyAsync(grads, mlp->g.ptr, N_PARAMS * 4, cudaMemcpyDefault, ctx->stream));
+  PG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  if (loss) *loss = l / (float)n;
+  return parrygpu_sync(ctx);
+}
+
+parrygpu_status parrygpu_mlp_get_params(parrygpu_ctx* ctx, const parrygpu_mlp* mlp, float* params) {
+  if (!ctx || !mlp || !params) return PARRYGPU_INVALID_ARG;
+  PG_CUDA(ctx, cudaSetDevice(ctx->device));
+  PG_CUDA(ctx, cudaMemcpyAsync(params, mlp->w.ptr, N_PARAMS * 4, cudaMemcpyDefault, ctx->stream));
+  PG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return PARRYGPU_OK;
+}
+
+parrygpu_status parrygpu_mlp_set_params(parrygpu_ctx* ctx, parrygpu_mlp* mlp, const float* params) {
+  if (!ctx || !mlp || !params) return PARRYGPU_INVALID_ARG;
+  PG_CUDA(ctx, cudaSetDevice(ctx->device));
+  PG_CUDA(ctx, cudaMemcpyAsync(mlp->w.ptr, params, N_PARAMS * 4, cudaMemcpyDefault, ctx->stream));
+  parrygpu_status s = refresh_bf16(ctx, mlp);
+  if (s != PARRYGPU_OK) return s;
+  PG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return PARRYGPU_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,66 @@
+"""The warm-start MLP's CUDA training kernels against the float64 numpy oracle (gradient check),
+training progress, checkpoint round trip, and the learned warm start on held-out hull pairs:
+fewer GJK iterations than the reference default direction, same answers within tolerance."""
+import numpy as np
+import pytest
+
+import parry_gb300 as pg
+from parry_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+
+def _unit(v):
+    return v / np.linalg.norm(v, axis=1, keepdims=True)
+
+
+def test_gradients_match_oracle(gpu_ctx):
+    from oracle import mlp_ref
+    rng = np.random.default_rng(3)
+    mlp = pg.WarmStartMLP(gpu_ctx, seed=5)
+    x = rng.normal(size=(512, 48)).astype(np.float32)
+    x[:, 39:] = 0.0
+    t = _unit(rng.normal(size=(512, 3))).astype(np.float32)
+    loss, g = mlp.loss_and_grads(x, t)
+    lref, gref = mlp_ref.loss_and_grads(mlp.get_params(), x, t.astype(np.float64))
+    assert abs(loss - lref) <= 1e-3 * max(1.0, abs(lref))
+    cos = float(np.dot(g, gref) / (np.linalg.norm(g) * np.linalg.norm(gref)))
+    rel = float(np.linalg.norm(g - gref) / np.linalg.norm(gref))
+    print(f"\ngradient check: cos {cos:.6f}, relative error {rel:.3e}")
+    assert cos > 0.9999 and rel < 1e-2
+
+
+def test_training_and_warm_start(gpu_ctx, tmp_path):
+    import torch
+    s_train, p_train = W.hull_pairs(65536, seed=101)
+    s_eval, p_eval = W.hull_pairs(32768, seed=202)
+    mlp = pg.WarmStartMLP(gpu_ctx, seed=1)
+    # labels: the direction the plain GJK/EPA ends with
+    dirs = np.zeros((len(p_train), 3), np.float32)
+    pg.contacts(gpu_ctx, s_train, p_train, 0.0, final_dirs=dirs)
+    f_train = torch.from_numpy(np.ascontiguousarray(mlp.features(s_train, p_train))).cuda()
+    t_train = torch.from_numpy(_unit(dirs.astype(np.float64)).astype(np.float32)).cuda()
+    losses = mlp.train(f_train, t_train, epochs=6, batch=4096, lr=2e-3)
+    print("\nloss per epoch:", losses)
+    assert losses[-1] < 0.5 * losses[0]
+    # checkpoint round trip
+    path = tmp_path / "mlp.bin"
+    mlp.save(path)
+    mlp2 = pg.WarmStartMLP(gpu_ctx, seed=99)
+    mlp2.load(path)
+    np.testing.assert_array_equal(mlp2.get_params(), mlp.get_params())
+    # held-out evaluation
+    fe = mlp.features(s_eval, p_eval)
+    init = mlp2.predict(fe)
+    h0, o0, st0 = pg.contacts(gpu_ctx, s_eval, p_eval, 0.0, want_stats=True)
+    h1, o1, st1 = pg.contacts(gpu_ctx, s_eval, p_eval, 0.0, init_dirs=init, want_stats=True)
+    it0 = (st0["gjk_iters"] + st0["epa_iters"]) / len(p_eval)
+    it1 = (st1["gjk_iters"] + st1["epa_iters"]) / len(p_eval)
+    print(f"GJK iterations per pair plain {st0['gjk_iters'] / len(p_eval):.3f} learned {st1['gjk_iters'] / len(p_eval):.3f}; "
+          f"GJK+EPA plain {it0:.3f} learned {it1:.3f}")
+    assert st1["gjk_iters"] < st0["gjk_iters"]
+    same = (h0 == h1).mean()
+    both = (h0 == 1) & (h1 == 1)
+    dd = np.abs(o0[both, 12] - o1[both, 12])
+    print(f"has-contact agreement {same:.5f}, depth |diff| p99 {np.quantile(dd, 0.99):.2e} max {dd.max():.2e}")
+    assert same > 0.999
