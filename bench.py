@@ -158,6 +158,7 @@ def contacts_section(ctx, stream, steps: int, warmup: int, n_pairs: int, flush) 
     t, prm, pos, pool = s.arrays()
     dev = tuple(torch.from_numpy(np.ascontiguousarray(a)).cuda() for a in (t.view(np.int32), prm, pos, pool))
     dpairs = torch.from_numpy(pairs.view(np.int32)).cuda()
+    contacts_section.device_inputs = (dev, dpairs)
     has = torch.empty(n_pairs, dtype=torch.uint8, device="cuda")
     res = torch.empty((n_pairs, 13), dtype=torch.float32, device="cuda")
     for _ in range(max(1, warmup)):
@@ -231,6 +232,82 @@ def contacts_section(ctx, stream, steps: int, warmup: int, n_pairs: int, flush) 
         "cpu_baseline": {"value": round(sample / cpu_s, 1), "unit": "pairs/s", "cores": threads, "kind": "port",
                          "sample": f"first {sample} pairs; C++ restatement of parry3d f32 query::contact"},
         "matches_oracle_on_sample": same,
+    }
+
+
+def learned_section(ctx, stream, dev_shapes, dev_pairs, n_eval: int, n_train: int, steps: int, flush) -> dict:
+    """Learned warm start: train the MLP on the plain GJK/EPA's final directions of `n_train`
+    held-out-seed hull pairs, then compare plain and learned init directions on the evaluation
+    pairs (the contacts section's pairs): mean iterations, pairs/s (MLP inference included in the
+    learned timing), and agreement of the answers."""
+    import numpy as np
+    import torch
+    import parry_gb300 as pg
+    from parry_gb300 import workloads as W
+
+    s_tr, p_tr = W.hull_pairs(n_train, seed=0x51AB1E)
+    t, prm, pos, pool = s_tr.arrays()
+    dtr = tuple(torch.from_numpy(np.ascontiguousarray(a)).cuda() for a in (t.view(np.int32), prm, pos, pool))
+    dptr = torch.from_numpy(p_tr.view(np.int32)).cuda()
+    labels = torch.empty((n_train, 3), dtype=torch.float32, device="cuda")
+    pg.contacts(ctx, dtr, dptr, 0.0, final_dirs=labels)
+    labels = labels / labels.norm(dim=1, keepdim=True).clamp_min(1e-12)
+    mlp = pg.WarmStartMLP(ctx, seed=7)
+    f_tr = mlp.features(dtr, dptr)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    losses = mlp.train(f_tr, labels, epochs=4, batch=8192, lr=2e-3)
+    torch.cuda.synchronize()
+    train_s = time.perf_counter() - t0
+    del dtr, dptr, f_tr, labels
+    has = torch.empty(n_eval, dtype=torch.uint8, device="cuda")
+    res = torch.empty((n_eval, 13), dtype=torch.float32, device="cuda")
+    has_l = torch.empty_like(has)
+    res_l = torch.empty_like(res)
+
+    def plain():
+        pg.contacts(ctx, dev_shapes, dev_pairs, 0.0, out=(has, res))
+
+    def learned():
+        f = mlp.features(dev_shapes, dev_pairs)
+        d = mlp.predict(f)
+        pg.contacts(ctx, dev_shapes, dev_pairs, 0.0, init_dirs=d, out=(has_l, res_l))
+
+    out = {}
+    for name, fn in (("plain", plain), ("learned", learned)):
+        fn()
+        torch.cuda.synchronize()
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+        for a, b in ev:
+            flush.zero_()
+            a.record(stream)
+            fn()
+            b.record(stream)
+        torch.cuda.synchronize()
+        out[name] = sum(a.elapsed_time(b) for a, b in ev) / steps
+    f = mlp.features(dev_shapes, dev_pairs)
+    d = mlp.predict(f)
+    _, _, st_p = pg.contacts(ctx, dev_shapes, dev_pairs, 0.0, out=(has, res), want_stats=True)
+    _, _, st_l = pg.contacts(ctx, dev_shapes, dev_pairs, 0.0, init_dirs=d, out=(has_l, res_l), want_stats=True)
+    hp, hl = has.cpu().numpy(), has_l.cpu().numpy()
+    both = (hp == 1) & (hl == 1)
+    dd = np.abs(res.cpu().numpy()[both, 12] - res_l.cpu().numpy()[both, 12])
+    ip = (st_p["gjk_iters"]) / n_eval
+    il = (st_l["gjk_iters"]) / n_eval
+    return {
+        "train_pairs": n_train, "eval_pairs": n_eval, "train_seconds": round(train_s, 3),
+        "loss_per_epoch": [round(float(x), 5) for x in losses],
+        "mean_gjk_iterations": {"plain": round(ip, 4), "learned": round(il, 4), "ratio": round(ip / il, 4)},
+        "mean_gjk_plus_epa_iterations": {
+            "plain": round((st_p["gjk_iters"] + st_p["epa_iters"]) / n_eval, 4),
+            "learned": round((st_l["gjk_iters"] + st_l["epa_iters"]) / n_eval, 4)},
+        "pairs_per_s": {"plain": round(n_eval / (out["plain"] / 1e3), 1), "learned": round(n_eval / (out["learned"] / 1e3), 1),
+                        "ratio": round(out["plain"] / out["learned"], 4)},
+        "ms_per_step": {"plain": round(out["plain"], 4), "learned_incl_mlp": round(out["learned"], 4)},
+        "answers": {"has_contact_agreement": round(float((hp == hl).mean()), 6),
+                    "depth_abs_diff_p99": float(np.quantile(dd, 0.99)) if dd.size else 0.0,
+                    "depth_abs_diff_max": float(dd.max()) if dd.size else 0.0},
+        "mlp_flops_per_pair": 2 * (48 * 128 + 3 * 128 * 128 + 128 * 3),
     }
 
 
@@ -359,8 +436,13 @@ def run_gb300(args) -> int:
     e2e_value = world * n / (e2e / 1e3) / 1e6
     same = bool(np.array_equal(feat_p.numpy(), feat.cpu().numpy()))
     contacts = None
+    learned = None
     if args.contact_pairs > 0:
         contacts = contacts_section(ctx, stream, args.steps, args.warmup, args.contact_pairs, flush)
+        if args.train_pairs > 0:
+            dev, dpairs = contacts_section.device_inputs
+            learned = learned_section(ctx, stream, dev, dpairs, args.contact_pairs, args.train_pairs, args.steps, flush)
+        contacts_section.device_inputs = None
 
     if rank == 0:
         cpu_value, stats, threads = cpu_oracle_rays(v, i, rays_h, reps=3)
@@ -390,6 +472,7 @@ def run_gb300(args) -> int:
             "gpu_launches": launches,
             "clocks": clocks,
             "contacts": contacts,
+            "learned_warm_start": learned,
         }
         print(json.dumps(line), flush=True)
     ctx.close()
@@ -407,6 +490,8 @@ def main() -> int:
     ap.add_argument("--n-rays", type=int, default=N_RAYS)
     ap.add_argument("--contact-pairs", type=int, default=1 << 20,
                     help="hull pairs of the GJK/EPA section (0 skips it)")
+    ap.add_argument("--train-pairs", type=int, default=1 << 21,
+                    help="training pairs of the learned warm-start section (0 skips it)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
