@@ -203,6 +203,40 @@ parrygpu_status parrygpu_contacts_with_dirs(parrygpu_ctx* ctx, const parrygpu_sh
                                             float prediction, const float* init_dirs, parrygpu_contact* out, uint8_t* has_contact,
                                             parrygpu_gjk_stats* stats, float* final_dirs);
 
+/* ---- persistent contact manifolds ----
+ * One fixed-size record per pair, the reference's ContactManifold<(), f32-data> with
+ * TrackedContact points (src/query/contact_manifolds/contact_manifold.rs:108-226, 662-800).
+ * 24 points bound every supported pair (face-face cuboids: 4 + 4 vertex and 16 edge contacts). */
+#define PARRYGPU_MANIFOLD_MAX_POINTS 24
+
+typedef struct parrygpu_tracked_contact {
+  float local_p1[3]; /* in shape 1's local frame */
+  float local_p2[3]; /* in shape 2's local frame */
+  float dist;        /* negative when penetrating */
+  uint32_t fid1;     /* PackedFeatureId: kind in bits 30-31 (1 vertex, 2 edge, 3 face, 0 unknown) */
+  uint32_t fid2;
+  float data;        /* user payload (e.g. an impulse), 0 for a new contact, carried by match_contacts */
+} parrygpu_tracked_contact;
+
+typedef struct parrygpu_manifold {
+  uint32_t n_points;
+  uint32_t status;   /* PARRYGPU_OK, or PARRYGPU_UNSUPPORTED_PAIR / PARRYGPU_INVALID_ARG for that pair */
+  float local_n1[3]; /* contact normal in shape 1's frame (also the GJK warm-start cache) */
+  float local_n2[3];
+  parrygpu_tracked_contact points[PARRYGPU_MANIFOLD_MAX_POINTS];
+} parrygpu_manifold;
+
+/* Replaces a loop of DefaultQueryDispatcher::contact_manifold_convex_convex(pos_a^-1 pos_b, a, b,
+ * None, None, prediction, &mut manifold) over the (a, b) rows of `pairs`
+ * (src/query/default_query_dispatcher.rs:749-831), updating `manifolds` (n_pairs records, host or
+ * device memory) in place: try_update_contacts, then the ball-ball, cuboid-cuboid (SAT + feature
+ * clipping), capsule-capsule, convex-ball and polygonal-feature-map (GJK/EPA + clipping) generators,
+ * then match_contacts. Zeroed records are ContactManifold::new(). Pairs with a convex polyhedron or
+ * triangle get status PARRYGPU_UNSUPPORTED_PAIR and keep their record (the reference's
+ * Err(Unsupported) leaves the manifold untouched). stats may be NULL (else the call synchronises). */
+parrygpu_status parrygpu_contact_manifolds(parrygpu_ctx* ctx, const parrygpu_shapes* shapes, const uint32_t* pairs, uint64_t n_pairs,
+                                           float prediction, parrygpu_manifold* manifolds, parrygpu_gjk_stats* stats);
+
 /* ---- learned GJK warm start (no reference counterpart: parry's init_dir hook is its only tie) ----
  * A 39 -> 128 -> 128 -> 128 -> 128 -> 3 MLP (GELU, BF16 weights and activations, FP32 accumulation
  * on the tensor cores) predicts contact_support_map_support_map_with_params's init_dir from the

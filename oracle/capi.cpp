@@ -7,6 +7,7 @@
 #include "ray.hpp"
 #include "contact.hpp"
 #include "shape_ray.hpp"
+#include "manifold.hpp"
 #include <thread>
 #include <vector>
 #include <algorithm>
@@ -191,6 +192,48 @@ void compound_cast(const Compound<R>* c, const float* pose7, const float* rays, 
   if (stats) { stats[0] = wide.load(); stats[1] = leaves.load(); }
 }
 
+
+// Manifold record (same words as parrygpu_manifold): n_points, status, local_n1[3], local_n2[3],
+// then MAX_POINTS x {local_p1[3], local_p2[3], dist, fid1, fid2, data}.
+constexpr int MF_MAX_POINTS = 24;
+constexpr int MF_WORDS = 8 + 10 * MF_MAX_POINTS;
+
+inline float wf(uint32_t w) { float f; std::memcpy(&f, &w, 4); return f; }
+inline uint32_t fw(float f) { uint32_t w; std::memcpy(&w, &f, 4); return w; }
+
+inline void manifold_load(const uint32_t* r, Manifold<float>& m) {
+  uint32_t n = r[0] > (uint32_t)MF_MAX_POINTS ? (uint32_t)MF_MAX_POINTS : r[0];
+  m.local_n1 = Vec3<float>(wf(r[2]), wf(r[3]), wf(r[4]));
+  m.local_n2 = Vec3<float>(wf(r[5]), wf(r[6]), wf(r[7]));
+  m.points.resize(n);
+  for (uint32_t i = 0; i < n; ++i) {
+    const uint32_t* q = r + 8 + 10 * i;
+    TrackedContact<float>& c = m.points[i];
+    c.local_p1 = Vec3<float>(wf(q[0]), wf(q[1]), wf(q[2]));
+    c.local_p2 = Vec3<float>(wf(q[3]), wf(q[4]), wf(q[5]));
+    c.dist = wf(q[6]);
+    c.fid1 = q[7];
+    c.fid2 = q[8];
+    c.data = wf(q[9]);
+  }
+}
+
+inline void manifold_store(const Manifold<float>& m, uint32_t* r) {
+  r[0] = (uint32_t)m.points.size();
+  r[2] = fw(m.local_n1.x); r[3] = fw(m.local_n1.y); r[4] = fw(m.local_n1.z);
+  r[5] = fw(m.local_n2.x); r[6] = fw(m.local_n2.y); r[7] = fw(m.local_n2.z);
+  for (size_t i = 0; i < m.points.size() && i < (size_t)MF_MAX_POINTS; ++i) {
+    uint32_t* q = r + 8 + 10 * i;
+    const TrackedContact<float>& c = m.points[i];
+    q[0] = fw(c.local_p1.x); q[1] = fw(c.local_p1.y); q[2] = fw(c.local_p1.z);
+    q[3] = fw(c.local_p2.x); q[4] = fw(c.local_p2.y); q[5] = fw(c.local_p2.z);
+    q[6] = fw(c.dist);
+    q[7] = c.fid1;
+    q[8] = c.fid2;
+    q[9] = fw(c.data);
+  }
+}
+
 }  // namespace
 
 extern "C" {
@@ -283,6 +326,32 @@ void oracle_compound_cast_rays_f32(void* c, const float* pose7, const float* ray
 void oracle_compound_cast_rays_f64(void* c, const float* pose7, const float* rays, uint64_t n, float max_toi, int solid, int lowest,
                                    int threads, uint32_t* part, double* toi, double* normal, uint64_t* stats) {
   compound_cast<double, double>((Compound<double>*)c, pose7, rays, n, max_toi, solid, lowest, threads, part, toi, normal, stats);
+}
+
+// DefaultQueryDispatcher::contact_manifold_convex_convex per (a, b) row of `pairs`, updating the
+// records in place. Unsupported pairs keep their record and get status 2. stats: gjk_iters,
+// epa_iters, epa_calls, unsupported pairs, largest point count.
+void oracle_manifolds_f32(const uint32_t* types, const float* params, const float* poses, const float* hullv, uint32_t nhv,
+                          uint64_t nshapes, const uint32_t* pairs, uint64_t npairs, float prediction, int threads, uint32_t* records,
+                          uint64_t* stats) {
+  ShapeSet<float> set(types, params, poses, hullv, nhv, nshapes);
+  std::atomic<uint64_t> gi{0}, ei{0}, ec{0}, un{0}, mx{0};
+  parallel_for(npairs, threads, [&](uint64_t k) {
+    uint32_t a = pairs[2 * k], b = pairs[2 * k + 1];
+    uint32_t* r = records + (size_t)MF_WORDS * k;
+    Manifold<float> m;
+    manifold_load(r, m);
+    GjkStats st;
+    Iso<float> pos12 = set.poses[a].inv_mul(set.poses[b]);
+    bool ok = contact_manifold_convex_convex(pos12, set.shapes[a], set.shapes[b], prediction, m, &st);
+    gi += st.gjk_iters; ei += st.epa_iters; ec += st.epa_calls;
+    if (!ok) { un += 1; r[1] = 2; return; }
+    r[1] = 0;
+    uint64_t np = m.points.size(), cur = mx.load();
+    while (np > cur && !mx.compare_exchange_weak(cur, np)) {}
+    manifold_store(m, r);
+  });
+  if (stats) { stats[0] = gi.load(); stats[1] = ei.load(); stats[2] = ec.load(); stats[3] = un.load(); stats[4] = mx.load(); }
 }
 
 uint64_t oracle_pairs_count(void* p) { return ((PairBuf*)p)->v.size() / 2; }

@@ -42,6 +42,7 @@ template <class R> struct PointProj {
   bool is_inside;
   Vec3<R> point;
   int face = -1;  // cuboid: FeatureId::Face(i) when the projection is on a face, -1 otherwise
+  Vec3<R> shift;  // cuboid: the shift do_project_local_point returns (ls = pt + shift)
 };
 
 // point_aabb.rs:9-132 on the cuboid [-h, h] with solid = false (project_local_point_and_get_feature).
@@ -73,6 +74,7 @@ template <class R> inline PointProj<R> project_cuboid(const Vec3<R>& h, const Ve
     out.is_inside = true;
   }
   out.point = ls;
+  out.shift = shift;
   // feature: only the face case is needed (feature_normal_at_point fallback)
   int nz = 0, last_nz = 0;
   for (int i = 0; i < 3; ++i) { if (shift[i] == R(0)) nz++; else last_nz = i; }

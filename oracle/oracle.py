@@ -44,6 +44,7 @@ _SIGS = {
     "oracle_compound_free_f64": (None, [P]),
     "oracle_compound_cast_rays_f32": (None, [P, P, P, U64, F32, I32, I32, I32, P, P, P, P]),
     "oracle_compound_cast_rays_f64": (None, [P, P, P, U64, F32, I32, I32, I32, P, P, P, P]),
+    "oracle_manifolds_f32": (None, [P, P, P, P, U32, U64, P, U64, F32, I32, P, P]),
     "oracle_pairs_count": (U64, [P]),
     "oracle_pairs_copy": (None, [P, P]),
     "oracle_pairs_free": (None, [P]),
@@ -205,6 +206,29 @@ def contacts(shapes, pairs: np.ndarray, prediction: float, init_dirs: np.ndarray
     return has, out, {"gjk_iters": int(st[0]), "epa_iters": int(st[1]), "epa_calls": int(st[2]),
                       "epa_max_faces": int(st[3]), "epa_max_verts": int(st[4]), "epa_max_silhouette": int(st[5]),
                       "support_vertices": int(st[6])}
+
+
+MANIFOLD_MAX_POINTS = 24
+MANIFOLD_WORDS = 8 + 10 * MANIFOLD_MAX_POINTS
+
+
+def empty_manifolds(k: int) -> np.ndarray:
+    """k zeroed manifold records (uint32 words, the parrygpu_manifold layout): ContactManifold::new()."""
+    return np.zeros((k, MANIFOLD_WORDS), np.uint32)
+
+
+def contact_manifolds(shapes, pairs: np.ndarray, prediction: float, records: np.ndarray, threads: int | None = None) -> dict:
+    """DefaultQueryDispatcher::contact_manifold_convex_convex(pos_a^-1 pos_b, a, b, prediction, manifold)
+    for every (a, b) row of `pairs`, updating `records` (k x MANIFOLD_WORDS uint32) in place."""
+    t, prm, pos, pool = _shape_arrays(shapes)
+    pairs = np.ascontiguousarray(pairs, np.uint32).reshape(-1, 2)
+    k = len(pairs)
+    assert records.dtype == np.uint32 and records.shape == (k, MANIFOLD_WORDS) and records.flags.c_contiguous
+    st = np.zeros(5, np.uint64)
+    lib().oracle_manifolds_f32(_p(t), _p(prm), _p(pos), _p(pool), len(pool), len(t), _p(pairs), k, float(prediction),
+                               threads if threads is not None else default_threads(), _p(records), _p(st))
+    return {"gjk_iters": int(st[0]), "epa_iters": int(st[1]), "epa_calls": int(st[2]), "unsupported": int(st[3]),
+            "max_points": int(st[4])}
 
 
 class Compound:

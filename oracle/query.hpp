@@ -28,7 +28,8 @@ namespace oracle {
 template <class R> inline R eps_default() { return std::numeric_limits<R>::epsilon(); }
 template <class R> inline R gjk_eps_tol() { return eps_default<R>() * R(10); }
 
-enum ShapeType : uint32_t { SHAPE_BALL = 0, SHAPE_CUBOID = 1, SHAPE_CAPSULE = 2, SHAPE_CONVEX = 3, SHAPE_TRIANGLE = 4 };
+enum ShapeType : uint32_t { SHAPE_BALL = 0, SHAPE_CUBOID = 1, SHAPE_CAPSULE = 2, SHAPE_CONVEX = 3, SHAPE_TRIANGLE = 4,
+                            SHAPE_SEGMENT_PFM = 5 /* a capsule's axis segment, as its polygonal feature map */ };
 
 // One convex shape. Capsule = Capsule::new_y(half_height, radius): segment (0,-h,0)-(0,h,0).
 template <class R> struct Shape {
@@ -54,6 +55,11 @@ template <class R> struct Shape {
         Vec3<R> a(0, -half_height, 0), b(0, half_height, 0);
         if (dot(d, a) > dot(d, b)) return a + d * radius;
         return b + d * radius;
+      }
+      case SHAPE_SEGMENT_PFM: {
+        // segment.rs:461-467: a if a.dir > b.dir else b
+        Vec3<R> a(0, -half_height, 0), b(0, half_height, 0);
+        return dot(a, dir) > dot(b, dir) ? a : b;
       }
       case SHAPE_TRIANGLE: {
         // triangle.rs:697-715: ties resolve towards the later vertex

@@ -14,6 +14,7 @@ one batched call here:
     TriMesh::cast_ray(m, ray, t, solid)                TriMesh.cast_rays(rays, t, solid, pose)
     Shape::compute_aabb(pos).loosened(m)               shape_aabbs(ctx, shapes, margin)
     query::contact(pos1, g1, pos2, g2, prediction)     contacts(ctx, shapes, pairs, prediction, init_dirs)
+    dispatcher.contact_manifold_convex_convex(...)     contact_manifolds(ctx, shapes, pairs, prediction, manifolds)
     Compound::new(shapes)                              Compound(ctx, shapes)
     Compound::cast_ray_and_get_normal(m, ray, t, s)    Compound.cast_rays_and_get_normal(rays, t, solid, pose)
 
@@ -30,10 +31,11 @@ import numpy as np
 from . import _capi
 from ._capi import ParryGpuError, lib, check
 
-__all__ = ["Context", "Bvh", "TriMesh", "Compound", "ShapeSet", "WarmStartMLP", "shape_aabbs", "contacts", "ParryGpuError",
-           "NO_HIT", "lib"]
+__all__ = ["Context", "Bvh", "TriMesh", "Compound", "ShapeSet", "WarmStartMLP", "shape_aabbs", "contacts", "contact_manifolds",
+           "new_manifolds", "ParryGpuError", "NO_HIT", "lib"]
 
 from .shapes import ShapeSet  # noqa: E402
+from .manifold import new_manifolds, MANIFOLD_DTYPE, RECORD_WORDS  # noqa: E402
 
 NO_HIT = 0xFFFFFFFF
 
@@ -310,6 +312,26 @@ def contacts(ctx: Context, shapes, pairs, prediction: float, init_dirs=None, wan
     if want_stats:
         return has, res, {"gjk_iters": stats.gjk_iterations, "epa_iters": stats.epa_iterations, "epa_calls": stats.epa_calls}
     return has, res
+
+
+def contact_manifolds(ctx: Context, shapes, pairs, prediction: float, manifolds, want_stats: bool = False):
+    """Batched DefaultQueryDispatcher::contact_manifold_convex_convex over the (a, b) rows of `pairs`,
+    updating `manifolds` in place: a numpy array of parry_gb300.manifold.MANIFOLD_DTYPE records (k,),
+    or a torch int32/uint32 tensor of shape (k, RECORD_WORDS) (a CUDA tensor is updated on the device).
+    Returns the stats dict when want_stats."""
+    st = _StagedShapes(shapes)
+    kp, pp = _as_input(pairs, np.uint32)
+    k = int(kp.shape[0]) if kp is not None else 0
+    if _is_torch(manifolds):
+        assert manifolds.is_contiguous() and tuple(manifolds.shape) == (k, RECORD_WORDS) and manifolds.element_size() == 4
+    else:
+        assert manifolds.dtype == MANIFOLD_DTYPE and manifolds.flags.c_contiguous and len(manifolds) == k
+    stats = _capi.ParryGpuGjkStats()
+    check(lib().parrygpu_contact_manifolds(ctx.handle, C.byref(st.struct), pp, k, float(prediction), C.c_void_p(_dptr(manifolds)),
+                                           C.byref(stats) if want_stats else None), ctx.handle)
+    if want_stats:
+        return {"gjk_iters": stats.gjk_iterations, "epa_iters": stats.epa_iterations, "epa_calls": stats.epa_calls}
+    return None
 
 
 class Compound:

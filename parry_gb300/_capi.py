@@ -57,6 +57,7 @@ SIGNATURES: dict[str, tuple] = {
     "parrygpu_shapes_aabbs": (I32, [P, P, F32, P]),
     "parrygpu_contacts": (I32, [P, P, P, U64, F32, P, P, P, P]),
     "parrygpu_contacts_with_dirs": (I32, [P, P, P, U64, F32, P, P, P, P, P]),
+    "parrygpu_contact_manifolds": (I32, [P, P, P, U64, F32, P, P]),
     "parrygpu_mlp_create": (I32, [P, U64, C.POINTER(P)]),
     "parrygpu_mlp_destroy": (None, [P]),
     "parrygpu_mlp_features": (I32, [P, P, P, U64, P]),

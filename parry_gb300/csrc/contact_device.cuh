@@ -1,0 +1,150 @@
+// Device-side pieces shared by the batched contact and contact-manifold kernels: the shape-array
+// view, pair validation, point projections on cuboids and capsules, and the EPA work queue.
+//   point projections  src/query/point/point_aabb.rs:9-132, src/query/point/point_capsule.rs:7-51
+// (paths relative to the parry repository).
+#pragma once
+#include "internal.hpp"
+#include "gjk_device.cuh"
+
+namespace pg {
+
+constexpr int QUEUE_WORDS = 40;  // pair, dim, 4 x CSO (9 words), pad
+
+struct ShapeArrays {
+  const uint32_t* types;
+  const float4* params;
+  const float* poses;
+  const float* pool;
+  uint64_t n_shapes;
+  uint64_t n_vertices;
+};
+
+// Rejects out-of-range pair indices and vertex ranges (reported as a capacity / argument error
+// through the context's error word; the pair reports no contact).
+__device__ __forceinline__ bool valid_pair(const ShapeArrays& sh, uint32_t a, uint32_t b) {
+  if (a >= sh.n_shapes || b >= sh.n_shapes) return false;
+  uint32_t ids[2] = {a, b};
+#pragma unroll
+  for (int k = 0; k < 2; ++k) {
+    uint32_t t = sh.types[ids[k]];
+    if (t > SH_TRIANGLE) return false;
+    if (t == SH_CONVEX || t == SH_TRIANGLE) {
+      float4 p = sh.params[ids[k]];
+      uint64_t first = __float_as_uint(p.x), cnt = __float_as_uint(p.y);
+      if (cnt == 0 || first + cnt > sh.n_vertices || (t == SH_TRIANGLE && cnt != 3)) return false;
+    }
+  }
+  return true;
+}
+
+struct PointProj {
+  bool inside;
+  V3 point;
+  int face;
+  V3 shift;  // cuboid: the shift of do_project_local_point (point = pt + shift)
+};
+
+// point_aabb.rs:9-132 on [-h, h] with solid = false.
+__device__ __forceinline__ PointProj project_cuboid(V3 h, V3 pt) {
+  V3 mins = -h, maxs = h;
+  V3 mins_pt = mins - pt, pt_maxs = pt - maxs;
+  V3 z = v3(0.f, 0.f, 0.f);
+  V3 shift = vmax(mins_pt, z) - vmax(pt_maxs, z);
+  bool inside = shift.x == 0.0f && shift.y == 0.0f && shift.z == 0.0f;
+  PointProj out;
+  V3 ls;
+  if (!inside) {
+    ls = pt + shift;
+    out.inside = false;
+  } else {
+    float best = -FLT_MAX;
+    bool is_mins = false;
+    int best_id = 0;
+    float mp[3] = {mins_pt.x, mins_pt.y, mins_pt.z}, pm[3] = {pt_maxs.x, pt_maxs.y, pt_maxs.z};
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      if (mp[i] < pm[i]) {
+        if (pm[i] > best) { best_id = i; is_mins = false; best = pm[i]; }
+      } else if (mp[i] > best) { best_id = i; is_mins = true; best = mp[i]; }
+    }
+    float s[3] = {0.f, 0.f, 0.f};
+    s[best_id] = is_mins ? best : -best;
+    shift = v3(s[0], s[1], s[2]);
+    ls = pt + shift;
+    out.inside = true;
+  }
+  out.point = ls;
+  out.shift = shift;
+  out.face = -1;
+  float sh[3] = {shift.x, shift.y, shift.z}, l[3] = {ls.x, ls.y, ls.z}, mn[3] = {mins.x, mins.y, mins.z}, mx[3] = {maxs.x, maxs.y, maxs.z};
+  int nz = 0, last_nz = 0;
+#pragma unroll
+  for (int i = 0; i < 3; ++i) { if (sh[i] == 0.0f) nz++; else last_nz = i; }
+  if (nz == 3) {
+    for (int i = 0; i < 3; ++i) {
+      if (l[i] > mx[i] - EPS) { out.face = i; break; }
+      if (l[i] <= mn[i] + EPS) { out.face = i + 3; break; }
+    }
+  } else if (nz == 2) {
+    float center = (mn[last_nz] + mx[last_nz]) * 0.5f;
+    out.face = l[last_nz] < center ? last_nz + 3 : last_nz;
+  }
+  return out;
+}
+
+// point_capsule.rs:7-51 with solid = false.
+__device__ __forceinline__ PointProj project_capsule(float hh, float radius, V3 pt) {
+  Loc loc;
+  V3 a = v3(0.f, -hh, 0.f), b = v3(0.f, hh, 0.f);
+  V3 proj = project_segment(a, b, pt, &loc);
+  V3 dir;
+  float dist;
+  PointProj out;
+  out.face = -1;
+  if (try_normalize(pt - proj, EPS, &dir, &dist)) {
+    out.inside = dist <= radius;
+    out.point = proj + dir * radius;
+    return out;
+  }
+  V3 sd;
+  out.inside = true;
+  if (try_normalize(b - a, EPS, &sd)) {
+    float sign = copysignf(1.0f, sd.z);
+    float aa = -1.0f / (sign + sd.z);
+    float bb = sd.x * sd.y * aa;
+    V3 t = v3(1.0f + sign * sd.x * sd.x * aa, sign * bb, -sign * sd.x);
+    out.point = proj + t * radius;
+  } else {
+    out.point = proj + v3(0.f, radius, 0.f);
+  }
+  return out;
+}
+
+__device__ __forceinline__ void enqueue(uint32_t* __restrict__ queue, unsigned long long* __restrict__ qcount, uint64_t k, const Simplex& s) {
+  unsigned long long slot = atomicAdd(qcount, 1ull);
+  uint32_t* e = queue + (size_t)slot * QUEUE_WORDS;
+  e[0] = (uint32_t)k;
+  e[1] = (uint32_t)s.dim;
+  for (int i = 0; i <= s.dim; ++i) {
+    float* f = reinterpret_cast<float*>(e + 2 + 9 * i);
+    f[0] = s.v[i].p.x; f[1] = s.v[i].p.y; f[2] = s.v[i].p.z;
+    f[3] = s.v[i].o1.x; f[4] = s.v[i].o1.y; f[5] = s.v[i].o1.z;
+    f[6] = s.v[i].o2.x; f[7] = s.v[i].o2.y; f[8] = s.v[i].o2.z;
+  }
+}
+
+// Queue entry layout: pair index, simplex dimension, then dim + 1 CSO points (p, o1, o2).
+__device__ __forceinline__ void dequeue(const uint32_t* __restrict__ e, uint64_t* k, Simplex* s) {
+  *k = e[0];
+  simplex_reset(*s, CSO{});
+  s->dim = (int)e[1];
+  for (int i = 0; i <= s->dim; ++i) {
+    const float* f = reinterpret_cast<const float*>(e + 2 + 9 * i);
+    s->v[i] = CSO{v3(f[0], f[1], f[2]), v3(f[3], f[4], f[5]), v3(f[6], f[7], f[8])};
+  }
+}
+
+// Stages a parrygpu_shapes description on the device (host arrays are copied, device arrays used in place).
+parrygpu_status stage_shapes(parrygpu_ctx* ctx, const parrygpu_shapes* s, ShapeArrays* out);
+
+}  // namespace pg

@@ -122,6 +122,7 @@ parrygpu_status parrygpu_sync(parrygpu_ctx* ctx) {
     if (err & ERR_STACK_OVERFLOW) return set_error(ctx, PARRYGPU_STACK_OVERFLOW, "traversal stack overflow");
     if (err & ERR_CAPACITY) return set_error(ctx, PARRYGPU_CAPACITY_EXCEEDED, "output capacity exceeded");
     if (err & ERR_POLYTOPE_FULL) return set_error(ctx, PARRYGPU_CAPACITY_EXCEEDED, "EPA polytope capacity exceeded");
+    if (err & ERR_BAD_INDEX) return set_error(ctx, PARRYGPU_INVALID_ARG, "a pair index or vertex range is out of bounds");
   }
   return PARRYGPU_OK;
 }

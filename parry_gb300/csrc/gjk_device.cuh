@@ -15,7 +15,9 @@
 
 namespace pg {
 
-enum : uint32_t { SH_BALL = 0, SH_CUBOID = 1, SH_CAPSULE = 2, SH_CONVEX = 3, SH_TRIANGLE = 4, SH_ORIGIN = 255 };
+// SH_SEGMENT is a capsule's axis segment (its polygonal feature map, shape.rs:855-857): only
+// built on the device, never a type of the C ABI.
+enum : uint32_t { SH_BALL = 0, SH_CUBOID = 1, SH_CAPSULE = 2, SH_CONVEX = 3, SH_TRIANGLE = 4, SH_SEGMENT = 5, SH_ORIGIN = 255 };
 
 constexpr float EPS = 1.1920929e-7f;         // f32::EPSILON
 constexpr float GJK_EPS_TOL = EPS * 10.0f;   // gjk::eps_tol()
@@ -94,6 +96,11 @@ __device__ __forceinline__ V3 local_support(const ShapeDev& s, V3 dir) {
       V3 a = v3(0.f, -s.a, 0.f), b = v3(0.f, s.a, 0.f);
       if (dot(d, a) > dot(d, b)) return a + d * s.b;
       return b + d * s.b;
+    }
+    case SH_SEGMENT: {
+      // segment.rs:461-467
+      V3 a = v3(0.f, -s.a, 0.f), b = v3(0.f, s.a, 0.f);
+      return dot(a, dir) > dot(b, dir) ? a : b;
     }
     case SH_TRIANGLE: {
       V3 p0 = ldv(s.pts), p1 = ldv(s.pts + 3), p2 = ldv(s.pts + 6);

@@ -15,6 +15,7 @@ enum : uint32_t {
   ERR_CAPACITY = 1u << 1,
   ERR_TIMEOUT = 1u << 2,
   ERR_POLYTOPE_FULL = 1u << 3,
+  ERR_BAD_INDEX = 1u << 4,
 };
 
 // A grow-only device buffer owned by a context or a handle.

@@ -85,3 +85,44 @@ def mixed_scene(n: int, seed: int, extent: float = 6.0):
         else:
             s.add_triangle(*rng.uniform(-1.2, 1.2, (3, 3)), pose)
     return s
+
+
+def primitive_scene(n: int, seed: int, extent: float = 4.0):
+    """(types, params, poses) of balls, cuboids and capsules (types cycling 0, 1, 2) at random poses:
+    the shape kinds with contact-manifold generators."""
+    rng = np.random.default_rng(seed)
+    types = (np.arange(n) % 3).astype(np.uint32)
+    params = np.zeros((n, 4), np.float32)
+    for i in range(n):
+        if types[i] == 0:
+            params[i, 0] = rng.uniform(0.3, 1.5)
+        elif types[i] == 1:
+            params[i, :3] = rng.uniform(0.3, 1.5, 3)
+        else:
+            params[i, :2] = (rng.uniform(0.2, 1.2), rng.uniform(0.2, 0.8))
+    q = rng.normal(size=(n, 4))
+    q /= np.linalg.norm(q, axis=1, keepdims=True)
+    poses = np.concatenate([q, rng.uniform(-extent, extent, (n, 3))], axis=1).astype(np.float32)
+    return types, params, poses
+
+
+def moved_poses(poses: np.ndarray, frame: int, seed: int, step: float = 0.01, angle: float = 0.01) -> np.ndarray:
+    """Poses after `frame` steps of a small per-shape drift and spin (renormalised quaternions)."""
+    rng = np.random.default_rng(seed)
+    n = len(poses)
+    v = rng.normal(size=(n, 3)) * step
+    w = rng.normal(size=(n, 3)) * angle
+    out = poses.astype(np.float64).copy()
+    out[:, 4:7] += v * frame
+    # q <- exp(w * frame / 2) * q
+    th = np.linalg.norm(w, axis=1) * frame
+    ax = w / np.maximum(np.linalg.norm(w, axis=1, keepdims=True), 1e-30)
+    dq = np.concatenate([ax * np.sin(th / 2)[:, None], np.cos(th / 2)[:, None]], axis=1)
+    qi, qj, qk, qw = out[:, 0], out[:, 1], out[:, 2], out[:, 3]
+    di, dj, dk, dw = dq[:, 0], dq[:, 1], dq[:, 2], dq[:, 3]
+    out[:, 0] = dw * qi + di * qw + dj * qk - dk * qj
+    out[:, 1] = dw * qj - di * qk + dj * qw + dk * qi
+    out[:, 2] = dw * qk + di * qj - dj * qi + dk * qw
+    out[:, 3] = dw * qw - di * qi - dj * qj - dk * qk
+    out[:, :4] /= np.linalg.norm(out[:, :4], axis=1, keepdims=True)
+    return out.astype(np.float32)

@@ -1,0 +1,125 @@
+"""Persistent contact manifolds on the GPU against the oracle: bit-exact records over several frames."""
+import json
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from parry_gb300 import manifold as M
+from parry_gb300.shapes import ShapeSet, pose7, BALL, CUBOID
+from tests._contact_cases import primitive_scene, moved_poses
+from tests._helpers import brute_force_pairs
+
+pytestmark = pytest.mark.gpu
+
+KA = json.loads((Path(__file__).parent / "golden" / "known_answers.json").read_text())
+
+
+def assert_records_equal(got: np.ndarray, want: np.ndarray):
+    """Same status and point count; bit-identical normals and valid points."""
+    np.testing.assert_array_equal(got["status"], want["status"])
+    np.testing.assert_array_equal(got["n_points"], want["n_points"])
+    gw, ww = M.as_words(got), M.as_words(want)
+    np.testing.assert_array_equal(gw[:, 2:8], ww[:, 2:8])
+    n = want["n_points"].astype(np.int64)
+    valid = np.arange(M.MAX_POINTS)[None, :] < n[:, None]
+    gp = gw[:, 8:].reshape(len(got), M.MAX_POINTS, 10)
+    wp = ww[:, 8:].reshape(len(want), M.MAX_POINTS, 10)
+    bad = np.nonzero(np.any(gp[valid] != wp[valid], axis=1))[0]
+    assert len(bad) == 0, f"{len(bad)} points differ"
+
+
+def _both(O, pg, ctx, shapes, pairs, pred, rec_gpu, rec_cpu):
+    pg.contact_manifolds(ctx, shapes, pairs, pred, rec_gpu)
+    O.contact_manifolds(shapes, pairs, pred, M.as_words(rec_cpu))
+
+
+def test_doc_test_cases(gpu_ctx, oracle_lib):
+    import parry_gb300 as pg
+    O = oracle_lib
+    for key in ("manifold_ball_ball_overlap", "manifold_ball_ball_prediction"):
+        c = KA[key]
+        s = ShapeSet.from_arrays(np.array([BALL, BALL], np.uint32), np.array([[c["radius1"], 0, 0, 0], [c["radius2"], 0, 0, 0]], np.float32),
+                                 np.array([pose7(), pose7(c["pos12"])], np.float32))
+        g, w = M.new_manifolds(1), M.new_manifolds(1)
+        _both(O, pg, gpu_ctx, s, np.array([[0, 1]], np.uint32), c["prediction"], g, w)
+        assert g["n_points"][0] == 1
+        assert_records_equal(g, w)
+    c = KA["manifold_cuboid_stack"]
+    s = ShapeSet.from_arrays(np.array([CUBOID, CUBOID], np.uint32),
+                             np.array([[*c["half_extents1"], 0], [*c["half_extents2"], 0]], np.float32),
+                             np.array([pose7(), pose7(c["pos12"])], np.float32))
+    g, w = M.new_manifolds(1), M.new_manifolds(1)
+    _both(O, pg, gpu_ctx, s, np.array([[0, 1]], np.uint32), c["prediction"], g, w)
+    assert g["n_points"][0] >= 4
+    assert_records_equal(g, w)
+
+
+@pytest.mark.parametrize("seed", [1, 2])
+def test_frames_bit_exact(gpu_ctx, oracle_lib, seed):
+    """Several frames of a drifting scene: every pair kind, warm records, data carried by feature ids."""
+    import parry_gb300 as pg
+    O = oracle_lib
+    t, p, q0 = primitive_scene(1500, seed, extent=6.0)
+    pred = 0.05
+    pairs = brute_force_pairs(O.shape_aabbs(ShapeSet.from_arrays(t, p, q0), 0.4))
+    assert len(pairs) > 2000
+    kinds = {(int(t[a]), int(t[b])) for a, b in pairs}
+    assert len(kinds) >= 8
+    g, w = M.new_manifolds(len(pairs)), M.new_manifolds(len(pairs))
+    for f in range(5):
+        shapes = ShapeSet.from_arrays(t, p, moved_poses(q0, f, seed + 100, step=0.02, angle=0.02))
+        _both(O, pg, gpu_ctx, shapes, pairs, pred, g, w)
+        assert_records_equal(g, w)
+        assert np.all(g["status"] == M.STATUS_OK)
+        # a solver would store impulses in `data`; give both the same values
+        vals = (np.arange(len(pairs) * M.MAX_POINTS, dtype=np.float32).reshape(-1, M.MAX_POINTS) + f * 0.5)
+        g["points"]["data"] = vals
+        w["points"]["data"] = vals
+    assert int(g["n_points"].sum()) > len(pairs) // 4
+
+
+def test_device_records_in_place(gpu_ctx, oracle_lib):
+    """Records resident in device memory (a CUDA tensor) are updated in place, as host records are."""
+    torch = pytest.importorskip("torch")
+    import parry_gb300 as pg
+    O = oracle_lib
+    t, p, q = primitive_scene(800, 9, extent=5.0)
+    shapes = ShapeSet.from_arrays(t, p, q)
+    pairs = brute_force_pairs(O.shape_aabbs(shapes, 0.2))
+    w = M.new_manifolds(len(pairs))
+    d = torch.zeros((len(pairs), M.RECORD_WORDS), dtype=torch.int32, device="cuda")
+    tt, pp, qq, pool = shapes.arrays()
+    dev_shapes = (torch.from_numpy(tt.view(np.int32)).cuda(), torch.from_numpy(pp).cuda(), torch.from_numpy(qq).cuda(),
+                  torch.from_numpy(pool).cuda())
+    dpairs = torch.from_numpy(pairs.view(np.int32)).cuda()
+    for f in range(3):
+        q2 = moved_poses(q, f, 77)
+        dev_shapes = (dev_shapes[0], dev_shapes[1], torch.from_numpy(q2).cuda(), dev_shapes[3])
+        pg.contact_manifolds(gpu_ctx, dev_shapes, dpairs, 0.02, d)
+        gpu_ctx.sync()
+        O.contact_manifolds(ShapeSet.from_arrays(t, p, q2), pairs, 0.02, M.as_words(w))
+        got = M.as_records(d.cpu().numpy().view(np.uint32).copy())
+        assert_records_equal(got, w)
+
+
+def test_unsupported_and_invalid(gpu_ctx, oracle_lib):
+    import parry_gb300 as pg
+    O = oracle_lib
+    s = ShapeSet()
+    s.add_ball(1.0)
+    s.add_convex(np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0], [0, 0, 1]], np.float32), pose7((0.5, 0, 0)))
+    s.add_cuboid((1, 1, 1), pose7((0, 1.5, 0)))
+    pairs = np.array([[0, 1], [0, 2]], np.uint32)
+    g, w = M.new_manifolds(2), M.new_manifolds(2)
+    g["n_points"][0] = 3
+    w["n_points"][0] = 3
+    _both(O, pg, gpu_ctx, s, pairs, 0.0, g, w)
+    assert g["status"][0] == M.STATUS_UNSUPPORTED and g["n_points"][0] == 3
+    assert g["status"][1] == M.STATUS_OK and g["n_points"][1] == 1
+    assert_records_equal(g, w)
+    bad = np.array([[0, 7]], np.uint32)
+    r = M.new_manifolds(1)
+    with pytest.raises(pg.ParryGpuError):
+        pg.contact_manifolds(gpu_ctx, s, bad, 0.0, r)
+    assert r["status"][0] == 1  # PARRYGPU_INVALID_ARG
