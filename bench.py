@@ -235,6 +235,136 @@ def contacts_section(ctx, stream, steps: int, warmup: int, n_pairs: int, flush) 
     }
 
 
+def manifolds_section(ctx, stream, steps: int, warmup: int, n_pairs: int, flush) -> dict:
+    """Persistent contact manifolds on ball/cuboid/capsule pairs drifting frame to frame: each step
+    updates every pair's record in place at the next frame's poses (device-resident), plus a cold
+    update from empty records, the end-to-end call through host records, a bit-exact check against
+    the oracle on a sample, and the oracle CPU baseline."""
+    import numpy as np
+    import torch
+    import parry_gb300 as pg
+    from parry_gb300 import workloads as W
+    from parry_gb300 import manifold as M
+    from oracle import build as ob
+    ob.build()
+    from oracle import oracle as O
+
+    t, prm, pos0, pairs = W.primitive_pairs(n_pairs)
+    frames = warmup + steps + 1
+    dt_ = torch.from_numpy(t.view(np.int32)).cuda()
+    dp_ = torch.from_numpy(prm).cuda()
+    dpool = torch.zeros((0, 3), dtype=torch.float32, device="cuda")
+    dpairs = torch.from_numpy(pairs.view(np.int32)).cuda()
+    host_poses = [W.drifted_poses(pos0, f) for f in range(frames)]
+    dposes = [torch.from_numpy(p).cuda() for p in host_poses]
+    rec = torch.zeros((n_pairs, M.RECORD_WORDS), dtype=torch.int32, device="cuda")
+    pred = 0.02
+    # cold: empty records, every generator from scratch
+    cold_ms = []
+    for _ in range(3):
+        rec.zero_()
+        flush.zero_()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        pg.contact_manifolds(ctx, (dt_, dp_, dposes[0], dpool), dpairs, pred, rec)
+        b.record(stream)
+        torch.cuda.synchronize()
+        cold_ms.append(a.elapsed_time(b))
+    for f in range(1, warmup + 1):
+        pg.contact_manifolds(ctx, (dt_, dp_, dposes[f], dpool), dpairs, pred, rec)
+    torch.cuda.synchronize()
+    before_last = None
+    ctx.enable_kernel_timing(True)
+    ctx.reset_kernel_timing()
+    l0 = ctx.kernel_launches
+    st_ev = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    en_ev = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    for k in range(steps):
+        f = warmup + 1 + k
+        if k == steps - 1:
+            torch.cuda.synchronize()
+            before_last = rec[: min(n_pairs, 65536)].cpu().numpy().view(np.uint32).copy()
+        flush.zero_()
+        st_ev[k].record(stream)
+        pg.contact_manifolds(ctx, (dt_, dp_, dposes[f], dpool), dpairs, pred, rec)
+        en_ev[k].record(stream)
+    torch.cuda.synchronize()
+    ms = sum(a.elapsed_time(b) for a, b in zip(st_ev, en_ev)) / steps
+    m_ms, m_n = ctx.kernel_time("manifolds_main")
+    e_ms, e_n = ctx.kernel_time("manifolds_epa")
+    ctx.enable_kernel_timing(False)
+    launches = ctx.kernel_launches - l0
+    last_f = warmup + steps
+    after = rec.cpu().numpy().view(np.uint32).copy()
+    recs_after = M.as_records(after)
+    # bit-exact check on a sample: the oracle applies the last frame to the same starting records
+    sample = len(before_last)
+    shapes_last = pg.ShapeSet.from_arrays(t, prm, host_poses[last_f])
+    chk = before_last.copy()
+    O.contact_manifolds(shapes_last, pairs[:sample], pred, chk)
+    g, w = recs_after[:sample], M.as_records(chk)
+    n = w["n_points"].astype(np.int64)
+    valid = np.arange(M.MAX_POINTS)[None, :] < n[:, None]
+    gp = after[:sample, 8:].reshape(sample, M.MAX_POINTS, 10)
+    wp = chk[:, 8:].reshape(sample, M.MAX_POINTS, 10)
+    same = bool(np.array_equal(g["n_points"], w["n_points"]) and np.array_equal(after[:sample, :8], chk[:, :8])
+                and np.array_equal(gp[valid], wp[valid]))
+    # end to end: pinned host records and shape arrays, both copies inside the timed region
+    host_rec = torch.from_numpy(after.view(np.int32)).pin_memory()
+    ht = torch.from_numpy(t.view(np.int32)).pin_memory()
+    hp = torch.from_numpy(prm).pin_memory()
+    hq = [torch.from_numpy(p).pin_memory() for p in host_poses]
+    hpool = torch.zeros((0, 3), dtype=torch.float32)
+    hpairs = torch.from_numpy(pairs.view(np.int32)).pin_memory()
+    pg.contact_manifolds(ctx, (ht, hp, hq[0], hpool), hpairs, pred, host_rec)
+    e2e = []
+    for k in range(steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        pg.contact_manifolds(ctx, (ht, hp, hq[(k + 1) % frames], hpool), hpairs, pred, host_rec)
+        e2e.append((time.perf_counter() - t0) * 1e3)
+    e2e_ms = statistics.mean(e2e)
+    h2d = t.nbytes + prm.nbytes + host_poses[0].nbytes + pairs.nbytes + after.nbytes
+    d2h = after.nbytes
+    # oracle CPU baseline on a bounded sample (one frame update from the same records)
+    threads = os.cpu_count() or 1
+    csample = min(n_pairs, 262144)
+    base = after[:csample].copy()
+    t0 = time.perf_counter()
+    O.contact_manifolds(pg.ShapeSet.from_arrays(t, prm, host_poses[0]), pairs[:csample], pred, base, threads=threads)
+    cpu_s = time.perf_counter() - t0
+    npts = recs_after["n_points"].astype(np.float64)
+    mean_pts = float(npts.mean())
+    # algorithmic bytes per pair: pair 8 B, two shapes (type 4 + params 16 + pose 28), record
+    # header and live points read and written (32 B + 40 B per point each way)
+    bytes_per_pair = 8 + 2 * 48 + 2 * (32 + 40 * mean_pts)
+    kernel_ms = m_ms / max(m_n, 1) + e_ms / max(e_n, 1)
+    achieved = bytes_per_pair * n_pairs / (kernel_ms / 1e3) / 1e9
+    peak, peak_kind = measured_peak_hbm()
+    kinds = np.bincount((t[pairs[:, 0]] * 3 + t[pairs[:, 1]]).astype(np.int64), minlength=9)
+    return {
+        "workload": "ball/cuboid/capsule pairs (uniform kinds), random relative pose at distance U[0.5, 3], drifting "
+                    "frame to frame (v U[-0.3, 0.3]^3, w U[-0.5, 0.5]^3, dt 1/60), prediction 0.02",
+        "pairs": n_pairs, "metric": "manifold pair updates/s", "value": round(n_pairs / (ms / 1e3), 1), "unit": "pairs/s",
+        "ms_per_step": round(ms, 4), "cold_ms": round(min(cold_ms), 4),
+        "cold_value": round(n_pairs / (min(cold_ms) / 1e3), 1),
+        "kernel_ms": {"main": round(m_ms / max(m_n, 1), 4), "epa": round(e_ms / max(e_n, 1), 4)},
+        "gpu_launches": launches,
+        "mean_points": round(mean_pts, 3), "pairs_with_points": round(float((npts > 0).mean()), 4),
+        "pair_kinds": [int(x) for x in kinds],
+        "e2e": {"value": round(n_pairs / (e2e_ms / 1e3), 1), "unit": "pairs/s", "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h), "ms_per_step": round(e2e_ms, 3)},
+        "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                     "frac": round(achieved / peak, 5), "peak_source": peak_kind, "bytes_per_pair": round(bytes_per_pair, 1),
+                     "bytes_model": "pair 8 + 2 x (type 4 + params 16 + pose 28) + record header and live points read and "
+                                    "written (2 x (32 + 40 x mean points))"},
+        "cpu_baseline": {"value": round(csample / cpu_s, 1), "unit": "pairs/s", "cores": threads, "kind": "port",
+                         "sample": f"one frame update of the first {csample} pairs; C++ restatement of parry3d f32"},
+        "matches_oracle_on_sample": same, "oracle_sample": sample,
+    }
+
+
 def learned_section(ctx, stream, dev_shapes, dev_pairs, n_eval: int, n_train: int, steps: int, flush) -> dict:
     """Learned warm start: train the MLP on the plain GJK/EPA's final directions of `n_train`
     held-out-seed hull pairs, then compare plain and learned init directions on the evaluation
@@ -437,6 +567,9 @@ def run_gb300(args) -> int:
     same = bool(np.array_equal(feat_p.numpy(), feat.cpu().numpy()))
     contacts = None
     learned = None
+    manifolds = None
+    if args.manifold_pairs > 0:
+        manifolds = manifolds_section(ctx, stream, args.steps, args.warmup, args.manifold_pairs, flush)
     if args.contact_pairs > 0:
         contacts = contacts_section(ctx, stream, args.steps, args.warmup, args.contact_pairs, flush)
         if args.train_pairs > 0:
@@ -473,6 +606,7 @@ def run_gb300(args) -> int:
             "clocks": clocks,
             "contacts": contacts,
             "learned_warm_start": learned,
+            "manifolds": manifolds,
         }
         print(json.dumps(line), flush=True)
     ctx.close()
@@ -490,6 +624,8 @@ def main() -> int:
     ap.add_argument("--n-rays", type=int, default=N_RAYS)
     ap.add_argument("--contact-pairs", type=int, default=1 << 20,
                     help="hull pairs of the GJK/EPA section (0 skips it)")
+    ap.add_argument("--manifold-pairs", type=int, default=1 << 20,
+                    help="ball/cuboid/capsule pairs of the contact-manifold section (0 skips it)")
     ap.add_argument("--train-pairs", type=int, default=1 << 21,
                     help="training pairs of the learned warm-start section (0 skips it)")
     args = ap.parse_args()

@@ -140,3 +140,50 @@ def broadphase_shapes(n: int = 131072, extent: float = 200.0, seed: int = 0x9A77
     poses[:, 5] = uniform(seed, 9, n, -extent, extent)
     poses[:, 6] = uniform(seed, 10, n, -extent, extent)
     return ShapeSet.from_arrays(types, params.astype(np.float32), poses.astype(np.float32))
+
+
+def primitive_pairs(n_pairs: int, seed: int = 0x9A77E3):
+    """Contact-manifold workload: pair k = (shape 2k at the identity, shape 2k+1 at a random relative
+    pose: uniform rotation, translation = unit direction x U[0.5, 3]). Types are balls, cuboids and
+    capsules drawn uniformly per shape (all six pair kinds); ball radius U[0.5, 1], cuboid half
+    extents U[0.4, 1] each, capsule half height U[0.2, 0.8] and radius U[0.3, 0.6].
+    Returns (types u32, params f32 (n, 4), poses f32 (n, 7), pairs (n_pairs, 2) u32)."""
+    from .shapes import BALL, CUBOID, CAPSULE
+    n = 2 * n_pairs
+    types = (splitmix64(seed, 1, n) % np.uint64(3)).astype(np.uint32)
+    params = np.zeros((n, 4), np.float64)
+    ball, cub, cap = types == BALL, types == CUBOID, types == CAPSULE
+    params[ball, 0] = uniform(seed, 2, n, 0.5, 1.0)[ball]
+    for j in range(3):
+        params[cub, j] = uniform(seed, 3 + j, n, 0.4, 1.0)[cub]
+    params[cap, 0] = uniform(seed, 6, n, 0.2, 0.8)[cap]
+    params[cap, 1] = uniform(seed, 7, n, 0.3, 0.6)[cap]
+    poses = np.zeros((n, 7), np.float64)
+    poses[:, 3] = 1.0
+    poses[1::2, 0:4] = _unit_quats(seed, 20, n_pairs)
+    poses[1::2, 4:7] = _sphere_dirs(seed, 30, n_pairs) * uniform(seed, 32, n_pairs, 0.5, 3.0)[:, None]
+    pairs = np.stack([np.arange(0, n, 2), np.arange(1, n, 2)], axis=1).astype(np.uint32)
+    return types, params.astype(np.float32), poses.astype(np.float32), pairs
+
+
+def drifted_poses(poses: np.ndarray, frame: int, seed: int = 0x9A77E4, dt: float = 1.0 / 60.0, speed: float = 0.3,
+                  spin: float = 0.5) -> np.ndarray:
+    """Poses after `frame` steps of dt: each shape moves with a velocity U([-speed, speed]^3) and
+    spins with an angular velocity U([-spin, spin]^3) (exponential map, renormalised)."""
+    n = len(poses)
+    v = np.stack([uniform(seed, 40 + j, n, -speed, speed) for j in range(3)], axis=1)
+    w = np.stack([uniform(seed, 43 + j, n, -spin, spin) for j in range(3)], axis=1)
+    out = poses.astype(np.float64).copy()
+    out[:, 4:7] += v * (dt * frame)
+    ang = w * (dt * frame)
+    th = np.linalg.norm(ang, axis=1)
+    ax = ang / np.maximum(th, 1e-30)[:, None]
+    s, c = np.sin(th / 2), np.cos(th / 2)
+    di, dj, dk, dw = ax[:, 0] * s, ax[:, 1] * s, ax[:, 2] * s, c
+    qi, qj, qk, qw = out[:, 0].copy(), out[:, 1].copy(), out[:, 2].copy(), out[:, 3].copy()
+    out[:, 0] = dw * qi + di * qw + dj * qk - dk * qj
+    out[:, 1] = dw * qj - di * qk + dj * qw + dk * qi
+    out[:, 2] = dw * qk + di * qj - dj * qi + dk * qw
+    out[:, 3] = dw * qw - di * qi - dj * qj - dk * qk
+    out[:, :4] /= np.linalg.norm(out[:, :4], axis=1, keepdims=True)
+    return out.astype(np.float32)
