@@ -249,11 +249,14 @@ def manifolds_section(ctx, stream, steps: int, warmup: int, n_pairs: int, flush)
     ob.build()
     from oracle import oracle as O
 
-    t, prm, pos0, pairs = W.primitive_pairs(n_pairs)
+    t, prm, pos0, pool, poly, pairs = W.primitive_pairs(n_pairs)
     frames = warmup + steps + 1
     dt_ = torch.from_numpy(t.view(np.int32)).cuda()
     dp_ = torch.from_numpy(prm).cuda()
-    dpool = torch.zeros((0, 3), dtype=torch.float32, device="cuda")
+    dpool = torch.from_numpy(pool).cuda()
+    hulls, topo = poly
+    dpoly = (torch.from_numpy(hulls.view(np.int32)).cuda(),
+             {k: torch.from_numpy(v.view(np.int32) if v.dtype == np.uint32 else v).cuda() for k, v in topo.items()})
     dpairs = torch.from_numpy(pairs.view(np.int32)).cuda()
     host_poses = [W.drifted_poses(pos0, f) for f in range(frames)]
     dposes = [torch.from_numpy(p).cuda() for p in host_poses]
@@ -266,12 +269,12 @@ def manifolds_section(ctx, stream, steps: int, warmup: int, n_pairs: int, flush)
         flush.zero_()
         a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         a.record(stream)
-        pg.contact_manifolds(ctx, (dt_, dp_, dposes[0], dpool), dpairs, pred, rec)
+        pg.contact_manifolds(ctx, (dt_, dp_, dposes[0], dpool, dpoly), dpairs, pred, rec)
         b.record(stream)
         torch.cuda.synchronize()
         cold_ms.append(a.elapsed_time(b))
     for f in range(1, warmup + 1):
-        pg.contact_manifolds(ctx, (dt_, dp_, dposes[f], dpool), dpairs, pred, rec)
+        pg.contact_manifolds(ctx, (dt_, dp_, dposes[f], dpool, dpoly), dpairs, pred, rec)
     torch.cuda.synchronize()
     before_last = None
     ctx.enable_kernel_timing(True)
@@ -286,7 +289,7 @@ def manifolds_section(ctx, stream, steps: int, warmup: int, n_pairs: int, flush)
             before_last = rec[: min(n_pairs, 65536)].cpu().numpy().view(np.uint32).copy()
         flush.zero_()
         st_ev[k].record(stream)
-        pg.contact_manifolds(ctx, (dt_, dp_, dposes[f], dpool), dpairs, pred, rec)
+        pg.contact_manifolds(ctx, (dt_, dp_, dposes[f], dpool, dpoly), dpairs, pred, rec)
         en_ev[k].record(stream)
     torch.cuda.synchronize()
     ms = sum(a.elapsed_time(b) for a, b in zip(st_ev, en_ev)) / steps
@@ -299,7 +302,7 @@ def manifolds_section(ctx, stream, steps: int, warmup: int, n_pairs: int, flush)
     recs_after = M.as_records(after)
     # bit-exact check on a sample: the oracle applies the last frame to the same starting records
     sample = len(before_last)
-    shapes_last = pg.ShapeSet.from_arrays(t, prm, host_poses[last_f])
+    shapes_last = pg.ShapeSet.from_arrays(t, prm, host_poses[last_f], pool, poly)
     chk = before_last.copy()
     O.contact_manifolds(shapes_last, pairs[:sample], pred, chk)
     g, w = recs_after[:sample], M.as_records(chk)
@@ -314,25 +317,28 @@ def manifolds_section(ctx, stream, steps: int, warmup: int, n_pairs: int, flush)
     ht = torch.from_numpy(t.view(np.int32)).pin_memory()
     hp = torch.from_numpy(prm).pin_memory()
     hq = [torch.from_numpy(p).pin_memory() for p in host_poses]
-    hpool = torch.zeros((0, 3), dtype=torch.float32)
+    hpool = torch.from_numpy(pool).pin_memory()
+    hpoly = (torch.from_numpy(hulls.view(np.int32)).pin_memory(),
+             {k: torch.from_numpy(v.view(np.int32) if v.dtype == np.uint32 else v).pin_memory() for k, v in topo.items()})
     hpairs = torch.from_numpy(pairs.view(np.int32)).pin_memory()
-    pg.contact_manifolds(ctx, (ht, hp, hq[0], hpool), hpairs, pred, host_rec)
+    pg.contact_manifolds(ctx, (ht, hp, hq[0], hpool, hpoly), hpairs, pred, host_rec)
     e2e = []
     for k in range(steps):
         flush.zero_()
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        pg.contact_manifolds(ctx, (ht, hp, hq[(k + 1) % frames], hpool), hpairs, pred, host_rec)
+        pg.contact_manifolds(ctx, (ht, hp, hq[(k + 1) % frames], hpool, hpoly), hpairs, pred, host_rec)
         e2e.append((time.perf_counter() - t0) * 1e3)
     e2e_ms = statistics.mean(e2e)
-    h2d = t.nbytes + prm.nbytes + host_poses[0].nbytes + pairs.nbytes + after.nbytes
+    h2d = (t.nbytes + prm.nbytes + host_poses[0].nbytes + pool.nbytes + hulls.nbytes + sum(v.nbytes for v in topo.values())
+           + pairs.nbytes + after.nbytes)
     d2h = after.nbytes
     # oracle CPU baseline on a bounded sample (one frame update from the same records)
     threads = os.cpu_count() or 1
     csample = min(n_pairs, 262144)
     base = after[:csample].copy()
     t0 = time.perf_counter()
-    O.contact_manifolds(pg.ShapeSet.from_arrays(t, prm, host_poses[0]), pairs[:csample], pred, base, threads=threads)
+    O.contact_manifolds(pg.ShapeSet.from_arrays(t, prm, host_poses[0], pool, poly), pairs[:csample], pred, base, threads=threads)
     cpu_s = time.perf_counter() - t0
     npts = recs_after["n_points"].astype(np.float64)
     mean_pts = float(npts.mean())
@@ -342,10 +348,10 @@ def manifolds_section(ctx, stream, steps: int, warmup: int, n_pairs: int, flush)
     kernel_ms = m_ms / max(m_n, 1) + e_ms / max(e_n, 1)
     achieved = bytes_per_pair * n_pairs / (kernel_ms / 1e3) / 1e9
     peak, peak_kind = measured_peak_hbm()
-    kinds = np.bincount((t[pairs[:, 0]] * 3 + t[pairs[:, 1]]).astype(np.int64), minlength=9)
+    kinds = np.bincount((t[pairs[:, 0]] * 4 + t[pairs[:, 1]]).astype(np.int64), minlength=16)
     return {
-        "workload": "ball/cuboid/capsule pairs (uniform kinds), random relative pose at distance U[0.5, 3], drifting "
-                    "frame to frame (v U[-0.3, 0.3]^3, w U[-0.5, 0.5]^3, dt 1/60), prediction 0.02",
+        "workload": "ball/cuboid/capsule/convex-hull(16-64 points) pairs (uniform kinds), random relative pose at distance "
+                    "U[0.5, 3], drifting frame to frame (v U[-0.3, 0.3]^3, w U[-0.5, 0.5]^3, dt 1/60), prediction 0.02",
         "pairs": n_pairs, "metric": "manifold pair updates/s", "value": round(n_pairs / (ms / 1e3), 1), "unit": "pairs/s",
         "ms_per_step": round(ms, 4), "cold_ms": round(min(cold_ms), 4),
         "cold_value": round(n_pairs / (min(cold_ms) / 1e3), 1),

@@ -150,11 +150,43 @@ typedef enum parrygpu_shape_type {
   PARRYGPU_BALL = 0,     /* Ball::new(r)                        params {r, 0, 0, 0} */
   PARRYGPU_CUBOID = 1,   /* Cuboid::new(half_extents)           params {hx, hy, hz, 0} */
   PARRYGPU_CAPSULE = 2,  /* Capsule::new_y(half_height, radius) params {half_height, radius, 0, 0} */
-  PARRYGPU_CONVEX = 3,   /* ConvexPolyhedron vertex cloud       params {first vertex, vertex count (u32 bits), 0, 0} */
+  PARRYGPU_CONVEX = 3,   /* ConvexPolyhedron                    params {first vertex, vertex count, hull + 1, 0} (u32 bits);
+                          * hull + 1 = 0: a vertex cloud without topology (support maps only, no manifolds) */
   PARRYGPU_TRIANGLE = 4  /* Triangle::new(a, b, c)              params {first vertex (u32 bits), 3, 0, 0} */
 } parrygpu_shape_type;
 
-/* A set of shapes with their poses (SoA). Convex and triangle vertices live in one pool. */
+/* Topology of ConvexPolyhedron shapes (src/shape/convex_polyhedron.rs:172-185), all hulls
+ * concatenated. Ids stored in the index arrays are hull-local, as the reference's feature ids are.
+ *   hulls          n_hulls x 8 u32: first vertex (in the shapes' vertex pool), vertex count,
+ *                  first face, face count, first edge, edge count, ok, reserved
+ *   face_normals   n_faces x 3            Face::normal
+ *   face_ranges    n_faces x 2 u32        first entry (global) in face_vertices / face_edges, count
+ *   face_vertices  n_face_entries         vertices_adj_to_face (hull-local vertex ids)
+ *   face_edges     n_face_entries         edges_adj_to_face (hull-local edge ids)
+ *   vertex_ranges  n_vertices x 2 u32     per vertex of the shapes' pool: first entry (global) in
+ *                                         vertex_faces / vertex_edges, count (Vertex)
+ *   vertex_faces   n_vertex_entries       faces_adj_to_vertex (hull-local face ids)
+ *   vertex_edges   n_vertex_entries       edges_adj_to_vertex (hull-local edge ids)
+ *   edge_dirs      n_edges x 3            Edge::dir */
+typedef struct parrygpu_polyhedra {
+  uint64_t n_hulls;
+  const uint32_t* hulls;
+  uint64_t n_faces;
+  const float* face_normals;
+  const uint32_t* face_ranges;
+  uint64_t n_face_entries;
+  const uint32_t* face_vertices;
+  const uint32_t* face_edges;
+  const uint32_t* vertex_ranges;
+  uint64_t n_vertex_entries;
+  const uint32_t* vertex_faces;
+  const uint32_t* vertex_edges;
+  uint64_t n_edges;
+  const float* edge_dirs;
+} parrygpu_polyhedra;
+
+/* A set of shapes with their poses (SoA). Convex and triangle vertices live in one pool.
+ * polyhedra (may be NULL) carries the topology the manifold generators need for CONVEX shapes. */
 typedef struct parrygpu_shapes {
   uint64_t n;
   const uint32_t* types;   /* n */
@@ -162,7 +194,25 @@ typedef struct parrygpu_shapes {
   const float* poses;      /* n x 7 (pose7) */
   const float* vertices;   /* n_vertices x 3 */
   uint64_t n_vertices;
+  const parrygpu_polyhedra* polyhedra;
 } parrygpu_shapes;
+
+/* ConvexPolyhedron::from_convex_hull (src/shape/convex_polyhedron.rs:264-268) for n_hulls point
+ * clouds (hull h = points[first[h] .. first[h] + count[h]]), on the host with `threads` threads
+ * (0 = all). The triangulation comes from this library's own hull builder (the reference's
+ * quickhull numbering is not reproduced: identical triangles for points in general position, other
+ * face / vertex ids); from_convex_mesh (:390-639) is restated step for step. A hull whose points span
+ * less than 3-D keeps its points with no topology (ok = 0). Read the result with
+ * parrygpu_polyhedra_sizes (points, faces, face entries, vertex entries, edges) and
+ * parrygpu_polyhedra_copy (buffers sized from those counts; hulls: n_hulls x 8). */
+typedef struct parrygpu_polyhedra_builder parrygpu_polyhedra_builder;
+parrygpu_status parrygpu_polyhedra_build(const float* points, const uint32_t* first, const uint32_t* count, uint64_t n_hulls,
+                                         uint32_t threads, parrygpu_polyhedra_builder** out);
+parrygpu_status parrygpu_polyhedra_sizes(const parrygpu_polyhedra_builder* b, uint64_t* sizes);
+parrygpu_status parrygpu_polyhedra_copy(const parrygpu_polyhedra_builder* b, float* points, uint32_t* hulls, float* face_normals,
+                                        uint32_t* face_ranges, uint32_t* face_vertices, uint32_t* face_edges, uint32_t* vertex_ranges,
+                                        uint32_t* vertex_faces, uint32_t* vertex_edges, float* edge_dirs);
+void parrygpu_polyhedra_builder_destroy(parrygpu_polyhedra_builder* b);
 
 /* Same layout as the reference's Contact (src/query/contact/contact.rs:71-105), world space. */
 typedef struct parrygpu_contact {

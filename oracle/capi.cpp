@@ -86,10 +86,54 @@ struct PairBuf {
 };
 
 // A shape set in the C-ABI layout: types[n], params[n x 4], poses[n x 7], convex vertex pool.
+// Same field layout as parrygpu_polyhedra (the library's C ABI for ConvexPolyhedron topology).
+struct PolyIn {
+  uint64_t n_hulls;
+  const uint32_t* hulls;
+  uint64_t n_faces;
+  const float* face_normals;
+  const uint32_t* face_ranges;
+  uint64_t n_face_entries;
+  const uint32_t* face_vertices;
+  const uint32_t* face_edges;
+  const uint32_t* vertex_ranges;
+  uint64_t n_vertex_entries;
+  const uint32_t* vertex_faces;
+  const uint32_t* vertex_edges;
+  uint64_t n_edges;
+  const float* edge_dirs;
+};
+
 template <class R> struct ShapeSet {
   std::vector<Shape<R>> shapes;
   std::vector<Iso<R>> poses;
   std::vector<Vec3<R>> pool;
+  std::vector<HullTopo> topos;
+  // Attaches hull topology to convex shapes whose params[2] (u32 bits) holds hull index + 1.
+  void attach(const float* params, const PolyIn* ph) {
+    if (!ph) return;
+    topos.resize(ph->n_hulls);
+    for (uint64_t h = 0; h < ph->n_hulls; ++h) {
+      const uint32_t* r = ph->hulls + 8 * h;
+      HullTopo& t = topos[h];
+      t.n_faces = r[3];
+      t.n_edges = r[5];
+      t.face_normals = ph->face_normals + 3 * (size_t)r[2];
+      t.face_ranges = ph->face_ranges + 2 * (size_t)r[2];
+      t.face_vertices = ph->face_vertices;
+      t.face_edges = ph->face_edges;
+      t.vertex_ranges = ph->vertex_ranges + 2 * (size_t)r[0];
+      t.vertex_faces = ph->vertex_faces;
+      t.vertex_edges = ph->vertex_edges;
+      t.edge_dirs = ph->edge_dirs + 3 * (size_t)r[4];
+    }
+    for (size_t i = 0; i < shapes.size(); ++i) {
+      if (shapes[i].type != SHAPE_CONVEX) continue;
+      uint32_t h1;
+      std::memcpy(&h1, params + 4 * i + 2, 4);
+      if (h1 && h1 - 1 < ph->n_hulls && topos[h1 - 1].n_faces) shapes[i].topo = &topos[h1 - 1];
+    }
+  }
   ShapeSet(const uint32_t* types, const float* params, const float* poses7, const float* hullv, uint32_t nhv, uint64_t n) {
     pool.resize(nhv);
     for (uint32_t i = 0; i < nhv; ++i) pool[i] = Vec3<R>(R(hullv[3 * i]), R(hullv[3 * i + 1]), R(hullv[3 * i + 2]));
@@ -332,9 +376,10 @@ void oracle_compound_cast_rays_f64(void* c, const float* pose7, const float* ray
 // records in place. Unsupported pairs keep their record and get status 2. stats: gjk_iters,
 // epa_iters, epa_calls, unsupported pairs, largest point count.
 void oracle_manifolds_f32(const uint32_t* types, const float* params, const float* poses, const float* hullv, uint32_t nhv,
-                          uint64_t nshapes, const uint32_t* pairs, uint64_t npairs, float prediction, int threads, uint32_t* records,
-                          uint64_t* stats) {
+                          uint64_t nshapes, const void* poly, const uint32_t* pairs, uint64_t npairs, float prediction, int threads,
+                          uint32_t* records, uint64_t* stats) {
   ShapeSet<float> set(types, params, poses, hullv, nhv, nshapes);
+  set.attach(params, (const PolyIn*)poly);
   std::atomic<uint64_t> gi{0}, ei{0}, ec{0}, un{0}, mx{0};
   parallel_for(npairs, threads, [&](uint64_t k) {
     uint32_t a = pairs[2 * k], b = pairs[2 * k + 1];

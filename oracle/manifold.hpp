@@ -188,6 +188,68 @@ template <class R> inline PolyFeature<R> segment_feature(R hh) {
   return f;
 }
 
+// ConvexPolyhedron::local_support_feature (convex_polyhedron.rs:959-991): the face whose normal has
+// the largest dot product with dir (first on ties), at most its first 4 vertices.
+template <class R> inline PolyFeature<R> hull_support_feature(const Shape<R>& s, const Vec3<R>& dir) {
+  const HullTopo& t = *s.topo;
+  auto normal = [&](uint32_t f) { return Vec3<R>(R(t.face_normals[3 * f]), R(t.face_normals[3 * f + 1]), R(t.face_normals[3 * f + 2])); };
+  uint32_t best = 0;
+  R best_dot = dot(normal(0), dir);
+  for (uint32_t f = 1; f < t.n_faces; ++f) {
+    R d = dot(normal(f), dir);
+    if (d > best_dot) { best = f; best_dot = d; }
+  }
+  PolyFeature<R> out{};
+  uint32_t first = t.face_ranges[2 * best], num = std::min(t.face_ranges[2 * best + 1], 4u);
+  for (uint32_t i = 0; i < num; ++i) {
+    uint32_t vid = t.face_vertices[first + i], eid = t.face_edges[first + i];
+    out.vertices[i] = s.pts[vid];
+    out.vids[i] = pfid_vertex(vid);
+    out.eids[i] = pfid_edge(eid);
+  }
+  out.fid = pfid_face(best);
+  out.num_vertices = (int)num;
+  return out;
+}
+
+// f32 sin / cos of (PI / 180 as f32), the eps of ConvexPolyhedron::support_feature_id_toward
+// (convex_polyhedron.rs:919-922), correctly rounded.
+template <class R> inline R hull_feature_seps() { return R(0.017452406f); }
+template <class R> inline R hull_feature_ceps() { return R(0.9998477f); }
+
+// ConvexPolyhedron::support_feature_id_toward_eps (convex_polyhedron.rs:885-917) as a PackedFeatureId.
+template <class R> inline uint32_t hull_support_feature_id(const Shape<R>& s, const Vec3<R>& local_dir) {
+  const HullTopo& t = *s.topo;
+  R seps = hull_feature_seps<R>(), ceps = hull_feature_ceps<R>();
+  uint32_t vid = 0;
+  R best = dot(s.pts[0], local_dir);
+  for (uint32_t i = 1; i < s.npts; ++i) {
+    R d = dot(s.pts[i], local_dir);
+    if (d > best) { best = d; vid = i; }
+  }
+  uint32_t first = t.vertex_ranges[2 * vid], num = t.vertex_ranges[2 * vid + 1];
+  for (uint32_t i = 0; i < num; ++i) {
+    uint32_t f = t.vertex_faces[first + i];
+    Vec3<R> n(R(t.face_normals[3 * f]), R(t.face_normals[3 * f + 1]), R(t.face_normals[3 * f + 2]));
+    if (dot(n, local_dir) >= ceps) return pfid_face(f);
+  }
+  for (uint32_t i = 0; i < num; ++i) {
+    uint32_t e = t.vertex_edges[first + i];
+    Vec3<R> d(R(t.edge_dirs[3 * e]), R(t.edge_dirs[3 * e + 1]), R(t.edge_dirs[3 * e + 2]));
+    if (std::fabs(dot(d, local_dir)) <= seps) return pfid_edge(e);
+  }
+  return pfid_vertex(vid);
+}
+
+// ConvexPolyhedron::project_local_point_and_get_feature (point_support_map.rs:55-77).
+template <class R> inline uint32_t hull_projection_feature(const Shape<R>& s, const Vec3<R>& pt, const PointProj<R>& proj) {
+  Vec3<R> dpt = pt - proj.point;
+  Vec3<R> local_dir = proj.is_inside ? -dpt : dpt;
+  Vec3<R> u;
+  if (try_normalize(local_dir, eps_default<R>(), &u)) return hull_support_feature_id(s, u);
+  return PFID_UNKNOWN;
+}
+
 // clip_segment_segment (clip/clip_segment_segment.rs): two clipping points (p1, p2, feat1, feat2)
 template <class R> struct ClipPt {
   Vec3<R> p1, p2;
@@ -426,13 +488,20 @@ template <class R> inline uint32_t cuboid_projection_feature(const Vec3<R>& he, 
 
 // contact_manifolds_convex_ball.rs:45-145 for a cuboid or capsule shape1 (no normal constraints)
 template <class R>
-inline void manifold_convex_ball(const Iso<R>& pos12, const Shape<R>& s1, R radius2, R prediction, Manifold<R>& m, bool flipped) {
+inline void manifold_convex_ball(const Iso<R>& pos12, const Shape<R>& s1, R radius2, R prediction, Manifold<R>& m, bool flipped,
+                                 GjkStats* st) {
   Vec3<R> lp21 = pos12.tra;
   Vec3<R> proj;
   bool inside;
   uint32_t fid1;
   if (s1.type == SHAPE_CUBOID) fid1 = cuboid_projection_feature(s1.half, lp21, &proj, &inside);
-  else { PointProj<R> p = project_capsule(s1.half_height, s1.radius, lp21); proj = p.point; inside = p.is_inside; fid1 = pfid_face(0); }
+  else if (s1.type == SHAPE_CAPSULE) {
+    PointProj<R> p = project_capsule(s1.half_height, s1.radius, lp21);
+    proj = p.point; inside = p.is_inside; fid1 = pfid_face(0);
+  } else {
+    PointProj<R> p = project_support_map(s1, lp21, st);
+    proj = p.point; inside = p.is_inside; fid1 = hull_projection_feature(s1, lp21, p);
+  }
   Vec3<R> lp1 = proj;
   Vec3<R> dpos = lp21 - lp1;
   Vec3<R> n1;
@@ -544,7 +613,9 @@ template <class R> inline void manifold_pfm_pfm(const Iso<R>& pos12, const Shape
     Vec3<R> n1 = r.dir;
     Vec3<R> n2 = pos12.inverse_transform_vector(-r.dir);
     auto feature_of = [](const Shape<R>& s, const Vec3<R>& d) {
-      return s.type == SHAPE_CUBOID ? cuboid_support_face(s.half, d) : segment_feature(s.half_height);
+      if (s.type == SHAPE_CUBOID) return cuboid_support_face(s.half, d);
+      if (s.type == SHAPE_CONVEX) return hull_support_feature(s, d);
+      return segment_feature(s.half_height);
     };
     PolyFeature<R> f1 = feature_of(s1, n1), f2 = feature_of(s2, n2);
     feature_contacts(pos12, n1, f1, f2, m, false);
@@ -571,14 +642,16 @@ template <class R> inline void manifold_pfm_pfm(const Iso<R>& pos12, const Shape
 template <class R>
 inline bool contact_manifold_convex_convex(const Iso<R>& pos12, const Shape<R>& s1, const Shape<R>& s2, R prediction, Manifold<R>& m,
                                            GjkStats* st = nullptr) {
-  auto ok = [](const Shape<R>& s) { return s.type == SHAPE_BALL || s.type == SHAPE_CUBOID || s.type == SHAPE_CAPSULE; };
+  auto ok = [](const Shape<R>& s) {
+    return s.type == SHAPE_BALL || s.type == SHAPE_CUBOID || s.type == SHAPE_CAPSULE || (s.type == SHAPE_CONVEX && s.topo && s.topo->n_faces);
+  };
   if (!ok(s1) || !ok(s2)) return false;
   if (s1.type == SHAPE_BALL && s2.type == SHAPE_BALL) manifold_ball_ball(pos12, s1.radius, s2.radius, prediction, m);
   else if (s1.type == SHAPE_CUBOID && s2.type == SHAPE_CUBOID) manifold_cuboid_cuboid(pos12, s1.half, s2.half, prediction, m);
   else if (s1.type == SHAPE_CAPSULE && s2.type == SHAPE_CAPSULE)
     manifold_capsule_capsule(pos12, s1.half_height, s1.radius, s2.half_height, s2.radius, prediction, m);
-  else if (s1.type == SHAPE_BALL) manifold_convex_ball(pos12.inverse(), s2, s1.radius, prediction, m, true);
-  else if (s2.type == SHAPE_BALL) manifold_convex_ball(pos12, s1, s2.radius, prediction, m, false);
+  else if (s1.type == SHAPE_BALL) manifold_convex_ball(pos12.inverse(), s2, s1.radius, prediction, m, true, st);
+  else if (s2.type == SHAPE_BALL) manifold_convex_ball(pos12, s1, s2.radius, prediction, m, false, st);
   else manifold_pfm_pfm(pos12, s1, s2, prediction, m, st);
   return true;
 }

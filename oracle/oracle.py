@@ -44,7 +44,7 @@ _SIGS = {
     "oracle_compound_free_f64": (None, [P]),
     "oracle_compound_cast_rays_f32": (None, [P, P, P, U64, F32, I32, I32, I32, P, P, P, P]),
     "oracle_compound_cast_rays_f64": (None, [P, P, P, U64, F32, I32, I32, I32, P, P, P, P]),
-    "oracle_manifolds_f32": (None, [P, P, P, P, U32, U64, P, U64, F32, I32, P, P]),
+    "oracle_manifolds_f32": (None, [P, P, P, P, U32, U64, P, P, U64, F32, I32, P, P]),
     "oracle_pairs_count": (U64, [P]),
     "oracle_pairs_copy": (None, [P, P]),
     "oracle_pairs_free": (None, [P]),
@@ -208,6 +208,29 @@ def contacts(shapes, pairs: np.ndarray, prediction: float, init_dirs: np.ndarray
                       "support_vertices": int(st[6])}
 
 
+class _PolyIn(C.Structure):
+    """Field layout of the library's parrygpu_polyhedra (ConvexPolyhedron topology)."""
+    _fields_ = [("n_hulls", U64), ("hulls", P), ("n_faces", U64), ("face_normals", P), ("face_ranges", P),
+                ("n_face_entries", U64), ("face_vertices", P), ("face_edges", P), ("vertex_ranges", P),
+                ("n_vertex_entries", U64), ("vertex_faces", P), ("vertex_edges", P), ("n_edges", U64), ("edge_dirs", P)]
+
+
+def _poly_struct(shapes):
+    """(pointer to a _PolyIn or None, keep-alive) for a ShapeSet's hull topology."""
+    poly = shapes.polyhedra() if hasattr(shapes, "polyhedra") else None
+    if poly is None:
+        return None, None
+    hulls, topo = poly
+    arrs = {"hulls": np.ascontiguousarray(hulls, np.uint32)}
+    for key, val in topo.items():
+        arrs[key] = np.ascontiguousarray(val, np.float32 if key in ("face_normals", "edge_dirs") else np.uint32)
+    ptr = {key: (a.ctypes.data if a.size else None) for key, a in arrs.items()}
+    st = _PolyIn(len(arrs["hulls"]), ptr["hulls"], len(arrs["face_normals"]), ptr["face_normals"], ptr["face_ranges"],
+                 len(arrs["face_vertices"]), ptr["face_vertices"], ptr["face_edges"], ptr["vertex_ranges"],
+                 len(arrs["vertex_faces"]), ptr["vertex_faces"], ptr["vertex_edges"], len(arrs["edge_dirs"]), ptr["edge_dirs"])
+    return C.cast(C.pointer(st), C.c_void_p), (st, arrs)
+
+
 MANIFOLD_MAX_POINTS = 24
 MANIFOLD_WORDS = 8 + 10 * MANIFOLD_MAX_POINTS
 
@@ -225,8 +248,10 @@ def contact_manifolds(shapes, pairs: np.ndarray, prediction: float, records: np.
     k = len(pairs)
     assert records.dtype == np.uint32 and records.shape == (k, MANIFOLD_WORDS) and records.flags.c_contiguous
     st = np.zeros(5, np.uint64)
-    lib().oracle_manifolds_f32(_p(t), _p(prm), _p(pos), _p(pool), len(pool), len(t), _p(pairs), k, float(prediction),
+    poly, keep = _poly_struct(shapes)
+    lib().oracle_manifolds_f32(_p(t), _p(prm), _p(pos), _p(pool), len(pool), len(t), poly, _p(pairs), k, float(prediction),
                                threads if threads is not None else default_threads(), _p(records), _p(st))
+    del keep
     return {"gjk_iters": int(st[0]), "epa_iters": int(st[1]), "epa_calls": int(st[2]), "unsupported": int(st[3]),
             "max_points": int(st[4])}
 

@@ -31,6 +31,21 @@ template <class R> inline R gjk_eps_tol() { return eps_default<R>() * R(10); }
 enum ShapeType : uint32_t { SHAPE_BALL = 0, SHAPE_CUBOID = 1, SHAPE_CAPSULE = 2, SHAPE_CONVEX = 3, SHAPE_TRIANGLE = 4,
                             SHAPE_SEGMENT_PFM = 5 /* a capsule's axis segment, as its polygonal feature map */ };
 
+// ConvexPolyhedron topology of one hull (convex_polyhedron.rs:172-185, built by from_convex_mesh),
+// ids hull-local. face_normals / face_ranges / vertex_ranges / edge_dirs point at this hull's rows;
+// the ranges index the shared face_vertices / face_edges / vertex_faces / vertex_edges arrays.
+struct HullTopo {
+  uint32_t n_faces = 0, n_edges = 0;
+  const float* face_normals = nullptr;
+  const uint32_t* face_ranges = nullptr;
+  const uint32_t* face_vertices = nullptr;
+  const uint32_t* face_edges = nullptr;
+  const uint32_t* vertex_ranges = nullptr;
+  const uint32_t* vertex_faces = nullptr;
+  const uint32_t* vertex_edges = nullptr;
+  const float* edge_dirs = nullptr;
+};
+
 // One convex shape. Capsule = Capsule::new_y(half_height, radius): segment (0,-h,0)-(0,h,0).
 template <class R> struct Shape {
   uint32_t type = SHAPE_BALL;
@@ -39,6 +54,7 @@ template <class R> struct Shape {
   R half_height = 0;            // capsule
   const Vec3<R>* pts = nullptr; // convex hull vertices (triangle: its 3 vertices)
   uint32_t npts = 0;
+  const HullTopo* topo = nullptr;  // convex: face topology when built as a ConvexPolyhedron
 
   // SupportMap::local_support_point
   Vec3<R> local_support(const Vec3<R>& dir) const {

@@ -260,19 +260,40 @@ class _StagedShapes:
     """Keeps the arrays of a ShapeSet (or of device tensors) alive behind a parrygpu_shapes struct."""
 
     def __init__(self, shapes):
+        poly = None
         if isinstance(shapes, ShapeSet):
             t, prm, pos, pool = shapes.arrays()
+            poly = shapes.polyhedra()
+        elif len(shapes) == 5:
+            t, prm, pos, pool, poly = shapes
         else:
             t, prm, pos, pool = shapes
         kt, pt = _as_input(t, np.uint32)
         kp, pp = _as_input(prm, np.float32)
         kq, pq = _as_input(pos, np.float32)
         kv, pv = _as_input(pool, np.float32)
-        self.keep = (kt, kp, kq, kv)
+        self.keep = [kt, kp, kq, kv]
         self.n = int(kt.shape[0])
+        self.poly_struct = None
+        poly_ptr = None
+        if poly is not None:
+            hulls, topo = poly
+            ptrs = {}
+            for name, arr, dt in [("hulls", hulls, np.uint32)] + [(k, topo[k], np.float32 if k in ("face_normals", "edge_dirs")
+                                                                   else np.uint32) for k in topo]:
+                ka, pa = _as_input(arr, dt)
+                self.keep.append(ka)
+                size = ka.numel() if _is_torch(ka) else ka.size
+                ptrs[name] = pa.value if (pa is not None and size) else None
+            self.poly_struct = _capi.ParryGpuPolyhedra(
+                int(hulls.shape[0]), ptrs["hulls"], int(topo["face_normals"].shape[0]), ptrs["face_normals"], ptrs["face_ranges"],
+                int(topo["face_vertices"].shape[0]), ptrs["face_vertices"], ptrs["face_edges"], ptrs["vertex_ranges"],
+                int(topo["vertex_faces"].shape[0]), ptrs["vertex_faces"], ptrs["vertex_edges"], int(topo["edge_dirs"].shape[0]),
+                ptrs["edge_dirs"])
+            poly_ptr = C.cast(C.pointer(self.poly_struct), C.c_void_p).value
         self.struct = _capi.ParryGpuShapes(self.n, pt.value if pt else None, pp.value if pp else None,
                                            pq.value if pq else None, pv.value if (pv and kv.shape[0]) else None,
-                                           int(kv.shape[0]) if kv is not None else 0)
+                                           int(kv.shape[0]) if kv is not None else 0, poly_ptr)
         self.ref = kq
 
 

@@ -30,7 +30,7 @@ def nvcc() -> str:
 
 
 def _sources() -> list[Path]:
-    return sorted(CSRC.glob("*.cu"))
+    return sorted(CSRC.glob("*.cu")) + sorted(CSRC.glob("*.cpp"))
 
 
 def _needs_build() -> bool:
@@ -54,6 +54,8 @@ def build(force: bool = False, verbose: bool = False) -> Path:
         obj = BUILD / (src.stem + ".o")
         fmad = "--fmad=true" if src.name in FMAD_OK else "--fmad=false"
         cmd = [cc, "-c", str(src), "-o", str(obj), fmad] + common
+        if src.suffix == ".cpp":  # host-only code: no contraction of f32 arithmetic (aarch64 gcc contracts by default)
+            cmd += ["-Xcompiler", "-ffp-contract=off", "-Xcompiler", "-pthread"]
         if verbose:
             print(" ".join(cmd), file=sys.stderr)
         r = subprocess.run(cmd, capture_output=True, text=True)

@@ -58,6 +58,10 @@ SIGNATURES: dict[str, tuple] = {
     "parrygpu_contacts": (I32, [P, P, P, U64, F32, P, P, P, P]),
     "parrygpu_contacts_with_dirs": (I32, [P, P, P, U64, F32, P, P, P, P, P]),
     "parrygpu_contact_manifolds": (I32, [P, P, P, U64, F32, P, P]),
+    "parrygpu_polyhedra_build": (I32, [P, P, P, U64, U32, C.POINTER(P)]),
+    "parrygpu_polyhedra_sizes": (I32, [P, P]),
+    "parrygpu_polyhedra_copy": (I32, [P, P, P, P, P, P, P, P, P, P, P]),
+    "parrygpu_polyhedra_builder_destroy": (None, [P]),
     "parrygpu_mlp_create": (I32, [P, U64, C.POINTER(P)]),
     "parrygpu_mlp_destroy": (None, [P]),
     "parrygpu_mlp_features": (I32, [P, P, P, U64, P]),
@@ -74,9 +78,16 @@ SIGNATURES: dict[str, tuple] = {
 }
 
 
+class ParryGpuPolyhedra(C.Structure):
+    _fields_ = [("n_hulls", C.c_uint64), ("hulls", C.c_void_p), ("n_faces", C.c_uint64), ("face_normals", C.c_void_p),
+                ("face_ranges", C.c_void_p), ("n_face_entries", C.c_uint64), ("face_vertices", C.c_void_p),
+                ("face_edges", C.c_void_p), ("vertex_ranges", C.c_void_p), ("n_vertex_entries", C.c_uint64),
+                ("vertex_faces", C.c_void_p), ("vertex_edges", C.c_void_p), ("n_edges", C.c_uint64), ("edge_dirs", C.c_void_p)]
+
+
 class ParryGpuShapes(C.Structure):
     _fields_ = [("n", C.c_uint64), ("types", C.c_void_p), ("params", C.c_void_p), ("poses", C.c_void_p),
-                ("vertices", C.c_void_p), ("n_vertices", C.c_uint64)]
+                ("vertices", C.c_void_p), ("n_vertices", C.c_uint64), ("polyhedra", C.c_void_p)]
 
 
 class ParryGpuGjkStats(C.Structure):

@@ -330,7 +330,32 @@ parrygpu_status pg::stage_shapes(parrygpu_ctx* ctx, const parrygpu_shapes* s, Sh
   if ((st = stage_input(ctx, ctx->stage_in[2], s->poses, (size_t)s->n * 28, &q)) != PARRYGPU_OK) return st;
   if ((st = stage_input(ctx, ctx->stage_in[3], s->vertices, (size_t)s->n_vertices * 12, &v)) != PARRYGPU_OK) return st;
   if (((uintptr_t)p & 15) != 0) return set_error(ctx, PARRYGPU_INVALID_ARG, "shape params must be 16-byte aligned");
-  *out = ShapeArrays{(const uint32_t*)t, (const float4*)p, (const float*)q, (const float*)v, s->n, s->n_vertices};
+  *out = ShapeArrays{(const uint32_t*)t, (const float4*)p, (const float*)q, (const float*)v, s->n, s->n_vertices, PolyArrays{}};
+  if (const parrygpu_polyhedra* ph = s->polyhedra) {
+    PolyArrays& pa = out->poly;
+    const void* d[9];
+    const void* src[9] = {ph->hulls, ph->face_normals, ph->face_ranges, ph->face_vertices, ph->face_edges, ph->vertex_ranges,
+                          ph->vertex_faces, ph->vertex_edges, ph->edge_dirs};
+    size_t bytes[9] = {(size_t)ph->n_hulls * 32, (size_t)ph->n_faces * 12, (size_t)ph->n_faces * 8, (size_t)ph->n_face_entries * 4,
+                       (size_t)ph->n_face_entries * 4, (size_t)s->n_vertices * 8, (size_t)ph->n_vertex_entries * 4,
+                       (size_t)ph->n_vertex_entries * 4, (size_t)ph->n_edges * 12};
+    for (int k = 0; k < 9; ++k)
+      if ((st = stage_input(ctx, ctx->stage_poly[k], src[k], bytes[k], &d[k])) != PARRYGPU_OK) return st;
+    pa.hulls = (const uint32_t*)d[0];
+    pa.face_normals = (const float*)d[1];
+    pa.face_ranges = (const uint32_t*)d[2];
+    pa.face_vertices = (const uint32_t*)d[3];
+    pa.face_edges = (const uint32_t*)d[4];
+    pa.vertex_ranges = (const uint32_t*)d[5];
+    pa.vertex_faces = (const uint32_t*)d[6];
+    pa.vertex_edges = (const uint32_t*)d[7];
+    pa.edge_dirs = (const float*)d[8];
+    pa.n_hulls = ph->n_hulls;
+    pa.n_faces = ph->n_faces;
+    pa.n_face_entries = ph->n_face_entries;
+    pa.n_vertex_entries = ph->n_vertex_entries;
+    pa.n_edges = ph->n_edges;
+  }
   return PARRYGPU_OK;
 }
 

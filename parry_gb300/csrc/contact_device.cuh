@@ -10,6 +10,20 @@ namespace pg {
 
 constexpr int QUEUE_WORDS = 40;  // pair, dim, 4 x CSO (9 words), pad
 
+// ConvexPolyhedron topology on the device (parrygpu_polyhedra); all null when absent.
+struct PolyArrays {
+  const uint32_t* hulls;          // x8: first vertex, vertex count, first face, face count, first edge, edge count, ok, 0
+  const float* face_normals;      // x3
+  const uint32_t* face_ranges;    // x2
+  const uint32_t* face_vertices;
+  const uint32_t* face_edges;
+  const uint32_t* vertex_ranges;  // x2, parallel to the vertex pool
+  const uint32_t* vertex_faces;
+  const uint32_t* vertex_edges;
+  const float* edge_dirs;         // x3
+  uint64_t n_hulls, n_faces, n_face_entries, n_vertex_entries, n_edges;
+};
+
 struct ShapeArrays {
   const uint32_t* types;
   const float4* params;
@@ -17,6 +31,7 @@ struct ShapeArrays {
   const float* pool;
   uint64_t n_shapes;
   uint64_t n_vertices;
+  PolyArrays poly;
 };
 
 // Rejects out-of-range pair indices and vertex ranges (reported as a capacity / argument error
@@ -120,10 +135,14 @@ __device__ __forceinline__ PointProj project_capsule(float hh, float radius, V3 
   return out;
 }
 
-__device__ __forceinline__ void enqueue(uint32_t* __restrict__ queue, unsigned long long* __restrict__ qcount, uint64_t k, const Simplex& s) {
+// Appends (pair k, simplex) to the EPA queue; `tag` (word 39) tells the EPA kernel which query the
+// pair came from.
+__device__ __forceinline__ void enqueue(uint32_t* __restrict__ queue, unsigned long long* __restrict__ qcount, uint64_t k, const Simplex& s,
+                                        uint32_t tag = 0) {
   unsigned long long slot = atomicAdd(qcount, 1ull);
   uint32_t* e = queue + (size_t)slot * QUEUE_WORDS;
   e[0] = (uint32_t)k;
+  e[QUEUE_WORDS - 1] = tag;
   e[1] = (uint32_t)s.dim;
   for (int i = 0; i <= s.dim; ++i) {
     float* f = reinterpret_cast<float*>(e + 2 + 9 * i);

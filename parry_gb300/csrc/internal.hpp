@@ -44,7 +44,7 @@ struct parrygpu_ctx {
   uint32_t* d_err = nullptr;    // device error word
   uint32_t* h_err = nullptr;    // pinned mirror
   // Scratch reused across calls (sort buffers, staging of host inputs/outputs, counters).
-  DevBuf sort_k[2], sort_v[2], sort_hist, stage_in[8], stage_out[4], misc, counters;
+  DevBuf sort_k[2], sort_v[2], sort_hist, stage_in[8], stage_out[4], misc, counters, stage_poly[9];
   DevBuf ray_keys, ray_order;
   // contact pipeline scratch: EPA queue (pair + simplex per entry) and per-slot polytope workspaces
   DevBuf ct_queue, ct_counters, epa_ws;

@@ -250,6 +250,101 @@ __device__ __forceinline__ PolyFeature segment_feature(float hh) {
   return f;
 }
 
+// One ConvexPolyhedron's topology (hull-local ids); see parrygpu_polyhedra.
+struct HullDev {
+  const float* face_normals;    // this hull's faces x 3
+  const uint32_t* face_ranges;  // this hull's faces x 2 (global first entry, count)
+  const uint32_t* face_vertices;
+  const uint32_t* face_edges;
+  const uint32_t* vertex_ranges;  // this hull's vertices x 2 (global first entry, count)
+  const uint32_t* vertex_faces;
+  const uint32_t* vertex_edges;
+  const float* edge_dirs;  // this hull's edges x 3
+  uint32_t n_faces, n_edges;
+  uint64_t n_face_entries, n_vertex_entries;
+};
+
+// The topology of convex shape i (params.z = hull index + 1), checked against the array sizes.
+__device__ __forceinline__ bool load_hull(const ShapeArrays& sh, uint32_t i, HullDev* h) {
+  const PolyArrays& P = sh.poly;
+  if (!P.hulls || sh.types[i] != SH_CONVEX) return false;
+  float4 prm = sh.params[i];
+  uint32_t h1 = __float_as_uint(prm.z);
+  if (h1 == 0 || h1 > P.n_hulls) return false;
+  const uint32_t* r = P.hulls + 8 * (size_t)(h1 - 1);
+  uint32_t first_vertex = __float_as_uint(prm.x), nv = __float_as_uint(prm.y);
+  if (r[3] == 0 || r[0] != first_vertex || r[1] != nv) return false;
+  if ((uint64_t)r[2] + r[3] > P.n_faces || (uint64_t)r[4] + r[5] > P.n_edges) return false;
+  h->face_normals = P.face_normals + 3 * (size_t)r[2];
+  h->face_ranges = P.face_ranges + 2 * (size_t)r[2];
+  h->face_vertices = P.face_vertices;
+  h->face_edges = P.face_edges;
+  h->vertex_ranges = P.vertex_ranges + 2 * (size_t)first_vertex;
+  h->vertex_faces = P.vertex_faces;
+  h->vertex_edges = P.vertex_edges;
+  h->edge_dirs = P.edge_dirs + 3 * (size_t)r[4];
+  h->n_faces = r[3];
+  h->n_edges = r[5];
+  h->n_face_entries = P.n_face_entries;
+  h->n_vertex_entries = P.n_vertex_entries;
+  return true;
+}
+
+// ConvexPolyhedron::local_support_feature (convex_polyhedron.rs:959-991). Out-of-range topology
+// indices set *bad and yield an empty feature.
+static __device__ __noinline__ PolyFeature hull_support_feature(const ShapeDev& s, const HullDev& h, V3 dir, bool* bad) {
+  uint32_t best = 0;
+  float best_dot = dot(ldv(h.face_normals), dir);
+  for (uint32_t f = 1; f < h.n_faces; ++f) {
+    float d = dot(ldv(h.face_normals + 3 * f), dir);
+    if (d > best_dot) { best = f; best_dot = d; }
+  }
+  PolyFeature out;
+#pragma unroll
+  for (int i = 0; i < 4; ++i) { out.v[i] = v3(0.f, 0.f, 0.f); out.vids[i] = 0; out.eids[i] = 0; }
+  uint32_t first = h.face_ranges[2 * best], num = min(h.face_ranges[2 * best + 1], 4u);
+  out.fid = pf_face(best);
+  out.nv = 0;
+  if ((uint64_t)first + num > h.n_face_entries) { *bad = true; return out; }
+  for (uint32_t i = 0; i < num; ++i) {
+    uint32_t vid = h.face_vertices[first + i], eid = h.face_edges[first + i];
+    if (vid >= s.npts || eid >= h.n_edges) { *bad = true; out.nv = 0; return out; }
+    out.v[i] = ldv(s.pts + 3 * vid);
+    out.vids[i] = pf_vertex(vid);
+    out.eids[i] = pf_edge(eid);
+  }
+  out.nv = (int)num;
+  return out;
+}
+
+// sin / cos of (PI / 180 as f32), correctly rounded: ConvexPolyhedron::support_feature_id_toward's
+// eps (convex_polyhedron.rs:919-922).
+constexpr float HULL_SEPS = 0.017452406f;
+constexpr float HULL_CEPS = 0.9998477f;
+
+// ConvexPolyhedron::support_feature_id_toward_eps (convex_polyhedron.rs:885-917) as a PackedFeatureId.
+static __device__ __noinline__ uint32_t hull_support_feature_id(const ShapeDev& s, const HullDev& h, V3 dir, bool* bad) {
+  uint32_t vid = 0;
+  float best = dot(ldv(s.pts), dir);
+  for (uint32_t i = 1; i < s.npts; ++i) {
+    float d = dot(ldv(s.pts + 3 * i), dir);
+    if (d > best) { best = d; vid = i; }
+  }
+  uint32_t first = h.vertex_ranges[2 * vid], num = h.vertex_ranges[2 * vid + 1];
+  if ((uint64_t)first + num > h.n_vertex_entries) { *bad = true; return PF_UNKNOWN; }
+  for (uint32_t i = 0; i < num; ++i) {
+    uint32_t f = h.vertex_faces[first + i];
+    if (f >= h.n_faces) { *bad = true; return PF_UNKNOWN; }
+    if (dot(ldv(h.face_normals + 3 * f), dir) >= HULL_CEPS) return pf_face(f);
+  }
+  for (uint32_t i = 0; i < num; ++i) {
+    uint32_t e = h.vertex_edges[first + i];
+    if (e >= h.n_edges) { *bad = true; return PF_UNKNOWN; }
+    if (fabsf(dot(ldv(h.edge_dirs + 3 * e), dir)) <= HULL_SEPS) return pf_edge(e);
+  }
+  return pf_vertex(vid);
+}
+
 // clip_segment_segment (clip_segment_segment.rs): the two clipped points (p1, p2) and their
 // feature codes (0 = first vertex, 1 = edge, 2 = second vertex).
 struct ClipPt {
@@ -500,29 +595,18 @@ __device__ __forceinline__ void mf_capsule_capsule(const Rec& r, const Pose& pos
   }
 }
 
-// contact_manifold_convex_ball for a cuboid or capsule shape 1 (contact_manifolds_convex_ball.rs:45-145,
-// no normal constraints).
-__device__ __forceinline__ void mf_convex_ball(const Rec& r, const Pose& pos12, const ShapeDev& s1, float radius2, float prediction,
-                                               bool flipped) {
+// The end of contact_manifold_convex_ball (contact_manifolds_convex_ball.rs:61-145, no normal
+// constraints) from the projection of the ball centre (pos12.t) on shape 1.
+__device__ __forceinline__ void finish_convex_ball(const Rec& r, const Pose& pos12, V3 lp1, bool inside, uint32_t fid1, float radius2,
+                                                   float prediction, bool flipped) {
   V3 lp21 = pos12.t;
-  PointProj p;
-  uint32_t fid1;
-  if (s1.type == SH_CUBOID) {
-    V3 he = v3(s1.a, s1.b, s1.c);
-    p = project_cuboid(he, lp21);
-    fid1 = cuboid_projection_feature(he, p);
-  } else {
-    p = project_capsule(s1.a, s1.b, lp21);
-    fid1 = pf_face(0);
-  }
-  V3 lp1 = p.point;
   V3 n1;
   float dist;
   if (!try_normalize(lp21 - lp1, 0.0f, &n1, &dist)) {
     if (!try_normalize(pos12.t, 0.0f, &n1)) n1 = v3(1.f, 0.f, 0.f);
     dist = 0.0f;
   }
-  if (p.inside) { n1 = -n1; dist = -dist; }
+  if (inside) { n1 = -n1; dist = -dist; }
   if (dist <= radius2 + prediction) {
     V3 n2 = pose_inv_rotate(pos12, -n1);
     V3 lp2 = n2 * radius2;
@@ -538,6 +622,31 @@ __device__ __forceinline__ void mf_convex_ball(const Rec& r, const Pose& pos12, 
   } else {
     r.w[0] = 0;
   }
+}
+
+// contact_manifold_convex_ball for a cuboid or capsule shape 1: analytic projection.
+__device__ __forceinline__ void mf_convex_ball(const Rec& r, const Pose& pos12, const ShapeDev& s1, float radius2, float prediction,
+                                               bool flipped) {
+  V3 lp21 = pos12.t;
+  PointProj p;
+  uint32_t fid1;
+  if (s1.type == SH_CUBOID) {
+    V3 he = v3(s1.a, s1.b, s1.c);
+    p = project_cuboid(he, lp21);
+    fid1 = cuboid_projection_feature(he, p);
+  } else {
+    p = project_capsule(s1.a, s1.b, lp21);
+    fid1 = pf_face(0);
+  }
+  finish_convex_ball(r, pos12, p.point, p.inside, fid1, radius2, prediction, flipped);
+}
+
+// ConvexPolyhedron::project_local_point_and_get_feature's feature (point_support_map.rs:62-76).
+__device__ __forceinline__ uint32_t hull_projection_feature(const ShapeDev& s, const HullDev& h, V3 pt, V3 proj, bool inside, bool* bad) {
+  V3 dpt = pt - proj;
+  V3 dir;
+  if (try_normalize(inside ? -dpt : dpt, EPS, &dir)) return hull_support_feature_id(s, h, dir, bad);
+  return PF_UNKNOWN;
 }
 
 __device__ __forceinline__ V3 cuboid_support(V3 he, V3 d) { return v3(copysignf(he.x, d.x), copysignf(he.y, d.y), copysignf(he.z, d.z)); }
@@ -621,13 +730,15 @@ __device__ __forceinline__ ShapeDev pfm_of(const ShapeDev& s, float* border) {
   return p;
 }
 
-__device__ __forceinline__ PolyFeature support_feature(const ShapeDev& s, V3 dir) {
-  return s.type == SH_CUBOID ? cuboid_support_face(v3(s.a, s.b, s.c), dir) : segment_feature(s.a);
+__device__ __forceinline__ PolyFeature support_feature(const ShapeDev& s, const HullDev& h, V3 dir, bool* bad) {
+  if (s.type == SH_CUBOID) return cuboid_support_face(v3(s.a, s.b, s.c), dir);
+  if (s.type == SH_CONVEX) return hull_support_feature(s, h, dir, bad);
+  return segment_feature(s.a);
 }
 
 // The part of contact_manifold_pfm_pfm after the GJK / EPA query (contact_manifolds_pfm_pfm.rs:77-162).
-static __device__ __noinline__ void finish_pfm(const Rec& r, const Pose& pos12, const ShapeDev& s1, const ShapeDev& s2, int kind, V3 p1, V3 p2,
-                                               V3 dir, bool* overflow) {
+static __device__ __noinline__ void finish_pfm(const Rec& r, const Pose& pos12, const ShapeDev& s1, const HullDev& h1, const ShapeDev& s2,
+                                               const HullDev& h2, int kind, V3 p1, V3 p2, V3 dir, bool* overflow, bool* bad) {
   float br1 = s1.type == SH_CAPSULE ? s1.b : 0.0f, br2 = s2.type == SH_CAPSULE ? s2.b : 0.0f;
   OldPts old;
   save_old(r, old);
@@ -635,7 +746,7 @@ static __device__ __noinline__ void finish_pfm(const Rec& r, const Pose& pos12, 
   if (kind == GJK_CLOSEST) {
     V3 n1 = dir;
     V3 n2 = pose_inv_rotate(pos12, -dir);
-    PolyFeature f1 = support_feature(s1, n1), f2 = support_feature(s2, n2);
+    PolyFeature f1 = support_feature(s1, h1, n1, bad), f2 = support_feature(s2, h2, n2, bad);
     feature_contacts(pos12, n1, f1, f2, wr, false);
     wr.push(p1, pose_inv_point(pos12, p2), PF_UNKNOWN, PF_UNKNOWN, dot(p2 - p1, n1), false);
     if (br1 != 0.0f || br2 != 0.0f) {
@@ -657,7 +768,33 @@ static __device__ __noinline__ void finish_pfm(const Rec& r, const Pose& pos12, 
   *overflow |= wr.overflow;
 }
 
-__device__ __forceinline__ bool has_generator(uint32_t t) { return t == SH_BALL || t == SH_CUBOID || t == SH_CAPSULE; }
+// Pair kinds with a manifold generator here: balls, cuboids, capsules, and convex shapes that carry
+// ConvexPolyhedron topology.
+__device__ __forceinline__ bool has_generator(const ShapeArrays& sh, uint32_t i, HullDev* h) {
+  uint32_t t = sh.types[i];
+  if (t == SH_BALL || t == SH_CUBOID || t == SH_CAPSULE) return true;
+  return t == SH_CONVEX && load_hull(sh, i, h);
+}
+
+// EPA queue tags of the manifold kernels.
+enum : uint32_t { TAG_PFM = 0, TAG_BALL_SECOND = 1, TAG_BALL_FIRST = 2 };
+
+// GJK projection of the ball centre `center` (in the hull's frame) onto the hull
+// (point_support_map.rs:17-57 up to the EPA fallback): true with *proj when GJK ends outside,
+// false with the simplex `s` for EPA.
+__device__ __forceinline__ bool hull_project_gjk(const ShapeDev& cs, V3 center, V3* proj, Simplex& s, uint32_t* iters) {
+  Pose m{0.f, 0.f, 0.f, 1.f, -center};
+  Pose minv = pose_inverse(m);
+  Pose m_inv{0.f, 0.f, 0.f, 1.f, center};
+  ShapeDev origin;
+  origin.type = SH_ORIGIN;
+  V3 dir;
+  if (!try_normalize(-m.t, EPS, &dir)) dir = v3(1.f, 0.f, 0.f);
+  simplex_reset(s, cso_from_shapes(m_inv, cs, origin, dir));
+  GjkOut g = gjk_closest_points(minv, cs, origin, FLT_MAX, s, iters);
+  if (g.kind == GJK_CLOSEST) { *proj = g.p1; return true; }
+  return false;
+}
 
 __global__ void __launch_bounds__(MF_THREADS) k_manifolds_main(ShapeArrays sh, const uint32_t* __restrict__ pairs, uint64_t n, float prediction,
                                                                uint32_t* __restrict__ recs, uint32_t* __restrict__ queue,
@@ -668,27 +805,42 @@ __global__ void __launch_bounds__(MF_THREADS) k_manifolds_main(ShapeArrays sh, c
   if (k < n) {
     Rec r{recs + (size_t)k * MF_WORDS};
     uint32_t a = pairs[2 * k], b = pairs[2 * k + 1];
+    HullDev h1, h2;
     if (!valid_pair(sh, a, b)) {
       atomicOr(err, ERR_BAD_INDEX);
       r.w[1] = PARRYGPU_INVALID_ARG;
-    } else if (!has_generator(sh.types[a]) || !has_generator(sh.types[b])) {
+    } else if (!has_generator(sh, a, &h1) || !has_generator(sh, b, &h2)) {
       r.w[1] = PARRYGPU_UNSUPPORTED_PAIR;  // Err(Unsupported): the manifold is left as it was
     } else {
       r.w[1] = PARRYGPU_OK;
       ShapeDev s1 = load_shape(sh.types, sh.params, sh.pool, a);
       ShapeDev s2 = load_shape(sh.types, sh.params, sh.pool, b);
       Pose pos12 = pose_inv_mul(load_pose(sh.poses, a), load_pose(sh.poses, b));
-      bool overflow = false;
+      bool overflow = false, bad = false;
       if (s1.type == SH_BALL && s2.type == SH_BALL) {
         mf_ball_ball(r, pos12, s1.a, s2.a, prediction);
       } else if (s1.type == SH_CUBOID && s2.type == SH_CUBOID) {
         mf_cuboid_cuboid(r, pos12, v3(s1.a, s1.b, s1.c), v3(s2.a, s2.b, s2.c), prediction, &overflow);
       } else if (s1.type == SH_CAPSULE && s2.type == SH_CAPSULE) {
         mf_capsule_capsule(r, pos12, s1.a, s1.b, s2.a, s2.b, prediction);
-      } else if (s1.type == SH_BALL) {
-        mf_convex_ball(r, pose_inverse(pos12), s2, s1.a, prediction, true);
-      } else if (s2.type == SH_BALL) {
-        mf_convex_ball(r, pos12, s1, s2.a, prediction, false);
+      } else if (s1.type == SH_BALL || s2.type == SH_BALL) {
+        bool ball_first = s1.type == SH_BALL;
+        Pose cpos = ball_first ? pose_inverse(pos12) : pos12;
+        const ShapeDev& cs = ball_first ? s2 : s1;
+        const HullDev& ch = ball_first ? h2 : h1;
+        float radius = ball_first ? s1.a : s2.a;
+        if (cs.type != SH_CONVEX) {
+          mf_convex_ball(r, cpos, cs, radius, prediction, ball_first);
+        } else {
+          V3 proj;
+          Simplex s;
+          if (hull_project_gjk(cs, cpos.t, &proj, s, &iters)) {
+            uint32_t fid = hull_projection_feature(cs, ch, cpos.t, proj, false, &bad);
+            finish_convex_ball(r, cpos, proj, false, fid, radius, prediction, ball_first);
+          } else {
+            enqueue(queue, qcount, k, s, ball_first ? TAG_BALL_FIRST : TAG_BALL_SECOND);
+          }
+        }
       } else if (!try_update_contacts(r, pos12, COS_1_DEGREES, 1.0e-6f)) {
         // contact_manifold_pfm_pfm: GJK warm-started from the cached normal
         float br1, br2;
@@ -699,10 +851,11 @@ __global__ void __launch_bounds__(MF_THREADS) k_manifolds_main(ShapeArrays sh, c
         Simplex s;
         simplex_reset(s, cso_from_shapes(pos12, p1, p2, dir));
         GjkOut g = gjk_closest_points(pos12, p1, p2, total_prediction, s, &iters);
-        if (g.kind == GJK_INTERSECTION) enqueue(queue, qcount, k, s);
-        else finish_pfm(r, pos12, s1, s2, g.kind, g.p1, g.p2, g.dir, &overflow);
+        if (g.kind == GJK_INTERSECTION) enqueue(queue, qcount, k, s, TAG_PFM);
+        else finish_pfm(r, pos12, s1, h1, s2, h2, g.kind, g.p1, g.p2, g.dir, &overflow, &bad);
       }
       if (overflow) atomicOr(err, ERR_CAPACITY);
+      if (bad) atomicOr(err, ERR_BAD_INDEX);
     }
   }
   if (stats) {
@@ -711,8 +864,8 @@ __global__ void __launch_bounds__(MF_THREADS) k_manifolds_main(ShapeArrays sh, c
   }
 }
 
-__global__ void __launch_bounds__(MF_EPA_THREADS) k_manifolds_epa(ShapeArrays sh, const uint32_t* __restrict__ pairs, uint32_t* __restrict__ recs,
-                                                                  const uint32_t* __restrict__ queue,
+__global__ void __launch_bounds__(MF_EPA_THREADS) k_manifolds_epa(ShapeArrays sh, const uint32_t* __restrict__ pairs, float prediction,
+                                                                  uint32_t* __restrict__ recs, const uint32_t* __restrict__ queue,
                                                                   const unsigned long long* __restrict__ qcount, uint32_t* __restrict__ ws_pool,
                                                                   unsigned long long* __restrict__ stats, uint32_t* __restrict__ err) {
   const uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x;
@@ -720,25 +873,50 @@ __global__ void __launch_bounds__(MF_EPA_THREADS) k_manifolds_epa(ShapeArrays sh
   const unsigned long long total = *qcount;
   uint32_t iters = 0, calls = 0;
   for (unsigned long long e = slot; e < total; e += (unsigned long long)gridDim.x * blockDim.x) {
+    const uint32_t* q = queue + (size_t)e * QUEUE_WORDS;
     uint64_t k;
     Simplex s;
-    dequeue(queue + (size_t)e * QUEUE_WORDS, &k, &s);
+    dequeue(q, &k, &s);
+    uint32_t tag = q[QUEUE_WORDS - 1];
     uint32_t a = pairs[2 * k], b = pairs[2 * k + 1];
     ShapeDev s1 = load_shape(sh.types, sh.params, sh.pool, a);
     ShapeDev s2 = load_shape(sh.types, sh.params, sh.pool, b);
+    HullDev h1, h2;
+    load_hull(sh, a, &h1);
+    load_hull(sh, b, &h2);
     Pose pos12 = pose_inv_mul(load_pose(sh.poses, a), load_pose(sh.poses, b));
-    float br1, br2;
-    ShapeDev p1 = pfm_of(s1, &br1), p2 = pfm_of(s2, &br2);
     V3 q1, q2, nn;
     calls++;
-    int res = epa_closest_points(ws, pos12, p1, p2, s, &q1, &q2, &nn, &iters);
-    if (res == EPA_OVERFLOW) atomicOr(err, ERR_POLYTOPE_FULL);
-    bool overflow = false;
+    bool overflow = false, bad = false;
     Rec r{recs + (size_t)k * MF_WORDS};
-    // EPA failure: contact_support_map_support_map_with_params returns NoIntersection(x axis)
-    if (res == EPA_OK) finish_pfm(r, pos12, s1, s2, GJK_CLOSEST, q1, q2, nn, &overflow);
-    else finish_pfm(r, pos12, s1, s2, GJK_NO_INTERSECTION, q1, q2, v3(1.f, 0.f, 0.f), &overflow);
+    if (tag == TAG_PFM) {
+      float br1, br2;
+      ShapeDev p1 = pfm_of(s1, &br1), p2 = pfm_of(s2, &br2);
+      int res = epa_closest_points(ws, pos12, p1, p2, s, &q1, &q2, &nn, &iters);
+      if (res == EPA_OVERFLOW) atomicOr(err, ERR_POLYTOPE_FULL);
+      // EPA failure: contact_support_map_support_map_with_params returns NoIntersection(x axis)
+      if (res == EPA_OK) finish_pfm(r, pos12, s1, h1, s2, h2, GJK_CLOSEST, q1, q2, nn, &overflow, &bad);
+      else finish_pfm(r, pos12, s1, h1, s2, h2, GJK_NO_INTERSECTION, q1, q2, v3(1.f, 0.f, 0.f), &overflow, &bad);
+    } else {
+      // the ball centre is inside the hull: EPA projection (point_support_map.rs:42-55)
+      bool ball_first = tag == TAG_BALL_FIRST;
+      Pose cpos = ball_first ? pose_inverse(pos12) : pos12;
+      const ShapeDev& cs = ball_first ? s2 : s1;
+      const HullDev& ch = ball_first ? h2 : h1;
+      float radius = ball_first ? s1.a : s2.a;
+      V3 center = cpos.t;
+      Pose m{0.f, 0.f, 0.f, 1.f, -center};
+      Pose minv = pose_inverse(m);
+      ShapeDev origin;
+      origin.type = SH_ORIGIN;
+      int res = epa_closest_points(ws, minv, cs, origin, s, &q1, &q2, &nn, &iters);
+      if (res == EPA_OVERFLOW) atomicOr(err, ERR_POLYTOPE_FULL);
+      V3 proj = res == EPA_OK ? q1 : center;
+      uint32_t fid = hull_projection_feature(cs, ch, center, proj, true, &bad);
+      finish_convex_ball(r, cpos, proj, true, fid, radius, prediction, ball_first);
+    }
     if (overflow) atomicOr(err, ERR_CAPACITY);
+    if (bad) atomicOr(err, ERR_BAD_INDEX);
   }
   if (stats) {
     uint32_t w = __reduce_add_sync(0xffffffffu, iters);
@@ -789,7 +967,7 @@ parrygpu_status parrygpu_contact_manifolds(parrygpu_ctx* ctx, const parrygpu_sha
   }
   {
     KernelTimer kt(ctx, "manifolds_epa");
-    k_manifolds_epa<<<epa_blocks, MF_EPA_THREADS, 0, ctx->stream>>>(sh, (const uint32_t*)dp, (uint32_t*)d_rec, ctx->ct_queue.as<uint32_t>(),
+    k_manifolds_epa<<<epa_blocks, MF_EPA_THREADS, 0, ctx->stream>>>(sh, (const uint32_t*)dp, prediction, (uint32_t*)d_rec, ctx->ct_queue.as<uint32_t>(),
                                                                    ctr, ctx->epa_ws.as<uint32_t>(), ctr + 1, ctx->d_err);
     kt.stop();
     PG_LAUNCHED(ctx);

@@ -1,0 +1,50 @@
+"""ConvexPolyhedron topology (the host-side input of the hull contact-manifold generators).
+
+build_polyhedra(pool, first, count) runs ConvexPolyhedron::from_convex_hull for many point clouds
+at once through libparrygpu's host builder (parrygpu_polyhedra_build) and returns the hull points
+and the topology arrays in the parrygpu_polyhedra layout (include/parry_gpu.h).
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+TOPOLOGY_KEYS = ("face_normals", "face_ranges", "face_vertices", "face_edges", "vertex_ranges", "vertex_faces", "vertex_edges",
+                 "edge_dirs")
+
+
+def build_polyhedra(pool: np.ndarray, first: np.ndarray, count: np.ndarray, threads: int = 0):
+    """Returns (points (m, 3) f32, hulls (n, 8) u32, topology dict). hulls rows: first vertex (in
+    `points`), vertex count, first face, face count, first edge, edge count, ok, 0."""
+    from ._capi import lib, check
+    pool = np.ascontiguousarray(pool, np.float32).reshape(-1, 3)
+    first = np.ascontiguousarray(first, np.uint32)
+    count = np.ascontiguousarray(count, np.uint32)
+    n = len(first)
+    L = lib()
+    h = C.c_void_p()
+    check(L.parrygpu_polyhedra_build(pool.ctypes.data, first.ctypes.data, count.ctypes.data, n, int(threads), C.byref(h)))
+    try:
+        sizes = np.zeros(5, np.uint64)
+        check(L.parrygpu_polyhedra_sizes(h, sizes.ctypes.data))
+        npts, nf, nfe, nve, ne = (int(x) for x in sizes)
+        points = np.zeros((npts, 3), np.float32)
+        hulls = np.zeros((n, 8), np.uint32)
+        topo = {
+            "face_normals": np.zeros((nf, 3), np.float32), "face_ranges": np.zeros((nf, 2), np.uint32),
+            "face_vertices": np.zeros(nfe, np.uint32), "face_edges": np.zeros(nfe, np.uint32),
+            "vertex_ranges": np.zeros((npts, 2), np.uint32), "vertex_faces": np.zeros(nve, np.uint32),
+            "vertex_edges": np.zeros(nve, np.uint32), "edge_dirs": np.zeros((ne, 3), np.float32),
+        }
+        check(L.parrygpu_polyhedra_copy(h, points.ctypes.data, hulls.ctypes.data, *[topo[k].ctypes.data for k in TOPOLOGY_KEYS]))
+    finally:
+        L.parrygpu_polyhedra_builder_destroy(h)
+    return points, hulls, topo
+
+
+def empty_topology() -> dict:
+    return {"face_normals": np.zeros((0, 3), np.float32), "face_ranges": np.zeros((0, 2), np.uint32),
+            "face_vertices": np.zeros(0, np.uint32), "face_edges": np.zeros(0, np.uint32),
+            "vertex_ranges": np.zeros((0, 2), np.uint32), "vertex_faces": np.zeros(0, np.uint32),
+            "vertex_edges": np.zeros(0, np.uint32), "edge_dirs": np.zeros((0, 3), np.float32)}

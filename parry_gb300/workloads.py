@@ -142,15 +142,18 @@ def broadphase_shapes(n: int = 131072, extent: float = 200.0, seed: int = 0x9A77
     return ShapeSet.from_arrays(types, params.astype(np.float32), poses.astype(np.float32))
 
 
-def primitive_pairs(n_pairs: int, seed: int = 0x9A77E3):
+def primitive_pairs(n_pairs: int, seed: int = 0x9A77E3, hulls: bool = True, n_hull_shapes: int = 4096):
     """Contact-manifold workload: pair k = (shape 2k at the identity, shape 2k+1 at a random relative
-    pose: uniform rotation, translation = unit direction x U[0.5, 3]). Types are balls, cuboids and
-    capsules drawn uniformly per shape (all six pair kinds); ball radius U[0.5, 1], cuboid half
-    extents U[0.4, 1] each, capsule half height U[0.2, 0.8] and radius U[0.3, 0.6].
-    Returns (types u32, params f32 (n, 4), poses f32 (n, 7), pairs (n_pairs, 2) u32)."""
-    from .shapes import BALL, CUBOID, CAPSULE
+    pose: uniform rotation, translation = unit direction x U[0.5, 3]). Kinds are drawn uniformly per
+    shape among balls (radius U[0.5, 1]), cuboids (half extents U[0.4, 1]), capsules (half height
+    U[0.2, 0.8], radius U[0.3, 0.6]) and, with `hulls`, convex hulls of 16-64 points on spheres
+    scaled per axis by U[0.25, 1] (ConvexPolyhedron topology; `n_hull_shapes` distinct hulls shared
+    by all hull shapes). Returns (types u32, params f32 (n, 4), poses f32 (n, 7), pool, polyhedra,
+    pairs (n_pairs, 2) u32); polyhedra is None without hulls."""
+    from .shapes import BALL, CUBOID, CAPSULE, CONVEX
     n = 2 * n_pairs
-    types = (splitmix64(seed, 1, n) % np.uint64(3)).astype(np.uint32)
+    kinds = 4 if hulls else 3
+    types = (splitmix64(seed, 1, n) % np.uint64(kinds)).astype(np.uint32)
     params = np.zeros((n, 4), np.float64)
     ball, cub, cap = types == BALL, types == CUBOID, types == CAPSULE
     params[ball, 0] = uniform(seed, 2, n, 0.5, 1.0)[ball]
@@ -158,12 +161,27 @@ def primitive_pairs(n_pairs: int, seed: int = 0x9A77E3):
         params[cub, j] = uniform(seed, 3 + j, n, 0.4, 1.0)[cub]
     params[cap, 0] = uniform(seed, 6, n, 0.2, 0.8)[cap]
     params[cap, 1] = uniform(seed, 7, n, 0.3, 0.6)[cap]
+    params = params.astype(np.float32)
+    pool = np.zeros((0, 3), np.float32)
+    poly = None
+    if hulls:
+        from .polyhedra import build_polyhedra
+        cloud, first, count = ellipsoid_hulls(n_hull_shapes, seed, 50, 16, 64)
+        # ellipsoid_hulls scales by U[0.5, 2]; halve to keep sizes comparable with the primitives
+        pool, hull_rec, topo = build_polyhedra(cloud * 0.5, first, count)
+        poly = (hull_rec, topo)
+        cvx = types == CONVEX
+        pick = (splitmix64(seed, 8, n) % np.uint64(n_hull_shapes)).astype(np.int64)
+        pu = params.view(np.uint32)
+        pu[cvx, 0] = hull_rec[pick[cvx], 0]
+        pu[cvx, 1] = hull_rec[pick[cvx], 1]
+        pu[cvx, 2] = np.where(hull_rec[pick[cvx], 6] == 1, pick[cvx] + 1, 0).astype(np.uint32)
     poses = np.zeros((n, 7), np.float64)
     poses[:, 3] = 1.0
     poses[1::2, 0:4] = _unit_quats(seed, 20, n_pairs)
     poses[1::2, 4:7] = _sphere_dirs(seed, 30, n_pairs) * uniform(seed, 32, n_pairs, 0.5, 3.0)[:, None]
     pairs = np.stack([np.arange(0, n, 2), np.arange(1, n, 2)], axis=1).astype(np.uint32)
-    return types, params.astype(np.float32), poses.astype(np.float32), pairs
+    return types, params, poses.astype(np.float32), pool, poly, pairs
 
 
 def drifted_poses(poses: np.ndarray, frame: int, seed: int = 0x9A77E4, dt: float = 1.0 / 60.0, speed: float = 0.3,

@@ -126,3 +126,27 @@ def moved_poses(poses: np.ndarray, frame: int, seed: int, step: float = 0.01, an
     out[:, 3] = dw * qw - di * qi - dj * qj - dk * qk
     out[:, :4] /= np.linalg.norm(out[:, :4], axis=1, keepdims=True)
     return out.astype(np.float32)
+
+
+def hull_scene(n: int, seed: int, extent: float = 5.0):
+    """Balls, cuboids, capsules and convex hulls (16-64 points on scaled spheres, built as
+    ConvexPolyhedron topology), types cycling 0..3, at random poses. Returns (ShapeSet, poses)."""
+    from parry_gb300 import workloads as W
+    rng = np.random.default_rng(seed)
+    s = ShapeSet()
+    pool, first, count = W.ellipsoid_hulls(64, seed=seed, stream=3, nmin=16, nmax=64)
+    q = rng.normal(size=(n, 4))
+    q /= np.linalg.norm(q, axis=1, keepdims=True)
+    poses = np.concatenate([q, rng.uniform(-extent, extent, (n, 3))], axis=1).astype(np.float32)
+    for i in range(n):
+        t = i % 4
+        if t == 0:
+            s.add_ball(rng.uniform(0.3, 1.2), poses[i])
+        elif t == 1:
+            s.add_cuboid(rng.uniform(0.3, 1.2, 3), poses[i])
+        elif t == 2:
+            s.add_capsule(rng.uniform(0.2, 0.9), rng.uniform(0.2, 0.6), poses[i])
+        else:
+            h = (i // 4) % 64
+            s.add_convex_hull(pool[first[h]:first[h] + count[h]], poses[i])
+    return s, poses

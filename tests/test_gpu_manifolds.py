@@ -123,3 +123,29 @@ def test_unsupported_and_invalid(gpu_ctx, oracle_lib):
     with pytest.raises(pg.ParryGpuError):
         pg.contact_manifolds(gpu_ctx, s, bad, 0.0, r)
     assert r["status"][0] == 1  # PARRYGPU_INVALID_ARG
+
+
+@pytest.mark.parametrize("seed", [3, 4])
+def test_hull_frames_bit_exact(gpu_ctx, oracle_lib, seed):
+    """Scenes with ConvexPolyhedron hulls (16-64 points) next to balls, cuboids and capsules, over
+    several frames: pfm-pfm with hull faces, convex-ball with hull features, EPA fallbacks."""
+    import parry_gb300 as pg
+    from tests._contact_cases import hull_scene
+    O = oracle_lib
+    shapes0, q0 = hull_scene(1600, seed, extent=6.0)
+    pairs = brute_force_pairs(O.shape_aabbs(shapes0, 0.3))
+    t = shapes0.arrays()[0]
+    kinds = {(int(t[a]), int(t[b])) for a, b in pairs}
+    assert {(3, 3), (0, 3), (1, 3), (2, 3)} <= kinds or {(3, 3), (3, 0), (3, 1), (3, 2)} & kinds
+    g, w = M.new_manifolds(len(pairs)), M.new_manifolds(len(pairs))
+    for f in range(4):
+        shapes = shapes0.with_poses(moved_poses(q0, f, seed + 200, step=0.02, angle=0.02))
+        st = pg.contact_manifolds(gpu_ctx, shapes, pairs, 0.05, g, want_stats=True)
+        O.contact_manifolds(shapes, pairs, 0.05, M.as_words(w))
+        assert_records_equal(g, w)
+        assert np.all(g["status"] == M.STATUS_OK)
+        if f == 0:
+            assert st["epa_calls"] > 0
+        vals = np.arange(len(pairs) * M.MAX_POINTS, dtype=np.float32).reshape(-1, M.MAX_POINTS) * 0.25 + f
+        g["points"]["data"] = vals
+        w["points"]["data"] = vals

@@ -228,3 +228,70 @@ def test_flipped_pairs_mirror(oracle_lib, kinds):
         np.testing.assert_allclose(r1["points"]["dist"][live, 0], r2["points"]["dist"][live, 0], atol=2e-6)
         np.testing.assert_allclose(r1["points"]["local_p1"][live, 0], r2["points"]["local_p2"][live, 0], atol=2e-5)
         np.testing.assert_array_equal(r1["points"]["fid1"][live, 0], r2["points"]["fid2"][live, 0])
+
+
+def test_hull_topology_is_a_convex_polyhedron():
+    """The host hull builder's topology: closed (Euler V - E + F with merged faces), every vertex
+    behind every face plane, unit normals, counter-clockwise faces, consistent adjacency."""
+    from tests._contact_cases import hull_scene
+    s, _ = hull_scene(64, 4)
+    t, p, q, pool = s.arrays()
+    hulls, topo = s.polyhedra()
+    assert len(hulls) == 16 and np.all(hulls[:, 6] == 1)
+    for r in hulls:
+        v0, nv, f0, nf, e0, ne = (int(x) for x in r[:6])
+        pts = pool[v0:v0 + nv].astype(np.float64)
+        fr = topo["face_ranges"][f0:f0 + nf]
+        fn = topo["face_normals"][f0:f0 + nf].astype(np.float64)
+        np.testing.assert_allclose(np.linalg.norm(fn, axis=1), 1.0, atol=1e-6)
+        assert int(fr[:, 1].sum()) >= 3 * nf and np.all(fr[:, 1] >= 3)
+        for f in range(nf):
+            vids = topo["face_vertices"][fr[f, 0]:fr[f, 0] + fr[f, 1]]
+            a = pts[vids[0]]
+            assert ((pts - a) @ fn[f]).max() < 1e-5
+            # counter-clockwise around the outward normal
+            c = np.cross(pts[vids[1]] - pts[vids[0]], pts[vids[2]] - pts[vids[0]])
+            assert c @ fn[f] > 0
+        # each vertex's adjacency lists the faces it belongs to
+        vr = topo["vertex_ranges"][v0:v0 + nv]
+        for v in range(nv):
+            faces = set(topo["vertex_faces"][vr[v, 0]:vr[v, 0] + vr[v, 1]].tolist())
+            expect = {f for f in range(nf) if v in topo["face_vertices"][fr[f, 0]:fr[f, 0] + fr[f, 1]]}
+            assert faces == expect
+
+
+def test_hull_manifolds_agree_with_contact_query(oracle_lib):
+    """Hull pairs (pfm-pfm with ConvexPolyhedron features, convex-ball with hull features) against
+    the contact query on the same scene."""
+    from tests._contact_cases import hull_scene
+    O = oracle_lib
+    shapes, _ = hull_scene(700, 21)
+    pairs = brute_force_pairs(O.shape_aabbs(shapes, 0.1))
+    t = shapes.arrays()[0]
+    kinds = {(int(t[a]), int(t[b])) for a, b in pairs}
+    assert {(3, 3), (0, 3), (1, 3), (2, 3)} & kinds
+    pred = 0.1
+    rec = M.new_manifolds(len(pairs))
+    st = O.contact_manifolds(shapes, pairs, pred, M.as_words(rec), threads=4)
+    assert st["unsupported"] == 0
+    has, out, _ = O.contacts(shapes, pairs, pred, precision="f64", threads=4)
+    n = rec["n_points"]
+    deep = has.astype(bool) & (out[:, 12] < -1e-3)
+    assert np.all(n[deep] > 0)
+    assert np.all(n[~has.astype(bool)] == 0)
+    hull_pairs = (t[pairs[:, 0]] == 3) | (t[pairs[:, 1]] == 3)
+    checked = 0
+    for k in np.nonzero(deep & hull_pairs)[0]:
+        # the GJK/EPA point is one of the manifold points (pfm_pfm pushes it; convex-ball has only
+        # it); clipped feature vertices may lie deeper along the normal
+        dists = rec[k]["points"]["dist"][:n[k]]
+        assert np.min(np.abs(dists - out[k, 12])) < 2e-3, k
+        assert dists.min() <= out[k, 12] + 2e-3, k
+        checked += 1
+    assert checked > 50
+    # hull-ball contacts carry the hull feature (face, edge or vertex) of the projection
+    hb = np.nonzero(deep & (((t[pairs[:, 0]] == 3) & (t[pairs[:, 1]] == 0)) | ((t[pairs[:, 0]] == 0) & (t[pairs[:, 1]] == 3))))[0]
+    assert len(hb) > 5
+    for k in hb:
+        f = rec[k]["points"]["fid1"][0] if t[pairs[k, 0]] == 3 else rec[k]["points"]["fid2"][0]
+        assert (int(f) >> 30) in (1, 2, 3)
