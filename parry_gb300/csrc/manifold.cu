@@ -1,5 +1,5 @@
 // Batched persistent contact manifolds (parry3d's ContactManifold) for convex pairs of balls,
-// cuboids and capsules, updated in place from one frame to the next.
+// cuboids, capsules and ConvexPolyhedron hulls, updated in place from one frame to the next.
 //
 // Paths relative to the parry repository:
 //   record update / matching  src/query/contact_manifolds/contact_manifold.rs:662-770
@@ -16,8 +16,8 @@
 //
 // Pipeline (one stream):
 //   k_manifolds_main  one thread per pair. Analytic generators finish in place; the polygonal-feature
-//                     path (cuboid-capsule) runs GJK and, when GJK ends inside the Minkowski
-//                     difference, appends (pair, simplex) to the EPA queue.
+//                     path (cuboid/capsule/hull pairs) runs GJK and the hull-ball path a GJK point
+//                     projection; when GJK ends inside, (pair, simplex, tag) goes to the EPA queue.
 //   k_manifolds_epa   persistent loop over the queue (epa_device.cuh workspace slots), then the same
 //                     feature clipping as the main kernel.
 // Every step keeps the reference's evaluation order (compiled with --fmad=false) so the records match
