@@ -371,6 +371,88 @@ def manifolds_section(ctx, stream, steps: int, warmup: int, n_pairs: int, flush)
     }
 
 
+def scene_section(ctx, stream, frames: int, warmup: int, flush) -> dict:
+    """The per-frame pipeline on 262,144 moving shapes (ball / cuboid / capsule / hull, 25 % each) in
+    an 800-wide cube with 4,194,304 rays per frame: integrate, AABBs, refit, pairs, manifolds carried
+    per pair, rays; `frames` frames replayed from a CUDA graph, a stage split from one eager frame, the
+    end-to-end frame with its outputs read back to the host, and the oracle frame on the host cores."""
+    import numpy as np
+    import torch
+    import parry_gb300 as pg
+    from parry_gb300 import workloads as W
+    from oracle import build as ob
+    ob.build()
+    from oracle import oracle as O
+
+    t, prm, pos, pool, poly, vel, rays = W.frame_scene()
+    shapes = pg.ShapeSet.from_arrays(t, prm, pos, pool, poly)
+    pred, dt, max_toi = 0.1, 1.0 / 60.0, 100.0
+    sc = pg.Scene(ctx, shapes, vel, pred, 1 << 20)
+    sc.set_rays(torch.from_numpy(rays).cuda(), max_toi)
+    sc.step(dt, 2 * max(1, (warmup + 1) // 2), use_graph=True)
+    torch.cuda.synchronize()
+    l0 = ctx.kernel_launches
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    flush.zero_()
+    a.record(stream)
+    sc.step(dt, frames, use_graph=True)
+    b.record(stream)
+    torch.cuda.synchronize()
+    graph_ms = a.elapsed_time(b) / frames
+    launches = ctx.kernel_launches - l0
+    frame_no, npairs = sc.info()
+    # stage split: one eager frame with per-stage events
+    ctx.enable_kernel_timing(True)
+    ctx.reset_kernel_timing()
+    sc.step(dt, 1, use_graph=False)
+    stages = {}
+    for name in ("integrate", "aabbs", "refit", "pairs", "carry", "manifolds", "rays"):
+        ms, n = ctx.kernel_time("scene_" + name)
+        stages[name] = round(ms / max(n, 1), 4)
+    ctx.enable_kernel_timing(False)
+    st = sc.read()
+    npts = st["manifolds"]["n_points"]
+    hits = int((st["ray_part"] != pg.NO_HIT).sum())
+    # end to end: each frame's outputs (pairs, manifold records, ray hits) read back to the host
+    e2e = []
+    for _ in range(3):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        sc.step(dt, 1, use_graph=False)
+        out = sc.read()
+        e2e.append((time.perf_counter() - t0) * 1e3)
+    e2e_ms = statistics.mean(e2e)
+    d2h = out["poses"].nbytes + out["pairs"].nbytes + out["manifolds"].nbytes + out["ray_part"].nbytes + \
+        out["ray_toi"].nbytes + out["ray_normal"].nbytes
+    sc.close()
+    # the oracle frame on the host cores: the full shape set, a 262,144-ray sample scaled to 4,194,304
+    threads = os.cpu_count() or 1
+    sample = 262144
+    t0 = time.perf_counter()
+    O.scene_frames(shapes, vel, pred, dt, 1, threads=threads)
+    t_frame = time.perf_counter() - t0
+    moved = shapes.with_poses(O.integrate(pos, vel, dt))
+    comp = O.Compound(moved)
+    t0 = time.perf_counter()
+    comp.cast_rays_and_get_normal(rays[:sample], max_toi, solid=True, threads=threads)
+    t_rays = (time.perf_counter() - t0) * (len(rays) / sample)
+    cpu_frame_ms = (t_frame + t_rays) * 1e3
+    return {
+        "workload": "262,144 shapes (ball/cuboid/capsule/hull 16-64 points, 25 % each, sizes log-uniform [0.25, 4]) in "
+                    "[-400, 400)^3, v U[-5, 5]^3, w U[-1, 1]^3, dt 1/60, prediction 0.1, 4,194,304 rays (max_toi 100) per frame",
+        "metric": "frames/s", "value": round(1e3 / graph_ms, 2), "unit": "frames/s", "ms_per_frame": round(graph_ms, 4),
+        "frames": frames, "graph": True, "gpu_launches": launches, "pairs_per_frame": int(npairs),
+        "pairs_with_points": int((npts > 0).sum()), "ray_hits": hits,
+        "rays_per_s_in_pipeline": round(len(rays) * 1e3 / graph_ms, 1),
+        "stage_ms_eager_frame": stages,
+        "e2e": {"value": round(1e3 / e2e_ms, 2), "unit": "frames/s", "ms_per_step": round(e2e_ms, 3), "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": int(d2h), "note": "each frame's poses, pairs, manifold records and ray hits read to the host"},
+        "cpu_baseline": {"value": round(1e3 / cpu_frame_ms, 3), "unit": "frames/s", "cores": threads, "kind": "port",
+                         "sample": f"one oracle frame on all shapes (binned BVH rebuilt) plus rays timed on {sample} and scaled "
+                                   f"to {len(rays)}; C++ restatement of parry3d f32"},
+    }
+
+
 def learned_section(ctx, stream, dev_shapes, dev_pairs, n_eval: int, n_train: int, steps: int, flush) -> dict:
     """Learned warm start: train the MLP on the plain GJK/EPA's final directions of `n_train`
     held-out-seed hull pairs, then compare plain and learned init directions on the evaluation
@@ -574,8 +656,11 @@ def run_gb300(args) -> int:
     contacts = None
     learned = None
     manifolds = None
+    scene = None
     if args.manifold_pairs > 0:
         manifolds = manifolds_section(ctx, stream, args.steps, args.warmup, args.manifold_pairs, flush)
+    if args.scene_frames > 0:
+        scene = scene_section(ctx, stream, args.scene_frames, args.warmup, flush)
     if args.contact_pairs > 0:
         contacts = contacts_section(ctx, stream, args.steps, args.warmup, args.contact_pairs, flush)
         if args.train_pairs > 0:
@@ -613,6 +698,7 @@ def run_gb300(args) -> int:
             "contacts": contacts,
             "learned_warm_start": learned,
             "manifolds": manifolds,
+            "frame_pipeline": scene,
         }
         print(json.dumps(line), flush=True)
     ctx.close()
@@ -632,6 +718,8 @@ def main() -> int:
                     help="hull pairs of the GJK/EPA section (0 skips it)")
     ap.add_argument("--manifold-pairs", type=int, default=1 << 20,
                     help="ball/cuboid/capsule pairs of the contact-manifold section (0 skips it)")
+    ap.add_argument("--scene-frames", type=int, default=100,
+                    help="frames of the per-frame pipeline section (0 skips it)")
     ap.add_argument("--train-pairs", type=int, default=1 << 21,
                     help="training pairs of the learned warm-start section (0 skips it)")
     args = ap.parse_args()

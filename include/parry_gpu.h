@@ -287,6 +287,36 @@ typedef struct parrygpu_manifold {
 parrygpu_status parrygpu_contact_manifolds(parrygpu_ctx* ctx, const parrygpu_shapes* shapes, const uint32_t* pairs, uint64_t n_pairs,
                                            float prediction, parrygpu_manifold* manifolds, parrygpu_gjk_stats* stats);
 
+/* ---- per-frame pipeline over moving shapes ----
+ * No single reference counterpart: one frame chains the parry calls a physics engine makes each step
+ * on a set of convex shapes —
+ *   pose integration (decision D-5, parry has no integrator: x += v dt; q := normalize(q + dt/2 (0, w) q)),
+ *   Shape::compute_aabb(pos).loosened(prediction / 2) (aabb.rs:982), Bvh refit (bvh_refit.rs:170),
+ *   Bvh::traverse_bvtt_single_tree (bvh_traverse_bvtt.rs:19), contact_manifold_convex_convex per pair
+ *   (default_query_dispatcher.rs:749) with each pair's manifold kept from the previous frame while the
+ *   pair persists (a new pair starts from ContactManifold::new()), and
+ *   RayCast::cast_ray_and_get_normal of a fixed ray set against the shapes (Compound semantics,
+ *   ray_composite_shape.rs:86-105, lowest shape index on exact ties).
+ * velocities: n x 6 floats (linear xyz, angular xyz, world frame). The scene copies every input; the
+ * BVH is built once at creation and refit each frame. pair_capacity bounds the pairs kept per frame
+ * (pairs beyond it are dropped and raise CAPACITY_EXCEEDED at the next sync). */
+typedef struct parrygpu_scene parrygpu_scene;
+parrygpu_status parrygpu_scene_create(parrygpu_ctx* ctx, const parrygpu_shapes* shapes, const float* velocities, float prediction,
+                                      uint64_t pair_capacity, parrygpu_scene** out);
+void parrygpu_scene_destroy(parrygpu_scene* scene);
+/* The rays cast each frame (n x 6 floats) and their max_toi; outputs are read with parrygpu_scene_read. */
+parrygpu_status parrygpu_scene_set_rays(parrygpu_ctx* ctx, parrygpu_scene* scene, const float* rays, uint64_t n_rays, float max_toi);
+/* Advances `frames` frames of duration dt, asynchronously. With use_graph != 0 the frame pair is
+ * captured once into a CUDA graph (re-captured when dt or the rays change) and replayed. */
+parrygpu_status parrygpu_scene_step(parrygpu_ctx* ctx, parrygpu_scene* scene, float dt, uint32_t frames, int use_graph);
+/* Frames advanced so far and the current frame's pair count (synchronises; reports device errors). */
+parrygpu_status parrygpu_scene_info(parrygpu_ctx* ctx, const parrygpu_scene* scene, uint64_t* frame, uint64_t* n_pairs);
+/* Copies the current state (every pointer may be NULL): poses (n x 7), the first min(cap, n_pairs)
+ * pairs (2 x u32, unsorted) with their manifold records, and the last frame's ray results (shape
+ * index or UINT32_MAX, toi, world normal). Synchronises. */
+parrygpu_status parrygpu_scene_read(parrygpu_ctx* ctx, const parrygpu_scene* scene, float* poses, uint32_t* pairs,
+                                    parrygpu_manifold* manifolds, uint64_t cap, uint32_t* ray_part, float* ray_toi, float* ray_normal);
+
 /* ---- learned GJK warm start (no reference counterpart: parry's init_dir hook is its only tie) ----
  * A 39 -> 128 -> 128 -> 128 -> 128 -> 3 MLP (GELU, BF16 weights and activations, FP32 accumulation
  * on the tensor cores) predicts contact_support_map_support_map_with_params's init_dir from the

@@ -399,6 +399,34 @@ void oracle_manifolds_f32(const uint32_t* types, const float* params, const floa
   if (stats) { stats[0] = gi.load(); stats[1] = ei.load(); stats[2] = ec.load(); stats[3] = un.load(); stats[4] = mx.load(); }
 }
 
+// Pose integration of the frame pipeline (decision D-5; parry has no integrator), f32, in this
+// evaluation order: x += v dt; r = (0, w) q; q := (q + r dt/2) / |q + r dt/2|.
+void oracle_integrate_f32(float* poses, const float* vel, uint64_t n, float dt) {
+  for (uint64_t i = 0; i < n; ++i) {
+    float* p = poses + 7 * i;
+    const float* v = vel + 6 * i;
+    float qi = p[0], qj = p[1], qk = p[2], qw = p[3];
+    float wx = v[3], wy = v[4], wz = v[5];
+    float h = 0.5f * dt;
+    float ri = (wx * qw + wy * qk) - wz * qj;
+    float rj = (wy * qw + wz * qi) - wx * qk;
+    float rk = (wz * qw + wx * qj) - wy * qi;
+    float rw = -((wx * qi + wy * qj) + wz * qk);
+    qi = qi + ri * h;
+    qj = qj + rj * h;
+    qk = qk + rk * h;
+    qw = qw + rw * h;
+    float l = std::sqrt(((qi * qi + qj * qj) + qk * qk) + qw * qw);
+    p[0] = qi / l;
+    p[1] = qj / l;
+    p[2] = qk / l;
+    p[3] = qw / l;
+    p[4] = p[4] + v[0] * dt;
+    p[5] = p[5] + v[1] * dt;
+    p[6] = p[6] + v[2] * dt;
+  }
+}
+
 uint64_t oracle_pairs_count(void* p) { return ((PairBuf*)p)->v.size() / 2; }
 void oracle_pairs_copy(void* p, uint32_t* out) { std::memcpy(out, ((PairBuf*)p)->v.data(), ((PairBuf*)p)->v.size() * 4); }
 void oracle_pairs_free(void* p) { delete (PairBuf*)p; }

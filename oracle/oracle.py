@@ -45,6 +45,7 @@ _SIGS = {
     "oracle_compound_cast_rays_f32": (None, [P, P, P, U64, F32, I32, I32, I32, P, P, P, P]),
     "oracle_compound_cast_rays_f64": (None, [P, P, P, U64, F32, I32, I32, I32, P, P, P, P]),
     "oracle_manifolds_f32": (None, [P, P, P, P, U32, U64, P, P, U64, F32, I32, P, P]),
+    "oracle_integrate_f32": (None, [P, P, U64, F32]),
     "oracle_pairs_count": (U64, [P]),
     "oracle_pairs_copy": (None, [P, P]),
     "oracle_pairs_free": (None, [P]),
@@ -288,3 +289,42 @@ class Compound:
             getattr(lib(), f"oracle_compound_free_{self.prec}")(self._h)
         except Exception:
             pass
+
+
+def integrate(poses: np.ndarray, velocities: np.ndarray, dt: float) -> np.ndarray:
+    """One pose-integration step of the frame pipeline (decision D-5), f32; returns new poses."""
+    out = np.ascontiguousarray(poses, np.float32).copy()
+    vel = np.ascontiguousarray(velocities, np.float32)
+    lib().oracle_integrate_f32(_p(out), _p(vel), len(out), float(dt))
+    return out
+
+
+def scene_frames(shapes, velocities: np.ndarray, prediction: float, dt: float, frames: int, rays: np.ndarray | None = None,
+                 max_toi: float = 100.0, threads: int | None = None) -> dict:
+    """The frame pipeline restated with the oracle pieces: integrate, AABBs loosened by prediction / 2,
+    binned-BVH self pairs, contact manifolds kept per pair across frames (new pairs start empty), and
+    the rays cast against the final frame's shapes (Compound semantics, lowest index on ties).
+    Returns poses, sorted pairs, their manifold words, and the ray results."""
+    poses = np.ascontiguousarray(shapes.arrays()[2], np.float32).copy()
+    records: dict = {}
+    pairs = np.zeros((0, 2), np.uint32)
+    recs = np.zeros((0, MANIFOLD_WORDS), np.uint32)
+    s = shapes
+    for _ in range(frames):
+        poses = integrate(poses, velocities, dt)
+        s = shapes.with_poses(poses)
+        aabbs = shape_aabbs(s, 0.5 * prediction)
+        pairs = canonical_sorted_pairs(Bvh(aabbs).traverse_bvtt_single_tree()) if len(aabbs) > 1 else np.zeros((0, 2), np.uint32)
+        recs = np.zeros((len(pairs), MANIFOLD_WORDS), np.uint32)
+        for i, (a, b) in enumerate(pairs):
+            old = records.get((int(a), int(b)))
+            if old is not None:
+                recs[i] = old
+        contact_manifolds(s, pairs, prediction, recs, threads=threads)
+        records = {(int(a), int(b)): recs[i].copy() for i, (a, b) in enumerate(pairs)}
+    out = {"poses": poses, "pairs": pairs, "manifolds": recs}
+    if rays is not None:
+        c = Compound(s)
+        part, toi, nrm = c.cast_rays_and_get_normal(rays, max_toi, solid=True, threads=threads)
+        out.update(ray_part=part, ray_toi=toi, ray_normal=nrm)
+    return out

@@ -15,6 +15,7 @@ one batched call here:
     Shape::compute_aabb(pos).loosened(m)               shape_aabbs(ctx, shapes, margin)
     query::contact(pos1, g1, pos2, g2, prediction)     contacts(ctx, shapes, pairs, prediction, init_dirs)
     dispatcher.contact_manifold_convex_convex(...)     contact_manifolds(ctx, shapes, pairs, prediction, manifolds)
+    a physics step's queries on moving shapes          Scene(ctx, shapes, velocities, prediction, capacity).step(dt, frames)
     Compound::new(shapes)                              Compound(ctx, shapes)
     Compound::cast_ray_and_get_normal(m, ray, t, s)    Compound.cast_rays_and_get_normal(rays, t, solid, pose)
 
@@ -31,7 +32,7 @@ import numpy as np
 from . import _capi
 from ._capi import ParryGpuError, lib, check
 
-__all__ = ["Context", "Bvh", "TriMesh", "Compound", "ShapeSet", "WarmStartMLP", "shape_aabbs", "contacts", "contact_manifolds",
+__all__ = ["Context", "Bvh", "TriMesh", "Compound", "ShapeSet", "Scene", "WarmStartMLP", "shape_aabbs", "contacts", "contact_manifolds",
            "new_manifolds", "ParryGpuError", "NO_HIT", "lib"]
 
 from .shapes import ShapeSet  # noqa: E402
@@ -353,6 +354,68 @@ def contact_manifolds(ctx: Context, shapes, pairs, prediction: float, manifolds,
     if want_stats:
         return {"gjk_iters": stats.gjk_iterations, "epa_iters": stats.epa_iterations, "epa_calls": stats.epa_calls}
     return None
+
+
+class Scene:
+    """The per-frame pipeline over moving convex shapes (parrygpu_scene): integrate (x += v dt,
+    q := normalize(q + dt/2 (0, w) q)), AABBs loosened by prediction / 2, BVH refit, overlapping pairs,
+    contact manifolds kept per pair across frames, and a fixed ray set cast against the shapes."""
+
+    def __init__(self, ctx: Context, shapes, velocities, prediction: float, pair_capacity: int):
+        self._ctx = ctx
+        st = _StagedShapes(shapes)
+        self.n = st.n
+        kv, pv = _as_input(velocities, np.float32)
+        h = C.c_void_p()
+        check(lib().parrygpu_scene_create(ctx.handle, C.byref(st.struct), pv, float(prediction), int(pair_capacity), C.byref(h)),
+              ctx.handle)
+        self._h = h
+        self.capacity = int(pair_capacity)
+        self.n_rays = 0
+
+    def set_rays(self, rays, max_toi: float) -> None:
+        kr, pr = _as_input(rays, np.float32)
+        n = int(kr.shape[0]) if kr is not None else 0
+        check(lib().parrygpu_scene_set_rays(self._ctx.handle, self._h, pr, n, float(max_toi)), self._ctx.handle)
+        self.n_rays = n
+
+    def step(self, dt: float, frames: int = 1, use_graph: bool = True) -> None:
+        check(lib().parrygpu_scene_step(self._ctx.handle, self._h, float(dt), int(frames), 1 if use_graph else 0), self._ctx.handle)
+
+    def info(self) -> tuple[int, int]:
+        """(frames advanced, current pair count)."""
+        f, n = C.c_uint64(), C.c_uint64()
+        check(lib().parrygpu_scene_info(self._ctx.handle, self._h, C.byref(f), C.byref(n)), self._ctx.handle)
+        return f.value, n.value
+
+    def read(self) -> dict:
+        """Host copies of the current poses, pairs (unsorted) with their manifold records, and the
+        last frame's ray results."""
+        from .manifold import new_manifolds
+        _, npairs = self.info()
+        npairs = min(npairs, self.capacity)
+        poses = np.empty((self.n, 7), np.float32)
+        pairs = np.empty((npairs, 2), np.uint32)
+        recs = new_manifolds(npairs)
+        part = np.empty(self.n_rays, np.uint32)
+        toi = np.empty(self.n_rays, np.float32)
+        nrm = np.empty((self.n_rays, 3), np.float32)
+        check(lib().parrygpu_scene_read(self._ctx.handle, self._h, poses.ctypes.data, pairs.ctypes.data if npairs else None,
+                                        recs.ctypes.data if npairs else None, npairs, part.ctypes.data if self.n_rays else None,
+                                        toi.ctypes.data if self.n_rays else None, nrm.ctypes.data if self.n_rays else None),
+              self._ctx.handle)
+        return {"poses": poses, "pairs": pairs, "manifolds": recs, "ray_part": part, "ray_toi": toi, "ray_normal": nrm}
+
+    def close(self) -> None:
+        if getattr(self, "_h", None) is not None and self._h.value:
+            lib().parrygpu_scene_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 class Compound:

@@ -359,6 +359,13 @@ parrygpu_status pg::stage_shapes(parrygpu_ctx* ctx, const parrygpu_shapes* s, Sh
   return PARRYGPU_OK;
 }
 
+parrygpu_status pg::launch_shape_aabbs(parrygpu_ctx* ctx, const ShapeArrays& sh, uint64_t n, float margin, float* d_out) {
+  if (n == 0) return PARRYGPU_OK;
+  k_shape_aabbs<<<div_up(n, 256), 256, 0, ctx->stream>>>(sh, n, margin, d_out, ctx->d_err);
+  PG_LAUNCHED(ctx);
+  return PARRYGPU_OK;
+}
+
 parrygpu_status compound_part_aabbs(parrygpu_ctx* ctx, const parrygpu_compound* c, float* d_out) {
   ShapeArrays sh{c->types.as<uint32_t>(), c->params.as<float4>(), c->poses.as<float>(), c->pool.as<float>(), c->n, c->n_vertices};
   k_shape_aabbs<<<div_up(c->n, 256), 256, 0, ctx->stream>>>(sh, c->n, 0.0f, d_out, ctx->d_err);

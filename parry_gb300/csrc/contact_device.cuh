@@ -166,4 +166,14 @@ __device__ __forceinline__ void dequeue(const uint32_t* __restrict__ e, uint64_t
 // Stages a parrygpu_shapes description on the device (host arrays are copied, device arrays used in place).
 parrygpu_status stage_shapes(parrygpu_ctx* ctx, const parrygpu_shapes* s, ShapeArrays* out);
 
+// Launchers on device buffers, no allocation and no host synchronisation (graph-capturable):
+// Shape::compute_aabb(pos).loosened(margin) for n shapes (contact.cu);
+parrygpu_status launch_shape_aabbs(parrygpu_ctx* ctx, const ShapeArrays& sh, uint64_t n, float margin, float* d_out);
+// contact manifolds of the first min(cap, *d_count) pairs (manifold.cu) with caller-owned scratch
+// sized by manifolds_reserve(cap).
+parrygpu_status manifolds_reserve(parrygpu_ctx* ctx, uint64_t cap, DevBuf& queue, DevBuf& counters, DevBuf& epa_ws);
+parrygpu_status launch_manifolds(parrygpu_ctx* ctx, const ShapeArrays& sh, const uint32_t* d_pairs, uint64_t cap,
+                                 const unsigned long long* d_count, float prediction, uint32_t* d_recs, DevBuf& queue,
+                                 DevBuf& counters, DevBuf& epa_ws);
+
 }  // namespace pg

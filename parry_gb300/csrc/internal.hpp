@@ -141,6 +141,15 @@ parrygpu_status launch_trimesh_rays(parrygpu_ctx* ctx, const parrygpu_trimesh* m
 // their sorted position instead of the AABB index.
 parrygpu_status lbvh_build(parrygpu_ctx* ctx, parrygpu_bvh* bvh, const float* d_aabbs, uint32_t n, bool leaf_data_is_position);
 parrygpu_status lbvh_refit(parrygpu_ctx* ctx, parrygpu_bvh* bvh, const float* d_aabbs);
+// traverse_bvtt_single_tree into device buffers: pairs beyond `cap` are counted in *d_count but not
+// written. No allocation, no host synchronisation.
+parrygpu_status launch_self_pairs(parrygpu_ctx* ctx, const parrygpu_bvh* bvh, uint32_t* d_pairs, unsigned long long cap,
+                                  unsigned long long* d_count);
+
+// ---- shape-set ray casts (shape_ray.cu) on device buffers; `bvh` leaves hold shape indices ----
+parrygpu_status launch_shape_rays(parrygpu_ctx* ctx, const parrygpu_bvh* bvh, const uint32_t* types, const float* params,
+                                  const float* poses, const float* pool, const float* d_rays, uint32_t n, float max_toi, uint32_t* d_part,
+                                  float* d_toi, float* d_nrm);
 
 // ---- shapes (contact.cu) ----
 // World AABBs of a compound's parts (Shape::compute_aabb(pos)) into d_out (n x 6 floats).

@@ -449,6 +449,17 @@ static parrygpu_status run_pairs(parrygpu_ctx* ctx, uint32_t* pairs, uint64_t ca
   return PARRYGPU_OK;
 }
 
+parrygpu_status launch_self_pairs(parrygpu_ctx* ctx, const parrygpu_bvh* bvh, uint32_t* d_pairs, unsigned long long cap,
+                                  unsigned long long* d_count) {
+  uint32_t n = bvh->n_leaves;
+  if (n < 2) return PARRYGPU_OK;
+  k_self_pairs<<<div_up(n, PAIR_THREADS), PAIR_THREADS, 0, ctx->stream>>>(bvh->wide.as<WideNode>(), bvh->info.as<uint2>(),
+                                                                          bvh->leaf_parent.as<uint32_t>(), bvh->leaf_index.as<uint32_t>(), n,
+                                                                          d_pairs, cap, d_count, ctx->d_err);
+  PG_LAUNCHED(ctx);
+  return PARRYGPU_OK;
+}
+
 extern "C" {
 
 parrygpu_status parrygpu_bvh_build(parrygpu_ctx* ctx, const float* aabbs, uint32_t n, parrygpu_bvh** out) {

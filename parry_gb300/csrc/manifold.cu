@@ -796,11 +796,13 @@ __device__ __forceinline__ bool hull_project_gjk(const ShapeDev& cs, V3 center, 
   return false;
 }
 
+// `d_n` (may be null) holds a device-side pair count; the kernel then handles min(n, *d_n) pairs.
 __global__ void __launch_bounds__(MF_THREADS) k_manifolds_main(ShapeArrays sh, const uint32_t* __restrict__ pairs, uint64_t n, float prediction,
                                                                uint32_t* __restrict__ recs, uint32_t* __restrict__ queue,
                                                                unsigned long long* __restrict__ qcount, unsigned long long* __restrict__ stats,
-                                                               uint32_t* __restrict__ err) {
+                                                               uint32_t* __restrict__ err, const unsigned long long* __restrict__ d_n) {
   uint64_t k = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+  if (d_n && *d_n < n) n = *d_n;
   uint32_t iters = 0;
   if (k < n) {
     Rec r{recs + (size_t)k * MF_WORDS};
@@ -930,6 +932,34 @@ __global__ void __launch_bounds__(MF_EPA_THREADS) k_manifolds_epa(ShapeArrays sh
 
 }  // namespace
 
+// Manifold update of the first min(cap, *d_count) pairs on device buffers, without host
+// synchronisation or allocation: the frame pipeline's narrow phase, capturable in a CUDA graph. The
+// EPA queue, counters and polytope workspaces are the caller's (sized by manifolds_reserve), so a
+// captured graph never points at context scratch that a later call may reallocate.
+parrygpu_status pg::manifolds_reserve(parrygpu_ctx* ctx, uint64_t cap, DevBuf& queue, DevBuf& counters, DevBuf& epa_ws) {
+  PG_CUDA(ctx, queue.reserve((size_t)cap * QUEUE_WORDS * 4));
+  PG_CUDA(ctx, counters.reserve(64));
+  uint32_t epa_blocks = (uint32_t)(ctx->sm_count > 0 ? ctx->sm_count : 152) * 8;
+  PG_CUDA(ctx, epa_ws.reserve((size_t)(epa_blocks * MF_EPA_THREADS / 32) * EPA_SLOT_GROUP_BYTES));
+  return PARRYGPU_OK;
+}
+
+parrygpu_status pg::launch_manifolds(parrygpu_ctx* ctx, const ShapeArrays& sh, const uint32_t* d_pairs, uint64_t cap,
+                                     const unsigned long long* d_count, float prediction, uint32_t* d_recs, DevBuf& queue,
+                                     DevBuf& counters, DevBuf& epa_ws) {
+  if (cap == 0) return PARRYGPU_OK;
+  uint32_t epa_blocks = (uint32_t)(ctx->sm_count > 0 ? ctx->sm_count : 152) * 8;
+  unsigned long long* ctr = counters.as<unsigned long long>();
+  PG_CUDA(ctx, cudaMemsetAsync(ctr, 0, 64, ctx->stream));
+  k_manifolds_main<<<div_up(cap, MF_THREADS), MF_THREADS, 0, ctx->stream>>>(sh, d_pairs, cap, prediction, d_recs, queue.as<uint32_t>(), ctr,
+                                                                           nullptr, ctx->d_err, d_count);
+  PG_LAUNCHED(ctx);
+  k_manifolds_epa<<<epa_blocks, MF_EPA_THREADS, 0, ctx->stream>>>(sh, d_pairs, prediction, d_recs, queue.as<uint32_t>(), ctr,
+                                                                 epa_ws.as<uint32_t>(), nullptr, ctx->d_err);
+  PG_LAUNCHED(ctx);
+  return PARRYGPU_OK;
+}
+
 extern "C" {
 
 parrygpu_status parrygpu_contact_manifolds(parrygpu_ctx* ctx, const parrygpu_shapes* shapes, const uint32_t* pairs, uint64_t n_pairs,
@@ -961,7 +991,7 @@ parrygpu_status parrygpu_contact_manifolds(parrygpu_ctx* ctx, const parrygpu_sha
     KernelTimer kt(ctx, "manifolds_main");
     k_manifolds_main<<<div_up(n_pairs, MF_THREADS), MF_THREADS, 0, ctx->stream>>>(sh, (const uint32_t*)dp, n_pairs, prediction,
                                                                                (uint32_t*)d_rec, ctx->ct_queue.as<uint32_t>(), ctr, ctr + 1,
-                                                                               ctx->d_err);
+                                                                               ctx->d_err, nullptr);
     kt.stop();
     PG_LAUNCHED(ctx);
   }

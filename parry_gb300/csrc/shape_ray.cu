@@ -344,6 +344,18 @@ static parrygpu_status compound_copy_in(parrygpu_ctx* ctx, DevBuf& dst, const vo
   return PARRYGPU_OK;
 }
 
+parrygpu_status launch_shape_rays(parrygpu_ctx* ctx, const parrygpu_bvh* bvh, const uint32_t* types, const float* params,
+                                  const float* poses, const float* pool, const float* d_rays, uint32_t n, float max_toi, uint32_t* d_part,
+                                  float* d_toi, float* d_nrm) {
+  if (n == 0 || bvh->n_leaves == 0) return PARRYGPU_OK;
+  CompoundDev cd{types, (const float4*)params, poses, pool};
+  Pose pose{0.f, 0.f, 0.f, 1.f, v3(0.f, 0.f, 0.f)};
+  k_compound_rays<<<div_up(n, 128), 128, 0, ctx->stream>>>(bvh->wide.as<WideNode>(), cd, d_rays, n, max_toi, 1, 0, pose, d_part, d_toi,
+                                                           d_nrm, ctx->d_err);
+  PG_LAUNCHED(ctx);
+  return PARRYGPU_OK;
+}
+
 extern "C" {
 
 parrygpu_status parrygpu_compound_create(parrygpu_ctx* ctx, const parrygpu_shapes* shapes, parrygpu_compound** out) {

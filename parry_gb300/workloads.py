@@ -205,3 +205,44 @@ def drifted_poses(poses: np.ndarray, frame: int, seed: int = 0x9A77E4, dt: float
     out[:, 3] = dw * qw - di * qi - dj * qj - dk * qk
     out[:, :4] /= np.linalg.norm(out[:, :4], axis=1, keepdims=True)
     return out.astype(np.float32)
+
+
+def frame_scene(n: int = 262144, n_rays: int = 4194304, extent: float = 400.0, seed: int = 0x9A77E4):
+    """Per-frame pipeline workload: n shapes, kinds drawn uniformly per shape among balls (radius
+    log-uniform [0.25, 4]), cuboids (half extents log-uniform [0.25, 4], uniform rotation), capsules
+    (half height and radius log-uniform [0.25, 4]) and convex hulls of 16-64 points on spheres scaled
+    per axis by U[0.5, 2] (ConvexPolyhedron topology, one hull per hull shape); centres
+    U([-extent, extent)^3), velocities U[-5, 5]^3, angular velocities U[-1, 1]^3. Rays: origins
+    U([-extent, extent)^3), directions uniform on the sphere.
+    Returns (types, params, poses, pool, polyhedra, velocities (n, 6), rays (n_rays, 6))."""
+    from .shapes import BALL, CUBOID, CAPSULE, CONVEX
+    from .polyhedra import build_polyhedra
+    types = (splitmix64(seed, 1, n) % np.uint64(4)).astype(np.uint32)
+    params = np.zeros((n, 4), np.float64)
+    ball, cub, cap, cvx = types == BALL, types == CUBOID, types == CAPSULE, types == CONVEX
+    params[ball, 0] = _log_uniform(seed, 2, n, 0.25, 4.0)[ball]
+    for j in range(3):
+        params[cub, j] = _log_uniform(seed, 3 + j, n, 0.25, 4.0)[cub]
+    params[cap, 0] = _log_uniform(seed, 6, n, 0.25, 4.0)[cap]
+    params[cap, 1] = _log_uniform(seed, 7, n, 0.25, 4.0)[cap]
+    params = params.astype(np.float32)
+    hull_ids = np.nonzero(cvx)[0]
+    cloud, first, count = ellipsoid_hulls(len(hull_ids), seed, 50, 16, 64)
+    pool, hulls, topo = build_polyhedra(cloud, first, count)
+    pu = params.view(np.uint32)
+    pu[hull_ids, 0] = hulls[:, 0]
+    pu[hull_ids, 1] = hulls[:, 1]
+    pu[hull_ids, 2] = np.where(hulls[:, 6] == 1, np.arange(len(hull_ids)) + 1, 0).astype(np.uint32)
+    poses = np.zeros((n, 7), np.float64)
+    poses[:, 0:4] = _unit_quats(seed, 20, n)
+    for j in range(3):
+        poses[:, 4 + j] = uniform(seed, 30 + j, n, -extent, extent)
+    vel = np.zeros((n, 6), np.float64)
+    for j in range(3):
+        vel[:, j] = uniform(seed, 40 + j, n, -5.0, 5.0)
+        vel[:, 3 + j] = uniform(seed, 43 + j, n, -1.0, 1.0)
+    rays = np.zeros((n_rays, 6), np.float64)
+    for j in range(3):
+        rays[:, j] = uniform(seed, 60 + j, n_rays, -extent, extent)
+    rays[:, 3:] = _sphere_dirs(seed, 63, n_rays)
+    return (types, params, poses.astype(np.float32), pool, (hulls, topo), vel.astype(np.float32), rays.astype(np.float32))
