@@ -147,9 +147,11 @@ parrygpu_status launch_self_pairs(parrygpu_ctx* ctx, const parrygpu_bvh* bvh, ui
                                   unsigned long long* d_count);
 
 // ---- shape-set ray casts (shape_ray.cu) on device buffers; `bvh` leaves hold shape indices ----
+// `order` (may be null): thread k casts ray order[k], stored at slot k of d_rays (the rays were
+// permuted into that order), and writes its results to slot order[k].
 parrygpu_status launch_shape_rays(parrygpu_ctx* ctx, const parrygpu_bvh* bvh, const uint32_t* types, const float* params,
-                                  const float* poses, const float* pool, const float* d_rays, uint32_t n, float max_toi, uint32_t* d_part,
-                                  float* d_toi, float* d_nrm);
+                                  const float* poses, const float* pool, const float* d_rays, const uint32_t* order, uint32_t n,
+                                  float max_toi, uint32_t* d_part, float* d_toi, float* d_nrm);
 
 // ---- shapes (contact.cu) ----
 // World AABBs of a compound's parts (Shape::compute_aabb(pos)) into d_out (n x 6 floats).

@@ -30,7 +30,7 @@ struct parrygpu_scene {
   parrygpu_bvh bvh;
   DevBuf pairs[2], recs[2], keys[2], vals[2], counts;
   DevBuf mf_queue, mf_counters, mf_epa;  // narrow-phase scratch owned by the scene (stable for the graph)
-  DevBuf rays, ray_part, ray_toi, ray_nrm;
+  DevBuf rays, ray_order, ray_part, ray_toi, ray_nrm;  // rays stored in Morton order of their origins
   int cur = 0;
   uint64_t frame = 0;
   cudaGraphExec_t exec = nullptr;
@@ -125,6 +125,15 @@ __global__ void k_table_insert(const uint32_t* __restrict__ pairs, const unsigne
   atomicOr(err, ERR_CAPACITY);
 }
 
+__global__ void k_gather_rays(const float* __restrict__ src, const uint32_t* __restrict__ order, uint64_t n, float* __restrict__ dst) {
+  uint64_t k = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  const float* a = src + 6 * (size_t)order[k];
+  float* b = dst + 6 * k;
+#pragma unroll
+  for (int j = 0; j < 6; ++j) b[j] = a[j];
+}
+
 }  // namespace
 
 static ShapeArrays scene_shapes(const parrygpu_scene* sc) {
@@ -203,7 +212,8 @@ static parrygpu_status scene_frame(parrygpu_ctx* ctx, parrygpu_scene* sc, float 
   if (sc->n_rays) {
     KernelTimer kt(ctx, "scene_rays");
     if ((s = launch_shape_rays(ctx, &sc->bvh, sc->types.as<uint32_t>(), sc->params.as<float>(), sc->poses.as<float>(), sc->pool.as<float>(),
-                               sc->rays.as<float>(), (uint32_t)sc->n_rays, sc->max_toi, sc->ray_part.as<uint32_t>(), sc->ray_toi.as<float>(),
+                               sc->rays.as<float>(), sc->ray_order.as<uint32_t>(), (uint32_t)sc->n_rays, sc->max_toi,
+                               sc->ray_part.as<uint32_t>(), sc->ray_toi.as<float>(),
                                sc->ray_nrm.as<float>())) != PARRYGPU_OK)
       return s;
     kt.stop();
@@ -325,7 +335,7 @@ void parrygpu_scene_destroy(parrygpu_scene* sc) {
   cudaDeviceSynchronize();  // frames in flight still read the scene's buffers
   drop_graph(sc);
   for (DevBuf* d : {&sc->types, &sc->params, &sc->poses, &sc->vel, &sc->pool, &sc->aabbs, &sc->counts, &sc->mf_queue, &sc->mf_counters,
-                    &sc->mf_epa, &sc->rays, &sc->ray_part,
+                    &sc->mf_epa, &sc->rays, &sc->ray_order, &sc->ray_part,
                     &sc->ray_toi, &sc->ray_nrm, &sc->bvh.wide, &sc->bvh.leaf_parent, &sc->bvh.node_parent, &sc->bvh.leaf_index,
                     &sc->bvh.flags, &sc->bvh.root_aabb, &sc->bvh.info})
     d->release();
@@ -346,13 +356,37 @@ parrygpu_status parrygpu_scene_set_rays(parrygpu_ctx* ctx, parrygpu_scene* sc, c
   PG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   drop_graph(sc);  // the captured frame bakes in the ray buffers
   parrygpu_status s;
-  if ((s = copy_in(ctx, sc->rays, rays, n_rays * 24)) != PARRYGPU_OK) return s;
+  // rays in input order into scratch, then permuted into the Morton order of their origins (coherent
+  // traversal); ray_order maps a stored slot back to the input slot for the results
+  uint32_t n = (uint32_t)n_rays;
+  PG_CUDA(ctx, sc->ray_order.reserve(n_rays * 4 + 16));
+  PG_CUDA(ctx, sc->rays.reserve(n_rays * 24 + 16));
+  if (n > 0) {
+    DevBuf tmp;
+    if ((s = copy_in(ctx, tmp, rays, n_rays * 24)) != PARRYGPU_OK) { tmp.release(); return s; }
+    if ((s = radix_sort_reserve(ctx, n)) != PARRYGPU_OK) { tmp.release(); return s; }
+    PG_CUDA(ctx, ctx->misc.reserve(64));
+    uint32_t* bounds = ctx->misc.as<uint32_t>() + 8;
+    if ((s = launch_ray_keys(ctx, tmp.as<float>(), n, bounds, ctx->sort_k[0].as<uint32_t>(), ctx->sort_v[0].as<uint32_t>())) !=
+        PARRYGPU_OK) {
+      tmp.release();
+      return s;
+    }
+    int rb;
+    if ((s = radix_sort_pairs(ctx, n, 30, &rb)) != PARRYGPU_OK) { tmp.release(); return s; }
+    PG_CUDA(ctx, cudaMemcpyAsync(sc->ray_order.ptr, ctx->sort_v[rb].ptr, n_rays * 4, cudaMemcpyDeviceToDevice, ctx->stream));
+    k_gather_rays<<<div_up(n_rays, SC_THREADS), SC_THREADS, 0, ctx->stream>>>(tmp.as<float>(), sc->ray_order.as<uint32_t>(), n_rays,
+                                                                             sc->rays.as<float>());
+    PG_LAUNCHED(ctx);
+    cudaError_t e = cudaStreamSynchronize(ctx->stream);
+    tmp.release();
+    if (e != cudaSuccess) return check_cuda(ctx, e, "scene ray ordering");
+  }
   PG_CUDA(ctx, sc->ray_part.reserve(n_rays * 4 + 16));
   PG_CUDA(ctx, sc->ray_toi.reserve(n_rays * 4 + 16));
   PG_CUDA(ctx, sc->ray_nrm.reserve(n_rays * 12 + 16));
   sc->n_rays = n_rays;
   sc->max_toi = max_toi;
-  if (!is_device_ptr(rays)) PG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   return PARRYGPU_OK;
 }
 

@@ -269,13 +269,17 @@ struct CompoundDev {
   const float* pool;
 };
 
+// Thread k handles ray r = order[k] (order may be null: r = k), read from slot k when the rays were
+// already permuted into that order (rays_permuted), else from slot r; results go to slot r.
 __global__ void __launch_bounds__(128) k_compound_rays(const WideNode* __restrict__ wide, CompoundDev cd, const float* __restrict__ rays,
                                                        uint32_t n, float max_toi, int solid, int has_pose, Pose cpose,
                                                        uint32_t* __restrict__ part_out, float* __restrict__ toi_out,
-                                                       float* __restrict__ normal_out, uint32_t* __restrict__ err) {
-  uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
-  if (r >= n) return;
-  const float* rp = rays + 6 * (size_t)r;
+                                                       float* __restrict__ normal_out, uint32_t* __restrict__ err,
+                                                       const uint32_t* __restrict__ order, int rays_permuted) {
+  uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  uint32_t r = order ? order[k] : k;
+  const float* rp = rays + 6 * (size_t)(rays_permuted ? k : r);
   V3 o = v3(rp[0], rp[1], rp[2]), dir = v3(rp[3], rp[4], rp[5]);
   if (has_pose) { o = pose_inv_point(cpose, o); dir = pose_inv_rotate(cpose, dir); }
   uint32_t zmask = (dir.x == 0.0f ? 1u : 0u) | (dir.y == 0.0f ? 2u : 0u) | (dir.z == 0.0f ? 4u : 0u);
@@ -345,13 +349,13 @@ static parrygpu_status compound_copy_in(parrygpu_ctx* ctx, DevBuf& dst, const vo
 }
 
 parrygpu_status launch_shape_rays(parrygpu_ctx* ctx, const parrygpu_bvh* bvh, const uint32_t* types, const float* params,
-                                  const float* poses, const float* pool, const float* d_rays, uint32_t n, float max_toi, uint32_t* d_part,
-                                  float* d_toi, float* d_nrm) {
+                                  const float* poses, const float* pool, const float* d_rays, const uint32_t* order, uint32_t n,
+                                  float max_toi, uint32_t* d_part, float* d_toi, float* d_nrm) {
   if (n == 0 || bvh->n_leaves == 0) return PARRYGPU_OK;
   CompoundDev cd{types, (const float4*)params, poses, pool};
   Pose pose{0.f, 0.f, 0.f, 1.f, v3(0.f, 0.f, 0.f)};
   k_compound_rays<<<div_up(n, 128), 128, 0, ctx->stream>>>(bvh->wide.as<WideNode>(), cd, d_rays, n, max_toi, 1, 0, pose, d_part, d_toi,
-                                                           d_nrm, ctx->d_err);
+                                                           d_nrm, ctx->d_err, order, order ? 1 : 0);
   PG_LAUNCHED(ctx);
   return PARRYGPU_OK;
 }
@@ -441,10 +445,22 @@ parrygpu_status parrygpu_compound_cast_rays(parrygpu_ctx* ctx, const parrygpu_co
     if (d_nrm) PG_CUDA(ctx, cudaMemsetAsync(d_nrm, 0, (size_t)n * 12, ctx->stream));
   } else {
     CompoundDev cd{c->types.as<uint32_t>(), c->params.as<float4>(), c->poses.as<float>(), c->pool.as<float>()};
+    const uint32_t* order = nullptr;
+    if (ctx->cfg.sort_rays && n > 4096) {  // Morton order of the origins: coherent traversal
+      if ((s = radix_sort_reserve(ctx, n)) != PARRYGPU_OK) return s;
+      PG_CUDA(ctx, ctx->misc.reserve(64));
+      uint32_t* bounds = ctx->misc.as<uint32_t>() + 8;
+      if ((s = launch_ray_keys(ctx, (const float*)d_rays, n, bounds, ctx->sort_k[0].as<uint32_t>(), ctx->sort_v[0].as<uint32_t>())) !=
+          PARRYGPU_OK)
+        return s;
+      int rb;
+      if ((s = radix_sort_pairs(ctx, n, 30, &rb)) != PARRYGPU_OK) return s;
+      order = ctx->sort_v[rb].as<uint32_t>();
+    }
     KernelTimer kt(ctx, "compound_rays");
     k_compound_rays<<<div_up(n, 128), 128, 0, ctx->stream>>>(c->bvh.wide.as<WideNode>(), cd, (const float*)d_rays, n, max_toi, solid,
                                                              pose7 ? 1 : 0, pose, (uint32_t*)d_part, (float*)d_toi, (float*)d_nrm,
-                                                             ctx->d_err);
+                                                             ctx->d_err, order, 0);
     kt.stop();
     PG_LAUNCHED(ctx);
   }
