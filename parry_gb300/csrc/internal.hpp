@@ -34,6 +34,13 @@ struct DevBuf {
   template <class T> T* as() const { return (T*)ptr; }
 };
 
+// Scratch of the wavefront shape-set ray cast (shape_ray.cu): candidate list, its counter, one
+// best-hit key and one overflow flag per ray.
+struct RayWaveScratch {
+  DevBuf cands, counter, keys, ovf;
+  uint64_t cap = 0;
+};
+
 struct parrygpu_ctx {
   int device = 0;
   cudaStream_t own_stream = nullptr;
@@ -48,6 +55,7 @@ struct parrygpu_ctx {
   DevBuf ray_keys, ray_order;
   // contact pipeline scratch: EPA queue (pair + simplex per entry) and per-slot polytope workspaces
   DevBuf ct_queue, ct_counters, epa_ws;
+  RayWaveScratch ray_wave;
   int sm_count = 0;
   // Optional per-kernel event timing (parrygpu_enable_kernel_timing).
   bool timing = false;
@@ -149,9 +157,11 @@ parrygpu_status launch_self_pairs(parrygpu_ctx* ctx, const parrygpu_bvh* bvh, ui
 // ---- shape-set ray casts (shape_ray.cu) on device buffers; `bvh` leaves hold shape indices ----
 // `order` (may be null): thread k casts ray order[k], stored at slot k of d_rays (the rays were
 // permuted into that order), and writes its results to slot order[k].
+// Runs the wavefront cast (shape_ray.cu) with `scratch` sized by shape_rays_reserve(n) beforehand.
+parrygpu_status shape_rays_reserve(parrygpu_ctx* ctx, RayWaveScratch& scratch, uint32_t n);
 parrygpu_status launch_shape_rays(parrygpu_ctx* ctx, const parrygpu_bvh* bvh, const uint32_t* types, const float* params,
                                   const float* poses, const float* pool, const float* d_rays, const uint32_t* order, uint32_t n,
-                                  float max_toi, uint32_t* d_part, float* d_toi, float* d_nrm);
+                                  float max_toi, uint32_t* d_part, float* d_toi, float* d_nrm, RayWaveScratch& scratch);
 
 // ---- shapes (contact.cu) ----
 // World AABBs of a compound's parts (Shape::compute_aabb(pos)) into d_out (n x 6 floats).

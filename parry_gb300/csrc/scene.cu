@@ -31,6 +31,7 @@ struct parrygpu_scene {
   DevBuf pairs[2], recs[2], keys[2], vals[2], counts;
   DevBuf mf_queue, mf_counters, mf_epa;  // narrow-phase scratch owned by the scene (stable for the graph)
   DevBuf rays, ray_order, ray_part, ray_toi, ray_nrm;  // rays stored in Morton order of their origins
+  RayWaveScratch ray_wave;
   int cur = 0;
   uint64_t frame = 0;
   cudaGraphExec_t exec = nullptr;
@@ -213,8 +214,8 @@ static parrygpu_status scene_frame(parrygpu_ctx* ctx, parrygpu_scene* sc, float 
     KernelTimer kt(ctx, "scene_rays");
     if ((s = launch_shape_rays(ctx, &sc->bvh, sc->types.as<uint32_t>(), sc->params.as<float>(), sc->poses.as<float>(), sc->pool.as<float>(),
                                sc->rays.as<float>(), sc->ray_order.as<uint32_t>(), (uint32_t)sc->n_rays, sc->max_toi,
-                               sc->ray_part.as<uint32_t>(), sc->ray_toi.as<float>(),
-                               sc->ray_nrm.as<float>())) != PARRYGPU_OK)
+                               sc->ray_part.as<uint32_t>(), sc->ray_toi.as<float>(), sc->ray_nrm.as<float>(), sc->ray_wave)) !=
+        PARRYGPU_OK)
       return s;
     kt.stop();
   }
@@ -340,6 +341,7 @@ void parrygpu_scene_destroy(parrygpu_scene* sc) {
                     &sc->bvh.flags, &sc->bvh.root_aabb, &sc->bvh.info})
     d->release();
   for (int k = 0; k < 9; ++k) sc->poly[k].release();
+  for (DevBuf* d : {&sc->ray_wave.cands, &sc->ray_wave.counter, &sc->ray_wave.keys, &sc->ray_wave.ovf}) d->release();
   for (int b = 0; b < 2; ++b) {
     sc->pairs[b].release();
     sc->recs[b].release();
@@ -382,6 +384,7 @@ parrygpu_status parrygpu_scene_set_rays(parrygpu_ctx* ctx, parrygpu_scene* sc, c
     tmp.release();
     if (e != cudaSuccess) return check_cuda(ctx, e, "scene ray ordering");
   }
+  if ((s = shape_rays_reserve(ctx, sc->ray_wave, n)) != PARRYGPU_OK) return s;
   PG_CUDA(ctx, sc->ray_part.reserve(n_rays * 4 + 16));
   PG_CUDA(ctx, sc->ray_toi.reserve(n_rays * 4 + 16));
   PG_CUDA(ctx, sc->ray_nrm.reserve(n_rays * 12 + 16));

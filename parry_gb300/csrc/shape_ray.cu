@@ -275,10 +275,12 @@ __global__ void __launch_bounds__(128) k_compound_rays(const WideNode* __restric
                                                        uint32_t n, float max_toi, int solid, int has_pose, Pose cpose,
                                                        uint32_t* __restrict__ part_out, float* __restrict__ toi_out,
                                                        float* __restrict__ normal_out, uint32_t* __restrict__ err,
-                                                       const uint32_t* __restrict__ order, int rays_permuted) {
+                                                       const uint32_t* __restrict__ order, int rays_permuted,
+                                                       const uint8_t* __restrict__ only) {
   uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= n) return;
   uint32_t r = order ? order[k] : k;
+  if (only && !only[r]) return;
   const float* rp = rays + 6 * (size_t)(rays_permuted ? k : r);
   V3 o = v3(rp[0], rp[1], rp[2]), dir = v3(rp[3], rp[4], rp[5]);
   if (has_pose) { o = pose_inv_point(cpose, o); dir = pose_inv_rotate(cpose, dir); }
@@ -340,6 +342,174 @@ __global__ void __launch_bounds__(128) k_compound_rays(const WideNode* __restric
   }
 }
 
+// ---- wavefront shape-set rays ----
+// The single-kernel traversal above carries the GJK ray cast's state (155 registers), which caps
+// the occupancy of the whole, latency-bound traversal. The wavefront form splits it:
+//   k_rays_wave   traversal + the analytic leaves (balls, cuboids, triangles) in few registers;
+//                 support-map leaves (capsules, hulls) whose box the ray enters before the best
+//                 analytic hit are appended to a candidate list, and the ray's best hit so far is
+//                 published as a 64-bit key (toi bits, shape index);
+//   k_rays_cand   one thread per candidate: the GJK ray cast (its result does not depend on the
+//                 max_toi bound, which only accepts or rejects), atomicMin of (toi, index);
+//   k_rays_finish the candidate holding its ray's minimum key writes the ray's result.
+// The minimum of (toi, index) over every hit with toi < max_toi is the single-kernel answer (nearest
+// hit, lowest index on exact ties). Rays whose candidates did not fit the list are redone by the
+// single kernel (mask `only`).
+struct RayCand {
+  uint32_t k, r, part, hit;
+  float t, nx, ny, nz;
+};
+
+__device__ __forceinline__ unsigned long long hit_key(float t, uint32_t part) {
+  return ((unsigned long long)__float_as_uint(t + 0.0f) << 32) | part;
+}
+
+__device__ __forceinline__ bool analytic_type(uint32_t t) { return t == SH_BALL || t == SH_CUBOID || t == SH_TRIANGLE; }
+
+// part_cast_ray for the analytic shapes only.
+__device__ __forceinline__ bool part_cast_ray_analytic(const ShapeDev& s, const Pose& pose, V3 wo, V3 wd, float max_toi, bool solid, float* toi,
+                                                       V3* n) {
+  V3 o = pose_inv_point(pose, wo), d = pose_inv_rotate(pose, wd);
+  V3 ln;
+  bool ok;
+  if (s.type == SH_BALL) ok = ray_ball(s.a, o, d, solid, max_toi, toi, &ln);
+  else if (s.type == SH_CUBOID) ok = ray_cuboid(v3(s.a, s.b, s.c), o, d, solid, max_toi, toi, &ln);
+  else ok = ray_triangle(ldv(s.pts), ldv(s.pts + 3), ldv(s.pts + 6), o, d, max_toi, toi, &ln);
+  if (ok) *n = pose_rotate(pose, ln);
+  return ok;
+}
+
+__device__ __forceinline__ void ray_of(const float* rays, const uint32_t* order, int permuted, uint32_t k, int has_pose, const Pose& cpose,
+                                       uint32_t* r, V3* o, V3* dir) {
+  *r = order ? order[k] : k;
+  const float* rp = rays + 6 * (size_t)(permuted ? k : *r);
+  *o = v3(rp[0], rp[1], rp[2]);
+  *dir = v3(rp[3], rp[4], rp[5]);
+  if (has_pose) { *o = pose_inv_point(cpose, *o); *dir = pose_inv_rotate(cpose, *dir); }
+}
+
+__global__ void __launch_bounds__(128) k_rays_wave(const WideNode* __restrict__ wide, CompoundDev cd, const float* __restrict__ rays, uint32_t n,
+                                                   float max_toi, int solid, int has_pose, Pose cpose, uint32_t* __restrict__ part_out,
+                                                   float* __restrict__ toi_out, float* __restrict__ normal_out, uint32_t* __restrict__ err,
+                                                   const uint32_t* __restrict__ order, int permuted, RayCand* __restrict__ cands,
+                                                   unsigned long long cap, unsigned long long* __restrict__ ccount,
+                                                   unsigned long long* __restrict__ keys, uint8_t* __restrict__ ovf) {
+  uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  uint32_t r;
+  V3 o, dir;
+  ray_of(rays, order, permuted, k, has_pose, cpose, &r, &o, &dir);
+  uint32_t zmask = (dir.x == 0.0f ? 1u : 0u) | (dir.y == 0.0f ? 2u : 0u) | (dir.z == 0.0f ? 4u : 0u);
+  V3 inv = v3(dir.x != 0.0f ? 1.0f / dir.x : 0.0f, dir.y != 0.0f ? 1.0f / dir.y : 0.0f, dir.z != 0.0f ? 1.0f / dir.z : 0.0f);
+  float best = max_toi;
+  uint32_t best_part = 0xffffffffu;
+  V3 best_n = v3(0.f, 0.f, 0.f);
+  bool have = false, overflow = false;
+  auto visit_leaf = [&](uint32_t part) {
+    uint32_t ty = cd.types[part];
+    if (!analytic_type(ty)) {
+      unsigned long long slot = atomicAdd(ccount, 1ull);
+      if (slot < cap) cands[slot] = RayCand{k, r, part, 0u, 0.f, 0.f, 0.f, 0.f};
+      else overflow = true;
+      return;
+    }
+    ShapeDev s = load_shape(cd.types, cd.params, cd.pool, part);
+    Pose p = load_pose(cd.poses, part);
+    float t;
+    V3 nn;
+    if (!part_cast_ray_analytic(s, p, o, dir, best, solid != 0, &t, &nn)) return;
+    if (t < best || (have && t == best && part < best_part)) { best = t; best_part = part; best_n = nn; have = true; }
+  };
+  WideNode w;
+  load_wide(wide, 0, &w);
+  if ((w.r.data & 0x3fffffffu) == 0u) {
+    float s0 = slab(w.l.mins, w.l.maxs, o, inv, zmask, max_toi);
+    if (s0 < max_toi) visit_leaf(w.l.children);
+  } else {
+    uint32_t stack[CRAY_STACK];
+    int sp = 0;
+    for (;;) {
+      float ls = slab(w.l.mins, w.l.maxs, o, inv, zmask, best);
+      float rs = slab(w.r.mins, w.r.maxs, o, inv, zmask, best);
+      const BvhNodeDev* nearn = &w.l;
+      const BvhNodeDev* farn = &w.r;
+      if (ls > rs) { float t = ls; ls = rs; rs = t; nearn = &w.r; farn = &w.l; }
+      uint32_t next = 0xffffffffu;
+      uint32_t far_child = farn->children, far_data = farn->data;
+      if (ls != FLT_MAX && (ls < best || (have && ls == best))) {
+        if ((nearn->data & 0x3fffffffu) == 1u) visit_leaf(nearn->children);
+        else next = nearn->children;
+      }
+      if (rs != FLT_MAX && (rs < best || (have && rs == best))) {
+        if ((far_data & 0x3fffffffu) == 1u) visit_leaf(far_child);
+        else if (next != 0xffffffffu) {
+          if (sp >= CRAY_STACK) { atomicOr(err, ERR_STACK_OVERFLOW); break; }
+          stack[sp++] = far_child;
+        } else next = far_child;
+      }
+      if (next == 0xffffffffu) {
+        if (sp == 0) break;
+        next = stack[--sp];
+      }
+      load_wide(wide, next, &w);
+    }
+  }
+  keys[r] = have ? hit_key(best, best_part) : ~0ull;
+  ovf[r] = overflow ? 1 : 0;
+  if (has_pose && have) best_n = pose_rotate(cpose, best_n);
+  part_out[r] = have ? best_part : 0xffffffffu;
+  toi_out[r] = have ? best : 0.0f;
+  if (normal_out) {
+    normal_out[3 * (size_t)r] = best_n.x;
+    normal_out[3 * (size_t)r + 1] = best_n.y;
+    normal_out[3 * (size_t)r + 2] = best_n.z;
+  }
+}
+
+// Candidates of the first min(cap, *ccount) entries; `n_cap` bounds the grid.
+__global__ void __launch_bounds__(128) k_rays_cand(CompoundDev cd, const float* __restrict__ rays, float max_toi, int solid, int has_pose,
+                                                   Pose cpose, const uint32_t* __restrict__ order, int permuted, RayCand* __restrict__ cands,
+                                                   unsigned long long cap, const unsigned long long* __restrict__ ccount,
+                                                   unsigned long long* __restrict__ keys) {
+  unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x;
+  unsigned long long c = *ccount;
+  if (i >= cap || i >= c) return;
+  RayCand cd_ = cands[i];
+  uint32_t r;
+  V3 o, dir;
+  ray_of(rays, order, permuted, cd_.k, has_pose, cpose, &r, &o, &dir);
+  ShapeDev s = load_shape(cd.types, cd.params, cd.pool, cd_.part);
+  Pose p = load_pose(cd.poses, cd_.part);
+  float t;
+  V3 nn;
+  // composite casts keep hits strictly below max_toi (CompositeShapeRef::cast_local_ray)
+  if (!part_cast_ray(s, p, o, dir, max_toi, solid != 0, &t, &nn) || !(t < max_toi)) return;
+  if (has_pose) nn = pose_rotate(cpose, nn);
+  cands[i].hit = 1u;
+  cands[i].t = t;
+  cands[i].nx = nn.x;
+  cands[i].ny = nn.y;
+  cands[i].nz = nn.z;
+  atomicMin(&keys[r], hit_key(t, cd_.part));
+}
+
+__global__ void __launch_bounds__(128) k_rays_finish(const RayCand* __restrict__ cands, unsigned long long cap,
+                                                     const unsigned long long* __restrict__ ccount, const unsigned long long* __restrict__ keys,
+                                                     uint32_t* __restrict__ part_out, float* __restrict__ toi_out, float* __restrict__ normal_out) {
+  unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x;
+  unsigned long long c = *ccount;
+  if (i >= cap || i >= c) return;
+  RayCand e = cands[i];
+  if (!e.hit || keys[e.r] != hit_key(e.t, e.part)) return;
+  part_out[e.r] = e.part;
+  toi_out[e.r] = e.t;
+  if (normal_out) {
+    normal_out[3 * (size_t)e.r] = e.nx;
+    normal_out[3 * (size_t)e.r + 1] = e.ny;
+    normal_out[3 * (size_t)e.r + 2] = e.nz;
+  }
+}
+
 }  // namespace
 
 static parrygpu_status compound_copy_in(parrygpu_ctx* ctx, DevBuf& dst, const void* src, size_t bytes) {
@@ -348,16 +518,46 @@ static parrygpu_status compound_copy_in(parrygpu_ctx* ctx, DevBuf& dst, const vo
   return PARRYGPU_OK;
 }
 
+parrygpu_status shape_rays_reserve(parrygpu_ctx* ctx, RayWaveScratch& sc, uint32_t n) {
+  uint64_t cap = 4ull * n + 1024;
+  PG_CUDA(ctx, sc.cands.reserve(cap * sizeof(RayCand)));
+  PG_CUDA(ctx, sc.counter.reserve(16));
+  PG_CUDA(ctx, sc.keys.reserve((size_t)n * 8 + 16));
+  PG_CUDA(ctx, sc.ovf.reserve((size_t)n + 16));
+  sc.cap = cap;
+  return PARRYGPU_OK;
+}
+
+// The wavefront cast of n rays (see k_rays_wave). No allocation, no host synchronisation.
+static parrygpu_status launch_wave(parrygpu_ctx* ctx, const WideNode* wide, CompoundDev cd, const float* d_rays, const uint32_t* order,
+                                   int permuted, uint32_t n, float max_toi, int solid, int has_pose, Pose pose, uint32_t* d_part,
+                                   float* d_toi, float* d_nrm, RayWaveScratch& sc) {
+  unsigned long long* cnt = sc.counter.as<unsigned long long>();
+  PG_CUDA(ctx, cudaMemsetAsync(cnt, 0, 8, ctx->stream));
+  k_rays_wave<<<div_up(n, 128), 128, 0, ctx->stream>>>(wide, cd, d_rays, n, max_toi, solid, has_pose, pose, d_part, d_toi, d_nrm, ctx->d_err,
+                                                       order, permuted, sc.cands.as<RayCand>(), sc.cap, cnt,
+                                                       sc.keys.as<unsigned long long>(), sc.ovf.as<uint8_t>());
+  PG_LAUNCHED(ctx);
+  k_rays_cand<<<div_up(sc.cap, 128), 128, 0, ctx->stream>>>(cd, d_rays, max_toi, solid, has_pose, pose, order, permuted,
+                                                            sc.cands.as<RayCand>(), sc.cap, cnt, sc.keys.as<unsigned long long>());
+  PG_LAUNCHED(ctx);
+  k_rays_finish<<<div_up(sc.cap, 128), 128, 0, ctx->stream>>>(sc.cands.as<RayCand>(), sc.cap, cnt, sc.keys.as<unsigned long long>(), d_part,
+                                                              d_toi, d_nrm);
+  PG_LAUNCHED(ctx);
+  // rays whose candidates overflowed the list: the single-kernel cast, for them only
+  k_compound_rays<<<div_up(n, 128), 128, 0, ctx->stream>>>(wide, cd, d_rays, n, max_toi, solid, has_pose, pose, d_part, d_toi, d_nrm,
+                                                           ctx->d_err, order, permuted, sc.ovf.as<uint8_t>());
+  PG_LAUNCHED(ctx);
+  return PARRYGPU_OK;
+}
+
 parrygpu_status launch_shape_rays(parrygpu_ctx* ctx, const parrygpu_bvh* bvh, const uint32_t* types, const float* params,
                                   const float* poses, const float* pool, const float* d_rays, const uint32_t* order, uint32_t n,
-                                  float max_toi, uint32_t* d_part, float* d_toi, float* d_nrm) {
+                                  float max_toi, uint32_t* d_part, float* d_toi, float* d_nrm, RayWaveScratch& scratch) {
   if (n == 0 || bvh->n_leaves == 0) return PARRYGPU_OK;
   CompoundDev cd{types, (const float4*)params, poses, pool};
   Pose pose{0.f, 0.f, 0.f, 1.f, v3(0.f, 0.f, 0.f)};
-  k_compound_rays<<<div_up(n, 128), 128, 0, ctx->stream>>>(bvh->wide.as<WideNode>(), cd, d_rays, n, max_toi, 1, 0, pose, d_part, d_toi,
-                                                           d_nrm, ctx->d_err, order, order ? 1 : 0);
-  PG_LAUNCHED(ctx);
-  return PARRYGPU_OK;
+  return launch_wave(ctx, bvh->wide.as<WideNode>(), cd, d_rays, order, order ? 1 : 0, n, max_toi, 1, 0, pose, d_part, d_toi, d_nrm, scratch);
 }
 
 extern "C" {
@@ -457,12 +657,12 @@ parrygpu_status parrygpu_compound_cast_rays(parrygpu_ctx* ctx, const parrygpu_co
       if ((s = radix_sort_pairs(ctx, n, 30, &rb)) != PARRYGPU_OK) return s;
       order = ctx->sort_v[rb].as<uint32_t>();
     }
+    if ((s = shape_rays_reserve(ctx, ctx->ray_wave, n)) != PARRYGPU_OK) return s;
     KernelTimer kt(ctx, "compound_rays");
-    k_compound_rays<<<div_up(n, 128), 128, 0, ctx->stream>>>(c->bvh.wide.as<WideNode>(), cd, (const float*)d_rays, n, max_toi, solid,
-                                                             pose7 ? 1 : 0, pose, (uint32_t*)d_part, (float*)d_toi, (float*)d_nrm,
-                                                             ctx->d_err, order, 0);
+    s = launch_wave(ctx, c->bvh.wide.as<WideNode>(), cd, (const float*)d_rays, order, 0, n, max_toi, solid, pose7 ? 1 : 0, pose,
+                    (uint32_t*)d_part, (float*)d_toi, (float*)d_nrm, ctx->ray_wave);
     kt.stop();
-    PG_LAUNCHED(ctx);
+    if (s != PARRYGPU_OK) return s;
   }
   if (c1) PG_CUDA(ctx, cudaMemcpyAsync(part, d_part, (size_t)n * 4, cudaMemcpyDeviceToHost, ctx->stream));
   if (c2) PG_CUDA(ctx, cudaMemcpyAsync(toi, d_toi, (size_t)n * 4, cudaMemcpyDeviceToHost, ctx->stream));

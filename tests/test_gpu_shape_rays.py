@@ -59,3 +59,29 @@ def test_set_poses_refit(gpu_ctx, oracle_lib):
     p, t, n = comp.cast_rays_and_get_normal(rays, 60.0, pose=pose)
     po, to, no = oracle_lib.Compound(s2).cast_rays_and_get_normal(rays, 60.0, pose=pose)
     _compare(p, t, n, po, to, no, "after set_poses")
+
+
+def test_candidate_overflow_falls_back_exactly(gpu_ctx, oracle_lib):
+    """A row of capsules and hulls along every ray: the support-map candidates overflow the wavefront
+    list (4 per ray + 1024), and the affected rays are recast by the single-kernel path."""
+    O = oracle_lib
+    s = pg.ShapeSet()
+    rng = np.random.default_rng(5)
+    pts = rng.normal(size=(24, 3))
+    pts /= np.linalg.norm(pts, axis=1, keepdims=True)
+    for i in range(400):
+        pose = (0.0, 0.0, 0.0, 1.0, 2.0 * i, 0.0, 0.0)
+        if i % 2:
+            s.add_capsule(0.4, 0.3, pose)
+        else:
+            s.add_convex(pts * 0.5, pose)
+    n = 64
+    o = np.stack([np.full(n, -5.0), rng.uniform(-0.2, 0.2, n), rng.uniform(-0.2, 0.2, n)], 1)
+    d = np.tile([1.0, 0.0, 0.0], (n, 1)) + rng.normal(scale=1e-3, size=(n, 3))
+    rays = np.concatenate([o, d], 1).astype(np.float32)
+    comp = pg.Compound(gpu_ctx, s)
+    for solid in (True, False):
+        p, t, nn = comp.cast_rays_and_get_normal(rays, 1000.0, solid=solid)
+        po, to, no = O.Compound(s).cast_rays_and_get_normal(rays, 1000.0, solid=solid)
+        _compare(p, t, nn, po, to, no, f"solid={solid}")
+        assert np.all(p != pg.NO_HIT)
