@@ -371,7 +371,7 @@ def manifolds_section(ctx, stream, steps: int, warmup: int, n_pairs: int, flush)
     }
 
 
-def scene_section(ctx, stream, frames: int, warmup: int, flush) -> dict:
+def scene_section(ctx, stream, frames: int, warmup: int, flush, n_shapes: int = 262144, n_rays: int = 4194304) -> dict:
     """The per-frame pipeline on 262,144 moving shapes (ball / cuboid / capsule / hull, 25 % each) in
     an 800-wide cube with 4,194,304 rays per frame: integrate, AABBs, refit, pairs, manifolds carried
     per pair, rays; `frames` frames replayed from a CUDA graph, a stage split from one eager frame, the
@@ -384,10 +384,12 @@ def scene_section(ctx, stream, frames: int, warmup: int, flush) -> dict:
     ob.build()
     from oracle import oracle as O
 
-    t, prm, pos, pool, poly, vel, rays = W.frame_scene()
+    # the shapes' density is kept when the scene is scaled down (cube side 800 at 262,144 shapes)
+    extent = 400.0 * (n_shapes / 262144.0) ** (1.0 / 3.0)
+    t, prm, pos, pool, poly, vel, rays = W.frame_scene(n_shapes, n_rays, extent)
     shapes = pg.ShapeSet.from_arrays(t, prm, pos, pool, poly)
     pred, dt, max_toi = 0.1, 1.0 / 60.0, 100.0
-    sc = pg.Scene(ctx, shapes, vel, pred, 1 << 20)
+    sc = pg.Scene(ctx, shapes, vel, pred, max(1 << 16, 4 * n_shapes))
     sc.set_rays(torch.from_numpy(rays).cuda(), max_toi)
     sc.step(dt, 2 * max(1, (warmup + 1) // 2), use_graph=True)
     torch.cuda.synchronize()
@@ -427,7 +429,7 @@ def scene_section(ctx, stream, frames: int, warmup: int, flush) -> dict:
     sc.close()
     # the oracle frame on the host cores: the full shape set, a 262,144-ray sample scaled to 4,194,304
     threads = os.cpu_count() or 1
-    sample = 262144
+    sample = min(262144, len(rays))
     t0 = time.perf_counter()
     O.scene_frames(shapes, vel, pred, dt, 1, threads=threads)
     t_frame = time.perf_counter() - t0
@@ -438,8 +440,9 @@ def scene_section(ctx, stream, frames: int, warmup: int, flush) -> dict:
     t_rays = (time.perf_counter() - t0) * (len(rays) / sample)
     cpu_frame_ms = (t_frame + t_rays) * 1e3
     return {
-        "workload": "262,144 shapes (ball/cuboid/capsule/hull 16-64 points, 25 % each, sizes log-uniform [0.25, 4]) in "
-                    "[-400, 400)^3, v U[-5, 5]^3, w U[-1, 1]^3, dt 1/60, prediction 0.1, 4,194,304 rays (max_toi 100) per frame",
+        "workload": f"{n_shapes:,} shapes (ball/cuboid/capsule/hull 16-64 points, 25 % each, sizes log-uniform [0.25, 4]) in "
+                    f"[-{extent:.0f}, {extent:.0f})^3, v U[-5, 5]^3, w U[-1, 1]^3, dt 1/60, prediction 0.1, {n_rays:,} rays "
+                    "(max_toi 100) per frame",
         "metric": "frames/s", "value": round(1e3 / graph_ms, 2), "unit": "frames/s", "ms_per_frame": round(graph_ms, 4),
         "frames": frames, "graph": True, "gpu_launches": launches, "pairs_per_frame": int(npairs),
         "pairs_with_points": int((npts > 0).sum()), "ray_hits": hits,
@@ -660,7 +663,7 @@ def run_gb300(args) -> int:
     if args.manifold_pairs > 0:
         manifolds = manifolds_section(ctx, stream, args.steps, args.warmup, args.manifold_pairs, flush)
     if args.scene_frames > 0:
-        scene = scene_section(ctx, stream, args.scene_frames, args.warmup, flush)
+        scene = scene_section(ctx, stream, args.scene_frames, args.warmup, flush, args.scene_shapes, args.scene_rays)
     if args.contact_pairs > 0:
         contacts = contacts_section(ctx, stream, args.steps, args.warmup, args.contact_pairs, flush)
         if args.train_pairs > 0:
@@ -720,6 +723,8 @@ def main() -> int:
                     help="ball/cuboid/capsule pairs of the contact-manifold section (0 skips it)")
     ap.add_argument("--scene-frames", type=int, default=100,
                     help="frames of the per-frame pipeline section (0 skips it)")
+    ap.add_argument("--scene-shapes", type=int, default=262144, help="shapes of the per-frame pipeline section")
+    ap.add_argument("--scene-rays", type=int, default=4194304, help="rays per frame of the per-frame pipeline section")
     ap.add_argument("--train-pairs", type=int, default=1 << 21,
                     help="training pairs of the learned warm-start section (0 skips it)")
     args = ap.parse_args()

@@ -12,34 +12,47 @@
 
 namespace pg {
 
-constexpr int EPA_MAX_VERTS = 128;
-constexpr int EPA_MAX_FACES = 512;
-constexpr int EPA_MAX_SIL = 64;
-constexpr int EPA_STACK = 256;
-constexpr int EPA_W_VERTS = 0;                                   // 9 words per vertex
-constexpr int EPA_W_FACES = EPA_W_VERTS + 9 * EPA_MAX_VERTS;     // 9 words per face
-constexpr int EPA_W_HEAP = EPA_W_FACES + 9 * EPA_MAX_FACES;      // 2 words per heap entry
-constexpr int EPA_W_SIL = EPA_W_HEAP + 2 * EPA_MAX_FACES;        // 1 word per silhouette edge
-constexpr int EPA_W_STACK = EPA_W_SIL + EPA_MAX_SIL;             // 1 word per stack entry
-constexpr int EPA_WORDS = EPA_W_STACK + EPA_STACK;               // words per slot
-constexpr size_t EPA_SLOT_GROUP_BYTES = (size_t)EPA_WORDS * 32 * 4;  // one warp's 32 slots
+// Fixed capacities and word offsets of one polytope workspace.
+template <int MV, int MF, int MS, int MSTK>
+struct EpaLayout {
+  static constexpr int MAX_VERTS = MV, MAX_FACES = MF, MAX_SIL = MS, STACK = MSTK;
+  static constexpr int W_VERTS = 0;                       // 9 words per vertex
+  static constexpr int W_FACES = W_VERTS + 9 * MV;        // 9 words per face
+  static constexpr int W_HEAP = W_FACES + 9 * MF;         // 2 words per heap entry
+  static constexpr int W_SIL = W_HEAP + 2 * MF;           // 1 word per silhouette edge
+  static constexpr int W_STACK = W_SIL + MS;              // 1 word per stack entry
+  static constexpr int WORDS = W_STACK + MSTK;            // words per workspace
+};
+// Per-thread workspaces in global memory, and the smaller per-warp workspaces in shared memory
+// (a pair that outgrows the latter is redone with the former).
+using EpaGlobalLayout = EpaLayout<128, 512, 64, 256>;
+using EpaSmemLayout = EpaLayout<64, 192, 64, 128>;
 
-struct EpaWs {
-  uint32_t* base;  // slot's first word (lane-interleaved, stride 32)
-  __device__ __forceinline__ uint32_t& w(int i) const { return base[(size_t)i * 32]; }
-  __device__ __forceinline__ float& f(int i) const { return reinterpret_cast<float&>(base[(size_t)i * 32]); }
+constexpr int EPA_MAX_VERTS = EpaGlobalLayout::MAX_VERTS;
+constexpr int EPA_MAX_FACES = EpaGlobalLayout::MAX_FACES;
+constexpr int EPA_WORDS = EpaGlobalLayout::WORDS;                     // words per slot
+constexpr size_t EPA_SLOT_GROUP_BYTES = (size_t)EPA_WORDS * 32 * 4;   // one warp's 32 slots
+
+// A workspace view: word i at base[i * STRIDE] (STRIDE 32: a lane-interleaved global slot; STRIDE 1:
+// a warp's shared-memory workspace, read and written identically by all its lanes).
+template <class L, int STRIDE>
+struct EpaWsT {
+  using Layout = L;
+  uint32_t* base;
+  __device__ __forceinline__ uint32_t& w(int i) const { return base[(size_t)i * STRIDE]; }
+  __device__ __forceinline__ float& f(int i) const { return reinterpret_cast<float&>(base[(size_t)i * STRIDE]); }
   // vertices
   __device__ __forceinline__ void set_vert(int v, const CSO& c) const {
-    int o = EPA_W_VERTS + 9 * v;
+    int o = L::W_VERTS + 9 * v;
     f(o) = c.p.x; f(o + 1) = c.p.y; f(o + 2) = c.p.z;
     f(o + 3) = c.o1.x; f(o + 4) = c.o1.y; f(o + 5) = c.o1.z;
     f(o + 6) = c.o2.x; f(o + 7) = c.o2.y; f(o + 8) = c.o2.z;
   }
-  __device__ __forceinline__ V3 vp(int v) const { int o = EPA_W_VERTS + 9 * v; return v3(f(o), f(o + 1), f(o + 2)); }
-  __device__ __forceinline__ V3 vo1(int v) const { int o = EPA_W_VERTS + 9 * v + 3; return v3(f(o), f(o + 1), f(o + 2)); }
-  __device__ __forceinline__ V3 vo2(int v) const { int o = EPA_W_VERTS + 9 * v + 6; return v3(f(o), f(o + 1), f(o + 2)); }
+  __device__ __forceinline__ V3 vp(int v) const { int o = L::W_VERTS + 9 * v; return v3(f(o), f(o + 1), f(o + 2)); }
+  __device__ __forceinline__ V3 vo1(int v) const { int o = L::W_VERTS + 9 * v + 3; return v3(f(o), f(o + 1), f(o + 2)); }
+  __device__ __forceinline__ V3 vo2(int v) const { int o = L::W_VERTS + 9 * v + 6; return v3(f(o), f(o + 1), f(o + 2)); }
   // faces: word0 = pts (3 x u8) | deleted << 24; word1 = adj0 | adj1 << 16; word2 = adj2; 3-5 normal; 6-8 bcoords
-  __device__ __forceinline__ int fo(int fid) const { return EPA_W_FACES + 9 * fid; }
+  __device__ __forceinline__ int fo(int fid) const { return L::W_FACES + 9 * fid; }
   __device__ __forceinline__ int pt(int fid, int k) const { return (w(fo(fid)) >> (8 * k)) & 0xff; }
   __device__ __forceinline__ bool deleted(int fid) const { return (w(fo(fid)) >> 24) != 0; }
   __device__ __forceinline__ void set_deleted(int fid) const { w(fo(fid)) |= 0x01000000u; }
@@ -54,13 +67,17 @@ struct EpaWs {
   __device__ __forceinline__ V3 normal(int fid) const { int o = fo(fid) + 3; return v3(f(o), f(o + 1), f(o + 2)); }
   __device__ __forceinline__ float bc(int fid, int k) const { return f(fo(fid) + 6 + k); }
 };
+using EpaWs = EpaWsT<EpaGlobalLayout, 32>;
+using EpaWsSmem = EpaWsT<EpaSmemLayout, 1>;
 
+template <class WS>
 struct EpaHeap {
-  const EpaWs* ws;
+  const WS* ws;
   int len;
-  __device__ __forceinline__ uint32_t id(int i) const { return ws->w(EPA_W_HEAP + 2 * i); }
-  __device__ __forceinline__ float nd(int i) const { return ws->f(EPA_W_HEAP + 2 * i + 1); }
-  __device__ __forceinline__ void put(int i, uint32_t fid, float d) const { ws->w(EPA_W_HEAP + 2 * i) = fid; ws->f(EPA_W_HEAP + 2 * i + 1) = d; }
+  static constexpr int H = WS::Layout::W_HEAP;
+  __device__ __forceinline__ uint32_t id(int i) const { return ws->w(H + 2 * i); }
+  __device__ __forceinline__ float nd(int i) const { return ws->f(H + 2 * i + 1); }
+  __device__ __forceinline__ void put(int i, uint32_t fid, float d) const { ws->w(H + 2 * i) = fid; ws->f(H + 2 * i + 1) = d; }
   // FaceId::cmp: -1 / 0 / 1 (NaN -> 0)
   static __device__ __forceinline__ int cmp(float a, float b) { return a < b ? -1 : (a > b ? 1 : 0); }
   __device__ int sift_up(int start, int pos) {
@@ -119,7 +136,8 @@ struct EpaHeap {
 };
 
 // Face::new (epa3.rs:90-118): writes face `fid`, returns whether the origin projects inside it.
-static __device__ __noinline__ bool epa_new_face(const EpaWs& ws, int fid, int p0, int p1, int p2, int a0, int a1, int a2) {
+template <class WS>
+static __device__ __noinline__ bool epa_new_face(const WS& ws, int fid, int p0, int p1, int p2, int a0, int a1, int a2) {
   V3 A = ws.vp(p0), B = ws.vp(p1), C = ws.vp(p2);
   Loc loc;
   V3 proj = project_triangle(A, B, C, v3(0.f, 0.f, 0.f), &loc);
@@ -153,20 +171,23 @@ static __device__ __noinline__ bool epa_new_face(const EpaWs& ws, int fid, int p
   return inside;
 }
 
-__device__ __forceinline__ void epa_face_closest_points(const EpaWs& ws, int fid, V3* p1, V3* p2) {
+template <class WS>
+__device__ __forceinline__ void epa_face_closest_points(const WS& ws, int fid, V3* p1, V3* p2) {
   int a = ws.pt(fid, 0), b = ws.pt(fid, 1), c = ws.pt(fid, 2);
   float b0 = ws.bc(fid, 0), b1 = ws.bc(fid, 1), b2 = ws.bc(fid, 2);
   *p1 = (ws.vo1(a) * b0 + ws.vo1(b) * b1) + ws.vo1(c) * b2;
   *p2 = (ws.vo2(a) * b0 + ws.vo2(b) * b1) + ws.vo2(c) * b2;
 }
 
-__device__ __forceinline__ int epa_next_ccw(const EpaWs& ws, int fid, int id) {
+template <class WS>
+__device__ __forceinline__ int epa_next_ccw(const WS& ws, int fid, int id) {
   if (ws.pt(fid, 0) == id) return 1;
   if (ws.pt(fid, 1) == id) return 2;
   return 0;
 }
 
-__device__ __forceinline__ bool epa_can_be_seen_by(const EpaWs& ws, int fid, int point, int opp) {
+template <class WS>
+__device__ __forceinline__ bool epa_can_be_seen_by(const WS& ws, int fid, int point, int opp) {
   V3 p0 = ws.vp(ws.pt(fid, opp));
   V3 p1 = ws.vp(ws.pt(fid, (opp + 1) % 3));
   V3 p2 = ws.vp(ws.pt(fid, (opp + 2) % 3));
@@ -180,14 +201,16 @@ __device__ __forceinline__ bool epa_can_be_seen_by(const EpaWs& ws, int fid, int
 enum : int { EPA_NONE = 0, EPA_OK = 1, EPA_OVERFLOW = 2 };
 
 // EPA::closest_points. `iters` counts support evaluations. Returns EPA_OK with (p1, p2, n),
-// EPA_NONE for the reference's None, EPA_OVERFLOW when a fixed capacity was exceeded.
-static __device__ __noinline__ int epa_closest_points(const EpaWs& ws, const Pose& pos12, const ShapeDev& g1, const ShapeDev& g2,
-                                               const Simplex& simplex, V3* p1, V3* p2, V3* n, uint32_t* iters) {
+// EPA_NONE for the reference's None, EPA_OVERFLOW when a fixed capacity was exceeded. `sup(dir)`
+// is CSOPoint::from_shapes(pos12, g1, g2, dir).
+template <class WS, class Sup>
+__device__ __forceinline__ int epa_closest_points_t(const WS& ws, Sup sup, const Simplex& simplex, V3* p1, V3* p2, V3* n, uint32_t* iters) {
+  using L = typename WS::Layout;
   const float eps_tol = EPS * 100.0f;
   int nverts = simplex.dim + 1;
   for (int i = 0; i < nverts; ++i) ws.set_vert(i, simplex.v[i]);
   int nfaces = 0;
-  EpaHeap heap{&ws, 0};
+  EpaHeap<WS> heap{&ws, 0};
   if (simplex.dim == 0) {
     *p1 = v3(0.f, 0.f, 0.f); *p2 = v3(0.f, 0.f, 0.f); *n = v3(0.f, 1.f, 0.f);
     return EPA_OK;
@@ -217,7 +240,7 @@ static __device__ __noinline__ int epa_closest_points(const EpaWs& ws, const Pos
       V3 v = ws.vp(1) - ws.vp(0);
       V3 a = fabsf(v.x) > fabsf(v.y) ? v3(v.z, 0.0f, -v.x) : v3(0.0f, -v.z, v.y);
       a = normalize(a);
-      ws.set_vert(2, cso_from_shapes(pos12, g1, g2, cross(a, v)));
+      ws.set_vert(2, sup(cross(a, v)));
       nverts = 3;
     }
     epa_new_face(ws, 0, 0, 1, 2, 1, 1, 1);
@@ -241,8 +264,8 @@ static __device__ __noinline__ int epa_closest_points(const EpaWs& ws, const Pos
     int fadj[3] = {ws.adj(fid, 0), ws.adj(fid, 1), ws.adj(fid, 2)};
     V3 fnormal = ws.normal(fid);
     float fbc[3] = {ws.bc(fid, 0), ws.bc(fid, 1), ws.bc(fid, 2)};
-    if (nverts >= EPA_MAX_VERTS) return EPA_OVERFLOW;
-    CSO cso = cso_from_shapes(pos12, g1, g2, fnormal);
+    if (nverts >= L::MAX_VERTS) return EPA_OVERFLOW;
+    CSO cso = sup(fnormal);
     int support_id = nverts;
     ws.set_vert(nverts++, cso);
     float candidate = dot(cso.p, fnormal);
@@ -261,33 +284,33 @@ static __device__ __noinline__ int epa_closest_points(const EpaWs& ws, const Pos
     for (int k = 2; k >= 0; --k) {
       int a = fadj[k];
       int o = epa_next_ccw(ws, a, fpts[k]);
-      ws.w(EPA_W_STACK + sp++) = (uint32_t)a | ((uint32_t)o << 16);
+      ws.w(L::W_STACK + sp++) = (uint32_t)a | ((uint32_t)o << 16);
     }
     while (sp > 0) {
-      uint32_t e = ws.w(EPA_W_STACK + --sp);
+      uint32_t e = ws.w(L::W_STACK + --sp);
       int id = (int)(e & 0xffff), opp = (int)(e >> 16);
       if (ws.deleted(id)) continue;
       if (!epa_can_be_seen_by(ws, id, support_id, opp)) {
-        if (nsil >= EPA_MAX_SIL) return EPA_OVERFLOW;
-        ws.w(EPA_W_SIL + nsil++) = (uint32_t)id | ((uint32_t)opp << 16);
+        if (nsil >= L::MAX_SIL) return EPA_OVERFLOW;
+        ws.w(L::W_SIL + nsil++) = (uint32_t)id | ((uint32_t)opp << 16);
       } else {
         ws.set_deleted(id);
         int a1 = (opp + 2) % 3, a2 = opp;
         int adj1 = ws.adj(id, a1), adj2 = ws.adj(id, a2);
         int o1 = epa_next_ccw(ws, adj1, ws.pt(id, a1));
         int o2 = epa_next_ccw(ws, adj2, ws.pt(id, a2));
-        if (sp + 2 > EPA_STACK) return EPA_OVERFLOW;
-        ws.w(EPA_W_STACK + sp++) = (uint32_t)adj2 | ((uint32_t)o2 << 16);
-        ws.w(EPA_W_STACK + sp++) = (uint32_t)adj1 | ((uint32_t)o1 << 16);
+        if (sp + 2 > L::STACK) return EPA_OVERFLOW;
+        ws.w(L::W_STACK + sp++) = (uint32_t)adj2 | ((uint32_t)o2 << 16);
+        ws.w(L::W_STACK + sp++) = (uint32_t)adj1 | ((uint32_t)o1 << 16);
       }
     }
     int first_new = nfaces;
     if (nsil == 0) return EPA_NONE;
     for (int s = 0; s < nsil; ++s) {
-      uint32_t e = ws.w(EPA_W_SIL + s);
+      uint32_t e = ws.w(L::W_SIL + s);
       int sfid = (int)(e & 0xffff), opp = (int)(e >> 16);
       if (ws.deleted(sfid)) continue;
-      if (nfaces >= EPA_MAX_FACES || heap.len >= EPA_MAX_FACES) return EPA_OVERFLOW;
+      if (nfaces >= L::MAX_FACES || heap.len >= L::MAX_FACES) return EPA_OVERFLOW;
       int new_id = nfaces;
       int pt1 = ws.pt(sfid, (opp + 2) % 3);
       int pt2 = ws.pt(sfid, (opp + 1) % 3);
@@ -317,6 +340,12 @@ static __device__ __noinline__ int epa_closest_points(const EpaWs& ws, const Pos
   epa_face_closest_points(ws, (int)best_id, p1, p2);
   *n = ws.normal((int)best_id);
   return EPA_OK;
+}
+
+// The per-thread form over a global-memory slot.
+static __device__ __noinline__ int epa_closest_points(const EpaWs& ws, const Pose& pos12, const ShapeDev& g1, const ShapeDev& g2,
+                                                      const Simplex& simplex, V3* p1, V3* p2, V3* n, uint32_t* iters) {
+  return epa_closest_points_t(ws, [&](V3 d) { return cso_from_shapes(pos12, g1, g2, d); }, simplex, p1, p2, n, iters);
 }
 
 }  // namespace pg

@@ -54,7 +54,7 @@ struct parrygpu_ctx {
   DevBuf sort_k[2], sort_v[2], sort_hist, stage_in[8], stage_out[4], misc, counters, stage_poly[9];
   DevBuf ray_keys, ray_order;
   // contact pipeline scratch: EPA queue (pair + simplex per entry) and per-slot polytope workspaces
-  DevBuf ct_queue, ct_counters, epa_ws;
+  DevBuf ct_queue, ct_counters, epa_ws, ct_retry;
   RayWaveScratch ray_wave;
   int sm_count = 0;
   // Optional per-kernel event timing (parrygpu_enable_kernel_timing).

@@ -345,23 +345,28 @@ __global__ void __launch_bounds__(128) k_compound_rays(const WideNode* __restric
 // ---- wavefront shape-set rays ----
 // The single-kernel traversal above carries the GJK ray cast's state (155 registers), which caps
 // the occupancy of the whole, latency-bound traversal. The wavefront form splits it:
-//   k_rays_wave   traversal + the analytic leaves (balls, cuboids, triangles) in few registers;
-//                 support-map leaves (capsules, hulls) whose box the ray enters before the best
-//                 analytic hit are appended to a candidate list, and the ray's best hit so far is
-//                 published as a 64-bit key (toi bits, shape index);
-//   k_rays_cand   one thread per candidate: the GJK ray cast (its result does not depend on the
-//                 max_toi bound, which only accepts or rejects), atomicMin of (toi, index);
-//   k_rays_finish the candidate holding its ray's minimum key writes the ray's result.
+//   k_rays_wave     traversal + the analytic leaves (balls, cuboids, triangles) in few registers.
+//                   A support-map leaf (capsule, hull) whose box the ray enters before the best
+//                   analytic hit becomes a candidate with its box entry time: the ray's nearest
+//                   candidate goes to its own slot of list A, the others to the shared list B.
+//                   The ray's best hit so far is published as the 64-bit key (toi bits, index).
+//   k_rays_cand     GJK ray casts (their toi does not depend on the max_toi bound, which only
+//                   accepts or rejects) for list A, then for list B skipping candidates whose box
+//                   entry lies beyond the ray's current best; atomicMin of (toi, index).
+//   k_rays_finish   the candidate holding its ray's minimum key writes the ray's result.
 // The minimum of (toi, index) over every hit with toi < max_toi is the single-kernel answer (nearest
-// hit, lowest index on exact ties). Rays whose candidates did not fit the list are redone by the
+// hit, lowest index on exact ties). Rays whose candidates did not fit list B are redone by the
 // single kernel (mask `only`).
 struct RayCand {
   uint32_t k, r, part, hit;
-  float t, nx, ny, nz;
+  float tmin, t, nx, ny, nz, pad;
 };
 
 __device__ __forceinline__ unsigned long long hit_key(float t, uint32_t part) {
   return ((unsigned long long)__float_as_uint(t + 0.0f) << 32) | part;
+}
+__device__ __forceinline__ float key_toi(unsigned long long key) {
+  return key == ~0ull ? FLT_MAX : __uint_as_float((uint32_t)(key >> 32));
 }
 
 __device__ __forceinline__ bool analytic_type(uint32_t t) { return t == SH_BALL || t == SH_CUBOID || t == SH_TRIANGLE; }
@@ -388,12 +393,19 @@ __device__ __forceinline__ void ray_of(const float* rays, const uint32_t* order,
   if (has_pose) { *o = pose_inv_point(cpose, *o); *dir = pose_inv_rotate(cpose, *dir); }
 }
 
+struct WaveBufs {
+  RayCand* a;            // one slot per ray (index k)
+  RayCand* b;            // shared list
+  unsigned long long cap;
+  unsigned long long* count;
+  unsigned long long* keys;  // per ray (index r)
+  uint8_t* ovf;              // per ray (index r)
+};
+
 __global__ void __launch_bounds__(128) k_rays_wave(const WideNode* __restrict__ wide, CompoundDev cd, const float* __restrict__ rays, uint32_t n,
                                                    float max_toi, int solid, int has_pose, Pose cpose, uint32_t* __restrict__ part_out,
                                                    float* __restrict__ toi_out, float* __restrict__ normal_out, uint32_t* __restrict__ err,
-                                                   const uint32_t* __restrict__ order, int permuted, RayCand* __restrict__ cands,
-                                                   unsigned long long cap, unsigned long long* __restrict__ ccount,
-                                                   unsigned long long* __restrict__ keys, uint8_t* __restrict__ ovf) {
+                                                   const uint32_t* __restrict__ order, int permuted, WaveBufs wb) {
   uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= n) return;
   uint32_t r;
@@ -405,12 +417,23 @@ __global__ void __launch_bounds__(128) k_rays_wave(const WideNode* __restrict__ 
   uint32_t best_part = 0xffffffffu;
   V3 best_n = v3(0.f, 0.f, 0.f);
   bool have = false, overflow = false;
-  auto visit_leaf = [&](uint32_t part) {
+  uint32_t near_part = 0xffffffffu;
+  float near_tmin = FLT_MAX;
+  auto defer = [&](uint32_t part, float tmin) {
+    unsigned long long slot = atomicAdd(wb.count, 1ull);
+    if (slot < wb.cap) wb.b[slot] = RayCand{k, r, part, 0u, tmin, 0.f, 0.f, 0.f, 0.f, 0.f};
+    else overflow = true;
+  };
+  auto visit_leaf = [&](uint32_t part, float tmin) {
     uint32_t ty = cd.types[part];
     if (!analytic_type(ty)) {
-      unsigned long long slot = atomicAdd(ccount, 1ull);
-      if (slot < cap) cands[slot] = RayCand{k, r, part, 0u, 0.f, 0.f, 0.f, 0.f};
-      else overflow = true;
+      if (tmin < near_tmin) {
+        if (near_part != 0xffffffffu) defer(near_part, near_tmin);
+        near_part = part;
+        near_tmin = tmin;
+      } else {
+        defer(part, tmin);
+      }
       return;
     }
     ShapeDev s = load_shape(cd.types, cd.params, cd.pool, part);
@@ -424,7 +447,7 @@ __global__ void __launch_bounds__(128) k_rays_wave(const WideNode* __restrict__ 
   load_wide(wide, 0, &w);
   if ((w.r.data & 0x3fffffffu) == 0u) {
     float s0 = slab(w.l.mins, w.l.maxs, o, inv, zmask, max_toi);
-    if (s0 < max_toi) visit_leaf(w.l.children);
+    if (s0 < max_toi) visit_leaf(w.l.children, s0);
   } else {
     uint32_t stack[CRAY_STACK];
     int sp = 0;
@@ -437,11 +460,11 @@ __global__ void __launch_bounds__(128) k_rays_wave(const WideNode* __restrict__ 
       uint32_t next = 0xffffffffu;
       uint32_t far_child = farn->children, far_data = farn->data;
       if (ls != FLT_MAX && (ls < best || (have && ls == best))) {
-        if ((nearn->data & 0x3fffffffu) == 1u) visit_leaf(nearn->children);
+        if ((nearn->data & 0x3fffffffu) == 1u) visit_leaf(nearn->children, ls);
         else next = nearn->children;
       }
       if (rs != FLT_MAX && (rs < best || (have && rs == best))) {
-        if ((far_data & 0x3fffffffu) == 1u) visit_leaf(far_child);
+        if ((far_data & 0x3fffffffu) == 1u) visit_leaf(far_child, rs);
         else if (next != 0xffffffffu) {
           if (sp >= CRAY_STACK) { atomicOr(err, ERR_STACK_OVERFLOW); break; }
           stack[sp++] = far_child;
@@ -454,8 +477,9 @@ __global__ void __launch_bounds__(128) k_rays_wave(const WideNode* __restrict__ 
       load_wide(wide, next, &w);
     }
   }
-  keys[r] = have ? hit_key(best, best_part) : ~0ull;
-  ovf[r] = overflow ? 1 : 0;
+  wb.a[k] = RayCand{k, r, near_part, 0u, near_tmin, 0.f, 0.f, 0.f, 0.f, 0.f};
+  wb.keys[r] = have ? hit_key(best, best_part) : ~0ull;
+  wb.ovf[r] = overflow ? 1 : 0;
   if (has_pose && have) best_n = pose_rotate(cpose, best_n);
   part_out[r] = have ? best_part : 0xffffffffu;
   toi_out[r] = have ? best : 0.0f;
@@ -466,47 +490,58 @@ __global__ void __launch_bounds__(128) k_rays_wave(const WideNode* __restrict__ 
   }
 }
 
-// Candidates of the first min(cap, *ccount) entries; `n_cap` bounds the grid.
-__global__ void __launch_bounds__(128) k_rays_cand(CompoundDev cd, const float* __restrict__ rays, float max_toi, int solid, int has_pose,
-                                                   Pose cpose, const uint32_t* __restrict__ order, int permuted, RayCand* __restrict__ cands,
-                                                   unsigned long long cap, const unsigned long long* __restrict__ ccount,
-                                                   unsigned long long* __restrict__ keys) {
-  unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x;
-  unsigned long long c = *ccount;
-  if (i >= cap || i >= c) return;
-  RayCand cd_ = cands[i];
+// One candidate: the GJK ray cast unless its box entry lies beyond the ray's current best (a later
+// hit cannot win; an entry equal to the best may still tie with a lower index).
+__device__ __forceinline__ void run_candidate(const CompoundDev& cd, const float* rays, float max_toi, int solid, int has_pose, const Pose& cpose,
+                                              const uint32_t* order, int permuted, RayCand* e, unsigned long long* keys) {
+  RayCand c = *e;
+  if (c.part == 0xffffffffu || c.tmin > key_toi(keys[c.r])) return;
   uint32_t r;
   V3 o, dir;
-  ray_of(rays, order, permuted, cd_.k, has_pose, cpose, &r, &o, &dir);
-  ShapeDev s = load_shape(cd.types, cd.params, cd.pool, cd_.part);
-  Pose p = load_pose(cd.poses, cd_.part);
+  ray_of(rays, order, permuted, c.k, has_pose, cpose, &r, &o, &dir);
+  ShapeDev s = load_shape(cd.types, cd.params, cd.pool, c.part);
+  Pose p = load_pose(cd.poses, c.part);
   float t;
   V3 nn;
   // composite casts keep hits strictly below max_toi (CompositeShapeRef::cast_local_ray)
   if (!part_cast_ray(s, p, o, dir, max_toi, solid != 0, &t, &nn) || !(t < max_toi)) return;
   if (has_pose) nn = pose_rotate(cpose, nn);
-  cands[i].hit = 1u;
-  cands[i].t = t;
-  cands[i].nx = nn.x;
-  cands[i].ny = nn.y;
-  cands[i].nz = nn.z;
-  atomicMin(&keys[r], hit_key(t, cd_.part));
+  e->hit = 1u;
+  e->t = t;
+  e->nx = nn.x;
+  e->ny = nn.y;
+  e->nz = nn.z;
+  atomicMin(&keys[r], hit_key(t, c.part));
 }
 
-__global__ void __launch_bounds__(128) k_rays_finish(const RayCand* __restrict__ cands, unsigned long long cap,
-                                                     const unsigned long long* __restrict__ ccount, const unsigned long long* __restrict__ keys,
+// List A (one entry per ray, grid over the rays) or list B (grid-stride over min(cap, *count)).
+__global__ void __launch_bounds__(128) k_rays_cand(CompoundDev cd, const float* __restrict__ rays, float max_toi, int solid, int has_pose,
+                                                   Pose cpose, const uint32_t* __restrict__ order, int permuted, RayCand* __restrict__ list,
+                                                   unsigned long long n, const unsigned long long* __restrict__ count,
+                                                   unsigned long long* __restrict__ keys) {
+  unsigned long long m = n;
+  if (count && *count < m) m = *count;
+  for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < m;
+       i += (unsigned long long)gridDim.x * blockDim.x)
+    run_candidate(cd, rays, max_toi, solid, has_pose, cpose, order, permuted, list + i, keys);
+}
+
+__global__ void __launch_bounds__(128) k_rays_finish(const RayCand* __restrict__ list, unsigned long long n,
+                                                     const unsigned long long* __restrict__ count, const unsigned long long* __restrict__ keys,
                                                      uint32_t* __restrict__ part_out, float* __restrict__ toi_out, float* __restrict__ normal_out) {
-  unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x;
-  unsigned long long c = *ccount;
-  if (i >= cap || i >= c) return;
-  RayCand e = cands[i];
-  if (!e.hit || keys[e.r] != hit_key(e.t, e.part)) return;
-  part_out[e.r] = e.part;
-  toi_out[e.r] = e.t;
-  if (normal_out) {
-    normal_out[3 * (size_t)e.r] = e.nx;
-    normal_out[3 * (size_t)e.r + 1] = e.ny;
-    normal_out[3 * (size_t)e.r + 2] = e.nz;
+  unsigned long long m = n;
+  if (count && *count < m) m = *count;
+  for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < m;
+       i += (unsigned long long)gridDim.x * blockDim.x) {
+    RayCand e = list[i];
+    if (!e.hit || keys[e.r] != hit_key(e.t, e.part)) continue;
+    part_out[e.r] = e.part;
+    toi_out[e.r] = e.t;
+    if (normal_out) {
+      normal_out[3 * (size_t)e.r] = e.nx;
+      normal_out[3 * (size_t)e.r + 1] = e.ny;
+      normal_out[3 * (size_t)e.r + 2] = e.nz;
+    }
   }
 }
 
@@ -520,7 +555,7 @@ static parrygpu_status compound_copy_in(parrygpu_ctx* ctx, DevBuf& dst, const vo
 
 parrygpu_status shape_rays_reserve(parrygpu_ctx* ctx, RayWaveScratch& sc, uint32_t n) {
   uint64_t cap = 4ull * n + 1024;
-  PG_CUDA(ctx, sc.cands.reserve(cap * sizeof(RayCand)));
+  PG_CUDA(ctx, sc.cands.reserve((cap + n) * sizeof(RayCand)));  // list A (n slots) then list B (cap)
   PG_CUDA(ctx, sc.counter.reserve(16));
   PG_CUDA(ctx, sc.keys.reserve((size_t)n * 8 + 16));
   PG_CUDA(ctx, sc.ovf.reserve((size_t)n + 16));
@@ -533,18 +568,22 @@ static parrygpu_status launch_wave(parrygpu_ctx* ctx, const WideNode* wide, Comp
                                    int permuted, uint32_t n, float max_toi, int solid, int has_pose, Pose pose, uint32_t* d_part,
                                    float* d_toi, float* d_nrm, RayWaveScratch& sc) {
   unsigned long long* cnt = sc.counter.as<unsigned long long>();
+  WaveBufs wb{sc.cands.as<RayCand>(), sc.cands.as<RayCand>() + n, sc.cap, cnt, sc.keys.as<unsigned long long>(), sc.ovf.as<uint8_t>()};
+  uint32_t grid = (uint32_t)(ctx->sm_count > 0 ? ctx->sm_count : 152) * 16;
   PG_CUDA(ctx, cudaMemsetAsync(cnt, 0, 8, ctx->stream));
   k_rays_wave<<<div_up(n, 128), 128, 0, ctx->stream>>>(wide, cd, d_rays, n, max_toi, solid, has_pose, pose, d_part, d_toi, d_nrm, ctx->d_err,
-                                                       order, permuted, sc.cands.as<RayCand>(), sc.cap, cnt,
-                                                       sc.keys.as<unsigned long long>(), sc.ovf.as<uint8_t>());
+                                                       order, permuted, wb);
   PG_LAUNCHED(ctx);
-  k_rays_cand<<<div_up(sc.cap, 128), 128, 0, ctx->stream>>>(cd, d_rays, max_toi, solid, has_pose, pose, order, permuted,
-                                                            sc.cands.as<RayCand>(), sc.cap, cnt, sc.keys.as<unsigned long long>());
+  k_rays_cand<<<div_up(n, 128), 128, 0, ctx->stream>>>(cd, d_rays, max_toi, solid, has_pose, pose, order, permuted, wb.a, n, nullptr,
+                                                       wb.keys);
   PG_LAUNCHED(ctx);
-  k_rays_finish<<<div_up(sc.cap, 128), 128, 0, ctx->stream>>>(sc.cands.as<RayCand>(), sc.cap, cnt, sc.keys.as<unsigned long long>(), d_part,
-                                                              d_toi, d_nrm);
+  k_rays_cand<<<grid, 128, 0, ctx->stream>>>(cd, d_rays, max_toi, solid, has_pose, pose, order, permuted, wb.b, sc.cap, cnt, wb.keys);
   PG_LAUNCHED(ctx);
-  // rays whose candidates overflowed the list: the single-kernel cast, for them only
+  k_rays_finish<<<grid, 128, 0, ctx->stream>>>(wb.a, n, nullptr, wb.keys, d_part, d_toi, d_nrm);
+  PG_LAUNCHED(ctx);
+  k_rays_finish<<<grid, 128, 0, ctx->stream>>>(wb.b, sc.cap, cnt, wb.keys, d_part, d_toi, d_nrm);
+  PG_LAUNCHED(ctx);
+  // rays whose candidates overflowed list B: the single-kernel cast, for them only
   k_compound_rays<<<div_up(n, 128), 128, 0, ctx->stream>>>(wide, cd, d_rays, n, max_toi, solid, has_pose, pose, d_part, d_toi, d_nrm,
                                                            ctx->d_err, order, permuted, sc.ovf.as<uint8_t>());
   PG_LAUNCHED(ctx);
