@@ -293,8 +293,7 @@ def manifolds_section(ctx, stream, steps: int, warmup: int, n_pairs: int, flush)
         en_ev[k].record(stream)
     torch.cuda.synchronize()
     ms = sum(a.elapsed_time(b) for a, b in zip(st_ev, en_ev)) / steps
-    m_ms, m_n = ctx.kernel_time("manifolds_main")
-    e_ms, e_n = ctx.kernel_time("manifolds_epa")
+    m_ms, m_n = ctx.kernel_time("manifolds")
     ctx.enable_kernel_timing(False)
     launches = ctx.kernel_launches - l0
     last_f = warmup + steps
@@ -345,7 +344,7 @@ def manifolds_section(ctx, stream, steps: int, warmup: int, n_pairs: int, flush)
     # algorithmic bytes per pair: pair 8 B, two shapes (type 4 + params 16 + pose 28), record
     # header and live points read and written (32 B + 40 B per point each way)
     bytes_per_pair = 8 + 2 * 48 + 2 * (32 + 40 * mean_pts)
-    kernel_ms = m_ms / max(m_n, 1) + e_ms / max(e_n, 1)
+    kernel_ms = m_ms / max(m_n, 1)
     achieved = bytes_per_pair * n_pairs / (kernel_ms / 1e3) / 1e9
     peak, peak_kind = measured_peak_hbm()
     kinds = np.bincount((t[pairs[:, 0]] * 4 + t[pairs[:, 1]]).astype(np.int64), minlength=16)
@@ -355,7 +354,7 @@ def manifolds_section(ctx, stream, steps: int, warmup: int, n_pairs: int, flush)
         "pairs": n_pairs, "metric": "manifold pair updates/s", "value": round(n_pairs / (ms / 1e3), 1), "unit": "pairs/s",
         "ms_per_step": round(ms, 4), "cold_ms": round(min(cold_ms), 4),
         "cold_value": round(n_pairs / (min(cold_ms) / 1e3), 1),
-        "kernel_ms": {"main": round(m_ms / max(m_n, 1), 4), "epa": round(e_ms / max(e_n, 1), 4)},
+        "kernel_ms": round(kernel_ms, 4),
         "gpu_launches": launches,
         "mean_points": round(mean_pts, 3), "pairs_with_points": round(float((npts > 0).mean()), 4),
         "pair_kinds": [int(x) for x in kinds],

@@ -356,12 +356,12 @@ __global__ void __launch_bounds__(32 * WEPA_WARPS) k_contacts_epa_warp(ShapeArra
     ContactOut c;
     bool ok = false;
     V3 p1, p2, nn;
-    calls++;
+    uint32_t pair_iters = 0;  // counted only when this kernel finishes the pair
     int r;
     if (ps.path == PATH_SUPPORT) {
       stage_hull(ps.s1, hull1);
       stage_hull(ps.s2, hull2);
-      r = epa_closest_points_t(ws, [&](V3 d) { return warp_cso(ps.pos12, ps.s1, ps.s2, d); }, s, &p1, &p2, &nn, &iters);
+      r = epa_closest_points_t(ws, [&](V3 d) { return warp_cso(ps.pos12, ps.s1, ps.s2, d); }, s, &p1, &p2, &nn, &pair_iters);
     } else {
       ShapeDev cs = *ps.convex;
       stage_hull(cs, hull1);
@@ -369,13 +369,15 @@ __global__ void __launch_bounds__(32 * WEPA_WARPS) k_contacts_epa_warp(ShapeArra
       Pose minv = pose_inverse(m);
       ShapeDev origin;
       origin.type = SH_ORIGIN;
-      r = epa_closest_points_t(ws, [&](V3 d) { return warp_cso(minv, cs, origin, d); }, s, &p1, &p2, &nn, &iters);
+      r = epa_closest_points_t(ws, [&](V3 d) { return warp_cso(minv, cs, origin, d); }, s, &p1, &p2, &nn, &pair_iters);
     }
     if (r == EPA_OVERFLOW) {
       if (lane == 0) retry[atomicAdd(rcount, 1ull)] = (uint32_t)e;
       __syncwarp();
       continue;
     }
+    iters += pair_iters;
+    calls++;
     if (lane == 0) {
       if (ps.path == PATH_SUPPORT) {
         if (r == EPA_OK) { ok = true; finish_support_pair(ps.pos12, p1, p2, nn, &c); }

@@ -171,9 +171,9 @@ parrygpu_status stage_shapes(parrygpu_ctx* ctx, const parrygpu_shapes* s, ShapeA
 parrygpu_status launch_shape_aabbs(parrygpu_ctx* ctx, const ShapeArrays& sh, uint64_t n, float margin, float* d_out);
 // contact manifolds of the first min(cap, *d_count) pairs (manifold.cu) with caller-owned scratch
 // sized by manifolds_reserve(cap).
-parrygpu_status manifolds_reserve(parrygpu_ctx* ctx, uint64_t cap, DevBuf& queue, DevBuf& counters, DevBuf& epa_ws);
+parrygpu_status manifolds_reserve(parrygpu_ctx* ctx, uint64_t cap, MfScratch& scratch);
+// d_count may be null (then all `cap` pairs); returns after queuing the launches.
 parrygpu_status launch_manifolds(parrygpu_ctx* ctx, const ShapeArrays& sh, const uint32_t* d_pairs, uint64_t cap,
-                                 const unsigned long long* d_count, float prediction, uint32_t* d_recs, DevBuf& queue,
-                                 DevBuf& counters, DevBuf& epa_ws);
+                                 const unsigned long long* d_count, float prediction, uint32_t* d_recs, MfScratch& scratch);
 
 }  // namespace pg

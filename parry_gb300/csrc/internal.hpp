@@ -41,6 +41,13 @@ struct RayWaveScratch {
   uint64_t cap = 0;
 };
 
+// Scratch of the contact-manifold kernels (manifold.cu): EPA queue, counters (queue length, stats,
+// bin lengths), per-kind pair bins, per-slot EPA polytope workspaces.
+struct MfScratch {
+  DevBuf queue, counters, bins, epa_ws;
+  uint64_t cap = 0;
+};
+
 struct parrygpu_ctx {
   int device = 0;
   cudaStream_t own_stream = nullptr;
@@ -56,6 +63,7 @@ struct parrygpu_ctx {
   // contact pipeline scratch: EPA queue (pair + simplex per entry) and per-slot polytope workspaces
   DevBuf ct_queue, ct_counters, epa_ws, ct_retry;
   RayWaveScratch ray_wave;
+  MfScratch mf;
   int sm_count = 0;
   // Optional per-kernel event timing (parrygpu_enable_kernel_timing).
   bool timing = false;

@@ -15,9 +15,11 @@
 //   clipping                  src/query/clip/clip_segment_segment.rs
 //
 // Pipeline (one stream):
-//   k_manifolds_main  one thread per pair. Analytic generators finish in place; the polygonal-feature
-//                     path (cuboid/capsule/hull pairs) runs GJK and the hull-ball path a GJK point
-//                     projection; when GJK ends inside, (pair, simplex, tag) goes to the EPA queue.
+//   k_mf_classify     status of each pair and its generator kind (pairs binned by kind).
+//   k_mf_kind<K>      one thread per pair of bin K. Analytic generators finish in place; the
+//                     polygonal-feature path (cuboid/capsule/hull pairs) runs GJK and the hull-ball
+//                     path a GJK point projection; when GJK ends inside, (pair, simplex, tag) goes to
+//                     the EPA queue.
 //   k_manifolds_epa   persistent loop over the queue (epa_device.cuh workspace slots), then the same
 //                     feature clipping as the main kernel.
 // Every step keeps the reference's evaluation order (compiled with --fmad=false) so the records match
@@ -797,13 +799,30 @@ __device__ __forceinline__ bool hull_project_gjk(const ShapeDev& cs, V3 center, 
 }
 
 // `d_n` (may be null) holds a device-side pair count; the kernel then handles min(n, *d_n) pairs.
-__global__ void __launch_bounds__(MF_THREADS) k_manifolds_main(ShapeArrays sh, const uint32_t* __restrict__ pairs, uint64_t n, float prediction,
-                                                               uint32_t* __restrict__ recs, uint32_t* __restrict__ queue,
-                                                               unsigned long long* __restrict__ qcount, unsigned long long* __restrict__ stats,
-                                                               uint32_t* __restrict__ err, const unsigned long long* __restrict__ d_n) {
+// The pairs are binned by generator kind first (k_mf_classify), then each kind runs its own small
+// kernel over its bin: warps see one code path, the simple kinds keep few registers, and the
+// instruction cache holds one generator at a time.
+enum : uint32_t { MK_BALL_BALL = 0, MK_CUBOID_CUBOID, MK_CAPSULE_CAPSULE, MK_CONVEX_BALL, MK_HULL_BALL, MK_PFM, MK_KINDS };
+// counters: [0] EPA queue length, [1..3] GJK / EPA stats, [4 + kind] bin lengths
+constexpr int MF_CTR_BINS = 4;
+
+__device__ __forceinline__ uint32_t manifold_kind(uint32_t t1, uint32_t t2) {
+  if (t1 == SH_BALL && t2 == SH_BALL) return MK_BALL_BALL;
+  if (t1 == SH_CUBOID && t2 == SH_CUBOID) return MK_CUBOID_CUBOID;
+  if (t1 == SH_CAPSULE && t2 == SH_CAPSULE) return MK_CAPSULE_CAPSULE;
+  if (t1 == SH_BALL || t2 == SH_BALL) return (t1 == SH_CONVEX || t2 == SH_CONVEX) ? MK_HULL_BALL : MK_CONVEX_BALL;
+  return MK_PFM;
+}
+
+// Status of each pair (invalid / unsupported records keep their content) and its bin, appended with
+// warp-aggregated atomics. `d_n` (may be null) holds a device-side pair count: min(n, *d_n) pairs.
+__global__ void __launch_bounds__(MF_THREADS) k_mf_classify(ShapeArrays sh, const uint32_t* __restrict__ pairs, uint64_t n,
+                                                            uint32_t* __restrict__ recs, uint32_t* __restrict__ bins, uint64_t stride,
+                                                            unsigned long long* __restrict__ ctr, uint32_t* __restrict__ err,
+                                                            const unsigned long long* __restrict__ d_n) {
   uint64_t k = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
   if (d_n && *d_n < n) n = *d_n;
-  uint32_t iters = 0;
+  uint32_t kind = MK_KINDS;
   if (k < n) {
     Rec r{recs + (size_t)k * MF_WORDS};
     uint32_t a = pairs[2 * k], b = pairs[2 * k + 1];
@@ -815,36 +834,64 @@ __global__ void __launch_bounds__(MF_THREADS) k_manifolds_main(ShapeArrays sh, c
       r.w[1] = PARRYGPU_UNSUPPORTED_PAIR;  // Err(Unsupported): the manifold is left as it was
     } else {
       r.w[1] = PARRYGPU_OK;
-      ShapeDev s1 = load_shape(sh.types, sh.params, sh.pool, a);
-      ShapeDev s2 = load_shape(sh.types, sh.params, sh.pool, b);
-      Pose pos12 = pose_inv_mul(load_pose(sh.poses, a), load_pose(sh.poses, b));
-      bool overflow = false, bad = false;
-      if (s1.type == SH_BALL && s2.type == SH_BALL) {
-        mf_ball_ball(r, pos12, s1.a, s2.a, prediction);
-      } else if (s1.type == SH_CUBOID && s2.type == SH_CUBOID) {
-        mf_cuboid_cuboid(r, pos12, v3(s1.a, s1.b, s1.c), v3(s2.a, s2.b, s2.c), prediction, &overflow);
-      } else if (s1.type == SH_CAPSULE && s2.type == SH_CAPSULE) {
-        mf_capsule_capsule(r, pos12, s1.a, s1.b, s2.a, s2.b, prediction);
-      } else if (s1.type == SH_BALL || s2.type == SH_BALL) {
-        bool ball_first = s1.type == SH_BALL;
-        Pose cpos = ball_first ? pose_inverse(pos12) : pos12;
-        const ShapeDev& cs = ball_first ? s2 : s1;
-        const HullDev& ch = ball_first ? h2 : h1;
-        float radius = ball_first ? s1.a : s2.a;
-        if (cs.type != SH_CONVEX) {
-          mf_convex_ball(r, cpos, cs, radius, prediction, ball_first);
-        } else {
-          V3 proj;
-          Simplex s;
-          if (hull_project_gjk(cs, cpos.t, &proj, s, &iters)) {
-            uint32_t fid = hull_projection_feature(cs, ch, cpos.t, proj, false, &bad);
-            finish_convex_ball(r, cpos, proj, false, fid, radius, prediction, ball_first);
-          } else {
-            enqueue(queue, qcount, k, s, ball_first ? TAG_BALL_FIRST : TAG_BALL_SECOND);
-          }
-        }
-      } else if (!try_update_contacts(r, pos12, COS_1_DEGREES, 1.0e-6f)) {
+      kind = manifold_kind(sh.types[a], sh.types[b]);
+    }
+  }
+  const uint32_t lane = threadIdx.x & 31;
+  uint32_t mask = __match_any_sync(0xffffffffu, kind);
+  uint32_t leader = (uint32_t)__ffs(mask) - 1;
+  unsigned long long base = 0;
+  if (kind < MK_KINDS && lane == leader) base = atomicAdd(&ctr[MF_CTR_BINS + kind], (unsigned long long)__popc(mask));
+  base = __shfl_sync(mask, base, leader);
+  if (kind < MK_KINDS) bins[(size_t)kind * stride + base + __popc(mask & ((1u << lane) - 1))] = (uint32_t)k;
+}
+
+template <uint32_t KIND>
+__global__ void __launch_bounds__(MF_THREADS) k_mf_kind(ShapeArrays sh, const uint32_t* __restrict__ pairs, float prediction,
+                                                        uint32_t* __restrict__ recs, const uint32_t* __restrict__ bins, uint64_t stride,
+                                                        unsigned long long* __restrict__ ctr, uint32_t* __restrict__ queue,
+                                                        uint32_t* __restrict__ err) {
+  const unsigned long long cnt = ctr[MF_CTR_BINS + KIND];
+  uint32_t iters = 0;
+  for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < cnt;
+       i += (unsigned long long)gridDim.x * blockDim.x) {
+    uint64_t k = bins[(size_t)KIND * stride + i];
+    Rec r{recs + (size_t)k * MF_WORDS};
+    uint32_t a = pairs[2 * k], b = pairs[2 * k + 1];
+    ShapeDev s1 = load_shape(sh.types, sh.params, sh.pool, a);
+    ShapeDev s2 = load_shape(sh.types, sh.params, sh.pool, b);
+    Pose pos12 = pose_inv_mul(load_pose(sh.poses, a), load_pose(sh.poses, b));
+    bool overflow = false, bad = false;
+    if constexpr (KIND == MK_BALL_BALL) {
+      mf_ball_ball(r, pos12, s1.a, s2.a, prediction);
+    } else if constexpr (KIND == MK_CUBOID_CUBOID) {
+      mf_cuboid_cuboid(r, pos12, v3(s1.a, s1.b, s1.c), v3(s2.a, s2.b, s2.c), prediction, &overflow);
+    } else if constexpr (KIND == MK_CAPSULE_CAPSULE) {
+      mf_capsule_capsule(r, pos12, s1.a, s1.b, s2.a, s2.b, prediction);
+    } else if constexpr (KIND == MK_CONVEX_BALL) {
+      bool ball_first = s1.type == SH_BALL;
+      mf_convex_ball(r, ball_first ? pose_inverse(pos12) : pos12, ball_first ? s2 : s1, ball_first ? s1.a : s2.a, prediction, ball_first);
+    } else if constexpr (KIND == MK_HULL_BALL) {
+      bool ball_first = s1.type == SH_BALL;
+      Pose cpos = ball_first ? pose_inverse(pos12) : pos12;
+      const ShapeDev& cs = ball_first ? s2 : s1;
+      HullDev ch{};
+      load_hull(sh, ball_first ? b : a, &ch);
+      float radius = ball_first ? s1.a : s2.a;
+      V3 proj;
+      Simplex s;
+      if (hull_project_gjk(cs, cpos.t, &proj, s, &iters)) {
+        uint32_t fid = hull_projection_feature(cs, ch, cpos.t, proj, false, &bad);
+        finish_convex_ball(r, cpos, proj, false, fid, radius, prediction, ball_first);
+      } else {
+        enqueue(queue, ctr, k, s, ball_first ? TAG_BALL_FIRST : TAG_BALL_SECOND);
+      }
+    } else {
+      if (!try_update_contacts(r, pos12, COS_1_DEGREES, 1.0e-6f)) {
         // contact_manifold_pfm_pfm: GJK warm-started from the cached normal
+        HullDev h1{}, h2{};
+        load_hull(sh, a, &h1);
+        load_hull(sh, b, &h2);
         float br1, br2;
         ShapeDev p1 = pfm_of(s1, &br1), p2 = pfm_of(s2, &br2);
         V3 dir;
@@ -853,16 +900,16 @@ __global__ void __launch_bounds__(MF_THREADS) k_manifolds_main(ShapeArrays sh, c
         Simplex s;
         simplex_reset(s, cso_from_shapes(pos12, p1, p2, dir));
         GjkOut g = gjk_closest_points(pos12, p1, p2, total_prediction, s, &iters);
-        if (g.kind == GJK_INTERSECTION) enqueue(queue, qcount, k, s, TAG_PFM);
+        if (g.kind == GJK_INTERSECTION) enqueue(queue, ctr, k, s, TAG_PFM);
         else finish_pfm(r, pos12, s1, h1, s2, h2, g.kind, g.p1, g.p2, g.dir, &overflow, &bad);
       }
-      if (overflow) atomicOr(err, ERR_CAPACITY);
-      if (bad) atomicOr(err, ERR_BAD_INDEX);
     }
+    if (overflow) atomicOr(err, ERR_CAPACITY);
+    if (bad) atomicOr(err, ERR_BAD_INDEX);
   }
-  if (stats) {
+  if (KIND == MK_HULL_BALL || KIND == MK_PFM) {
     uint32_t w = __reduce_add_sync(0xffffffffu, iters);
-    if ((threadIdx.x & 31) == 0 && w) atomicAdd(&stats[0], (unsigned long long)w);
+    if ((threadIdx.x & 31) == 0 && w) atomicAdd(&ctr[1], (unsigned long long)w);
   }
 }
 
@@ -933,29 +980,51 @@ __global__ void __launch_bounds__(MF_EPA_THREADS) k_manifolds_epa(ShapeArrays sh
 }  // namespace
 
 // Manifold update of the first min(cap, *d_count) pairs on device buffers, without host
-// synchronisation or allocation: the frame pipeline's narrow phase, capturable in a CUDA graph. The
-// EPA queue, counters and polytope workspaces are the caller's (sized by manifolds_reserve), so a
-// captured graph never points at context scratch that a later call may reallocate.
-parrygpu_status pg::manifolds_reserve(parrygpu_ctx* ctx, uint64_t cap, DevBuf& queue, DevBuf& counters, DevBuf& epa_ws) {
-  PG_CUDA(ctx, queue.reserve((size_t)cap * QUEUE_WORDS * 4));
-  PG_CUDA(ctx, counters.reserve(64));
+// synchronisation or allocation once the scratch is reserved: the frame pipeline's narrow phase,
+// capturable in a CUDA graph. The scratch is the caller's, so a captured graph never points at
+// context scratch that a later call may reallocate.
+parrygpu_status pg::manifolds_reserve(parrygpu_ctx* ctx, uint64_t cap, MfScratch& sc) {
+  PG_CUDA(ctx, sc.queue.reserve((size_t)cap * QUEUE_WORDS * 4));
+  PG_CUDA(ctx, sc.counters.reserve(128));
+  PG_CUDA(ctx, sc.bins.reserve((size_t)cap * MK_KINDS * 4));
   uint32_t epa_blocks = (uint32_t)(ctx->sm_count > 0 ? ctx->sm_count : 152) * 8;
-  PG_CUDA(ctx, epa_ws.reserve((size_t)(epa_blocks * MF_EPA_THREADS / 32) * EPA_SLOT_GROUP_BYTES));
+  PG_CUDA(ctx, sc.epa_ws.reserve((size_t)(epa_blocks * MF_EPA_THREADS / 32) * EPA_SLOT_GROUP_BYTES));
+  if (cap > sc.cap) sc.cap = cap;
+  return PARRYGPU_OK;
+}
+
+template <uint32_t KIND>
+static parrygpu_status launch_kind(parrygpu_ctx* ctx, const ShapeArrays& sh, const uint32_t* d_pairs, float prediction, uint32_t* d_recs,
+                                   MfScratch& sc, uint64_t stride, uint32_t grid) {
+  k_mf_kind<KIND><<<grid, MF_THREADS, 0, ctx->stream>>>(sh, d_pairs, prediction, d_recs, sc.bins.as<uint32_t>(), stride,
+                                                        sc.counters.as<unsigned long long>(), sc.queue.as<uint32_t>(), ctx->d_err);
+  PG_LAUNCHED(ctx);
   return PARRYGPU_OK;
 }
 
 parrygpu_status pg::launch_manifolds(parrygpu_ctx* ctx, const ShapeArrays& sh, const uint32_t* d_pairs, uint64_t cap,
-                                     const unsigned long long* d_count, float prediction, uint32_t* d_recs, DevBuf& queue,
-                                     DevBuf& counters, DevBuf& epa_ws) {
+                                     const unsigned long long* d_count, float prediction, uint32_t* d_recs, MfScratch& sc) {
   if (cap == 0) return PARRYGPU_OK;
-  uint32_t epa_blocks = (uint32_t)(ctx->sm_count > 0 ? ctx->sm_count : 152) * 8;
-  unsigned long long* ctr = counters.as<unsigned long long>();
-  PG_CUDA(ctx, cudaMemsetAsync(ctr, 0, 64, ctx->stream));
-  k_manifolds_main<<<div_up(cap, MF_THREADS), MF_THREADS, 0, ctx->stream>>>(sh, d_pairs, cap, prediction, d_recs, queue.as<uint32_t>(), ctr,
-                                                                           nullptr, ctx->d_err, d_count);
+  if (cap > sc.cap) return set_error(ctx, PARRYGPU_INVALID_ARG, "manifold scratch reserved for fewer pairs");
+  const uint64_t stride = cap;
+  uint32_t sms = (uint32_t)(ctx->sm_count > 0 ? ctx->sm_count : 152);
+  uint32_t epa_blocks = sms * 8;
+  uint32_t grid = div_up(cap, MF_THREADS);
+  if (grid > sms * 16) grid = sms * 16;
+  unsigned long long* ctr = sc.counters.as<unsigned long long>();
+  PG_CUDA(ctx, cudaMemsetAsync(ctr, 0, 128, ctx->stream));
+  k_mf_classify<<<div_up(cap, MF_THREADS), MF_THREADS, 0, ctx->stream>>>(sh, d_pairs, cap, d_recs, sc.bins.as<uint32_t>(), stride, ctr,
+                                                                        ctx->d_err, d_count);
   PG_LAUNCHED(ctx);
-  k_manifolds_epa<<<epa_blocks, MF_EPA_THREADS, 0, ctx->stream>>>(sh, d_pairs, prediction, d_recs, queue.as<uint32_t>(), ctr,
-                                                                 epa_ws.as<uint32_t>(), nullptr, ctx->d_err);
+  parrygpu_status s;
+  if ((s = launch_kind<MK_BALL_BALL>(ctx, sh, d_pairs, prediction, d_recs, sc, stride, grid)) != PARRYGPU_OK) return s;
+  if ((s = launch_kind<MK_CUBOID_CUBOID>(ctx, sh, d_pairs, prediction, d_recs, sc, stride, grid)) != PARRYGPU_OK) return s;
+  if ((s = launch_kind<MK_CAPSULE_CAPSULE>(ctx, sh, d_pairs, prediction, d_recs, sc, stride, grid)) != PARRYGPU_OK) return s;
+  if ((s = launch_kind<MK_CONVEX_BALL>(ctx, sh, d_pairs, prediction, d_recs, sc, stride, grid)) != PARRYGPU_OK) return s;
+  if ((s = launch_kind<MK_HULL_BALL>(ctx, sh, d_pairs, prediction, d_recs, sc, stride, grid)) != PARRYGPU_OK) return s;
+  if ((s = launch_kind<MK_PFM>(ctx, sh, d_pairs, prediction, d_recs, sc, stride, grid)) != PARRYGPU_OK) return s;
+  k_manifolds_epa<<<epa_blocks, MF_EPA_THREADS, 0, ctx->stream>>>(sh, d_pairs, prediction, d_recs, sc.queue.as<uint32_t>(), ctr,
+                                                                 sc.epa_ws.as<uint32_t>(), ctr + 1, ctx->d_err);
   PG_LAUNCHED(ctx);
   return PARRYGPU_OK;
 }
@@ -980,27 +1049,13 @@ parrygpu_status parrygpu_contact_manifolds(parrygpu_ctx* ctx, const parrygpu_sha
   bool c_rec;
   if ((s = stage_output(ctx, ctx->stage_out[0], manifolds, rec_bytes, &d_rec, &c_rec)) != PARRYGPU_OK) return s;
   if (c_rec) PG_CUDA(ctx, cudaMemcpyAsync(d_rec, manifolds, rec_bytes, cudaMemcpyHostToDevice, ctx->stream));
-  PG_CUDA(ctx, ctx->ct_queue.reserve((size_t)n_pairs * QUEUE_WORDS * 4));
-  PG_CUDA(ctx, ctx->ct_counters.reserve(64));
-  uint32_t epa_blocks = (uint32_t)(ctx->sm_count > 0 ? ctx->sm_count : 152) * 8;
-  uint32_t slots = epa_blocks * MF_EPA_THREADS;
-  PG_CUDA(ctx, ctx->epa_ws.reserve((size_t)(slots / 32) * EPA_SLOT_GROUP_BYTES));
-  unsigned long long* ctr = ctx->ct_counters.as<unsigned long long>();  // [0] queue count, [1..3] stats
-  PG_CUDA(ctx, cudaMemsetAsync(ctr, 0, 64, ctx->stream));
+  if ((s = manifolds_reserve(ctx, n_pairs, ctx->mf)) != PARRYGPU_OK) return s;
+  unsigned long long* ctr = ctx->mf.counters.as<unsigned long long>();  // [0] queue count, [1..3] stats
   {
-    KernelTimer kt(ctx, "manifolds_main");
-    k_manifolds_main<<<div_up(n_pairs, MF_THREADS), MF_THREADS, 0, ctx->stream>>>(sh, (const uint32_t*)dp, n_pairs, prediction,
-                                                                               (uint32_t*)d_rec, ctx->ct_queue.as<uint32_t>(), ctr, ctr + 1,
-                                                                               ctx->d_err, nullptr);
+    KernelTimer kt(ctx, "manifolds");
+    if ((s = launch_manifolds(ctx, sh, (const uint32_t*)dp, n_pairs, nullptr, prediction, (uint32_t*)d_rec, ctx->mf)) != PARRYGPU_OK)
+      return s;
     kt.stop();
-    PG_LAUNCHED(ctx);
-  }
-  {
-    KernelTimer kt(ctx, "manifolds_epa");
-    k_manifolds_epa<<<epa_blocks, MF_EPA_THREADS, 0, ctx->stream>>>(sh, (const uint32_t*)dp, prediction, (uint32_t*)d_rec, ctx->ct_queue.as<uint32_t>(),
-                                                                   ctr, ctx->epa_ws.as<uint32_t>(), ctr + 1, ctx->d_err);
-    kt.stop();
-    PG_LAUNCHED(ctx);
   }
   if (c_rec) PG_CUDA(ctx, cudaMemcpyAsync(manifolds, d_rec, rec_bytes, cudaMemcpyDeviceToHost, ctx->stream));
   if (stats) {

@@ -29,7 +29,7 @@ struct parrygpu_scene {
   bool has_poly = false;
   parrygpu_bvh bvh;
   DevBuf pairs[2], recs[2], keys[2], vals[2], counts;
-  DevBuf mf_queue, mf_counters, mf_epa;  // narrow-phase scratch owned by the scene (stable for the graph)
+  MfScratch mf;  // narrow-phase scratch owned by the scene (stable for the graph)
   DevBuf rays, ray_order, ray_part, ray_toi, ray_nrm;  // rays stored in Morton order of their origins
   RayWaveScratch ray_wave;
   int cur = 0;
@@ -206,7 +206,7 @@ static parrygpu_status scene_frame(parrygpu_ctx* ctx, parrygpu_scene* sc, float 
   {
     KernelTimer kt(ctx, "scene_manifolds");
     if ((s = launch_manifolds(ctx, sh, sc->pairs[nw].as<uint32_t>(), sc->cap, cnt + nw, sc->prediction, sc->recs[nw].as<uint32_t>(),
-                              sc->mf_queue, sc->mf_counters, sc->mf_epa)) != PARRYGPU_OK)
+                              sc->mf)) != PARRYGPU_OK)
       return s;
     kt.stop();
   }
@@ -322,7 +322,7 @@ parrygpu_status parrygpu_scene_create(parrygpu_ctx* ctx, const parrygpu_shapes* 
   }
   PG_CUDA(ctx, sc->counts.reserve(16));
   PG_CUDA(ctx, cudaMemsetAsync(sc->counts.ptr, 0, 16, ctx->stream));
-  if ((s = manifolds_reserve(ctx, pair_capacity, sc->mf_queue, sc->mf_counters, sc->mf_epa)) != PARRYGPU_OK) return fail(s);
+  if ((s = manifolds_reserve(ctx, pair_capacity, sc->mf)) != PARRYGPU_OK) return fail(s);
   ShapeArrays sh = scene_shapes(sc);
   if ((s = launch_shape_aabbs(ctx, sh, sc->n, 0.5f * prediction, sc->aabbs.as<float>())) != PARRYGPU_OK) return fail(s);
   if ((s = lbvh_build(ctx, &sc->bvh, sc->aabbs.as<float>(), (uint32_t)sc->n, false)) != PARRYGPU_OK) return fail(s);
@@ -335,8 +335,8 @@ void parrygpu_scene_destroy(parrygpu_scene* sc) {
   if (!sc) return;
   cudaDeviceSynchronize();  // frames in flight still read the scene's buffers
   drop_graph(sc);
-  for (DevBuf* d : {&sc->types, &sc->params, &sc->poses, &sc->vel, &sc->pool, &sc->aabbs, &sc->counts, &sc->mf_queue, &sc->mf_counters,
-                    &sc->mf_epa, &sc->rays, &sc->ray_order, &sc->ray_part,
+  for (DevBuf* d : {&sc->types, &sc->params, &sc->poses, &sc->vel, &sc->pool, &sc->aabbs, &sc->counts, &sc->mf.queue, &sc->mf.counters,
+                    &sc->mf.epa_ws, &sc->mf.bins, &sc->rays, &sc->ray_order, &sc->ray_part,
                     &sc->ray_toi, &sc->ray_nrm, &sc->bvh.wide, &sc->bvh.leaf_parent, &sc->bvh.node_parent, &sc->bvh.leaf_index,
                     &sc->bvh.flags, &sc->bvh.root_aabb, &sc->bvh.info})
     d->release();
