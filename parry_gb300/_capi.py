@@ -109,7 +109,8 @@ class ParryGpuError(RuntimeError):
 
 class ParryGpuConfig(C.Structure):
     _fields_ = [("device", C.c_int), ("ray_block", C.c_uint32), ("sort_rays", C.c_uint32), ("ray_sort_key", C.c_uint32),
-                ("reserved", C.c_uint32 * 4)]
+                ("ray_tree", C.c_uint32), ("epa_blocks_per_sm", C.c_uint32), ("epa_warp", C.c_uint32),
+                ("reserved", C.c_uint32 * 1)]
 
 
 _lib = None

@@ -560,7 +560,9 @@ parrygpu_status parrygpu_contacts_with_dirs(parrygpu_ctx* ctx, const parrygpu_sh
   PG_CUDA(ctx, ctx->ct_queue.reserve((size_t)n_pairs * QUEUE_WORDS * 4));
   PG_CUDA(ctx, ctx->ct_retry.reserve((size_t)n_pairs * 4));
   PG_CUDA(ctx, ctx->ct_counters.reserve(64));
-  uint32_t epa_blocks = (uint32_t)(ctx->sm_count > 0 ? ctx->sm_count : 152) * 8;
+  uint32_t epa_per_sm = ctx->cfg.epa_blocks_per_sm ? ctx->cfg.epa_blocks_per_sm : 8;
+  if (epa_per_sm > 32) epa_per_sm = 32;
+  uint32_t epa_blocks = (uint32_t)(ctx->sm_count > 0 ? ctx->sm_count : 152) * epa_per_sm;
   uint32_t slots = epa_blocks * EPA_THREADS;
   PG_CUDA(ctx, ctx->epa_ws.reserve((size_t)(slots / 32) * EPA_SLOT_GROUP_BYTES));
   unsigned long long* ctr = ctx->ct_counters.as<unsigned long long>();  // [0] queue count, [1..3] stats
@@ -580,14 +582,18 @@ parrygpu_status parrygpu_contacts_with_dirs(parrygpu_ctx* ctx, const parrygpu_sh
       PG_CUDA(ctx, cudaFuncSetAttribute(k_contacts_epa_warp, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)WEPA_SMEM));
       attr_set = true;
     }
+    // warp path: all pairs through the shared-memory kernel, the per-thread kernel redoes the
+    // listed overflows; per-thread path: the warp kernel is given no pairs (qcount is read as 0)
     uint32_t warp_blocks = (uint32_t)(ctx->sm_count > 0 ? ctx->sm_count : 152) * 3;
-    k_contacts_epa_warp<<<warp_blocks, 32 * WEPA_WARPS, WEPA_SMEM, ctx->stream>>>(
+    if (!ctx->cfg.epa_warp) warp_blocks = 0;
+    if (warp_blocks) k_contacts_epa_warp<<<warp_blocks, 32 * WEPA_WARPS, WEPA_SMEM, ctx->stream>>>(
         sh, (const uint32_t*)dp, prediction, (float*)d_out, (uint8_t*)d_has, ctx->ct_queue.as<uint32_t>(), ctr, ctr + 4,
         ctx->ct_retry.as<uint32_t>(), ctr + 5, ctr + 1, (float*)d_dirs);
-    PG_LAUNCHED(ctx);
+    if (warp_blocks) PG_LAUNCHED(ctx);
     k_contacts_epa<<<epa_blocks, EPA_THREADS, 0, ctx->stream>>>(sh, (const uint32_t*)dp, prediction, (float*)d_out, (uint8_t*)d_has,
                                                                 ctx->ct_queue.as<uint32_t>(), ctr, ctx->epa_ws.as<uint32_t>(), ctr + 1,
-                                                                ctx->d_err, (float*)d_dirs, ctx->ct_retry.as<uint32_t>(), ctr + 5);
+                                                                ctx->d_err, (float*)d_dirs,
+                                                                warp_blocks ? ctx->ct_retry.as<uint32_t>() : nullptr, ctr + 5);
     kt.stop();
     PG_LAUNCHED(ctx);
   }

@@ -105,6 +105,7 @@ struct parrygpu_trimesh {
   uint32_t n_vertices = 0, n_triangles = 0;
   parrygpu_bvh bvh;     // leaves store the sorted position of the triangle in `soup`
   DevBuf soup;          // per sorted position: a.xyz b.x | b.yz c.xy | c.z orig 0 0  (3 x float4)
+  DevBuf quads;         // 4-wide nodes collapsed from the binary tree (one per wide node, 128 B)
 };
 
 // A shape set under one BVH (the reference's Compound), with device copies of the shape arrays.
