@@ -581,7 +581,7 @@ def run_gb300(args) -> int:
     n = args.n_rays
     v, i = W.terrain_mesh()
     rays_h = W.terrain_rays(n)
-    ctx = pg.Context(device=local, ray_tree=args.ray_tree)
+    ctx = pg.Context(device=local)
     # One explicit stream shared by the library and the timing events (torch's default stream
     # handle is 0, which the library would map to its own stream).
     stream = torch.cuda.Stream()
@@ -722,8 +722,6 @@ def main() -> int:
                     help="ball/cuboid/capsule pairs of the contact-manifold section (0 skips it)")
     ap.add_argument("--scene-frames", type=int, default=100,
                     help="frames of the per-frame pipeline section (0 skips it)")
-    ap.add_argument("--ray-tree", type=int, default=0, choices=[0, 1],
-                    help="TriMesh ray traversal: 0 = 4-wide collapsed nodes, 1 = the binary tree")
     ap.add_argument("--scene-shapes", type=int, default=262144, help="shapes of the per-frame pipeline section")
     ap.add_argument("--scene-rays", type=int, default=4194304, help="rays per frame of the per-frame pipeline section")
     ap.add_argument("--train-pairs", type=int, default=1 << 21,

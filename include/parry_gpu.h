@@ -52,11 +52,8 @@ typedef struct parrygpu_config {
   uint32_t sort_rays;      /* 1 = Morton-sort rays before traversal (default), 0 = input order */
   uint32_t ray_sort_key;   /* 0 = 30-bit Morton code of the origin; 1 = direction octant (3 bits)
                               above a 27-bit Morton code of the origin */
-  uint32_t ray_tree;       /* TriMesh ray traversal: 0 = 4-wide nodes collapsed from the binary tree
-                              (default), 1 = the binary BvhNodeWide tree itself */
-  uint32_t epa_blocks_per_sm; /* contacts EPA: resident 64-thread blocks per SM (0 = library default) */
-  uint32_t epa_warp;       /* contacts EPA: 1 = one pair per warp in shared memory, 0 = one pair per thread */
-  uint32_t reserved[1];
+  uint32_t epa_blocks_per_sm; /* contacts EPA: resident 64-thread blocks per SM (0 = library default, 8) */
+  uint32_t reserved[3];
 } parrygpu_config;
 
 /* ---- context ---------------------------------------------------------------------------- */

@@ -78,17 +78,15 @@ def _alloc_like(ref, shape, dtype):
 class Context:
     """A device context (one CUDA stream). Mirrors nothing in parry, which is single-threaded CPU."""
 
-    def __init__(self, device: int = 0, ray_block: int = 0, sort_rays: bool = True, ray_sort_key: int = 0, ray_tree: int = 0,
-                 epa_blocks_per_sm: int = 0, epa_warp: int = 0):
+    def __init__(self, device: int = 0, ray_block: int = 0, sort_rays: bool = True, ray_sort_key: int = 0,
+                 epa_blocks_per_sm: int = 0):
         cfg = _capi.ParryGpuConfig()
         lib().parrygpu_default_config(C.byref(cfg))
         cfg.device = device
         cfg.ray_block = ray_block
         cfg.sort_rays = 1 if sort_rays else 0
         cfg.ray_sort_key = ray_sort_key
-        cfg.ray_tree = ray_tree
         cfg.epa_blocks_per_sm = epa_blocks_per_sm
-        cfg.epa_warp = epa_warp
         h = C.c_void_p()
         check(lib().parrygpu_create(C.byref(h), C.byref(cfg)))
         self._h = h

@@ -109,8 +109,7 @@ class ParryGpuError(RuntimeError):
 
 class ParryGpuConfig(C.Structure):
     _fields_ = [("device", C.c_int), ("ray_block", C.c_uint32), ("sort_rays", C.c_uint32), ("ray_sort_key", C.c_uint32),
-                ("ray_tree", C.c_uint32), ("epa_blocks_per_sm", C.c_uint32), ("epa_warp", C.c_uint32),
-                ("reserved", C.c_uint32 * 1)]
+                ("epa_blocks_per_sm", C.c_uint32), ("reserved", C.c_uint32 * 3)]
 
 
 _lib = None

@@ -214,15 +214,12 @@ __global__ void __launch_bounds__(EPA_THREADS) k_contacts_epa(ShapeArrays sh, co
                                                               float* __restrict__ out, uint8_t* __restrict__ has,
                                                               const uint32_t* __restrict__ queue, const unsigned long long* __restrict__ qcount,
                                                               uint32_t* __restrict__ ws_pool, unsigned long long* __restrict__ stats,
-                                                              uint32_t* __restrict__ err, float* __restrict__ final_dirs,
-                                                              const uint32_t* __restrict__ retry, const unsigned long long* __restrict__ rcount) {
+                                                              uint32_t* __restrict__ err, float* __restrict__ final_dirs) {
   const uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x;
   EpaWs ws{ws_pool + (size_t)(slot >> 5) * (EPA_WORDS * 32) + (slot & 31)};
-  // every queued pair, or only the listed ones (pairs the shared-memory warp kernel could not hold)
-  const unsigned long long total = retry ? *rcount : *qcount;
+  const unsigned long long total = *qcount;
   uint32_t iters = 0, calls = 0;
-  for (unsigned long long i = slot; i < total; i += (unsigned long long)gridDim.x * blockDim.x) {
-    unsigned long long e = retry ? retry[i] : i;
+  for (unsigned long long e = slot; e < total; e += (unsigned long long)gridDim.x * blockDim.x) {
     const uint32_t* q = queue + (size_t)e * QUEUE_WORDS;
     uint64_t k = q[0];
     Simplex s;
@@ -271,136 +268,6 @@ __global__ void __launch_bounds__(EPA_THREADS) k_contacts_epa(ShapeArrays sh, co
       if (w) atomicAdd(&stats[1], (unsigned long long)w);
       if (cw) atomicAdd(&stats[2], (unsigned long long)cw);
     }
-  }
-}
-
-// ---- one pair per warp EPA ----
-// The per-thread EPA re-reads both hulls from memory at every expansion and keeps its polytope in a
-// global slot (ncu: 38 % L2 hit rate, ~55 KB of DRAM traffic per EPA call). Here a warp takes one
-// queued pair: both hulls (up to 256 vertices each) are staged once into shared memory with
-// coalesced loads, the support scan is split across the lanes and merged by a warp-shuffle argmax
-// (first index on ties, as the sequential scan), and the polytope lives in the warp's shared-memory
-// workspace, where every lane runs the same scalar EPA steps on the same data (uniform control
-// flow). Pairs that outgrow the smaller shared-memory capacities are listed for the per-thread
-// kernel, which redoes them from the queue.
-constexpr int WEPA_WARPS = 4;
-constexpr int WEPA_STAGE = 256;
-constexpr int WEPA_WARP_WORDS = EpaSmemLayout::WORDS + 6 * WEPA_STAGE;
-constexpr size_t WEPA_SMEM = (size_t)WEPA_WARPS * WEPA_WARP_WORDS * 4;
-
-// point_cloud_support_point over the lanes: lane l scans indices 1 + l, 33 + l, ... seeded with
-// vertex 0, keeping the first index of its strict maximum; the merge prefers the larger value, then
-// the smaller index. NaN products never win, as in the sequential scan.
-__device__ __forceinline__ V3 warp_local_support(const ShapeDev& s, V3 dir) {
-  if (s.type != SH_CONVEX) return local_support(s, dir);
-  const uint32_t lane = threadIdx.x & 31;
-  const float* P = s.pts;
-  float bv = dot(v3(P[0], P[1], P[2]), dir);
-  uint32_t bi = 0;
-  for (uint32_t i = 1 + lane; i < s.npts; i += 32) {
-    float d = dot(v3(P[3 * i], P[3 * i + 1], P[3 * i + 2]), dir);
-    if (d > bv) { bv = d; bi = i; }
-  }
-#pragma unroll
-  for (int off = 16; off > 0; off >>= 1) {
-    float ov = __shfl_xor_sync(0xffffffffu, bv, off);
-    uint32_t oi = __shfl_xor_sync(0xffffffffu, bi, off);
-    if (ov > bv || (ov == bv && oi < bi)) { bv = ov; bi = oi; }
-  }
-  return v3(P[3 * bi], P[3 * bi + 1], P[3 * bi + 2]);
-}
-__device__ __forceinline__ V3 warp_world_support(const ShapeDev& s, const Pose& m, V3 dir) {
-  if (s.type == SH_ORIGIN) return m.t;
-  return pose_point(m, warp_local_support(s, pose_inv_rotate(m, dir)));
-}
-__device__ __forceinline__ CSO warp_cso(const Pose& pos12, const ShapeDev& g1, const ShapeDev& g2, V3 dir) {
-  V3 sp1 = warp_local_support(g1, dir);
-  V3 sp2 = warp_world_support(g2, pos12, -dir);
-  return CSO{sp1 - sp2, sp1, sp2};
-}
-// Copies a hull's vertices into shared memory (all lanes) and points the shape at the copy.
-__device__ __forceinline__ void stage_hull(ShapeDev& s, float* dst) {
-  if (s.type != SH_CONVEX || s.npts > WEPA_STAGE) return;
-  const uint32_t lane = threadIdx.x & 31;
-  for (uint32_t i = lane; i < 3 * s.npts; i += 32) dst[i] = s.pts[i];
-  __syncwarp();
-  s.pts = dst;
-}
-
-__global__ void __launch_bounds__(32 * WEPA_WARPS) k_contacts_epa_warp(ShapeArrays sh, const uint32_t* __restrict__ pairs, float prediction,
-                                                                      float* __restrict__ out, uint8_t* __restrict__ has,
-                                                                      const uint32_t* __restrict__ queue,
-                                                                      const unsigned long long* __restrict__ qcount,
-                                                                      unsigned long long* __restrict__ qhead, uint32_t* __restrict__ retry,
-                                                                      unsigned long long* __restrict__ rcount,
-                                                                      unsigned long long* __restrict__ stats, float* __restrict__ final_dirs) {
-  extern __shared__ uint32_t wepa_smem[];
-  const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  uint32_t* wbase = wepa_smem + (size_t)warp * WEPA_WARP_WORDS;
-  EpaWsSmem ws{wbase};
-  float* hull1 = reinterpret_cast<float*>(wbase + EpaSmemLayout::WORDS);
-  float* hull2 = hull1 + 3 * WEPA_STAGE;
-  const unsigned long long total = *qcount;
-  uint32_t iters = 0, calls = 0;
-  for (;;) {
-    unsigned long long e = 0;
-    if (lane == 0) e = atomicAdd(qhead, 1ull);
-    e = __shfl_sync(0xffffffffu, e, 0);
-    if (e >= total) break;
-    const uint32_t* q = queue + (size_t)e * QUEUE_WORDS;
-    uint64_t k;
-    Simplex s;
-    dequeue(q, &k, &s);
-    PairSetup ps;
-    setup_pair(sh, pairs[2 * k], pairs[2 * k + 1], &ps);
-    ContactOut c;
-    bool ok = false;
-    V3 p1, p2, nn;
-    uint32_t pair_iters = 0;  // counted only when this kernel finishes the pair
-    int r;
-    if (ps.path == PATH_SUPPORT) {
-      stage_hull(ps.s1, hull1);
-      stage_hull(ps.s2, hull2);
-      r = epa_closest_points_t(ws, [&](V3 d) { return warp_cso(ps.pos12, ps.s1, ps.s2, d); }, s, &p1, &p2, &nn, &pair_iters);
-    } else {
-      ShapeDev cs = *ps.convex;
-      stage_hull(cs, hull1);
-      Pose m{0.f, 0.f, 0.f, 1.f, -ps.cpos.t};
-      Pose minv = pose_inverse(m);
-      ShapeDev origin;
-      origin.type = SH_ORIGIN;
-      r = epa_closest_points_t(ws, [&](V3 d) { return warp_cso(minv, cs, origin, d); }, s, &p1, &p2, &nn, &pair_iters);
-    }
-    if (r == EPA_OVERFLOW) {
-      if (lane == 0) retry[atomicAdd(rcount, 1ull)] = (uint32_t)e;
-      __syncwarp();
-      continue;
-    }
-    iters += pair_iters;
-    calls++;
-    if (lane == 0) {
-      if (ps.path == PATH_SUPPORT) {
-        if (r == EPA_OK) { ok = true; finish_support_pair(ps.pos12, p1, p2, nn, &c); }
-        if (final_dirs) {
-          V3 fd = r == EPA_OK ? nn : v3(1.f, 0.f, 0.f);  // GJKResult::NoIntersection(x) when EPA fails
-          final_dirs[3 * k] = fd.x; final_dirs[3 * k + 1] = fd.y; final_dirs[3 * k + 2] = fd.z;
-        }
-      } else {
-        const ShapeDev& cs = *ps.convex;
-        PointProj proj;
-        proj.face = -1;
-        proj.inside = true;
-        proj.point = r == EPA_OK ? p1 : ps.cpos.t;
-        ok = finish_convex_ball(ps.cpos, cs, proj, ps.radius, prediction, &c);
-        if (ok && ps.path == PATH_BALL_FIRST) flip(&c);
-      }
-      write_out(out, has, k, ok, c, ps.pa, ps.pb);
-    }
-    __syncwarp();  // the next pair reuses the workspace and the staged hulls
-  }
-  if (stats && lane == 0) {
-    if (iters) atomicAdd(&stats[1], (unsigned long long)iters);
-    if (calls) atomicAdd(&stats[2], (unsigned long long)calls);
   }
 }
 
@@ -558,7 +425,6 @@ parrygpu_status parrygpu_contacts_with_dirs(parrygpu_ctx* ctx, const parrygpu_sh
   bool c_dirs = false;
   if ((s = stage_output(ctx, ctx->stage_out[2], final_dirs, (size_t)n_pairs * 12, &d_dirs, &c_dirs)) != PARRYGPU_OK) return s;
   PG_CUDA(ctx, ctx->ct_queue.reserve((size_t)n_pairs * QUEUE_WORDS * 4));
-  PG_CUDA(ctx, ctx->ct_retry.reserve((size_t)n_pairs * 4));
   PG_CUDA(ctx, ctx->ct_counters.reserve(64));
   uint32_t epa_per_sm = ctx->cfg.epa_blocks_per_sm ? ctx->cfg.epa_blocks_per_sm : 8;
   if (epa_per_sm > 32) epa_per_sm = 32;
@@ -577,23 +443,9 @@ parrygpu_status parrygpu_contacts_with_dirs(parrygpu_ctx* ctx, const parrygpu_sh
   }
   {
     KernelTimer kt(ctx, "contacts_epa");
-    static bool attr_set = false;
-    if (!attr_set) {
-      PG_CUDA(ctx, cudaFuncSetAttribute(k_contacts_epa_warp, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)WEPA_SMEM));
-      attr_set = true;
-    }
-    // warp path: all pairs through the shared-memory kernel, the per-thread kernel redoes the
-    // listed overflows; per-thread path: the warp kernel is given no pairs (qcount is read as 0)
-    uint32_t warp_blocks = (uint32_t)(ctx->sm_count > 0 ? ctx->sm_count : 152) * 3;
-    if (!ctx->cfg.epa_warp) warp_blocks = 0;
-    if (warp_blocks) k_contacts_epa_warp<<<warp_blocks, 32 * WEPA_WARPS, WEPA_SMEM, ctx->stream>>>(
-        sh, (const uint32_t*)dp, prediction, (float*)d_out, (uint8_t*)d_has, ctx->ct_queue.as<uint32_t>(), ctr, ctr + 4,
-        ctx->ct_retry.as<uint32_t>(), ctr + 5, ctr + 1, (float*)d_dirs);
-    if (warp_blocks) PG_LAUNCHED(ctx);
     k_contacts_epa<<<epa_blocks, EPA_THREADS, 0, ctx->stream>>>(sh, (const uint32_t*)dp, prediction, (float*)d_out, (uint8_t*)d_has,
                                                                 ctx->ct_queue.as<uint32_t>(), ctr, ctx->epa_ws.as<uint32_t>(), ctr + 1,
-                                                                ctx->d_err, (float*)d_dirs,
-                                                                warp_blocks ? ctx->ct_retry.as<uint32_t>() : nullptr, ctr + 5);
+                                                                ctx->d_err, (float*)d_dirs);
     kt.stop();
     PG_LAUNCHED(ctx);
   }

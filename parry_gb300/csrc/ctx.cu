@@ -97,7 +97,6 @@ void parrygpu_destroy(parrygpu_ctx* ctx) {
   ctx->ct_queue.release();
   ctx->ct_counters.release();
   ctx->epa_ws.release();
-  ctx->ct_retry.release();
   for (DevBuf* d : {&ctx->mf.queue, &ctx->mf.counters, &ctx->mf.bins, &ctx->mf.epa_ws}) d->release();
   for (DevBuf* d : {&ctx->ray_wave.cands, &ctx->ray_wave.counter, &ctx->ray_wave.keys, &ctx->ray_wave.ovf}) d->release();
   if (ctx->d_err) cudaFree(ctx->d_err);

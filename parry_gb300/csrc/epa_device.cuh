@@ -23,18 +23,15 @@ struct EpaLayout {
   static constexpr int W_STACK = W_SIL + MS;              // 1 word per stack entry
   static constexpr int WORDS = W_STACK + MSTK;            // words per workspace
 };
-// Per-thread workspaces in global memory, and the smaller per-warp workspaces in shared memory
-// (a pair that outgrows the latter is redone with the former).
+// Per-thread workspaces in global memory.
 using EpaGlobalLayout = EpaLayout<128, 512, 64, 256>;
-using EpaSmemLayout = EpaLayout<64, 192, 64, 128>;
 
 constexpr int EPA_MAX_VERTS = EpaGlobalLayout::MAX_VERTS;
 constexpr int EPA_MAX_FACES = EpaGlobalLayout::MAX_FACES;
 constexpr int EPA_WORDS = EpaGlobalLayout::WORDS;                     // words per slot
 constexpr size_t EPA_SLOT_GROUP_BYTES = (size_t)EPA_WORDS * 32 * 4;   // one warp's 32 slots
 
-// A workspace view: word i at base[i * STRIDE] (STRIDE 32: a lane-interleaved global slot; STRIDE 1:
-// a warp's shared-memory workspace, read and written identically by all its lanes).
+// A workspace view: word i at base[i * STRIDE] (STRIDE 32: a lane-interleaved global slot).
 template <class L, int STRIDE>
 struct EpaWsT {
   using Layout = L;
@@ -68,7 +65,6 @@ struct EpaWsT {
   __device__ __forceinline__ float bc(int fid, int k) const { return f(fo(fid) + 6 + k); }
 };
 using EpaWs = EpaWsT<EpaGlobalLayout, 32>;
-using EpaWsSmem = EpaWsT<EpaSmemLayout, 1>;
 
 template <class WS>
 struct EpaHeap {

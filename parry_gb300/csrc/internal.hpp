@@ -61,7 +61,7 @@ struct parrygpu_ctx {
   DevBuf sort_k[2], sort_v[2], sort_hist, stage_in[8], stage_out[4], misc, counters, stage_poly[9];
   DevBuf ray_keys, ray_order;
   // contact pipeline scratch: EPA queue (pair + simplex per entry) and per-slot polytope workspaces
-  DevBuf ct_queue, ct_counters, epa_ws, ct_retry;
+  DevBuf ct_queue, ct_counters, epa_ws;
   RayWaveScratch ray_wave;
   MfScratch mf;
   int sm_count = 0;
@@ -105,7 +105,6 @@ struct parrygpu_trimesh {
   uint32_t n_vertices = 0, n_triangles = 0;
   parrygpu_bvh bvh;     // leaves store the sorted position of the triangle in `soup`
   DevBuf soup;          // per sorted position: a.xyz b.x | b.yz c.xy | c.z orig 0 0  (3 x float4)
-  DevBuf quads;         // 4-wide nodes collapsed from the binary tree (one per wide node, 128 B)
 };
 
 // A shape set under one BVH (the reference's Compound), with device copies of the shape arrays.

@@ -23,7 +23,6 @@ using namespace pg;
 namespace {
 
 constexpr int RAY_STACK = 64;
-constexpr int QUAD_STACK = 96;
 
 struct TriHit {
   float toi;
@@ -110,52 +109,8 @@ __device__ __forceinline__ void load_tri(const float4* __restrict__ soup, uint32
   *orig = __float_as_uint(z.y);
 }
 
-// A 4-wide node collapsed from binary wide node i: its children, each replaced by its own two
-// children when it is internal. Slots are SoA so a node is eight float4 loads (one 128-byte line).
-// child = the triangle's sorted position for a leaf slot, the binary wide index (= quad index) of
-// the grandchild for an inner slot; kind 0 = empty, 1 = leaf, 2 = inner. The slab boxes are the
-// binary tree's own boxes, so pruning decisions match the binary traversal's.
-struct __align__(128) QuadNode {
-  float mnx[4], mny[4], mnz[4], mxx[4], mxy[4], mxz[4];
-  uint32_t child[4], kind[4];
-};
-
-__global__ void k_build_quads(const WideNode* __restrict__ wide, uint32_t n_wide, QuadNode* __restrict__ quads) {
-  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n_wide) return;
-  WideNode w;
-  load_wide(wide, i, &w);
-  QuadNode q;
-  int m = 0;
-  auto put = [&](const BvhNodeDev& c) {
-    bool leaf = (c.data & 0x3fffffffu) == 1u;
-    q.mnx[m] = c.mins.x; q.mny[m] = c.mins.y; q.mnz[m] = c.mins.z;
-    q.mxx[m] = c.maxs.x; q.mxy[m] = c.maxs.y; q.mxz[m] = c.maxs.z;
-    q.child[m] = c.children;
-    q.kind[m] = leaf ? 1u : 2u;
-    ++m;
-  };
-  const BvhNodeDev* cs[2] = {&w.l, &w.r};
-  for (int s = 0; s < 2; ++s) {
-    const BvhNodeDev& c = *cs[s];
-    if ((c.data & 0x3fffffffu) == 0u) continue;  // empty (partial root)
-    if ((c.data & 0x3fffffffu) == 1u) { put(c); continue; }
-    WideNode g;
-    load_wide(wide, c.children, &g);
-    put(g.l);
-    if ((g.r.data & 0x3fffffffu) != 0u) put(g.r);
-  }
-  for (; m < 4; ++m) {
-    q.mnx[m] = q.mny[m] = q.mnz[m] = 0.f;
-    q.mxx[m] = q.mxy[m] = q.mxz[m] = 0.f;
-    q.child[m] = 0xffffffffu;
-    q.kind[m] = 0u;
-  }
-  quads[i] = q;
-}
-
-template <bool HAS_POSE, bool WANT_NORMAL, bool QUAD>
-__global__ void k_trimesh_rays(const WideNode* __restrict__ wide, const QuadNode* __restrict__ quads, const float4* __restrict__ soup, uint32_t n_tris,
+template <bool HAS_POSE, bool WANT_NORMAL>
+__global__ void k_trimesh_rays(const WideNode* __restrict__ wide, const float4* __restrict__ soup, uint32_t n_tris,
                                const float* __restrict__ rays, const uint32_t* __restrict__ order, uint32_t n, float max_toi,
                                Pose pose, uint32_t* __restrict__ feat, float* __restrict__ toi_out, float* __restrict__ normal_out,
                                uint32_t* __restrict__ err) {
@@ -194,53 +149,6 @@ __global__ void k_trimesh_rays(const WideNode* __restrict__ wide, const QuadNode
     // Partial root (single triangle), bvh_traverse.rs:354-362.
     float s = slab(root.l.mins, root.l.maxs, o, inv, zmask, max_toi);
     if (s < max_toi) try_leaf(root.l.children);
-  } else if constexpr (QUAD) {
-    uint32_t stack[QUAD_STACK];
-    int sp = 0;
-    uint32_t cur = 0;
-    for (;;) {
-      const float4* qp = reinterpret_cast<const float4*>(quads + cur);
-      float4 mnx = __ldg(qp), mny = __ldg(qp + 1), mnz = __ldg(qp + 2), mxx = __ldg(qp + 3), mxy = __ldg(qp + 4), mxz = __ldg(qp + 5);
-      uint4 ch = __ldg(reinterpret_cast<const uint4*>(qp + 6)), kd = __ldg(reinterpret_cast<const uint4*>(qp + 7));
-      float ts[4];
-      ts[0] = kd.x ? slab(make_float3(mnx.x, mny.x, mnz.x), make_float3(mxx.x, mxy.x, mxz.x), o, inv, zmask, best) : FLT_MAX;
-      ts[1] = kd.y ? slab(make_float3(mnx.y, mny.y, mnz.y), make_float3(mxx.y, mxy.y, mxz.y), o, inv, zmask, best) : FLT_MAX;
-      ts[2] = kd.z ? slab(make_float3(mnx.z, mny.z, mnz.z), make_float3(mxx.z, mxy.z, mxz.z), o, inv, zmask, best) : FLT_MAX;
-      ts[3] = kd.w ? slab(make_float3(mnx.w, mny.w, mnz.w), make_float3(mxx.w, mxy.w, mxz.w), o, inv, zmask, best) : FLT_MAX;
-      uint32_t chs[4] = {ch.x, ch.y, ch.z, ch.w}, kds[4] = {kd.x, kd.y, kd.z, kd.w};
-      // leaves first, nearest first (they may lower `best` before the inner slots are pushed)
-      float it[4];
-      uint32_t ic[4];
-      int m = 0;
-#pragma unroll
-      for (int j = 0; j < 4; ++j) {
-        if (ts[j] == FLT_MAX || !(ts[j] < best || (have && ts[j] == best))) continue;
-        if (kds[j] == 1u) try_leaf(chs[j]);
-        else { it[m] = ts[j]; ic[m] = chs[j]; ++m; }
-      }
-      // inner slots still in range, nearest popped first
-      uint32_t next = 0xffffffffu;
-      float nt = FLT_MAX;
-      for (int j = 0; j < m; ++j) {
-        if (!(it[j] < best || (have && it[j] == best))) continue;
-        if (it[j] < nt) {
-          if (next != 0xffffffffu) {
-            if (sp >= QUAD_STACK) { atomicOr(err, ERR_STACK_OVERFLOW); next = 0xffffffffu; sp = 0; break; }
-            stack[sp++] = next;
-          }
-          next = ic[j];
-          nt = it[j];
-        } else {
-          if (sp >= QUAD_STACK) { atomicOr(err, ERR_STACK_OVERFLOW); next = 0xffffffffu; sp = 0; break; }
-          stack[sp++] = ic[j];
-        }
-      }
-      if (next == 0xffffffffu) {
-        if (sp == 0) break;
-        next = stack[--sp];
-      }
-      cur = next;
-    }
   } else {
     uint32_t stack[RAY_STACK];
     int sp = 0;
@@ -421,13 +329,6 @@ parrygpu_status parrygpu_trimesh_create(parrygpu_ctx* ctx, const float* vertices
       k_tri_soup<<<div_up(n_triangles, 256), 256, 0, ctx->stream>>>((const float*)dv, (const uint32_t*)di, m->bvh.leaf_index.as<uint32_t>(),
                                                                      n_triangles, n_vertices, m->soup.as<float4>());
       ctx->launches++;
-      if (m->bvh.n_wide > 0 && m->quads.reserve((size_t)m->bvh.n_wide * sizeof(QuadNode)) == cudaSuccess) {
-        k_build_quads<<<div_up(m->bvh.n_wide, 128), 128, 0, ctx->stream>>>(m->bvh.wide.as<WideNode>(), m->bvh.n_wide, m->quads.as<QuadNode>());
-        ctx->launches++;
-      } else {
-        cudaGetLastError();
-        m->quads.release();  // traversal falls back to the binary tree
-      }
     }
     cudaError_t se = cudaStreamSynchronize(ctx->stream);
     aabbs.release();
@@ -446,7 +347,7 @@ parrygpu_status parrygpu_trimesh_create(parrygpu_ctx* ctx, const float* vertices
 void parrygpu_trimesh_destroy(parrygpu_trimesh* m) {
   if (!m) return;
   for (DevBuf* d : {&m->bvh.wide, &m->bvh.leaf_parent, &m->bvh.node_parent, &m->bvh.leaf_index, &m->bvh.flags, &m->bvh.root_aabb,
-                    &m->bvh.info, &m->soup, &m->quads})
+                    &m->bvh.info, &m->soup})
     d->release();
   delete m;
 }
@@ -507,20 +408,13 @@ parrygpu_status parrygpu_trimesh_cast_rays(parrygpu_ctx* ctx, const parrygpu_tri
     uint32_t bs = ctx->cfg.ray_block ? ctx->cfg.ray_block : 128;
     const WideNode* w = mesh->bvh.wide.as<WideNode>();
     const float4* soup = mesh->soup.as<float4>();
-    const QuadNode* qd = mesh->quads.as<QuadNode>();
-    bool quad = ctx->cfg.ray_tree == 0 && qd != nullptr;
-#define PG_RAY_LAUNCH(P, N, Q)                                                                                                   \
-  k_trimesh_rays<P, N, Q><<<div_up(n, bs), bs, 0, ctx->stream>>>(w, qd, soup, mesh->n_triangles, (const float*)d_rays, order, n, \
-                                                                 max_toi, pose, (uint32_t*)d_feat, (float*)d_toi,               \
-                                                                 (float*)d_nrm, ctx->d_err)
+#define PG_RAY_LAUNCH(P, N)                                                                                               \
+  k_trimesh_rays<P, N><<<div_up(n, bs), bs, 0, ctx->stream>>>(w, soup, mesh->n_triangles, (const float*)d_rays, order, n, \
+                                                              max_toi, pose, (uint32_t*)d_feat, (float*)d_toi,            \
+                                                              (float*)d_nrm, ctx->d_err)
     KernelTimer kt(ctx, "trimesh_rays");
-    if (quad) {
-      if (has_pose) { if (d_nrm) PG_RAY_LAUNCH(true, true, true); else PG_RAY_LAUNCH(true, false, true); }
-      else { if (d_nrm) PG_RAY_LAUNCH(false, true, true); else PG_RAY_LAUNCH(false, false, true); }
-    } else {
-      if (has_pose) { if (d_nrm) PG_RAY_LAUNCH(true, true, false); else PG_RAY_LAUNCH(true, false, false); }
-      else { if (d_nrm) PG_RAY_LAUNCH(false, true, false); else PG_RAY_LAUNCH(false, false, false); }
-    }
+    if (has_pose) { if (d_nrm) PG_RAY_LAUNCH(true, true); else PG_RAY_LAUNCH(true, false); }
+    else { if (d_nrm) PG_RAY_LAUNCH(false, true); else PG_RAY_LAUNCH(false, false); }
 #undef PG_RAY_LAUNCH
     kt.stop();
     PG_LAUNCHED(ctx);
@@ -555,18 +449,11 @@ parrygpu_status launch_trimesh_rays(parrygpu_ctx* ctx, const parrygpu_trimesh* m
   uint32_t bs = ctx->cfg.ray_block ? ctx->cfg.ray_block : 128;
   const WideNode* w = mesh->bvh.wide.as<WideNode>();
   const float4* soup = mesh->soup.as<float4>();
-  const QuadNode* qd = mesh->quads.as<QuadNode>();
-  bool quad = ctx->cfg.ray_tree == 0 && qd != nullptr;
-#define PG_RAY_LAUNCH2(P, N, Q)                                                                                                    \
-  k_trimesh_rays<P, N, Q><<<div_up(n, bs), bs, 0, ctx->stream>>>(w, qd, soup, mesh->n_triangles, d_rays, order, n, max_toi, pose, \
-                                                                 d_feat, d_toi, d_nrm, ctx->d_err)
-  if (quad) {
-    if (has_pose) { if (d_nrm) PG_RAY_LAUNCH2(true, true, true); else PG_RAY_LAUNCH2(true, false, true); }
-    else { if (d_nrm) PG_RAY_LAUNCH2(false, true, true); else PG_RAY_LAUNCH2(false, false, true); }
-  } else {
-    if (has_pose) { if (d_nrm) PG_RAY_LAUNCH2(true, true, false); else PG_RAY_LAUNCH2(true, false, false); }
-    else { if (d_nrm) PG_RAY_LAUNCH2(false, true, false); else PG_RAY_LAUNCH2(false, false, false); }
-  }
+#define PG_RAY_LAUNCH2(P, N)                                                                                                   \
+  k_trimesh_rays<P, N><<<div_up(n, bs), bs, 0, ctx->stream>>>(w, soup, mesh->n_triangles, d_rays, order, n, max_toi, pose, d_feat, \
+                                                              d_toi, d_nrm, ctx->d_err)
+  if (has_pose) { if (d_nrm) PG_RAY_LAUNCH2(true, true); else PG_RAY_LAUNCH2(true, false); }
+  else { if (d_nrm) PG_RAY_LAUNCH2(false, true); else PG_RAY_LAUNCH2(false, false); }
 #undef PG_RAY_LAUNCH2
   PG_LAUNCHED(ctx);
   return PARRYGPU_OK;
