@@ -142,6 +142,43 @@ def cpu_oracle_rays(v, i, rays, reps: int):
     return len(rays) / statistics.median(times) / 1e6, stats, threads
 
 
+def rays_f64_error(v, i, rays, feat, toi, nrm, sample: int = 131072) -> dict:
+    """Error of the device results against the f64 oracle (parry3d-f64 restated) on the first
+    `sample` rays: hit agreement, relative toi error and normal error where both hit the same triangle."""
+    import numpy as np
+    from oracle import oracle as O
+    k = min(sample, len(rays))
+    f64, t64, n64 = O.TriMesh(v, i, "f64").cast_rays_and_get_normal(rays[:k], MAX_TOI)
+    f32 = np.asarray(feat[:k]).view(np.uint32)
+    both = (f32 == f64) & (f64 != 0xFFFFFFFF)
+    rel = np.abs(np.asarray(toi[:k], np.float64)[both] - t64[both]) / np.maximum(np.abs(t64[both]), 1e-30)
+    nerr = np.linalg.norm(np.asarray(nrm[:k], np.float64)[both] - n64[both], axis=1)
+    return {"sample_rays": k, "same_hit_triangle": round(float(np.mean(f32 == f64)), 7),
+            "toi_rel_err_max": float(rel.max(initial=0.0)), "toi_rel_err_p99": float(np.quantile(rel, 0.99)) if rel.size else 0.0,
+            "normal_err_max": float(nerr.max(initial=0.0))}
+
+
+def contacts_f64_error(s, pairs, has, res, sample: int = 16384) -> dict:
+    """Error of the device contacts against the f64 oracle on the first `sample` pairs: has-contact
+    agreement, and where both report a contact the depth, normal and contact-point errors."""
+    import numpy as np
+    from oracle import oracle as O
+    k = min(sample, len(pairs))
+    h64, o64, _ = O.contacts(s, pairs[:k], 0.0, precision="f64", threads=os.cpu_count() or 1)
+    h32 = np.asarray(has[:k])
+    r32 = np.asarray(res[:k], np.float64)
+    both = (h32 != 0) & (h64 != 0)
+    dist = np.abs(r32[both, 12] - o64[both, 12])
+    nerr = np.linalg.norm(r32[both, 6:9] - o64[both, 6:9], axis=1)
+    perr = np.maximum(np.linalg.norm(r32[both, 0:3] - o64[both, 0:3], axis=1),
+                      np.linalg.norm(r32[both, 3:6] - o64[both, 3:6], axis=1))
+    q = lambda a: float(np.quantile(a, 0.99)) if a.size else 0.0  # noqa: E731
+    return {"sample_pairs": k, "has_contact_agreement": round(float(np.mean(h32 == h64)), 7),
+            "depth_abs_err_max": float(dist.max(initial=0.0)), "depth_abs_err_p99": q(dist),
+            "normal_err_max": float(nerr.max(initial=0.0)), "normal_err_p99": q(nerr),
+            "point_err_max": float(perr.max(initial=0.0)), "point_err_p99": q(perr)}
+
+
 def contacts_section(ctx, stream, steps: int, warmup: int, n_pairs: int, flush) -> dict:
     """Batched query::contact on uneven convex-hull pairs (8-256 vertices, log-uniform), the
     GJK/EPA workload: device-resident pairs/s, end-to-end pairs/s through host buffers, kernel
@@ -161,6 +198,10 @@ def contacts_section(ctx, stream, steps: int, warmup: int, n_pairs: int, flush) 
     contacts_section.device_inputs = (dev, dpairs)
     has = torch.empty(n_pairs, dtype=torch.uint8, device="cuda")
     res = torch.empty((n_pairs, 13), dtype=torch.float32, device="cuda")
+    t0 = time.perf_counter()
+    chosen = pg.autotune_contacts(ctx, dev, dpairs[: min(n_pairs, 131072)], 0.0, reps=2)
+    tune = {"chosen": {"epa_blocks_per_sm": chosen["epa_blocks_per_sm"]}, "sample_pairs": min(n_pairs, 131072),
+            "seconds": round(time.perf_counter() - t0, 3)}
     for _ in range(max(1, warmup)):
         pg.contacts(ctx, dev, dpairs, 0.0, out=(has, res))
     torch.cuda.synchronize()
@@ -178,6 +219,7 @@ def contacts_section(ctx, stream, steps: int, warmup: int, n_pairs: int, flush) 
     ms = sum(a.elapsed_time(b) for a, b in zip(st_ev, en_ev)) / steps
     g_ms, g_n = ctx.kernel_time("contacts_gjk")
     e_ms, e_n = ctx.kernel_time("contacts_epa")
+    b_ms, b_n = ctx.kernel_time("contacts_bin")
     ctx.enable_kernel_timing(False)
     launches = ctx.kernel_launches - l0
     _, _, gst = pg.contacts(ctx, dev, dpairs, 0.0, out=(has, res), want_stats=True)
@@ -218,8 +260,10 @@ def contacts_section(ctx, stream, steps: int, warmup: int, n_pairs: int, flush) 
     return {
         "workload": "convex hull pairs, 8-256 vertices log-uniform on ellipsoids, random relative pose, prediction 0",
         "pairs": n_pairs, "metric": "contact pairs/s", "value": round(n_pairs / (ms / 1e3), 1), "unit": "pairs/s",
-        "ms_per_step": round(ms, 4), "kernel_ms": {"gjk": round(g_ms / max(g_n, 1), 4), "epa": round(e_ms / max(e_n, 1), 4)},
+        "ms_per_step": round(ms, 4), "kernel_ms": {"bin": round(b_ms / max(b_n, 1), 4), "gjk": round(g_ms / max(g_n, 1), 4),
+                                          "epa": round(e_ms / max(e_n, 1), 4)},
         "gpu_launches": launches,
+        "autotune": tune,
         "e2e": {"value": round(n_pairs / (e2e_ms / 1e3), 1), "unit": "pairs/s", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h), "ms_per_step": round(e2e_ms, 3)},
         "mean_iterations": {"gjk": round(gst["gjk_iters"] / n_pairs, 4), "epa": round(gst["epa_iters"] / n_pairs, 4),
@@ -232,6 +276,7 @@ def contacts_section(ctx, stream, steps: int, warmup: int, n_pairs: int, flush) 
         "cpu_baseline": {"value": round(sample / cpu_s, 1), "unit": "pairs/s", "cores": threads, "kind": "port",
                          "sample": f"first {sample} pairs; C++ restatement of parry3d f32 query::contact"},
         "matches_oracle_on_sample": same,
+        "error_vs_f64_oracle": contacts_f64_error(s, pairs, has.cpu().numpy(), res.cpu().numpy()),
     }
 
 
@@ -581,7 +626,8 @@ def run_gb300(args) -> int:
     n = args.n_rays
     v, i = W.terrain_mesh()
     rays_h = W.terrain_rays(n)
-    ctx = pg.Context(device=local)
+    fixed = args.ray_sort is not None
+    ctx = pg.Context(device=local, sort_rays=fixed and args.ray_sort >= 0, ray_sort_key=max(args.ray_sort or 0, 0))
     # One explicit stream shared by the library and the timing events (torch's default stream
     # handle is 0, which the library would map to its own stream).
     stream = torch.cuda.Stream()
@@ -593,6 +639,14 @@ def run_gb300(args) -> int:
     toi = torch.empty(n, dtype=torch.float32, device="cuda")
     nrm = torch.empty((n, 3), dtype=torch.float32, device="cuda")
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+
+    # launch configuration: tuned on the first 262,144 rays unless fixed on the command line
+    tune = None
+    if not fixed:
+        t0 = time.perf_counter()
+        chosen = mesh.autotune(rays_d[: min(n, 262144)], MAX_TOI, reps=3)
+        tune = {"chosen": {k: chosen[k] for k in ("sort_rays", "ray_sort_key", "ray_traversal", "ray_block", "ray_refill")},
+                "sample_rays": min(n, 262144), "seconds": round(time.perf_counter() - t0, 3)}
 
     def step():
         mesh.cast_rays_and_get_normal(rays_d, MAX_TOI, out=(feat, toi, nrm))
@@ -695,6 +749,8 @@ def run_gb300(args) -> int:
                          "kernel_ms": round(k_avg, 4), "sort_ms": round(s_ms / max(s_n, 1), 4)},
             "cpu_baseline": {"value": round(cpu_value, 3), "unit": "Mrays/s", "cores": threads, "kind": "port",
                              "sample": f"the full workload ({n} rays), median of 3; C++ restatement of parry3d f32"},
+            "autotune": tune if tune else {"fixed": ctx.config},
+            "error_vs_f64_oracle": rays_f64_error(v, i, rays_h, feat.cpu().numpy(), toi.cpu().numpy(), nrm.cpu().numpy()),
             "gpu_launches": launches,
             "clocks": clocks,
             "contacts": contacts,
@@ -722,6 +778,9 @@ def main() -> int:
                     help="ball/cuboid/capsule pairs of the contact-manifold section (0 skips it)")
     ap.add_argument("--scene-frames", type=int, default=100,
                     help="frames of the per-frame pipeline section (0 skips it)")
+    ap.add_argument("--ray-sort", type=int, default=None, choices=[-1, 0, 1, 2],
+                    help="fixed ray ordering before TriMesh traversal (-1 none, else the ray_sort_key mode); "
+                         "default: chosen by the autotuner")
     ap.add_argument("--scene-shapes", type=int, default=262144, help="shapes of the per-frame pipeline section")
     ap.add_argument("--scene-rays", type=int, default=4194304, help="rays per frame of the per-frame pipeline section")
     ap.add_argument("--train-pairs", type=int, default=1 << 21,

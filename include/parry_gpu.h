@@ -48,12 +48,18 @@ typedef struct parrygpu_compound parrygpu_compound;
 
 typedef struct parrygpu_config {
   int device;              /* CUDA device ordinal */
-  uint32_t ray_block;      /* threads per block for ray traversal (0 = library default) */
+  uint32_t ray_block;      /* threads per block for TriMesh ray traversal: 0 (library default, 128) or a
+                              multiple of 32 up to 1024 */
   uint32_t sort_rays;      /* 1 = Morton-sort rays before traversal (default), 0 = input order */
   uint32_t ray_sort_key;   /* 0 = 30-bit Morton code of the origin; 1 = direction octant (3 bits)
-                              above a 27-bit Morton code of the origin */
-  uint32_t epa_blocks_per_sm; /* contacts EPA: resident 64-thread blocks per SM (0 = library default, 8) */
-  uint32_t reserved[3];
+                              above a 27-bit Morton code of the origin; 2 = the top 16 bits of the
+                              origin's Morton code (two radix passes instead of four) */
+  uint32_t epa_blocks_per_sm; /* contacts EPA: resident 64-thread blocks per SM (0 = library default, 8; at most 32) */
+  uint32_t ray_traversal;  /* TriMesh ray traversal: 0 = library default (1); 1 = one ray per thread;
+                              2 = persistent warps that fetch new rays as lanes finish theirs */
+  uint32_t ray_refill;     /* traversal 2: a warp fetches rays once this many of its lanes are idle
+                              (0 = library default, 16; at most 32) */
+  uint32_t reserved[1];
 } parrygpu_config;
 
 /* ---- context ---------------------------------------------------------------------------- */
@@ -365,6 +371,25 @@ parrygpu_status parrygpu_compound_set_poses(parrygpu_ctx* ctx, parrygpu_compound
  * world-space normal (normal may be NULL). Exact toi ties resolve to the lowest part index. */
 parrygpu_status parrygpu_compound_cast_rays(parrygpu_ctx* ctx, const parrygpu_compound* compound, const float* pose7, const float* rays,
                                             uint32_t n, float max_toi, int solid, uint32_t* part, float* toi, float* normal);
+
+/* ---- launch-configuration autotuner -------------------------------------------------------- */
+/* No reference counterpart (parry runs on the CPU). Answers never depend on the configuration;
+ * these only pick how the same work maps onto the SMs, for the caller's own inputs. */
+
+/* Copies the context's current configuration into *out. */
+parrygpu_status parrygpu_get_config(const parrygpu_ctx* ctx, parrygpu_config* out);
+/* Times parrygpu_trimesh_cast_rays on `rays` (device or host; copied to the device once, outputs
+ * kept on the device) for each candidate ray ordering (input order; 30-bit Morton; octant + 27-bit
+ * Morton; 16-bit Morton prefix) x traversal (one ray per thread at 64, 128, 256 threads per block;
+ * dynamic fetch refilling at 8, 16, 24 idle lanes): one untimed run then `reps` timed runs each
+ * (0 = 3). The fastest candidate becomes the context's configuration and is
+ * copied to *chosen (may be NULL). On an error the configuration is left unchanged. */
+parrygpu_status parrygpu_autotune_trimesh_rays(parrygpu_ctx* ctx, const parrygpu_trimesh* mesh, const float* pose7, const float* rays,
+                                               uint32_t n, float max_toi, uint32_t reps, parrygpu_config* chosen);
+/* Times parrygpu_contacts on (shapes, pairs) for each EPA residency (4, 6, 8, 12, 16 blocks per
+ * SM), `reps` timed runs each (0 = 2), and keeps the fastest as for the ray tuner. */
+parrygpu_status parrygpu_autotune_contacts(parrygpu_ctx* ctx, const parrygpu_shapes* shapes, const uint32_t* pairs, uint64_t n_pairs,
+                                           float prediction, uint32_t reps, parrygpu_config* chosen);
 
 #ifdef __cplusplus
 }

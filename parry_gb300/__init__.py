@@ -75,11 +75,16 @@ def _alloc_like(ref, shape, dtype):
     return a, C.c_void_p(a.ctypes.data)
 
 
+def _config_dict(cfg) -> dict:
+    return {"device": cfg.device, "ray_block": cfg.ray_block, "sort_rays": bool(cfg.sort_rays), "ray_sort_key": cfg.ray_sort_key,
+            "epa_blocks_per_sm": cfg.epa_blocks_per_sm, "ray_traversal": cfg.ray_traversal, "ray_refill": cfg.ray_refill}
+
+
 class Context:
     """A device context (one CUDA stream). Mirrors nothing in parry, which is single-threaded CPU."""
 
     def __init__(self, device: int = 0, ray_block: int = 0, sort_rays: bool = True, ray_sort_key: int = 0,
-                 epa_blocks_per_sm: int = 0):
+                 epa_blocks_per_sm: int = 0, ray_traversal: int = 0, ray_refill: int = 0):
         cfg = _capi.ParryGpuConfig()
         lib().parrygpu_default_config(C.byref(cfg))
         cfg.device = device
@@ -87,6 +92,8 @@ class Context:
         cfg.sort_rays = 1 if sort_rays else 0
         cfg.ray_sort_key = ray_sort_key
         cfg.epa_blocks_per_sm = epa_blocks_per_sm
+        cfg.ray_traversal = ray_traversal
+        cfg.ray_refill = ray_refill
         h = C.c_void_p()
         check(lib().parrygpu_create(C.byref(h), C.byref(cfg)))
         self._h = h
@@ -117,6 +124,13 @@ class Context:
         ms, n = C.c_double(0.0), C.c_uint64(0)
         check(lib().parrygpu_kernel_time(self._h, kernel.encode(), C.byref(ms), C.byref(n)), self._h)
         return ms.value, n.value
+
+    @property
+    def config(self) -> dict:
+        """The context's launch configuration (parrygpu_config fields)."""
+        cfg = _capi.ParryGpuConfig()
+        check(lib().parrygpu_get_config(self._h, C.byref(cfg)), self._h)
+        return _config_dict(cfg)
 
     def close(self) -> None:
         if getattr(self, "_h", None):
@@ -236,6 +250,16 @@ class TriMesh:
         feature = triangle (front face), triangle + n_triangles (back face) or NO_HIT."""
         return self._cast(rays, max_toi, solid, pose, True, out)
 
+    def autotune(self, rays, max_toi: float, pose=None, reps: int = 3) -> dict:
+        """Times this mesh's ray cast on `rays` for each candidate ray ordering and block size and
+        keeps the fastest in the context's configuration; returns the chosen configuration."""
+        kr, pr = _as_input(rays, np.float32)
+        kp, pp = _as_input(pose, np.float32) if pose is not None else (None, None)
+        cfg = _capi.ParryGpuConfig()
+        check(lib().parrygpu_autotune_trimesh_rays(self.ctx.handle, self._h, pp, pr, int(kr.shape[0]), float(max_toi), int(reps),
+                                                   C.byref(cfg)), self.ctx.handle)
+        return _config_dict(cfg)
+
     def cast_rays(self, rays, max_toi: float, solid: bool = True, pose=None, out=None):
         """Batched RayCast::cast_ray (toi only). Returns (feature, toi)."""
         f, t, _ = self._cast(rays, max_toi, solid, pose, False, out)
@@ -336,6 +360,17 @@ def contacts(ctx: Context, shapes, pairs, prediction: float, init_dirs=None, wan
     if want_stats:
         return has, res, {"gjk_iters": stats.gjk_iterations, "epa_iters": stats.epa_iterations, "epa_calls": stats.epa_calls}
     return has, res
+
+
+def autotune_contacts(ctx: Context, shapes, pairs, prediction: float = 0.0, reps: int = 2) -> dict:
+    """Times contacts(shapes, pairs, prediction) for each EPA residency and keeps the fastest in the
+    context's configuration; returns the chosen configuration."""
+    st = _StagedShapes(shapes)
+    kp, pp = _as_input(pairs, np.uint32)
+    cfg = _capi.ParryGpuConfig()
+    check(lib().parrygpu_autotune_contacts(ctx.handle, C.byref(st.struct), pp, int(kp.shape[0]), float(prediction), int(reps),
+                                           C.byref(cfg)), ctx.handle)
+    return _config_dict(cfg)
 
 
 def contact_manifolds(ctx: Context, shapes, pairs, prediction: float, manifolds, want_stats: bool = False):

@@ -56,6 +56,9 @@ SIGNATURES: dict[str, tuple] = {
     "parrygpu_trimesh_cast_rays_noalloc": (I32, [P, P, P, P, U32, F32, I32, P, P, P]),
     "parrygpu_shapes_aabbs": (I32, [P, P, F32, P]),
     "parrygpu_contacts": (I32, [P, P, P, U64, F32, P, P, P, P]),
+    "parrygpu_get_config": (I32, [P, P]),
+    "parrygpu_autotune_trimesh_rays": (I32, [P, P, P, P, U32, F32, U32, P]),
+    "parrygpu_autotune_contacts": (I32, [P, P, P, U64, F32, U32, P]),
     "parrygpu_contacts_with_dirs": (I32, [P, P, P, U64, F32, P, P, P, P, P]),
     "parrygpu_contact_manifolds": (I32, [P, P, P, U64, F32, P, P]),
     "parrygpu_polyhedra_build": (I32, [P, P, P, U64, U32, C.POINTER(P)]),
@@ -109,7 +112,8 @@ class ParryGpuError(RuntimeError):
 
 class ParryGpuConfig(C.Structure):
     _fields_ = [("device", C.c_int), ("ray_block", C.c_uint32), ("sort_rays", C.c_uint32), ("ray_sort_key", C.c_uint32),
-                ("epa_blocks_per_sm", C.c_uint32), ("reserved", C.c_uint32 * 3)]
+                ("epa_blocks_per_sm", C.c_uint32), ("ray_traversal", C.c_uint32), ("ray_refill", C.c_uint32),
+                ("reserved", C.c_uint32 * 1)]
 
 
 _lib = None

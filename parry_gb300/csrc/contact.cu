@@ -130,13 +130,34 @@ __device__ __forceinline__ void flip(ContactOut* c) {
   t = c->n1; c->n1 = c->n2; c->n2 = t;
 }
 
+// Binning key of a pair: the vertices one support evaluation of the pair scans (vertex count of
+// a convex / triangle shape, 1 for the others, summed over the two shapes; capped at 1023).
+// Threads of a warp then run pairs of similar cost, and so do the EPA queue entries they append.
+__global__ void k_pair_cost_keys(ShapeArrays sh, const uint32_t* __restrict__ pairs, uint32_t n, uint32_t* __restrict__ keys,
+                                 uint32_t* __restrict__ vals) {
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  uint32_t a = pairs[2 * (size_t)i], b = pairs[2 * (size_t)i + 1];
+  uint32_t c = 2;
+  if (a < sh.n_shapes && b < sh.n_shapes) {
+    uint32_t ta = sh.types[a], tb = sh.types[b];
+    uint32_t ca = (ta == SH_CONVEX || ta == SH_TRIANGLE) ? __float_as_uint(sh.params[a].y) : 1u;
+    uint32_t cb = (tb == SH_CONVEX || tb == SH_TRIANGLE) ? __float_as_uint(sh.params[b].y) : 1u;
+    c = (ca > 1023u ? 1023u : ca) + (cb > 1023u ? 1023u : cb);
+  }
+  keys[i] = c > 1023u ? 1023u : c;
+  vals[i] = i;
+}
+
+// Thread i handles pair order[i] (order = NULL: pair i).
 __global__ void __launch_bounds__(CT_THREADS) k_contacts_main(ShapeArrays sh, const uint32_t* __restrict__ pairs, uint64_t n,
-                                                              float prediction, const float* __restrict__ init_dirs,
-                                                              float* __restrict__ out, uint8_t* __restrict__ has,
-                                                              uint32_t* __restrict__ queue, unsigned long long* __restrict__ qcount,
-                                                              unsigned long long* __restrict__ stats, uint32_t* __restrict__ err,
-                                                              float* __restrict__ final_dirs) {
+                                                              const uint32_t* __restrict__ order, float prediction,
+                                                              const float* __restrict__ init_dirs, float* __restrict__ out,
+                                                              uint8_t* __restrict__ has, uint32_t* __restrict__ queue,
+                                                              unsigned long long* __restrict__ qcount, unsigned long long* __restrict__ stats,
+                                                              uint32_t* __restrict__ err, float* __restrict__ final_dirs) {
   uint64_t k = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+  if (order && k < n) k = order[k];
   uint32_t iters = 0;
   if (k < n && !valid_pair(sh, pairs[2 * k], pairs[2 * k + 1])) {
     atomicOr(err, ERR_CAPACITY);
@@ -216,7 +237,7 @@ __global__ void __launch_bounds__(EPA_THREADS) k_contacts_epa(ShapeArrays sh, co
                                                               uint32_t* __restrict__ ws_pool, unsigned long long* __restrict__ stats,
                                                               uint32_t* __restrict__ err, float* __restrict__ final_dirs) {
   const uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x;
-  EpaWs ws{ws_pool + (size_t)(slot >> 5) * (EPA_WORDS * 32) + (slot & 31)};
+  EpaWs ws = epa_slot(ws_pool, slot);
   const unsigned long long total = *qcount;
   uint32_t iters = 0, calls = 0;
   for (unsigned long long e = slot; e < total; e += (unsigned long long)gridDim.x * blockDim.x) {
@@ -430,14 +451,28 @@ parrygpu_status parrygpu_contacts_with_dirs(parrygpu_ctx* ctx, const parrygpu_sh
   if (epa_per_sm > 32) epa_per_sm = 32;
   uint32_t epa_blocks = (uint32_t)(ctx->sm_count > 0 ? ctx->sm_count : 152) * epa_per_sm;
   uint32_t slots = epa_blocks * EPA_THREADS;
-  PG_CUDA(ctx, ctx->epa_ws.reserve((size_t)(slots / 32) * EPA_SLOT_GROUP_BYTES));
+  PG_CUDA(ctx, ctx->epa_ws.reserve((size_t)slots * EPA_SLOT_BYTES));
   unsigned long long* ctr = ctx->ct_counters.as<unsigned long long>();  // [0] queue count, [1..3] stats
   PG_CUDA(ctx, cudaMemsetAsync(ctr, 0, 64, ctx->stream));
+  // pairs binned by support-scan cost (a 10-bit key, two radix passes)
+  const uint32_t* order = nullptr;
+  if (n_pairs > 4096 && n_pairs < 0xffffffffull) {
+    uint32_t n = (uint32_t)n_pairs;
+    if ((s = radix_sort_reserve(ctx, n)) != PARRYGPU_OK) return s;
+    KernelTimer kt(ctx, "contacts_bin");
+    k_pair_cost_keys<<<div_up(n, 256), 256, 0, ctx->stream>>>(sh, (const uint32_t*)dp, n, ctx->sort_k[0].as<uint32_t>(),
+                                                                ctx->sort_v[0].as<uint32_t>());
+    PG_LAUNCHED(ctx);
+    int rb;
+    if ((s = radix_sort_pairs(ctx, n, 10, &rb)) != PARRYGPU_OK) return s;
+    kt.stop();
+    order = ctx->sort_v[rb].as<uint32_t>();
+  }
   {
     KernelTimer kt(ctx, "contacts_gjk");
     k_contacts_main<<<div_up(n_pairs, CT_THREADS), CT_THREADS, 0, ctx->stream>>>(
-        sh, (const uint32_t*)dp, n_pairs, prediction, (const float*)di, (float*)d_out, (uint8_t*)d_has, ctx->ct_queue.as<uint32_t>(),
-        ctr, ctr + 1, ctx->d_err, (float*)d_dirs);
+        sh, (const uint32_t*)dp, n_pairs, order, prediction, (const float*)di, (float*)d_out, (uint8_t*)d_has,
+        ctx->ct_queue.as<uint32_t>(), ctr, ctr + 1, ctx->d_err, (float*)d_dirs);
     kt.stop();
     PG_LAUNCHED(ctx);
   }

@@ -1,12 +1,15 @@
 // Device-side EPA (src/query/epa/epa3.rs:17-675, path relative to the parry repository).
 //
-// The polytope lives in a per-thread workspace slot in global memory, interleaved across the 32
-// slots of a warp (word w of slot s at base[w * 32 + s % 32]) so that lanes touching the same
-// element index coalesce. Fixed capacities replace the reference's Vecs; exceeding one aborts the
-// pair and raises a capacity error (observed maxima on 8-256-vertex hull pairs: 239 faces,
-// 55 vertices, silhouettes of 10 edges). The reference's recursive silhouette walk becomes an
-// explicit stack visiting faces in the same order, and its BinaryHeap is restated with the same
-// sift operations so that ties between face distances pop in the same order.
+// The polytope lives in a per-thread workspace slot in global memory, one contiguous block of
+// words per slot: the lanes of a warp work on different faces and heap positions at any moment,
+// so records are laid out for one lane's accesses. A vertex's CSO point is one 16-byte word group
+// (read with one vector load); its two witness points, used only for the final closest points,
+// sit in a separate array; a face is 8 words, one 32-byte sector. Fixed capacities replace the
+// reference's Vecs; exceeding one aborts the pair and raises a capacity error (observed maxima on
+// 8-256-vertex hull pairs: 239 faces, 55 vertices, silhouettes of 10 edges). The reference's
+// recursive silhouette walk becomes an explicit stack visiting faces in the same order, and its
+// BinaryHeap is restated with the same sift operations so that ties between face distances pop
+// in the same order.
 #pragma once
 #include "gjk_device.cuh"
 
@@ -16,12 +19,14 @@ namespace pg {
 template <int MV, int MF, int MS, int MSTK>
 struct EpaLayout {
   static constexpr int MAX_VERTS = MV, MAX_FACES = MF, MAX_SIL = MS, STACK = MSTK;
-  static constexpr int W_VERTS = 0;                       // 9 words per vertex
-  static constexpr int W_FACES = W_VERTS + 9 * MV;        // 9 words per face
-  static constexpr int W_HEAP = W_FACES + 9 * MF;         // 2 words per heap entry
+  static constexpr int W_VP = 0;                          // 4 words per vertex: CSO point (x, y, z, -)
+  static constexpr int W_VO = W_VP + 4 * MV;              // 6 words per vertex: witness points orig1, orig2
+  static constexpr int W_FACES = W_VO + 6 * MV;           // 8 words per face
+  static constexpr int W_HEAP = W_FACES + 8 * MF;         // 2 words per heap entry
   static constexpr int W_SIL = W_HEAP + 2 * MF;           // 1 word per silhouette edge
   static constexpr int W_STACK = W_SIL + MS;              // 1 word per stack entry
   static constexpr int WORDS = W_STACK + MSTK;            // words per workspace
+  static_assert(W_FACES % 8 == 0 && WORDS % 8 == 0, "faces and slots start on 32-byte boundaries");
 };
 // Per-thread workspaces in global memory.
 using EpaGlobalLayout = EpaLayout<128, 512, 64, 256>;
@@ -29,27 +34,30 @@ using EpaGlobalLayout = EpaLayout<128, 512, 64, 256>;
 constexpr int EPA_MAX_VERTS = EpaGlobalLayout::MAX_VERTS;
 constexpr int EPA_MAX_FACES = EpaGlobalLayout::MAX_FACES;
 constexpr int EPA_WORDS = EpaGlobalLayout::WORDS;                     // words per slot
-constexpr size_t EPA_SLOT_GROUP_BYTES = (size_t)EPA_WORDS * 32 * 4;   // one warp's 32 slots
+constexpr size_t EPA_SLOT_BYTES = (size_t)EPA_WORDS * 4;             // bytes per slot
 
-// A workspace view: word i at base[i * STRIDE] (STRIDE 32: a lane-interleaved global slot).
-template <class L, int STRIDE>
+// A workspace view over one slot (word i at base[i]; base 32-byte aligned).
+template <class L>
 struct EpaWsT {
   using Layout = L;
   uint32_t* base;
-  __device__ __forceinline__ uint32_t& w(int i) const { return base[(size_t)i * STRIDE]; }
-  __device__ __forceinline__ float& f(int i) const { return reinterpret_cast<float&>(base[(size_t)i * STRIDE]); }
+  __device__ __forceinline__ uint32_t& w(int i) const { return base[i]; }
+  __device__ __forceinline__ float& f(int i) const { return reinterpret_cast<float&>(base[i]); }
   // vertices
   __device__ __forceinline__ void set_vert(int v, const CSO& c) const {
-    int o = L::W_VERTS + 9 * v;
-    f(o) = c.p.x; f(o + 1) = c.p.y; f(o + 2) = c.p.z;
-    f(o + 3) = c.o1.x; f(o + 4) = c.o1.y; f(o + 5) = c.o1.z;
-    f(o + 6) = c.o2.x; f(o + 7) = c.o2.y; f(o + 8) = c.o2.z;
+    *reinterpret_cast<float4*>(base + L::W_VP + 4 * v) = make_float4(c.p.x, c.p.y, c.p.z, 0.0f);
+    int o = L::W_VO + 6 * v;
+    f(o) = c.o1.x; f(o + 1) = c.o1.y; f(o + 2) = c.o1.z;
+    f(o + 3) = c.o2.x; f(o + 4) = c.o2.y; f(o + 5) = c.o2.z;
   }
-  __device__ __forceinline__ V3 vp(int v) const { int o = L::W_VERTS + 9 * v; return v3(f(o), f(o + 1), f(o + 2)); }
-  __device__ __forceinline__ V3 vo1(int v) const { int o = L::W_VERTS + 9 * v + 3; return v3(f(o), f(o + 1), f(o + 2)); }
-  __device__ __forceinline__ V3 vo2(int v) const { int o = L::W_VERTS + 9 * v + 6; return v3(f(o), f(o + 1), f(o + 2)); }
-  // faces: word0 = pts (3 x u8) | deleted << 24; word1 = adj0 | adj1 << 16; word2 = adj2; 3-5 normal; 6-8 bcoords
-  __device__ __forceinline__ int fo(int fid) const { return L::W_FACES + 9 * fid; }
+  __device__ __forceinline__ V3 vp(int v) const {
+    float4 q = *reinterpret_cast<const float4*>(base + L::W_VP + 4 * v);
+    return v3(q.x, q.y, q.z);
+  }
+  __device__ __forceinline__ V3 vo1(int v) const { int o = L::W_VO + 6 * v; return v3(f(o), f(o + 1), f(o + 2)); }
+  __device__ __forceinline__ V3 vo2(int v) const { int o = L::W_VO + 6 * v + 3; return v3(f(o), f(o + 1), f(o + 2)); }
+  // faces: word0 = pts (3 x u8) | deleted << 24; word1 = adj0 | adj1 << 16; word2 = adj2; 3-5 normal
+  __device__ __forceinline__ int fo(int fid) const { return L::W_FACES + 8 * fid; }
   __device__ __forceinline__ int pt(int fid, int k) const { return (w(fo(fid)) >> (8 * k)) & 0xff; }
   __device__ __forceinline__ bool deleted(int fid) const { return (w(fo(fid)) >> 24) != 0; }
   __device__ __forceinline__ void set_deleted(int fid) const { w(fo(fid)) |= 0x01000000u; }
@@ -62,9 +70,10 @@ struct EpaWsT {
     else w(fo(fid) + 2) = (uint32_t)v;
   }
   __device__ __forceinline__ V3 normal(int fid) const { int o = fo(fid) + 3; return v3(f(o), f(o + 1), f(o + 2)); }
-  __device__ __forceinline__ float bc(int fid, int k) const { return f(fo(fid) + 6 + k); }
 };
-using EpaWs = EpaWsT<EpaGlobalLayout, 32>;
+using EpaWs = EpaWsT<EpaGlobalLayout>;
+// The workspace of slot `slot` in a pool of EPA_WORDS-word slots.
+__device__ __forceinline__ EpaWs epa_slot(uint32_t* pool, uint32_t slot) { return EpaWs{pool + (size_t)slot * EPA_WORDS}; }
 
 template <class WS>
 struct EpaHeap {
@@ -131,14 +140,14 @@ struct EpaHeap {
   }
 };
 
-// Face::new (epa3.rs:90-118): writes face `fid`, returns whether the origin projects inside it.
-template <class WS>
-static __device__ __noinline__ bool epa_new_face(const WS& ws, int fid, int p0, int p1, int p2, int a0, int a1, int a2) {
-  V3 A = ws.vp(p0), B = ws.vp(p1), C = ws.vp(p2);
+// The barycentric part of Face::new (epa3.rs:90-118): the projection of the origin on triangle
+// (A, B, C) as barycentric coordinates, and whether the origin projects inside it. A face's
+// coordinates are not stored: they are recomputed from its vertices by this same function (same
+// inputs, same operations, same bits) for the one face whose closest points are returned.
+static __device__ __noinline__ bool epa_face_bcoords(V3 A, V3 B, V3 C, float bc[3]) {
   Loc loc;
   V3 proj = project_triangle(A, B, C, v3(0.f, 0.f, 0.f), &loc);
-  float bc[3] = {0.f, 0.f, 0.f};
-  bool inside;
+  bc[0] = 0.f; bc[1] = 0.f; bc[2] = 0.f;
   if (loc.kind == LOC_VERTEX || loc.kind == LOC_EDGE) {
     if (loc.kind == LOC_VERTEX) bc[loc.id] = 1.0f;
     else {
@@ -149,13 +158,20 @@ static __device__ __noinline__ bool epa_new_face(const WS& ws, int fid, int p0, 
     }
     bool is_inside = fabsf(proj.x) <= EPS && fabsf(proj.y) <= EPS && fabsf(proj.z) <= EPS;
     float tol = EPS * 100.0f;
-    inside = is_inside || dot(proj, proj) < tol * tol;
+    return is_inside || dot(proj, proj) < tol * tol;
   } else if (loc.kind == LOC_FACE) {
     bc[0] = loc.bc[0]; bc[1] = loc.bc[1]; bc[2] = loc.bc[2];
-    inside = true;
-  } else {
-    inside = false;
+    return true;
   }
+  return false;
+}
+
+// Face::new (epa3.rs:90-118): writes face `fid`, returns whether the origin projects inside it.
+template <class WS>
+static __device__ __noinline__ bool epa_new_face(const WS& ws, int fid, int p0, int p1, int p2, int a0, int a1, int a2) {
+  V3 A = ws.vp(p0), B = ws.vp(p1), C = ws.vp(p2);
+  float bc[3];
+  bool inside = epa_face_bcoords(A, B, C, bc);
   V3 n;
   if (!try_normalize(cross(B - A, C - A), EPS, &n)) n = v3(0.f, 0.f, 0.f);
   int o = ws.fo(fid);
@@ -163,16 +179,21 @@ static __device__ __noinline__ bool epa_new_face(const WS& ws, int fid, int p0, 
   ws.w(o + 1) = (uint32_t)a0 | ((uint32_t)a1 << 16);
   ws.w(o + 2) = (uint32_t)a2;
   ws.f(o + 3) = n.x; ws.f(o + 4) = n.y; ws.f(o + 5) = n.z;
-  ws.f(o + 6) = bc[0]; ws.f(o + 7) = bc[1]; ws.f(o + 8) = bc[2];
   return inside;
+}
+
+// Face::closest_points (epa3.rs:120-129) for the face with vertices (a, b, c).
+template <class WS>
+__device__ __forceinline__ void epa_closest_points_of(const WS& ws, int a, int b, int c, V3* p1, V3* p2) {
+  float bc[3];
+  epa_face_bcoords(ws.vp(a), ws.vp(b), ws.vp(c), bc);
+  *p1 = (ws.vo1(a) * bc[0] + ws.vo1(b) * bc[1]) + ws.vo1(c) * bc[2];
+  *p2 = (ws.vo2(a) * bc[0] + ws.vo2(b) * bc[1]) + ws.vo2(c) * bc[2];
 }
 
 template <class WS>
 __device__ __forceinline__ void epa_face_closest_points(const WS& ws, int fid, V3* p1, V3* p2) {
-  int a = ws.pt(fid, 0), b = ws.pt(fid, 1), c = ws.pt(fid, 2);
-  float b0 = ws.bc(fid, 0), b1 = ws.bc(fid, 1), b2 = ws.bc(fid, 2);
-  *p1 = (ws.vo1(a) * b0 + ws.vo1(b) * b1) + ws.vo1(c) * b2;
-  *p2 = (ws.vo2(a) * b0 + ws.vo2(b) * b1) + ws.vo2(c) * b2;
+  epa_closest_points_of(ws, ws.pt(fid, 0), ws.pt(fid, 1), ws.pt(fid, 2), p1, p2);
 }
 
 template <class WS>
@@ -259,7 +280,6 @@ __device__ __forceinline__ int epa_closest_points_t(const WS& ws, Sup sup, const
     int fpts[3] = {ws.pt(fid, 0), ws.pt(fid, 1), ws.pt(fid, 2)};
     int fadj[3] = {ws.adj(fid, 0), ws.adj(fid, 1), ws.adj(fid, 2)};
     V3 fnormal = ws.normal(fid);
-    float fbc[3] = {ws.bc(fid, 0), ws.bc(fid, 1), ws.bc(fid, 2)};
     if (nverts >= L::MAX_VERTS) return EPA_OVERFLOW;
     CSO cso = sup(fnormal);
     int support_id = nverts;
@@ -316,10 +336,7 @@ __device__ __forceinline__ int epa_closest_points_t(const WS& ws, Sup sup, const
       if (inside) {
         float dist = dot(ws.normal(new_id), ws.vp(ws.pt(new_id, 0)));
         if (dist < curr_dist) {
-          V3 a0 = ws.vo1(fpts[0]), a1 = ws.vo1(fpts[1]), a2 = ws.vo1(fpts[2]);
-          V3 b0 = ws.vo2(fpts[0]), b1 = ws.vo2(fpts[1]), b2 = ws.vo2(fpts[2]);
-          *p1 = (a0 * fbc[0] + a1 * fbc[1]) + a2 * fbc[2];
-          *p2 = (b0 * fbc[0] + b1 * fbc[1]) + b2 * fbc[2];
+          epa_closest_points_of(ws, fpts[0], fpts[1], fpts[2], p1, p2);
           *n = fnormal;
           return EPA_OK;
         }

@@ -110,7 +110,7 @@ struct parrygpu_trimesh {
 // A shape set under one BVH (the reference's Compound), with device copies of the shape arrays.
 struct parrygpu_compound {
   uint64_t n = 0, n_vertices = 0;
-  DevBuf types, params, poses, pool, aabbs;
+  DevBuf types, params, poses, pool, aabbs, hull_box;
   parrygpu_bvh bvh;
 };
 
@@ -148,9 +148,13 @@ parrygpu_status radix_sort_pairs_in(parrygpu_ctx* ctx, uint32_t n, int key_bits,
 uint32_t radix_sort_hist_entries(uint32_t n);
 
 // ---- ray casts (ray.cu): launch helpers on caller-provided device buffers (no allocation) ----
-parrygpu_status launch_ray_keys(parrygpu_ctx* ctx, const float* d_rays, uint32_t n, uint32_t* bounds, uint32_t* keys, uint32_t* vals);
+// Key width (bits) of the ray ordering for the context's ray_sort_key mode.
+inline int ray_sort_bits(const parrygpu_ctx* ctx) { return ctx->cfg.ray_sort_key == 2 ? 16 : 30; }
+parrygpu_status launch_ray_keys(parrygpu_ctx* ctx, const float* d_rays, uint32_t n, uint32_t* bounds, uint32_t* keys, uint32_t* vals,
+                                uint32_t key_mode);
 parrygpu_status launch_trimesh_rays(parrygpu_ctx* ctx, const parrygpu_trimesh* mesh, const float* pose7_host, const float* d_rays,
-                                    const uint32_t* order, uint32_t n, float max_toi, uint32_t* d_feat, float* d_toi, float* d_nrm);
+                                    const uint32_t* order, uint32_t n, float max_toi, uint32_t* d_feat, float* d_toi, float* d_nrm,
+                                    uint32_t* counter);
 
 // ---- LBVH (lbvh.cu) ----
 // Builds `bvh` from `n` device AABBs (n x 6 floats). When leaf_data_is_position, leaf nodes store
@@ -167,9 +171,12 @@ parrygpu_status launch_self_pairs(parrygpu_ctx* ctx, const parrygpu_bvh* bvh, ui
 // permuted into that order), and writes its results to slot order[k].
 // Runs the wavefront cast (shape_ray.cu) with `scratch` sized by shape_rays_reserve(n) beforehand.
 parrygpu_status shape_rays_reserve(parrygpu_ctx* ctx, RayWaveScratch& scratch, uint32_t n);
+// Local vertex bounds of the convex shapes (2 float4 per shape) for the shape-set ray filter.
+parrygpu_status launch_hull_boxes(parrygpu_ctx* ctx, const uint32_t* types, const float* params, const float* pool, uint32_t n,
+                                  uint64_t n_vertices, float* box);
 parrygpu_status launch_shape_rays(parrygpu_ctx* ctx, const parrygpu_bvh* bvh, const uint32_t* types, const float* params,
-                                  const float* poses, const float* pool, const float* d_rays, const uint32_t* order, uint32_t n,
-                                  float max_toi, uint32_t* d_part, float* d_toi, float* d_nrm, RayWaveScratch& scratch);
+                                  const float* poses, const float* pool, const float* hull_box, const float* d_rays, const uint32_t* order,
+                                  uint32_t n, float max_toi, uint32_t* d_part, float* d_toi, float* d_nrm, RayWaveScratch& scratch);
 
 // ---- shapes (contact.cu) ----
 // World AABBs of a compound's parts (Shape::compute_aabb(pos)) into d_out (n x 6 floats).

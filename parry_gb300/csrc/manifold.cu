@@ -918,7 +918,7 @@ __global__ void __launch_bounds__(MF_EPA_THREADS) k_manifolds_epa(ShapeArrays sh
                                                                   const unsigned long long* __restrict__ qcount, uint32_t* __restrict__ ws_pool,
                                                                   unsigned long long* __restrict__ stats, uint32_t* __restrict__ err) {
   const uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x;
-  EpaWs ws{ws_pool + (size_t)(slot >> 5) * (EPA_WORDS * 32) + (slot & 31)};
+  EpaWs ws = epa_slot(ws_pool, slot);
   const unsigned long long total = *qcount;
   uint32_t iters = 0, calls = 0;
   for (unsigned long long e = slot; e < total; e += (unsigned long long)gridDim.x * blockDim.x) {
@@ -988,7 +988,7 @@ parrygpu_status pg::manifolds_reserve(parrygpu_ctx* ctx, uint64_t cap, MfScratch
   PG_CUDA(ctx, sc.counters.reserve(128));
   PG_CUDA(ctx, sc.bins.reserve((size_t)cap * MK_KINDS * 4));
   uint32_t epa_blocks = (uint32_t)(ctx->sm_count > 0 ? ctx->sm_count : 152) * 8;
-  PG_CUDA(ctx, sc.epa_ws.reserve((size_t)(epa_blocks * MF_EPA_THREADS / 32) * EPA_SLOT_GROUP_BYTES));
+  PG_CUDA(ctx, sc.epa_ws.reserve((size_t)epa_blocks * MF_EPA_THREADS * EPA_SLOT_BYTES));
   if (cap > sc.cap) sc.cap = cap;
   return PARRYGPU_OK;
 }

@@ -22,10 +22,10 @@ namespace {
 constexpr uint32_t NA_MAX = PARRYGPU_NOALLOC_MAX_RAYS;
 constexpr uint32_t NA_TILE = 2048;  // keys per radix-sort tile (sort.cu)
 constexpr uint32_t NA_HIST = ((NA_MAX + NA_TILE - 1) / NA_TILE) * 256;
-constexpr uint32_t NA_BOUNDS = 64;  // ray-origin bounds (6 words used), padded to 256 bytes
+constexpr uint32_t NA_BOUNDS = 64;  // ray-origin bounds (words 0-5) and the traversal's ray counter (word 32), 256 bytes
 constexpr size_t NA_WORDS = 4 * (size_t)NA_MAX + NA_HIST + NA_BOUNDS;
 
-// keys0 | vals0 | keys1 | vals1 | histogram | bounds
+// keys0 | vals0 | keys1 | vals1 | histogram | bounds + ray counter
 static __device__ __align__(256) uint32_t g_ray_scratch[NA_WORDS];
 
 constexpr int NA_MAX_DEVICES = 64;
@@ -97,10 +97,10 @@ extern "C" parrygpu_status parrygpu_trimesh_cast_rays_noalloc(parrygpu_ctx* ctx,
   if (ctx->cfg.sort_rays && n > 1) {
     // launch_ray_keys clears the bounds words first; every histogram entry the sort reads is
     // rewritten by its histogram pass, and the keys/values are fully written before use.
-    if ((s = launch_ray_keys(ctx, rays, n, bounds, k0, v0)) != PARRYGPU_OK) return s;
+    if ((s = launch_ray_keys(ctx, rays, n, bounds, k0, v0, ctx->cfg.ray_sort_key)) != PARRYGPU_OK) return s;
     int rb = 0;
-    if ((s = radix_sort_pairs_in(ctx, n, 30, k0, v0, k1, v1, hist, &rb)) != PARRYGPU_OK) return s;
+    if ((s = radix_sort_pairs_in(ctx, n, ray_sort_bits(ctx), k0, v0, k1, v1, hist, &rb)) != PARRYGPU_OK) return s;
     order = rb ? v1 : v0;
   }
-  return launch_trimesh_rays(ctx, mesh, pose_ptr, rays, order, n, max_toi, feature, toi, normal);
+  return launch_trimesh_rays(ctx, mesh, pose_ptr, rays, order, n, max_toi, feature, toi, normal, bounds + 32);
 }

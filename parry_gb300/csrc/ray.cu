@@ -109,14 +109,17 @@ __device__ __forceinline__ void load_tri(const float4* __restrict__ soup, uint32
   *orig = __float_as_uint(z.y);
 }
 
-template <bool HAS_POSE, bool WANT_NORMAL>
-__global__ void k_trimesh_rays(const WideNode* __restrict__ wide, const float4* __restrict__ soup, uint32_t n_tris,
-                               const float* __restrict__ rays, const uint32_t* __restrict__ order, uint32_t n, float max_toi,
-                               Pose pose, uint32_t* __restrict__ feat, float* __restrict__ toi_out, float* __restrict__ normal_out,
-                               uint32_t* __restrict__ err) {
-  uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= n) return;
-  uint32_t r = order ? order[k] : k;
+// Per-ray traversal state: the ray in mesh space and its best hit so far.
+struct RayState {
+  V3 o, dir, inv;
+  uint32_t zmask;
+  float best;
+  uint32_t best_orig, best_pos;
+  bool have;
+};
+
+template <bool HAS_POSE>
+__device__ __forceinline__ void ray_init(const float* __restrict__ rays, uint32_t r, float max_toi, const Pose& pose, RayState* st) {
   const float* rp = rays + 6 * (size_t)r;
   V3 o = v3(rp[0], rp[1], rp[2]);
   V3 dir = v3(rp[3], rp[4], rp[5]);
@@ -124,74 +127,73 @@ __global__ void k_trimesh_rays(const WideNode* __restrict__ wide, const float4* 
     o = pose_inv_point(pose, o);
     dir = pose_inv_rotate(pose, dir);
   }
-  uint32_t zmask = (dir.x == 0.0f ? 1u : 0u) | (dir.y == 0.0f ? 2u : 0u) | (dir.z == 0.0f ? 4u : 0u);
-  V3 inv = v3(dir.x != 0.0f ? 1.0f / dir.x : 0.0f, dir.y != 0.0f ? 1.0f / dir.y : 0.0f, dir.z != 0.0f ? 1.0f / dir.z : 0.0f);
+  st->o = o;
+  st->dir = dir;
+  st->zmask = (dir.x == 0.0f ? 1u : 0u) | (dir.y == 0.0f ? 2u : 0u) | (dir.z == 0.0f ? 4u : 0u);
+  st->inv = v3(dir.x != 0.0f ? 1.0f / dir.x : 0.0f, dir.y != 0.0f ? 1.0f / dir.y : 0.0f, dir.z != 0.0f ? 1.0f / dir.z : 0.0f);
+  st->best = max_toi;
+  st->best_orig = 0xffffffffu;
+  st->best_pos = 0xffffffffu;
+  st->have = false;
+}
 
-  float best = max_toi;
-  uint32_t best_orig = 0xffffffffu, best_pos = 0xffffffffu;
-  bool have = false;
+// Triangle::cast_local_ray_and_get_normal on soup triangle `pos` (accepts toi <= best); exact
+// toi ties keep the lowest original triangle index.
+__device__ __forceinline__ void ray_try_leaf(const float4* __restrict__ soup, uint32_t pos, RayState* st) {
+  V3 a, b, c;
+  uint32_t orig;
+  load_tri(soup, pos, &a, &b, &c, &orig);
+  TriHit h;
+  if (!ray_triangle_toi(a, b, c, st->o, st->dir, &h)) return;
+  if (!(h.toi <= st->best)) return;
+  if (h.toi < st->best || (st->have && h.toi == st->best && orig < st->best_orig)) {
+    st->best = h.toi; st->best_orig = orig; st->best_pos = pos; st->have = true;
+  }
+}
 
-  auto try_leaf = [&](uint32_t pos) {
-    V3 a, b, c;
-    uint32_t orig;
-    load_tri(soup, pos, &a, &b, &c, &orig);
-    TriHit h;
-    if (!ray_triangle_toi(a, b, c, o, dir, &h)) return;
-    if (!(h.toi <= best)) return;  // Triangle::cast_local_ray_and_get_normal: toi <= max_toi
-    if (h.toi < best || (have && h.toi == best && orig < best_orig)) {
-      best = h.toi; best_orig = orig; best_pos = pos; have = true;
-    }
-  };
-
-  WideNode root;
-  load_wide(wide, 0, &root);
-  if ((root.r.data & 0x3fffffffu) == 0u) {
-    // Partial root (single triangle), bvh_traverse.rs:354-362.
-    float s = slab(root.l.mins, root.l.maxs, o, inv, zmask, max_toi);
-    if (s < max_toi) try_leaf(root.l.children);
-  } else {
-    uint32_t stack[RAY_STACK];
-    int sp = 0;
-    WideNode w = root;
-    for (;;) {
-      float ls = slab(w.l.mins, w.l.maxs, o, inv, zmask, best);
-      float rs = slab(w.r.mins, w.r.maxs, o, inv, zmask, best);
-      const BvhNodeDev* nearn = &w.l;
-      const BvhNodeDev* farn = &w.r;
-      if (ls > rs) { float t = ls; ls = rs; rs = t; nearn = &w.r; farn = &w.l; }
-      uint32_t next = 0xffffffffu;
-      if (ls != FLT_MAX && (ls < best || (have && ls == best))) {
-        if ((nearn->data & 0x3fffffffu) == 1u) try_leaf(nearn->children);
-        else next = nearn->children;
-      }
-      if (rs != FLT_MAX && (rs < best || (have && rs == best))) {
-        if ((farn->data & 0x3fffffffu) == 1u) {
-          try_leaf(farn->children);
-        } else if (next != 0xffffffffu) {
-          if (sp >= RAY_STACK) { atomicOr(err, ERR_STACK_OVERFLOW); break; }
-          stack[sp++] = farn->children;
-        } else {
-          next = farn->children;
-        }
-      }
-      if (next == 0xffffffffu) {
-        if (sp == 0) break;
-        next = stack[--sp];
-      }
-      load_wide(wide, next, &w);
+// One traversal step at wide node `w`: both children's slab tests, leaf children tested at once,
+// the nearer internal child returned (the farther one pushed), or the next stack entry; returns
+// 0xffffffff when the traversal is over (or the stack overflowed, with the error flag raised).
+__device__ __forceinline__ uint32_t ray_step(const WideNode& w, const float4* __restrict__ soup, RayState* st, uint32_t* stack, int* sp,
+                                             uint32_t* __restrict__ err) {
+  float ls = slab(w.l.mins, w.l.maxs, st->o, st->inv, st->zmask, st->best);
+  float rs = slab(w.r.mins, w.r.maxs, st->o, st->inv, st->zmask, st->best);
+  const BvhNodeDev* nearn = &w.l;
+  const BvhNodeDev* farn = &w.r;
+  if (ls > rs) { float t = ls; ls = rs; rs = t; nearn = &w.r; farn = &w.l; }
+  uint32_t next = 0xffffffffu;
+  if (ls != FLT_MAX && (ls < st->best || (st->have && ls == st->best))) {
+    if ((nearn->data & 0x3fffffffu) == 1u) ray_try_leaf(soup, nearn->children, st);
+    else next = nearn->children;
+  }
+  if (rs != FLT_MAX && (rs < st->best || (st->have && rs == st->best))) {
+    if ((farn->data & 0x3fffffffu) == 1u) {
+      ray_try_leaf(soup, farn->children, st);
+    } else if (next != 0xffffffffu) {
+      if (*sp >= RAY_STACK) { atomicOr(err, ERR_STACK_OVERFLOW); return 0xffffffffu; }
+      stack[(*sp)++] = farn->children;
+    } else {
+      next = farn->children;
     }
   }
+  if (next == 0xffffffffu && *sp > 0) next = stack[--(*sp)];
+  return next;
+}
 
-  if (have) {
+// Writes ray r's answer (feature, toi, normal facing the origin) from its final state.
+template <bool HAS_POSE, bool WANT_NORMAL>
+__device__ __forceinline__ void ray_finish(const float4* __restrict__ soup, uint32_t n_tris, const Pose& pose, const RayState& st, uint32_t r,
+                                           uint32_t* __restrict__ feat, float* __restrict__ toi_out, float* __restrict__ normal_out) {
+  if (st.have) {
     V3 a, b, c;
     uint32_t orig;
-    load_tri(soup, best_pos, &a, &b, &c, &orig);
+    load_tri(soup, st.best_pos, &a, &b, &c, &orig);
     TriHit h;
-    ray_triangle_toi(a, b, c, o, dir, &h);
-    feat[r] = h.fid == 1u ? best_orig + n_tris : best_orig;
-    toi_out[r] = best;
+    ray_triangle_toi(a, b, c, st.o, st.dir, &h);
+    feat[r] = h.fid == 1u ? st.best_orig + n_tris : st.best_orig;
+    toi_out[r] = st.best;
     if (WANT_NORMAL) {
-      V3 nrm = ray_triangle_normal(a, b, c, o);
+      V3 nrm = ray_triangle_normal(a, b, c, st.o);
       if (HAS_POSE) nrm = pose_rotate(pose, nrm);
       normal_out[3 * (size_t)r + 0] = nrm.x;
       normal_out[3 * (size_t)r + 1] = nrm.y;
@@ -204,6 +206,86 @@ __global__ void k_trimesh_rays(const WideNode* __restrict__ wide, const float4* 
       normal_out[3 * (size_t)r + 0] = 0.0f;
       normal_out[3 * (size_t)r + 1] = 0.0f;
       normal_out[3 * (size_t)r + 2] = 0.0f;
+    }
+  }
+}
+
+// One ray per thread: the whole traversal of ray order[k] (or k) in thread k.
+template <bool HAS_POSE, bool WANT_NORMAL>
+__global__ void k_trimesh_rays(const WideNode* __restrict__ wide, const float4* __restrict__ soup, uint32_t n_tris,
+                               const float* __restrict__ rays, const uint32_t* __restrict__ order, uint32_t n, float max_toi,
+                               Pose pose, uint32_t* __restrict__ feat, float* __restrict__ toi_out, float* __restrict__ normal_out,
+                               uint32_t* __restrict__ err) {
+  uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  uint32_t r = order ? order[k] : k;
+  RayState st;
+  ray_init<HAS_POSE>(rays, r, max_toi, pose, &st);
+  WideNode w;
+  load_wide(wide, 0, &w);
+  if ((w.r.data & 0x3fffffffu) == 0u) {
+    // Partial root (single triangle), bvh_traverse.rs:354-362.
+    float s0 = slab(w.l.mins, w.l.maxs, st.o, st.inv, st.zmask, max_toi);
+    if (s0 < max_toi) ray_try_leaf(soup, w.l.children, &st);
+  } else {
+    uint32_t stack[RAY_STACK];
+    int sp = 0;
+    for (;;) {
+      uint32_t next = ray_step(w, soup, &st, stack, &sp, err);
+      if (next == 0xffffffffu) break;
+      load_wide(wide, next, &w);
+    }
+  }
+  ray_finish<HAS_POSE, WANT_NORMAL>(soup, n_tris, pose, st, r, feat, toi_out, normal_out);
+}
+
+// Persistent warps with dynamic ray fetch: every lane runs one traversal step per loop turn, and
+// once at least `refill` lanes of the warp have finished their rays, the warp takes that many new
+// ray slots from a global counter with one atomicAdd. Lanes whose rays end early pick up new rays
+// instead of idling until the warp's longest traversal ends. The per-ray work and answers are
+// those of k_trimesh_rays. Requires a non-leaf root (two or more triangles).
+template <bool HAS_POSE, bool WANT_NORMAL>
+__global__ void __launch_bounds__(128) k_trimesh_rays_fetch(const WideNode* __restrict__ wide, const float4* __restrict__ soup,
+                                                            uint32_t n_tris, const float* __restrict__ rays,
+                                                            const uint32_t* __restrict__ order, uint32_t n, float max_toi, Pose pose,
+                                                            uint32_t* __restrict__ feat, float* __restrict__ toi_out,
+                                                            float* __restrict__ normal_out, uint32_t* __restrict__ err,
+                                                            uint32_t* __restrict__ next_ray, uint32_t refill) {
+  const unsigned FULL = 0xffffffffu;
+  const uint32_t lane = threadIdx.x & 31u;
+  uint32_t stack[RAY_STACK];
+  int sp = 0;
+  bool active = false, exhausted = false;
+  uint32_t r = 0, cur = 0;
+  RayState st;
+  for (;;) {
+    const unsigned idle = __ballot_sync(FULL, !active);
+    const uint32_t n_idle = (uint32_t)__popc(idle);
+    if (!exhausted && n_idle >= refill) {  // warp-uniform
+      uint32_t base = 0;
+      if (lane == 0) base = atomicAdd(next_ray, n_idle);
+      base = __shfl_sync(FULL, base, 0);
+      if (base >= n || n - base <= n_idle) exhausted = true;
+      if (!active) {
+        uint32_t k = base + (uint32_t)__popc(idle & ((1u << lane) - 1u));
+        if (k < n) {
+          r = order ? order[k] : k;
+          ray_init<HAS_POSE>(rays, r, max_toi, pose, &st);
+          sp = 0;
+          cur = 0;
+          active = true;
+        }
+      }
+    }
+    if (__ballot_sync(FULL, active) == 0u) break;  // only once the counter is exhausted
+    if (active) {
+      WideNode w;
+      load_wide(wide, cur, &w);
+      cur = ray_step(w, soup, &st, stack, &sp, err);
+      if (cur == 0xffffffffu) {
+        ray_finish<HAS_POSE, WANT_NORMAL>(soup, n_tris, pose, st, r, feat, toi_out, normal_out);
+        active = false;
+      }
     }
   }
 }
@@ -291,6 +373,8 @@ __global__ void k_ray_keys(const float* __restrict__ rays, uint32_t n, const uin
     const float* d = rays + 6 * (size_t)i + 3;
     uint32_t oct = (d[0] < 0.0f ? 4u : 0u) | (d[1] < 0.0f ? 2u : 0u) | (d[2] < 0.0f ? 1u : 0u);
     key = (oct << 27) | (key >> 3);
+  } else if (key_mode == 2) {
+    key >>= 14;  // the top 16 bits of the Morton code: a two-pass sort
   }
   keys[i] = key;
   vals[i] = i;
@@ -400,24 +484,18 @@ parrygpu_status parrygpu_trimesh_cast_rays(parrygpu_ctx* ctx, const parrygpu_tri
       PG_LAUNCHED(ctx);
       int rb;
       KernelTimer kt(ctx, "ray_sort");
-      s = radix_sort_pairs(ctx, n, 30, &rb);
+      s = radix_sort_pairs(ctx, n, ray_sort_bits(ctx), &rb);
       kt.stop();
       if (s != PARRYGPU_OK) return s;
       order = ctx->sort_v[rb].as<uint32_t>();
     }
-    uint32_t bs = ctx->cfg.ray_block ? ctx->cfg.ray_block : 128;
-    const WideNode* w = mesh->bvh.wide.as<WideNode>();
-    const float4* soup = mesh->soup.as<float4>();
-#define PG_RAY_LAUNCH(P, N)                                                                                               \
-  k_trimesh_rays<P, N><<<div_up(n, bs), bs, 0, ctx->stream>>>(w, soup, mesh->n_triangles, (const float*)d_rays, order, n, \
-                                                              max_toi, pose, (uint32_t*)d_feat, (float*)d_toi,            \
-                                                              (float*)d_nrm, ctx->d_err)
+    PG_CUDA(ctx, ctx->misc.reserve(128));
+    float p7[7] = {pose.qi, pose.qj, pose.qk, pose.qw, pose.t.x, pose.t.y, pose.t.z};
     KernelTimer kt(ctx, "trimesh_rays");
-    if (has_pose) { if (d_nrm) PG_RAY_LAUNCH(true, true); else PG_RAY_LAUNCH(true, false); }
-    else { if (d_nrm) PG_RAY_LAUNCH(false, true); else PG_RAY_LAUNCH(false, false); }
-#undef PG_RAY_LAUNCH
+    s = launch_trimesh_rays(ctx, mesh, has_pose ? p7 : nullptr, (const float*)d_rays, order, n, max_toi, (uint32_t*)d_feat, (float*)d_toi,
+                            (float*)d_nrm, ctx->misc.as<uint32_t>() + 16);
     kt.stop();
-    PG_LAUNCHED(ctx);
+    if (s != PARRYGPU_OK) return s;
   }
   if (c_feat) PG_CUDA(ctx, cudaMemcpyAsync(feature, d_feat, (size_t)n * 4, cudaMemcpyDeviceToHost, ctx->stream));
   if (c_toi) PG_CUDA(ctx, cudaMemcpyAsync(toi, d_toi, (size_t)n * 4, cudaMemcpyDeviceToHost, ctx->stream));
@@ -430,31 +508,49 @@ parrygpu_status parrygpu_trimesh_cast_rays(parrygpu_ctx* ctx, const parrygpu_tri
 
 // Launches the ray-ordering keys (origin bounds into `bounds`, 6 words, then Morton keys) on
 // caller-provided device buffers. Allocates nothing.
-parrygpu_status launch_ray_keys(parrygpu_ctx* ctx, const float* d_rays, uint32_t n, uint32_t* bounds, uint32_t* keys, uint32_t* vals) {
+parrygpu_status launch_ray_keys(parrygpu_ctx* ctx, const float* d_rays, uint32_t n, uint32_t* bounds, uint32_t* keys, uint32_t* vals,
+                                uint32_t key_mode) {
   PG_CUDA(ctx, cudaMemsetAsync(bounds, 0xff, 12, ctx->stream));
   PG_CUDA(ctx, cudaMemsetAsync(bounds + 3, 0x00, 12, ctx->stream));
   k_ray_bounds<<<div_up(n, 256 * 8), 256, 0, ctx->stream>>>(d_rays, n, bounds);
   PG_LAUNCHED(ctx);
-  k_ray_keys<<<div_up(n, 256), 256, 0, ctx->stream>>>(d_rays, n, bounds, keys, vals, ctx->cfg.ray_sort_key);
+  k_ray_keys<<<div_up(n, 256), 256, 0, ctx->stream>>>(d_rays, n, bounds, keys, vals, key_mode);
   PG_LAUNCHED(ctx);
   return PARRYGPU_OK;
 }
 
-// Launches the traversal kernel on device buffers (order may be NULL). Allocates nothing.
+// Launches the traversal kernel of the context's configuration on device buffers (order may be
+// NULL; `counter` = one device word for the dynamic-fetch traversal's ray counter, zeroed here).
+// Allocates nothing.
 parrygpu_status launch_trimesh_rays(parrygpu_ctx* ctx, const parrygpu_trimesh* mesh, const float* pose7_host, const float* d_rays,
-                                    const uint32_t* order, uint32_t n, float max_toi, uint32_t* d_feat, float* d_toi, float* d_nrm) {
+                                    const uint32_t* order, uint32_t n, float max_toi, uint32_t* d_feat, float* d_toi, float* d_nrm,
+                                    uint32_t* counter) {
   Pose pose{0.f, 0.f, 0.f, 1.f, v3(0.f, 0.f, 0.f)};
   bool has_pose = pose7_host != nullptr;
   if (has_pose) pose = Pose{pose7_host[0], pose7_host[1], pose7_host[2], pose7_host[3], v3(pose7_host[4], pose7_host[5], pose7_host[6])};
-  uint32_t bs = ctx->cfg.ray_block ? ctx->cfg.ray_block : 128;
   const WideNode* w = mesh->bvh.wide.as<WideNode>();
   const float4* soup = mesh->soup.as<float4>();
-#define PG_RAY_LAUNCH2(P, N)                                                                                                   \
-  k_trimesh_rays<P, N><<<div_up(n, bs), bs, 0, ctx->stream>>>(w, soup, mesh->n_triangles, d_rays, order, n, max_toi, pose, d_feat, \
-                                                              d_toi, d_nrm, ctx->d_err)
-  if (has_pose) { if (d_nrm) PG_RAY_LAUNCH2(true, true); else PG_RAY_LAUNCH2(true, false); }
-  else { if (d_nrm) PG_RAY_LAUNCH2(false, true); else PG_RAY_LAUNCH2(false, false); }
-#undef PG_RAY_LAUNCH2
+  // the fetch traversal needs an internal root (two or more triangles) and headroom in its counter
+  if (ctx->cfg.ray_traversal == 2 && mesh->n_triangles >= 2 && n <= 0xF0000000u) {
+    uint32_t refill = ctx->cfg.ray_refill ? ctx->cfg.ray_refill : 16;
+    auto kern = has_pose ? (d_nrm ? k_trimesh_rays_fetch<true, true> : k_trimesh_rays_fetch<true, false>)
+                         : (d_nrm ? k_trimesh_rays_fetch<false, true> : k_trimesh_rays_fetch<false, false>);
+    int per_sm = 0;
+    PG_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 128, 0));
+    if (per_sm < 1) per_sm = 1;
+    uint32_t blocks = (uint32_t)(ctx->sm_count > 0 ? ctx->sm_count : 152) * (uint32_t)per_sm;
+    uint32_t need = div_up(n, 128);
+    if (blocks > need) blocks = need;
+    PG_CUDA(ctx, cudaMemsetAsync(counter, 0, 4, ctx->stream));
+    kern<<<blocks, 128, 0, ctx->stream>>>(w, soup, mesh->n_triangles, d_rays, order, n, max_toi, pose, d_feat, d_toi, d_nrm, ctx->d_err,
+                                          counter, refill);
+    PG_LAUNCHED(ctx);
+    return PARRYGPU_OK;
+  }
+  uint32_t bs = ctx->cfg.ray_block ? ctx->cfg.ray_block : 128;
+  auto kern = has_pose ? (d_nrm ? k_trimesh_rays<true, true> : k_trimesh_rays<true, false>)
+                       : (d_nrm ? k_trimesh_rays<false, true> : k_trimesh_rays<false, false>);
+  kern<<<div_up(n, bs), bs, 0, ctx->stream>>>(w, soup, mesh->n_triangles, d_rays, order, n, max_toi, pose, d_feat, d_toi, d_nrm, ctx->d_err);
   PG_LAUNCHED(ctx);
   return PARRYGPU_OK;
 }

@@ -24,7 +24,7 @@ using namespace pg;
 struct parrygpu_scene {
   uint64_t n = 0, n_vertices = 0, cap = 0, table_size = 0, n_rays = 0;
   float prediction = 0.0f, max_toi = 0.0f;
-  DevBuf types, params, poses, vel, pool, aabbs, poly[9];
+  DevBuf types, params, poses, vel, pool, aabbs, hull_box, poly[9];
   parrygpu_polyhedra poly_counts{};
   bool has_poly = false;
   parrygpu_bvh bvh;
@@ -213,7 +213,7 @@ static parrygpu_status scene_frame(parrygpu_ctx* ctx, parrygpu_scene* sc, float 
   if (sc->n_rays) {
     KernelTimer kt(ctx, "scene_rays");
     if ((s = launch_shape_rays(ctx, &sc->bvh, sc->types.as<uint32_t>(), sc->params.as<float>(), sc->poses.as<float>(), sc->pool.as<float>(),
-                               sc->rays.as<float>(), sc->ray_order.as<uint32_t>(), (uint32_t)sc->n_rays, sc->max_toi,
+                               sc->hull_box.as<float>(), sc->rays.as<float>(), sc->ray_order.as<uint32_t>(), (uint32_t)sc->n_rays, sc->max_toi,
                                sc->ray_part.as<uint32_t>(), sc->ray_toi.as<float>(), sc->ray_nrm.as<float>(), sc->ray_wave)) !=
         PARRYGPU_OK)
       return s;
@@ -313,6 +313,10 @@ parrygpu_status parrygpu_scene_create(parrygpu_ctx* ctx, const parrygpu_shapes* 
       if ((s = copy_in(ctx, sc->poly[k], src[k], bytes[k])) != PARRYGPU_OK) return fail(s);
   }
   PG_CUDA(ctx, sc->aabbs.reserve(sc->n * 24));
+  PG_CUDA(ctx, sc->hull_box.reserve(sc->n * 32));
+  if ((s = launch_hull_boxes(ctx, sc->types.as<uint32_t>(), sc->params.as<float>(), sc->pool.as<float>(), (uint32_t)sc->n, sc->n_vertices,
+                             sc->hull_box.as<float>())) != PARRYGPU_OK)
+    return fail(s);
   for (int b = 0; b < 2; ++b) {
     PG_CUDA(ctx, sc->pairs[b].reserve(pair_capacity * 8));
     PG_CUDA(ctx, sc->recs[b].reserve(pair_capacity * (size_t)REC_WORDS * 4));
@@ -335,7 +339,7 @@ void parrygpu_scene_destroy(parrygpu_scene* sc) {
   if (!sc) return;
   cudaDeviceSynchronize();  // frames in flight still read the scene's buffers
   drop_graph(sc);
-  for (DevBuf* d : {&sc->types, &sc->params, &sc->poses, &sc->vel, &sc->pool, &sc->aabbs, &sc->counts, &sc->mf.queue, &sc->mf.counters,
+  for (DevBuf* d : {&sc->types, &sc->params, &sc->poses, &sc->vel, &sc->pool, &sc->aabbs, &sc->hull_box, &sc->counts, &sc->mf.queue, &sc->mf.counters,
                     &sc->mf.epa_ws, &sc->mf.bins, &sc->rays, &sc->ray_order, &sc->ray_part,
                     &sc->ray_toi, &sc->ray_nrm, &sc->bvh.wide, &sc->bvh.leaf_parent, &sc->bvh.node_parent, &sc->bvh.leaf_index,
                     &sc->bvh.flags, &sc->bvh.root_aabb, &sc->bvh.info})
@@ -369,7 +373,7 @@ parrygpu_status parrygpu_scene_set_rays(parrygpu_ctx* ctx, parrygpu_scene* sc, c
     if ((s = radix_sort_reserve(ctx, n)) != PARRYGPU_OK) { tmp.release(); return s; }
     PG_CUDA(ctx, ctx->misc.reserve(64));
     uint32_t* bounds = ctx->misc.as<uint32_t>() + 8;
-    if ((s = launch_ray_keys(ctx, tmp.as<float>(), n, bounds, ctx->sort_k[0].as<uint32_t>(), ctx->sort_v[0].as<uint32_t>())) !=
+    if ((s = launch_ray_keys(ctx, tmp.as<float>(), n, bounds, ctx->sort_k[0].as<uint32_t>(), ctx->sort_v[0].as<uint32_t>(), 0u)) !=
         PARRYGPU_OK) {
       tmp.release();
       return s;

@@ -14,6 +14,8 @@
 #include "gjk_device.cuh"
 #include "lbvh_device.cuh"
 
+#include <cooperative_groups.h>
+
 using namespace pg;
 
 namespace {
@@ -267,7 +269,75 @@ struct CompoundDev {
   const float4* params;
   const float* poses;
   const float* pool;
+  const float4* hull_box;  // per shape: local vertex bounds of a convex hull (min, max); may be null
 };
+
+// Local vertex bounds of every convex shape (one thread per shape); other shapes and invalid
+// vertex ranges get an unbounded box, which filters nothing.
+__global__ void k_hull_local_boxes(const uint32_t* __restrict__ types, const float4* __restrict__ params, const float* __restrict__ pool,
+                                   uint32_t n, uint64_t n_vertices, float4* __restrict__ box) {
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  float4 lo = make_float4(-FLT_MAX, -FLT_MAX, -FLT_MAX, 0.f), hi = make_float4(FLT_MAX, FLT_MAX, FLT_MAX, 0.f);
+  if (types[i] == SH_CONVEX) {
+    float4 p = params[i];
+    uint64_t first = __float_as_uint(p.x), count = __float_as_uint(p.y);
+    if (count > 0 && first + count <= n_vertices) {
+      const float* v = pool + 3 * first;
+      lo = make_float4(v[0], v[1], v[2], 0.f);
+      hi = lo;
+      for (uint64_t k = 1; k < count; ++k) {
+        float x = v[3 * k], y = v[3 * k + 1], z = v[3 * k + 2];
+        lo.x = fminf(lo.x, x); lo.y = fminf(lo.y, y); lo.z = fminf(lo.z, z);
+        hi.x = fmaxf(hi.x, x); hi.y = fmaxf(hi.y, y); hi.z = fmaxf(hi.z, z);
+      }
+    }
+  }
+  box[2 * (size_t)i] = lo;
+  box[2 * (size_t)i + 1] = hi;
+}
+
+// Conservative pre-test of a capsule / hull candidate: can the ray (world o, dir) reach the shape's
+// local box (capsule: its exact bounds; hull: its vertex bounds), inflated by a margin far above
+// the rounding of the transform and of the GJK ray cast, before `tlim`? A false answer proves the
+// GJK ray cast cannot return a hit at toi <= tlim, so the candidate is dropped without changing any
+// answer. *t_in receives a lower bound of the entry time.
+__device__ __forceinline__ bool local_box_may_hit(const CompoundDev& cd, uint32_t part, uint32_t ty, V3 o, V3 dir, float tlim, float* t_in) {
+  float3 lo, hi;
+  float4 prm = cd.params[part];
+  if (ty == SH_CAPSULE) {
+    lo = make_float3(-prm.y, -prm.x - prm.y, -prm.y);
+    hi = make_float3(prm.y, prm.x + prm.y, prm.y);
+  } else if (cd.hull_box) {
+    float4 a = cd.hull_box[2 * (size_t)part], b = cd.hull_box[2 * (size_t)part + 1];
+    lo = make_float3(a.x, a.y, a.z);
+    hi = make_float3(b.x, b.y, b.z);
+  } else {
+    *t_in = 0.0f;
+    return true;
+  }
+  Pose p = load_pose(cd.poses, part);
+  V3 ol = pose_inv_point(p, o), dl = pose_inv_rotate(p, dir);
+  float ext = fmaxf(fmaxf(fmaxf(fabsf(lo.x), fabsf(hi.x)), fmaxf(fabsf(lo.y), fabsf(hi.y))), fmaxf(fabsf(lo.z), fabsf(hi.z)));
+  float m = 1e-4f * (1.0f + ext + fmaxf(fmaxf(fabsf(ol.x), fabsf(ol.y)), fabsf(ol.z)));
+  if (!(ext < 1e30f)) { *t_in = 0.0f; return true; }  // unbounded box: no filter
+  float tmin = 0.0f, tmax = tlim + fabsf(tlim) * 1e-5f;
+  const float oo[3] = {ol.x, ol.y, ol.z}, dd[3] = {dl.x, dl.y, dl.z};
+  const float lov[3] = {lo.x - m, lo.y - m, lo.z - m}, hiv[3] = {hi.x + m, hi.y + m, hi.z + m};
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    if (fabsf(dd[i]) < 1e-30f) {
+      if (oo[i] < lov[i] || oo[i] > hiv[i]) return false;
+    } else {
+      float a = (lov[i] - oo[i]) / dd[i], b = (hiv[i] - oo[i]) / dd[i];
+      if (a > b) { float t = a; a = b; b = t; }
+      tmin = fmaxf(tmin, a);
+      tmax = fminf(tmax, b);
+    }
+  }
+  *t_in = tmin;
+  return tmin <= tmax;
+}
 
 // Thread k handles ray r = order[k] (order may be null: r = k), read from slot k when the rays were
 // already permuted into that order (rays_permuted), else from slot r; results go to slot r.
@@ -348,7 +418,8 @@ __global__ void __launch_bounds__(128) k_compound_rays(const WideNode* __restric
 //   k_rays_wave     traversal + the analytic leaves (balls, cuboids, triangles) in few registers.
 //                   A support-map leaf (capsule, hull) whose box the ray enters before the best
 //                   analytic hit becomes a candidate with its box entry time: the ray's nearest
-//                   candidate goes to its own slot of list A, the others to the shared list B.
+//                   candidate goes to list A, the others to list B (both compacted by
+//                   warp-aggregated appends, so the GJK kernels run on dense lists).
 //                   The ray's best hit so far is published as the 64-bit key (toi bits, index).
 //   k_rays_cand     GJK ray casts (their toi does not depend on the max_toi bound, which only
 //                   accepts or rejects) for list A, then for list B skipping candidates whose box
@@ -394,13 +465,22 @@ __device__ __forceinline__ void ray_of(const float* rays, const uint32_t* order,
 }
 
 struct WaveBufs {
-  RayCand* a;            // one slot per ray (index k)
-  RayCand* b;            // shared list
+  RayCand* a;            // nearest candidate of each ray that has one (capacity n)
+  RayCand* b;            // the other candidates (capacity cap)
   unsigned long long cap;
-  unsigned long long* count;
+  unsigned long long* count;    // [0] list B length, [1] list A length
   unsigned long long* keys;  // per ray (index r)
   uint8_t* ovf;              // per ray (index r)
 };
+
+// Appends one slot per calling thread to a list: one atomicAdd per group of converged threads.
+__device__ __forceinline__ unsigned long long append_slot(unsigned long long* counter) {
+  namespace cg = cooperative_groups;
+  cg::coalesced_group g = cg::coalesced_threads();
+  unsigned long long base = 0;
+  if (g.thread_rank() == 0) base = atomicAdd(counter, (unsigned long long)g.size());
+  return g.shfl(base, 0) + g.thread_rank();
+}
 
 __global__ void __launch_bounds__(128) k_rays_wave(const WideNode* __restrict__ wide, CompoundDev cd, const float* __restrict__ rays, uint32_t n,
                                                    float max_toi, int solid, int has_pose, Pose cpose, uint32_t* __restrict__ part_out,
@@ -420,13 +500,16 @@ __global__ void __launch_bounds__(128) k_rays_wave(const WideNode* __restrict__ 
   uint32_t near_part = 0xffffffffu;
   float near_tmin = FLT_MAX;
   auto defer = [&](uint32_t part, float tmin) {
-    unsigned long long slot = atomicAdd(wb.count, 1ull);
+    unsigned long long slot = append_slot(wb.count);
     if (slot < wb.cap) wb.b[slot] = RayCand{k, r, part, 0u, tmin, 0.f, 0.f, 0.f, 0.f, 0.f};
     else overflow = true;
   };
   auto visit_leaf = [&](uint32_t part, float tmin) {
     uint32_t ty = cd.types[part];
     if (!analytic_type(ty)) {
+      float t_box;
+      if (!local_box_may_hit(cd, part, ty, o, dir, best, &t_box)) return;
+      tmin = fmaxf(tmin, t_box);
       if (tmin < near_tmin) {
         if (near_part != 0xffffffffu) defer(near_part, near_tmin);
         near_part = part;
@@ -477,7 +560,7 @@ __global__ void __launch_bounds__(128) k_rays_wave(const WideNode* __restrict__ 
       load_wide(wide, next, &w);
     }
   }
-  wb.a[k] = RayCand{k, r, near_part, 0u, near_tmin, 0.f, 0.f, 0.f, 0.f, 0.f};
+  if (near_part != 0xffffffffu) wb.a[append_slot(wb.count + 1)] = RayCand{k, r, near_part, 0u, near_tmin, 0.f, 0.f, 0.f, 0.f, 0.f};
   wb.keys[r] = have ? hit_key(best, best_part) : ~0ull;
   wb.ovf[r] = overflow ? 1 : 0;
   if (has_pose && have) best_n = pose_rotate(cpose, best_n);
@@ -514,7 +597,7 @@ __device__ __forceinline__ void run_candidate(const CompoundDev& cd, const float
   atomicMin(&keys[r], hit_key(t, c.part));
 }
 
-// List A (one entry per ray, grid over the rays) or list B (grid-stride over min(cap, *count)).
+// Grid-stride over min(n, *count) entries of list A or list B.
 __global__ void __launch_bounds__(128) k_rays_cand(CompoundDev cd, const float* __restrict__ rays, float max_toi, int solid, int has_pose,
                                                    Pose cpose, const uint32_t* __restrict__ order, int permuted, RayCand* __restrict__ list,
                                                    unsigned long long n, const unsigned long long* __restrict__ count,
@@ -570,16 +653,15 @@ static parrygpu_status launch_wave(parrygpu_ctx* ctx, const WideNode* wide, Comp
   unsigned long long* cnt = sc.counter.as<unsigned long long>();
   WaveBufs wb{sc.cands.as<RayCand>(), sc.cands.as<RayCand>() + n, sc.cap, cnt, sc.keys.as<unsigned long long>(), sc.ovf.as<uint8_t>()};
   uint32_t grid = (uint32_t)(ctx->sm_count > 0 ? ctx->sm_count : 152) * 16;
-  PG_CUDA(ctx, cudaMemsetAsync(cnt, 0, 8, ctx->stream));
+  PG_CUDA(ctx, cudaMemsetAsync(cnt, 0, 16, ctx->stream));
   k_rays_wave<<<div_up(n, 128), 128, 0, ctx->stream>>>(wide, cd, d_rays, n, max_toi, solid, has_pose, pose, d_part, d_toi, d_nrm, ctx->d_err,
                                                        order, permuted, wb);
   PG_LAUNCHED(ctx);
-  k_rays_cand<<<div_up(n, 128), 128, 0, ctx->stream>>>(cd, d_rays, max_toi, solid, has_pose, pose, order, permuted, wb.a, n, nullptr,
-                                                       wb.keys);
+  k_rays_cand<<<grid, 128, 0, ctx->stream>>>(cd, d_rays, max_toi, solid, has_pose, pose, order, permuted, wb.a, n, cnt + 1, wb.keys);
   PG_LAUNCHED(ctx);
   k_rays_cand<<<grid, 128, 0, ctx->stream>>>(cd, d_rays, max_toi, solid, has_pose, pose, order, permuted, wb.b, sc.cap, cnt, wb.keys);
   PG_LAUNCHED(ctx);
-  k_rays_finish<<<grid, 128, 0, ctx->stream>>>(wb.a, n, nullptr, wb.keys, d_part, d_toi, d_nrm);
+  k_rays_finish<<<grid, 128, 0, ctx->stream>>>(wb.a, n, cnt + 1, wb.keys, d_part, d_toi, d_nrm);
   PG_LAUNCHED(ctx);
   k_rays_finish<<<grid, 128, 0, ctx->stream>>>(wb.b, sc.cap, cnt, wb.keys, d_part, d_toi, d_nrm);
   PG_LAUNCHED(ctx);
@@ -590,11 +672,19 @@ static parrygpu_status launch_wave(parrygpu_ctx* ctx, const WideNode* wide, Comp
   return PARRYGPU_OK;
 }
 
+parrygpu_status launch_hull_boxes(parrygpu_ctx* ctx, const uint32_t* types, const float* params, const float* pool, uint32_t n,
+                                  uint64_t n_vertices, float* box) {
+  if (n == 0) return PARRYGPU_OK;
+  k_hull_local_boxes<<<div_up(n, 256), 256, 0, ctx->stream>>>(types, (const float4*)params, pool, n, n_vertices, (float4*)box);
+  PG_LAUNCHED(ctx);
+  return PARRYGPU_OK;
+}
+
 parrygpu_status launch_shape_rays(parrygpu_ctx* ctx, const parrygpu_bvh* bvh, const uint32_t* types, const float* params,
-                                  const float* poses, const float* pool, const float* d_rays, const uint32_t* order, uint32_t n,
-                                  float max_toi, uint32_t* d_part, float* d_toi, float* d_nrm, RayWaveScratch& scratch) {
+                                  const float* poses, const float* pool, const float* hull_box, const float* d_rays, const uint32_t* order,
+                                  uint32_t n, float max_toi, uint32_t* d_part, float* d_toi, float* d_nrm, RayWaveScratch& scratch) {
   if (n == 0 || bvh->n_leaves == 0) return PARRYGPU_OK;
-  CompoundDev cd{types, (const float4*)params, poses, pool};
+  CompoundDev cd{types, (const float4*)params, poses, pool, (const float4*)hull_box};
   Pose pose{0.f, 0.f, 0.f, 1.f, v3(0.f, 0.f, 0.f)};
   return launch_wave(ctx, bvh->wide.as<WideNode>(), cd, d_rays, order, order ? 1 : 0, n, max_toi, 1, 0, pose, d_part, d_toi, d_nrm, scratch);
 }
@@ -620,6 +710,9 @@ parrygpu_status parrygpu_compound_create(parrygpu_ctx* ctx, const parrygpu_shape
   }
   if (c->n > 0) {
     if ((s = check_cuda(ctx, c->aabbs.reserve(c->n * 24), "compound aabbs")) != PARRYGPU_OK ||
+        (s = check_cuda(ctx, c->hull_box.reserve(c->n * 32), "compound hull boxes")) != PARRYGPU_OK ||
+        (s = launch_hull_boxes(ctx, c->types.as<uint32_t>(), c->params.as<float>(), c->pool.as<float>(), (uint32_t)c->n, c->n_vertices,
+                               c->hull_box.as<float>())) != PARRYGPU_OK ||
         (s = compound_part_aabbs(ctx, c, c->aabbs.as<float>())) != PARRYGPU_OK ||
         (s = lbvh_build(ctx, &c->bvh, c->aabbs.as<float>(), (uint32_t)c->n, false)) != PARRYGPU_OK) {
       parrygpu_compound_destroy(c);
@@ -637,7 +730,7 @@ parrygpu_status parrygpu_compound_create(parrygpu_ctx* ctx, const parrygpu_shape
 
 void parrygpu_compound_destroy(parrygpu_compound* c) {
   if (!c) return;
-  for (DevBuf* d : {&c->types, &c->params, &c->poses, &c->pool, &c->aabbs, &c->bvh.wide, &c->bvh.leaf_parent, &c->bvh.node_parent,
+  for (DevBuf* d : {&c->types, &c->params, &c->poses, &c->pool, &c->aabbs, &c->hull_box, &c->bvh.wide, &c->bvh.leaf_parent, &c->bvh.node_parent,
                     &c->bvh.leaf_index, &c->bvh.flags, &c->bvh.root_aabb, &c->bvh.info})
     d->release();
   delete c;
@@ -683,17 +776,17 @@ parrygpu_status parrygpu_compound_cast_rays(parrygpu_ctx* ctx, const parrygpu_co
     PG_CUDA(ctx, cudaMemsetAsync(d_toi, 0, (size_t)n * 4, ctx->stream));
     if (d_nrm) PG_CUDA(ctx, cudaMemsetAsync(d_nrm, 0, (size_t)n * 12, ctx->stream));
   } else {
-    CompoundDev cd{c->types.as<uint32_t>(), c->params.as<float4>(), c->poses.as<float>(), c->pool.as<float>()};
+    CompoundDev cd{c->types.as<uint32_t>(), c->params.as<float4>(), c->poses.as<float>(), c->pool.as<float>(), c->hull_box.as<float4>()};
     const uint32_t* order = nullptr;
     if (ctx->cfg.sort_rays && n > 4096) {  // Morton order of the origins: coherent traversal
       if ((s = radix_sort_reserve(ctx, n)) != PARRYGPU_OK) return s;
       PG_CUDA(ctx, ctx->misc.reserve(64));
       uint32_t* bounds = ctx->misc.as<uint32_t>() + 8;
-      if ((s = launch_ray_keys(ctx, (const float*)d_rays, n, bounds, ctx->sort_k[0].as<uint32_t>(), ctx->sort_v[0].as<uint32_t>())) !=
-          PARRYGPU_OK)
+      if ((s = launch_ray_keys(ctx, (const float*)d_rays, n, bounds, ctx->sort_k[0].as<uint32_t>(), ctx->sort_v[0].as<uint32_t>(),
+                               ctx->cfg.ray_sort_key)) != PARRYGPU_OK)
         return s;
       int rb;
-      if ((s = radix_sort_pairs(ctx, n, 30, &rb)) != PARRYGPU_OK) return s;
+      if ((s = radix_sort_pairs(ctx, n, ray_sort_bits(ctx), &rb)) != PARRYGPU_OK) return s;
       order = ctx->sort_v[rb].as<uint32_t>();
     }
     if ((s = shape_rays_reserve(ctx, ctx->ray_wave, n)) != PARRYGPU_OK) return s;

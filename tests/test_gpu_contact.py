@@ -108,3 +108,14 @@ def test_broadphase_pipeline(gpu_ctx, oracle_lib):
     ho, oo, _ = oracle_lib.contacts(s, pairs, 0.1)
     _compare(has, out, ho, oo, "broadphase contacts")
     print(f"\n{len(pairs)} candidate pairs, {int(ho.sum())} contacts")
+
+
+def test_autotune_contacts_keeps_answers(oracle_lib):
+    ctx = pg.Context(0)
+    s, pairs = W.hull_pairs(8192, seed=17)
+    cfg = pg.autotune_contacts(ctx, s, pairs, 0.0, reps=1)
+    assert cfg["epa_blocks_per_sm"] in (4, 6, 8, 12, 16) and ctx.config == cfg
+    has, out = pg.contacts(ctx, s, pairs, 0.0)
+    ho, oo, _ = oracle_lib.contacts(s, pairs, 0.0)
+    _compare(has, out, ho, oo, "after autotune")
+    ctx.close()

@@ -40,9 +40,10 @@ def test_golden_fixture(gpu_ctx):
     _compare(f, t, n, g["feature_f32"], g["toi_f32"], g["normal_f32"])
 
 
-@pytest.mark.parametrize("sort_rays", [True, False])
-def test_medium_terrain_vs_oracle(oracle_lib, sort_rays):
-    ctx = pg.Context(0, sort_rays=sort_rays)
+@pytest.mark.parametrize("sort_rays,key,traversal,refill", [(True, 0, 1, 0), (True, 1, 1, 0), (True, 2, 1, 0), (False, 0, 1, 0),
+                                                        (False, 0, 2, 8), (True, 0, 2, 16), (False, 0, 2, 32), (True, 2, 2, 1)])
+def test_medium_terrain_vs_oracle(oracle_lib, sort_rays, key, traversal, refill):
+    ctx = pg.Context(0, sort_rays=sort_rays, ray_sort_key=key, ray_traversal=traversal, ray_refill=refill)
     v, i = W.terrain_mesh(64, 32, seed=21)
     rays = W.terrain_rays(200_000, 64, 32, seed=21)
     m = pg.TriMesh(ctx, v, i)
@@ -85,6 +86,30 @@ def test_pose_and_cast_ray_variant(gpu_ctx, oracle_lib):
     np.testing.assert_array_equal(t2, t)
 
 
+def test_fetch_traversal_full_size_pose_and_no_normal(oracle_lib):
+    """The persistent dynamic-fetch traversal on the full terrain workload, with a mesh pose, and
+    through the toi-only variant, answers as the oracle."""
+    ctx = pg.Context(0, ray_traversal=2)
+    v, i = W.terrain_mesh()
+    rays = W.terrain_rays(1 << 20, seed=77)
+    m = pg.TriMesh(ctx, v, i)
+    f, t, n = m.cast_rays_and_get_normal(rays, 100.0)
+    om = oracle_lib.TriMesh(v, i)
+    fo, to, no = om.cast_rays_and_get_normal(rays, 100.0)
+    _compare(f, t, n, fo, to, no)
+    q = np.array([0.05, -0.1, 0.02, 0.99], np.float64)
+    q /= np.linalg.norm(q)
+    pose = np.array(list(q) + [1.0, 0.5, -2.0], np.float32)
+    sub = rays[:200_000]
+    f, t, n = m.cast_rays_and_get_normal(sub, 100.0, pose=pose)
+    fo, to, no = om.cast_rays_and_get_normal(sub, 100.0, pose=pose)
+    _compare(f, t, n, fo, to, no)
+    f2, t2 = m.cast_rays(sub, 100.0, pose=pose)
+    np.testing.assert_array_equal(f2, f)
+    np.testing.assert_array_equal(t2, t)
+    ctx.close()
+
+
 def test_device_and_pinned_buffers(gpu_ctx, oracle_lib):
     import torch
     v, i = W.terrain_mesh(32, 16, seed=8)
@@ -115,3 +140,30 @@ def test_edge_cases(gpu_ctx):
     # out-of-range index is rejected
     with pytest.raises(pg.ParryGpuError):
         pg.TriMesh(gpu_ctx, np.zeros((3, 3), np.float32), np.array([[0, 1, 5]], np.uint32))
+
+
+def test_autotune_keeps_answers(oracle_lib):
+    """The autotuner picks one of its candidates, installs it in the context, and the answers
+    after tuning are the oracle's."""
+    ctx = pg.Context(0)
+    v, i = W.terrain_mesh(64, 32, seed=5)
+    rays = W.terrain_rays(100_000, 64, 32, seed=5)
+    m = pg.TriMesh(ctx, v, i)
+    cfg = m.autotune(rays, 100.0, reps=1)
+    assert cfg["ray_sort_key"] in (0, 1, 2) and cfg["ray_traversal"] in (1, 2)
+    if cfg["ray_traversal"] == 1:
+        assert cfg["ray_block"] in (64, 128, 256)
+    else:
+        assert cfg["ray_refill"] in (8, 16, 24)
+    assert ctx.config == cfg
+    f, t, n = m.cast_rays_and_get_normal(rays, 100.0)
+    fo, to, no = oracle_lib.TriMesh(v, i).cast_rays_and_get_normal(rays, 100.0)
+    _compare(f, t, n, fo, to, no)
+    ctx.close()
+
+
+@pytest.mark.parametrize("kw", [{"ray_block": 48}, {"ray_block": 2048}, {"ray_sort_key": 3}, {"epa_blocks_per_sm": 64},
+                                {"ray_traversal": 3}, {"ray_refill": 33}])
+def test_invalid_config_rejected(kw):
+    with pytest.raises(Exception):
+        pg.Context(0, **kw)

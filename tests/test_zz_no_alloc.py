@@ -27,7 +27,8 @@ def _cast(fn, ctx, mesh, rays, torch):
     return st, feat, toi, nrm
 
 
-def test_noalloc_matches_existing_entry_point_on_two_calls():
+@pytest.mark.parametrize("traversal", [1, 2])
+def test_noalloc_matches_existing_entry_point_on_two_calls(traversal):
     torch = pytest.importorskip("torch")
     from parry_gb300 import _build
     _build.build()
@@ -35,7 +36,7 @@ def test_noalloc_matches_existing_entry_point_on_two_calls():
     from parry_gb300 import workloads as W
 
     lib = pg.lib()
-    ctx = pg.Context(device=0)
+    ctx = pg.Context(device=0, ray_traversal=traversal)
     try:
         v, i = W.terrain_mesh(64, 32, seed=31)
         mesh = pg.TriMesh(ctx, v, i)
