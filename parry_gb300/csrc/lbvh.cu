@@ -2,7 +2,7 @@
 //
 // Build pipeline (one CUDA stream, no host round trip):
 //   k_centroid_bounds  centroid bounds of the leaf AABBs (warp-reduced, order-preserving atomics)
-//   k_morton           30-bit Morton code of each normalised centroid, value = leaf index
+//   k_morton           30-bit Morton code of each centroid on a cubic grid over the centroid bounds, value = leaf index
 //   radix_sort_pairs   stable device radix sort (sort.cu); equal codes keep leaf-index order
 //   k_karras           Karras (2012) hierarchy: internal node i owns wide node i, root = wide 0,
 //                      exactly the reference's "root is BvhNodeWide 0" convention
@@ -53,13 +53,17 @@ __global__ void k_morton(const float* __restrict__ aabbs, uint32_t n, const uint
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const float* a = aabbs + 6 * (size_t)i;
+  // One scale for all axes (the longest centroid extent): the Morton grid cells are cubes, so a
+  // flat set (a height field, a floor) is split along its long axes first instead of spending a
+  // third of the hierarchy on its thin one.
+  float ext = 0.0f;
+#pragma unroll
+  for (int d = 0; d < 3; ++d) ext = fmaxf(ext, float_unflip(bounds[3 + d]) - float_unflip(bounds[d]));
   float u[3];
 #pragma unroll
   for (int d = 0; d < 3; ++d) {
-    float lo = float_unflip(bounds[d]), hi = float_unflip(bounds[3 + d]);
     float c = (a[d] + a[3 + d]) * 0.5f;
-    float ext = hi - lo;
-    u[d] = ext > 0.0f ? (c - lo) / ext : 0.5f;
+    u[d] = ext > 0.0f ? (c - float_unflip(bounds[d])) / ext : 0.5f;
   }
   keys[i] = morton30(u[0], u[1], u[2]);
   vals[i] = i;

@@ -361,13 +361,12 @@ __global__ void k_ray_keys(const float* __restrict__ rays, uint32_t n, const uin
                            uint32_t* __restrict__ vals, uint32_t key_mode) {
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
+  float ext = 0.0f;  // one scale for all axes: cubic Morton cells
+#pragma unroll
+  for (int d = 0; d < 3; ++d) ext = fmaxf(ext, float_unflip(bounds[3 + d]) - float_unflip(bounds[d]));
   float u[3];
 #pragma unroll
-  for (int d = 0; d < 3; ++d) {
-    float lo = float_unflip(bounds[d]), hi = float_unflip(bounds[3 + d]);
-    float ext = hi - lo;
-    u[d] = ext > 0.0f ? (rays[6 * (size_t)i + d] - lo) / ext : 0.5f;
-  }
+  for (int d = 0; d < 3; ++d) u[d] = ext > 0.0f ? (rays[6 * (size_t)i + d] - float_unflip(bounds[d])) / ext : 0.5f;
   uint32_t key = morton30(u[0], u[1], u[2]);
   if (key_mode == 1) {
     const float* d = rays + 6 * (size_t)i + 3;
