@@ -85,6 +85,54 @@ __device__ __forceinline__ Pose pose_inverse(const Pose& s) {
   return r;
 }
 
+// Support point of a vertex cloud (point_cloud_support_point). Kept out of line: it is called
+// from every support evaluation of every kernel, and one shared copy keeps the large GJK / EPA /
+// manifold kernels within the instruction cache.
+static __device__ __noinline__ V3 convex_support(const float* __restrict__ pts, uint32_t npts, V3 dir) {
+  // First index of the maximum dot product (point_cloud_support_point: best = 0, then strict
+  // `>`). Four partial scans, each seeded with vertex 0, keep four independent compare chains;
+  // each keeps the first index of its own maximum (its indices increase), and the merge prefers
+  // the larger value, then the smaller index - the sequential answer (NaN dot products never
+  // replace, as in the sequential scan). Vertices are 12 bytes; from the first vertex whose
+  // address is 16-byte aligned, groups of four are read as three 16-byte loads, one vertex per
+  // chain; the vertices before and after those groups go to chain 0.
+  const uint32_t n = npts;
+  const float d0 = dot(ldv(pts), dir);
+  uint32_t bi[4] = {0u, 0u, 0u, 0u};
+  float bd[4] = {d0, d0, d0, d0};
+  uint32_t h = 0;
+  const uintptr_t addr = reinterpret_cast<uintptr_t>(pts);
+  while (h < 4 && ((addr + 12u * h) & 15u) != 0) ++h;
+  uint32_t i = 1;
+  if (h < 4 && h + 4 <= n) {
+    for (; i < h; ++i) {  // leading vertices: chain 0 (indices below the body's)
+      float d = dot(ldv(pts + 3 * i), dir);
+      if (d > bd[0]) { bd[0] = d; bi[0] = i; }
+    }
+    const float4* q = reinterpret_cast<const float4*>(pts + 3 * h);
+    for (i = h; i + 4 <= n; i += 4, q += 3) {
+      float4 a = __ldg(q), b = __ldg(q + 1), c = __ldg(q + 2);
+      float e0 = dot(v3(a.x, a.y, a.z), dir), e1 = dot(v3(a.w, b.x, b.y), dir);
+      float e2 = dot(v3(b.z, b.w, c.x), dir), e3 = dot(v3(c.y, c.z, c.w), dir);
+      if (e0 > bd[0]) { bd[0] = e0; bi[0] = i; }
+      if (e1 > bd[1]) { bd[1] = e1; bi[1] = i + 1; }
+      if (e2 > bd[2]) { bd[2] = e2; bi[2] = i + 2; }
+      if (e3 > bd[3]) { bd[3] = e3; bi[3] = i + 3; }
+    }
+  }
+  for (; i < n; ++i) {  // trailing vertices (or all of a short / unaligned cloud): chain 0
+    float d = dot(ldv(pts + 3 * i), dir);
+    if (d > bd[0]) { bd[0] = d; bi[0] = i; }
+  }
+  uint32_t best = bi[0];
+  float bv = bd[0];
+#pragma unroll
+  for (int l = 1; l < 4; ++l) {
+    if (bd[l] > bv || (bd[l] == bv && bi[l] < best)) { bv = bd[l]; best = bi[l]; }
+  }
+  return ldv(pts + 3 * best);
+}
+
 // SupportMap::local_support_point
 __device__ __forceinline__ V3 local_support(const ShapeDev& s, V3 dir) {
   switch (s.type) {
@@ -108,49 +156,7 @@ __device__ __forceinline__ V3 local_support(const ShapeDev& s, V3 dir) {
       if (d1 > d2) return d1 > d3 ? p0 : p2;
       return d2 > d3 ? p1 : p2;
     }
-    case SH_CONVEX: {
-      // First index of the maximum dot product (point_cloud_support_point: best = 0, then strict
-      // `>`). Four partial scans, each seeded with vertex 0, keep four independent compare chains;
-      // each keeps the first index of its own maximum (its indices increase), and the merge prefers
-      // the larger value, then the smaller index - the sequential answer (NaN dot products never
-      // replace, as in the sequential scan). Vertices are 12 bytes; from the first vertex whose
-      // address is 16-byte aligned, groups of four are read as three 16-byte loads.
-      const uint32_t n = s.npts;
-      const float d0 = dot(ldv(s.pts), dir);
-      uint32_t bi[4] = {0u, 0u, 0u, 0u};
-      float bd[4] = {d0, d0, d0, d0};
-      uint32_t h = 0;
-      const uintptr_t addr = reinterpret_cast<uintptr_t>(s.pts);
-      while (h < 4 && ((addr + 12u * h) & 15u) != 0) ++h;
-      uint32_t i = 1;
-      if (h < 4 && h + 4 <= n) {
-        for (; i < h; ++i) {
-          float d = dot(ldv(s.pts + 3 * i), dir);
-          if (d > bd[i & 3]) { bd[i & 3] = d; bi[i & 3] = i; }
-        }
-        const float4* q = reinterpret_cast<const float4*>(s.pts + 3 * h);
-        for (i = h; i + 4 <= n; i += 4, q += 3) {
-          float4 a = __ldg(q), b = __ldg(q + 1), c = __ldg(q + 2);
-          float e0 = dot(v3(a.x, a.y, a.z), dir), e1 = dot(v3(a.w, b.x, b.y), dir);
-          float e2 = dot(v3(b.z, b.w, c.x), dir), e3 = dot(v3(c.y, c.z, c.w), dir);
-          if (e0 > bd[0]) { bd[0] = e0; bi[0] = i; }
-          if (e1 > bd[1]) { bd[1] = e1; bi[1] = i + 1; }
-          if (e2 > bd[2]) { bd[2] = e2; bi[2] = i + 2; }
-          if (e3 > bd[3]) { bd[3] = e3; bi[3] = i + 3; }
-        }
-      }
-      for (; i < n; ++i) {
-        float d = dot(ldv(s.pts + 3 * i), dir);
-        if (d > bd[i & 3]) { bd[i & 3] = d; bi[i & 3] = i; }
-      }
-      uint32_t best = bi[0];
-      float bv = bd[0];
-#pragma unroll
-      for (int l = 1; l < 4; ++l) {
-        if (bd[l] > bv || (bd[l] == bv && bi[l] < best)) { bv = bd[l]; best = bi[l]; }
-      }
-      return ldv(s.pts + 3 * best);
-    }
+    case SH_CONVEX: return convex_support(s.pts, s.npts, dir);
     default: return v3(0.f, 0.f, 0.f);  // ConstantOrigin
   }
 }

@@ -65,6 +65,10 @@ struct parrygpu_ctx {
   RayWaveScratch ray_wave;
   MfScratch mf;
   int sm_count = 0;
+  // Second stream for pipelined host-buffer calls (chunks alternate between it and `stream`),
+  // with the fork / join events that order it after and before the context stream's work.
+  cudaStream_t aux_stream = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   // Optional per-kernel event timing (parrygpu_enable_kernel_timing).
   bool timing = false;
   std::map<std::string, std::vector<std::pair<cudaEvent_t, cudaEvent_t>>> pending;

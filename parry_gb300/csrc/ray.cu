@@ -435,6 +435,61 @@ void parrygpu_trimesh_destroy(parrygpu_trimesh* m) {
   delete m;
 }
 
+// Host-buffer calls without a ray ordering run in chunks alternating between the context stream
+// and a second stream: the host<->device copies of one chunk overlap the traversal of the other
+// (each chunk's upload, traversal and download stay in order on its stream). Answers are those of
+// the single-shot call: every ray is independent.
+constexpr uint32_t PIPE_MIN_CHUNK = 65536;
+
+static parrygpu_status cast_rays_pipelined(parrygpu_ctx* ctx, const parrygpu_trimesh* mesh, const float* pose_host, const float* rays,
+                                           uint32_t n, float max_toi, uint32_t* feature, float* toi, float* normal, bool host_in,
+                                           bool h_feat, bool h_toi, bool h_nrm) {
+  if (!ctx->aux_stream) {
+    PG_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->aux_stream, cudaStreamNonBlocking));
+    PG_CUDA(ctx, cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming));
+    PG_CUDA(ctx, cudaEventCreateWithFlags(&ctx->ev_join, cudaEventDisableTiming));
+  }
+  const float* d_rays = rays;
+  uint32_t* d_feat = feature;
+  float *d_toi = toi, *d_nrm = normal;
+  if (host_in) { PG_CUDA(ctx, ctx->stage_in[2].reserve((size_t)n * 24)); d_rays = ctx->stage_in[2].as<float>(); }
+  if (h_feat) { PG_CUDA(ctx, ctx->stage_out[1].reserve((size_t)n * 4)); d_feat = ctx->stage_out[1].as<uint32_t>(); }
+  if (h_toi) { PG_CUDA(ctx, ctx->stage_out[2].reserve((size_t)n * 4)); d_toi = ctx->stage_out[2].as<float>(); }
+  if (h_nrm) { PG_CUDA(ctx, ctx->stage_out[3].reserve((size_t)n * 12)); d_nrm = ctx->stage_out[3].as<float>(); }
+  PG_CUDA(ctx, ctx->misc.reserve(128));
+  uint32_t* counters = ctx->misc.as<uint32_t>() + 16;  // one fetch counter per stream
+  cudaStream_t main = ctx->stream;
+  cudaStream_t lanes[2] = {main, ctx->aux_stream};
+  PG_CUDA(ctx, cudaEventRecord(ctx->ev_fork, main));
+  PG_CUDA(ctx, cudaStreamWaitEvent(ctx->aux_stream, ctx->ev_fork, 0));
+  uint32_t chunks = n / PIPE_MIN_CHUNK;
+  if (chunks > 8) chunks = 8;
+  if (chunks < 2) chunks = 2;
+  const uint32_t chunk = ((n + chunks - 1) / chunks + 255u) & ~255u;
+  parrygpu_status s = PARRYGPU_OK;
+  cudaError_t e = cudaSuccess;
+  for (uint32_t c = 0, off = 0; off < n && s == PARRYGPU_OK && e == cudaSuccess; ++c, off += chunk) {
+    const uint32_t m = n - off < chunk ? n - off : chunk;
+    cudaStream_t st = lanes[c & 1];
+    ctx->stream = st;
+    if (host_in) e = cudaMemcpyAsync((void*)(d_rays + 6 * (size_t)off), rays + 6 * (size_t)off, (size_t)m * 24, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess)
+      s = launch_trimesh_rays(ctx, mesh, pose_host, d_rays + 6 * (size_t)off, nullptr, m, max_toi, d_feat + off, d_toi + off,
+                              d_nrm ? d_nrm + 3 * (size_t)off : nullptr, counters + (c & 1));
+    if (s == PARRYGPU_OK && e == cudaSuccess && h_feat) e = cudaMemcpyAsync(feature + off, d_feat + off, (size_t)m * 4, cudaMemcpyDeviceToHost, st);
+    if (s == PARRYGPU_OK && e == cudaSuccess && h_toi) e = cudaMemcpyAsync(toi + off, d_toi + off, (size_t)m * 4, cudaMemcpyDeviceToHost, st);
+    if (s == PARRYGPU_OK && e == cudaSuccess && h_nrm)
+      e = cudaMemcpyAsync(normal + 3 * (size_t)off, d_nrm + 3 * (size_t)off, (size_t)m * 12, cudaMemcpyDeviceToHost, st);
+  }
+  ctx->stream = main;
+  cudaError_t je = cudaEventRecord(ctx->ev_join, ctx->aux_stream);
+  if (je == cudaSuccess) je = cudaStreamWaitEvent(main, ctx->ev_join, 0);
+  if (s != PARRYGPU_OK) return s;
+  if (e != cudaSuccess) return check_cuda(ctx, e, "pipelined ray cast");
+  if (je != cudaSuccess) return check_cuda(ctx, je, "pipelined ray cast join");
+  return parrygpu_sync(ctx);
+}
+
 parrygpu_status parrygpu_trimesh_cast_rays(parrygpu_ctx* ctx, const parrygpu_trimesh* mesh, const float* pose7, const float* rays,
                                            uint32_t n, float max_toi, int solid, uint32_t* feature, float* toi, float* normal) {
   (void)solid;
@@ -453,6 +508,14 @@ parrygpu_status parrygpu_trimesh_cast_rays(parrygpu_ctx* ctx, const parrygpu_tri
       for (int i = 0; i < 7; ++i) p[i] = pose7[i];
     }
     pose = Pose{p[0], p[1], p[2], p[3], v3(p[4], p[5], p[6])};
+  }
+  {
+    const bool host_in = !is_device_ptr(rays), h_feat = !is_device_ptr(feature), h_toi = !is_device_ptr(toi);
+    const bool h_nrm = normal && !is_device_ptr(normal);
+    if ((host_in || h_feat || h_toi || h_nrm) && mesh->n_triangles > 0 && !ctx->cfg.sort_rays && n >= 2 * PIPE_MIN_CHUNK) {
+      float p7[7] = {pose.qi, pose.qj, pose.qk, pose.qw, pose.t.x, pose.t.y, pose.t.z};
+      return cast_rays_pipelined(ctx, mesh, has_pose ? p7 : nullptr, rays, n, max_toi, feature, toi, normal, host_in, h_feat, h_toi, h_nrm);
+    }
   }
   const void* d_rays = nullptr;
   parrygpu_status s = stage_input(ctx, ctx->stage_in[2], rays, (size_t)n * 24, &d_rays);

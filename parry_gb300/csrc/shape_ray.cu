@@ -464,22 +464,52 @@ __device__ __forceinline__ void ray_of(const float* rays, const uint32_t* order,
   if (has_pose) { *o = pose_inv_point(cpose, *o); *dir = pose_inv_rotate(cpose, *dir); }
 }
 
+// Candidate lists are two-ended: capsule candidates fill a list from the front, hull candidates
+// from the back, so each kind's entries are contiguous and the GJK kernels run warps of one kind
+// (a capsule's support is O(1), a hull's a vertex scan). A list's 64-bit counter holds the front
+// count (low half) and the back count (high half).
 struct WaveBufs {
   RayCand* a;            // nearest candidate of each ray that has one (capacity n)
   RayCand* b;            // the other candidates (capacity cap)
   unsigned long long cap;
-  unsigned long long* count;    // [0] list B length, [1] list A length
+  unsigned long long* count;    // [0] list B counter, [1] list A counter, [2] list B first-failure snapshot
   unsigned long long* keys;  // per ray (index r)
   uint8_t* ovf;              // per ray (index r)
 };
 
-// Appends one slot per calling thread to a list: one atomicAdd per group of converged threads.
-__device__ __forceinline__ unsigned long long append_slot(unsigned long long* counter) {
+// Appends one slot per calling thread to a two-ended list of `cap` entries (kind 0 at the front,
+// kind 1 at the back) with one atomicAdd per group of converged threads. A group whose slots do
+// not all fit gets none (returns ~0), and its leader records the counter value it found in *fail
+// (atomicMin): counters only grow, so every later group fails too, and the first failure's value
+// is the count of slots actually written at each end.
+__device__ __forceinline__ unsigned long long append_slot2(unsigned long long* counter, unsigned long long cap, uint32_t kind,
+                                                           unsigned long long* fail) {
   namespace cg = cooperative_groups;
   cg::coalesced_group g = cg::coalesced_threads();
+  const unsigned back = g.ballot(kind != 0);
+  const uint32_t n1 = (uint32_t)__popc(back), n0 = g.size() - n1;
   unsigned long long base = 0;
-  if (g.thread_rank() == 0) base = atomicAdd(counter, (unsigned long long)g.size());
-  return g.shfl(base, 0) + g.thread_rank();
+  if (g.thread_rank() == 0) base = atomicAdd(counter, (unsigned long long)n0 | ((unsigned long long)n1 << 32));
+  base = g.shfl(base, 0);
+  const unsigned long long lo = base & 0xffffffffull, hi = base >> 32;
+  if (lo + hi + n0 + n1 > cap) {
+    if (fail && g.thread_rank() == 0) atomicMin(fail, base);
+    return ~0ull;
+  }
+  const uint32_t below = (uint32_t)__popc(back & ((1u << g.thread_rank()) - 1u));  // back-kind threads of lower rank
+  return kind ? cap - 1ull - (hi + below) : lo + (g.thread_rank() - below);
+}
+
+// Entries of a two-ended list: [0, front) and [cap - back, cap), as one index space.
+__device__ __forceinline__ void list_extent(const unsigned long long* counter, const unsigned long long* fail, unsigned long long* front,
+                                            unsigned long long* back) {
+  unsigned long long c = *counter;
+  if (fail && *fail != ~0ull) c = *fail;
+  *front = c & 0xffffffffull;
+  *back = c >> 32;
+}
+__device__ __forceinline__ unsigned long long list_slot(unsigned long long i, unsigned long long front, unsigned long long cap) {
+  return i < front ? i : cap - 1ull - (i - front);
 }
 
 __global__ void __launch_bounds__(128) k_rays_wave(const WideNode* __restrict__ wide, CompoundDev cd, const float* __restrict__ rays, uint32_t n,
@@ -500,8 +530,9 @@ __global__ void __launch_bounds__(128) k_rays_wave(const WideNode* __restrict__ 
   uint32_t near_part = 0xffffffffu;
   float near_tmin = FLT_MAX;
   auto defer = [&](uint32_t part, float tmin) {
-    unsigned long long slot = append_slot(wb.count);
-    if (slot < wb.cap) wb.b[slot] = RayCand{k, r, part, 0u, tmin, 0.f, 0.f, 0.f, 0.f, 0.f};
+    if (overflow) return;  // this ray is recast by the single kernel anyway
+    unsigned long long slot = append_slot2(wb.count, wb.cap, cd.types[part] == SH_CAPSULE ? 0u : 1u, wb.count + 2);
+    if (slot != ~0ull) wb.b[slot] = RayCand{k, r, part, 0u, tmin, 0.f, 0.f, 0.f, 0.f, 0.f};
     else overflow = true;
   };
   auto visit_leaf = [&](uint32_t part, float tmin) {
@@ -560,7 +591,11 @@ __global__ void __launch_bounds__(128) k_rays_wave(const WideNode* __restrict__ 
       load_wide(wide, next, &w);
     }
   }
-  if (near_part != 0xffffffffu) wb.a[append_slot(wb.count + 1)] = RayCand{k, r, near_part, 0u, near_tmin, 0.f, 0.f, 0.f, 0.f, 0.f};
+  if (near_part != 0xffffffffu) {
+    // at most one entry per ray: list A (n entries) never fills
+    unsigned long long slot = append_slot2(wb.count + 1, n, cd.types[near_part] == SH_CAPSULE ? 0u : 1u, nullptr);
+    wb.a[slot] = RayCand{k, r, near_part, 0u, near_tmin, 0.f, 0.f, 0.f, 0.f, 0.f};
+  }
   wb.keys[r] = have ? hit_key(best, best_part) : ~0ull;
   wb.ovf[r] = overflow ? 1 : 0;
   if (has_pose && have) best_n = pose_rotate(cpose, best_n);
@@ -597,26 +632,29 @@ __device__ __forceinline__ void run_candidate(const CompoundDev& cd, const float
   atomicMin(&keys[r], hit_key(t, c.part));
 }
 
-// Grid-stride over min(n, *count) entries of list A or list B.
+// Grid-stride over the entries of a two-ended list of capacity `cap` (fail may be null).
 __global__ void __launch_bounds__(128) k_rays_cand(CompoundDev cd, const float* __restrict__ rays, float max_toi, int solid, int has_pose,
                                                    Pose cpose, const uint32_t* __restrict__ order, int permuted, RayCand* __restrict__ list,
-                                                   unsigned long long n, const unsigned long long* __restrict__ count,
-                                                   unsigned long long* __restrict__ keys) {
-  unsigned long long m = n;
-  if (count && *count < m) m = *count;
+                                                   unsigned long long cap, const unsigned long long* __restrict__ count,
+                                                   const unsigned long long* __restrict__ fail, unsigned long long* __restrict__ keys) {
+  unsigned long long front, back;
+  list_extent(count, fail, &front, &back);
+  const unsigned long long m = front + back;
   for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < m;
        i += (unsigned long long)gridDim.x * blockDim.x)
-    run_candidate(cd, rays, max_toi, solid, has_pose, cpose, order, permuted, list + i, keys);
+    run_candidate(cd, rays, max_toi, solid, has_pose, cpose, order, permuted, list + list_slot(i, front, cap), keys);
 }
 
-__global__ void __launch_bounds__(128) k_rays_finish(const RayCand* __restrict__ list, unsigned long long n,
-                                                     const unsigned long long* __restrict__ count, const unsigned long long* __restrict__ keys,
-                                                     uint32_t* __restrict__ part_out, float* __restrict__ toi_out, float* __restrict__ normal_out) {
-  unsigned long long m = n;
-  if (count && *count < m) m = *count;
+__global__ void __launch_bounds__(128) k_rays_finish(const RayCand* __restrict__ list, unsigned long long cap,
+                                                     const unsigned long long* __restrict__ count, const unsigned long long* __restrict__ fail,
+                                                     const unsigned long long* __restrict__ keys, uint32_t* __restrict__ part_out,
+                                                     float* __restrict__ toi_out, float* __restrict__ normal_out) {
+  unsigned long long front, back;
+  list_extent(count, fail, &front, &back);
+  const unsigned long long m = front + back;
   for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < m;
        i += (unsigned long long)gridDim.x * blockDim.x) {
-    RayCand e = list[i];
+    RayCand e = list[list_slot(i, front, cap)];
     if (!e.hit || keys[e.r] != hit_key(e.t, e.part)) continue;
     part_out[e.r] = e.part;
     toi_out[e.r] = e.t;
@@ -637,9 +675,10 @@ static parrygpu_status compound_copy_in(parrygpu_ctx* ctx, DevBuf& dst, const vo
 }
 
 parrygpu_status shape_rays_reserve(parrygpu_ctx* ctx, RayWaveScratch& sc, uint32_t n) {
-  uint64_t cap = 4ull * n + 1024;
+  if (n > (1u << 30)) return set_error(ctx, PARRYGPU_INVALID_ARG, "shape-set ray casts take at most 2^30 rays per call");
+  uint64_t cap = 4ull * n + 1024;  // below 2^32: the list counters pack two 32-bit counts
   PG_CUDA(ctx, sc.cands.reserve((cap + n) * sizeof(RayCand)));  // list A (n slots) then list B (cap)
-  PG_CUDA(ctx, sc.counter.reserve(16));
+  PG_CUDA(ctx, sc.counter.reserve(32));
   PG_CUDA(ctx, sc.keys.reserve((size_t)n * 8 + 16));
   PG_CUDA(ctx, sc.ovf.reserve((size_t)n + 16));
   sc.cap = cap;
@@ -654,16 +693,19 @@ static parrygpu_status launch_wave(parrygpu_ctx* ctx, const WideNode* wide, Comp
   WaveBufs wb{sc.cands.as<RayCand>(), sc.cands.as<RayCand>() + n, sc.cap, cnt, sc.keys.as<unsigned long long>(), sc.ovf.as<uint8_t>()};
   uint32_t grid = (uint32_t)(ctx->sm_count > 0 ? ctx->sm_count : 152) * 16;
   PG_CUDA(ctx, cudaMemsetAsync(cnt, 0, 16, ctx->stream));
+  PG_CUDA(ctx, cudaMemsetAsync(cnt + 2, 0xff, 8, ctx->stream));
   k_rays_wave<<<div_up(n, 128), 128, 0, ctx->stream>>>(wide, cd, d_rays, n, max_toi, solid, has_pose, pose, d_part, d_toi, d_nrm, ctx->d_err,
                                                        order, permuted, wb);
   PG_LAUNCHED(ctx);
-  k_rays_cand<<<grid, 128, 0, ctx->stream>>>(cd, d_rays, max_toi, solid, has_pose, pose, order, permuted, wb.a, n, cnt + 1, wb.keys);
+  k_rays_cand<<<grid, 128, 0, ctx->stream>>>(cd, d_rays, max_toi, solid, has_pose, pose, order, permuted, wb.a, n, cnt + 1, nullptr,
+                                             wb.keys);
   PG_LAUNCHED(ctx);
-  k_rays_cand<<<grid, 128, 0, ctx->stream>>>(cd, d_rays, max_toi, solid, has_pose, pose, order, permuted, wb.b, sc.cap, cnt, wb.keys);
+  k_rays_cand<<<grid, 128, 0, ctx->stream>>>(cd, d_rays, max_toi, solid, has_pose, pose, order, permuted, wb.b, sc.cap, cnt, cnt + 2,
+                                             wb.keys);
   PG_LAUNCHED(ctx);
-  k_rays_finish<<<grid, 128, 0, ctx->stream>>>(wb.a, n, cnt + 1, wb.keys, d_part, d_toi, d_nrm);
+  k_rays_finish<<<grid, 128, 0, ctx->stream>>>(wb.a, n, cnt + 1, nullptr, wb.keys, d_part, d_toi, d_nrm);
   PG_LAUNCHED(ctx);
-  k_rays_finish<<<grid, 128, 0, ctx->stream>>>(wb.b, sc.cap, cnt, wb.keys, d_part, d_toi, d_nrm);
+  k_rays_finish<<<grid, 128, 0, ctx->stream>>>(wb.b, sc.cap, cnt, cnt + 2, wb.keys, d_part, d_toi, d_nrm);
   PG_LAUNCHED(ctx);
   // rays whose candidates overflowed list B: the single-kernel cast, for them only
   k_compound_rays<<<div_up(n, 128), 128, 0, ctx->stream>>>(wide, cd, d_rays, n, max_toi, solid, has_pose, pose, d_part, d_toi, d_nrm,

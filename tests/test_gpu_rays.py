@@ -167,3 +167,25 @@ def test_autotune_keeps_answers(oracle_lib):
 def test_invalid_config_rejected(kw):
     with pytest.raises(Exception):
         pg.Context(0, **kw)
+
+
+@pytest.mark.parametrize("traversal", [1, 2])
+def test_pipelined_host_buffers(oracle_lib, traversal):
+    """Host-buffer calls without a ray ordering run in chunks over two streams; pageable, pinned,
+    device-in / host-out and toi-only calls all answer as the oracle."""
+    import torch
+    ctx = pg.Context(0, sort_rays=False, ray_traversal=traversal)
+    v, i = W.terrain_mesh(128, 64, seed=9)
+    rays = W.terrain_rays(600_001, 128, 64, seed=9)  # not a multiple of the chunk size
+    m = pg.TriMesh(ctx, v, i)
+    fo, to, no = oracle_lib.TriMesh(v, i).cast_rays_and_get_normal(rays, 100.0)
+    f, t, n = m.cast_rays_and_get_normal(rays, 100.0)  # pageable numpy
+    _compare(f, t, n, fo, to, no)
+    fp, tp, np_ = m.cast_rays_and_get_normal(torch.from_numpy(rays).pin_memory(), 100.0)  # pinned
+    _compare(fp.numpy().view(np.uint32), tp.numpy(), np_.numpy(), fo, to, no)
+    feat = np.empty(len(rays), np.uint32)
+    toi = np.empty(len(rays), np.float32)
+    m.cast_rays(torch.from_numpy(rays).cuda(), 100.0, out=(feat, toi, None))  # device in, host out, no normals
+    np.testing.assert_array_equal(feat, fo)
+    np.testing.assert_array_equal(toi, t)
+    ctx.close()
