@@ -56,7 +56,9 @@ typedef struct parrygpu_config {
                               origin's Morton code (two radix passes instead of four) */
   uint32_t epa_blocks_per_sm; /* contacts EPA: resident 64-thread blocks per SM (0 = library default, 8; at most 32) */
   uint32_t ray_traversal;  /* TriMesh ray traversal: 0 = library default (1); 1 = one ray per thread;
-                              2 = persistent warps that fetch new rays as lanes finish theirs */
+                              2 = persistent warps that fetch new rays as lanes finish theirs;
+                              3 = one ray per thread with leaf tests postponed until the warp's
+                              lanes all hold one ("while-while") */
   uint32_t ray_refill;     /* traversal 2: a warp fetches rays once this many of its lanes are idle
                               (0 = library default, 16; at most 32) */
   uint32_t reserved[1];
@@ -380,9 +382,9 @@ parrygpu_status parrygpu_compound_cast_rays(parrygpu_ctx* ctx, const parrygpu_co
 parrygpu_status parrygpu_get_config(const parrygpu_ctx* ctx, parrygpu_config* out);
 /* Times parrygpu_trimesh_cast_rays on `rays` (device or host; copied to the device once, outputs
  * kept on the device) for each candidate ray ordering (input order; 30-bit Morton; octant + 27-bit
- * Morton; 16-bit Morton prefix) x traversal (one ray per thread at 64, 128, 256 threads per block;
- * dynamic fetch refilling at 8, 16, 24 idle lanes): one untimed run then `reps` timed runs each
- * (0 = 3). The fastest candidate becomes the context's configuration and is
+ * Morton; 16-bit Morton prefix) x traversal (one ray per thread, and postponed leaves, at 64, 128,
+ * 256 threads per block; dynamic fetch refilling at 8, 16, 24 idle lanes): one untimed run then
+ * `reps` timed runs each (0 = 3). The fastest candidate becomes the context's configuration and is
  * copied to *chosen (may be NULL). On an error the configuration is left unchanged. */
 parrygpu_status parrygpu_autotune_trimesh_rays(parrygpu_ctx* ctx, const parrygpu_trimesh* mesh, const float* pose7, const float* rays,
                                                uint32_t n, float max_toi, uint32_t reps, parrygpu_config* chosen);

@@ -38,9 +38,9 @@ struct RayCandidate {
 };
 
 // Ray orderings: input order; 30-bit Morton code of the origin; direction octant above a 27-bit
-// Morton code; top 16 bits of the Morton code. Each with one ray per thread at 64 / 128 / 256
-// threads per block, and with the persistent dynamic-fetch traversal refilling at 8 / 16 / 24
-// idle lanes.
+// Morton code; top 16 bits of the Morton code. Each with one ray per thread and with postponed
+// leaves, at 64 / 128 / 256 threads per block, and with the persistent dynamic-fetch traversal
+// refilling at 8 / 16 / 24 idle lanes.
 constexpr uint32_t SORTS[4][2] = {{0, 0}, {1, 0}, {1, 1}, {1, 2}};
 constexpr uint32_t BLOCKS[3] = {64, 128, 256};
 constexpr uint32_t REFILLS[3] = {8, 16, 24};
@@ -79,10 +79,11 @@ parrygpu_status parrygpu_autotune_trimesh_rays(parrygpu_ctx* ctx, const parrygpu
   parrygpu_config best = saved;
   float best_ms = -1.0f;
   parrygpu_status s = PARRYGPU_OK;
-  RayCandidate cands[4 * 6];
+  RayCandidate cands[4 * 9];
   int nc = 0;
   for (const auto& so : SORTS) {
     for (uint32_t b : BLOCKS) cands[nc++] = RayCandidate{so[0], so[1], 1u, b, 0u};
+    for (uint32_t b : BLOCKS) cands[nc++] = RayCandidate{so[0], so[1], 3u, b, 0u};
     for (uint32_t f : REFILLS) cands[nc++] = RayCandidate{so[0], so[1], 2u, 0u, f};
   }
   for (int ci = 0; ci < nc; ++ci) {

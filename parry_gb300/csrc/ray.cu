@@ -239,6 +239,82 @@ __global__ void k_trimesh_rays(const WideNode* __restrict__ wide, const float4* 
   ray_finish<HAS_POSE, WANT_NORMAL>(soup, n_tris, pose, st, r, feat, toi_out, normal_out);
 }
 
+// Postponed leaves ("while-while" traversal): a lane that meets a leaf child keeps it (up to two)
+// and goes on stepping through nodes while some lane of its warp has still found no leaf; then the
+// whole warp tests its pending triangles together. Triangle tests - the divergent part of a step -
+// run with most lanes active, at the price of node steps pruned by a best hit that is not yet
+// lowered. A pending leaf is tested only if its box entry still passes the acceptance test of the
+// moment; the answer (nearest hit, lowest index on exact ties) does not depend on the order.
+template <bool HAS_POSE, bool WANT_NORMAL>
+__global__ void k_trimesh_rays_ww(const WideNode* __restrict__ wide, const float4* __restrict__ soup, uint32_t n_tris,
+                                  const float* __restrict__ rays, const uint32_t* __restrict__ order, uint32_t n, float max_toi, Pose pose,
+                                  uint32_t* __restrict__ feat, float* __restrict__ toi_out, float* __restrict__ normal_out,
+                                  uint32_t* __restrict__ err) {
+  const unsigned FULL = 0xffffffffu;
+  const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool live = k < n;
+  uint32_t r = 0;
+  RayState st;
+  uint32_t cur = 0xffffffffu;  // next wide node to step, none when ~0
+  uint32_t p0 = 0xffffffffu, p1 = 0xffffffffu;  // pending leaves (soup positions)
+  float e0 = 0.f, e1 = 0.f;                    // their box entries
+  uint32_t stack[RAY_STACK];
+  int sp = 0;
+  if (live) {
+    r = order ? order[k] : k;
+    ray_init<HAS_POSE>(rays, r, max_toi, pose, &st);
+    cur = 0;
+  }
+  auto accept = [&](float t) { return t != FLT_MAX && (t < st.best || (st.have && t == st.best)); };
+  for (;;) {
+    // node phase: step while some lane has nodes left and no pending leaf
+    while (__any_sync(FULL, cur != 0xffffffffu && p0 == 0xffffffffu)) {
+      if (cur == 0xffffffffu || p1 != 0xffffffffu) continue;  // nothing to step, or both leaf slots full
+      WideNode w;
+      load_wide(wide, cur, &w);
+      float ls = slab(w.l.mins, w.l.maxs, st.o, st.inv, st.zmask, st.best);
+      float rs = slab(w.r.mins, w.r.maxs, st.o, st.inv, st.zmask, st.best);
+      const BvhNodeDev* nearn = &w.l;
+      const BvhNodeDev* farn = &w.r;
+      if (ls > rs) { float t = ls; ls = rs; rs = t; nearn = &w.r; farn = &w.l; }
+      uint32_t next = 0xffffffffu;
+      const float ts[2] = {ls, rs};
+      const BvhNodeDev* cs[2] = {nearn, farn};
+#pragma unroll
+      for (int c = 0; c < 2; ++c) {
+        if (!accept(ts[c])) continue;
+        if ((cs[c]->data & 0x3fffffffu) == 1u) {
+          if (p0 == 0xffffffffu) { p0 = cs[c]->children; e0 = ts[c]; }
+          else if (p1 == 0xffffffffu) { p1 = cs[c]->children; e1 = ts[c]; }
+          else ray_try_leaf(soup, cs[c]->children, &st);  // third leaf of a speculative step: tested now
+        } else if (next == 0xffffffffu) {
+          next = cs[c]->children;
+        } else if (sp >= RAY_STACK) {
+          atomicOr(err, ERR_STACK_OVERFLOW);
+          next = 0xffffffffu;
+          sp = 0;
+          break;
+        } else {
+          stack[sp++] = cs[c]->children;
+        }
+      }
+      if (next == 0xffffffffu && sp > 0) next = stack[--sp];
+      cur = next;
+    }
+    // leaf phase: every lane tests its pending triangles
+    if (p0 != 0xffffffffu) {
+      if (accept(e0)) ray_try_leaf(soup, p0, &st);
+      p0 = 0xffffffffu;
+    }
+    if (p1 != 0xffffffffu) {
+      if (accept(e1)) ray_try_leaf(soup, p1, &st);
+      p1 = 0xffffffffu;
+    }
+    if (!__any_sync(FULL, cur != 0xffffffffu)) break;
+  }
+  if (live) ray_finish<HAS_POSE, WANT_NORMAL>(soup, n_tris, pose, st, r, feat, toi_out, normal_out);
+}
+
 // Persistent warps with dynamic ray fetch: every lane runs one traversal step per loop turn, and
 // once at least `refill` lanes of the warp have finished their rays, the warp takes that many new
 // ray slots from a global counter with one atomicAdd. Lanes whose rays end early pick up new rays
@@ -610,6 +686,14 @@ parrygpu_status launch_trimesh_rays(parrygpu_ctx* ctx, const parrygpu_trimesh* m
     return PARRYGPU_OK;
   }
   uint32_t bs = ctx->cfg.ray_block ? ctx->cfg.ray_block : 128;
+  if (ctx->cfg.ray_traversal == 3 && mesh->n_triangles >= 2) {
+    auto kern = has_pose ? (d_nrm ? k_trimesh_rays_ww<true, true> : k_trimesh_rays_ww<true, false>)
+                         : (d_nrm ? k_trimesh_rays_ww<false, true> : k_trimesh_rays_ww<false, false>);
+    kern<<<div_up(n, bs), bs, 0, ctx->stream>>>(w, soup, mesh->n_triangles, d_rays, order, n, max_toi, pose, d_feat, d_toi, d_nrm,
+                                                ctx->d_err);
+    PG_LAUNCHED(ctx);
+    return PARRYGPU_OK;
+  }
   auto kern = has_pose ? (d_nrm ? k_trimesh_rays<true, true> : k_trimesh_rays<true, false>)
                        : (d_nrm ? k_trimesh_rays<false, true> : k_trimesh_rays<false, false>);
   kern<<<div_up(n, bs), bs, 0, ctx->stream>>>(w, soup, mesh->n_triangles, d_rays, order, n, max_toi, pose, d_feat, d_toi, d_nrm, ctx->d_err);

@@ -41,7 +41,8 @@ def test_golden_fixture(gpu_ctx):
 
 
 @pytest.mark.parametrize("sort_rays,key,traversal,refill", [(True, 0, 1, 0), (True, 1, 1, 0), (True, 2, 1, 0), (False, 0, 1, 0),
-                                                        (False, 0, 2, 8), (True, 0, 2, 16), (False, 0, 2, 32), (True, 2, 2, 1)])
+                                                        (False, 0, 2, 8), (True, 0, 2, 16), (False, 0, 2, 32), (True, 2, 2, 1),
+                                                        (False, 0, 3, 0), (True, 1, 3, 0)])
 def test_medium_terrain_vs_oracle(oracle_lib, sort_rays, key, traversal, refill):
     ctx = pg.Context(0, sort_rays=sort_rays, ray_sort_key=key, ray_traversal=traversal, ray_refill=refill)
     v, i = W.terrain_mesh(64, 32, seed=21)
@@ -86,10 +87,11 @@ def test_pose_and_cast_ray_variant(gpu_ctx, oracle_lib):
     np.testing.assert_array_equal(t2, t)
 
 
-def test_fetch_traversal_full_size_pose_and_no_normal(oracle_lib):
-    """The persistent dynamic-fetch traversal on the full terrain workload, with a mesh pose, and
-    through the toi-only variant, answers as the oracle."""
-    ctx = pg.Context(0, ray_traversal=2)
+@pytest.mark.parametrize("traversal", [2, 3])
+def test_fetch_traversal_full_size_pose_and_no_normal(oracle_lib, traversal):
+    """The persistent dynamic-fetch and the postponed-leaf traversals on the full terrain workload,
+    with a mesh pose, and through the toi-only variant, answer as the oracle."""
+    ctx = pg.Context(0, ray_traversal=traversal)
     v, i = W.terrain_mesh()
     rays = W.terrain_rays(1 << 20, seed=77)
     m = pg.TriMesh(ctx, v, i)
@@ -150,8 +152,8 @@ def test_autotune_keeps_answers(oracle_lib):
     rays = W.terrain_rays(100_000, 64, 32, seed=5)
     m = pg.TriMesh(ctx, v, i)
     cfg = m.autotune(rays, 100.0, reps=1)
-    assert cfg["ray_sort_key"] in (0, 1, 2) and cfg["ray_traversal"] in (1, 2)
-    if cfg["ray_traversal"] == 1:
+    assert cfg["ray_sort_key"] in (0, 1, 2) and cfg["ray_traversal"] in (1, 2, 3)
+    if cfg["ray_traversal"] in (1, 3):
         assert cfg["ray_block"] in (64, 128, 256)
     else:
         assert cfg["ray_refill"] in (8, 16, 24)
@@ -163,13 +165,13 @@ def test_autotune_keeps_answers(oracle_lib):
 
 
 @pytest.mark.parametrize("kw", [{"ray_block": 48}, {"ray_block": 2048}, {"ray_sort_key": 3}, {"epa_blocks_per_sm": 64},
-                                {"ray_traversal": 3}, {"ray_refill": 33}])
+                                {"ray_traversal": 4}, {"ray_refill": 33}])
 def test_invalid_config_rejected(kw):
     with pytest.raises(Exception):
         pg.Context(0, **kw)
 
 
-@pytest.mark.parametrize("traversal", [1, 2])
+@pytest.mark.parametrize("traversal", [1, 2, 3])
 def test_pipelined_host_buffers(oracle_lib, traversal):
     """Host-buffer calls without a ray ordering run in chunks over two streams; pageable, pinned,
     device-in / host-out and toi-only calls all answer as the oracle."""

@@ -27,7 +27,7 @@ def _cast(fn, ctx, mesh, rays, torch):
     return st, feat, toi, nrm
 
 
-@pytest.mark.parametrize("traversal", [1, 2])
+@pytest.mark.parametrize("traversal", [1, 2, 3])
 def test_noalloc_matches_existing_entry_point_on_two_calls(traversal):
     torch = pytest.importorskip("torch")
     from parry_gb300 import _build
