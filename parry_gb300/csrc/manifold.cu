@@ -802,16 +802,25 @@ __device__ __forceinline__ bool hull_project_gjk(const ShapeDev& cs, V3 center, 
 // The pairs are binned by generator kind first (k_mf_classify), then each kind runs its own small
 // kernel over its bin: warps see one code path, the simple kinds keep few registers, and the
 // instruction cache holds one generator at a time.
-enum : uint32_t { MK_BALL_BALL = 0, MK_CUBOID_CUBOID, MK_CAPSULE_CAPSULE, MK_CONVEX_BALL, MK_HULL_BALL, MK_PFM, MK_KINDS };
+// The polyhedral pairs (contact_manifold_pfm_pfm) are split by shape kinds - cuboid-capsule,
+// cuboid-hull, capsule-hull, hull-hull - so that a warp runs one support and feature path.
+enum : uint32_t {
+  MK_BALL_BALL = 0, MK_CUBOID_CUBOID, MK_CAPSULE_CAPSULE, MK_CONVEX_BALL, MK_HULL_BALL,
+  MK_PFM, MK_PFM_CUBOID_HULL, MK_PFM_CAPSULE_HULL, MK_PFM_HULL_HULL, MK_KINDS
+};
 // counters: [0] EPA queue length, [1..3] GJK / EPA stats, [4 + kind] bin lengths
 constexpr int MF_CTR_BINS = 4;
+static_assert(MF_CTR_BINS + MK_KINDS <= 16, "the 128-byte counter block holds every bin length");
 
 __device__ __forceinline__ uint32_t manifold_kind(uint32_t t1, uint32_t t2) {
   if (t1 == SH_BALL && t2 == SH_BALL) return MK_BALL_BALL;
   if (t1 == SH_CUBOID && t2 == SH_CUBOID) return MK_CUBOID_CUBOID;
   if (t1 == SH_CAPSULE && t2 == SH_CAPSULE) return MK_CAPSULE_CAPSULE;
   if (t1 == SH_BALL || t2 == SH_BALL) return (t1 == SH_CONVEX || t2 == SH_CONVEX) ? MK_HULL_BALL : MK_CONVEX_BALL;
-  return MK_PFM;
+  const bool h1 = t1 == SH_CONVEX, h2 = t2 == SH_CONVEX;
+  if (h1 && h2) return MK_PFM_HULL_HULL;
+  if (h1 || h2) return (h1 ? t2 : t1) == SH_CUBOID ? MK_PFM_CUBOID_HULL : MK_PFM_CAPSULE_HULL;
+  return MK_PFM;  // cuboid-capsule
 }
 
 // Status of each pair (invalid / unsupported records keep their content) and its bin, appended with
@@ -907,7 +916,7 @@ __global__ void __launch_bounds__(MF_THREADS) k_mf_kind(ShapeArrays sh, const ui
     if (overflow) atomicOr(err, ERR_CAPACITY);
     if (bad) atomicOr(err, ERR_BAD_INDEX);
   }
-  if (KIND == MK_HULL_BALL || KIND == MK_PFM) {
+  if (KIND >= MK_HULL_BALL) {
     uint32_t w = __reduce_add_sync(0xffffffffu, iters);
     if ((threadIdx.x & 31) == 0 && w) atomicAdd(&ctr[1], (unsigned long long)w);
   }
@@ -1023,6 +1032,9 @@ parrygpu_status pg::launch_manifolds(parrygpu_ctx* ctx, const ShapeArrays& sh, c
   if ((s = launch_kind<MK_CONVEX_BALL>(ctx, sh, d_pairs, prediction, d_recs, sc, stride, grid)) != PARRYGPU_OK) return s;
   if ((s = launch_kind<MK_HULL_BALL>(ctx, sh, d_pairs, prediction, d_recs, sc, stride, grid)) != PARRYGPU_OK) return s;
   if ((s = launch_kind<MK_PFM>(ctx, sh, d_pairs, prediction, d_recs, sc, stride, grid)) != PARRYGPU_OK) return s;
+  if ((s = launch_kind<MK_PFM_CUBOID_HULL>(ctx, sh, d_pairs, prediction, d_recs, sc, stride, grid)) != PARRYGPU_OK) return s;
+  if ((s = launch_kind<MK_PFM_CAPSULE_HULL>(ctx, sh, d_pairs, prediction, d_recs, sc, stride, grid)) != PARRYGPU_OK) return s;
+  if ((s = launch_kind<MK_PFM_HULL_HULL>(ctx, sh, d_pairs, prediction, d_recs, sc, stride, grid)) != PARRYGPU_OK) return s;
   k_manifolds_epa<<<epa_blocks, MF_EPA_THREADS, 0, ctx->stream>>>(sh, d_pairs, prediction, d_recs, sc.queue.as<uint32_t>(), ctr,
                                                                  sc.epa_ws.as<uint32_t>(), ctr + 1, ctx->d_err);
   PG_LAUNCHED(ctx);
