@@ -179,6 +179,168 @@ def contacts_f64_error(s, pairs, has, res, sample: int = 16384) -> dict:
             "point_err_max": float(perr.max(initial=0.0)), "point_err_p99": q(perr)}
 
 
+def broadphase_section(ctx, stream, steps: int, warmup: int, n_shapes: int, flush) -> dict:
+    """Broadphase + narrow phase on 131,072 balls and cuboids (50/50) in a cube of side 400: shape
+    AABBs loosened by prediction/2, LBVH build, all overlapping pairs (traverse_bvtt_single_tree),
+    query::contact(prediction 0.1) on every pair. A step is the whole sequence on device-resident
+    shapes; the pair count comes back to the host to size the contact call. Checked against the
+    oracle's sorted pair set and contacts; the oracle runs the same sequence as the CPU baseline."""
+    import numpy as np
+    import torch
+    import parry_gb300 as pg
+    from parry_gb300 import workloads as W
+    from oracle import build as ob
+    ob.build()
+    from oracle import oracle as O
+
+    pred = 0.1
+    s = W.broadphase_shapes(n_shapes)
+    t, prm, pos, pool = s.arrays()
+    dev = tuple(torch.from_numpy(np.ascontiguousarray(a)).cuda() for a in (t.view(np.int32), prm, pos, pool))
+    aabbs = torch.empty((n_shapes, 6), dtype=torch.float32, device="cuda")
+    pg.shape_aabbs(ctx, dev, pred / 2, out=aabbs)
+    bvh = pg.Bvh.from_leaves(ctx, aabbs)
+    cap = 8 * n_shapes
+    pairs = torch.empty((cap, 2), dtype=torch.int32, device="cuda")
+    has = torch.empty(cap, dtype=torch.uint8, device="cuda")
+    res = torch.empty((cap, 13), dtype=torch.float32, device="cuda")
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+    split = np.zeros(3)
+
+    def step(record: bool):
+        if record:
+            ev[0].record(stream)
+        pg.shape_aabbs(ctx, dev, pred / 2, out=aabbs)
+        bvh.rebuild(aabbs)
+        if record:
+            ev[1].record(stream)
+        m = bvh.traverse_bvtt_single_tree_into(pairs)
+        if record:
+            ev[2].record(stream)
+        pg.contacts(ctx, dev, pairs[:m], pred, out=(has[:m], res[:m]))
+        if record:
+            ev[3].record(stream)
+        return m
+
+    for _ in range(max(1, warmup)):
+        m = step(False)
+    torch.cuda.synchronize()
+    l0 = ctx.kernel_launches
+    times = []
+    for _ in range(steps):
+        flush.zero_()
+        m = step(True)
+        torch.cuda.synchronize()
+        times.append(ev[0].elapsed_time(ev[3]))
+        split += [ev[0].elapsed_time(ev[1]), ev[1].elapsed_time(ev[2]), ev[2].elapsed_time(ev[3])]
+    launches = (ctx.kernel_launches - l0) // max(steps, 1)
+    ms = statistics.mean(times)
+    # oracle: the same sequence on the host cores (binned BVH, its own traversal), timed
+    threads = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    oa = O.shape_aabbs(s, pred / 2)
+    opairs = O.canonical_sorted_pairs(O.Bvh(oa).traverse_bvtt_single_tree())
+    oh, oo, _ = O.contacts(s, opairs, pred, threads=threads)
+    cpu_s = time.perf_counter() - t0
+    dev_pairs = pairs[:m].cpu().numpy().view(np.uint32)
+    order = np.lexsort((dev_pairs[:, 1], dev_pairs[:, 0]))
+    same_pairs = bool(np.array_equal(dev_pairs[order], opairs))
+    same_has = same_pairs and bool(np.array_equal(has[:m].cpu().numpy()[order], oh))
+    bvh.close()
+    return {
+        "workload": f"{n_shapes} balls and cuboids (50/50), radius / half extents log-uniform [0.25, 4], uniform rotations, "
+                    "centres U([-200, 200)^3); AABBs loosened by 0.05; LBVH; all overlapping pairs; query::contact(prediction 0.1)",
+        "metric": "broadphase+contact steps/s", "value": round(1e3 / ms, 2), "unit": "steps/s", "ms_per_step": round(ms, 4),
+        "shapes_per_s": round(n_shapes / (ms / 1e3), 1), "pairs": int(m), "contacts": int(oh.sum()),
+        "stage_ms": {"aabbs_and_build": round(split[0] / steps, 4), "pairs": round(split[1] / steps, 4),
+                     "contacts": round(split[2] / steps, 4)},
+        "gpu_launches": int(launches),
+        "matches_oracle": {"pair_set": same_pairs, "has_contact": same_has},
+        "cpu_baseline": {"value": round(1.0 / cpu_s, 3), "unit": "steps/s", "cores": threads, "kind": "port",
+                         "sample": "one full step: oracle shape AABBs, parry binned BVH build, traversal, contacts over all threads"},
+    }
+
+
+def mixed_contacts(ctx, stream, steps: int, n_pairs: int, flush) -> dict:
+    """query::contact on the uneven hull workload with balls, cuboids and capsules mixed in (a shape
+    of each pair is any of the four kinds, hulls of 8-256 vertices): device-resident pairs/s, the
+    oracle check and CPU baseline on a sample."""
+    import numpy as np
+    import torch
+    import parry_gb300 as pg
+    from parry_gb300 import workloads as W
+    from oracle import oracle as O
+
+    s, pairs = W.mixed_contact_pairs(n_pairs)
+    t, prm, pos, pool = s.arrays()
+    dev = tuple(torch.from_numpy(np.ascontiguousarray(a)).cuda() for a in (t.view(np.int32), prm, pos, pool))
+    dpairs = torch.from_numpy(pairs.view(np.int32)).cuda()
+    has = torch.empty(n_pairs, dtype=torch.uint8, device="cuda")
+    res = torch.empty((n_pairs, 13), dtype=torch.float32, device="cuda")
+    pg.contacts(ctx, dev, dpairs, 0.0, out=(has, res))
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    for a, b in ev:
+        flush.zero_()
+        a.record(stream)
+        pg.contacts(ctx, dev, dpairs, 0.0, out=(has, res))
+        b.record(stream)
+    torch.cuda.synchronize()
+    ms = statistics.mean(a.elapsed_time(b) for a, b in ev)
+    sample = min(n_pairs, 131072)
+    threads = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    oh, oo, _ = O.contacts(s, pairs[:sample], 0.0, threads=threads)
+    cpu_s = time.perf_counter() - t0
+    return {"workload": "pairs of balls, cuboids, capsules and 8-256-vertex hulls (uniform kinds), random relative pose, prediction 0",
+            "pairs": n_pairs, "value": round(n_pairs / (ms / 1e3), 1), "unit": "pairs/s", "ms_per_step": round(ms, 4),
+            "contact_fraction": round(float(has.float().mean().item()), 4),
+            "matches_oracle_on_sample": bool(np.array_equal(oh, has[:sample].cpu().numpy())),
+            "cpu_baseline": {"value": round(sample / cpu_s, 1), "unit": "pairs/s", "cores": threads, "kind": "port",
+                             "sample": f"first {sample} pairs"}}
+
+
+def shape_cast_section(ctx, stream, steps: int, n_pairs: int, flush) -> dict:
+    """query::cast_shapes on separated ball / cuboid / capsule / hull pairs closing at 0.5-2 units per
+    unit time (W.shape_cast_pairs, max_toi 100): device-resident pairs/s, oracle check and CPU
+    baseline on a sample."""
+    import numpy as np
+    import torch
+    import parry_gb300 as pg
+    from parry_gb300 import workloads as W
+    from oracle import oracle as O
+
+    s, pairs, vels = W.shape_cast_pairs(n_pairs)
+    t, prm, pos, pool = s.arrays()
+    dev = tuple(torch.from_numpy(np.ascontiguousarray(a)).cuda() for a in (t.view(np.int32), prm, pos, pool))
+    dpairs = torch.from_numpy(pairs.view(np.int32)).cuda()
+    dvel = torch.from_numpy(vels).cuda()
+    st = torch.empty(n_pairs, dtype=torch.uint8, device="cuda")
+    res = torch.empty((n_pairs, 13), dtype=torch.float32, device="cuda")
+    pg.cast_shapes(ctx, dev, dpairs, dvel, max_toi=100.0, out=(st, res))
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    for a, b in ev:
+        flush.zero_()
+        a.record(stream)
+        pg.cast_shapes(ctx, dev, dpairs, dvel, max_toi=100.0, out=(st, res))
+        b.record(stream)
+    torch.cuda.synchronize()
+    ms = statistics.mean(a.elapsed_time(b) for a, b in ev)
+    sample = min(n_pairs, 131072)
+    threads = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    so, oo, _ = O.cast_shapes(s, pairs[:sample], vels, max_toi=100.0, threads=threads)
+    cpu_s = time.perf_counter() - t0
+    got = st[:sample].cpu().numpy()
+    return {"workload": "separated ball/cuboid/capsule/hull(8-256) pairs closing at U[0.5, 2], max_toi 100",
+            "metric": "shape casts/s", "pairs": n_pairs, "value": round(n_pairs / (ms / 1e3), 1), "unit": "pairs/s",
+            "ms_per_step": round(ms, 4), "hit_fraction": round(float((st != 255).float().mean().item()), 4),
+            "matches_oracle_on_sample": bool(np.array_equal(got, so)),
+            "cpu_baseline": {"value": round(sample / cpu_s, 1), "unit": "pairs/s", "cores": threads, "kind": "port",
+                             "sample": f"first {sample} pairs"}}
+
+
 def contacts_section(ctx, stream, steps: int, warmup: int, n_pairs: int, flush) -> dict:
     """Batched query::contact on uneven convex-hull pairs (8-256 vertices, log-uniform), the
     GJK/EPA workload: device-resident pairs/s, end-to-end pairs/s through host buffers, kernel
@@ -277,6 +439,7 @@ def contacts_section(ctx, stream, steps: int, warmup: int, n_pairs: int, flush) 
                          "sample": f"first {sample} pairs; C++ restatement of parry3d f32 query::contact"},
         "matches_oracle_on_sample": same,
         "error_vs_f64_oracle": contacts_f64_error(s, pairs, has.cpu().numpy(), res.cpu().numpy()),
+        "mixed_shapes": mixed_contacts(ctx, stream, steps, n_pairs, flush),
     }
 
 
@@ -717,6 +880,12 @@ def run_gb300(args) -> int:
         manifolds = manifolds_section(ctx, stream, args.steps, args.warmup, args.manifold_pairs, flush)
     if args.scene_frames > 0:
         scene = scene_section(ctx, stream, args.scene_frames, args.warmup, flush, args.scene_shapes, args.scene_rays)
+    shape_cast = None
+    if args.cast_pairs > 0:
+        shape_cast = shape_cast_section(ctx, stream, args.steps, args.cast_pairs, flush)
+    broadphase = None
+    if args.broadphase_shapes > 0:
+        broadphase = broadphase_section(ctx, stream, args.steps, args.warmup, args.broadphase_shapes, flush)
     if args.contact_pairs > 0:
         contacts = contacts_section(ctx, stream, args.steps, args.warmup, args.contact_pairs, flush)
         if args.train_pairs > 0:
@@ -757,6 +926,8 @@ def run_gb300(args) -> int:
             "learned_warm_start": learned,
             "manifolds": manifolds,
             "frame_pipeline": scene,
+            "broadphase": broadphase,
+            "shape_cast": shape_cast,
         }
         print(json.dumps(line), flush=True)
     ctx.close()
@@ -772,6 +943,9 @@ def main() -> int:
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--n-rays", type=int, default=N_RAYS)
+    ap.add_argument("--cast-pairs", type=int, default=1 << 20, help="pairs of the shape-casting section (0 skips it)")
+    ap.add_argument("--broadphase-shapes", type=int, default=131072,
+                    help="balls and cuboids of the broadphase + contact section (0 skips it)")
     ap.add_argument("--contact-pairs", type=int, default=1 << 20,
                     help="hull pairs of the GJK/EPA section (0 skips it)")
     ap.add_argument("--manifold-pairs", type=int, default=1 << 20,

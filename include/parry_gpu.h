@@ -61,7 +61,9 @@ typedef struct parrygpu_config {
                               lanes all hold one ("while-while") */
   uint32_t ray_refill;     /* traversal 2: a warp fetches rays once this many of its lanes are idle
                               (0 = library default, 16; at most 32) */
-  uint32_t reserved[1];
+  uint32_t ray_chunks;     /* host-buffer ray casts without a ray ordering: chunks over two streams
+                              (0 = library default: one per 262,144 rays, 2 to 4; 1 = no chunking; at
+                              most 64) */
 } parrygpu_config;
 
 /* ---- context ---------------------------------------------------------------------------- */
@@ -95,6 +97,10 @@ parrygpu_status parrygpu_reset_kernel_timing(parrygpu_ctx* ctx);
  * stored in the reference's 64-byte BvhNodeWide layout with the root in wide node 0. */
 parrygpu_status parrygpu_bvh_build(parrygpu_ctx* ctx, const float* aabbs, uint32_t n, parrygpu_bvh** out);
 void parrygpu_bvh_destroy(parrygpu_bvh* bvh);
+/* Bvh::from_leaves again into an existing handle (a new tree over `n` AABBs; the handle's device
+ * storage is reused and grows only when n exceeds every earlier size). Asynchronous for device
+ * AABBs, like parrygpu_bvh_build. */
+parrygpu_status parrygpu_bvh_rebuild(parrygpu_ctx* ctx, parrygpu_bvh* bvh, const float* aabbs, uint32_t n);
 /* Replaces Bvh::insert_or_update_partially for every leaf followed by Bvh::refit
  * (src/partitioning/bvh/bvh_insert.rs:209-231, src/partitioning/bvh/bvh_refit.rs:170-180):
  * leaf i takes aabbs[i] and every internal AABB is recomputed bottom-up; topology is kept. */
@@ -358,6 +364,46 @@ uint64_t parrygpu_mlp_param_count(void);
 /* Copies the FP32 master parameters out / in (checkpoint and resume; the BF16 copies follow). */
 parrygpu_status parrygpu_mlp_get_params(parrygpu_ctx* ctx, const parrygpu_mlp* mlp, float* params);
 parrygpu_status parrygpu_mlp_set_params(parrygpu_ctx* ctx, parrygpu_mlp* mlp, const float* params);
+
+/* ---- shape casting (time of impact under translation) ------------------------------------- */
+
+/* ShapeCastOptions (src/query/shape_cast/shape_cast.rs:230-270); the reference's default is
+ * {FLT_MAX, 0, 1, 1}. */
+typedef struct parrygpu_shape_cast_options {
+  float max_time_of_impact;
+  float target_distance;
+  uint32_t stop_at_penetration;
+  uint32_t compute_impact_geometry_on_penetration;
+} parrygpu_shape_cast_options;
+
+/* ShapeCastHit (shape_cast.rs:40-60): witness points and normals in each shape's local frame. */
+typedef struct parrygpu_shape_cast_hit {
+  float time_of_impact;
+  float witness1[3];
+  float witness2[3];
+  float normal1[3];
+  float normal2[3];
+} parrygpu_shape_cast_hit;
+
+/* ShapeCastStatus values written per pair; PARRYGPU_CAST_NONE where the reference returns None. */
+enum {
+  PARRYGPU_CAST_OUT_OF_ITERATIONS = 0,
+  PARRYGPU_CAST_CONVERGED = 1,
+  PARRYGPU_CAST_FAILED = 2,
+  PARRYGPU_CAST_PENETRATING_OR_WITHIN_TARGET_DIST = 3,
+  PARRYGPU_CAST_NONE = 255
+};
+
+/* Replaces a loop of query::cast_shapes(pos_a, vel_a, a, pos_b, vel_b, b, options)
+ * (src/query/shape_cast/shape_cast.rs:275-286 -> DefaultQueryDispatcher::cast_shapes,
+ * src/query/default_query_dispatcher.rs:434-538) over the (a, b) rows of `pairs`, for balls
+ * (cast_shapes_ball_ball) and support-map shapes (cuboid, capsule, convex, triangle:
+ * cast_shapes_support_map_support_map). velocities: one linear velocity per shape (n x 3 floats).
+ * out[k] / status[k] receive the hit of pair k. stats (may be NULL; else the call synchronises)
+ * counts the GJK / EPA work of the penetration contacts. */
+parrygpu_status parrygpu_cast_shapes(parrygpu_ctx* ctx, const parrygpu_shapes* shapes, const uint32_t* pairs, uint64_t n_pairs,
+                                     const float* velocities, const parrygpu_shape_cast_options* options, parrygpu_shape_cast_hit* out,
+                                     uint8_t* status, parrygpu_gjk_stats* stats);
 
 /* ---- Compound (shape set) ray casts ------------------------------------------------------- */
 

@@ -8,6 +8,7 @@
 #include "contact.hpp"
 #include "shape_ray.hpp"
 #include "manifold.hpp"
+#include "shape_cast.hpp"
 #include <thread>
 #include <vector>
 #include <algorithm>
@@ -197,6 +198,41 @@ void contacts(const uint32_t* types, const float* params, const float* poses, co
     stats[0] = gi.load(); stats[1] = ei.load(); stats[2] = ec.load();
     stats[3] = mf.load(); stats[4] = mv.load(); stats[5] = ms.load(); stats[6] = sv.load();
   }
+}
+
+// query::cast_shapes per (a, b) pair; vels = per-shape linear velocities (n x 3). opts = max toi,
+// target distance, stop_at_penetration, compute_impact_geometry_on_penetration. out per pair:
+// toi, witness1, witness2, normal1, normal2 (13 values); status[k] = ShapeCastStatus or 0xff (None).
+template <class R, class O>
+void cast_shapes_batch(const uint32_t* types, const float* params, const float* poses, const float* hullv, uint32_t nhv, uint64_t nshapes,
+                       const uint32_t* pairs, uint64_t npairs, const float* vels, const float* opts, int threads, O* out, uint8_t* status,
+                       uint64_t* stats) {
+  ShapeSet<R> set(types, params, poses, hullv, nhv, nshapes);
+  ShapeCastOptions<R> opt;
+  opt.max_time_of_impact = R(opts[0]);
+  opt.target_distance = R(opts[1]);
+  opt.stop_at_penetration = opts[2] != 0.0f;
+  opt.compute_impact_geometry_on_penetration = opts[3] != 0.0f;
+  std::atomic<uint64_t> gi{0}, ei{0}, ec{0};
+  parallel_for(npairs, threads, [&](uint64_t k) {
+    uint32_t a = pairs[2 * k], b = pairs[2 * k + 1];
+    Vec3<R> v1(R(vels[3 * a]), R(vels[3 * a + 1]), R(vels[3 * a + 2])), v2(R(vels[3 * b]), R(vels[3 * b + 1]), R(vels[3 * b + 2]));
+    ShapeCastHit<R> h;
+    GjkStats st;
+    bool ok = cast_shapes(set.poses[a], v1, set.shapes[a], set.poses[b], v2, set.shapes[b], opt, &h, &st);
+    gi += st.gjk_iters; ei += st.epa_iters; ec += st.epa_calls;
+    O* o = out + 13 * k;
+    if (ok) {
+      o[0] = O(h.toi);
+      const Vec3<R>* v[4] = {&h.witness1, &h.witness2, &h.normal1, &h.normal2};
+      for (int j = 0; j < 4; ++j) { o[1 + 3 * j] = O(v[j]->x); o[2 + 3 * j] = O(v[j]->y); o[3 + 3 * j] = O(v[j]->z); }
+      status[k] = (uint8_t)h.status;
+    } else {
+      for (int j = 0; j < 13; ++j) o[j] = O(0);
+      status[k] = 0xff;
+    }
+  });
+  if (stats) { stats[0] = gi.load(); stats[1] = ei.load(); stats[2] = ec.load(); }
 }
 
 template <class R> Compound<R>* make_compound(const uint32_t* types, const float* params, const float* poses, const float* hullv,
@@ -430,5 +466,16 @@ void oracle_integrate_f32(float* poses, const float* vel, uint64_t n, float dt) 
 uint64_t oracle_pairs_count(void* p) { return ((PairBuf*)p)->v.size() / 2; }
 void oracle_pairs_copy(void* p, uint32_t* out) { std::memcpy(out, ((PairBuf*)p)->v.data(), ((PairBuf*)p)->v.size() * 4); }
 void oracle_pairs_free(void* p) { delete (PairBuf*)p; }
+
+void oracle_cast_shapes_f32(const uint32_t* types, const float* params, const float* poses, const float* hullv, uint32_t nhv,
+                            uint64_t nshapes, const uint32_t* pairs, uint64_t npairs, const float* vels, const float* opts, int threads,
+                            float* out, uint8_t* status, uint64_t* stats) {
+  cast_shapes_batch<float, float>(types, params, poses, hullv, nhv, nshapes, pairs, npairs, vels, opts, threads, out, status, stats);
+}
+void oracle_cast_shapes_f64(const uint32_t* types, const float* params, const float* poses, const float* hullv, uint32_t nhv,
+                            uint64_t nshapes, const uint32_t* pairs, uint64_t npairs, const float* vels, const float* opts, int threads,
+                            double* out, uint8_t* status, uint64_t* stats) {
+  cast_shapes_batch<double, double>(types, params, poses, hullv, nhv, nshapes, pairs, npairs, vels, opts, threads, out, status, stats);
+}
 
 }  // extern "C"

@@ -37,6 +37,8 @@ _SIGS = {
     "oracle_bvh_leaf_pairs_f32": (P, [P, P]),
     "oracle_shape_aabbs_f32": (None, [P, P, P, P, U32, U64, F32, P]),
     "oracle_contacts_f32": (None, [P, P, P, P, U32, U64, P, U64, F32, P, I32, P, P, P]),
+    "oracle_cast_shapes_f32": (None, [P, P, P, P, U32, U64, P, U64, P, P, I32, P, P, P]),
+    "oracle_cast_shapes_f64": (None, [P, P, P, P, U32, U64, P, U64, P, P, I32, P, P, P]),
     "oracle_contacts_f64": (None, [P, P, P, P, U32, U64, P, U64, F32, P, I32, P, P, P]),
     "oracle_compound_new_f32": (P, [P, P, P, P, U32, U64]),
     "oracle_compound_new_f64": (P, [P, P, P, P, U32, U64]),
@@ -207,6 +209,31 @@ def contacts(shapes, pairs: np.ndarray, prediction: float, init_dirs: np.ndarray
     return has, out, {"gjk_iters": int(st[0]), "epa_iters": int(st[1]), "epa_calls": int(st[2]),
                       "epa_max_faces": int(st[3]), "epa_max_verts": int(st[4]), "epa_max_silhouette": int(st[5]),
                       "support_vertices": int(st[6])}
+
+
+def cast_shapes(shapes, pairs: np.ndarray, velocities: np.ndarray, max_toi: float = float(np.finfo(np.float32).max),
+                target_distance: float = 0.0, stop_at_penetration: bool = True, compute_impact_geometry_on_penetration: bool = True,
+                precision: str = "f32", threads: int | None = None):
+    """query::cast_shapes(pos_a, vel_a, a, pos_b, vel_b, b, options) per (a, b) row of `pairs`;
+    velocities = per-shape linear velocities (n, 3).
+
+    Returns (status u8 (k,) = ShapeCastStatus (0 out of iterations, 1 converged, 2 failed,
+    3 penetrating or within target distance) or 255 for None, out (k, 13) = toi, witness1,
+    witness2, normal1, normal2, stats dict)."""
+    t, prm, pos, pool = _shape_arrays(shapes)
+    pairs = np.ascontiguousarray(pairs, np.uint32).reshape(-1, 2)
+    vel = np.ascontiguousarray(velocities, np.float32).reshape(-1, 3)
+    k = len(pairs)
+    dt = np.float32 if precision == "f32" else np.float64
+    out = np.empty((k, 13), dt)
+    status = np.empty(k, np.uint8)
+    st = np.zeros(3, np.uint64)
+    opts = np.array([max_toi, target_distance, 1.0 if stop_at_penetration else 0.0,
+                     1.0 if compute_impact_geometry_on_penetration else 0.0], np.float32)
+    getattr(lib(), f"oracle_cast_shapes_{precision}")(_p(t), _p(prm), _p(pos), _p(pool), len(pool), len(t), _p(pairs), k, _p(vel),
+                                                      _p(opts), threads if threads is not None else default_threads(), _p(out),
+                                                      _p(status), _p(st))
+    return status, out, {"gjk_iters": int(st[0]), "epa_iters": int(st[1]), "epa_calls": int(st[2])}
 
 
 class _PolyIn(C.Structure):

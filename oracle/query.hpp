@@ -94,6 +94,18 @@ template <class R> struct Shape {
       }
     }
   }
+  // SupportMap::local_support_point_toward for a unit direction: the ball and the capsule use it
+  // without renormalising (ball.rs:247-249, capsule.rs:412-418); the others forward to
+  // local_support_point (support_map.rs:302).
+  Vec3<R> local_support_toward(const Vec3<R>& u) const {
+    if (type == SHAPE_BALL) return u * radius;
+    if (type == SHAPE_CAPSULE) {
+      Vec3<R> a(0, -half_height, 0), b(0, half_height, 0);
+      if (dot(u, a) > dot(u, b)) return a + u * radius;
+      return b + u * radius;
+    }
+    return local_support(u);
+  }
   // SupportMap::support_point(transform, dir)
   Vec3<R> support(const Iso<R>& m, const Vec3<R>& dir) const {
     Vec3<R> ld = m.inverse_transform_vector(dir);
@@ -118,11 +130,28 @@ inline thread_local uint64_t g_support_vertices = 0;
 
 template <class R> struct Support {
   const Shape<R>* shape;  // nullptr = ConstantOrigin
+  // RoundShapeRef (round_shape.rs:330-349): support toward the normalised direction plus the
+  // direction times the border radius.
+  bool round = false;
+  R border = R(0);
   static void count(const Shape<R>* s) {
     if (s && (s->type == SHAPE_CONVEX || s->type == SHAPE_TRIANGLE)) g_support_vertices += s->npts;
   }
-  Vec3<R> local(const Vec3<R>& d) const { count(shape); return shape ? shape->local_support(d) : Vec3<R>(); }
-  Vec3<R> world(const Iso<R>& m, const Vec3<R>& d) const { count(shape); return shape ? shape->support(m, d) : m.tra; }
+  Vec3<R> local(const Vec3<R>& d) const {
+    count(shape);
+    if (!shape) return Vec3<R>();
+    if (round) {
+      Vec3<R> u = normalize(d);  // Unit::new_normalize
+      return shape->local_support_toward(u) + u * border;
+    }
+    return shape->local_support(d);
+  }
+  Vec3<R> world(const Iso<R>& m, const Vec3<R>& d) const {
+    if (!shape) { count(shape); return m.tra; }
+    if (round) return m.transform_point(local(m.inverse_transform_vector(d)));
+    count(shape);
+    return shape->support(m, d);
+  }
 };
 
 template <class R>

@@ -114,9 +114,12 @@ template <class R> inline bool ray_toi_with_halfspace(const Vec3<R>& center, con
   return false;
 }
 
-// gjk.rs:660-795 minkowski_ray_cast with pos12 = identity and g2 = ConstantOrigin (cast_local_ray).
+// gjk.rs:660-795 minkowski_ray_cast: ray cast on the Minkowski difference g1 - pos12 * g2. On a hit
+// returns the toi (in units of the ray direction's length) and the normal; `simplex` is left as
+// the reference leaves it (directional_distance reads its witness points).
 template <class R>
-inline bool gjk_cast_local_ray(const Shape<R>& shape, VoronoiSimplex<R>& simplex, const Ray<R>& ray, R max_toi, R* toi_out, Vec3<R>* n_out) {
+inline bool minkowski_ray_cast(const Iso<R>& pos12, const Support<R>& g1, const Support<R>& g2, const Ray<R>& ray, R max_toi,
+                               VoronoiSimplex<R>& simplex, R* toi_out, Vec3<R>* n_out) {
   const R eps_tol = gjk_eps_tol<R>();
   const R eps_rel = std::sqrt(eps_tol);
   R ray_length = norm(ray.dir);
@@ -125,9 +128,7 @@ inline bool gjk_cast_local_ray(const Shape<R>& shape, VoronoiSimplex<R>& simplex
   Ray<R> curr{ray.origin, ray.dir / ray_length};
   Vec3<R> dir = -curr.dir;
   Vec3<R> ldir = dir;
-  Iso<R> id;
-  Support<R> g1{&shape}, g2{nullptr};
-  CSOPoint<R> sp = cso_from_shapes(id, g1, g2, dir);
+  CSOPoint<R> sp = cso_from_shapes(pos12, g1, g2, dir);
   simplex.reset(sp.translate(-curr.origin));
   Vec3<R> proj = simplex.project_origin_and_reduce();
   R max_bound = std::numeric_limits<R>::max();
@@ -144,7 +145,7 @@ inline bool gjk_cast_local_ray(const Shape<R>& shape, VoronoiSimplex<R>& simplex
       last_chance = true;
       support_point = CSOPoint<R>::single_point(proj + curr.origin);
     } else {
-      support_point = cso_from_shapes(id, g1, g2, dir);
+      support_point = cso_from_shapes(pos12, g1, g2, dir);
     }
     if (last_chance && ltoi > R(0)) { *toi_out = ltoi / ray_length; *n_out = ldir; return true; }
     R t;
@@ -174,6 +175,14 @@ inline bool gjk_cast_local_ray(const Shape<R>& shape, VoronoiSimplex<R>& simplex
     niter += 1;
     if (niter == 100) return false;
   }
+}
+
+// gjk.rs:519-534 cast_local_ray: minkowski_ray_cast with pos12 = identity and g2 = ConstantOrigin.
+template <class R>
+inline bool gjk_cast_local_ray(const Shape<R>& shape, VoronoiSimplex<R>& simplex, const Ray<R>& ray, R max_toi, R* toi_out, Vec3<R>* n_out) {
+  Iso<R> id;
+  Support<R> g1{&shape}, g2{nullptr};
+  return minkowski_ray_cast(id, g1, g2, ray, max_toi, simplex, toi_out, n_out);
 }
 
 // ray_support_map.rs:19-71

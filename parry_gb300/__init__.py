@@ -55,7 +55,7 @@ def _as_input(x, dtype):
     if x is None:
         return None, None
     if _is_torch(x):
-        tdt = {np.float32: torch.float32, np.uint32: torch.int32}[dtype]
+        tdt = {np.float32: torch.float32, np.uint32: torch.int32, np.uint8: torch.uint8}[dtype]
         if x.dtype != tdt and not (dtype is np.uint32 and x.dtype in (torch.int32, torch.uint32)):
             x = x.to(tdt)
         x = x.contiguous()
@@ -67,7 +67,7 @@ def _as_input(x, dtype):
 def _alloc_like(ref, shape, dtype):
     """Allocates an output on the same side (numpy / torch CPU / torch CUDA) as `ref`."""
     if _is_torch(ref):
-        tdt = {np.float32: torch.float32, np.uint32: torch.int32}[dtype]
+        tdt = {np.float32: torch.float32, np.uint32: torch.int32, np.uint8: torch.uint8}[dtype]
         pin = ref.device.type == "cpu" and ref.is_pinned()
         t = torch.empty(shape, dtype=tdt, device=ref.device, pin_memory=pin)
         return t, C.c_void_p(t.data_ptr())
@@ -77,14 +77,14 @@ def _alloc_like(ref, shape, dtype):
 
 def _config_dict(cfg) -> dict:
     return {"device": cfg.device, "ray_block": cfg.ray_block, "sort_rays": bool(cfg.sort_rays), "ray_sort_key": cfg.ray_sort_key,
-            "epa_blocks_per_sm": cfg.epa_blocks_per_sm, "ray_traversal": cfg.ray_traversal, "ray_refill": cfg.ray_refill}
+            "epa_blocks_per_sm": cfg.epa_blocks_per_sm, "ray_traversal": cfg.ray_traversal, "ray_refill": cfg.ray_refill, "ray_chunks": cfg.ray_chunks}
 
 
 class Context:
     """A device context (one CUDA stream). Mirrors nothing in parry, which is single-threaded CPU."""
 
     def __init__(self, device: int = 0, ray_block: int = 0, sort_rays: bool = True, ray_sort_key: int = 0,
-                 epa_blocks_per_sm: int = 0, ray_traversal: int = 0, ray_refill: int = 0):
+                 epa_blocks_per_sm: int = 0, ray_traversal: int = 0, ray_refill: int = 0, ray_chunks: int = 0):
         cfg = _capi.ParryGpuConfig()
         lib().parrygpu_default_config(C.byref(cfg))
         cfg.device = device
@@ -94,6 +94,7 @@ class Context:
         cfg.epa_blocks_per_sm = epa_blocks_per_sm
         cfg.ray_traversal = ray_traversal
         cfg.ray_refill = ray_refill
+        cfg.ray_chunks = ray_chunks
         h = C.c_void_p()
         check(lib().parrygpu_create(C.byref(h), C.byref(cfg)))
         self._h = h
@@ -173,6 +174,11 @@ class Bvh:
         check(lib().parrygpu_bvh_build(ctx.handle, p, n, C.byref(h)), ctx.handle)
         return cls(ctx, h)
 
+    def rebuild(self, aabbs) -> None:
+        """Bvh::from_leaves over new AABBs into this handle (its device storage is reused)."""
+        ka, pa = _as_input(aabbs, np.float32)
+        check(lib().parrygpu_bvh_rebuild(self.ctx.handle, self._h, pa, int(ka.shape[0])), self.ctx.handle)
+
     def refit(self, aabbs) -> None:
         """insert_or_update_partially for every leaf, then Bvh::refit (topology kept)."""
         keep, p = _as_input(aabbs, np.float32)
@@ -198,6 +204,17 @@ class Bvh:
         """All intersecting leaf pairs (each unordered pair once) as canonical (min, max) rows."""
         hint = cap_hint if cap_hint is not None else 4 * self.leaf_count()
         return _pairs_call(self.ctx, lib().parrygpu_bvh_self_pairs, (self._h,), sorted, hint)
+
+    def traverse_bvtt_single_tree_into(self, out, sorted: bool = False) -> int:
+        """The same pairs written into `out` ((cap, 2) u32 / int32, host or device); returns the total
+        pair count (raises CAPACITY_EXCEEDED when it is above cap, with the count in the message)."""
+        n = C.c_uint64(0)
+        st = lib().parrygpu_bvh_self_pairs(self.ctx.handle, self._h, C.c_void_p(_dptr(out)), C.c_uint64(int(out.shape[0])), C.byref(n),
+                                           1 if sorted else 0)
+        if st == 3:
+            raise RuntimeError(f"pair capacity {int(out.shape[0])} exceeded: {n.value} pairs")
+        check(st, self.ctx.handle)
+        return int(n.value)
 
     def leaf_pairs(self, other: "Bvh", sorted: bool = True, cap_hint: int | None = None) -> np.ndarray:
         """Bvh::leaf_pairs(&other, aabb-intersection check) as (leaf of self, leaf of other) rows."""
@@ -324,10 +341,13 @@ class _StagedShapes:
         self.ref = kq
 
 
-def shape_aabbs(ctx: Context, shapes, margin: float = 0.0):
+def shape_aabbs(ctx: Context, shapes, margin: float = 0.0, out=None):
     """Shape::compute_aabb(pos).loosened(margin) for every shape: (n, 6) = mins, maxs."""
     st = _StagedShapes(shapes)
-    out, po = _alloc_like(st.ref, (st.n, 6), np.float32)
+    if out is None:
+        out, po = _alloc_like(st.ref, (st.n, 6), np.float32)
+    else:
+        po = C.c_void_p(_dptr(out))
     check(lib().parrygpu_shapes_aabbs(ctx.handle, C.byref(st.struct), float(margin), po), ctx.handle)
     return out
 
@@ -360,6 +380,35 @@ def contacts(ctx: Context, shapes, pairs, prediction: float, init_dirs=None, wan
     if want_stats:
         return has, res, {"gjk_iters": stats.gjk_iterations, "epa_iters": stats.epa_iterations, "epa_calls": stats.epa_calls}
     return has, res
+
+
+CAST_NONE = 255
+
+
+def cast_shapes(ctx: Context, shapes, pairs, velocities, max_toi: float = float(np.finfo(np.float32).max),
+                target_distance: float = 0.0, stop_at_penetration: bool = True, compute_impact_geometry_on_penetration: bool = True,
+                want_stats: bool = False, out=None):
+    """Batched query::cast_shapes over the (a, b) rows of `pairs`; velocities = per-shape linear
+    velocities (n, 3). Returns (status u8 (k,) = ShapeCastStatus or CAST_NONE, hits f32 (k, 13) =
+    toi, witness1, witness2, normal1, normal2 in each shape's local frame) [, stats dict]."""
+    st = _StagedShapes(shapes)
+    kp, pp = _as_input(pairs, np.uint32)
+    kv, pv = _as_input(velocities, np.float32)
+    k = int(kp.shape[0]) if kp is not None else 0
+    if out is None:
+        res, pr = _alloc_like(kp, (k, 13), np.float32)
+        status, ps = _alloc_like(kp, (k,), np.uint8)
+    else:
+        status, res = out
+        ps, pr = C.c_void_p(_dptr(status)), C.c_void_p(_dptr(res))
+    opts = _capi.ParryGpuShapeCastOptions(float(max_toi), float(target_distance), 1 if stop_at_penetration else 0,
+                                          1 if compute_impact_geometry_on_penetration else 0)
+    stats = _capi.ParryGpuGjkStats()
+    check(lib().parrygpu_cast_shapes(ctx.handle, C.byref(st.struct), pp, k, pv, C.byref(opts), pr, ps,
+                                     C.byref(stats) if want_stats else None), ctx.handle)
+    if want_stats:
+        return status, res, {"gjk_iters": stats.gjk_iterations, "epa_iters": stats.epa_iterations, "epa_calls": stats.epa_calls}
+    return status, res
 
 
 def autotune_contacts(ctx: Context, shapes, pairs, prediction: float = 0.0, reps: int = 2) -> dict:

@@ -44,6 +44,7 @@ SIGNATURES: dict[str, tuple] = {
     "parrygpu_kernel_time": (I32, [P, C.c_char_p, C.POINTER(C.c_double), PU64]),
     "parrygpu_reset_kernel_timing": (I32, [P]),
     "parrygpu_bvh_build": (I32, [P, P, U32, C.POINTER(P)]),
+    "parrygpu_bvh_rebuild": (I32, [P, P, P, U32]),
     "parrygpu_bvh_destroy": (None, [P]),
     "parrygpu_bvh_refit": (I32, [P, P, P]),
     "parrygpu_bvh_self_pairs": (I32, [P, P, P, U64, PU64, I32]),
@@ -57,6 +58,7 @@ SIGNATURES: dict[str, tuple] = {
     "parrygpu_shapes_aabbs": (I32, [P, P, F32, P]),
     "parrygpu_contacts": (I32, [P, P, P, U64, F32, P, P, P, P]),
     "parrygpu_get_config": (I32, [P, P]),
+    "parrygpu_cast_shapes": (I32, [P, P, P, U64, P, P, P, P, P]),
     "parrygpu_autotune_trimesh_rays": (I32, [P, P, P, P, U32, F32, U32, P]),
     "parrygpu_autotune_contacts": (I32, [P, P, P, U64, F32, U32, P]),
     "parrygpu_contacts_with_dirs": (I32, [P, P, P, U64, F32, P, P, P, P, P]),
@@ -99,6 +101,11 @@ class ParryGpuShapes(C.Structure):
                 ("vertices", C.c_void_p), ("n_vertices", C.c_uint64), ("polyhedra", C.c_void_p)]
 
 
+class ParryGpuShapeCastOptions(C.Structure):
+    _fields_ = [("max_time_of_impact", C.c_float), ("target_distance", C.c_float), ("stop_at_penetration", C.c_uint32),
+                ("compute_impact_geometry_on_penetration", C.c_uint32)]
+
+
 class ParryGpuGjkStats(C.Structure):
     _fields_ = [("gjk_iterations", C.c_uint64), ("epa_iterations", C.c_uint64), ("epa_calls", C.c_uint64),
                 ("reserved", C.c_uint64)]
@@ -113,7 +120,7 @@ class ParryGpuError(RuntimeError):
 class ParryGpuConfig(C.Structure):
     _fields_ = [("device", C.c_int), ("ray_block", C.c_uint32), ("sort_rays", C.c_uint32), ("ray_sort_key", C.c_uint32),
                 ("epa_blocks_per_sm", C.c_uint32), ("ray_traversal", C.c_uint32), ("ray_refill", C.c_uint32),
-                ("reserved", C.c_uint32 * 1)]
+                ("ray_chunks", C.c_uint32)]
 
 
 _lib = None

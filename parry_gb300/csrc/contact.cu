@@ -231,16 +231,23 @@ __global__ void __launch_bounds__(CT_THREADS) k_contacts_main(ShapeArrays sh, co
   }
 }
 
+// EPA of the queued pairs. Regular pass (BIG = false): queue entries [0, *qcount); a pair whose
+// polytope outgrows the regular slot is appended to `ovf` (its result left to the second pass).
+// Second pass (BIG = true): the entries listed in `ovf` [0, *qcount), on large slots; a pair that
+// outgrows those raises the capacity error.
+template <bool BIG>
 __global__ void __launch_bounds__(EPA_THREADS) k_contacts_epa(ShapeArrays sh, const uint32_t* __restrict__ pairs, float prediction,
                                                               float* __restrict__ out, uint8_t* __restrict__ has,
                                                               const uint32_t* __restrict__ queue, const unsigned long long* __restrict__ qcount,
                                                               uint32_t* __restrict__ ws_pool, unsigned long long* __restrict__ stats,
-                                                              uint32_t* __restrict__ err, float* __restrict__ final_dirs) {
+                                                              uint32_t* __restrict__ err, float* __restrict__ final_dirs,
+                                                              uint32_t* __restrict__ ovf, unsigned long long* __restrict__ ovf_count) {
   const uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x;
-  EpaWs ws = epa_slot(ws_pool, slot);
+  auto ws = [&]() { if constexpr (BIG) return epa_slot_big(ws_pool, slot); else return epa_slot(ws_pool, slot); }();
   const unsigned long long total = *qcount;
   uint32_t iters = 0, calls = 0;
-  for (unsigned long long e = slot; e < total; e += (unsigned long long)gridDim.x * blockDim.x) {
+  for (unsigned long long i = slot; i < total; i += (unsigned long long)gridDim.x * blockDim.x) {
+    const unsigned long long e = BIG ? ovf[i] : i;
     const uint32_t* q = queue + (size_t)e * QUEUE_WORDS;
     uint64_t k = q[0];
     Simplex s;
@@ -255,10 +262,18 @@ __global__ void __launch_bounds__(EPA_THREADS) k_contacts_epa(ShapeArrays sh, co
     ContactOut c;
     bool ok = false;
     V3 p1, p2, nn;
-    calls++;
+    const uint32_t iters0 = iters;
+    // a pair outgrowing the regular slot goes to the second pass: counted there, results written there
+    auto outgrown = [&](int r) {
+      if (r != EPA_OVERFLOW) return false;
+      if (BIG) { atomicOr(err, ERR_POLYTOPE_FULL); return false; }
+      ovf[atomicAdd(ovf_count, 1ull)] = (uint32_t)e;
+      iters = iters0;
+      return true;
+    };
     if (ps.path == PATH_SUPPORT) {
       int r = epa_closest_points(ws, ps.pos12, ps.s1, ps.s2, s, &p1, &p2, &nn, &iters);
-      if (r == EPA_OVERFLOW) atomicOr(err, ERR_POLYTOPE_FULL);
+      if (outgrown(r)) continue;
       if (r == EPA_OK) { ok = true; finish_support_pair(ps.pos12, p1, p2, nn, &c); }
       if (final_dirs) {
         V3 fd = r == EPA_OK ? nn : v3(1.f, 0.f, 0.f);  // GJKResult::NoIntersection(x) when EPA fails
@@ -275,11 +290,12 @@ __global__ void __launch_bounds__(EPA_THREADS) k_contacts_epa(ShapeArrays sh, co
       proj.face = -1;
       proj.inside = true;
       int r = epa_closest_points(ws, minv, cs, origin, s, &p1, &p2, &nn, &iters);
-      if (r == EPA_OVERFLOW) atomicOr(err, ERR_POLYTOPE_FULL);
+      if (outgrown(r)) continue;
       proj.point = r == EPA_OK ? p1 : center;
       ok = finish_convex_ball(ps.cpos, cs, proj, ps.radius, prediction, &c);
       if (ok && ps.path == PATH_BALL_FIRST) flip(&c);
     }
+    calls++;
     write_out(out, has, k, ok, c, ps.pa, ps.pb);
   }
   if (stats) {
@@ -452,7 +468,9 @@ parrygpu_status parrygpu_contacts_with_dirs(parrygpu_ctx* ctx, const parrygpu_sh
   uint32_t epa_blocks = (uint32_t)(ctx->sm_count > 0 ? ctx->sm_count : 152) * epa_per_sm;
   uint32_t slots = epa_blocks * EPA_THREADS;
   PG_CUDA(ctx, ctx->epa_ws.reserve((size_t)slots * EPA_SLOT_BYTES));
-  unsigned long long* ctr = ctx->ct_counters.as<unsigned long long>();  // [0] queue count, [1..3] stats
+  PG_CUDA(ctx, ctx->epa_ws_big.reserve((size_t)EPA_BIG_SLOTS * EPA_BIG_SLOT_BYTES));
+  PG_CUDA(ctx, ctx->ct_ovf.reserve((size_t)n_pairs * 4));
+  unsigned long long* ctr = ctx->ct_counters.as<unsigned long long>();  // [0] queue count, [1..3] stats, [4] overflow count
   PG_CUDA(ctx, cudaMemsetAsync(ctr, 0, 64, ctx->stream));
   // pairs binned by support-scan cost (a 10-bit key, two radix passes)
   const uint32_t* order = nullptr;
@@ -478,9 +496,14 @@ parrygpu_status parrygpu_contacts_with_dirs(parrygpu_ctx* ctx, const parrygpu_sh
   }
   {
     KernelTimer kt(ctx, "contacts_epa");
-    k_contacts_epa<<<epa_blocks, EPA_THREADS, 0, ctx->stream>>>(sh, (const uint32_t*)dp, prediction, (float*)d_out, (uint8_t*)d_has,
-                                                                ctx->ct_queue.as<uint32_t>(), ctr, ctx->epa_ws.as<uint32_t>(), ctr + 1,
-                                                                ctx->d_err, (float*)d_dirs);
+    k_contacts_epa<false><<<epa_blocks, EPA_THREADS, 0, ctx->stream>>>(
+        sh, (const uint32_t*)dp, prediction, (float*)d_out, (uint8_t*)d_has, ctx->ct_queue.as<uint32_t>(), ctr,
+        ctx->epa_ws.as<uint32_t>(), ctr + 1, ctx->d_err, (float*)d_dirs, ctx->ct_ovf.as<uint32_t>(), ctr + 4);
+    PG_LAUNCHED(ctx);
+    // pairs whose polytope outgrew the regular slots, on the large slots (an empty list exits at once)
+    k_contacts_epa<true><<<EPA_BIG_SLOTS / EPA_THREADS, EPA_THREADS, 0, ctx->stream>>>(
+        sh, (const uint32_t*)dp, prediction, (float*)d_out, (uint8_t*)d_has, ctx->ct_queue.as<uint32_t>(), ctr + 4,
+        ctx->epa_ws_big.as<uint32_t>(), ctr + 1, ctx->d_err, (float*)d_dirs, ctx->ct_ovf.as<uint32_t>(), nullptr);
     kt.stop();
     PG_LAUNCHED(ctx);
   }

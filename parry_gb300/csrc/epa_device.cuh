@@ -5,8 +5,10 @@
 // so records are laid out for one lane's accesses. A vertex's CSO point is one 16-byte word group
 // (read with one vector load); its two witness points, used only for the final closest points,
 // sit in a separate array; a face is 8 words, one 32-byte sector. Fixed capacities replace the
-// reference's Vecs; exceeding one aborts the pair and raises a capacity error (observed maxima on
-// 8-256-vertex hull pairs: 239 faces, 55 vertices, silhouettes of 10 edges). The reference's
+// reference's Vecs; exceeding one aborts the pair and raises a capacity error. Vertices are bounded
+// by the 100 expansions (at most 105); faces are not: observed maxima over 1,048,576 pairs are 243
+// faces (8-256-vertex hulls) and 512 (hulls mixed with cuboids, where flat contacts run all 100
+// expansions), so the face capacity is 1,024, with silhouettes of at most 13 edges. The reference's
 // recursive silhouette walk becomes an explicit stack visiting faces in the same order, and its
 // BinaryHeap is restated with the same sift operations so that ties between face distances pop
 // in the same order.
@@ -29,7 +31,7 @@ struct EpaLayout {
   static_assert(W_FACES % 8 == 0 && WORDS % 8 == 0, "faces and slots start on 32-byte boundaries");
 };
 // Per-thread workspaces in global memory.
-using EpaGlobalLayout = EpaLayout<128, 512, 64, 256>;
+using EpaGlobalLayout = EpaLayout<128, 1024, 64, 256>;
 
 constexpr int EPA_MAX_VERTS = EpaGlobalLayout::MAX_VERTS;
 constexpr int EPA_MAX_FACES = EpaGlobalLayout::MAX_FACES;
@@ -74,6 +76,16 @@ struct EpaWsT {
 using EpaWs = EpaWsT<EpaGlobalLayout>;
 // The workspace of slot `slot` in a pool of EPA_WORDS-word slots.
 __device__ __forceinline__ EpaWs epa_slot(uint32_t* pool, uint32_t slot) { return EpaWs{pool + (size_t)slot * EPA_WORDS}; }
+
+// Large workspaces for the few pairs whose polytope outgrows the regular slot (a second pass over
+// those pairs only, on a small pool of these slots).
+using EpaBigLayout = EpaLayout<128, 8192, 64, 1024>;
+using EpaWsBig = EpaWsT<EpaBigLayout>;
+constexpr size_t EPA_BIG_SLOT_BYTES = (size_t)EpaBigLayout::WORDS * 4;
+constexpr uint32_t EPA_BIG_SLOTS = 640;  // 10 blocks of 64 threads: 216 MB
+__device__ __forceinline__ EpaWsBig epa_slot_big(uint32_t* pool, uint32_t slot) {
+  return EpaWsBig{pool + (size_t)slot * EpaBigLayout::WORDS};
+}
 
 template <class WS>
 struct EpaHeap {
@@ -356,7 +368,8 @@ __device__ __forceinline__ int epa_closest_points_t(const WS& ws, Sup sup, const
 }
 
 // The per-thread form over a global-memory slot.
-static __device__ __noinline__ int epa_closest_points(const EpaWs& ws, const Pose& pos12, const ShapeDev& g1, const ShapeDev& g2,
+template <class WS>
+static __device__ __noinline__ int epa_closest_points(const WS& ws, const Pose& pos12, const ShapeDev& g1, const ShapeDev& g2,
                                                       const Simplex& simplex, V3* p1, V3* p2, V3* n, uint32_t* iters) {
   return epa_closest_points_t(ws, [&](V3 d) { return cso_from_shapes(pos12, g1, g2, d); }, simplex, p1, p2, n, iters);
 }

@@ -61,7 +61,7 @@ struct parrygpu_ctx {
   DevBuf sort_k[2], sort_v[2], sort_hist, stage_in[8], stage_out[4], misc, counters, stage_poly[9];
   DevBuf ray_keys, ray_order;
   // contact pipeline scratch: EPA queue (pair + simplex per entry) and per-slot polytope workspaces
-  DevBuf ct_queue, ct_counters, epa_ws;
+  DevBuf ct_queue, ct_counters, epa_ws, epa_ws_big, ct_ovf;
   RayWaveScratch ray_wave;
   MfScratch mf;
   int sm_count = 0;

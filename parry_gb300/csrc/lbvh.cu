@@ -482,6 +482,17 @@ parrygpu_status parrygpu_bvh_build(parrygpu_ctx* ctx, const float* aabbs, uint32
   return PARRYGPU_OK;
 }
 
+parrygpu_status parrygpu_bvh_rebuild(parrygpu_ctx* ctx, parrygpu_bvh* bvh, const float* aabbs, uint32_t n) {
+  if (!ctx || !bvh) return PARRYGPU_INVALID_ARG;
+  PG_CUDA(ctx, cudaSetDevice(ctx->device));
+  const void* d_aabbs = nullptr;
+  parrygpu_status s = stage_input(ctx, ctx->stage_in[0], aabbs, (size_t)n * 24, &d_aabbs);
+  if (s != PARRYGPU_OK) return s;
+  if ((s = lbvh_build(ctx, bvh, (const float*)d_aabbs, n, false)) != PARRYGPU_OK) return s;
+  if (d_aabbs != aabbs) PG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return PARRYGPU_OK;
+}
+
 void parrygpu_bvh_destroy(parrygpu_bvh* b) {
   if (!b) return;
   for (DevBuf* d : {&b->wide, &b->leaf_parent, &b->node_parent, &b->leaf_index, &b->flags, &b->root_aabb, &b->info}) d->release();

@@ -803,7 +803,8 @@ __device__ __forceinline__ bool hull_project_gjk(const ShapeDev& cs, V3 center, 
 // kernel over its bin: warps see one code path, the simple kinds keep few registers, and the
 // instruction cache holds one generator at a time.
 // The polyhedral pairs (contact_manifold_pfm_pfm) are split by shape kinds - cuboid-capsule,
-// cuboid-hull, capsule-hull, hull-hull - so that a warp runs one support and feature path.
+// cuboid-hull, capsule-hull, hull-hull - so that a warp runs one support and feature path; one
+// kernel (k_mf_kind<MK_PFM>) runs the four bins.
 enum : uint32_t {
   MK_BALL_BALL = 0, MK_CUBOID_CUBOID, MK_CAPSULE_CAPSULE, MK_CONVEX_BALL, MK_HULL_BALL,
   MK_PFM, MK_PFM_CUBOID_HULL, MK_PFM_CAPSULE_HULL, MK_PFM_HULL_HULL, MK_KINDS
@@ -860,11 +861,19 @@ __global__ void __launch_bounds__(MF_THREADS) k_mf_kind(ShapeArrays sh, const ui
                                                         uint32_t* __restrict__ recs, const uint32_t* __restrict__ bins, uint64_t stride,
                                                         unsigned long long* __restrict__ ctr, uint32_t* __restrict__ queue,
                                                         uint32_t* __restrict__ err) {
-  const unsigned long long cnt = ctr[MF_CTR_BINS + KIND];
+  // The polyhedral kernel walks its four sub-bins as one index space: warps see one pair kind (but
+  // at the bin boundaries), and one launch keeps the sub-bins' slowest pairs overlapped.
+  constexpr uint32_t LAST = KIND == MK_PFM ? MK_PFM_HULL_HULL : KIND;
+  unsigned long long cnt = 0;
+#pragma unroll
+  for (uint32_t b = KIND; b <= LAST; ++b) cnt += ctr[MF_CTR_BINS + b];
   uint32_t iters = 0;
   for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < cnt;
        i += (unsigned long long)gridDim.x * blockDim.x) {
-    uint64_t k = bins[(size_t)KIND * stride + i];
+    uint32_t bin = KIND;
+    unsigned long long j = i;
+    while (bin < LAST && j >= ctr[MF_CTR_BINS + bin]) { j -= ctr[MF_CTR_BINS + bin]; ++bin; }
+    uint64_t k = bins[(size_t)bin * stride + j];
     Rec r{recs + (size_t)k * MF_WORDS};
     uint32_t a = pairs[2 * k], b = pairs[2 * k + 1];
     ShapeDev s1 = load_shape(sh.types, sh.params, sh.pool, a);
@@ -1032,9 +1041,6 @@ parrygpu_status pg::launch_manifolds(parrygpu_ctx* ctx, const ShapeArrays& sh, c
   if ((s = launch_kind<MK_CONVEX_BALL>(ctx, sh, d_pairs, prediction, d_recs, sc, stride, grid)) != PARRYGPU_OK) return s;
   if ((s = launch_kind<MK_HULL_BALL>(ctx, sh, d_pairs, prediction, d_recs, sc, stride, grid)) != PARRYGPU_OK) return s;
   if ((s = launch_kind<MK_PFM>(ctx, sh, d_pairs, prediction, d_recs, sc, stride, grid)) != PARRYGPU_OK) return s;
-  if ((s = launch_kind<MK_PFM_CUBOID_HULL>(ctx, sh, d_pairs, prediction, d_recs, sc, stride, grid)) != PARRYGPU_OK) return s;
-  if ((s = launch_kind<MK_PFM_CAPSULE_HULL>(ctx, sh, d_pairs, prediction, d_recs, sc, stride, grid)) != PARRYGPU_OK) return s;
-  if ((s = launch_kind<MK_PFM_HULL_HULL>(ctx, sh, d_pairs, prediction, d_recs, sc, stride, grid)) != PARRYGPU_OK) return s;
   k_manifolds_epa<<<epa_blocks, MF_EPA_THREADS, 0, ctx->stream>>>(sh, d_pairs, prediction, d_recs, sc.queue.as<uint32_t>(), ctr,
                                                                  sc.epa_ws.as<uint32_t>(), ctr + 1, ctx->d_err);
   PG_LAUNCHED(ctx);

@@ -121,6 +121,52 @@ def hull_pairs(n_pairs: int, seed: int = 0x9A77E2, nmin: int = 8, nmax: int = 25
     return ShapeSet.from_arrays(types, params, poses.astype(np.float32), pool), pairs
 
 
+def mixed_contact_pairs(n_pairs: int, seed: int = 0x9A77E5, nmin: int = 8, nmax: int = 256):
+    """The uneven GJK/EPA workload with primitives mixed in: each shape of pair k (shapes 2k at the
+    identity and 2k+1 at a random relative pose, as hull_pairs) is, uniformly, a ball (radius
+    log-uniform [0.5, 2]), a cuboid (half extents log-uniform [0.5, 2]), a capsule (half height and
+    radius log-uniform [0.25, 1.5]) or a hull of N ~ log-uniform[nmin, nmax] points on an ellipsoid.
+    Returns (ShapeSet, pairs (n, 2) u32)."""
+    from .shapes import ShapeSet, BALL, CUBOID, CAPSULE, CONVEX
+    n = 2 * n_pairs
+    kinds = (splitmix64(seed, 1, n) % np.uint64(4)).astype(np.uint32)
+    types = np.array([BALL, CUBOID, CAPSULE, CONVEX], np.uint32)[kinds]
+    params = np.zeros((n, 4), np.float32)
+    pu = params.view(np.uint32)
+    ball, cub, cap, cvx = types == BALL, types == CUBOID, types == CAPSULE, types == CONVEX
+    params[ball, 0] = _log_uniform(seed, 2, n, 0.5, 2.0)[ball]
+    for j in range(3):
+        params[cub, j] = _log_uniform(seed, 3 + j, n, 0.5, 2.0)[cub]
+    params[cap, 0] = _log_uniform(seed, 6, n, 0.25, 1.5)[cap]
+    params[cap, 1] = _log_uniform(seed, 7, n, 0.25, 1.5)[cap]
+    hull_ids = np.nonzero(cvx)[0]
+    pool, first, count = ellipsoid_hulls(len(hull_ids), seed, 10, nmin, nmax)
+    pu[hull_ids, 0] = first
+    pu[hull_ids, 1] = count
+    poses = np.zeros((n, 7), np.float64)
+    poses[:, 3] = 1.0
+    poses[1::2, 0:4] = _unit_quats(seed, 20, n_pairs)
+    poses[1::2, 4:7] = _sphere_dirs(seed, 30, n_pairs) * uniform(seed, 32, n_pairs, 0.5, 3.0)[:, None]
+    pairs = np.stack([np.arange(0, n, 2), np.arange(1, n, 2)], axis=1).astype(np.uint32)
+    return ShapeSet.from_arrays(types, params, poses.astype(np.float32), pool), pairs
+
+
+def shape_cast_pairs(n_pairs: int, seed: int = 0x9A77E6, spread: float = 6.0):
+    """Shape-casting workload: the mixed_contact_pairs shapes with the second shape of each pair moved
+    `spread` away in a random direction; per-shape velocities N(0, 0.3^2) per axis, plus, for the
+    second shape, a speed U[0.5, 2] back towards the first. Returns (ShapeSet, pairs (n, 2) u32,
+    velocities (2n, 3) f32)."""
+    from .shapes import ShapeSet
+    s, pairs = mixed_contact_pairs(n_pairs, seed=seed)
+    t, prm, pos, pool = s.arrays()
+    pos = pos.copy()
+    d = _sphere_dirs(seed, 40, n_pairs).astype(np.float32)
+    pos[1::2, 4:7] += spread * d
+    vels = np.stack([uniform(seed, 43 + j, 2 * n_pairs, -0.5, 0.5) for j in range(3)], axis=1).astype(np.float32)
+    vels[1::2] -= d * uniform(seed, 46, n_pairs, 0.5, 2.0)[:, None].astype(np.float32)
+    return ShapeSet.from_arrays(t, prm, pos, pool), pairs, vels
+
+
 def broadphase_shapes(n: int = 131072, extent: float = 200.0, seed: int = 0x9A77E1):
     """Broadphase workload: n shapes, even indices balls (radius log-uniform [0.25, 4]), odd indices
     cuboids (half extents log-uniform [0.25, 4], uniform rotation), centres U([-extent, extent)^3)."""

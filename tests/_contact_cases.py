@@ -150,3 +150,54 @@ def hull_scene(n: int, seed: int, extent: float = 5.0):
             h = (i // 4) % 64
             s.add_convex_hull(pool[first[h]:first[h] + count[h]], poses[i])
     return s, poses
+
+
+def toi_cases():
+    """The reference's time-of-impact tests as (ShapeSet, pairs (k, 2), per-shape velocities (n, 3),
+    expectations): each expectation is ("toi", value), ("toi_rel", value), ("none",) or ("some",)."""
+    s = ShapeSet()
+    pairs, vels, expect = [], [], []
+
+    def add(shape_a, shape_b, va, vb, e):
+        pairs.append((shape_a, shape_b))
+        vels.extend([va, vb])
+        expect.append(e)
+
+    c = KA["toi_ball_ball"]
+    a = s.add_ball(c["radius"], pose7([0, 0, 0]))
+    b = s.add_ball(c["radius"], pose7(c["pos2"]))
+    add(a, b, c["vel1"], c["vel2"], ("toi", c["expect_toi"]))
+    c = KA["toi_ball_triangle_tiny_velocity"]
+    a = s.add_ball(c["radius"], pose7([0, 0, 0]))
+    b = s.add_triangle(*c["triangle"], pose=pose7(c["pos2"]))
+    add(a, b, c["vel1"], c["vel2"], ("none",))
+    c = KA["toi_ball_cuboid"]
+    for case in c["cases"]:
+        a = s.add_ball(c["ball_radius"], pose7(case["ball_pos"]))
+        b = s.add_cuboid(c["cuboid_half_extents"], pose7([0, 0, 0]))
+        if "expect_toi" in case:
+            e = ("toi", case["expect_toi"])
+        elif "expect_toi_relative_eq" in case:
+            dv = np.array(case["ball_vel"]) - np.array(case["cuboid_vel"])
+            e = ("toi_rel", (np.sqrt(3.0) - 1.0) / np.linalg.norm(dv))
+        else:
+            e = ("none",)
+        add(a, b, case["ball_vel"], case["cuboid_vel"], e)
+    c = KA["toi_still_cuboids"]
+    for case in c["cases"]:
+        a = s.add_cuboid(c["half_extents"], pose7(c["pos1"]))
+        b = s.add_cuboid(c["half_extents"], pose7([0, 0, 0]))
+        add(a, b, [0.0, case["v_y"], 0.0], [0.0, 0.0, 0.0], ("none",) if case["expect"] is None else ("some",))
+    return s, np.array(pairs, np.uint32), np.array(vels, np.float32), expect
+
+
+def check_toi(status, out, expect):
+    for k, e in enumerate(expect):
+        if e[0] == "none":
+            assert status[k] == 255, (k, e, status[k])
+        else:
+            assert status[k] != 255, (k, e)
+            if e[0] == "toi":
+                assert out[k, 0] == np.float32(e[1]), (k, out[k, 0], e)
+            elif e[0] == "toi_rel":
+                assert abs(out[k, 0] - e[1]) <= 1e-5 * abs(e[1]), (k, out[k, 0], e)

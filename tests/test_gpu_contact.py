@@ -119,3 +119,24 @@ def test_autotune_contacts_keeps_answers(oracle_lib):
     ho, oo, _ = oracle_lib.contacts(s, pairs, 0.0)
     _compare(has, out, ho, oo, "after autotune")
     ctx.close()
+
+
+def test_mixed_shapes_and_long_epa(gpu_ctx, oracle_lib):
+    """Hulls mixed with balls, cuboids and capsules; includes a capsule-capsule pair whose EPA runs
+    all 100 expansions and builds 512 faces (rounded supports never converge exactly)."""
+    from parry_gb300.shapes import ShapeSet, CAPSULE
+    s, pairs = W.mixed_contact_pairs(200_000, seed=23)
+    has, out, st = pg.contacts(gpu_ctx, s, pairs, 0.0, want_stats=True)
+    ho, oo, sto = oracle_lib.contacts(s, pairs, 0.0)
+    _compare(has, out, ho, oo, "mixed shapes")
+    assert st["epa_iters"] == sto["epa_iters"]
+    types = np.array([CAPSULE, CAPSULE], np.uint32)
+    params = np.array([[0.9470748, 0.28093398, 0, 0], [0.80303407, 0.6510845, 0, 0]], np.float32)
+    poses = np.array([[0, 0, 0, 1, 0, 0, 0],
+                      [-0.30348304, -0.23253627, -0.85818106, 0.3425641, -0.5920257, -0.42291966, -0.22780326]], np.float32)
+    s2 = ShapeSet.from_arrays(types, params, poses)
+    p2 = np.array([[0, 1]], np.uint32)
+    has, out, st = pg.contacts(gpu_ctx, s2, p2, 0.0, want_stats=True)
+    ho, oo, sto = oracle_lib.contacts(s2, p2, 0.0)
+    assert sto["epa_max_faces"] >= 500 and st["epa_iters"] == sto["epa_iters"] == 101
+    _compare(has, out, ho, oo, "capsule pair with 512 EPA faces")

@@ -165,18 +165,18 @@ def test_autotune_keeps_answers(oracle_lib):
 
 
 @pytest.mark.parametrize("kw", [{"ray_block": 48}, {"ray_block": 2048}, {"ray_sort_key": 3}, {"epa_blocks_per_sm": 64},
-                                {"ray_traversal": 4}, {"ray_refill": 33}])
+                                {"ray_traversal": 4}, {"ray_refill": 33}, {"ray_chunks": 65}])
 def test_invalid_config_rejected(kw):
     with pytest.raises(Exception):
         pg.Context(0, **kw)
 
 
-@pytest.mark.parametrize("traversal", [1, 2, 3])
-def test_pipelined_host_buffers(oracle_lib, traversal):
+@pytest.mark.parametrize("traversal,chunks", [(1, 0), (2, 0), (3, 0), (1, 1), (1, 3), (1, 64)])
+def test_pipelined_host_buffers(oracle_lib, traversal, chunks):
     """Host-buffer calls without a ray ordering run in chunks over two streams; pageable, pinned,
     device-in / host-out and toi-only calls all answer as the oracle."""
     import torch
-    ctx = pg.Context(0, sort_rays=False, ray_traversal=traversal)
+    ctx = pg.Context(0, sort_rays=False, ray_traversal=traversal, ray_chunks=chunks)
     v, i = W.terrain_mesh(128, 64, seed=9)
     rays = W.terrain_rays(600_001, 128, 64, seed=9)  # not a multiple of the chunk size
     m = pg.TriMesh(ctx, v, i)
