@@ -341,6 +341,83 @@ def shape_cast_section(ctx, stream, steps: int, n_pairs: int, flush) -> dict:
                              "sample": f"first {sample} pairs"}}
 
 
+def trimesh_contacts_section(ctx, stream, frames: int, warmup: int, n_shapes: int, flush) -> dict:
+    """Contact manifolds of mixed shapes against the 65,536-triangle terrain, frame after frame
+    (contact_manifolds_trimesh_shape with its workspace): ball / cuboid / capsule / hull(16-64)
+    shapes drifting down onto the height field; a step is one frame's update on device-resident
+    shapes. Checked bit-exact against the oracle's frame loop on a sample of shapes, which is also
+    the CPU baseline."""
+    import numpy as np
+    import torch
+    import parry_gb300 as pg
+    from parry_gb300 import workloads as W
+    from parry_gb300.shapes import ShapeSet
+    from oracle import build as ob
+    ob.build()
+    from oracle import oracle as O
+
+    v, i = W.terrain_mesh()
+    t, prm, pos0, pool, poly, _ = W.primitive_pairs(n_shapes // 2, seed=0x9A77E7)
+    n = len(t)
+    rng = np.random.default_rng(7)
+    pos0 = pos0.copy()
+    pos0[:, 4] = rng.uniform(2, 254, n)
+    pos0[:, 6] = rng.uniform(2, 126, n)
+    pos0[:, 5] = rng.uniform(1.0, 6.0, n)
+    vel = np.zeros((n, 3), np.float32)
+    vel[:, 1] = -rng.uniform(0.01, 0.05, n).astype(np.float32)
+    vel[:, 0] = rng.normal(0, 0.01, n).astype(np.float32)
+    total = warmup + frames
+    poses = np.repeat(pos0[None], total, 0)
+    poses[:, :, 4:7] += vel[None] * np.arange(total, dtype=np.float32)[:, None, None]
+    dpos = torch.from_numpy(poses).cuda()
+    hulls, topo = poly
+    dpoly = (torch.from_numpy(hulls.view(np.int32)).cuda(),
+             {k: torch.from_numpy(x.view(np.int32) if x.dtype == np.uint32 else x).cuda() for k, x in topo.items()})
+    dt_, dp_, dpool = (torch.from_numpy(t.view(np.int32)).cuda(), torch.from_numpy(prm).cuda(), torch.from_numpy(pool).cuda())
+    mesh = pg.TriMesh(ctx, v, i)
+    K = 64
+    tc = pg.TriMeshContacts(ctx, mesh, n, K)
+    pred = 0.02
+    for f in range(warmup):
+        tc.update((dt_, dp_, dpos[f], dpool, dpoly), pred)
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(frames)]
+    l0 = ctx.kernel_launches
+    for k, (a, b) in enumerate(ev):
+        flush.zero_()
+        a.record(stream)
+        tc.update((dt_, dp_, dpos[warmup + k], dpool, dpoly), pred)
+        b.record(stream)
+    torch.cuda.synchronize()
+    launches = (ctx.kernel_launches - l0) // max(frames, 1)
+    ms = statistics.mean(a.elapsed_time(b) for a, b in ev)
+    counts, tris, recs = tc.read()
+    active = int(counts.sum())
+    with_points = int(sum((recs[s, :counts[s]]["n_points"] > 0).sum() for s in range(n)))
+    # oracle frame loop on a sample of shapes (the same frames), timed for the CPU baseline
+    sample = min(n, 2048)
+    sel = np.arange(sample)
+    ref = O.TriMeshContacts(v, i, sample)
+    mesh_pose = np.array([0, 0, 0, 1, 0, 0, 0], np.float32)
+    threads = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    for f in range(total):
+        ref.update(mesh_pose, ShapeSet.from_arrays(t[sel], prm[sel], poses[f][sel], pool, poly), pred, threads)
+    cpu_s = (time.perf_counter() - t0) / total
+    same = all(int(counts[s]) == len(ref.inter[s]) and np.array_equal(tris[s, :counts[s]], ref.inter[s]) for s in range(sample))
+    tc.close()
+    mesh.close()
+    return {"workload": f"{n} ball/cuboid/capsule/hull(16-64) shapes drifting onto the 65,536-triangle terrain, prediction {pred}, "
+                        f"at most {K} triangles per shape",
+            "metric": "frames/s", "value": round(1e3 / ms, 2), "unit": "frames/s", "ms_per_frame": round(ms, 4), "frames": frames,
+            "shape_triangle_manifolds": active, "with_points": with_points,
+            "manifold_updates_per_s": round(active / (ms / 1e3), 1), "gpu_launches": int(launches),
+            "interferences_match_oracle_on_sample": bool(same),
+            "cpu_baseline": {"value": round(sample / n / cpu_s, 3), "unit": "frames/s", "cores": threads, "kind": "port",
+                             "sample": f"the first {sample} shapes (one frame scaled to all {n}); C++ manifolds, numpy workspace"}}
+
+
 def contacts_section(ctx, stream, steps: int, warmup: int, n_pairs: int, flush) -> dict:
     """Batched query::contact on uneven convex-hull pairs (8-256 vertices, log-uniform), the
     GJK/EPA workload: device-resident pairs/s, end-to-end pairs/s through host buffers, kernel
@@ -880,6 +957,9 @@ def run_gb300(args) -> int:
         manifolds = manifolds_section(ctx, stream, args.steps, args.warmup, args.manifold_pairs, flush)
     if args.scene_frames > 0:
         scene = scene_section(ctx, stream, args.scene_frames, args.warmup, flush, args.scene_shapes, args.scene_rays)
+    trimesh_contacts = None
+    if args.terrain_shapes > 0:
+        trimesh_contacts = trimesh_contacts_section(ctx, stream, args.steps, args.warmup, args.terrain_shapes, flush)
     shape_cast = None
     if args.cast_pairs > 0:
         shape_cast = shape_cast_section(ctx, stream, args.steps, args.cast_pairs, flush)
@@ -928,6 +1008,7 @@ def run_gb300(args) -> int:
             "frame_pipeline": scene,
             "broadphase": broadphase,
             "shape_cast": shape_cast,
+            "trimesh_contacts": trimesh_contacts,
         }
         print(json.dumps(line), flush=True)
     ctx.close()
@@ -944,6 +1025,7 @@ def main() -> int:
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--n-rays", type=int, default=N_RAYS)
     ap.add_argument("--cast-pairs", type=int, default=1 << 20, help="pairs of the shape-casting section (0 skips it)")
+    ap.add_argument("--terrain-shapes", type=int, default=65536, help="shapes of the TriMesh contact-manifold section (0 skips it)")
     ap.add_argument("--broadphase-shapes", type=int, default=131072,
                     help="balls and cuboids of the broadphase + contact section (0 skips it)")
     ap.add_argument("--contact-pairs", type=int, default=1 << 20,

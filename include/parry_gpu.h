@@ -296,9 +296,13 @@ typedef struct parrygpu_manifold {
  * (src/query/default_query_dispatcher.rs:749-831), updating `manifolds` (n_pairs records, host or
  * device memory) in place: try_update_contacts, then the ball-ball, cuboid-cuboid (SAT + feature
  * clipping), capsule-capsule, convex-ball and polygonal-feature-map (GJK/EPA + clipping) generators,
- * then match_contacts. Zeroed records are ContactManifold::new(). Pairs with a convex polyhedron or
- * triangle get status PARRYGPU_UNSUPPORTED_PAIR and keep their record (the reference's
- * Err(Unsupported) leaves the manifold untouched). stats may be NULL (else the call synchronises). */
+ * then match_contacts; triangles take the convex-ball, cuboid-triangle (SAT + clipping) and
+ * polygonal-feature-map paths. Zeroed records are ContactManifold::new(). Pairs with a shape that has
+ * no generator (a convex hull given without ConvexPolyhedron topology, a segment) get status
+ * PARRYGPU_UNSUPPORTED_PAIR and keep their record (the reference's Err(Unsupported) leaves the
+ * manifold untouched). A row (PARRYGPU_PAIR_NONE, PARRYGPU_PAIR_NONE) is an empty slot: skipped, its
+ * record and status untouched. stats may be NULL (else the call synchronises). */
+#define PARRYGPU_PAIR_NONE 0xFFFFFFFFu
 parrygpu_status parrygpu_contact_manifolds(parrygpu_ctx* ctx, const parrygpu_shapes* shapes, const uint32_t* pairs, uint64_t n_pairs,
                                            float prediction, parrygpu_manifold* manifolds, parrygpu_gjk_stats* stats);
 
@@ -364,6 +368,30 @@ uint64_t parrygpu_mlp_param_count(void);
 /* Copies the FP32 master parameters out / in (checkpoint and resume; the BF16 copies follow). */
 parrygpu_status parrygpu_mlp_get_params(parrygpu_ctx* ctx, const parrygpu_mlp* mlp, float* params);
 parrygpu_status parrygpu_mlp_set_params(parrygpu_ctx* ctx, parrygpu_mlp* mlp, const float* params);
+
+/* ---- contact manifolds against a TriMesh ------------------------------------------------- */
+
+typedef struct parrygpu_trimesh_contacts parrygpu_trimesh_contacts;
+
+/* Replaces, for n_shapes shapes against one TriMesh, the per-pair state of
+ * contact_manifolds_trimesh_shape (src/query/contact_manifolds/contact_manifolds_trimesh_shape.rs:
+ * 82-228): its TriMeshShapeContactManifoldsWorkspace (the shape's AABB in the mesh frame and the
+ * interfering triangles) and one ContactManifold per interfering triangle. Each shape holds at most
+ * max_per_shape triangles at once (more raises PARRYGPU_CAPACITY_EXCEEDED at the next sync). */
+parrygpu_status parrygpu_trimesh_contacts_create(parrygpu_ctx* ctx, const parrygpu_trimesh* mesh, uint32_t n_shapes, uint32_t max_per_shape,
+                                                 parrygpu_trimesh_contacts** out);
+void parrygpu_trimesh_contacts_destroy(parrygpu_trimesh_contacts* contacts);
+/* One frame: for every shape s (shapes->n == n_shapes) the reference's
+ * contact_manifolds_trimesh_shape(dispatcher, mesh_pose^-1 * pose_s, mesh, shape_s, prediction,
+ * manifolds, workspace) with the mesh as shape 1 and no pseudo-normals. mesh_pose7: host pointer to
+ * the mesh pose, NULL = identity. Interfering triangles are kept in ascending index order. */
+parrygpu_status parrygpu_trimesh_contacts_update(parrygpu_ctx* ctx, parrygpu_trimesh_contacts* contacts, const float* mesh_pose7,
+                                                 const parrygpu_shapes* shapes, float prediction);
+/* Copies the current state (host or device buffers; any may be NULL): counts (n_shapes), triangles
+ * (n_shapes x max_per_shape: slot j of shape s is valid for j < counts[s]) and the manifold of each
+ * slot (n_shapes x max_per_shape records; shape 1 of a record is the triangle). Synchronises. */
+parrygpu_status parrygpu_trimesh_contacts_read(parrygpu_ctx* ctx, const parrygpu_trimesh_contacts* contacts, uint32_t* counts,
+                                               uint32_t* triangles, parrygpu_manifold* manifolds);
 
 /* ---- shape casting (time of impact under translation) ------------------------------------- */
 

@@ -409,8 +409,9 @@ void oracle_compound_cast_rays_f64(void* c, const float* pose7, const float* ray
 }
 
 // DefaultQueryDispatcher::contact_manifold_convex_convex per (a, b) row of `pairs`, updating the
-// records in place. Unsupported pairs keep their record and get status 2. stats: gjk_iters,
-// epa_iters, epa_calls, unsupported pairs, largest point count.
+// records in place. Unsupported pairs keep their record and get status 2; a row (0xFFFFFFFF,
+// 0xFFFFFFFF) is an empty slot, skipped with its record untouched. stats: gjk_iters, epa_iters,
+// epa_calls, unsupported pairs, largest point count.
 void oracle_manifolds_f32(const uint32_t* types, const float* params, const float* poses, const float* hullv, uint32_t nhv,
                           uint64_t nshapes, const void* poly, const uint32_t* pairs, uint64_t npairs, float prediction, int threads,
                           uint32_t* records, uint64_t* stats) {
@@ -419,6 +420,7 @@ void oracle_manifolds_f32(const uint32_t* types, const float* params, const floa
   std::atomic<uint64_t> gi{0}, ei{0}, ec{0}, un{0}, mx{0};
   parallel_for(npairs, threads, [&](uint64_t k) {
     uint32_t a = pairs[2 * k], b = pairs[2 * k + 1];
+    if (a == 0xFFFFFFFFu && b == 0xFFFFFFFFu) return;
     uint32_t* r = records + (size_t)MF_WORDS * k;
     Manifold<float> m;
     manifold_load(r, m);
@@ -476,6 +478,17 @@ void oracle_cast_shapes_f64(const uint32_t* types, const float* params, const fl
                             uint64_t nshapes, const uint32_t* pairs, uint64_t npairs, const float* vels, const float* opts, int threads,
                             double* out, uint8_t* status, uint64_t* stats) {
   cast_shapes_batch<double, double>(types, params, poses, hullv, nhv, nshapes, pairs, npairs, vels, opts, threads, out, status, stats);
+}
+
+// pos1^-1 * pos2 for one pose1 and n poses2 (Isometry::inv_mul), as pose7.
+void oracle_inv_mul_f32(const float* pose1, const float* poses2, uint64_t n, float* out) {
+  Iso<float> p1 = Iso<float>::from_pose7(pose1);
+  for (uint64_t i = 0; i < n; ++i) {
+    Iso<float> r = p1.inv_mul(Iso<float>::from_pose7(poses2 + 7 * i));
+    float* o = out + 7 * i;
+    o[0] = r.rot.i; o[1] = r.rot.j; o[2] = r.rot.k; o[3] = r.rot.w;
+    o[4] = r.tra.x; o[5] = r.tra.y; o[6] = r.tra.z;
+  }
 }
 
 }  // extern "C"

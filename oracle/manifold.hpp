@@ -188,6 +188,43 @@ template <class R> inline PolyFeature<R> segment_feature(R hh) {
   return f;
 }
 
+// PolygonalFeature::from(Triangle) (polygonal_feature3d.rs:37-47): the whole triangle, whatever the
+// direction (Triangle::support_face, triangle.rs:280-282; polygonal_feature_map.rs:36-40).
+template <class R> inline PolyFeature<R> triangle_feature(const Shape<R>& s) {
+  PolyFeature<R> f;
+  f.vertices[0] = s.pts[0]; f.vertices[1] = s.pts[1]; f.vertices[2] = s.pts[2]; f.vertices[3] = s.pts[2];
+  const uint32_t ids[4] = {0, 1, 2, 2};
+  for (int i = 0; i < 4; ++i) { f.vids[i] = pfid_vertex(ids[i]); f.eids[i] = pfid_edge(ids[i]); }
+  f.fid = pfid_face(0);
+  f.num_vertices = 3;
+  return f;
+}
+
+// approx::relative_eq with f32::EPSILON (or f64) as both the absolute and relative epsilon.
+template <class R> inline bool relative_eq_scalar(R a, R b) {
+  if (a == b) return true;
+  if (std::isinf(a) || std::isinf(b)) return false;
+  R d = std::fabs(a - b);
+  if (d <= eps_default<R>()) return true;
+  R largest = std::fabs(b) > std::fabs(a) ? std::fabs(b) : std::fabs(a);
+  return d <= largest * eps_default<R>();
+}
+template <class R> inline bool relative_eq_v3(const Vec3<R>& a, const Vec3<R>& b) {
+  return relative_eq_scalar(a.x, b.x) && relative_eq_scalar(a.y, b.y) && relative_eq_scalar(a.z, b.z);
+}
+
+// Triangle::project_local_point_and_get_feature (point_triangle.rs:26-48, 3-D: solid location,
+// is_inside = relative_eq!(projection, point) by compute_result :5-18, OnSolid inside).
+template <class R> inline uint32_t triangle_projection_feature(const Shape<R>& s, const Vec3<R>& pt, Vec3<R>* proj, bool* inside) {
+  Loc<R> loc;
+  *proj = project_triangle(s.pts[0], s.pts[1], s.pts[2], pt, &loc);
+  if (loc.kind == LOC_SOLID) { *inside = true; return pfid_face(0); }
+  *inside = relative_eq_v3(*proj, pt);
+  if (loc.kind == LOC_VERTEX) return pfid_vertex((uint32_t)loc.id);
+  if (loc.kind == LOC_EDGE) return pfid_edge((uint32_t)loc.id);
+  return pfid_face((uint32_t)loc.id);
+}
+
 // ConvexPolyhedron::local_support_feature (convex_polyhedron.rs:959-991): the face whose normal has
 // the largest dot product with dir (first on ties), at most its first 4 vertices.
 template <class R> inline PolyFeature<R> hull_support_feature(const Shape<R>& s, const Vec3<R>& dir) {
@@ -495,6 +532,7 @@ inline void manifold_convex_ball(const Iso<R>& pos12, const Shape<R>& s1, R radi
   bool inside;
   uint32_t fid1;
   if (s1.type == SHAPE_CUBOID) fid1 = cuboid_projection_feature(s1.half, lp21, &proj, &inside);
+  else if (s1.type == SHAPE_TRIANGLE) fid1 = triangle_projection_feature(s1, lp21, &proj, &inside);
   else if (s1.type == SHAPE_CAPSULE) {
     PointProj<R> p = project_capsule(s1.half_height, s1.radius, lp21);
     proj = p.point; inside = p.is_inside; fid1 = pfid_face(0);
@@ -589,6 +627,101 @@ template <class R> inline void manifold_cuboid_cuboid(const Iso<R>& pos12, const
   m.match_contacts(old);
 }
 
+// sat_cuboid_support_map.rs:54-73 with a triangle as the support map.
+template <class R>
+inline std::pair<R, Vec3<R>> sat_cuboid_triangle_normal_oneway(const Vec3<R>& he1, const Shape<R>& tri2, const Iso<R>& pos12) {
+  R best = -std::numeric_limits<R>::max();
+  Vec3<R> best_dir;
+  for (int i = 0; i < 3; ++i) {
+    for (R sign : {R(-1), R(1)}) {
+      Vec3<R> axis1;
+      axis1[i] = sign;
+      Vec3<R> pt2 = tri2.support(pos12, -axis1);  // support_point_toward(pos12, -axis1)
+      R sep = pt2[i] * sign - he1[i];
+      if (sep > best) { best = sep; best_dir = axis1; }
+    }
+  }
+  return {best, best_dir};
+}
+
+// sat_cuboid_point.rs point_cuboid_find_local_separating_normal_oneway (the triangle's first vertex
+// and normal against the cuboid, in the triangle's frame).
+template <class R>
+inline std::pair<R, Vec3<R>> sat_point_cuboid_normal_oneway(const Vec3<R>& point1, bool has_normal, const Vec3<R>& normal1, const Vec3<R>& he2,
+                                                            const Iso<R>& pos12) {
+  R best = -std::numeric_limits<R>::max();
+  Vec3<R> best_dir;
+  if (has_normal) {
+    Vec3<R> axis1 = dot(pos12.tra - point1, normal1) >= R(0) ? normal1 : -normal1;
+    Shape<R> cub;
+    cub.type = SHAPE_CUBOID;
+    cub.half = he2;
+    Vec3<R> pt2 = cub.support(pos12, -axis1);
+    R sep = dot(pt2 - point1, axis1);
+    if (sep > best) { best = sep; best_dir = axis1; }
+  }
+  return {best, best_dir};
+}
+
+// sat_cuboid_triangle.rs cuboid_triangle_find_local_separating_edge_twoway (3-D)
+template <class R>
+inline std::pair<R, Vec3<R>> sat_cuboid_triangle_edge_twoway(const Vec3<R>& he1, const Shape<R>& tri2, const Iso<R>& pos12) {
+  Vec3<R> a = pos12.transform_point(tri2.pts[0]), b = pos12.transform_point(tri2.pts[1]), c = pos12.transform_point(tri2.pts[2]);
+  Vec3<R> ab = b - a, bc = c - b, ca = a - c;
+  const Vec3<R> axes[9] = {Vec3<R>(0, -ab.z, ab.y), Vec3<R>(ab.z, 0, -ab.x), Vec3<R>(-ab.y, ab.x, 0),
+                           Vec3<R>(0, -bc.z, bc.y), Vec3<R>(bc.z, 0, -bc.x), Vec3<R>(-bc.y, bc.x, 0),
+                           Vec3<R>(0, -ca.z, ca.y), Vec3<R>(ca.z, 0, -ca.x), Vec3<R>(-ca.y, ca.x, 0)};
+  R best = -std::numeric_limits<R>::max();
+  Vec3<R> best_axis = axes[0];
+  Shape<R> cub;
+  cub.type = SHAPE_CUBOID;
+  cub.half = he1;
+  for (int i = 0; i < 9; ++i) {
+    const Vec3<R>& axis = axes[i];
+    R d0 = dot(axis, a), d1 = i < 6 ? dot(axis, c) : dot(axis, b);
+    R n2 = norm_squared(axis);
+    if (n2 > eps_default<R>()) {
+      R n = std::sqrt(n2);
+      Vec3<R> pt1 = cub.local_support(axis);
+      R dot1 = dot(pt1, axis) / n;
+      R mn = d0 > d1 ? d1 : d0, mx = d0 > d1 ? d0 : d1;  // utils::sort2
+      R sep_a = mn / n - dot1;
+      R sep_b = -mx / n - dot1;
+      if (sep_a > best) { best = sep_a; best_axis = axis / n; }
+      if (sep_b > best) { best = sep_b; best_axis = -axis / n; }
+    }
+  }
+  return {best, best_axis};
+}
+
+// contact_manifolds_cuboid_triangle.rs:57-174 (no normal constraints): the cuboid is shape 1 of
+// the SAT; `flipped` when the triangle is the manifold's first shape.
+template <class R>
+inline void manifold_cuboid_triangle(const Iso<R>& pos12, const Iso<R>& pos21, const Vec3<R>& he1, const Shape<R>& tri2, R prediction,
+                                     Manifold<R>& m, bool flipped) {
+  if ((!flipped && m.try_update_contacts(pos12)) || (flipped && m.try_update_contacts(pos21))) return;
+  auto sep1 = sat_cuboid_triangle_normal_oneway(he1, tri2, pos12);
+  if (sep1.first > prediction) { m.points.clear(); return; }
+  Vec3<R> tn;
+  bool has_n = try_normalize(cross(tri2.pts[1] - tri2.pts[0], tri2.pts[2] - tri2.pts[0]), eps_default<R>(), &tn);
+  auto sep2 = sat_point_cuboid_normal_oneway(tri2.pts[0], has_n, tn, he1, pos21);
+  if (sep2.first > prediction) { m.points.clear(); return; }
+  auto sep3 = sat_cuboid_triangle_edge_twoway(he1, tri2, pos12);
+  if (sep3.first > prediction) { m.points.clear(); return; }
+  Vec3<R> normal1 = sep1.second;
+  if (sep2.first > sep1.first && sep2.first > sep3.first) normal1 = pos12.transform_vector(-sep2.second);
+  else if (sep3.first > sep1.first) normal1 = sep3.second;
+  Vec3<R> normal2 = pos21.transform_vector(-normal1);
+  PolyFeature<R> f1 = cuboid_support_face(he1, normal1);
+  PolyFeature<R> f2 = triangle_feature(tri2);
+  auto old = m.points;
+  m.points.clear();
+  feature_contacts(pos12, normal1, f1, f2, m, flipped);
+  if (flipped) { m.local_n1 = normal2; m.local_n2 = normal1; }
+  else { m.local_n1 = normal1; m.local_n2 = normal2; }
+  m.match_contacts(old);
+}
+
 // contact_manifolds_pfm_pfm.rs:44-162 for cuboids and capsules (capsule = segment + border radius);
 // no normal constraints.
 template <class R> inline void manifold_pfm_pfm(const Iso<R>& pos12, const Shape<R>& s1, const Shape<R>& s2, R prediction, Manifold<R>& m,
@@ -615,6 +748,7 @@ template <class R> inline void manifold_pfm_pfm(const Iso<R>& pos12, const Shape
     auto feature_of = [](const Shape<R>& s, const Vec3<R>& d) {
       if (s.type == SHAPE_CUBOID) return cuboid_support_face(s.half, d);
       if (s.type == SHAPE_CONVEX) return hull_support_feature(s, d);
+      if (s.type == SHAPE_TRIANGLE) return triangle_feature(s);
       return segment_feature(s.half_height);
     };
     PolyFeature<R> f1 = feature_of(s1, n1), f2 = feature_of(s2, n2);
@@ -637,17 +771,21 @@ template <class R> inline void manifold_pfm_pfm(const Iso<R>& pos12, const Shape
   m.match_contacts(old);
 }
 
-// DefaultQueryDispatcher::contact_manifold_convex_convex for balls, cuboids and capsules.
-// Returns false (Unsupported) for other shapes.
+// DefaultQueryDispatcher::contact_manifold_convex_convex (default_query_dispatcher.rs:749-831) for
+// balls, cuboids, capsules, triangles and convex polyhedra (no normal constraints). Returns false
+// (Unsupported) for other shapes.
 template <class R>
 inline bool contact_manifold_convex_convex(const Iso<R>& pos12, const Shape<R>& s1, const Shape<R>& s2, R prediction, Manifold<R>& m,
                                            GjkStats* st = nullptr) {
   auto ok = [](const Shape<R>& s) {
-    return s.type == SHAPE_BALL || s.type == SHAPE_CUBOID || s.type == SHAPE_CAPSULE || (s.type == SHAPE_CONVEX && s.topo && s.topo->n_faces);
+    return s.type == SHAPE_BALL || s.type == SHAPE_CUBOID || s.type == SHAPE_CAPSULE || s.type == SHAPE_TRIANGLE ||
+           (s.type == SHAPE_CONVEX && s.topo && s.topo->n_faces);
   };
   if (!ok(s1) || !ok(s2)) return false;
   if (s1.type == SHAPE_BALL && s2.type == SHAPE_BALL) manifold_ball_ball(pos12, s1.radius, s2.radius, prediction, m);
   else if (s1.type == SHAPE_CUBOID && s2.type == SHAPE_CUBOID) manifold_cuboid_cuboid(pos12, s1.half, s2.half, prediction, m);
+  else if (s1.type == SHAPE_CUBOID && s2.type == SHAPE_TRIANGLE) manifold_cuboid_triangle(pos12, pos12.inverse(), s1.half, s2, prediction, m, false);
+  else if (s1.type == SHAPE_TRIANGLE && s2.type == SHAPE_CUBOID) manifold_cuboid_triangle(pos12.inverse(), pos12, s2.half, s1, prediction, m, true);
   else if (s1.type == SHAPE_CAPSULE && s2.type == SHAPE_CAPSULE)
     manifold_capsule_capsule(pos12, s1.half_height, s1.radius, s2.half_height, s2.radius, prediction, m);
   else if (s1.type == SHAPE_BALL) manifold_convex_ball(pos12.inverse(), s2, s1.radius, prediction, m, true, st);

@@ -38,6 +38,7 @@ _SIGS = {
     "oracle_shape_aabbs_f32": (None, [P, P, P, P, U32, U64, F32, P]),
     "oracle_contacts_f32": (None, [P, P, P, P, U32, U64, P, U64, F32, P, I32, P, P, P]),
     "oracle_cast_shapes_f32": (None, [P, P, P, P, U32, U64, P, U64, P, P, I32, P, P, P]),
+    "oracle_inv_mul_f32": (None, [P, P, U64, P]),
     "oracle_cast_shapes_f64": (None, [P, P, P, P, U32, U64, P, U64, P, P, I32, P, P, P]),
     "oracle_contacts_f64": (None, [P, P, P, P, U32, U64, P, U64, F32, P, I32, P, P, P]),
     "oracle_compound_new_f32": (P, [P, P, P, P, U32, U64]),
@@ -282,6 +283,105 @@ def contact_manifolds(shapes, pairs: np.ndarray, prediction: float, records: np.
     del keep
     return {"gjk_iters": int(st[0]), "epa_iters": int(st[1]), "epa_calls": int(st[2]), "unsupported": int(st[3]),
             "max_points": int(st[4])}
+
+
+def inv_mul(pose1: np.ndarray, poses2: np.ndarray) -> np.ndarray:
+    """Isometry::inv_mul: pose1^-1 * pose2 for each row of poses2 (pose7, f32)."""
+    p1 = np.ascontiguousarray(pose1, np.float32).reshape(7)
+    p2 = np.ascontiguousarray(poses2, np.float32).reshape(-1, 7)
+    out = np.empty_like(p2)
+    lib().oracle_inv_mul_f32(_p(p1), _p(p2), len(p2), _p(out))
+    return out
+
+
+def _with_triangles(shapes, tri_vertices: np.ndarray, mesh_pose: np.ndarray):
+    """The shapes followed by one Triangle shape per mesh triangle (vertices appended to the pool,
+    posed at the mesh pose): triangle t has shape index n + t."""
+    from parry_gb300.shapes import ShapeSet, TRIANGLE
+    t, prm, pos, pool = shapes.arrays()
+    n, nt = len(t), len(tri_vertices)
+    first = np.arange(nt, dtype=np.uint32) * 3 + np.uint32(len(pool))
+    tp = np.zeros((nt, 4), np.float32)
+    tp.view(np.uint32)[:, 0] = first
+    tp.view(np.uint32)[:, 1] = 3
+    poly = shapes.polyhedra()
+    if poly is not None:
+        hulls, topo = poly
+        topo = dict(topo)
+        topo["vertex_ranges"] = np.concatenate([topo["vertex_ranges"], np.zeros((3 * nt, 2), np.uint32)])
+        poly = (hulls, topo)
+    return ShapeSet.from_arrays(np.concatenate([t, np.full(nt, TRIANGLE, np.uint32)]), np.concatenate([prm, tp]),
+                                np.concatenate([pos, np.repeat(np.asarray(mesh_pose, np.float32).reshape(1, 7), nt, 0)]),
+                                np.concatenate([pool, tri_vertices.reshape(-1, 3)]), poly)
+
+
+class TriMeshContacts:
+    """contact_manifolds_trimesh_shape (contact_manifolds_trimesh_shape.rs:82-228) for each shape of a
+    set against one TriMesh (the mesh is shape 1; no pseudo-normals, so no normal constraints),
+    frame after frame, with the reference's workspace: the shape's AABB in the mesh frame loosened by
+    the prediction, kept while it still contains the new one (else enlarged by min(extent / 10, 0.1)
+    per axis and the triangles whose AABBs intersect it queried again), and one ContactManifold per
+    interfering triangle carried over by triangle id. Interferences are kept in ascending triangle
+    order: the reference's carry-over loop walks old and new lists as sorted lists, and its BVH
+    returns them in tree order, which depends on the tree (a deviation recorded as D-8)."""
+
+    def __init__(self, vertices: np.ndarray, indices: np.ndarray, n_shapes: int):
+        v = np.ascontiguousarray(vertices, np.float32).reshape(-1, 3)
+        i = np.ascontiguousarray(indices, np.uint32).reshape(-1, 3)
+        self.tri = np.ascontiguousarray(v[i], np.float32)  # (nt, 3, 3)
+        # aabb_triangle.rs: a.min(b).min(c), a.max(b).max(c)
+        self.tri_min = np.minimum(np.minimum(self.tri[:, 0], self.tri[:, 1]), self.tri[:, 2])
+        self.tri_max = np.maximum(np.maximum(self.tri[:, 0], self.tri[:, 1]), self.tri[:, 2])
+        # Sweep index on x: triangles sorted by their AABB's min x; a query [lo, hi] on x can only
+        # meet triangles whose min x lies in [lo - widest x extent, hi]. The answer is the same set
+        # of triangles as the reference's BVH query (AABB intersection), found faster.
+        self.sweep = np.argsort(self.tri_min[:, 0], kind="stable")
+        self.sweep_x = self.tri_min[self.sweep, 0]
+        self.widest_x = float((self.tri_max[:, 0] - self.tri_min[:, 0]).max()) if len(self.tri) else 0.0
+        big = np.float32(np.finfo(np.float32).max)
+        self.aabb = np.concatenate([np.full((n_shapes, 3), big, np.float32), np.full((n_shapes, 3), -big, np.float32)], 1)
+        self.inter = [np.zeros(0, np.uint32) for _ in range(n_shapes)]
+        self.records = [empty_manifolds(0) for _ in range(n_shapes)]
+
+    def update(self, mesh_pose: np.ndarray, shapes, prediction: float, threads: int | None = None) -> dict:
+        t, prm, pos, pool = shapes.arrays()
+        n = len(t)
+        rel = inv_mul(mesh_pose, pos)
+        nb = shape_aabbs(shapes.with_poses(rel), prediction)  # compute_aabb(pos12).loosened(prediction)
+        f0, f1 = np.float32(0.1), np.float32(10.0)
+        for s in range(n):
+            mins, maxs = nb[s, :3].copy(), nb[s, 3:].copy()
+            same = bool(np.all(self.aabb[s, :3] <= mins) and np.all(self.aabb[s, 3:] >= maxs))
+            if same:
+                continue
+            extra = np.minimum((maxs - mins) / f1, f0)
+            mins, maxs = mins - extra, maxs + extra
+            a = np.searchsorted(self.sweep_x, np.float64(mins[0]) - self.widest_x, "left")
+            b = np.searchsorted(self.sweep_x, maxs[0], "right")
+            cand = self.sweep[a:b]
+            hit = np.all(self.tri_min[cand] <= maxs, 1) & np.all(self.tri_max[cand] >= mins, 1)
+            new = np.sort(cand[hit]).astype(np.uint32)
+            old, old_rec = self.inter[s], self.records[s]
+            rec = empty_manifolds(len(new))
+            j = np.searchsorted(old, new)
+            found = (j < len(old)) & (old[np.minimum(j, max(len(old) - 1, 0))] == new) if len(old) else np.zeros(len(new), bool)
+            rec[found] = old_rec[j[found]]
+            self.inter[s], self.records[s] = new, rec
+            self.aabb[s, :3], self.aabb[s, 3:] = mins, maxs
+        combined = _with_triangles(shapes, self.tri, mesh_pose)
+        counts = [len(x) for x in self.inter]
+        if sum(counts) == 0:
+            return {"pairs": 0}
+        pairs = np.concatenate([np.stack([self.inter[s] + np.uint32(n), np.full(counts[s], s, np.uint32)], 1)
+                                for s in range(n) if counts[s]]).astype(np.uint32)
+        recs = np.ascontiguousarray(np.concatenate([self.records[s] for s in range(n) if counts[s]]))
+        st = contact_manifolds(combined, pairs, prediction, recs, threads)
+        k = 0
+        for s in range(n):
+            self.records[s] = recs[k:k + counts[s]].copy()
+            k += counts[s]
+        st["pairs"] = int(len(pairs))
+        return st
 
 
 class Compound:

@@ -382,6 +382,47 @@ def contacts(ctx: Context, shapes, pairs, prediction: float, init_dirs=None, wan
     return has, res
 
 
+class TriMeshContacts:
+    """contact_manifolds_trimesh_shape for n_shapes shapes against one TriMesh, frame after frame
+    (the workspace and the per-triangle ContactManifolds live on the device). update() runs one
+    frame; read() returns (counts (n,), triangles (n, K) u32, manifolds (n, K) MANIFOLD_DTYPE),
+    slot j of shape s valid for j < counts[s]; shape 1 of each manifold is the triangle."""
+
+    def __init__(self, ctx: Context, mesh: TriMesh, n_shapes: int, max_per_shape: int = 64):
+        self.ctx, self.mesh, self.n, self.k = ctx, mesh, int(n_shapes), int(max_per_shape)
+        h = C.c_void_p()
+        check(lib().parrygpu_trimesh_contacts_create(ctx.handle, mesh._h, self.n, self.k, C.byref(h)), ctx.handle)
+        self._h = h
+
+    def update(self, shapes, prediction: float, mesh_pose=None) -> None:
+        st = _StagedShapes(shapes)
+        pp = None
+        if mesh_pose is not None:
+            self._pose = np.ascontiguousarray(mesh_pose, np.float32).reshape(7)
+            pp = C.c_void_p(self._pose.ctypes.data)
+        check(lib().parrygpu_trimesh_contacts_update(self.ctx.handle, self._h, pp, C.byref(st.struct), float(prediction)), self.ctx.handle)
+        self._staged = st  # keep device inputs alive until the next update
+
+    def read(self):
+        counts = np.empty(self.n, np.uint32)
+        tris = np.empty((self.n, self.k), np.uint32)
+        recs = np.zeros(self.n * self.k, MANIFOLD_DTYPE)
+        check(lib().parrygpu_trimesh_contacts_read(self.ctx.handle, self._h, C.c_void_p(counts.ctypes.data), C.c_void_p(tris.ctypes.data),
+                                                   C.c_void_p(recs.ctypes.data)), self.ctx.handle)
+        return counts, tris, recs.reshape(self.n, self.k)
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            lib().parrygpu_trimesh_contacts_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 CAST_NONE = 255
 
 

@@ -59,6 +59,10 @@ SIGNATURES: dict[str, tuple] = {
     "parrygpu_contacts": (I32, [P, P, P, U64, F32, P, P, P, P]),
     "parrygpu_get_config": (I32, [P, P]),
     "parrygpu_cast_shapes": (I32, [P, P, P, U64, P, P, P, P, P]),
+    "parrygpu_trimesh_contacts_create": (I32, [P, P, U32, U32, C.POINTER(P)]),
+    "parrygpu_trimesh_contacts_destroy": (None, [P]),
+    "parrygpu_trimesh_contacts_update": (I32, [P, P, P, P, F32]),
+    "parrygpu_trimesh_contacts_read": (I32, [P, P, P, P, P]),
     "parrygpu_autotune_trimesh_rays": (I32, [P, P, P, P, U32, F32, U32, P]),
     "parrygpu_autotune_contacts": (I32, [P, P, P, U64, F32, U32, P]),
     "parrygpu_contacts_with_dirs": (I32, [P, P, P, U64, F32, P, P, P, P, P]),

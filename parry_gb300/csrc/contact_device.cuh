@@ -168,6 +168,39 @@ parrygpu_status stage_shapes(parrygpu_ctx* ctx, const parrygpu_shapes* s, ShapeA
 
 // Launchers on device buffers, no allocation and no host synchronisation (graph-capturable):
 // Shape::compute_aabb(pos).loosened(margin) for n shapes (contact.cu);
+// Shape::compute_aabb(pos) (aabb_ball.rs:7-33, aabb_cuboid.rs:9-14 with isometry_ops.rs:16-18,
+// aabb_capsule.rs:8-20, aabb_utils.rs:58-86 for a point cloud).
+__device__ __forceinline__ void shape_world_aabb(const ShapeDev& s, const Pose& p, V3* mn, V3* mx) {
+  if (s.type == SH_BALL) {
+    *mn = p.t + v3(-s.a, -s.a, -s.a);
+    *mx = p.t + v3(s.a, s.a, s.a);
+  } else if (s.type == SH_CUBOID) {
+    // |R| h with R = to_rotation_matrix (isometry_ops.rs:14-19), row r = (|m_r0| hx + |m_r1| hy) + |m_r2| hz
+    float ww = p.qw * p.qw, ii = p.qi * p.qi, jj = p.qj * p.qj, kk = p.qk * p.qk;
+    float ij = p.qi * p.qj * 2.0f, wk = p.qw * p.qk * 2.0f, wj = p.qw * p.qj * 2.0f;
+    float ik = p.qi * p.qk * 2.0f, jk = p.qj * p.qk * 2.0f, wi = p.qw * p.qi * 2.0f;
+    float m00 = ww + ii - jj - kk, m01 = ij - wk, m02 = wj + ik;
+    float m10 = wk + ij, m11 = ww - ii + jj - kk, m12 = jk - wi;
+    float m20 = ik - wj, m21 = wi + jk, m22 = ww - ii - jj + kk;
+    V3 he = v3((fabsf(m00) * s.a + fabsf(m01) * s.b) + fabsf(m02) * s.c, (fabsf(m10) * s.a + fabsf(m11) * s.b) + fabsf(m12) * s.c,
+               (fabsf(m20) * s.a + fabsf(m21) * s.b) + fabsf(m22) * s.c);
+    *mn = p.t - he;
+    *mx = p.t + he;
+  } else if (s.type == SH_CAPSULE) {
+    V3 a = pose_point(p, v3(0.f, -s.a, 0.f)), b = pose_point(p, v3(0.f, s.a, 0.f));
+    *mn = vmin(a, b) - v3(s.b, s.b, s.b);
+    *mx = vmax(a, b) + v3(s.b, s.b, s.b);
+  } else {
+    *mn = pose_point(p, ldv(s.pts));
+    *mx = *mn;
+    for (uint32_t j = 1; j < s.npts; ++j) {
+      V3 q = pose_point(p, ldv(s.pts + 3 * j));
+      *mn = vmin(*mn, q);
+      *mx = vmax(*mx, q);
+    }
+  }
+}
+
 parrygpu_status launch_shape_aabbs(parrygpu_ctx* ctx, const ShapeArrays& sh, uint64_t n, float margin, float* d_out);
 // contact manifolds of the first min(cap, *d_count) pairs (manifold.cu) with caller-owned scratch
 // sized by manifolds_reserve(cap).

@@ -252,6 +252,41 @@ __device__ __forceinline__ PolyFeature segment_feature(float hh) {
   return f;
 }
 
+// PolygonalFeature::from(Triangle) (polygonal_feature3d.rs:37-47): the whole triangle whatever the
+// direction (Triangle::support_face, triangle.rs:280-282).
+__device__ __forceinline__ PolyFeature triangle_feature(const ShapeDev& s) {
+  PolyFeature f;
+  f.v[0] = ldv(s.pts); f.v[1] = ldv(s.pts + 3); f.v[2] = ldv(s.pts + 6); f.v[3] = f.v[2];
+  const uint32_t ids[4] = {0u, 1u, 2u, 2u};
+#pragma unroll
+  for (int i = 0; i < 4; ++i) { f.vids[i] = pf_vertex(ids[i]); f.eids[i] = pf_edge(ids[i]); }
+  f.fid = pf_face(0);
+  f.nv = 3;
+  return f;
+}
+
+// approx::relative_eq (f32::EPSILON absolute and relative) on each component.
+__device__ __forceinline__ bool relative_eq_f(float a, float b) {
+  if (a == b) return true;
+  if (isinf(a) || isinf(b)) return false;
+  float d = fabsf(a - b);
+  if (d <= EPS) return true;
+  float largest = fabsf(b) > fabsf(a) ? fabsf(b) : fabsf(a);
+  return d <= largest * EPS;
+}
+
+// Triangle::project_local_point_and_get_feature (point_triangle.rs:26-48, 3-D): the solid location,
+// is_inside = relative_eq!(projection, point) (compute_result, :5-18), OnSolid inside.
+__device__ __forceinline__ uint32_t triangle_projection_feature(const ShapeDev& s, V3 pt, V3* proj, bool* inside) {
+  Loc loc;
+  *proj = project_triangle(ldv(s.pts), ldv(s.pts + 3), ldv(s.pts + 6), pt, &loc);
+  if (loc.kind == LOC_SOLID) { *inside = true; return pf_face(0); }
+  *inside = relative_eq_f(proj->x, pt.x) && relative_eq_f(proj->y, pt.y) && relative_eq_f(proj->z, pt.z);
+  if (loc.kind == LOC_VERTEX) return pf_vertex((uint32_t)loc.id);
+  if (loc.kind == LOC_EDGE) return pf_edge((uint32_t)loc.id);
+  return pf_face((uint32_t)loc.id);
+}
+
 // One ConvexPolyhedron's topology (hull-local ids); see parrygpu_polyhedra.
 struct HullDev {
   const float* face_normals;    // this hull's faces x 3
@@ -626,7 +661,7 @@ __device__ __forceinline__ void finish_convex_ball(const Rec& r, const Pose& pos
   }
 }
 
-// contact_manifold_convex_ball for a cuboid or capsule shape 1: analytic projection.
+// contact_manifold_convex_ball for a cuboid, capsule or triangle shape 1: analytic projection.
 __device__ __forceinline__ void mf_convex_ball(const Rec& r, const Pose& pos12, const ShapeDev& s1, float radius2, float prediction,
                                                bool flipped) {
   V3 lp21 = pos12.t;
@@ -636,6 +671,8 @@ __device__ __forceinline__ void mf_convex_ball(const Rec& r, const Pose& pos12, 
     V3 he = v3(s1.a, s1.b, s1.c);
     p = project_cuboid(he, lp21);
     fid1 = cuboid_projection_feature(he, p);
+  } else if (s1.type == SH_TRIANGLE) {
+    fid1 = triangle_projection_feature(s1, lp21, &p.point, &p.inside);
   } else {
     p = project_capsule(s1.a, s1.b, lp21);
     fid1 = pf_face(0);
@@ -724,6 +761,102 @@ static __device__ __noinline__ void mf_cuboid_cuboid(const Rec& r, const Pose& p
   *overflow |= wr.overflow;
 }
 
+// sat::cuboid_support_map_find_local_separating_normal_oneway (sat_cuboid_support_map.rs:54-73)
+// with triangle 2 as the support map (support_point_toward = pos12 * local support).
+__device__ __forceinline__ float sat_cuboid_triangle_normal_oneway(V3 he1, const ShapeDev& tri2, const Pose& pos12, V3* best_dir) {
+  float best = -FLT_MAX;
+  V3 bd = v3(0.f, 0.f, 0.f);
+  const float h[3] = {he1.x, he1.y, he1.z};
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+      float sign = k == 0 ? -1.0f : 1.0f;
+      V3 axis1 = v3(i == 0 ? sign : 0.0f, i == 1 ? sign : 0.0f, i == 2 ? sign : 0.0f);
+      V3 pt2 = world_support(tri2, pos12, -axis1);
+      float sep = comp(pt2, i) * sign - h[i];
+      if (sep > best) { best = sep; bd = axis1; }
+    }
+  }
+  *best_dir = bd;
+  return best;
+}
+
+// sat::point_cuboid_find_local_separating_normal_oneway (sat_cuboid_point.rs) with the triangle's
+// first vertex and normal (triangle_cuboid_find_local_separating_normal_oneway, 3-D).
+__device__ __forceinline__ float sat_triangle_cuboid_normal_oneway(const ShapeDev& tri1, V3 he2, const Pose& pos12, V3* best_dir) {
+  float best = -FLT_MAX;
+  V3 bd = v3(0.f, 0.f, 0.f);
+  V3 a = ldv(tri1.pts), b = ldv(tri1.pts + 3), c = ldv(tri1.pts + 6);
+  V3 n;
+  if (try_normalize(cross(b - a, c - a), EPS, &n)) {  // Triangle::normal
+    V3 axis1 = dot(pos12.t - a, n) >= 0.0f ? n : -n;
+    V3 pt2 = pose_point(pos12, cuboid_support(he2, pose_inv_rotate(pos12, -axis1)));
+    float sep = dot(pt2 - a, axis1);
+    if (sep > best) { best = sep; bd = axis1; }
+  }
+  *best_dir = bd;
+  return best;
+}
+
+// sat::cuboid_triangle_find_local_separating_edge_twoway (sat_cuboid_triangle.rs, 3-D)
+static __device__ __noinline__ float sat_cuboid_triangle_edge_twoway(V3 he1, const ShapeDev& tri2, const Pose& pos12, V3* best_dir) {
+  V3 a = pose_point(pos12, ldv(tri2.pts)), b = pose_point(pos12, ldv(tri2.pts + 3)), c = pose_point(pos12, ldv(tri2.pts + 6));
+  V3 ab = b - a, bc = c - b, ca = a - c;
+  V3 axes[9] = {v3(0.0f, -ab.z, ab.y), v3(ab.z, 0.0f, -ab.x), v3(-ab.y, ab.x, 0.0f),
+                v3(0.0f, -bc.z, bc.y), v3(bc.z, 0.0f, -bc.x), v3(-bc.y, bc.x, 0.0f),
+                v3(0.0f, -ca.z, ca.y), v3(ca.z, 0.0f, -ca.x), v3(-ca.y, ca.x, 0.0f)};
+  float best = -FLT_MAX;
+  V3 bd = axes[0];
+#pragma unroll 1
+  for (int i = 0; i < 9; ++i) {
+    V3 axis = axes[i];
+    float d0 = dot(axis, a), d1 = i < 6 ? dot(axis, c) : dot(axis, b);
+    float n2 = dot(axis, axis);
+    if (n2 > EPS) {
+      float n = sqrtf(n2);
+      float dot1 = dot(cuboid_support(he1, axis), axis) / n;
+      float mn = d0 > d1 ? d1 : d0, mx = d0 > d1 ? d0 : d1;  // utils::sort2
+      float sep_a = mn / n - dot1;
+      float sep_b = -mx / n - dot1;
+      if (sep_a > best) { best = sep_a; bd = axis / n; }
+      if (sep_b > best) { best = sep_b; bd = -axis / n; }
+    }
+  }
+  *best_dir = bd;
+  return best;
+}
+
+// contact_manifold_cuboid_triangle (contact_manifolds_cuboid_triangle.rs:57-174, no normal
+// constraints): the cuboid is shape 1 of the SAT; `flipped` when the triangle is the record's first
+// shape (pos12: cuboid frame to triangle frame).
+static __device__ __noinline__ void mf_cuboid_triangle(const Rec& r, const Pose& pos12, const Pose& pos21, V3 he1, const ShapeDev& tri2,
+                                                       float prediction, bool flipped, bool* overflow) {
+  if (try_update_contacts(r, flipped ? pos21 : pos12, COS_1_DEGREES, 1.0e-6f)) return;
+  V3 d1, d2, d3;
+  float sep1 = sat_cuboid_triangle_normal_oneway(he1, tri2, pos12, &d1);
+  if (sep1 > prediction) { r.w[0] = 0; return; }
+  float sep2 = sat_triangle_cuboid_normal_oneway(tri2, he1, pos21, &d2);
+  if (sep2 > prediction) { r.w[0] = 0; return; }
+  float sep3 = sat_cuboid_triangle_edge_twoway(he1, tri2, pos12, &d3);
+  if (sep3 > prediction) { r.w[0] = 0; return; }
+  V3 normal1 = d1;
+  if (sep2 > sep1 && sep2 > sep3) normal1 = pose_rotate(pos12, -d2);
+  else if (sep3 > sep1) normal1 = d3;
+  V3 normal2 = pose_rotate(pos21, -normal1);
+  PolyFeature f1 = cuboid_support_face(he1, normal1);
+  PolyFeature f2 = triangle_feature(tri2);
+  OldPts old;
+  save_old(r, old);
+  Writer wr{r, 0, false};
+  feature_contacts(pos12, normal1, f1, f2, wr, flipped);
+  r.w[0] = wr.n;
+  if (flipped) set_normals(r, normal2, normal1);
+  else set_normals(r, normal1, normal2);
+  match_contacts(r, wr.n, old);
+  *overflow |= wr.overflow;
+}
+
 // The shape contact_manifold_pfm_pfm works on (a capsule is its segment plus a border radius).
 __device__ __forceinline__ ShapeDev pfm_of(const ShapeDev& s, float* border) {
   ShapeDev p = s;
@@ -735,6 +868,7 @@ __device__ __forceinline__ ShapeDev pfm_of(const ShapeDev& s, float* border) {
 __device__ __forceinline__ PolyFeature support_feature(const ShapeDev& s, const HullDev& h, V3 dir, bool* bad) {
   if (s.type == SH_CUBOID) return cuboid_support_face(v3(s.a, s.b, s.c), dir);
   if (s.type == SH_CONVEX) return hull_support_feature(s, h, dir, bad);
+  if (s.type == SH_TRIANGLE) return triangle_feature(s);
   return segment_feature(s.a);
 }
 
@@ -770,11 +904,11 @@ static __device__ __noinline__ void finish_pfm(const Rec& r, const Pose& pos12, 
   *overflow |= wr.overflow;
 }
 
-// Pair kinds with a manifold generator here: balls, cuboids, capsules, and convex shapes that carry
-// ConvexPolyhedron topology.
+// Pair kinds with a manifold generator here: balls, cuboids, capsules, triangles, and convex shapes
+// that carry ConvexPolyhedron topology.
 __device__ __forceinline__ bool has_generator(const ShapeArrays& sh, uint32_t i, HullDev* h) {
   uint32_t t = sh.types[i];
-  if (t == SH_BALL || t == SH_CUBOID || t == SH_CAPSULE) return true;
+  if (t == SH_BALL || t == SH_CUBOID || t == SH_CAPSULE || t == SH_TRIANGLE) return true;
   return t == SH_CONVEX && load_hull(sh, i, h);
 }
 
@@ -803,11 +937,12 @@ __device__ __forceinline__ bool hull_project_gjk(const ShapeDev& cs, V3 center, 
 // kernel over its bin: warps see one code path, the simple kinds keep few registers, and the
 // instruction cache holds one generator at a time.
 // The polyhedral pairs (contact_manifold_pfm_pfm) are split by shape kinds - cuboid-capsule,
-// cuboid-hull, capsule-hull, hull-hull - so that a warp runs one support and feature path; one
-// kernel (k_mf_kind<MK_PFM>) runs the four bins.
+// cuboid-hull, capsule-hull, hull-hull, any with a triangle - so that a warp runs one support and
+// feature path; one kernel (k_mf_kind<MK_PFM>) runs the five bins. Cuboid-triangle pairs have their
+// own generator (SAT, contact_manifolds_cuboid_triangle.rs).
 enum : uint32_t {
   MK_BALL_BALL = 0, MK_CUBOID_CUBOID, MK_CAPSULE_CAPSULE, MK_CONVEX_BALL, MK_HULL_BALL,
-  MK_PFM, MK_PFM_CUBOID_HULL, MK_PFM_CAPSULE_HULL, MK_PFM_HULL_HULL, MK_KINDS
+  MK_PFM, MK_PFM_CUBOID_HULL, MK_PFM_CAPSULE_HULL, MK_PFM_HULL_HULL, MK_PFM_TRIANGLE, MK_CUBOID_TRIANGLE, MK_KINDS
 };
 // counters: [0] EPA queue length, [1..3] GJK / EPA stats, [4 + kind] bin lengths
 constexpr int MF_CTR_BINS = 4;
@@ -818,6 +953,8 @@ __device__ __forceinline__ uint32_t manifold_kind(uint32_t t1, uint32_t t2) {
   if (t1 == SH_CUBOID && t2 == SH_CUBOID) return MK_CUBOID_CUBOID;
   if (t1 == SH_CAPSULE && t2 == SH_CAPSULE) return MK_CAPSULE_CAPSULE;
   if (t1 == SH_BALL || t2 == SH_BALL) return (t1 == SH_CONVEX || t2 == SH_CONVEX) ? MK_HULL_BALL : MK_CONVEX_BALL;
+  if ((t1 == SH_CUBOID && t2 == SH_TRIANGLE) || (t1 == SH_TRIANGLE && t2 == SH_CUBOID)) return MK_CUBOID_TRIANGLE;
+  if (t1 == SH_TRIANGLE || t2 == SH_TRIANGLE) return MK_PFM_TRIANGLE;
   const bool h1 = t1 == SH_CONVEX, h2 = t2 == SH_CONVEX;
   if (h1 && h2) return MK_PFM_HULL_HULL;
   if (h1 || h2) return (h1 ? t2 : t1) == SH_CUBOID ? MK_PFM_CUBOID_HULL : MK_PFM_CAPSULE_HULL;
@@ -825,7 +962,7 @@ __device__ __forceinline__ uint32_t manifold_kind(uint32_t t1, uint32_t t2) {
 }
 
 // Status of each pair (invalid / unsupported records keep their content) and its bin, appended with
-// warp-aggregated atomics. `d_n` (may be null) holds a device-side pair count: min(n, *d_n) pairs.
+// warp-aggregated atomics. A pair (PARRYGPU_PAIR_NONE, PARRYGPU_PAIR_NONE) is an empty slot: skipped. `d_n` (may be null) holds a device-side pair count: min(n, *d_n) pairs.
 __global__ void __launch_bounds__(MF_THREADS) k_mf_classify(ShapeArrays sh, const uint32_t* __restrict__ pairs, uint64_t n,
                                                             uint32_t* __restrict__ recs, uint32_t* __restrict__ bins, uint64_t stride,
                                                             unsigned long long* __restrict__ ctr, uint32_t* __restrict__ err,
@@ -837,7 +974,9 @@ __global__ void __launch_bounds__(MF_THREADS) k_mf_classify(ShapeArrays sh, cons
     Rec r{recs + (size_t)k * MF_WORDS};
     uint32_t a = pairs[2 * k], b = pairs[2 * k + 1];
     HullDev h1, h2;
-    if (!valid_pair(sh, a, b)) {
+    if (a == PARRYGPU_PAIR_NONE && b == PARRYGPU_PAIR_NONE) {
+      // an empty slot of a fixed-capacity pair list: no query, the record is left untouched
+    } else if (!valid_pair(sh, a, b)) {
       atomicOr(err, ERR_BAD_INDEX);
       r.w[1] = PARRYGPU_INVALID_ARG;
     } else if (!has_generator(sh, a, &h1) || !has_generator(sh, b, &h2)) {
@@ -861,9 +1000,9 @@ __global__ void __launch_bounds__(MF_THREADS) k_mf_kind(ShapeArrays sh, const ui
                                                         uint32_t* __restrict__ recs, const uint32_t* __restrict__ bins, uint64_t stride,
                                                         unsigned long long* __restrict__ ctr, uint32_t* __restrict__ queue,
                                                         uint32_t* __restrict__ err) {
-  // The polyhedral kernel walks its four sub-bins as one index space: warps see one pair kind (but
+  // The polyhedral kernel walks its five sub-bins as one index space: warps see one pair kind (but
   // at the bin boundaries), and one launch keeps the sub-bins' slowest pairs overlapped.
-  constexpr uint32_t LAST = KIND == MK_PFM ? MK_PFM_HULL_HULL : KIND;
+  constexpr uint32_t LAST = KIND == MK_PFM ? MK_PFM_TRIANGLE : KIND;
   unsigned long long cnt = 0;
 #pragma unroll
   for (uint32_t b = KIND; b <= LAST; ++b) cnt += ctr[MF_CTR_BINS + b];
@@ -886,6 +1025,9 @@ __global__ void __launch_bounds__(MF_THREADS) k_mf_kind(ShapeArrays sh, const ui
       mf_cuboid_cuboid(r, pos12, v3(s1.a, s1.b, s1.c), v3(s2.a, s2.b, s2.c), prediction, &overflow);
     } else if constexpr (KIND == MK_CAPSULE_CAPSULE) {
       mf_capsule_capsule(r, pos12, s1.a, s1.b, s2.a, s2.b, prediction);
+    } else if constexpr (KIND == MK_CUBOID_TRIANGLE) {
+      if (s1.type == SH_CUBOID) mf_cuboid_triangle(r, pos12, pose_inverse(pos12), v3(s1.a, s1.b, s1.c), s2, prediction, false, &overflow);
+      else mf_cuboid_triangle(r, pose_inverse(pos12), pos12, v3(s2.a, s2.b, s2.c), s1, prediction, true, &overflow);
     } else if constexpr (KIND == MK_CONVEX_BALL) {
       bool ball_first = s1.type == SH_BALL;
       mf_convex_ball(r, ball_first ? pose_inverse(pos12) : pos12, ball_first ? s2 : s1, ball_first ? s1.a : s2.a, prediction, ball_first);
@@ -925,7 +1067,7 @@ __global__ void __launch_bounds__(MF_THREADS) k_mf_kind(ShapeArrays sh, const ui
     if (overflow) atomicOr(err, ERR_CAPACITY);
     if (bad) atomicOr(err, ERR_BAD_INDEX);
   }
-  if (KIND >= MK_HULL_BALL) {
+  if (KIND >= MK_HULL_BALL && KIND != MK_CUBOID_TRIANGLE) {
     uint32_t w = __reduce_add_sync(0xffffffffu, iters);
     if ((threadIdx.x & 31) == 0 && w) atomicAdd(&ctr[1], (unsigned long long)w);
   }
@@ -1041,6 +1183,7 @@ parrygpu_status pg::launch_manifolds(parrygpu_ctx* ctx, const ShapeArrays& sh, c
   if ((s = launch_kind<MK_CONVEX_BALL>(ctx, sh, d_pairs, prediction, d_recs, sc, stride, grid)) != PARRYGPU_OK) return s;
   if ((s = launch_kind<MK_HULL_BALL>(ctx, sh, d_pairs, prediction, d_recs, sc, stride, grid)) != PARRYGPU_OK) return s;
   if ((s = launch_kind<MK_PFM>(ctx, sh, d_pairs, prediction, d_recs, sc, stride, grid)) != PARRYGPU_OK) return s;
+  if ((s = launch_kind<MK_CUBOID_TRIANGLE>(ctx, sh, d_pairs, prediction, d_recs, sc, stride, grid)) != PARRYGPU_OK) return s;
   k_manifolds_epa<<<epa_blocks, MF_EPA_THREADS, 0, ctx->stream>>>(sh, d_pairs, prediction, d_recs, sc.queue.as<uint32_t>(), ctr,
                                                                  sc.epa_ws.as<uint32_t>(), ctr + 1, ctx->d_err);
   PG_LAUNCHED(ctx);

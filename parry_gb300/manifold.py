@@ -25,6 +25,7 @@ import numpy as np
 
 MAX_POINTS = 24
 RECORD_WORDS = 8 + 10 * MAX_POINTS
+PAIR_NONE = 0xFFFFFFFF  # a pair row (PAIR_NONE, PAIR_NONE) is an empty slot: skipped, record untouched
 
 STATUS_OK = 0
 STATUS_UNSUPPORTED = 2

@@ -125,6 +125,27 @@ def test_unsupported_and_invalid(gpu_ctx, oracle_lib):
     assert r["status"][0] == 1  # PARRYGPU_INVALID_ARG
 
 
+def test_empty_slots_skipped(gpu_ctx, oracle_lib):
+    """Rows (PAIR_NONE, PAIR_NONE) of a fixed-capacity pair list are skipped: their records (status
+    included) stay as they were, the other rows match the oracle."""
+    import parry_gb300 as pg
+    O = oracle_lib
+    t, p, q = primitive_scene(400, 5, extent=4.0)
+    shapes = ShapeSet.from_arrays(t, p, q)
+    pairs = brute_force_pairs(O.shape_aabbs(shapes, 0.2)).copy()
+    assert len(pairs) > 20
+    empty = np.arange(0, len(pairs), 3)
+    pairs[empty] = M.PAIR_NONE
+    g, w = M.new_manifolds(len(pairs)), M.new_manifolds(len(pairs))
+    for r in (g, w):
+        r["n_points"][empty] = 5
+        r["status"][empty] = 77
+    _both(O, pg, gpu_ctx, shapes, pairs, 0.02, g, w)
+    assert np.all(g["n_points"][empty] == 5) and np.all(g["status"][empty] == 77)
+    assert_records_equal(g, w)
+    assert (g["n_points"] > 0).sum() > len(empty)
+
+
 @pytest.mark.parametrize("seed", [3, 4])
 def test_hull_frames_bit_exact(gpu_ctx, oracle_lib, seed):
     """Scenes with ConvexPolyhedron hulls (16-64 points) next to balls, cuboids and capsules, over
@@ -149,3 +170,40 @@ def test_hull_frames_bit_exact(gpu_ctx, oracle_lib, seed):
         vals = np.arange(len(pairs) * M.MAX_POINTS, dtype=np.float32).reshape(-1, M.MAX_POINTS) * 0.25 + f
         g["points"]["data"] = vals
         w["points"]["data"] = vals
+
+
+def test_triangle_pairs_frames_bit_exact(gpu_ctx, oracle_lib):
+    """Triangles of a height field (as Triangle shapes at the mesh pose) against balls, cuboids,
+    capsules and hulls settling onto them, over several frames: convex-ball with triangle
+    features, cuboid-triangle SAT, polyhedral pairs with the triangle face."""
+    import parry_gb300 as pg
+    from parry_gb300 import workloads as W
+    O = oracle_lib
+    v, i = W.terrain_mesh(48, 24, seed=13)
+    t, prm, pos, pool, poly, _ = W.primitive_pairs(300, seed=17)
+    n = len(t)
+    rng = np.random.default_rng(17)
+    pos = pos.copy()
+    pos[:, 4] = rng.uniform(1, 47, n)
+    pos[:, 6] = rng.uniform(1, 23, n)
+    pos[:, 5] = rng.uniform(0.5, 5.0, n)
+    mesh_pose = np.array([0.0, 0.0, 0.0, 1.0, 0.3, -0.2, 0.1], np.float32)
+    tri = np.ascontiguousarray(v[i], np.float32)
+    shapes = O._with_triangles(ShapeSet.from_arrays(t, prm, pos, pool, poly), tri, mesh_pose)
+    aabbs = O.shape_aabbs(shapes, 0.05)
+    a_s, a_t = aabbs[:n], aabbs[n:]
+    hit = np.all(a_s[:, None, :3] <= a_t[None, :, 3:], 2) & np.all(a_s[:, None, 3:] >= a_t[None, :, :3], 2)
+    si, ti = np.nonzero(hit)
+    pairs = np.stack([ti + n, si], 1).astype(np.uint32)
+    kinds = {int(t[s]) for s in si}
+    assert kinds == {0, 1, 2, 3} and len(pairs) > 2000
+    g, w = M.new_manifolds(len(pairs)), M.new_manifolds(len(pairs))
+    for f in range(4):
+        pf = pos.copy()
+        pf[:, 5] -= 0.08 * f
+        fs = O._with_triangles(ShapeSet.from_arrays(t, prm, pf, pool, poly), tri, mesh_pose)
+        pg.contact_manifolds(gpu_ctx, fs, pairs, 0.05, g)
+        O.contact_manifolds(fs, pairs, 0.05, M.as_words(w))
+        assert_records_equal(g, w)
+        assert np.all(g["status"] == M.STATUS_OK)
+        assert (g["n_points"] > 0).sum() > 200

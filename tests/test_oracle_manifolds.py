@@ -91,7 +91,8 @@ def test_cuboid_stack_doc_test(oracle_lib):
 
 
 def test_unsupported_pairs_leave_record(oracle_lib):
-    """Hulls and triangles have no manifold generator here: status Unsupported, record untouched."""
+    """A convex vertex cloud without ConvexPolyhedron topology has no manifold generator: status
+    Unsupported, record untouched; a triangle has one (the ball-triangle pair is generated)."""
     O = oracle_lib
     s = ShapeSet()
     s.add_ball(1.0)
@@ -102,10 +103,27 @@ def test_unsupported_pairs_leave_record(oracle_lib):
     rec["local_n1"] = 0.25
     before = rec.copy()
     st = O.contact_manifolds(s, np.array([[0, 1], [0, 2]], np.uint32), 0.1, M.as_words(rec), threads=1)
-    assert st["unsupported"] == 2
-    assert np.all(rec["status"] == M.STATUS_UNSUPPORTED)
-    np.testing.assert_array_equal(rec["n_points"], before["n_points"])
-    np.testing.assert_array_equal(rec["local_n1"], before["local_n1"])
+    assert st["unsupported"] == 1
+    assert rec["status"][0] == M.STATUS_UNSUPPORTED and rec["status"][1] == M.STATUS_OK
+    assert rec["n_points"][0] == before["n_points"][0]
+    np.testing.assert_array_equal(rec["local_n1"][0], before["local_n1"][0])
+
+
+def test_empty_slots_are_skipped(oracle_lib):
+    """A pair row (PAIR_NONE, PAIR_NONE) is an empty slot: no query, record and status untouched,
+    counted neither as a pair nor as unsupported."""
+    O = oracle_lib
+    s = ShapeSet()
+    s.add_ball(1.0)
+    s.add_ball(1.0, pose7((1.5, 0, 0)))
+    rec = M.new_manifolds(3)
+    rec["n_points"][1] = 9
+    rec["status"][1] = 77
+    pairs = np.array([[0, 1], [M.PAIR_NONE, M.PAIR_NONE], [1, 0]], np.uint32)
+    st = O.contact_manifolds(s, pairs, 0.1, M.as_words(rec), threads=1)
+    assert st["unsupported"] == 0
+    assert rec["n_points"][1] == 9 and rec["status"][1] == 77
+    assert rec["n_points"][0] == 1 and rec["n_points"][2] == 1
 
 
 def _scene(n, seed, frame=0):
