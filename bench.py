@@ -341,12 +341,14 @@ def shape_cast_section(ctx, stream, steps: int, n_pairs: int, flush) -> dict:
                              "sample": f"first {sample} pairs"}}
 
 
-def trimesh_contacts_section(ctx, stream, frames: int, warmup: int, n_shapes: int, flush) -> dict:
+def trimesh_contacts_section(ctx, stream, frames: int, warmup: int, n_shapes: int, flush, fix: bool = False,
+                             sample: int = 2048) -> dict:
     """Contact manifolds of mixed shapes against the 65,536-triangle terrain, frame after frame
     (contact_manifolds_trimesh_shape with its workspace): ball / cuboid / capsule / hull(16-64)
     shapes drifting down onto the height field; a step is one frame's update on device-resident
-    shapes. Checked bit-exact against the oracle's frame loop on a sample of shapes, which is also
-    the CPU baseline."""
+    shapes. With `fix` the mesh has TriMeshFlags::FIX_INTERNAL_EDGES (pseudo-normal constraints).
+    Interference lists and manifold records are checked bit-exact against the oracle's frame loop
+    on a sample of shapes, which is also the CPU baseline."""
     import numpy as np
     import torch
     import parry_gb300 as pg
@@ -375,7 +377,7 @@ def trimesh_contacts_section(ctx, stream, frames: int, warmup: int, n_shapes: in
     dpoly = (torch.from_numpy(hulls.view(np.int32)).cuda(),
              {k: torch.from_numpy(x.view(np.int32) if x.dtype == np.uint32 else x).cuda() for k, x in topo.items()})
     dt_, dp_, dpool = (torch.from_numpy(t.view(np.int32)).cuda(), torch.from_numpy(prm).cuda(), torch.from_numpy(pool).cuda())
-    mesh = pg.TriMesh(ctx, v, i)
+    mesh = pg.TriMesh(ctx, v, i, flags=pg.TRIMESH_FIX_INTERNAL_EDGES if fix else 0)
     K = 64
     tc = pg.TriMeshContacts(ctx, mesh, n, K)
     pred = 0.02
@@ -396,9 +398,9 @@ def trimesh_contacts_section(ctx, stream, frames: int, warmup: int, n_shapes: in
     active = int(counts.sum())
     with_points = int(sum((recs[s, :counts[s]]["n_points"] > 0).sum() for s in range(n)))
     # oracle frame loop on a sample of shapes (the same frames), timed for the CPU baseline
-    sample = min(n, 2048)
+    sample = min(n, sample)
     sel = np.arange(sample)
-    ref = O.TriMeshContacts(v, i, sample)
+    ref = O.TriMeshContacts(v, i, sample, fix_internal_edges=fix)
     mesh_pose = np.array([0, 0, 0, 1, 0, 0, 0], np.float32)
     threads = os.cpu_count() or 1
     t0 = time.perf_counter()
@@ -406,14 +408,24 @@ def trimesh_contacts_section(ctx, stream, frames: int, warmup: int, n_shapes: in
         ref.update(mesh_pose, ShapeSet.from_arrays(t[sel], prm[sel], poses[f][sel], pool, poly), pred, threads)
     cpu_s = (time.perf_counter() - t0) / total
     same = all(int(counts[s]) == len(ref.inter[s]) and np.array_equal(tris[s, :counts[s]], ref.inter[s]) for s in range(sample))
+    if same:
+        from parry_gb300 import manifold as M
+        g = np.concatenate([recs[s, :counts[s]] for s in range(sample)]).copy()
+        w = np.concatenate([ref.records[s].view(M.MANIFOLD_DTYPE).reshape(-1) for s in range(sample)]).copy()
+        g["status"] = 0
+        w["status"] = 0
+        gw, ww = M.as_words(g), M.as_words(w)
+        live = np.arange(M.MAX_POINTS)[None, :] < w["n_points"].astype(np.int64)[:, None]
+        same = bool(np.array_equal(g["n_points"], w["n_points"]) and np.array_equal(gw[:, :8], ww[:, :8]) and
+                    np.array_equal(gw[:, 8:].reshape(len(g), M.MAX_POINTS, 10)[live], ww[:, 8:].reshape(len(w), M.MAX_POINTS, 10)[live]))
     tc.close()
     mesh.close()
     return {"workload": f"{n} ball/cuboid/capsule/hull(16-64) shapes drifting onto the 65,536-triangle terrain, prediction {pred}, "
-                        f"at most {K} triangles per shape",
+                        f"at most {K} triangles per shape" + (", FIX_INTERNAL_EDGES (pseudo-normal constraints)" if fix else ""),
             "metric": "frames/s", "value": round(1e3 / ms, 2), "unit": "frames/s", "ms_per_frame": round(ms, 4), "frames": frames,
             "shape_triangle_manifolds": active, "with_points": with_points,
             "manifold_updates_per_s": round(active / (ms / 1e3), 1), "gpu_launches": int(launches),
-            "interferences_match_oracle_on_sample": bool(same),
+            "matches_oracle_on_sample": bool(same),
             "cpu_baseline": {"value": round(sample / n / cpu_s, 3), "unit": "frames/s", "cores": threads, "kind": "port",
                              "sample": f"the first {sample} shapes (one frame scaled to all {n}); C++ manifolds, numpy workspace"}}
 
@@ -438,8 +450,10 @@ def contacts_section(ctx, stream, steps: int, warmup: int, n_pairs: int, flush) 
     has = torch.empty(n_pairs, dtype=torch.uint8, device="cuda")
     res = torch.empty((n_pairs, 13), dtype=torch.float32, device="cuda")
     t0 = time.perf_counter()
-    chosen = pg.autotune_contacts(ctx, dev, dpairs[: min(n_pairs, 131072)], 0.0, reps=2)
-    tune = {"chosen": {"epa_blocks_per_sm": chosen["epa_blocks_per_sm"]}, "sample_pairs": min(n_pairs, 131072),
+    # EPA residency is tuned on the whole pair set: the best residency depends on how many pairs
+    # reach EPA at once, so a smaller sample picks for a different load
+    chosen = pg.autotune_contacts(ctx, dev, dpairs, 0.0, reps=1)
+    tune = {"chosen": {"epa_blocks_per_sm": chosen["epa_blocks_per_sm"]}, "sample_pairs": n_pairs,
             "seconds": round(time.perf_counter() - t0, 3)}
     for _ in range(max(1, warmup)):
         pg.contacts(ctx, dev, dpairs, 0.0, out=(has, res))
@@ -960,6 +974,8 @@ def run_gb300(args) -> int:
     trimesh_contacts = None
     if args.terrain_shapes > 0:
         trimesh_contacts = trimesh_contacts_section(ctx, stream, args.steps, args.warmup, args.terrain_shapes, flush)
+        trimesh_contacts["fix_internal_edges"] = trimesh_contacts_section(ctx, stream, args.steps, args.warmup, args.terrain_shapes,
+                                                                          flush, fix=True, sample=1024)
     shape_cast = None
     if args.cast_pairs > 0:
         shape_cast = shape_cast_section(ctx, stream, args.steps, args.cast_pairs, flush)

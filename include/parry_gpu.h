@@ -127,6 +127,26 @@ parrygpu_status parrygpu_bvh_copy_nodes(parrygpu_ctx* ctx, const parrygpu_bvh* b
 parrygpu_status parrygpu_trimesh_create(parrygpu_ctx* ctx, const float* vertices, uint32_t n_vertices,
                                         const uint32_t* indices, uint32_t n_triangles, parrygpu_trimesh** out);
 void parrygpu_trimesh_destroy(parrygpu_trimesh* mesh);
+
+/* TriMeshFlags bits (src/shape/trimesh.rs:470-507) that parrygpu_trimesh_set_flags accepts. */
+#define PARRYGPU_TRIMESH_ORIENTED (1u << 3)
+#define PARRYGPU_TRIMESH_MERGE_DUPLICATE_VERTICES (1u << 4)
+#define PARRYGPU_TRIMESH_FIX_INTERNAL_EDGES ((1u << 7) | (1u << 4))
+/* Replaces TriMesh::set_flags (trimesh.rs:748-800) for ORIENTED, MERGE_DUPLICATE_VERTICES and
+ * FIX_INTERNAL_EDGES; the other flags (topology, connected components, triangle deletion) return
+ * PARRYGPU_UNSUPPORTED_PAIR. With FIX_INTERNAL_EDGES the triangles' pseudo-normals are computed on
+ * the device (bit-identical vertices merged, edge pseudo-normal = sum of the unit normals of the
+ * triangles sharing the edge, compute_pseudo_normals :1348-1407) and every contact manifold against
+ * the mesh applies them as normal constraints. Triangle ids, the BVH and ray casts do not change. */
+parrygpu_status parrygpu_trimesh_set_flags(parrygpu_ctx* ctx, parrygpu_trimesh* mesh, uint32_t flags);
+/* TriMesh::triangle_normal_constraints for every triangle (trimesh.rs:1911-1931): pseudo = n_triangles
+ * x 12 floats (face normal, then the edge pseudo-normals of edges 01, 12, 20), valid[t] = 1 when the
+ * reference returns Some (FIX_INTERNAL_EDGES set, the face and all three edges normalisable). */
+parrygpu_status parrygpu_trimesh_normal_constraints(parrygpu_ctx* ctx, const parrygpu_trimesh* mesh, float* pseudo, uint8_t* valid);
+/* TrianglePseudoNormals::project_local_normal (src/shape/triangle_pseudo_normals.rs:35-99) for n rows:
+ * pseudo = n x 12 floats, dirs / out = n x 3 floats, ok[i] = 0 where the reference returns None. */
+parrygpu_status parrygpu_project_local_normals(parrygpu_ctx* ctx, const float* pseudo, const float* dirs, uint64_t n, float* out,
+                                               uint8_t* ok);
 /* Replaces a loop of RayCast::cast_ray_and_get_normal(m, ray, max_toi, solid) on a TriMesh
  * (src/query/ray/ray.rs:393-403 -> src/query/ray/ray_trimesh.rs:17-35). pose7 = the mesh pose m
  * (NULL = identity). rays: n x 6 floats. Outputs per ray:
@@ -383,8 +403,10 @@ parrygpu_status parrygpu_trimesh_contacts_create(parrygpu_ctx* ctx, const parryg
 void parrygpu_trimesh_contacts_destroy(parrygpu_trimesh_contacts* contacts);
 /* One frame: for every shape s (shapes->n == n_shapes) the reference's
  * contact_manifolds_trimesh_shape(dispatcher, mesh_pose^-1 * pose_s, mesh, shape_s, prediction,
- * manifolds, workspace) with the mesh as shape 1 and no pseudo-normals. mesh_pose7: host pointer to
- * the mesh pose, NULL = identity. Interfering triangles are kept in ascending index order. */
+ * manifolds, workspace) with the mesh as shape 1; when the mesh has FIX_INTERNAL_EDGES
+ * (parrygpu_trimesh_set_flags) each triangle's pseudo-normals constrain its manifolds' normals.
+ * mesh_pose7: host pointer to the mesh pose, NULL = identity. Interfering triangles are kept in
+ * ascending index order. */
 parrygpu_status parrygpu_trimesh_contacts_update(parrygpu_ctx* ctx, parrygpu_trimesh_contacts* contacts, const float* mesh_pose7,
                                                  const parrygpu_shapes* shapes, float prediction);
 /* Copies the current state (host or device buffers; any may be NULL): counts (n_shapes), triangles

@@ -412,12 +412,25 @@ void oracle_compound_cast_rays_f64(void* c, const float* pose7, const float* ray
 // records in place. Unsupported pairs keep their record and get status 2; a row (0xFFFFFFFF,
 // 0xFFFFFFFF) is an empty slot, skipped with its record untouched. stats: gjk_iters, epa_iters,
 // epa_calls, unsupported pairs, largest point count.
+// pseudo (may be null): rows of 12 floats (face, e01, e12, e20) of TrianglePseudoNormals; a triangle
+// shape of index >= pseudo_first whose params word 2 holds j > 0 has the normal constraints of row
+// j - 1.
 void oracle_manifolds_f32(const uint32_t* types, const float* params, const float* poses, const float* hullv, uint32_t nhv,
                           uint64_t nshapes, const void* poly, const uint32_t* pairs, uint64_t npairs, float prediction, int threads,
-                          uint32_t* records, uint64_t* stats) {
+                          uint32_t* records, uint64_t* stats, const float* pseudo, uint64_t pseudo_first) {
   ShapeSet<float> set(types, params, poses, hullv, nhv, nshapes);
   set.attach(params, (const PolyIn*)poly);
   std::atomic<uint64_t> gi{0}, ei{0}, ec{0}, un{0}, mx{0};
+  auto constraints = [&](uint32_t i, TriPseudoNormals<float>* pn) -> const TriPseudoNormals<float>* {
+    if (!pseudo || i < pseudo_first || types[i] != SHAPE_TRIANGLE) return nullptr;
+    uint32_t j;
+    std::memcpy(&j, params + 4 * (size_t)i + 2, 4);
+    if (j == 0) return nullptr;
+    const float* q = pseudo + 12 * (size_t)(j - 1);
+    pn->face = Vec3<float>(q[0], q[1], q[2]);
+    for (int e = 0; e < 3; ++e) pn->edges[e] = Vec3<float>(q[3 + 3 * e], q[4 + 3 * e], q[5 + 3 * e]);
+    return pn;
+  };
   parallel_for(npairs, threads, [&](uint64_t k) {
     uint32_t a = pairs[2 * k], b = pairs[2 * k + 1];
     if (a == 0xFFFFFFFFu && b == 0xFFFFFFFFu) return;
@@ -426,7 +439,10 @@ void oracle_manifolds_f32(const uint32_t* types, const float* params, const floa
     manifold_load(r, m);
     GjkStats st;
     Iso<float> pos12 = set.poses[a].inv_mul(set.poses[b]);
-    bool ok = contact_manifold_convex_convex(pos12, set.shapes[a], set.shapes[b], prediction, m, &st);
+    TriPseudoNormals<float> pa, pb;
+    const TriPseudoNormals<float>* ca = constraints(a, &pa);
+    const TriPseudoNormals<float>* cb = constraints(b, &pb);
+    bool ok = contact_manifold_convex_convex(pos12, set.shapes[a], set.shapes[b], prediction, m, &st, ca, cb);
     gi += st.gjk_iters; ei += st.epa_iters; ec += st.epa_calls;
     if (!ok) { un += 1; r[1] = 2; return; }
     r[1] = 0;
@@ -435,6 +451,25 @@ void oracle_manifolds_f32(const uint32_t* types, const float* params, const floa
     manifold_store(m, r);
   });
   if (stats) { stats[0] = gi.load(); stats[1] = ei.load(); stats[2] = ec.load(); stats[3] = un.load(); stats[4] = mx.load(); }
+}
+
+// TriMesh::triangle_normal_constraints of every triangle of a FIX_INTERNAL_EDGES mesh (12 floats per
+// triangle: face, e01, e12, e20; valid = 1 when Some).
+void oracle_trimesh_pseudo_normals_f32(const float* vtx, uint32_t nv, const uint32_t* idx, uint32_t nt, float* out, uint8_t* valid) {
+  trimesh_pseudo_normals<float>(vtx, nv, idx, nt, out, valid);
+}
+
+// TrianglePseudoNormals::project_local_normal for n (pseudo-normals, direction) rows; ok = 1 when Some.
+void oracle_project_local_normals_f32(const float* pn12, const float* dirs, uint64_t n, float* out, uint8_t* ok) {
+  for (uint64_t i = 0; i < n; ++i) {
+    const float* q = pn12 + 12 * i;
+    TriPseudoNormals<float> pn;
+    pn.face = Vec3<float>(q[0], q[1], q[2]);
+    for (int e = 0; e < 3; ++e) pn.edges[e] = Vec3<float>(q[3 + 3 * e], q[4 + 3 * e], q[5 + 3 * e]);
+    Vec3<float> d(dirs[3 * i], dirs[3 * i + 1], dirs[3 * i + 2]);
+    ok[i] = project_local_normal_mut(pn, &d) ? 1 : 0;
+    out[3 * i] = d.x; out[3 * i + 1] = d.y; out[3 * i + 2] = d.z;
+  }
 }
 
 // Pose integration of the frame pipeline (decision D-5; parry has no integrator), f32, in this

@@ -10,8 +10,13 @@
 //   src/shape/polygonal_feature3d.rs:60-439, src/shape/cuboid.rs:267-352 (support_face),
 //   src/shape/polygonal_feature_map.rs:30-46, src/shape/shape.rs:855-857 (capsule = segment + radius)
 //   src/query/clip/clip_segment_segment.rs, src/query/closest_points/closest_points_segment_segment.rs
+//   src/query/contact_manifolds/contact_manifolds_cuboid_triangle.rs:10-174 (with normal constraints)
+// Normal constraints (TrianglePseudoNormals of a TriMesh with FIX_INTERNAL_EDGES) enter the
+// convex-ball, cuboid-triangle and pfm-pfm generators as in the reference; nullptr = None.
 #pragma once
 #include "contact.hpp"
+#include "pseudo_normals.hpp"
+#include "ray.hpp"
 #include <cstring>
 
 namespace oracle {
@@ -523,10 +528,11 @@ template <class R> inline uint32_t cuboid_projection_feature(const Vec3<R>& he, 
   return pfid_edge((id << 2) | (uint32_t)last_zero);
 }
 
-// contact_manifolds_convex_ball.rs:45-145 for a cuboid or capsule shape1 (no normal constraints)
+// contact_manifolds_convex_ball.rs:45-145 for a cuboid, capsule, triangle or hull shape1; c1 / c2 are
+// the normal constraints of shape1 / the ball.
 template <class R>
 inline void manifold_convex_ball(const Iso<R>& pos12, const Shape<R>& s1, R radius2, R prediction, Manifold<R>& m, bool flipped,
-                                 GjkStats* st) {
+                                 GjkStats* st, const TriPseudoNormals<R>* c1 = nullptr, const TriPseudoNormals<R>* c2 = nullptr) {
   Vec3<R> lp21 = pos12.tra;
   Vec3<R> proj;
   bool inside;
@@ -551,7 +557,26 @@ inline void manifold_convex_ball(const Iso<R>& pos12, const Shape<R>& s1, R radi
   if (inside) { n1 = -n1; dist = -dist; }
   if (dist <= radius2 + prediction) {
     Vec3<R> n2 = pos12.inverse_transform_vector(-n1);
+    const Vec3<R> uncorrected_n2 = n2;
+    if (!project_local_normals(c1, c2, pos12, &n1, &n2)) {
+      m.points.clear();  // the contact got discarded by the normal correction
+      return;
+    }
     Vec3<R> lp2 = n2 * radius2;
+    if (!(uncorrected_n2 == n2)) {
+      // corrected normal: the contact point on shape1 is where the ray from the ball centre along
+      // the corrected normal meets it (Shape::cast_local_ray_and_get_normal, solid = false)
+      Ray<R> ray1{pos12.tra, inside ? n1 : -n1};
+      RayHit<R> hit;
+      if (s1.type != SHAPE_TRIANGLE || !ray_triangle(s1.pts[0], s1.pts[1], s1.pts[2], ray1, &hit) ||
+          !(hit.toi <= std::numeric_limits<R>::max())) {
+        m.points.clear();
+        return;
+      }
+      lp1 = ray1.origin + ray1.dir * hit.toi;
+      dist = inside ? -hit.toi : hit.toi;
+      fid1 = pfid_face(hit.fid);
+    }
     TrackedContact<R> c = TrackedContact<R>::make(lp1, lp2, fid1, pfid_face(0), dist - radius2, flipped);
     if (m.points.size() != 1) { m.points.clear(); m.points.push_back(c); }
     else m.points[0].copy_geometry_from(c);
@@ -694,11 +719,12 @@ inline std::pair<R, Vec3<R>> sat_cuboid_triangle_edge_twoway(const Vec3<R>& he1,
   return {best, best_axis};
 }
 
-// contact_manifolds_cuboid_triangle.rs:57-174 (no normal constraints): the cuboid is shape 1 of
-// the SAT; `flipped` when the triangle is the manifold's first shape.
+// contact_manifolds_cuboid_triangle.rs:57-174: the cuboid is shape 1 of the SAT; `flipped` when the
+// triangle is the manifold's first shape; c1 / c2 = normal constraints of the cuboid / triangle.
 template <class R>
 inline void manifold_cuboid_triangle(const Iso<R>& pos12, const Iso<R>& pos21, const Vec3<R>& he1, const Shape<R>& tri2, R prediction,
-                                     Manifold<R>& m, bool flipped) {
+                                     Manifold<R>& m, bool flipped, const TriPseudoNormals<R>* c1 = nullptr,
+                                     const TriPseudoNormals<R>* c2 = nullptr) {
   if ((!flipped && m.try_update_contacts(pos12)) || (flipped && m.try_update_contacts(pos21))) return;
   auto sep1 = sat_cuboid_triangle_normal_oneway(he1, tri2, pos12);
   if (sep1.first > prediction) { m.points.clear(); return; }
@@ -709,23 +735,36 @@ inline void manifold_cuboid_triangle(const Iso<R>& pos12, const Iso<R>& pos21, c
   auto sep3 = sat_cuboid_triangle_edge_twoway(he1, tri2, pos12);
   if (sep3.first > prediction) { m.points.clear(); return; }
   Vec3<R> normal1 = sep1.second;
-  if (sep2.first > sep1.first && sep2.first > sep3.first) normal1 = pos12.transform_vector(-sep2.second);
-  else if (sep3.first > sep1.first) normal1 = sep3.second;
+  R dist = sep1.first;
+  if (sep2.first > sep1.first && sep2.first > sep3.first) { normal1 = pos12.transform_vector(-sep2.second); dist = sep2.first; }
+  else if (sep3.first > sep1.first) { normal1 = sep3.second; dist = sep3.first; }
   Vec3<R> normal2 = pos21.transform_vector(-normal1);
+  if (!project_local_normals(c1, c2, pos12, &normal1, &normal2)) {
+    m.points.clear();  // the contact got discarded by the normal correction
+    return;
+  }
   PolyFeature<R> f1 = cuboid_support_face(he1, normal1);
   PolyFeature<R> f2 = triangle_feature(tri2);
   auto old = m.points;
   m.points.clear();
   feature_contacts(pos12, normal1, f1, f2, m, flipped);
+  if (c1 || c2) {
+    // drop points whose depth diverges from the unconstrained one (the reference's retain filter)
+    std::vector<TrackedContact<R>> kept;
+    for (const auto& c : m.points)
+      if (dist >= R(0) || c.dist >= R(0) || c.dist >= dist * R(5)) kept.push_back(c);
+    m.points.swap(kept);
+  }
   if (flipped) { m.local_n1 = normal2; m.local_n2 = normal1; }
   else { m.local_n1 = normal1; m.local_n2 = normal2; }
   m.match_contacts(old);
 }
 
-// contact_manifolds_pfm_pfm.rs:44-162 for cuboids and capsules (capsule = segment + border radius);
-// no normal constraints.
+// contact_manifolds_pfm_pfm.rs:44-162 for cuboids, capsules (segment + border radius), triangles and
+// hulls; c1 / c2 = normal constraints of shape 1 / 2.
 template <class R> inline void manifold_pfm_pfm(const Iso<R>& pos12, const Shape<R>& s1, const Shape<R>& s2, R prediction, Manifold<R>& m,
-                                                GjkStats* st) {
+                                                GjkStats* st, const TriPseudoNormals<R>* c1 = nullptr,
+                                                const TriPseudoNormals<R>* c2 = nullptr) {
   if (m.try_update_contacts_eps(pos12, cos_1_degrees<R>(), R(1.0e-6))) return;
   auto pfm = [](const Shape<R>& s, R* border) {
     Shape<R> p = s;
@@ -745,6 +784,8 @@ template <class R> inline void manifold_pfm_pfm(const Iso<R>& pos12, const Shape
   if (r.kind == GJK_CLOSEST_POINTS) {
     Vec3<R> n1 = r.dir;
     Vec3<R> n2 = pos12.inverse_transform_vector(-r.dir);
+    const R dist = dot(r.p2 - r.p1, n1);
+    if (!project_local_normals(c1, c2, pos12, &n1, &n2)) return;  // discarded: points cleared, no matching
     auto feature_of = [](const Shape<R>& s, const Vec3<R>& d) {
       if (s.type == SHAPE_CUBOID) return cuboid_support_face(s.half, d);
       if (s.type == SHAPE_CONVEX) return hull_support_feature(s, d);
@@ -753,7 +794,15 @@ template <class R> inline void manifold_pfm_pfm(const Iso<R>& pos12, const Shape
     };
     PolyFeature<R> f1 = feature_of(s1, n1), f2 = feature_of(s2, n2);
     feature_contacts(pos12, n1, f1, f2, m, false);
-    m.points.push_back(TrackedContact<R>::make(r.p1, pos12.inverse_transform_point(r.p2), PFID_UNKNOWN, PFID_UNKNOWN, dot(r.p2 - r.p1, n1), false));
+    // the GJK point only while the normal is GJK's own direction
+    if (n1 == r.dir)
+      m.points.push_back(TrackedContact<R>::make(r.p1, pos12.inverse_transform_point(r.p2), PFID_UNKNOWN, PFID_UNKNOWN, dot(r.p2 - r.p1, n1), false));
+    if (c1 || c2) {
+      std::vector<TrackedContact<R>> kept;
+      for (const auto& c : m.points)
+        if (dist >= R(0) || c.dist >= R(0) || c.dist >= dist * R(5)) kept.push_back(c);
+      m.points.swap(kept);
+    }
     if (br1 != R(0) || br2 != R(0)) {
       for (auto& c : m.points) {
         c.local_p1 += n1 * br1;
@@ -772,11 +821,12 @@ template <class R> inline void manifold_pfm_pfm(const Iso<R>& pos12, const Shape
 }
 
 // DefaultQueryDispatcher::contact_manifold_convex_convex (default_query_dispatcher.rs:749-831) for
-// balls, cuboids, capsules, triangles and convex polyhedra (no normal constraints). Returns false
-// (Unsupported) for other shapes.
+// balls, cuboids, capsules, triangles and convex polyhedra, with the optional normal constraints of
+// each shape. Returns false (Unsupported) for other shapes.
 template <class R>
 inline bool contact_manifold_convex_convex(const Iso<R>& pos12, const Shape<R>& s1, const Shape<R>& s2, R prediction, Manifold<R>& m,
-                                           GjkStats* st = nullptr) {
+                                           GjkStats* st = nullptr, const TriPseudoNormals<R>* c1 = nullptr,
+                                           const TriPseudoNormals<R>* c2 = nullptr) {
   auto ok = [](const Shape<R>& s) {
     return s.type == SHAPE_BALL || s.type == SHAPE_CUBOID || s.type == SHAPE_CAPSULE || s.type == SHAPE_TRIANGLE ||
            (s.type == SHAPE_CONVEX && s.topo && s.topo->n_faces);
@@ -784,13 +834,15 @@ inline bool contact_manifold_convex_convex(const Iso<R>& pos12, const Shape<R>& 
   if (!ok(s1) || !ok(s2)) return false;
   if (s1.type == SHAPE_BALL && s2.type == SHAPE_BALL) manifold_ball_ball(pos12, s1.radius, s2.radius, prediction, m);
   else if (s1.type == SHAPE_CUBOID && s2.type == SHAPE_CUBOID) manifold_cuboid_cuboid(pos12, s1.half, s2.half, prediction, m);
-  else if (s1.type == SHAPE_CUBOID && s2.type == SHAPE_TRIANGLE) manifold_cuboid_triangle(pos12, pos12.inverse(), s1.half, s2, prediction, m, false);
-  else if (s1.type == SHAPE_TRIANGLE && s2.type == SHAPE_CUBOID) manifold_cuboid_triangle(pos12.inverse(), pos12, s2.half, s1, prediction, m, true);
+  else if (s1.type == SHAPE_CUBOID && s2.type == SHAPE_TRIANGLE)
+    manifold_cuboid_triangle(pos12, pos12.inverse(), s1.half, s2, prediction, m, false, c1, c2);
+  else if (s1.type == SHAPE_TRIANGLE && s2.type == SHAPE_CUBOID)
+    manifold_cuboid_triangle(pos12.inverse(), pos12, s2.half, s1, prediction, m, true, c2, c1);
   else if (s1.type == SHAPE_CAPSULE && s2.type == SHAPE_CAPSULE)
     manifold_capsule_capsule(pos12, s1.half_height, s1.radius, s2.half_height, s2.radius, prediction, m);
-  else if (s1.type == SHAPE_BALL) manifold_convex_ball(pos12.inverse(), s2, s1.radius, prediction, m, true, st);
-  else if (s2.type == SHAPE_BALL) manifold_convex_ball(pos12, s1, s2.radius, prediction, m, false, st);
-  else manifold_pfm_pfm(pos12, s1, s2, prediction, m, st);
+  else if (s1.type == SHAPE_BALL) manifold_convex_ball(pos12.inverse(), s2, s1.radius, prediction, m, true, st, c2, c1);
+  else if (s2.type == SHAPE_BALL) manifold_convex_ball(pos12, s1, s2.radius, prediction, m, false, st, c1, c2);
+  else manifold_pfm_pfm(pos12, s1, s2, prediction, m, st, c1, c2);
   return true;
 }
 

@@ -47,7 +47,9 @@ _SIGS = {
     "oracle_compound_free_f64": (None, [P]),
     "oracle_compound_cast_rays_f32": (None, [P, P, P, U64, F32, I32, I32, I32, P, P, P, P]),
     "oracle_compound_cast_rays_f64": (None, [P, P, P, U64, F32, I32, I32, I32, P, P, P, P]),
-    "oracle_manifolds_f32": (None, [P, P, P, P, U32, U64, P, P, U64, F32, I32, P, P]),
+    "oracle_manifolds_f32": (None, [P, P, P, P, U32, U64, P, P, U64, F32, I32, P, P, P, U64]),
+    "oracle_trimesh_pseudo_normals_f32": (None, [P, U32, P, U32, P, P]),
+    "oracle_project_local_normals_f32": (None, [P, P, U64, P, P]),
     "oracle_integrate_f32": (None, [P, P, U64, F32]),
     "oracle_pairs_count": (U64, [P]),
     "oracle_pairs_copy": (None, [P, P]),
@@ -269,9 +271,14 @@ def empty_manifolds(k: int) -> np.ndarray:
     return np.zeros((k, MANIFOLD_WORDS), np.uint32)
 
 
-def contact_manifolds(shapes, pairs: np.ndarray, prediction: float, records: np.ndarray, threads: int | None = None) -> dict:
-    """DefaultQueryDispatcher::contact_manifold_convex_convex(pos_a^-1 pos_b, a, b, prediction, manifold)
-    for every (a, b) row of `pairs`, updating `records` (k x MANIFOLD_WORDS uint32) in place."""
+def contact_manifolds(shapes, pairs: np.ndarray, prediction: float, records: np.ndarray, threads: int | None = None,
+                      pseudo: np.ndarray | None = None, pseudo_first: int = 0) -> dict:
+    """DefaultQueryDispatcher::contact_manifold_convex_convex(pos_a^-1 pos_b, a, b, c_a, c_b, prediction,
+    manifold) for every (a, b) row of `pairs`, updating `records` (k x MANIFOLD_WORDS uint32) in
+    place. Normal constraints c: a triangle shape of index >= pseudo_first whose params word 2 holds
+    j > 0 uses row j - 1 of `pseudo` (rows of 12 floats: face, e01, e12, e20); else None."""
+    if pseudo is not None:
+        pseudo = np.ascontiguousarray(pseudo, np.float32).reshape(-1, 12)
     t, prm, pos, pool = _shape_arrays(shapes)
     pairs = np.ascontiguousarray(pairs, np.uint32).reshape(-1, 2)
     k = len(pairs)
@@ -279,10 +286,35 @@ def contact_manifolds(shapes, pairs: np.ndarray, prediction: float, records: np.
     st = np.zeros(5, np.uint64)
     poly, keep = _poly_struct(shapes)
     lib().oracle_manifolds_f32(_p(t), _p(prm), _p(pos), _p(pool), len(pool), len(t), poly, _p(pairs), k, float(prediction),
-                               threads if threads is not None else default_threads(), _p(records), _p(st))
+                               threads if threads is not None else default_threads(), _p(records), _p(st),
+                               _p(pseudo) if pseudo is not None and len(pseudo) else None, int(pseudo_first))
     del keep
     return {"gjk_iters": int(st[0]), "epa_iters": int(st[1]), "epa_calls": int(st[2]), "unsupported": int(st[3]),
             "max_points": int(st[4])}
+
+
+def trimesh_pseudo_normals(vertices: np.ndarray, indices: np.ndarray) -> tuple[np.ndarray, np.ndarray]:
+    """TriMesh::triangle_normal_constraints of every triangle of a mesh built with
+    TriMeshFlags::FIX_INTERNAL_EDGES (trimesh.rs:1251-1320, 1348-1407, 1911-1931): (nt, 12) f32 rows
+    (face, e01, e12, e20) and a (nt,) bool mask of the triangles that have constraints."""
+    v = np.ascontiguousarray(vertices, np.float32).reshape(-1, 3)
+    i = np.ascontiguousarray(indices, np.uint32).reshape(-1, 3)
+    out = np.zeros((len(i), 12), np.float32)
+    ok = np.zeros(len(i), np.uint8)
+    lib().oracle_trimesh_pseudo_normals_f32(_p(v), len(v), _p(i), len(i), _p(out), _p(ok))
+    return out, ok.astype(bool)
+
+
+def project_local_normals(pseudo: np.ndarray, dirs: np.ndarray) -> tuple[np.ndarray, np.ndarray]:
+    """TrianglePseudoNormals::project_local_normal (triangle_pseudo_normals.rs:35-99) per row:
+    (projected directions (n, 3), ok mask) - ok False is the reference's None."""
+    pn = np.ascontiguousarray(pseudo, np.float32).reshape(-1, 12)
+    d = np.ascontiguousarray(dirs, np.float32).reshape(-1, 3)
+    assert len(pn) == len(d)
+    out = np.zeros_like(d)
+    ok = np.zeros(len(d), np.uint8)
+    lib().oracle_project_local_normals_f32(_p(pn), _p(d), len(d), _p(out), _p(ok))
+    return out, ok.astype(bool)
 
 
 def inv_mul(pose1: np.ndarray, poses2: np.ndarray) -> np.ndarray:
@@ -294,9 +326,10 @@ def inv_mul(pose1: np.ndarray, poses2: np.ndarray) -> np.ndarray:
     return out
 
 
-def _with_triangles(shapes, tri_vertices: np.ndarray, mesh_pose: np.ndarray):
+def _with_triangles(shapes, tri_vertices: np.ndarray, mesh_pose: np.ndarray, constrained: np.ndarray | None = None):
     """The shapes followed by one Triangle shape per mesh triangle (vertices appended to the pool,
-    posed at the mesh pose): triangle t has shape index n + t."""
+    posed at the mesh pose): triangle t has shape index n + t; with `constrained` (mask), params
+    word 2 of triangle t is t + 1 where it has normal constraints (row t of the table)."""
     from parry_gb300.shapes import ShapeSet, TRIANGLE
     t, prm, pos, pool = shapes.arrays()
     n, nt = len(t), len(tri_vertices)
@@ -304,6 +337,8 @@ def _with_triangles(shapes, tri_vertices: np.ndarray, mesh_pose: np.ndarray):
     tp = np.zeros((nt, 4), np.float32)
     tp.view(np.uint32)[:, 0] = first
     tp.view(np.uint32)[:, 1] = 3
+    if constrained is not None:
+        tp.view(np.uint32)[:, 2] = np.where(constrained, np.arange(1, nt + 1, dtype=np.uint32), 0)
     poly = shapes.polyhedra()
     if poly is not None:
         hulls, topo = poly
@@ -317,17 +352,18 @@ def _with_triangles(shapes, tri_vertices: np.ndarray, mesh_pose: np.ndarray):
 
 class TriMeshContacts:
     """contact_manifolds_trimesh_shape (contact_manifolds_trimesh_shape.rs:82-228) for each shape of a
-    set against one TriMesh (the mesh is shape 1; no pseudo-normals, so no normal constraints),
-    frame after frame, with the reference's workspace: the shape's AABB in the mesh frame loosened by
+    set against one TriMesh (the mesh is shape 1), frame after frame; with fix_internal_edges
+    (TriMeshFlags::FIX_INTERNAL_EDGES) each triangle's TrianglePseudoNormals constrain the normals, with the reference's workspace: the shape's AABB in the mesh frame loosened by
     the prediction, kept while it still contains the new one (else enlarged by min(extent / 10, 0.1)
     per axis and the triangles whose AABBs intersect it queried again), and one ContactManifold per
     interfering triangle carried over by triangle id. Interferences are kept in ascending triangle
     order: the reference's carry-over loop walks old and new lists as sorted lists, and its BVH
     returns them in tree order, which depends on the tree (a deviation recorded as D-8)."""
 
-    def __init__(self, vertices: np.ndarray, indices: np.ndarray, n_shapes: int):
+    def __init__(self, vertices: np.ndarray, indices: np.ndarray, n_shapes: int, fix_internal_edges: bool = False):
         v = np.ascontiguousarray(vertices, np.float32).reshape(-1, 3)
         i = np.ascontiguousarray(indices, np.uint32).reshape(-1, 3)
+        self.pseudo, self.constrained = trimesh_pseudo_normals(v, i) if fix_internal_edges else (None, None)
         self.tri = np.ascontiguousarray(v[i], np.float32)  # (nt, 3, 3)
         # aabb_triangle.rs: a.min(b).min(c), a.max(b).max(c)
         self.tri_min = np.minimum(np.minimum(self.tri[:, 0], self.tri[:, 1]), self.tri[:, 2])
@@ -368,14 +404,14 @@ class TriMeshContacts:
             rec[found] = old_rec[j[found]]
             self.inter[s], self.records[s] = new, rec
             self.aabb[s, :3], self.aabb[s, 3:] = mins, maxs
-        combined = _with_triangles(shapes, self.tri, mesh_pose)
+        combined = _with_triangles(shapes, self.tri, mesh_pose, self.constrained)
         counts = [len(x) for x in self.inter]
         if sum(counts) == 0:
             return {"pairs": 0}
         pairs = np.concatenate([np.stack([self.inter[s] + np.uint32(n), np.full(counts[s], s, np.uint32)], 1)
                                 for s in range(n) if counts[s]]).astype(np.uint32)
         recs = np.ascontiguousarray(np.concatenate([self.records[s] for s in range(n) if counts[s]]))
-        st = contact_manifolds(combined, pairs, prediction, recs, threads)
+        st = contact_manifolds(combined, pairs, prediction, recs, threads, self.pseudo, n)
         k = 0
         for s in range(n):
             self.records[s] = recs[k:k + counts[s]].copy()

@@ -233,10 +233,18 @@ class Bvh:
             pass
 
 
-class TriMesh:
-    """shape::TriMesh for ray casts: vertices (n_v, 3) f32, indices (n_t, 3) u32."""
+# TriMeshFlags bits (src/shape/trimesh.rs:470-507) accepted by TriMesh(..., flags=) / set_flags.
+TRIMESH_ORIENTED = 1 << 3
+TRIMESH_MERGE_DUPLICATE_VERTICES = 1 << 4
+TRIMESH_FIX_INTERNAL_EDGES = (1 << 7) | (1 << 4)
 
-    def __init__(self, ctx: Context, vertices, indices):
+
+class TriMesh:
+    """shape::TriMesh: vertices (n_v, 3) f32, indices (n_t, 3) u32, optional TriMeshFlags
+    (TriMesh::with_flags; FIX_INTERNAL_EDGES computes the triangles' pseudo-normals, which then
+    constrain contact-manifold normals against the mesh)."""
+
+    def __init__(self, ctx: Context, vertices, indices, flags: int = 0):
         kv, pv = _as_input(vertices, np.float32)
         ki, pi = _as_input(indices, np.uint32)
         self.ctx = ctx
@@ -245,6 +253,23 @@ class TriMesh:
         h = C.c_void_p()
         check(lib().parrygpu_trimesh_create(ctx.handle, pv, self.n_vertices, pi, self.n_triangles, C.byref(h)), ctx.handle)
         self._h = h
+        self.flags = 0
+        if flags:
+            self.set_flags(flags)
+
+    def set_flags(self, flags: int) -> None:
+        """TriMesh::set_flags for ORIENTED / MERGE_DUPLICATE_VERTICES / FIX_INTERNAL_EDGES."""
+        check(lib().parrygpu_trimesh_set_flags(self.ctx.handle, self._h, int(flags)), self.ctx.handle)
+        self.flags = int(flags)
+
+    def normal_constraints(self):
+        """TriMesh::triangle_normal_constraints of every triangle: ((n_t, 12) f32 rows = face normal,
+        pseudo-normals of edges 01, 12, 20; (n_t,) bool, False where the reference returns None)."""
+        pn = np.zeros((self.n_triangles, 12), np.float32)
+        ok = np.zeros(self.n_triangles, np.uint8)
+        check(lib().parrygpu_trimesh_normal_constraints(self.ctx.handle, self._h, C.c_void_p(pn.ctypes.data),
+                                                        C.c_void_p(ok.ctypes.data)), self.ctx.handle)
+        return pn, ok.astype(bool)
 
     def _cast(self, rays, max_toi, solid, pose, want_normal, out=None):
         kr, pr = _as_input(rays, np.float32)
@@ -421,6 +446,20 @@ class TriMeshContacts:
             self.close()
         except Exception:
             pass
+
+
+def project_local_normals(ctx: Context, pseudo, dirs):
+    """TrianglePseudoNormals::project_local_normal per row: pseudo (n, 12) f32 (face, e01, e12, e20),
+    dirs (n, 3) f32. Returns (projected (n, 3) f32, ok (n,) bool; False = None)."""
+    pn = np.ascontiguousarray(pseudo, np.float32).reshape(-1, 12)
+    d = np.ascontiguousarray(dirs, np.float32).reshape(-1, 3)
+    if len(pn) != len(d):
+        raise ValueError("one pseudo-normal row per direction")
+    out = np.zeros_like(d)
+    ok = np.zeros(len(d), np.uint8)
+    check(lib().parrygpu_project_local_normals(ctx.handle, C.c_void_p(pn.ctypes.data), C.c_void_p(d.ctypes.data), len(d),
+                                               C.c_void_p(out.ctypes.data), C.c_void_p(ok.ctypes.data)), ctx.handle)
+    return out, ok.astype(bool)
 
 
 CAST_NONE = 255

@@ -53,6 +53,9 @@ SIGNATURES: dict[str, tuple] = {
     "parrygpu_bvh_copy_nodes": (I32, [P, P, P]),
     "parrygpu_trimesh_create": (I32, [P, P, U32, P, U32, C.POINTER(P)]),
     "parrygpu_trimesh_destroy": (None, [P]),
+    "parrygpu_trimesh_set_flags": (I32, [P, P, U32]),
+    "parrygpu_trimesh_normal_constraints": (I32, [P, P, P, P]),
+    "parrygpu_project_local_normals": (I32, [P, P, P, U64, P, P]),
     "parrygpu_trimesh_cast_rays": (I32, [P, P, P, P, U32, F32, I32, P, P, P]),
     "parrygpu_trimesh_cast_rays_noalloc": (I32, [P, P, P, P, U32, F32, I32, P, P, P]),
     "parrygpu_shapes_aabbs": (I32, [P, P, F32, P]),

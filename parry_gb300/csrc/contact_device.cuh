@@ -32,6 +32,10 @@ struct ShapeArrays {
   uint64_t n_shapes;
   uint64_t n_vertices;
   PolyArrays poly;
+  // Normal constraints (TrianglePseudoNormals rows of 12 floats) of a TriMesh's triangles: a
+  // triangle shape of index >= pseudo_first whose params word 2 holds j > 0 uses row j - 1.
+  const float* pseudo = nullptr;
+  uint64_t pseudo_first = 0;
 };
 
 // Rejects out-of-range pair indices and vertex ranges (reported as a capacity / argument error

@@ -109,6 +109,10 @@ struct parrygpu_trimesh {
   uint32_t n_vertices = 0, n_triangles = 0;
   parrygpu_bvh bvh;     // leaves store the sorted position of the triangle in `soup`
   DevBuf soup;          // per sorted position: a.xyz b.x | b.yz c.xy | c.z orig 0 0  (3 x float4)
+  uint32_t flags = 0;   // TriMeshFlags bits
+  DevBuf pseudo;        // with FIX_INTERNAL_EDGES: per original triangle, TrianglePseudoNormals (12 floats)
+  DevBuf pseudo_ok;     // per original triangle: 1 when triangle_normal_constraints is Some
+  bool constrained() const { return (flags & PARRYGPU_TRIMESH_FIX_INTERNAL_EDGES) == PARRYGPU_TRIMESH_FIX_INTERNAL_EDGES && pseudo.ptr; }
 };
 
 // A shape set under one BVH (the reference's Compound), with device copies of the shape arrays.
@@ -150,6 +154,8 @@ parrygpu_status radix_sort_reserve(parrygpu_ctx* ctx, uint32_t n);
 parrygpu_status radix_sort_pairs_in(parrygpu_ctx* ctx, uint32_t n, int key_bits, uint32_t* k0, uint32_t* v0, uint32_t* k1,
                                     uint32_t* v1, uint32_t* hist, int* result_buf);
 uint32_t radix_sort_hist_entries(uint32_t n);
+// In-place exclusive prefix sum of m words (buffer padded to a multiple of 4 words with zeros).
+parrygpu_status exclusive_scan_u32(parrygpu_ctx* ctx, uint32_t* data, uint32_t m);
 
 // ---- ray casts (ray.cu): launch helpers on caller-provided device buffers (no allocation) ----
 // Key width (bits) of the ray ordering for the context's ray_sort_key mode.

@@ -27,6 +27,8 @@
 #include "internal.hpp"
 #include "epa_device.cuh"
 #include "contact_device.cuh"
+#include "pseudo_device.cuh"
+#include "tri_ray_device.cuh"
 #include <cstring>
 
 using namespace pg;
@@ -100,6 +102,26 @@ struct Writer {
     n++;
   }
 };
+
+// The reference's filter after a normal correction (contact_manifolds_pfm_pfm.rs:126-136,
+// contact_manifolds_cuboid_triangle.rs:152-163): a point stays unless the unconstrained separation
+// `dist` and the point's distance are both negative and the point is over five times deeper; kept
+// points stay in order (Vec::retain).
+__device__ __forceinline__ void retain_close_depths(const Rec& r, Writer* wr, float dist) {
+  uint32_t k = 0;
+  for (uint32_t i = 0; i < wr->n; ++i) {
+    const int b = Rec::pt(i);
+    const float pd = r.f(b + 6);
+    if (dist >= 0.0f || pd >= 0.0f || pd >= dist * 5.0f) {
+      if (k != i) {
+        const int d = Rec::pt(k);
+        for (int w = 0; w < 10; ++w) r.w[d + w] = r.w[b + w];
+      }
+      ++k;
+    }
+  }
+  wr->n = k;
+}
 
 // TrackedContact::copy_geometry_from into point 0 (data kept).
 __device__ __forceinline__ void copy_geometry0(const Rec& r, V3 p1, V3 p2, uint32_t f1, uint32_t f2, float dist, bool flipped) {
@@ -632,10 +654,20 @@ __device__ __forceinline__ void mf_capsule_capsule(const Rec& r, const Pose& pos
   }
 }
 
-// The end of contact_manifold_convex_ball (contact_manifolds_convex_ball.rs:61-145, no normal
-// constraints) from the projection of the ball centre (pos12.t) on shape 1.
+// Row + 1 of shape i's normal constraints in sh.pseudo, 0 = none (only TriMesh triangles of a mesh
+// with FIX_INTERNAL_EDGES have some).
+__device__ __forceinline__ uint32_t constraint_row(const ShapeArrays& sh, uint32_t i) {
+  if (!sh.pseudo || i < sh.pseudo_first || sh.types[i] != SH_TRIANGLE) return 0u;
+  return __float_as_uint(sh.params[i].z);
+}
+
+// The end of contact_manifold_convex_ball (contact_manifolds_convex_ball.rs:61-145) from the
+// projection of the ball centre (pos12.t) on shape 1. c1 / c2: normal constraints of shape 1 / the
+// ball (null = None); a corrected normal moves the shape-1 point to where the ray from the ball
+// centre along it meets shape 1, which only a triangle (the one shape with constraints) supports.
 __device__ __forceinline__ void finish_convex_ball(const Rec& r, const Pose& pos12, V3 lp1, bool inside, uint32_t fid1, float radius2,
-                                                   float prediction, bool flipped) {
+                                                   float prediction, bool flipped, const TriPN* c1 = nullptr, const TriPN* c2 = nullptr,
+                                                   const ShapeDev* s1 = nullptr) {
   V3 lp21 = pos12.t;
   V3 n1;
   float dist;
@@ -646,6 +678,23 @@ __device__ __forceinline__ void finish_convex_ball(const Rec& r, const Pose& pos
   if (inside) { n1 = -n1; dist = -dist; }
   if (dist <= radius2 + prediction) {
     V3 n2 = pose_inv_rotate(pos12, -n1);
+    if (c1 || c2) {
+      const V3 uncorrected_n2 = n2;
+      if (!project_local_normals(c1, c2, pos12, &n1, &n2)) { r.w[0] = 0; return; }
+      if (!v3_eq(uncorrected_n2, n2)) {
+        // Shape::cast_local_ray_and_get_normal(ray from the ball centre, f32::MAX, solid = false)
+        const V3 rd = inside ? n1 : -n1;
+        TriHit h;
+        if (!s1 || s1->type != SH_TRIANGLE || !ray_triangle_toi(ldv(s1->pts), ldv(s1->pts + 3), ldv(s1->pts + 6), lp21, rd, &h) ||
+            !(h.toi <= FLT_MAX)) {
+          r.w[0] = 0;
+          return;
+        }
+        lp1 = lp21 + rd * h.toi;
+        dist = inside ? -h.toi : h.toi;
+        fid1 = pf_face(h.fid);
+      }
+    }
     V3 lp2 = n2 * radius2;
     if (r.n() != 1) {
       Writer wr{r, 0, false};
@@ -663,7 +712,7 @@ __device__ __forceinline__ void finish_convex_ball(const Rec& r, const Pose& pos
 
 // contact_manifold_convex_ball for a cuboid, capsule or triangle shape 1: analytic projection.
 __device__ __forceinline__ void mf_convex_ball(const Rec& r, const Pose& pos12, const ShapeDev& s1, float radius2, float prediction,
-                                               bool flipped) {
+                                               bool flipped, const TriPN* c1 = nullptr) {
   V3 lp21 = pos12.t;
   PointProj p;
   uint32_t fid1;
@@ -677,7 +726,7 @@ __device__ __forceinline__ void mf_convex_ball(const Rec& r, const Pose& pos12, 
     p = project_capsule(s1.a, s1.b, lp21);
     fid1 = pf_face(0);
   }
-  finish_convex_ball(r, pos12, p.point, p.inside, fid1, radius2, prediction, flipped);
+  finish_convex_ball(r, pos12, p.point, p.inside, fid1, radius2, prediction, flipped, c1, nullptr, &s1);
 }
 
 // ConvexPolyhedron::project_local_point_and_get_feature's feature (point_support_map.rs:62-76).
@@ -831,7 +880,7 @@ static __device__ __noinline__ float sat_cuboid_triangle_edge_twoway(V3 he1, con
 // constraints): the cuboid is shape 1 of the SAT; `flipped` when the triangle is the record's first
 // shape (pos12: cuboid frame to triangle frame).
 static __device__ __noinline__ void mf_cuboid_triangle(const Rec& r, const Pose& pos12, const Pose& pos21, V3 he1, const ShapeDev& tri2,
-                                                       float prediction, bool flipped, bool* overflow) {
+                                                       float prediction, bool flipped, bool* overflow, const float* pseudo, uint32_t j2) {
   if (try_update_contacts(r, flipped ? pos21 : pos12, COS_1_DEGREES, 1.0e-6f)) return;
   V3 d1, d2, d3;
   float sep1 = sat_cuboid_triangle_normal_oneway(he1, tri2, pos12, &d1);
@@ -841,15 +890,22 @@ static __device__ __noinline__ void mf_cuboid_triangle(const Rec& r, const Pose&
   float sep3 = sat_cuboid_triangle_edge_twoway(he1, tri2, pos12, &d3);
   if (sep3 > prediction) { r.w[0] = 0; return; }
   V3 normal1 = d1;
-  if (sep2 > sep1 && sep2 > sep3) normal1 = pose_rotate(pos12, -d2);
-  else if (sep3 > sep1) normal1 = d3;
+  float dist = sep1;
+  if (sep2 > sep1 && sep2 > sep3) { normal1 = pose_rotate(pos12, -d2); dist = sep2; }
+  else if (sep3 > sep1) { normal1 = d3; dist = sep3; }
   V3 normal2 = pose_rotate(pos21, -normal1);
+  // the triangle's normal constraints (the cuboid has none)
+  TriPN pn;
+  const TriPN* c2 = nullptr;
+  if (j2) { pn = load_tri_pn(pseudo, j2 - 1); c2 = &pn; }
+  if (c2 && !project_local_normals(nullptr, c2, pos12, &normal1, &normal2)) { r.w[0] = 0; return; }
   PolyFeature f1 = cuboid_support_face(he1, normal1);
   PolyFeature f2 = triangle_feature(tri2);
   OldPts old;
   save_old(r, old);
   Writer wr{r, 0, false};
   feature_contacts(pos12, normal1, f1, f2, wr, flipped);
+  if (c2) retain_close_depths(r, &wr, dist);
   r.w[0] = wr.n;
   if (flipped) set_normals(r, normal2, normal1);
   else set_normals(r, normal1, normal2);
@@ -872,19 +928,33 @@ __device__ __forceinline__ PolyFeature support_feature(const ShapeDev& s, const 
   return segment_feature(s.a);
 }
 
-// The part of contact_manifold_pfm_pfm after the GJK / EPA query (contact_manifolds_pfm_pfm.rs:77-162).
+// The part of contact_manifold_pfm_pfm after the GJK / EPA query (contact_manifolds_pfm_pfm.rs:77-162);
+// c1 / c2 = normal constraints of shape 1 / 2 (null = None).
 static __device__ __noinline__ void finish_pfm(const Rec& r, const Pose& pos12, const ShapeDev& s1, const HullDev& h1, const ShapeDev& s2,
-                                               const HullDev& h2, int kind, V3 p1, V3 p2, V3 dir, bool* overflow, bool* bad) {
+                                               const HullDev& h2, int kind, V3 p1, V3 p2, V3 dir, bool* overflow, bool* bad,
+                                               const float* pseudo, uint32_t j1, uint32_t j2) {
   float br1 = s1.type == SH_CAPSULE ? s1.b : 0.0f, br2 = s2.type == SH_CAPSULE ? s2.b : 0.0f;
+  TriPN pn1, pn2;
+  const TriPN* c1 = nullptr;
+  const TriPN* c2 = nullptr;
+  if (j1) { pn1 = load_tri_pn(pseudo, j1 - 1); c1 = &pn1; }
+  if (j2) { pn2 = load_tri_pn(pseudo, j2 - 1); c2 = &pn2; }
   OldPts old;
   save_old(r, old);
   Writer wr{r, 0, false};
   if (kind == GJK_CLOSEST) {
     V3 n1 = dir;
     V3 n2 = pose_inv_rotate(pos12, -dir);
+    const float dist = dot(p2 - p1, n1);
+    if ((c1 || c2) && !project_local_normals(c1, c2, pos12, &n1, &n2)) {
+      r.w[0] = 0;  // discarded: points cleared, cached normals and the old points' data left as they were
+      return;
+    }
     PolyFeature f1 = support_feature(s1, h1, n1, bad), f2 = support_feature(s2, h2, n2, bad);
     feature_contacts(pos12, n1, f1, f2, wr, false);
-    wr.push(p1, pose_inv_point(pos12, p2), PF_UNKNOWN, PF_UNKNOWN, dot(p2 - p1, n1), false);
+    // the GJK point only while the normal is GJK's own direction
+    if (v3_eq(n1, dir)) wr.push(p1, pose_inv_point(pos12, p2), PF_UNKNOWN, PF_UNKNOWN, dot(p2 - p1, n1), false);
+    if (c1 || c2) retain_close_depths(r, &wr, dist);
     if (br1 != 0.0f || br2 != 0.0f) {
       for (uint32_t i = 0; i < wr.n; ++i) {
         int b = Rec::pt(i);
@@ -1026,11 +1096,19 @@ __global__ void __launch_bounds__(MF_THREADS) k_mf_kind(ShapeArrays sh, const ui
     } else if constexpr (KIND == MK_CAPSULE_CAPSULE) {
       mf_capsule_capsule(r, pos12, s1.a, s1.b, s2.a, s2.b, prediction);
     } else if constexpr (KIND == MK_CUBOID_TRIANGLE) {
-      if (s1.type == SH_CUBOID) mf_cuboid_triangle(r, pos12, pose_inverse(pos12), v3(s1.a, s1.b, s1.c), s2, prediction, false, &overflow);
-      else mf_cuboid_triangle(r, pose_inverse(pos12), pos12, v3(s2.a, s2.b, s2.c), s1, prediction, true, &overflow);
+      if (s1.type == SH_CUBOID)
+        mf_cuboid_triangle(r, pos12, pose_inverse(pos12), v3(s1.a, s1.b, s1.c), s2, prediction, false, &overflow, sh.pseudo,
+                           constraint_row(sh, b));
+      else
+        mf_cuboid_triangle(r, pose_inverse(pos12), pos12, v3(s2.a, s2.b, s2.c), s1, prediction, true, &overflow, sh.pseudo,
+                           constraint_row(sh, a));
     } else if constexpr (KIND == MK_CONVEX_BALL) {
       bool ball_first = s1.type == SH_BALL;
-      mf_convex_ball(r, ball_first ? pose_inverse(pos12) : pos12, ball_first ? s2 : s1, ball_first ? s1.a : s2.a, prediction, ball_first);
+      const uint32_t j = constraint_row(sh, ball_first ? b : a);
+      TriPN pn;
+      if (j) pn = load_tri_pn(sh.pseudo, j - 1);
+      mf_convex_ball(r, ball_first ? pose_inverse(pos12) : pos12, ball_first ? s2 : s1, ball_first ? s1.a : s2.a, prediction, ball_first,
+                     j ? &pn : nullptr);
     } else if constexpr (KIND == MK_HULL_BALL) {
       bool ball_first = s1.type == SH_BALL;
       Pose cpos = ball_first ? pose_inverse(pos12) : pos12;
@@ -1061,7 +1139,8 @@ __global__ void __launch_bounds__(MF_THREADS) k_mf_kind(ShapeArrays sh, const ui
         simplex_reset(s, cso_from_shapes(pos12, p1, p2, dir));
         GjkOut g = gjk_closest_points(pos12, p1, p2, total_prediction, s, &iters);
         if (g.kind == GJK_INTERSECTION) enqueue(queue, ctr, k, s, TAG_PFM);
-        else finish_pfm(r, pos12, s1, h1, s2, h2, g.kind, g.p1, g.p2, g.dir, &overflow, &bad);
+        else finish_pfm(r, pos12, s1, h1, s2, h2, g.kind, g.p1, g.p2, g.dir, &overflow, &bad, sh.pseudo, constraint_row(sh, a),
+                        constraint_row(sh, b));
       }
     }
     if (overflow) atomicOr(err, ERR_CAPACITY);
@@ -1104,8 +1183,9 @@ __global__ void __launch_bounds__(MF_EPA_THREADS) k_manifolds_epa(ShapeArrays sh
       int res = epa_closest_points(ws, pos12, p1, p2, s, &q1, &q2, &nn, &iters);
       if (res == EPA_OVERFLOW) atomicOr(err, ERR_POLYTOPE_FULL);
       // EPA failure: contact_support_map_support_map_with_params returns NoIntersection(x axis)
-      if (res == EPA_OK) finish_pfm(r, pos12, s1, h1, s2, h2, GJK_CLOSEST, q1, q2, nn, &overflow, &bad);
-      else finish_pfm(r, pos12, s1, h1, s2, h2, GJK_NO_INTERSECTION, q1, q2, v3(1.f, 0.f, 0.f), &overflow, &bad);
+      const uint32_t j1 = constraint_row(sh, a), j2 = constraint_row(sh, b);
+      if (res == EPA_OK) finish_pfm(r, pos12, s1, h1, s2, h2, GJK_CLOSEST, q1, q2, nn, &overflow, &bad, sh.pseudo, j1, j2);
+      else finish_pfm(r, pos12, s1, h1, s2, h2, GJK_NO_INTERSECTION, q1, q2, v3(1.f, 0.f, 0.f), &overflow, &bad, sh.pseudo, j1, j2);
     } else {
       // the ball centre is inside the hull: EPA projection (point_support_map.rs:42-55)
       bool ball_first = tag == TAG_BALL_FIRST;

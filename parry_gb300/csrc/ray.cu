@@ -17,50 +17,13 @@
 #include "internal.hpp"
 #include "common.cuh"
 #include "lbvh_device.cuh"
+#include "tri_ray_device.cuh"
 
 using namespace pg;
 
 namespace {
 
 constexpr int RAY_STACK = 64;
-
-struct TriHit {
-  float toi;
-  uint32_t fid;
-};
-
-// src/query/ray/ray_triangle.rs:70-152, toi and face id only (normal recomputed for the winner).
-__device__ __forceinline__ bool ray_triangle_toi(V3 a, V3 b, V3 c, V3 o, V3 dir, TriHit* h) {
-  V3 ab = b - a;
-  V3 ac = c - a;
-  V3 n = cross(ab, ac);
-  float d = dot(n, dir);
-  if (d == 0.0f) return false;
-  V3 ap = o - a;
-  float t = dot(ap, n);
-  if ((t < 0.0f && d < 0.0f) || (t > 0.0f && d > 0.0f)) return false;
-  uint32_t fid = d < 0.0f ? 0u : 1u;
-  d = fabsf(d);
-  V3 e = -cross(dir, ap);
-  float v, w;
-  if (t < 0.0f) {
-    v = -dot(ac, e);
-    if (v < 0.0f || v > d) return false;
-    w = dot(ab, e);
-    if (w < 0.0f || v + w > d) return false;
-    float invd = 1.0f / d;
-    h->toi = -t * invd;
-  } else {
-    v = dot(ac, e);
-    if (v < 0.0f || v > d) return false;
-    w = -dot(ab, e);
-    if (w < 0.0f || v + w > d) return false;
-    float invd = 1.0f / d;
-    h->toi = t * invd;
-  }
-  h->fid = fid;
-  return true;
-}
 
 // Normal of the winning triangle, as ray_triangle.rs computes it (faces the ray origin).
 __device__ __forceinline__ V3 ray_triangle_normal(V3 a, V3 b, V3 c, V3 o) {
@@ -506,7 +469,7 @@ parrygpu_status parrygpu_trimesh_create(parrygpu_ctx* ctx, const float* vertices
 void parrygpu_trimesh_destroy(parrygpu_trimesh* m) {
   if (!m) return;
   for (DevBuf* d : {&m->bvh.wide, &m->bvh.leaf_parent, &m->bvh.node_parent, &m->bvh.leaf_index, &m->bvh.flags, &m->bvh.root_aabb,
-                    &m->bvh.info, &m->soup})
+                    &m->bvh.info, &m->soup, &m->pseudo, &m->pseudo_ok})
     d->release();
   delete m;
 }

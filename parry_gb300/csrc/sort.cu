@@ -188,3 +188,12 @@ parrygpu_status radix_sort_pairs_in(parrygpu_ctx* ctx, uint32_t n, int key_bits,
 }
 
 uint32_t radix_sort_hist_entries(uint32_t n) { return div_up(n ? n : 1, RS_TILE) * RS_BINS; }
+
+// In-place exclusive prefix sum of `m` words in one block (the buffer holds m rounded up to a
+// multiple of 4 words, the padding zeroed).
+parrygpu_status exclusive_scan_u32(parrygpu_ctx* ctx, uint32_t* data, uint32_t m) {
+  if (m == 0) return PARRYGPU_OK;
+  k_rs_scan<<<1, SCAN_THREADS, 0, ctx->stream>>>(data, (m + 3u) & ~3u);
+  PG_LAUNCHED(ctx);
+  return PARRYGPU_OK;
+}

@@ -7,7 +7,8 @@
 //   - one ContactManifold per interfering triangle, carried over by triangle id when the list is
 //     queried again (a new triangle starts from ContactManifold::new());
 //   - each (triangle, shape) manifold is DefaultQueryDispatcher::contact_manifold_convex_convex with
-//     the triangle as shape 1 (no pseudo-normals: no normal constraints).
+//     the triangle as shape 1 and, when the mesh has FIX_INTERNAL_EDGES, the triangle's
+//     pseudo-normals as its normal constraints (TriMesh::triangle_normal_constraints).
 // Interference lists are kept in ascending triangle order: the reference's carry-over loop walks the
 // old and new lists as sorted lists, and its BVH returns them in tree order.
 //
@@ -60,14 +61,16 @@ __global__ void k_invalid_aabbs(float* __restrict__ aabb, uint32_t n) {
 }
 
 // The triangle part of the combined shape set: triangle t is shape n + t with its vertices at pool
-// offset m + 3t, posed at the mesh pose.
-__global__ void k_fill_triangles(uint32_t n, uint32_t nt, uint64_t m, Pose mesh, uint32_t* __restrict__ types, float4* __restrict__ params,
-                                 float* __restrict__ poses) {
+// offset m + 3t, posed at the mesh pose; params word 2 = t + 1 when the triangle has normal
+// constraints (row t of the mesh's pseudo-normal table; `ok` null = none).
+__global__ void k_fill_triangles(uint32_t n, uint32_t nt, uint64_t m, Pose mesh, const uint8_t* __restrict__ ok,
+                                 uint32_t* __restrict__ types, float4* __restrict__ params, float* __restrict__ poses) {
   uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= nt) return;
   uint32_t i = n + t;
   types[i] = SH_TRIANGLE;
-  params[i] = make_float4(__uint_as_float((uint32_t)(m + 3ull * t)), __uint_as_float(3u), 0.0f, 0.0f);
+  const uint32_t row = (ok && ok[t]) ? t + 1u : 0u;
+  params[i] = make_float4(__uint_as_float((uint32_t)(m + 3ull * t)), __uint_as_float(3u), __uint_as_float(row), 0.0f);
   float* p = poses + 7 * (size_t)i;
   p[0] = mesh.qi; p[1] = mesh.qj; p[2] = mesh.qk; p[3] = mesh.qw; p[4] = mesh.t.x; p[5] = mesh.t.y; p[6] = mesh.t.z;
 }
@@ -267,11 +270,13 @@ parrygpu_status parrygpu_trimesh_contacts_update(parrygpu_ctx* ctx, parrygpu_tri
   if (m) PG_CUDA(ctx, cudaMemcpyAsync(tc->pool.ptr, sh.pool, m * 12, cudaMemcpyDeviceToDevice, ctx->stream));
   if (nt) PG_CUDA(ctx, cudaMemcpyAsync(tc->pool.as<float>() + 3 * m, tc->tri_pool.ptr, (size_t)nt * 36, cudaMemcpyDeviceToDevice, ctx->stream));
   if (nt) {
-    k_fill_triangles<<<div_up(nt, 256), 256, 0, ctx->stream>>>(n, nt, m, mesh, tc->types.as<uint32_t>(), tc->params.as<float4>(),
-                                                               tc->poses.as<float>());
+    k_fill_triangles<<<div_up(nt, 256), 256, 0, ctx->stream>>>(n, nt, m, mesh,
+                                                               tc->mesh->constrained() ? tc->mesh->pseudo_ok.as<uint8_t>() : nullptr,
+                                                               tc->types.as<uint32_t>(), tc->params.as<float4>(), tc->poses.as<float>());
     PG_LAUNCHED(ctx);
   }
-  ShapeArrays cs{tc->types.as<uint32_t>(), tc->params.as<float4>(), tc->poses.as<float>(), tc->pool.as<float>(), total, nv, sh.poly};
+  ShapeArrays cs{tc->types.as<uint32_t>(), tc->params.as<float4>(), tc->poses.as<float>(), tc->pool.as<float>(), total, nv, sh.poly,
+                 tc->mesh->constrained() ? tc->mesh->pseudo.as<float>() : nullptr, n};
   const int cur = tc->cur, nw = 1 - cur;
   {
     KernelTimer kt(ctx, "trimesh_contacts_workspace");

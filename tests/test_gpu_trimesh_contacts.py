@@ -28,15 +28,17 @@ def _scene(n_pairs, seed, nx=48, nz=24):
     return v, i, (t, prm, pos, pool, poly), vel
 
 
+@pytest.mark.parametrize("fix", [False, True])
 @pytest.mark.parametrize("mesh_pose", [None, [0.0, 0.0, 0.0, 1.0, 0.25, -0.5, 0.125]])
-def test_trimesh_contacts_frames_bit_exact(gpu_ctx, oracle_lib, mesh_pose):
+def test_trimesh_contacts_frames_bit_exact(gpu_ctx, oracle_lib, mesh_pose, fix):
+    """With and without TriMeshFlags::FIX_INTERNAL_EDGES (normal constraints from pseudo-normals)."""
     O = oracle_lib
     v, i, (t, prm, pos, pool, poly), vel = _scene(300, 21)
     n = len(t)
-    mesh = pg.TriMesh(gpu_ctx, v, i)
+    mesh = pg.TriMesh(gpu_ctx, v, i, flags=pg.TRIMESH_FIX_INTERNAL_EDGES if fix else 0)
     K = 256
     tc = pg.TriMeshContacts(gpu_ctx, mesh, n, K)
-    ref = O.TriMeshContacts(v, i, n)
+    ref = O.TriMeshContacts(v, i, n, fix_internal_edges=fix)
     mp = np.array([0, 0, 0, 1, 0, 0, 0], np.float32) if mesh_pose is None else np.array(mesh_pose, np.float32)
     moved = 0
     for f in range(6):
