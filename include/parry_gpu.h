@@ -120,6 +120,25 @@ parrygpu_status parrygpu_bvh_leaf_pairs(parrygpu_ctx* ctx, const parrygpu_bvh* a
 parrygpu_status parrygpu_bvh_info(const parrygpu_bvh* bvh, uint32_t* leaf_count, uint32_t* wide_node_count);
 /* Copies the tree's wide nodes (wide_node_count x 64 bytes, BvhNodeWide layout) into `out`. */
 parrygpu_status parrygpu_bvh_copy_nodes(parrygpu_ctx* ctx, const parrygpu_bvh* bvh, void* out);
+/* The reference's serialised Bvh (src/partitioning/bvh/bvh_tree.rs:1748-1761: nodes, parents,
+ * leaf_node_indices; BvhNodeIndex = (wide node << 1) | is_right, bvh_tree.rs:1244-1290), host or
+ * device buffers, any may be NULL: nodes = wide_node_count x 64 bytes, parents = wide_node_count
+ * u64 (the root's entry 0), leaf_nodes = leaf_capacity u64 indexed by leaf index (UINT64_MAX where no
+ * leaf has that index; a leaf index >= leaf_capacity raises CAPACITY_EXCEEDED). */
+parrygpu_status parrygpu_bvh_export(parrygpu_ctx* ctx, const parrygpu_bvh* bvh, void* nodes, uint64_t* parents, uint64_t* leaf_nodes,
+                                    uint64_t leaf_capacity);
+/* A tree from the reference's serialised nodes (n_wide BvhNodeWide records, host or device; e.g.
+ * deserialised from parry's serde / rkyv form): parents and depth-first leaf positions are derived
+ * on the device. Malformed trees (child index out of range, a node with two parents or none, leaf
+ * counts that do not add up) are rejected with INVALID_ARG. */
+parrygpu_status parrygpu_bvh_import(parrygpu_ctx* ctx, const void* nodes, uint32_t n_wide, parrygpu_bvh** out);
+/* Bvh::insert(aabb, leaf_index) (bvh_insert.rs:126-133) for k rows: a new leaf index is added, an
+ * existing one takes the new AABB (the last row wins); Bvh::remove(leaf_index) (bvh_tree.rs:2360) for
+ * k indices (indices without a leaf are ignored). The tree is rebuilt over the resulting leaf set
+ * (decision D-9: the layout differs from the reference's incremental edits, query answers do not).
+ * Afterwards parrygpu_bvh_refit takes 1 + (largest leaf index) AABB rows indexed by leaf index. */
+parrygpu_status parrygpu_bvh_insert(parrygpu_ctx* ctx, parrygpu_bvh* bvh, const float* aabbs, const uint32_t* leaf_ids, uint32_t k);
+parrygpu_status parrygpu_bvh_remove(parrygpu_ctx* ctx, parrygpu_bvh* bvh, const uint32_t* leaf_ids, uint32_t k);
 
 /* ---- TriMesh ray casts ------------------------------------------------------------------- */
 

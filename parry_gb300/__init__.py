@@ -174,6 +174,56 @@ class Bvh:
         check(lib().parrygpu_bvh_build(ctx.handle, p, n, C.byref(h)), ctx.handle)
         return cls(ctx, h)
 
+    @classmethod
+    def from_serialized(cls, ctx: Context, nodes) -> "Bvh":
+        """A tree in the reference's serialised layout (Bvh::nodes, BvhNodeWide records: (n_wide, 16)
+        float32 words or 64-byte rows), e.g. one built by parry; parents and leaf positions are
+        derived on the device."""
+        raw = np.ascontiguousarray(nodes)
+        raw = raw.view(np.float32).reshape(-1, 16) if raw.size else np.zeros((0, 16), np.float32)
+        h = C.c_void_p()
+        check(lib().parrygpu_bvh_import(ctx.handle, C.c_void_p(raw.ctypes.data) if len(raw) else None, len(raw), C.byref(h)), ctx.handle)
+        return cls(ctx, h)
+
+    def serialize(self, leaf_capacity: int | None = None):
+        """The reference's serialised Bvh: (nodes (n_wide, 16) f32 words in BvhNodeWide layout,
+        parents (n_wide,) u64 BvhNodeIndex, leaf_node_indices (leaf_capacity,) u64 BvhNodeIndex per
+        leaf index, 2**64 - 1 where no leaf has that index)."""
+        lc, wc = self.info()
+        cap = int(leaf_capacity) if leaf_capacity is not None else self.id_bound()
+        nodes = np.zeros((wc, 16), np.float32)
+        parents = np.zeros(wc, np.uint64)
+        leaves = np.zeros(cap, np.uint64)
+        check(lib().parrygpu_bvh_export(self.ctx.handle, self._h, C.c_void_p(nodes.ctypes.data) if wc else None,
+                                        C.c_void_p(parents.ctypes.data) if wc else None, C.c_void_p(leaves.ctypes.data) if cap else None,
+                                        cap), self.ctx.handle)
+        return nodes, parents, leaves
+
+    def id_bound(self) -> int:
+        """1 + the largest leaf index (the row count refit() expects)."""
+        nodes = self.nodes()
+        if len(nodes) == 0:
+            return 0
+        w = nodes.view(np.uint32)
+        leaf = (w[:, [7, 15]] & 0x3FFFFFFF) == 1
+        ids = w[:, [3, 11]][leaf]
+        return int(ids.max()) + 1 if len(ids) else 0
+
+    def insert(self, aabbs, leaf_ids) -> None:
+        """Bvh::insert for each (aabb, leaf index) row: new indices are added, existing ones get the
+        new AABB (the last row wins). The tree is rebuilt over the resulting leaves; refit() then
+        takes AABBs indexed by leaf index."""
+        ka, pa = _as_input(aabbs, np.float32)
+        ki, pi = _as_input(leaf_ids, np.uint32)
+        k = int(ki.shape[0]) if ki is not None else 0
+        check(lib().parrygpu_bvh_insert(self.ctx.handle, self._h, pa, pi, k), self.ctx.handle)
+
+    def remove(self, leaf_ids) -> None:
+        """Bvh::remove for each leaf index (indices without a leaf are ignored)."""
+        ki, pi = _as_input(leaf_ids, np.uint32)
+        k = int(ki.shape[0]) if ki is not None else 0
+        check(lib().parrygpu_bvh_remove(self.ctx.handle, self._h, pi, k), self.ctx.handle)
+
     def rebuild(self, aabbs) -> None:
         """Bvh::from_leaves over new AABBs into this handle (its device storage is reused)."""
         ka, pa = _as_input(aabbs, np.float32)

@@ -51,6 +51,10 @@ SIGNATURES: dict[str, tuple] = {
     "parrygpu_bvh_leaf_pairs": (I32, [P, P, P, P, U64, PU64, I32]),
     "parrygpu_bvh_info": (I32, [P, PU32, PU32]),
     "parrygpu_bvh_copy_nodes": (I32, [P, P, P]),
+    "parrygpu_bvh_export": (I32, [P, P, P, P, P, U64]),
+    "parrygpu_bvh_import": (I32, [P, P, U32, C.POINTER(P)]),
+    "parrygpu_bvh_insert": (I32, [P, P, P, P, U32]),
+    "parrygpu_bvh_remove": (I32, [P, P, P, U32]),
     "parrygpu_trimesh_create": (I32, [P, P, U32, P, U32, C.POINTER(P)]),
     "parrygpu_trimesh_destroy": (None, [P]),
     "parrygpu_trimesh_set_flags": (I32, [P, P, U32]),

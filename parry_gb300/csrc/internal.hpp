@@ -103,6 +103,7 @@ struct parrygpu_bvh {
   DevBuf info;          // per internal node: (split position gamma, last sorted leaf of its range)
   DevBuf root_aabb;     // 6 floats
   bool leaf_data_is_position = false;
+  uint32_t id_bound = 0;  // 1 + the largest leaf index (= n_leaves for a tree built over 0..n-1)
 };
 
 struct parrygpu_trimesh {
@@ -169,7 +170,9 @@ parrygpu_status launch_trimesh_rays(parrygpu_ctx* ctx, const parrygpu_trimesh* m
 // ---- LBVH (lbvh.cu) ----
 // Builds `bvh` from `n` device AABBs (n x 6 floats). When leaf_data_is_position, leaf nodes store
 // their sorted position instead of the AABB index.
-parrygpu_status lbvh_build(parrygpu_ctx* ctx, parrygpu_bvh* bvh, const float* d_aabbs, uint32_t n, bool leaf_data_is_position);
+// d_ids (may be null): leaf data of input leaf i is d_ids[i] instead of i (then id_bound = max id + 1).
+parrygpu_status lbvh_build(parrygpu_ctx* ctx, parrygpu_bvh* bvh, const float* d_aabbs, uint32_t n, bool leaf_data_is_position,
+                           const uint32_t* d_ids = nullptr, uint32_t id_bound = 0);
 parrygpu_status lbvh_refit(parrygpu_ctx* ctx, parrygpu_bvh* bvh, const float* d_aabbs);
 // traverse_bvtt_single_tree into device buffers: pairs beyond `cap` are counted in *d_count but not
 // written. No allocation, no host synchronisation.

@@ -77,11 +77,19 @@ __device__ __forceinline__ int lcp(const uint32_t* __restrict__ keys, int n, int
   return 32 + __clz((uint32_t)i ^ (uint32_t)j);
 }
 
+// Leaf data of sorted position i: the input index, or ids[input index] when the caller names its
+// leaves (Bvh::insert with arbitrary leaf indices).
+__device__ __forceinline__ uint32_t leaf_id(const uint32_t* __restrict__ sorted_vals, const uint32_t* __restrict__ ids, int i) {
+  const uint32_t v = sorted_vals[i];
+  return ids ? ids[v] : v;
+}
+
 __global__ void k_karras(const uint32_t* __restrict__ keys, const uint32_t* __restrict__ sorted_vals, int n,
                          WideNode* __restrict__ wide, uint32_t* __restrict__ leaf_parent, uint32_t* __restrict__ node_parent,
-                         uint32_t* __restrict__ leaf_index, uint2* __restrict__ info, int leaf_data_is_position) {
+                         uint32_t* __restrict__ leaf_index, uint2* __restrict__ info, int leaf_data_is_position,
+                         const uint32_t* __restrict__ ids) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) leaf_index[i] = sorted_vals[i];
+  if (i < n) leaf_index[i] = leaf_id(sorted_vals, ids, i);
   if (i >= n - 1) return;
   int d = (lcp(keys, n, i, i + 1) - lcp(keys, n, i, i - 1)) >= 0 ? 1 : -1;
   int dmin = lcp(keys, n, i, i - d);
@@ -102,7 +110,7 @@ __global__ void k_karras(const uint32_t* __restrict__ keys, const uint32_t* __re
   info[i] = make_uint2((uint32_t)gamma, (uint32_t)last);
   uint32_t lchild, lcount, rchild, rcount;
   if (first == gamma) {
-    lchild = leaf_data_is_position ? (uint32_t)gamma : sorted_vals[gamma];
+    lchild = leaf_data_is_position ? (uint32_t)gamma : leaf_id(sorted_vals, ids, gamma);
     lcount = 1;
     leaf_parent[gamma] = ((uint32_t)i << 1) | 0u;
   } else {
@@ -111,7 +119,7 @@ __global__ void k_karras(const uint32_t* __restrict__ keys, const uint32_t* __re
     node_parent[gamma] = ((uint32_t)i << 1) | 0u;
   }
   if (last == gamma + 1) {
-    rchild = leaf_data_is_position ? (uint32_t)(gamma + 1) : sorted_vals[gamma + 1];
+    rchild = leaf_data_is_position ? (uint32_t)(gamma + 1) : leaf_id(sorted_vals, ids, gamma + 1);
     rcount = 1;
     leaf_parent[gamma + 1] = ((uint32_t)i << 1) | 1u;
   } else {
@@ -133,12 +141,14 @@ __device__ __forceinline__ void store_node_aabb(BvhNodeDev* nd, float3 mn, float
   __stcg(f + 4, mx.x); __stcg(f + 5, mx.y); __stcg(f + 6, mx.z);
 }
 
+// rows (may be null): the AABB row of each sorted leaf when it is not the leaf data (a build over a
+// compact list of named leaves).
 __global__ void __launch_bounds__(FIT_THREADS) k_fit(const float* __restrict__ aabbs, uint32_t n, const uint32_t* __restrict__ leaf_index,
                                                      const uint32_t* __restrict__ leaf_parent, const uint32_t* __restrict__ node_parent,
-                                                     WideNode* wide, uint32_t* flags, float* root_aabb) {
+                                                     WideNode* wide, uint32_t* flags, float* root_aabb, const uint32_t* __restrict__ rows) {
   uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= n) return;
-  const float* a = aabbs + 6 * (size_t)leaf_index[p];
+  const float* a = aabbs + 6 * (size_t)(rows ? rows[p] : leaf_index[p]);
   float3 mn = make_float3(a[0], a[1], a[2]);
   float3 mx = make_float3(a[3], a[4], a[5]);
   uint32_t lp = leaf_parent[p];
@@ -171,26 +181,29 @@ __global__ void __launch_bounds__(FIT_THREADS) k_fit(const float* __restrict__ a
 
 // Single-leaf tree: the reference's "partial root" (right child zeroed, bvh_tree.rs:1921-1929).
 __global__ void k_single_leaf(const float* __restrict__ aabbs, WideNode* wide, uint32_t* leaf_index, uint32_t* leaf_parent,
-                              float* root_aabb, int leaf_data_is_position) {
+                              float* root_aabb, int leaf_data_is_position, const uint32_t* __restrict__ ids) {
   if (threadIdx.x != 0) return;
   WideNode w;
   float* f = reinterpret_cast<float*>(&w);
   for (int k = 0; k < 16; ++k) f[k] = 0.0f;
   w.l.mins = make_float3(aabbs[0], aabbs[1], aabbs[2]);
   w.l.maxs = make_float3(aabbs[3], aabbs[4], aabbs[5]);
-  w.l.children = 0;
+  const uint32_t id = (ids && !leaf_data_is_position) ? ids[0] : 0u;
+  w.l.children = id;
   w.l.data = 1u | (3u << 30);
   w.r.children = 0;
   w.r.data = 0;
   wide[0] = w;
-  leaf_index[0] = 0;
+  leaf_index[0] = id;
   leaf_parent[0] = 0;
   for (int k = 0; k < 6; ++k) root_aabb[k] = aabbs[k];
   (void)leaf_data_is_position;
 }
 
-__global__ void k_single_leaf_refit(const float* __restrict__ aabbs, WideNode* wide, float* root_aabb) {
+__global__ void k_single_leaf_refit(const float* __restrict__ aabbs, const uint32_t* __restrict__ leaf_index, int leaf_data_is_position,
+                                    WideNode* wide, float* root_aabb) {
   if (threadIdx.x != 0) return;
+  aabbs += leaf_data_is_position ? 0 : 6 * (size_t)leaf_index[0];
   wide[0].l.mins = make_float3(aabbs[0], aabbs[1], aabbs[2]);
   wide[0].l.maxs = make_float3(aabbs[3], aabbs[4], aabbs[5]);
   for (int k = 0; k < 6; ++k) root_aabb[k] = aabbs[k];
@@ -362,8 +375,12 @@ parrygpu_status sort_pairs_inplace(parrygpu_ctx* ctx, uint32_t* d_pairs, uint64_
 
 }  // namespace
 
-parrygpu_status lbvh_build(parrygpu_ctx* ctx, parrygpu_bvh* bvh, const float* d_aabbs, uint32_t n, bool leaf_data_is_position) {
+static parrygpu_status lbvh_fit(parrygpu_ctx* ctx, parrygpu_bvh* bvh, const float* d_aabbs, const uint32_t* rows);
+
+parrygpu_status lbvh_build(parrygpu_ctx* ctx, parrygpu_bvh* bvh, const float* d_aabbs, uint32_t n, bool leaf_data_is_position,
+                           const uint32_t* d_ids, uint32_t id_bound) {
   bvh->n_leaves = n;
+  bvh->id_bound = d_ids ? id_bound : n;
   bvh->leaf_data_is_position = leaf_data_is_position;
   bvh->n_wide = n == 0 ? 0 : (n == 1 ? 1 : n - 1);
   if (n == 0) return PARRYGPU_OK;
@@ -376,7 +393,7 @@ parrygpu_status lbvh_build(parrygpu_ctx* ctx, parrygpu_bvh* bvh, const float* d_
   PG_CUDA(ctx, bvh->root_aabb.reserve(6 * 4));
   if (n == 1) {
     k_single_leaf<<<1, 32, 0, ctx->stream>>>(d_aabbs, bvh->wide.as<WideNode>(), bvh->leaf_index.as<uint32_t>(),
-                                             bvh->leaf_parent.as<uint32_t>(), bvh->root_aabb.as<float>(), leaf_data_is_position);
+                                             bvh->leaf_parent.as<uint32_t>(), bvh->root_aabb.as<float>(), leaf_data_is_position, d_ids);
     PG_LAUNCHED(ctx);
     PG_CUDA(ctx, cudaMemsetAsync(bvh->info.ptr, 0, 8, ctx->stream));
     return PARRYGPU_OK;
@@ -397,23 +414,26 @@ parrygpu_status lbvh_build(parrygpu_ctx* ctx, parrygpu_bvh* bvh, const float* d_
   k_karras<<<div_up(n, 256), 256, 0, ctx->stream>>>(ctx->sort_k[rb].as<uint32_t>(), ctx->sort_v[rb].as<uint32_t>(), (int)n,
                                                     bvh->wide.as<WideNode>(), bvh->leaf_parent.as<uint32_t>(),
                                                     bvh->node_parent.as<uint32_t>(), bvh->leaf_index.as<uint32_t>(),
-                                                    bvh->info.as<uint2>(), leaf_data_is_position ? 1 : 0);
+                                                    bvh->info.as<uint2>(), leaf_data_is_position ? 1 : 0, d_ids);
   PG_LAUNCHED(ctx);
-  return lbvh_refit(ctx, bvh, d_aabbs);
+  return lbvh_fit(ctx, bvh, d_aabbs, d_ids ? ctx->sort_v[rb].as<uint32_t>() : nullptr);
 }
 
-parrygpu_status lbvh_refit(parrygpu_ctx* ctx, parrygpu_bvh* bvh, const float* d_aabbs) {
+parrygpu_status lbvh_refit(parrygpu_ctx* ctx, parrygpu_bvh* bvh, const float* d_aabbs) { return lbvh_fit(ctx, bvh, d_aabbs, nullptr); }
+
+static parrygpu_status lbvh_fit(parrygpu_ctx* ctx, parrygpu_bvh* bvh, const float* d_aabbs, const uint32_t* rows) {
   uint32_t n = bvh->n_leaves;
   if (n == 0) return PARRYGPU_OK;
   if (n == 1) {
-    k_single_leaf_refit<<<1, 32, 0, ctx->stream>>>(d_aabbs, bvh->wide.as<WideNode>(), bvh->root_aabb.as<float>());
+    k_single_leaf_refit<<<1, 32, 0, ctx->stream>>>(d_aabbs, bvh->leaf_index.as<uint32_t>(), bvh->leaf_data_is_position ? 1 : 0,
+                                                   bvh->wide.as<WideNode>(), bvh->root_aabb.as<float>());
     PG_LAUNCHED(ctx);
     return PARRYGPU_OK;
   }
   PG_CUDA(ctx, cudaMemsetAsync(bvh->flags.ptr, 0, (size_t)bvh->n_wide * 4, ctx->stream));
   k_fit<<<div_up(n, FIT_THREADS), FIT_THREADS, 0, ctx->stream>>>(d_aabbs, n, bvh->leaf_index.as<uint32_t>(), bvh->leaf_parent.as<uint32_t>(),
                                                                  bvh->node_parent.as<uint32_t>(), bvh->wide.as<WideNode>(),
-                                                                 bvh->flags.as<uint32_t>(), bvh->root_aabb.as<float>());
+                                                                 bvh->flags.as<uint32_t>(), bvh->root_aabb.as<float>(), rows);
   PG_LAUNCHED(ctx);
   return PARRYGPU_OK;
 }
@@ -503,7 +523,7 @@ parrygpu_status parrygpu_bvh_refit(parrygpu_ctx* ctx, parrygpu_bvh* bvh, const f
   if (!ctx || !bvh) return PARRYGPU_INVALID_ARG;
   PG_CUDA(ctx, cudaSetDevice(ctx->device));
   const void* d_aabbs = nullptr;
-  parrygpu_status s = stage_input(ctx, ctx->stage_in[0], aabbs, (size_t)bvh->n_leaves * 24, &d_aabbs);
+  parrygpu_status s = stage_input(ctx, ctx->stage_in[0], aabbs, (size_t)bvh->id_bound * 24, &d_aabbs);
   if (s != PARRYGPU_OK) return s;
   s = lbvh_refit(ctx, bvh, (const float*)d_aabbs);
   if (s != PARRYGPU_OK) return s;
@@ -517,7 +537,7 @@ parrygpu_status parrygpu_bvh_self_pairs(parrygpu_ctx* ctx, const parrygpu_bvh* b
   PG_CUDA(ctx, cudaSetDevice(ctx->device));
   if (bvh->n_leaves < 2) { if (n_out) *n_out = 0; return n_out ? PARRYGPU_OK : PARRYGPU_INVALID_ARG; }
   uint32_t n = bvh->n_leaves;
-  return run_pairs(ctx, pairs, cap, n_out, sorted, n - 1, n - 1, [&](uint32_t* dp, unsigned long long c, unsigned long long* cnt) {
+  return run_pairs(ctx, pairs, cap, n_out, sorted, bvh->id_bound - 1, bvh->id_bound - 1, [&](uint32_t* dp, unsigned long long c, unsigned long long* cnt) {
     k_self_pairs<<<div_up(n, PAIR_THREADS), PAIR_THREADS, 0, ctx->stream>>>(bvh->wide.as<WideNode>(), bvh->info.as<uint2>(),
                                                                             bvh->leaf_parent.as<uint32_t>(), bvh->leaf_index.as<uint32_t>(),
                                                                             n, dp, c, cnt, ctx->d_err);
@@ -532,7 +552,7 @@ parrygpu_status parrygpu_bvh_leaf_pairs(parrygpu_ctx* ctx, const parrygpu_bvh* a
   PG_CUDA(ctx, cudaSetDevice(ctx->device));
   if (a->n_leaves == 0 || b->n_leaves == 0) { if (n_out) *n_out = 0; return n_out ? PARRYGPU_OK : PARRYGPU_INVALID_ARG; }
   uint32_t na = a->n_leaves, nb = b->n_leaves;
-  return run_pairs(ctx, pairs, cap, n_out, sorted, na - 1, nb - 1, [&](uint32_t* dp, unsigned long long c, unsigned long long* cnt) {
+  return run_pairs(ctx, pairs, cap, n_out, sorted, a->id_bound - 1, b->id_bound - 1, [&](uint32_t* dp, unsigned long long c, unsigned long long* cnt) {
     k_leaf_pairs<<<div_up(na, PAIR_THREADS), PAIR_THREADS, 0, ctx->stream>>>(a->wide.as<WideNode>(), a->leaf_parent.as<uint32_t>(),
                                                                              a->leaf_index.as<uint32_t>(), na, b->wide.as<WideNode>(), nb,
                                                                              dp, c, cnt, ctx->d_err);

@@ -85,3 +85,20 @@ def random_aabbs(n: int, seed: int, extent: float = 100.0, size: float = 3.0) ->
     c = rng.uniform(-extent, extent, size=(n, 3))
     h = rng.uniform(0.05, size, size=(n, 3))
     return np.concatenate([c - h, c + h], axis=1).astype(np.float32)
+
+
+def serialized_links(nodes: np.ndarray) -> tuple[np.ndarray, dict]:
+    """The `parents` and `leaf_node_indices` a parry Bvh keeps beside its nodes (bvh_tree.rs:1755-1761)
+    recomputed from the nodes alone: parents[w] = BvhNodeIndex (wide << 1 | is_right) of the slot
+    holding wide node w (0 for the root); leaf index -> BvhNodeIndex of its slot."""
+    parents = np.zeros(len(nodes), np.uint64)
+    leaves = {}
+    u = nodes.view(np.uint32)
+    for w in range(len(nodes)):
+        for side in (0, 1):
+            ch, d = int(u[w, 8 * side + 3]), int(u[w, 8 * side + 7]) & 0x3FFFFFFF
+            if d == 1:
+                leaves[ch] = (w << 1) | side
+            elif d > 1:
+                parents[ch] = (w << 1) | side
+    return parents, leaves
