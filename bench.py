@@ -300,6 +300,64 @@ def mixed_contacts(ctx, stream, steps: int, n_pairs: int, flush) -> dict:
                              "sample": f"first {sample} pairs"}}
 
 
+def hull_build_section(ctx, steps: int, n_hulls: int) -> dict:
+    """ConvexPolyhedron::from_convex_hull for many clouds (16-64 points on ellipsoids, the hull
+    workload of the manifold and contact sections) on the GPU, inputs resident on the device; the
+    call is synchronous (it reads the output sizes back), so it is timed on the host clock. The
+    host builder (the same algorithm on all host threads) is the CPU baseline on a sample, and the
+    GPU output of that sample must equal the host's byte for byte."""
+    import ctypes as C
+    import numpy as np
+    import torch
+    from parry_gb300 import workloads as W
+    from parry_gb300._capi import lib, check
+    from parry_gb300.polyhedra import build_polyhedra
+
+    cloud, first, count = W.ellipsoid_hulls(n_hulls, 66, 7, 16, 64)
+    d_cloud, d_first, d_count = (torch.from_numpy(cloud).cuda(), torch.from_numpy(first.view(np.int32)).cuda(),
+                                 torch.from_numpy(count.view(np.int32)).cuda())
+    L = lib()
+
+    def run():
+        h = C.c_void_p()
+        check(L.parrygpu_polyhedra_build_gpu(ctx.handle, C.c_void_p(d_cloud.data_ptr()), len(cloud), C.c_void_p(d_first.data_ptr()),
+                                             C.c_void_p(d_count.data_ptr()), n_hulls, C.byref(h)), ctx.handle)
+        sizes = np.zeros(5, np.uint64)
+        check(L.parrygpu_polyhedra_gpu_sizes(h, C.c_void_p(sizes.ctypes.data)))
+        L.parrygpu_polyhedra_gpu_destroy(h)
+        return sizes
+
+    sizes = run()
+    torch.cuda.synchronize()
+    times = []
+    for _ in range(max(3, min(steps, 10))):
+        t0 = time.perf_counter()
+        run()
+        times.append(time.perf_counter() - t0)
+    ms = 1e3 * statistics.median(times)
+    # end to end: host clouds in, host arrays out
+    t0 = time.perf_counter()
+    build_polyhedra(cloud, first, count, ctx=ctx)
+    e2e_ms = 1e3 * (time.perf_counter() - t0)
+    sample = min(n_hulls, 65536)
+    sc = cloud[: int(first[sample - 1] + count[sample - 1])]
+    threads = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    host = build_polyhedra(sc, first[:sample], count[:sample], threads=threads)
+    cpu_s = time.perf_counter() - t0
+    dev = build_polyhedra(sc, first[:sample], count[:sample], ctx=ctx)
+    same = bool(all(np.array_equal(a.view(np.uint32), b.view(np.uint32)) for a, b in [(host[0], dev[0]), (host[1], dev[1])]) and
+                all(np.array_equal(host[2][k].view(np.uint32), dev[2][k].view(np.uint32)) for k in host[2]))
+    return {"workload": f"{n_hulls} clouds of 16-64 points on ellipsoids (log-uniform counts)", "metric": "hulls/s",
+            "value": round(n_hulls / (ms / 1e3), 1), "unit": "hulls/s", "ms_per_step": round(ms, 3),
+            "faces": int(sizes[1]), "edges": int(sizes[4]),
+            "e2e": {"value": round(n_hulls / (e2e_ms / 1e3), 1), "unit": "hulls/s", "ms": round(e2e_ms, 2),
+                    "h2d_bytes": int(cloud.nbytes + first.nbytes + count.nbytes)},
+            "matches_host_builder_on_sample": same,
+            "cpu_baseline": {"value": round(sample / cpu_s, 1), "unit": "hulls/s", "cores": threads, "kind": "port",
+                             "sample": f"first {sample} clouds; the same hull + from_convex_mesh code on host threads"}}
+
+
 def shape_cast_section(ctx, stream, steps: int, n_pairs: int, flush) -> dict:
     """query::cast_shapes on separated ball / cuboid / capsule / hull pairs closing at 0.5-2 units per
     unit time (W.shape_cast_pairs, max_toi 100): device-resident pairs/s, oracle check and CPU
@@ -976,6 +1034,9 @@ def run_gb300(args) -> int:
         trimesh_contacts = trimesh_contacts_section(ctx, stream, args.steps, args.warmup, args.terrain_shapes, flush)
         trimesh_contacts["fix_internal_edges"] = trimesh_contacts_section(ctx, stream, args.steps, args.warmup, args.terrain_shapes,
                                                                           flush, fix=True, sample=1024)
+    hull_build = None
+    if args.hull_clouds > 0:
+        hull_build = hull_build_section(ctx, args.steps, args.hull_clouds)
     shape_cast = None
     if args.cast_pairs > 0:
         shape_cast = shape_cast_section(ctx, stream, args.steps, args.cast_pairs, flush)
@@ -1025,6 +1086,7 @@ def run_gb300(args) -> int:
             "broadphase": broadphase,
             "shape_cast": shape_cast,
             "trimesh_contacts": trimesh_contacts,
+            "hull_build": hull_build,
         }
         print(json.dumps(line), flush=True)
     ctx.close()
@@ -1041,6 +1103,7 @@ def main() -> int:
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--n-rays", type=int, default=N_RAYS)
     ap.add_argument("--cast-pairs", type=int, default=1 << 20, help="pairs of the shape-casting section (0 skips it)")
+    ap.add_argument("--hull-clouds", type=int, default=1 << 20, help="clouds of the GPU hull-construction section (0 skips it)")
     ap.add_argument("--terrain-shapes", type=int, default=65536, help="shapes of the TriMesh contact-manifold section (0 skips it)")
     ap.add_argument("--broadphase-shapes", type=int, default=131072,
                     help="balls and cuboids of the broadphase + contact section (0 skips it)")

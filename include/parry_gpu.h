@@ -268,6 +268,21 @@ parrygpu_status parrygpu_polyhedra_copy(const parrygpu_polyhedra_builder* b, flo
                                         uint32_t* vertex_faces, uint32_t* vertex_edges, float* edge_dirs);
 void parrygpu_polyhedra_builder_destroy(parrygpu_polyhedra_builder* b);
 
+/* The same build on the GPU (one thread per cloud; the host builder's algorithm, the same bytes):
+ * points = n_points x 3, first / count = n_hulls (host or device; clouds of at most 65535 points).
+ * The result stays in device arrays owned by the handle: parrygpu_polyhedra_gpu_view gives a
+ * parrygpu_polyhedra of device pointers (and the hull points) to pass straight to the shape set,
+ * parrygpu_polyhedra_gpu_sizes / _copy read it out in the host builder's layout. */
+typedef struct parrygpu_polyhedra_gpu parrygpu_polyhedra_gpu;
+parrygpu_status parrygpu_polyhedra_build_gpu(parrygpu_ctx* ctx, const float* points, uint64_t n_points, const uint32_t* first,
+                                             const uint32_t* count, uint64_t n_hulls, parrygpu_polyhedra_gpu** out);
+parrygpu_status parrygpu_polyhedra_gpu_sizes(const parrygpu_polyhedra_gpu* g, uint64_t* sizes);
+parrygpu_status parrygpu_polyhedra_gpu_copy(parrygpu_ctx* ctx, const parrygpu_polyhedra_gpu* g, float* points, uint32_t* hulls,
+                                            float* face_normals, uint32_t* face_ranges, uint32_t* face_vertices, uint32_t* face_edges,
+                                            uint32_t* vertex_ranges, uint32_t* vertex_faces, uint32_t* vertex_edges, float* edge_dirs);
+parrygpu_status parrygpu_polyhedra_gpu_view(const parrygpu_polyhedra_gpu* g, const float** points, parrygpu_polyhedra* view);
+void parrygpu_polyhedra_gpu_destroy(parrygpu_polyhedra_gpu* g);
+
 /* Same layout as the reference's Contact (src/query/contact/contact.rs:71-105), world space. */
 typedef struct parrygpu_contact {
   float point1[3];

@@ -57,6 +57,11 @@ SIGNATURES: dict[str, tuple] = {
     "parrygpu_bvh_remove": (I32, [P, P, P, U32]),
     "parrygpu_trimesh_create": (I32, [P, P, U32, P, U32, C.POINTER(P)]),
     "parrygpu_trimesh_destroy": (None, [P]),
+    "parrygpu_polyhedra_build_gpu": (I32, [P, P, U64, P, P, U64, C.POINTER(P)]),
+    "parrygpu_polyhedra_gpu_sizes": (I32, [P, P]),
+    "parrygpu_polyhedra_gpu_copy": (I32, [P, P, P, P, P, P, P, P, P, P, P, P]),
+    "parrygpu_polyhedra_gpu_view": (I32, [P, P, P]),
+    "parrygpu_polyhedra_gpu_destroy": (None, [P]),
     "parrygpu_trimesh_set_flags": (I32, [P, P, U32]),
     "parrygpu_trimesh_normal_constraints": (I32, [P, P, P, P]),
     "parrygpu_project_local_normals": (I32, [P, P, P, U64, P, P]),

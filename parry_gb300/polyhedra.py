@@ -1,8 +1,9 @@
 """ConvexPolyhedron topology (the host-side input of the hull contact-manifold generators).
 
 build_polyhedra(pool, first, count) runs ConvexPolyhedron::from_convex_hull for many point clouds
-at once through libparrygpu's host builder (parrygpu_polyhedra_build) and returns the hull points
-and the topology arrays in the parrygpu_polyhedra layout (include/parry_gpu.h).
+at once through libparrygpu's builder - on the GPU (parrygpu_polyhedra_build_gpu) when given a
+Context, else on host threads (parrygpu_polyhedra_build) - and returns the hull points and the
+topology arrays in the parrygpu_polyhedra layout (include/parry_gpu.h).
 """
 from __future__ import annotations
 
@@ -14,15 +15,19 @@ TOPOLOGY_KEYS = ("face_normals", "face_ranges", "face_vertices", "face_edges", "
                  "edge_dirs")
 
 
-def build_polyhedra(pool: np.ndarray, first: np.ndarray, count: np.ndarray, threads: int = 0):
+def build_polyhedra(pool: np.ndarray, first: np.ndarray, count: np.ndarray, threads: int = 0, ctx=None):
     """Returns (points (m, 3) f32, hulls (n, 8) u32, topology dict). hulls rows: first vertex (in
-    `points`), vertex count, first face, face count, first edge, edge count, ok, 0."""
+    `points`), vertex count, first face, face count, first edge, edge count, ok, 0. With a Context
+    `ctx` the clouds are built on its GPU (parrygpu_polyhedra_build_gpu: the same bytes as the host
+    builder), else on `threads` host threads."""
     from ._capi import lib, check
     pool = np.ascontiguousarray(pool, np.float32).reshape(-1, 3)
     first = np.ascontiguousarray(first, np.uint32)
     count = np.ascontiguousarray(count, np.uint32)
     n = len(first)
     L = lib()
+    if ctx is not None:
+        return _build_gpu(ctx, pool, first, count)
     h = C.c_void_p()
     check(L.parrygpu_polyhedra_build(pool.ctypes.data, first.ctypes.data, count.ctypes.data, n, int(threads), C.byref(h)))
     try:
@@ -40,6 +45,33 @@ def build_polyhedra(pool: np.ndarray, first: np.ndarray, count: np.ndarray, thre
         check(L.parrygpu_polyhedra_copy(h, points.ctypes.data, hulls.ctypes.data, *[topo[k].ctypes.data for k in TOPOLOGY_KEYS]))
     finally:
         L.parrygpu_polyhedra_builder_destroy(h)
+    return points, hulls, topo
+
+
+def _build_gpu(ctx, pool, first, count):
+    from ._capi import lib, check
+    L = lib()
+    n = len(first)
+    h = C.c_void_p()
+    check(L.parrygpu_polyhedra_build_gpu(ctx.handle, C.c_void_p(pool.ctypes.data) if len(pool) else None, len(pool),
+                                         C.c_void_p(first.ctypes.data) if n else None, C.c_void_p(count.ctypes.data) if n else None,
+                                         n, C.byref(h)), ctx.handle)
+    try:
+        sizes = np.zeros(5, np.uint64)
+        check(L.parrygpu_polyhedra_gpu_sizes(h, C.c_void_p(sizes.ctypes.data)))
+        npts, nf, nfe, nve, ne = (int(x) for x in sizes)
+        points = np.zeros((npts, 3), np.float32)
+        hulls = np.zeros((n, 8), np.uint32)
+        topo = {
+            "face_normals": np.zeros((nf, 3), np.float32), "face_ranges": np.zeros((nf, 2), np.uint32),
+            "face_vertices": np.zeros(nfe, np.uint32), "face_edges": np.zeros(nfe, np.uint32),
+            "vertex_ranges": np.zeros((npts, 2), np.uint32), "vertex_faces": np.zeros(nve, np.uint32),
+            "vertex_edges": np.zeros(nve, np.uint32), "edge_dirs": np.zeros((ne, 3), np.float32),
+        }
+        ptr = lambda a: C.c_void_p(a.ctypes.data) if a.size else None
+        check(L.parrygpu_polyhedra_gpu_copy(ctx.handle, h, ptr(points), ptr(hulls), *[ptr(topo[k]) for k in TOPOLOGY_KEYS]), ctx.handle)
+    finally:
+        L.parrygpu_polyhedra_gpu_destroy(h)
     return points, hulls, topo
 
 
