@@ -4,13 +4,15 @@
 //
 //   1. clouds ordered by point count (one radix pass over a 16-bit key) so a warp walks clouds of
 //      similar size;
-//   2. sizes pass: every cloud is built and only its output sizes kept;
+//   2. build pass: every cloud is built once into a staging slot sized from its point count, its
+//      output sizes kept;
 //   3. one exclusive scan per output array gives every cloud its offsets;
-//   4. emit pass: every cloud is built again and written at its offsets, in the parrygpu_polyhedra
+//   4. copy pass (a warp per cloud): staged outputs to their offsets, in the parrygpu_polyhedra
 //      layout, into device arrays the handle owns (usable directly as parrygpu_polyhedra).
-// Building twice costs less than staging every cloud's topology: the workspaces are per thread,
-// interleaved across threads (element i of thread t at i * threads + t), and reused by each cloud
-// a thread takes.
+// When the staging slots would exceed a fixed budget (clouds of hundreds of points by the
+// million), steps 2 and 4 become a sizes pass and an emit pass that builds every cloud again.
+// The hull workspaces are per thread, interleaved across threads (element i of thread t at
+// i * threads + t), and reused by each cloud a thread takes.
 #include "internal.hpp"
 #include "hull_core.hpp"
 
@@ -22,7 +24,8 @@ using namespace hullcore;
 namespace {
 
 constexpr int HB_THREADS = 128;
-constexpr size_t HB_WS_BUDGET = size_t(6) << 30;  // bytes of per-thread workspaces at once
+constexpr size_t HB_WS_BUDGET = size_t(6) << 30;     // bytes of per-thread workspaces at once
+constexpr size_t HB_STAGE_BUDGET = size_t(12) << 30;  // staging above this: build twice instead
 
 // Thread t's spans over the interleaved workspace (arrays laid out one after another, each holding
 // capacity x threads elements).
@@ -128,6 +131,100 @@ __global__ void __launch_bounds__(HB_THREADS) k_hb_emit(WsLayout lay, uint64_t n
   }
 }
 
+// ---- one build per cloud, results staged ----
+// A cloud of n points fits its outputs in a staging slot laid out from HullCaps::of(n): points
+// (3n f32), vertex ranges (2n), face normals (3 per triangle bound), face ranges (2 per triangle
+// bound), face vertices, face edges, vertex faces, vertex edges (an entry bound each), edge
+// directions (3 per edge bound). Slots are whole 256-byte blocks.
+struct StageLayout {
+  uint32_t n, tris, entries, edges;
+  __host__ __device__ static StageLayout of(uint32_t count) {
+    const HullCaps c = HullCaps::of(count < 4 ? 4 : count);
+    return StageLayout{count, c.tris, c.entries, c.edges};
+  }
+  __host__ __device__ size_t words() const { return 3ull * n + 2ull * n + 5ull * tris + 4ull * entries + 3ull * edges; }
+  __host__ __device__ uint32_t blocks() const { return (uint32_t)((words() * 4 + 255) / 256); }
+  __device__ PolyOut view(uint32_t* base) const {
+    uint32_t* p = base;
+    PolyOut o;
+    o.points = reinterpret_cast<float*>(p); p += 3 * (size_t)n;
+    o.vertex_ranges = p; p += 2 * (size_t)n;
+    o.face_normals = reinterpret_cast<float*>(p); p += 3 * (size_t)tris;
+    o.face_ranges = p; p += 2 * (size_t)tris;
+    o.face_vertices = p; p += entries;
+    o.face_edges = p; p += entries;
+    o.vertex_faces = p; p += entries;
+    o.vertex_edges = p; p += entries;
+    o.edge_dirs = reinterpret_cast<float*>(p);
+    o.hulls = nullptr;
+    return o;
+  }
+};
+
+__global__ void k_hb_stage_blocks(uint64_t n_hulls, const uint32_t* __restrict__ count, uint32_t* __restrict__ blocks) {
+  const uint64_t h = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+  if (h >= n_hulls) return;
+  blocks[h] = StageLayout::of(count[h]).blocks();
+}
+
+// Build pass: every cloud built once, its output written to its staging slot (hull-relative
+// offsets, as the host builder keeps them) and its sizes recorded (SoA, 5 arrays of `stride`).
+__global__ void __launch_bounds__(HB_THREADS) k_hb_build(WsLayout lay, uint64_t n_hulls, const uint32_t* __restrict__ order,
+                                                         const float* __restrict__ pts, uint64_t n_points, const uint32_t* __restrict__ first,
+                                                         const uint32_t* __restrict__ count, const uint32_t* __restrict__ stage_off,
+                                                         uint32_t* __restrict__ stage, uint32_t* __restrict__ sizes, size_t stride,
+                                                         uint32_t* __restrict__ err) {
+  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= lay.threads) return;
+  HullWs ws = lay.at(t);
+  for (uint64_t k = t; k < n_hulls; k += lay.threads) {
+    const uint32_t h = order[k];
+    const uint32_t n = count[h];
+    HullOut r;
+    if (n <= lay.caps.n && (uint64_t)first[h] + n <= n_points) {
+      r = build_one(pts + 3 * (size_t)first[h], n, lay.caps, ws);
+      const PolyOut o = StageLayout::of(n).view(stage + (size_t)stage_off[h] * 64);
+      emit(ws, r, 0, 0, 0, 0, 0, 0, o);
+    } else {
+      atomicOr(err, ERR_BAD_INDEX);
+    }
+    sizes[0 * stride + h] = r.npts;
+    sizes[1 * stride + h] = r.ok ? r.nfaces : 0u;
+    sizes[2 * stride + h] = r.ok ? r.nfentries : 0u;
+    sizes[3 * stride + h] = r.ok ? r.nventries : 0u;
+    sizes[4 * stride + h] = r.ok ? r.nedges : 0u;
+  }
+}
+
+// One warp per cloud: its staged output to the final arrays at the scanned offsets (ranges
+// shifted by the cloud's entry offsets), and its hull record.
+__global__ void k_hb_copy(uint64_t n_hulls, const uint32_t* __restrict__ count, const uint32_t* __restrict__ stage_off,
+                          const uint32_t* __restrict__ stage, const uint32_t* __restrict__ sizes, const uint32_t* __restrict__ offsets,
+                          size_t stride, PolyOut o) {
+  const uint64_t h = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
+  const uint32_t lane = threadIdx.x & 31;
+  if (h >= n_hulls) return;
+  const StageLayout L = StageLayout::of(count[h]);
+  const PolyOut sv = L.view(const_cast<uint32_t*>(stage) + (size_t)stage_off[h] * 64);
+  const uint32_t np = sizes[0 * stride + h], nf = sizes[1 * stride + h], nfe = sizes[2 * stride + h], nve = sizes[3 * stride + h],
+                 ne = sizes[4 * stride + h];
+  const uint64_t vp = offsets[0 * stride + h], fp = offsets[1 * stride + h], fe = offsets[2 * stride + h], ve = offsets[3 * stride + h],
+                 ep = offsets[4 * stride + h];
+  if (lane == 0) {
+    uint32_t* rec = o.hulls + 8 * h;
+    const bool ok = ne > 0;  // a hull with topology has at least the 6 edges of a tetrahedron
+    rec[0] = (uint32_t)vp; rec[1] = np; rec[2] = (uint32_t)fp; rec[3] = nf; rec[4] = (uint32_t)ep; rec[5] = ne; rec[6] = ok ? 1u : 0u;
+    rec[7] = 0;
+  }
+  for (uint32_t i = lane; i < 3 * np; i += 32) o.points[3 * vp + i] = sv.points[i];
+  for (uint32_t i = lane; i < 2 * np; i += 32) o.vertex_ranges[2 * vp + i] = sv.vertex_ranges[i] + ((i & 1u) ? 0u : (uint32_t)ve);
+  for (uint32_t i = lane; i < 3 * nf; i += 32) o.face_normals[3 * fp + i] = sv.face_normals[i];
+  for (uint32_t i = lane; i < 2 * nf; i += 32) o.face_ranges[2 * fp + i] = sv.face_ranges[i] + ((i & 1u) ? 0u : (uint32_t)fe);
+  for (uint32_t i = lane; i < nfe; i += 32) { o.face_vertices[fe + i] = sv.face_vertices[i]; o.face_edges[fe + i] = sv.face_edges[i]; }
+  for (uint32_t i = lane; i < nve; i += 32) { o.vertex_faces[ve + i] = sv.vertex_faces[i]; o.vertex_edges[ve + i] = sv.vertex_edges[i]; }
+  for (uint32_t i = lane; i < 3 * ne; i += 32) o.edge_dirs[3 * ep + i] = sv.edge_dirs[i];
+}
+
 }  // namespace
 
 // Device arrays of a built batch, in the parrygpu_polyhedra layout.
@@ -149,9 +246,9 @@ parrygpu_status parrygpu_polyhedra_build_gpu(parrygpu_ctx* ctx, const float* poi
   g->n_hulls = n_hulls;
   struct Guard {
     parrygpu_polyhedra_gpu* g;
-    DevBuf ws, sizes, keys[2], vals[2], hist, misc;
+    DevBuf ws, sizes, keys[2], vals[2], hist, misc, stage, stage_off;
     ~Guard() {
-      for (DevBuf* d : {&ws, &sizes, &keys[0], &keys[1], &vals[0], &vals[1], &hist, &misc}) d->release();
+      for (DevBuf* d : {&ws, &sizes, &keys[0], &keys[1], &vals[0], &vals[1], &hist, &misc, &stage, &stage_off}) d->release();
       if (g) parrygpu_polyhedra_gpu_destroy(g);
     }
   } gd{g};
@@ -192,21 +289,39 @@ parrygpu_status parrygpu_polyhedra_build_gpu(parrygpu_ctx* ctx, const float* poi
   const uint32_t* order = gd.vals[rb].as<uint32_t>();
   PG_CUDA(ctx, gd.ws.reserve(ws_total(caps, threads)));
   WsLayout lay{caps, threads, gd.ws.as<char>()};
-  // sizes, padded per array to a multiple of 4 words for the scan
+  // sizes (then offsets), padded per array to a multiple of 4 words for the scan
   const size_t stride = ((size_t)nh + 4) & ~size_t(3);
   PG_CUDA(ctx, gd.sizes.reserve(5 * stride * 4));
   PG_CUDA(ctx, cudaMemsetAsync(gd.sizes.ptr, 0, 5 * stride * 4, ctx->stream));
   uint32_t* sizes = gd.sizes.as<uint32_t>();
-  // k_hb_sizes indexes its 5 arrays with stride n_hulls; copy them into the padded layout after
-  {
+  // staging slots (256-byte blocks) of the single-build path
+  PG_CUDA(ctx, gd.stage_off.reserve(stride * 4));
+  PG_CUDA(ctx, cudaMemsetAsync(gd.stage_off.ptr, 0, stride * 4, ctx->stream));
+  k_hb_stage_blocks<<<div_up(nh, 256), 256, 0, ctx->stream>>>(n_hulls, (const uint32_t*)dc, gd.stage_off.as<uint32_t>());
+  PG_LAUNCHED(ctx);
+  uint32_t sb[2] = {0, 0};
+  PG_CUDA(ctx, cudaMemcpyAsync(&sb[0], gd.stage_off.as<uint32_t>() + (nh - 1), 4, cudaMemcpyDeviceToHost, ctx->stream));
+  if ((s = exclusive_scan_u32(ctx, gd.stage_off.as<uint32_t>(), nh)) != PARRYGPU_OK) return s;
+  PG_CUDA(ctx, cudaMemcpyAsync(&sb[1], gd.stage_off.as<uint32_t>() + (nh - 1), 4, cudaMemcpyDeviceToHost, ctx->stream));
+  PG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  const size_t stage_bytes = ((size_t)sb[0] + sb[1]) * 256;
+  const bool staged = stage_bytes <= HB_STAGE_BUDGET && gd.stage.reserve(stage_bytes + 256) == cudaSuccess;
+  if (!staged) cudaGetLastError();  // a refused staging allocation only selects the two-pass path
+  if (staged) {
+    k_hb_build<<<div_up(threads, HB_THREADS), HB_THREADS, 0, ctx->stream>>>(lay, n_hulls, order, (const float*)dp, n_points,
+                                                                            (const uint32_t*)df, (const uint32_t*)dc, gd.stage_off.as<uint32_t>(),
+                                                                            gd.stage.as<uint32_t>(), sizes, stride, ctx->d_err);
+    PG_LAUNCHED(ctx);
+    PG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  } else {
+    // k_hb_sizes indexes its 5 arrays with stride n_hulls; copy them into the padded layout after
     DevBuf raw;
     PG_CUDA(ctx, raw.reserve(5 * (size_t)nh * 4));
     k_hb_sizes<<<div_up(threads, HB_THREADS), HB_THREADS, 0, ctx->stream>>>(lay, n_hulls, order, (const float*)dp, n_points,
                                                                             (const uint32_t*)df, (const uint32_t*)dc, raw.as<uint32_t>(),
                                                                             ctx->d_err);
-    cudaError_t le = cudaGetLastError();
+    cudaError_t ce = cudaGetLastError();
     ctx->launches++;
-    cudaError_t ce = le;
     for (int a = 0; a < 5 && ce == cudaSuccess; ++a)
       ce = cudaMemcpyAsync(sizes + a * stride, raw.as<uint32_t>() + (size_t)a * nh, (size_t)nh * 4, cudaMemcpyDeviceToDevice, ctx->stream);
     if (ce == cudaSuccess) ce = cudaStreamSynchronize(ctx->stream);
@@ -217,8 +332,14 @@ parrygpu_status parrygpu_polyhedra_build_gpu(parrygpu_ctx* ctx, const float* poi
   // totals, then offsets
   uint32_t last[5];
   for (int a = 0; a < 5; ++a) PG_CUDA(ctx, cudaMemcpyAsync(&last[a], sizes + a * stride + (nh - 1), 4, cudaMemcpyDeviceToHost, ctx->stream));
+  // the exclusive scans need the sizes of the single-build path twice: keep a copy
+  DevBuf counts_copy;
+  if (staged) {
+    PG_CUDA(ctx, counts_copy.reserve(5 * stride * 4));
+    PG_CUDA(ctx, cudaMemcpyAsync(counts_copy.ptr, sizes, 5 * stride * 4, cudaMemcpyDeviceToDevice, ctx->stream));
+  }
   for (int a = 0; a < 5; ++a)
-    if ((s = exclusive_scan_u32(ctx, sizes + a * stride, nh)) != PARRYGPU_OK) return s;
+    if ((s = exclusive_scan_u32(ctx, sizes + a * stride, nh)) != PARRYGPU_OK) { counts_copy.release(); return s; }
   uint32_t excl[5];
   for (int a = 0; a < 5; ++a) PG_CUDA(ctx, cudaMemcpyAsync(&excl[a], sizes + a * stride + (nh - 1), 4, cudaMemcpyDeviceToHost, ctx->stream));
   PG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
@@ -236,9 +357,20 @@ parrygpu_status parrygpu_polyhedra_build_gpu(parrygpu_ctx* ctx, const float* poi
   PolyOut o{g->points.as<float>(), g->hulls.as<uint32_t>(), g->face_normals.as<float>(), g->face_ranges.as<uint32_t>(),
             g->face_vertices.as<uint32_t>(), g->face_edges.as<uint32_t>(), g->vertex_ranges.as<uint32_t>(),
             g->vertex_faces.as<uint32_t>(), g->vertex_edges.as<uint32_t>(), g->edge_dirs.as<float>()};
-  k_hb_emit<<<div_up(threads, HB_THREADS), HB_THREADS, 0, ctx->stream>>>(lay, n_hulls, order, (const float*)dp, n_points,
-                                                                         (const uint32_t*)df, (const uint32_t*)dc, sizes, stride, o);
-  PG_LAUNCHED(ctx);
+  if (staged) {
+    k_hb_copy<<<(unsigned)div_up((uint64_t)nh * 32, 256), 256, 0, ctx->stream>>>(n_hulls, (const uint32_t*)dc, gd.stage_off.as<uint32_t>(),
+                                                                                 gd.stage.as<uint32_t>(), counts_copy.as<uint32_t>(), sizes,
+                                                                                 stride, o);
+    cudaError_t ce = cudaGetLastError();
+    ctx->launches++;
+    if (ce == cudaSuccess) ce = cudaStreamSynchronize(ctx->stream);
+    counts_copy.release();
+    if (ce != cudaSuccess) return check_cuda(ctx, ce, "hull copy");
+  } else {
+    k_hb_emit<<<div_up(threads, HB_THREADS), HB_THREADS, 0, ctx->stream>>>(lay, n_hulls, order, (const float*)dp, n_points,
+                                                                           (const uint32_t*)df, (const uint32_t*)dc, sizes, stride, o);
+    PG_LAUNCHED(ctx);
+  }
   PG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   if ((s = parrygpu_sync(ctx)) != PARRYGPU_OK) return s;
   *out = g;
