@@ -123,3 +123,17 @@ def test_insert_update_remove(gpu_ctx):
     b.insert(a[:3], np.array([10, 20, 30], np.uint32))
     assert b.leaf_count() == 3
     b.close()
+
+
+def test_edit_imported_tree(gpu_ctx, oracle_lib):
+    """A tree imported from parry's binned layout takes inserts and removals like a built one."""
+    a = random_aabbs(500, seed=21, extent=15.0)
+    nodes = np.ascontiguousarray(oracle_lib.Bvh(a).nodes()).view(np.float32).reshape(-1, 16)
+    b = pg.Bvh.from_serialized(gpu_ctx, nodes)
+    extra = random_aabbs(50, seed=22, extent=15.0)
+    b.insert(extra, np.arange(1000, 1050, dtype=np.uint32))
+    b.remove(np.arange(0, 500, 5, dtype=np.uint32))
+    ids = np.array(sorted(set(range(500)) - set(range(0, 500, 5))) + list(range(1000, 1050)), np.uint32)
+    boxes = np.concatenate([a[ids[ids < 500]], extra])
+    np.testing.assert_array_equal(b.traverse_bvtt_single_tree(), _pairs_by_id(ids, boxes))
+    b.close()

@@ -29,7 +29,8 @@ def _scene(n_pairs, seed, nx=48, nz=24):
 
 
 @pytest.mark.parametrize("fix", [False, True])
-@pytest.mark.parametrize("mesh_pose", [None, [0.0, 0.0, 0.0, 1.0, 0.25, -0.5, 0.125]])
+@pytest.mark.parametrize("mesh_pose", [None, [0.0, 0.0, 0.0, 1.0, 0.25, -0.5, 0.125],
+                                       [0.0, 0.2588190451, 0.0, 0.9659258263, 3.0, -0.25, -2.0]])
 def test_trimesh_contacts_frames_bit_exact(gpu_ctx, oracle_lib, mesh_pose, fix):
     """With and without TriMeshFlags::FIX_INTERNAL_EDGES (normal constraints from pseudo-normals)."""
     O = oracle_lib
@@ -67,5 +68,23 @@ def test_trimesh_contacts_frames_bit_exact(gpu_ctx, oracle_lib, mesh_pose, fix):
             moved += sum(not np.array_equal(a, b) for a, b in zip(first, ref.inter))
     assert moved > 0
     assert (got["n_points"] > 0).sum() > 200
+    tc.close()
+    mesh.close()
+
+
+def test_capacity_exceeded_is_reported(gpu_ctx):
+    """More interfering triangles than the per-shape capacity raise CAPACITY_EXCEEDED (the list is
+    truncated, never overrun); the context stays usable."""
+    v, i, (t, prm, pos, pool, poly), vel = _scene(40, 5)
+    n = len(t)
+    mesh = pg.TriMesh(gpu_ctx, v, i)
+    tc = pg.TriMeshContacts(gpu_ctx, mesh, n, 1)
+    with pytest.raises(pg.ParryGpuError):
+        tc.update(ShapeSet.from_arrays(t, prm, pos, pool, poly), 0.02)
+    tc.close()
+    tc = pg.TriMeshContacts(gpu_ctx, mesh, n, 256)
+    tc.update(ShapeSet.from_arrays(t, prm, pos, pool, poly), 0.02)
+    counts, _, _ = tc.read()
+    assert counts.max() > 1
     tc.close()
     mesh.close()
