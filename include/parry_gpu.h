@@ -64,6 +64,13 @@ typedef struct parrygpu_config {
   uint32_t ray_chunks;     /* host-buffer ray casts without a ray ordering: chunks over two streams
                               (0 = library default: one per 262,144 rays, 2 to 4; 1 = no chunking; at
                               most 64) */
+  uint32_t ray_host_access; /* host-buffer ray casts without a ray ordering whose host buffers are all
+                              page-locked (cudaHostAlloc / cudaHostRegister): 1 = the kernel reads the
+                              rays and writes the results in place over the host link (on
+                              Grace-Blackwell the coherent NVLink-C2C); 2 = staged through device
+                              copies, as ray_chunks says; 0 = library default: in place when the
+                              device's host link is coherent (it reads host memory through the
+                              host's page tables), else staged. Other host buffers are staged. */
 } parrygpu_config;
 
 /* ---- context ---------------------------------------------------------------------------- */

@@ -28,6 +28,20 @@ bool is_device_ptr(const void* p) {
   return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
 }
 
+bool is_addressable(const void* p) {
+  if (!p) return false;
+  cudaPointerAttributes a;
+  cudaError_t e = cudaPointerGetAttributes(&a, p);
+  if (e != cudaSuccess) { cudaGetLastError(); return false; }
+  return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged || (a.type == cudaMemoryTypeHost && a.devicePointer);
+}
+
+void* device_view_ptr(const void* p) {
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) { cudaGetLastError(); return const_cast<void*>(p); }
+  return a.devicePointer ? a.devicePointer : const_cast<void*>(p);
+}
+
 parrygpu_status stage_input(parrygpu_ctx* ctx, DevBuf& buf, const void* src, size_t bytes, const void** dptr) {
   if (bytes == 0) { *dptr = src; return PARRYGPU_OK; }
   if (!src) return set_error(ctx, PARRYGPU_INVALID_ARG, "null input pointer");
@@ -70,7 +84,7 @@ parrygpu_status parrygpu_create(parrygpu_ctx** out, const parrygpu_config* cfg) 
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) { cudaGetLastError(); return PARRYGPU_NO_DEVICE; }
   if (cfg && ((cfg->ray_block % 32) != 0 || cfg->ray_block > 1024 || cfg->ray_sort_key > 2 || cfg->epa_blocks_per_sm > 32 ||
-              cfg->ray_traversal > 3 || cfg->ray_refill > 32 || cfg->ray_chunks > 64))
+              cfg->ray_traversal > 3 || cfg->ray_refill > 32 || cfg->ray_chunks > 64 || cfg->ray_host_access > 2))
     return PARRYGPU_INVALID_ARG;
   parrygpu_ctx* ctx = new parrygpu_ctx();
   if (cfg) ctx->cfg = *cfg; else parrygpu_default_config(&ctx->cfg);
@@ -82,6 +96,11 @@ parrygpu_status parrygpu_create(parrygpu_ctx** out, const parrygpu_config* cfg) 
   if (e == cudaSuccess) e = cudaMemset(ctx->d_err, 0, sizeof(uint32_t));
   if (e == cudaSuccess) e = cudaMallocHost(&ctx->h_err, sizeof(uint32_t));
   if (e == cudaSuccess) e = cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, ctx->device);
+  if (e == cudaSuccess) {
+    int coherent = 0;
+    e = cudaDeviceGetAttribute(&coherent, cudaDevAttrPageableMemoryAccessUsesHostPageTables, ctx->device);
+    ctx->coherent_host = coherent != 0;
+  }
   if (e != cudaSuccess) { delete ctx; return PARRYGPU_CUDA_ERROR; }
   ctx->stream = ctx->own_stream;
   *out = ctx;

@@ -65,6 +65,7 @@ struct parrygpu_ctx {
   RayWaveScratch ray_wave;
   MfScratch mf;
   int sm_count = 0;
+  bool coherent_host = false;  // the device reads pageable host memory through the host's page tables (Grace NVLink-C2C)
   // Second stream for pipelined host-buffer calls (chunks alternate between it and `stream`),
   // with the fork / join events that order it after and before the context stream's work.
   cudaStream_t aux_stream = nullptr;
@@ -140,6 +141,12 @@ parrygpu_status check_cuda(parrygpu_ctx* ctx, cudaError_t e, const char* what);
 
 // ---- host/device pointer staging ----
 bool is_device_ptr(const void* p);
+// Device memory, or page-locked host memory with a device mapping (readable by kernels in place).
+bool is_addressable(const void* p);
+// The device-side address of an addressable pointer (the same value under unified addressing).
+void* device_view_ptr(const void* p);
+template <class T> inline T* device_view(T* p) { return static_cast<T*>(device_view_ptr(p)); }
+template <class T> inline const T* device_view(const T* p) { return static_cast<const T*>(device_view_ptr(p)); }
 // Returns a device pointer holding `bytes` of `src` (src itself when already on the device).
 parrygpu_status stage_input(parrygpu_ctx* ctx, DevBuf& buf, const void* src, size_t bytes, const void** dptr);
 // Returns a device pointer for an output of `bytes`; *needs_copy tells whether `dst` is host memory.

@@ -557,6 +557,21 @@ parrygpu_status parrygpu_trimesh_cast_rays(parrygpu_ctx* ctx, const parrygpu_tri
   {
     const bool host_in = !is_device_ptr(rays), h_feat = !is_device_ptr(feature), h_toi = !is_device_ptr(toi);
     const bool h_nrm = normal && !is_device_ptr(normal);
+    const bool in_place = ctx->cfg.ray_host_access == 1 || (ctx->cfg.ray_host_access == 0 && ctx->coherent_host);
+    if ((host_in || h_feat || h_toi || h_nrm) && mesh->n_triangles > 0 && !ctx->cfg.sort_rays && in_place &&
+        is_addressable(rays) && is_addressable(feature) && is_addressable(toi) && (!normal || is_addressable(normal))) {
+      // every buffer is device memory or page-locked host memory the device addresses in place:
+      // the traversal reads the rays and writes its results over the host link, no staging copies
+      PG_CUDA(ctx, ctx->misc.reserve(128));
+      float p7[7] = {pose.qi, pose.qj, pose.qk, pose.qw, pose.t.x, pose.t.y, pose.t.z};
+      KernelTimer kt(ctx, "trimesh_rays");
+      parrygpu_status s = launch_trimesh_rays(ctx, mesh, has_pose ? p7 : nullptr, device_view(rays), nullptr, n, max_toi,
+                                              device_view(feature), device_view(toi), normal ? device_view(normal) : nullptr,
+                                              ctx->misc.as<uint32_t>() + 16);
+      kt.stop();
+      if (s != PARRYGPU_OK) return s;
+      return parrygpu_sync(ctx);
+    }
     if ((host_in || h_feat || h_toi || h_nrm) && mesh->n_triangles > 0 && !ctx->cfg.sort_rays && ctx->cfg.ray_chunks != 1 &&
         n >= 2 * PIPE_MIN_CHUNK) {
       float p7[7] = {pose.qi, pose.qj, pose.qk, pose.qw, pose.t.x, pose.t.y, pose.t.z};

@@ -173,10 +173,10 @@ def test_invalid_config_rejected(kw):
 
 @pytest.mark.parametrize("traversal,chunks", [(1, 0), (2, 0), (3, 0), (1, 1), (1, 3), (1, 64)])
 def test_pipelined_host_buffers(oracle_lib, traversal, chunks):
-    """Host-buffer calls without a ray ordering run in chunks over two streams; pageable, pinned,
-    device-in / host-out and toi-only calls all answer as the oracle."""
+    """Host-buffer calls without a ray ordering, staged (ray_host_access = 2), run in chunks over two
+    streams; pageable, pinned, device-in / host-out and toi-only calls all answer as the oracle."""
     import torch
-    ctx = pg.Context(0, sort_rays=False, ray_traversal=traversal, ray_chunks=chunks)
+    ctx = pg.Context(0, sort_rays=False, ray_traversal=traversal, ray_chunks=chunks, ray_host_access=2)
     v, i = W.terrain_mesh(128, 64, seed=9)
     rays = W.terrain_rays(600_001, 128, 64, seed=9)  # not a multiple of the chunk size
     m = pg.TriMesh(ctx, v, i)
@@ -190,4 +190,31 @@ def test_pipelined_host_buffers(oracle_lib, traversal, chunks):
     m.cast_rays(torch.from_numpy(rays).cuda(), 100.0, out=(feat, toi, None))  # device in, host out, no normals
     np.testing.assert_array_equal(feat, fo)
     np.testing.assert_array_equal(toi, t)
+    ctx.close()
+
+
+@pytest.mark.parametrize("traversal", [1, 2, 3])
+def test_in_place_host_access(oracle_lib, traversal):
+    """ray_host_access = 1: with page-locked host buffers the traversal reads the rays and writes
+    the results in place (no staging); pageable buffers still go through the staged path. Answers
+    equal the oracle's either way."""
+    import torch
+    ctx = pg.Context(0, sort_rays=False, ray_traversal=traversal, ray_host_access=1)
+    assert ctx.config["ray_host_access"] == 1
+    v, i = W.terrain_mesh(128, 64, seed=9)
+    rays = W.terrain_rays(300_001, 128, 64, seed=9)
+    m = pg.TriMesh(ctx, v, i)
+    fo, to, no = oracle_lib.TriMesh(v, i).cast_rays_and_get_normal(rays, 100.0)
+    rp = torch.from_numpy(rays).pin_memory()
+    fp = torch.empty(len(rays), dtype=torch.int32, pin_memory=True)
+    tp = torch.empty(len(rays), dtype=torch.float32, pin_memory=True)
+    npn = torch.empty((len(rays), 3), dtype=torch.float32, pin_memory=True)
+    m.cast_rays_and_get_normal(rp, 100.0, out=(fp, tp, npn))
+    _compare(fp.numpy().view(np.uint32), tp.numpy(), npn.numpy(), fo, to, no)
+    f, t, n = m.cast_rays_and_get_normal(rays, 100.0)  # pageable: staged
+    _compare(f, t, n, fo, to, no)
+    # device rays, pinned outputs
+    fp.zero_()
+    m.cast_rays_and_get_normal(rp.cuda(), 100.0, out=(fp, tp, npn))
+    _compare(fp.numpy().view(np.uint32), tp.numpy(), npn.numpy(), fo, to, no)
     ctx.close()
