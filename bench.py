@@ -42,6 +42,19 @@ def config(world: int, n_rays: int) -> dict:
             "parallelism": f"replicas{world}"}
 
 
+def reduce_max(x: float, world: int) -> float:
+    """The largest x over the job's ranks (the slowest rank's time): one all_reduce of a float64 on
+    the process group's device (CUDA for NCCL, CPU for gloo); the value itself when alone."""
+    if world <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def dist_info():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -994,10 +1007,7 @@ def run_gb300(args) -> int:
     k_ms, k_n = ctx.kernel_time("trimesh_rays")
     s_ms, s_n = ctx.kernel_time("ray_sort")
     ctx.enable_kernel_timing(False)
-    if world > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = reduce_max(ms, world)
     value = world * n / (ms / 1e3) / 1e6
 
     # e2e: the same public call with pinned host buffers (H2D rays, D2H results inside the region)
@@ -1015,10 +1025,7 @@ def run_gb300(args) -> int:
         mesh.cast_rays_and_get_normal(rays_p, MAX_TOI, out=(feat_p, toi_p, nrm_p))
         e2e_ms.append((time.perf_counter() - t0) * 1e3)
     e2e = statistics.mean(e2e_ms)
-    if world > 1:
-        t = torch.tensor([e2e], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e = float(t.item())
+    e2e = reduce_max(e2e, world)
     e2e_value = world * n / (e2e / 1e3) / 1e6
     same = bool(np.array_equal(feat_p.numpy(), feat.cpu().numpy()))
     # the same call staged through device copies (ray_host_access = 2; the default above reads the
@@ -1039,10 +1046,7 @@ def run_gb300(args) -> int:
         mesh_ip.cast_rays_and_get_normal(rays_p, MAX_TOI, out=(feat_p, toi_p, nrm_p))
         ip_ms.append((time.perf_counter() - t0) * 1e3)
     ip = statistics.mean(ip_ms)
-    if world > 1:
-        t = torch.tensor([ip], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ip = float(t.item())
+    ip = reduce_max(ip, world)
     same_ip = bool(np.array_equal(feat_p.numpy(), feat.cpu().numpy()) and np.array_equal(toi_p.numpy(), toi.cpu().numpy()))
     e2e_staged = {"value": round(world * n / (ip / 1e3) / 1e6, 3), "unit": "Mrays/s", "ms_per_step": round(ip, 4),
                   "h2d_bytes_per_step": int(rays_p.numel() * 4), "d2h_bytes_per_step": int(n * 20), "matches_device_run": same_ip,
