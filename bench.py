@@ -749,6 +749,7 @@ def scene_section(ctx, stream, frames: int, warmup: int, flush, n_shapes: int = 
     import torch
     import parry_gb300 as pg
     from parry_gb300 import workloads as W
+    from parry_gb300 import manifold as M
     from oracle import build as ob
     ob.build()
     from oracle import oracle as O
@@ -800,14 +801,33 @@ def scene_section(ctx, stream, frames: int, warmup: int, flush, n_shapes: int = 
     threads = os.cpu_count() or 1
     sample = min(262144, len(rays))
     t0 = time.perf_counter()
-    O.scene_frames(shapes, vel, pred, dt, 1, threads=threads)
+    want = O.scene_frames(shapes, vel, pred, dt, 1, threads=threads)
     t_frame = time.perf_counter() - t0
     moved = shapes.with_poses(O.integrate(pos, vel, dt))
     comp = O.Compound(moved)
     t0 = time.perf_counter()
-    comp.cast_rays_and_get_normal(rays[:sample], max_toi, solid=True, threads=threads)
+    w_part, w_toi, w_nrm = comp.cast_rays_and_get_normal(rays[:sample], max_toi, solid=True, threads=threads)
     t_rays = (time.perf_counter() - t0) * (len(rays) / sample)
     cpu_frame_ms = (t_frame + t_rays) * 1e3
+    # parity of a fresh first frame with the oracle frame timed above: poses, the whole pair set, every
+    # manifold record, and the rays of the timed sample
+    sc = pg.Scene(ctx, shapes, vel, pred, max(1 << 16, 4 * n_shapes))
+    sc.set_rays(torch.from_numpy(rays).cuda(), max_toi)
+    sc.step(dt, 1, use_graph=False)
+    got = sc.read()
+    sc.close()
+    order = np.lexsort((got["pairs"][:, 1], got["pairs"][:, 0]))
+    gw = M.as_words(got["manifolds"])[order]
+    ww = want["manifolds"]
+    live = np.arange(M.MAX_POINTS)[None, :] < ww[:, 0].astype(np.int64)[:, None] if len(ww) else None
+    same = {
+        "poses": bool(np.array_equal(got["poses"], want["poses"])),
+        "pairs": bool(np.array_equal(got["pairs"][order], want["pairs"])),
+        "manifolds": bool(len(gw) == len(ww) and np.array_equal(gw[:, :8], ww[:, :8]) and np.array_equal(
+            gw[:, 8:].reshape(len(gw), M.MAX_POINTS, 10)[live], ww[:, 8:].reshape(len(ww), M.MAX_POINTS, 10)[live])),
+        "rays": bool(np.array_equal(got["ray_part"][:sample], w_part) and np.array_equal(got["ray_toi"][:sample], w_toi)
+                     and np.array_equal(got["ray_normal"][:sample], w_nrm)),
+    }
     return {
         "workload": f"{n_shapes:,} shapes (ball/cuboid/capsule/hull 16-64 points, 25 % each, sizes log-uniform [0.25, 4]) in "
                     f"[-{extent:.0f}, {extent:.0f})^3, v U[-5, 5]^3, w U[-1, 1]^3, dt 1/60, prediction 0.1, {n_rays:,} rays "
@@ -822,6 +842,9 @@ def scene_section(ctx, stream, frames: int, warmup: int, flush, n_shapes: int = 
         "cpu_baseline": {"value": round(1e3 / cpu_frame_ms, 3), "unit": "frames/s", "cores": threads, "kind": "port",
                          "sample": f"one oracle frame on all shapes (binned BVH rebuilt) plus rays timed on {sample} and scaled "
                                    f"to {len(rays)}; C++ restatement of parry3d f32"},
+        "matches_oracle": all(same.values()),
+        "matches_oracle_detail": same | {"checked": f"first frame: all {len(ww)} pairs and manifold records, the first "
+                                                    f"{sample} rays, bit-exact"},
     }
 
 
@@ -898,6 +921,37 @@ def learned_section(ctx, stream, dev_shapes, dev_pairs, n_eval: int, n_train: in
                     "depth_abs_diff_p99": float(np.quantile(dd, 0.99)) if dd.size else 0.0,
                     "depth_abs_diff_max": float(dd.max()) if dd.size else 0.0},
         "mlp_flops_per_pair": 2 * (48 * 128 + 3 * 128 * 128 + 128 * 3),
+    }
+
+
+def summarize(line: dict) -> dict:
+    """One short entry per section (throughput, unit, parity flag, main ratios), placed last in the
+    JSON line so that a reader of the output's tail sees every section's headline numbers."""
+    def pick(sec, *keys):
+        if not isinstance(sec, dict):
+            return None
+        out = {}
+        for k in keys:
+            v = sec
+            for part in k.split("."):
+                v = v.get(part) if isinstance(v, dict) else None
+            if v is not None:
+                out[k.replace(".", "_")] = v
+        return out
+
+    return {
+        "rays": {"value": line["value"], "unit": line["unit"], "e2e": line["e2e"]["value"],
+                 "roofline_frac": line["roofline"]["frac"], "cpu": line["cpu_baseline"]["value"]},
+        "contacts": pick(line.get("contacts"), "value", "unit", "kernel_ms", "matches_oracle_on_sample", "e2e.value",
+                         "cpu_baseline.value", "dram_bytes_per_pair", "mixed_shapes.value"),
+        "learned": pick(line.get("learned_warm_start"), "mean_gjk_iterations.ratio", "mean_gjk_plus_epa_iterations",
+                        "pairs_per_s.ratio", "answers.has_contact_agreement"),
+        "manifolds": pick(line.get("manifolds"), "value", "unit", "matches_oracle_on_sample"),
+        "frame_pipeline": pick(line.get("frame_pipeline"), "value", "unit", "matches_oracle", "e2e.value", "cpu_baseline.value"),
+        "broadphase": pick(line.get("broadphase"), "value", "unit", "matches_oracle"),
+        "shape_cast": pick(line.get("shape_cast"), "value", "unit", "matches_oracle_on_sample"),
+        "trimesh_contacts": pick(line.get("trimesh_contacts"), "value", "unit", "matches_oracle_on_sample"),
+        "hull_build": pick(line.get("hull_build"), "value", "unit", "matches_host_builder_on_sample"),
     }
 
 
@@ -1124,6 +1178,7 @@ def run_gb300(args) -> int:
             "trimesh_contacts": trimesh_contacts,
             "hull_build": hull_build,
         }
+        line["summary"] = summarize(line)
         print(json.dumps(line), flush=True)
     ctx.close()
     if world > 1:

@@ -134,16 +134,22 @@ parrygpu_status parrygpu_bvh_copy_nodes(parrygpu_ctx* ctx, const parrygpu_bvh* b
  * leaf has that index; a leaf index >= leaf_capacity raises CAPACITY_EXCEEDED). */
 parrygpu_status parrygpu_bvh_export(parrygpu_ctx* ctx, const parrygpu_bvh* bvh, void* nodes, uint64_t* parents, uint64_t* leaf_nodes,
                                     uint64_t leaf_capacity);
+/* Leaf indices (the `data` of a leaf node, the `leaf_ids` of an insert) are below this bound. A
+ * tree whose largest leaf index is L takes L + 1 AABB rows in parrygpu_bvh_refit, so the bound keeps
+ * that row count and the pair index range representable. */
+#define PARRYGPU_MAX_LEAF_INDEX 0x7ffffffeu
 /* A tree from the reference's serialised nodes (n_wide BvhNodeWide records, host or device; e.g.
  * deserialised from parry's serde / rkyv form): parents and depth-first leaf positions are derived
  * on the device. Malformed trees (child index out of range, a node with two parents or none, leaf
- * counts that do not add up) are rejected with INVALID_ARG. */
+ * counts that do not add up, a leaf index above PARRYGPU_MAX_LEAF_INDEX) are rejected with
+ * INVALID_ARG. */
 parrygpu_status parrygpu_bvh_import(parrygpu_ctx* ctx, const void* nodes, uint32_t n_wide, parrygpu_bvh** out);
 /* Bvh::insert(aabb, leaf_index) (bvh_insert.rs:126-133) for k rows: a new leaf index is added, an
  * existing one takes the new AABB (the last row wins); Bvh::remove(leaf_index) (bvh_tree.rs:2360) for
  * k indices (indices without a leaf are ignored). The tree is rebuilt over the resulting leaf set
  * (decision D-9: the layout differs from the reference's incremental edits, query answers do not).
- * Afterwards parrygpu_bvh_refit takes 1 + (largest leaf index) AABB rows indexed by leaf index. */
+ * Afterwards parrygpu_bvh_refit takes 1 + (largest leaf index) AABB rows indexed by leaf index.
+ * A leaf index above PARRYGPU_MAX_LEAF_INDEX is rejected with INVALID_ARG and leaves the tree as it was. */
 parrygpu_status parrygpu_bvh_insert(parrygpu_ctx* ctx, parrygpu_bvh* bvh, const float* aabbs, const uint32_t* leaf_ids, uint32_t k);
 parrygpu_status parrygpu_bvh_remove(parrygpu_ctx* ctx, parrygpu_bvh* bvh, const uint32_t* leaf_ids, uint32_t k);
 
@@ -196,11 +202,15 @@ parrygpu_status parrygpu_trimesh_cast_rays(parrygpu_ctx* ctx, const parrygpu_tri
  * cudaFree's device-wide wait). It allocates nothing: the ray-ordering scratch is a fixed array
  * inside the library, sized for PARRYGPU_NOALLOC_MAX_RAYS rays (about 4.3 MB, held on every GPU
  * that loads the library until exit). Larger batches are rejected with PARRYGPU_INVALID_ARG; split
- * them. rays, feature, toi and normal must be device pointers (host buffers would need staging);
- * pose7 may be host or device memory. The first call on a device looks up the array's device
- * address; make that first call before any stream capture. Every call shares the one array and it
- * keeps the last call's contents, so calls that overlap on the GPU race: keep them on one stream
- * or synchronise between them. Results match parrygpu_trimesh_cast_rays. */
+ * them. rays, feature, toi and normal must be device memory of the context's GPU (host buffers
+ * would need staging; another GPU's memory is rejected). pose7 may be host or device memory; a
+ * device pose7 is read back first, which waits for the context stream's earlier work and cannot
+ * happen inside a stream capture, so a frame loop that must not block passes a host pose7. The
+ * first call on a device looks up the array's device address; make that first call before any
+ * stream capture (later calls outside capture look it up again, so a cudaDeviceReset between calls
+ * is harmless). Every call shares the one array and it keeps the last call's contents, so calls
+ * that overlap on the GPU race: keep them on one stream or synchronise between them. Results match
+ * parrygpu_trimesh_cast_rays. */
 parrygpu_status parrygpu_trimesh_cast_rays_noalloc(parrygpu_ctx* ctx, const parrygpu_trimesh* mesh, const float* pose7,
                                                    const float* rays, uint32_t n, float max_toi, int solid, uint32_t* feature,
                                                    float* toi, float* normal);

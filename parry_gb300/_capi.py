@@ -1,8 +1,8 @@
 """ctypes binding of libparrygpu's C ABI (include/parry_gpu.h).
 
-This is the same binding a Python user of the C library would write; the Rust/C bindings a
-maintainer of the reference would add are shown in INTEGRATION.md. Loading fails loudly when the
-compiled library is missing: there is no CPU fallback.
+This is the same binding a Python user of the C library would write; a Rust caller binds the same
+`extern "C"` declarations. Loading fails loudly when the compiled library is missing: there is no
+CPU fallback.
 """
 from __future__ import annotations
 

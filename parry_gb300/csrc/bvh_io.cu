@@ -116,6 +116,7 @@ __global__ void k_import_leaves(const WideNode* __restrict__ wide, uint32_t n_wi
   const uint32_t pos = start + (s ? count_of(wide[w].l) : 0u);
   if (pos >= n || atomicExch(&seen[pos], 1u) != 0u) { atomicOr(err, ERR_BAD_INDEX); return; }
   const uint32_t id = side_of(wide[w], s).children;
+  if (id > PARRYGPU_MAX_LEAF_INDEX) { atomicOr(err, ERR_BAD_INDEX); return; }
   leaf_parent[pos] = slot;
   leaf_index[pos] = id;
   atomicMax(max_id, id);
@@ -235,7 +236,10 @@ parrygpu_status compact_and_rebuild(parrygpu_ctx* ctx, parrygpu_bvh* bvh, EditSc
   PG_CUDA(ctx, cudaMemcpyAsync(&h[2], max_id, 4, cudaMemcpyDeviceToHost, ctx->stream));
   PG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   const uint32_t count = h[0] + h[1];
-  s = lbvh_build(ctx, bvh, sc.aabbs_out.as<float>(), count, false, sc.ids_out.as<uint32_t>(), count ? h[2] + 1u : 0u);
+  const uint64_t id_bound = count ? (uint64_t)h[2] + 1u : 0u;
+  if (id_bound > (uint64_t)PARRYGPU_MAX_LEAF_INDEX + 1u)
+    return set_error(ctx, PARRYGPU_INVALID_ARG, "leaf index %u above PARRYGPU_MAX_LEAF_INDEX", h[2]);
+  s = lbvh_build(ctx, bvh, sc.aabbs_out.as<float>(), count, false, sc.ids_out.as<uint32_t>(), (uint32_t)id_bound);
   if (s != PARRYGPU_OK) return s;
   PG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   return parrygpu_sync(ctx);
@@ -340,6 +344,8 @@ parrygpu_status parrygpu_bvh_import(parrygpu_ctx* ctx, const void* nodes, uint32
     return set_error(ctx, PARRYGPU_INVALID_ARG, "not a BvhNodeWide tree (parent links or leaf counts)");
   b->n_wide = n_wide;
   b->n_leaves = n;
+  if (h[1] > PARRYGPU_MAX_LEAF_INDEX)  // unreachable after the kernel's check; kept for the row count below
+    return set_error(ctx, PARRYGPU_INVALID_ARG, "leaf index %u above PARRYGPU_MAX_LEAF_INDEX", h[1]);
   b->id_bound = h[1] + 1u;
   b->leaf_data_is_position = false;
   *out = b;
@@ -385,6 +391,8 @@ parrygpu_status parrygpu_bvh_insert(parrygpu_ctx* ctx, parrygpu_bvh* bvh, const 
   uint32_t hmax = 0;
   PG_CUDA(ctx, cudaMemcpyAsync(&hmax, max_id, 4, cudaMemcpyDeviceToHost, ctx->stream));
   PG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  if (hmax > PARRYGPU_MAX_LEAF_INDEX)  // nothing was changed yet: the tree stays as it was
+    return set_error(ctx, PARRYGPU_INVALID_ARG, "leaf index %u above PARRYGPU_MAX_LEAF_INDEX", hmax);
   int rb = 0;
   parrygpu_status s = radix_sort_pairs_in(ctx, m, bits_for(hmax), sc.keys[0].as<uint32_t>(), sc.vals[0].as<uint32_t>(),
                                           sc.keys[1].as<uint32_t>(), sc.vals[1].as<uint32_t>(), sc.hist.as<uint32_t>(), &rb);

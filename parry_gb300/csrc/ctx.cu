@@ -28,6 +28,14 @@ bool is_device_ptr(const void* p) {
   return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
 }
 
+bool on_other_device(const void* p, int device) {
+  if (!p) return false;
+  cudaPointerAttributes a;
+  cudaError_t e = cudaPointerGetAttributes(&a, p);
+  if (e != cudaSuccess) { cudaGetLastError(); return false; }
+  return a.type == cudaMemoryTypeDevice && a.device != device;
+}
+
 bool is_addressable(const void* p) {
   if (!p) return false;
   cudaPointerAttributes a;
@@ -45,6 +53,8 @@ void* device_view_ptr(const void* p) {
 parrygpu_status stage_input(parrygpu_ctx* ctx, DevBuf& buf, const void* src, size_t bytes, const void** dptr) {
   if (bytes == 0) { *dptr = src; return PARRYGPU_OK; }
   if (!src) return set_error(ctx, PARRYGPU_INVALID_ARG, "null input pointer");
+  if (on_other_device(src, ctx->device))
+    return set_error(ctx, PARRYGPU_INVALID_ARG, "an input buffer lives on another GPU than the context's device %d", ctx->device);
   if (is_device_ptr(src)) { *dptr = src; return PARRYGPU_OK; }
   PG_CUDA(ctx, buf.reserve(bytes));
   PG_CUDA(ctx, cudaMemcpyAsync(buf.ptr, src, bytes, cudaMemcpyHostToDevice, ctx->stream));
@@ -55,6 +65,8 @@ parrygpu_status stage_input(parrygpu_ctx* ctx, DevBuf& buf, const void* src, siz
 parrygpu_status stage_output(parrygpu_ctx* ctx, DevBuf& buf, void* dst, size_t bytes, void** dptr, bool* needs_copy) {
   *needs_copy = false;
   if (!dst) { *dptr = nullptr; return PARRYGPU_OK; }
+  if (on_other_device(dst, ctx->device))
+    return set_error(ctx, PARRYGPU_INVALID_ARG, "an output buffer lives on another GPU than the context's device %d", ctx->device);
   if (is_device_ptr(dst)) { *dptr = dst; return PARRYGPU_OK; }
   PG_CUDA(ctx, buf.reserve(bytes < 16 ? 16 : bytes));
   *dptr = buf.ptr;

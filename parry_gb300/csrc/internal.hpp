@@ -143,6 +143,8 @@ parrygpu_status check_cuda(parrygpu_ctx* ctx, cudaError_t e, const char* what);
 bool is_device_ptr(const void* p);
 // Device memory, or page-locked host memory with a device mapping (readable by kernels in place).
 bool is_addressable(const void* p);
+// True when p is device memory of a GPU other than `device` (managed and host memory: false).
+bool on_other_device(const void* p, int device);
 // The device-side address of an addressable pointer (the same value under unified addressing).
 void* device_view_ptr(const void* p);
 template <class T> inline T* device_view(T* p) { return static_cast<T*>(device_view_ptr(p)); }

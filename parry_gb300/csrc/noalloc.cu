@@ -34,19 +34,30 @@ uint32_t* g_scratch_addr[NA_MAX_DEVICES] = {};
 
 // Device address of g_ray_scratch on `device` (which must be current). In host code the array's
 // name is only a host-side stand-in, never a device address, so the address is looked up with
-// cudaGetSymbolAddress once per device and cached.
-parrygpu_status scratch_for_device(parrygpu_ctx* ctx, int device, uint32_t** out) {
+// cudaGetSymbolAddress. Outside stream capture it is looked up on every call (a lookup, no
+// allocation, once the module is loaded), so an address made stale by cudaDeviceReset is never
+// used; the cached value serves calls made while `stream` is being captured, which is why the first
+// call on a device must come before any capture.
+parrygpu_status scratch_for_device(parrygpu_ctx* ctx, int device, cudaStream_t stream, uint32_t** out) {
   if (device < 0 || device >= NA_MAX_DEVICES) return set_error(ctx, PARRYGPU_INVALID_ARG, "device ordinal %d out of range", device);
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  PG_CUDA(ctx, cudaStreamIsCapturing(stream, &cap));
   std::lock_guard<std::mutex> lock(g_setup_mutex);
-  if (!g_scratch_addr[device]) {
+  if (cap == cudaStreamCaptureStatusNone) {
     void* p = nullptr;
     cudaError_t e = cudaGetSymbolAddress(&p, g_ray_scratch);
     if (e != cudaSuccess || !p) return check_cuda(ctx, e == cudaSuccess ? cudaErrorInvalidSymbol : e, "cudaGetSymbolAddress(ray scratch)");
     g_scratch_addr[device] = static_cast<uint32_t*>(p);
+  } else if (!g_scratch_addr[device]) {
+    return set_error(ctx, PARRYGPU_INVALID_ARG,
+                     "parrygpu_trimesh_cast_rays_noalloc: the first call on device %d must come before any stream capture", device);
   }
   *out = g_scratch_addr[device];
   return PARRYGPU_OK;
 }
+
+// Device memory of the context's device, or managed memory.
+bool on_ctx_device(const void* p, int device) { return is_device_ptr(p) && !on_other_device(p, device); }
 
 }  // namespace
 
@@ -63,9 +74,14 @@ extern "C" parrygpu_status parrygpu_trimesh_cast_rays_noalloc(parrygpu_ctx* ctx,
   if (n == 0) return PARRYGPU_OK;
   if (!rays || !feature || !toi) return set_error(ctx, PARRYGPU_INVALID_ARG, "rays, feature and toi are required");
   PG_CUDA(ctx, cudaSetDevice(ctx->device));
-  if (!is_device_ptr(rays) || !is_device_ptr(feature) || !is_device_ptr(toi) || (normal && !is_device_ptr(normal)))
+  const int dev = ctx->device;
+  if (!on_ctx_device(rays, dev) || !on_ctx_device(feature, dev) || !on_ctx_device(toi, dev) || (normal && !on_ctx_device(normal, dev)))
     return set_error(ctx, PARRYGPU_INVALID_ARG,
-                     "parrygpu_trimesh_cast_rays_noalloc needs device pointers for rays and outputs (host buffers would need staging)");
+                     "parrygpu_trimesh_cast_rays_noalloc needs rays and outputs in device memory of the context's GPU %d "
+                     "(host buffers would need staging; another GPU's memory is not read in place)",
+                     dev);
+  if (pose7 && on_other_device(pose7, dev))
+    return set_error(ctx, PARRYGPU_INVALID_ARG, "parrygpu_trimesh_cast_rays_noalloc: pose7 lives on another GPU than %d", dev);
   float pose_host[7];
   const float* pose_ptr = nullptr;
   if (pose7) {
@@ -85,7 +101,7 @@ extern "C" parrygpu_status parrygpu_trimesh_cast_rays_noalloc(parrygpu_ctx* ctx,
   }
   if (radix_sort_hist_entries(n) > NA_HIST) return set_error(ctx, PARRYGPU_INVALID_ARG, "sort histogram exceeds the fixed scratch");
   uint32_t* base = nullptr;
-  parrygpu_status s = scratch_for_device(ctx, ctx->device, &base);
+  parrygpu_status s = scratch_for_device(ctx, ctx->device, ctx->stream, &base);
   if (s != PARRYGPU_OK) return s;
   uint32_t* k0 = base;
   uint32_t* v0 = base + NA_MAX;

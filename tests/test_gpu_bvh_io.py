@@ -76,8 +76,19 @@ def test_import_rejects_malformed(gpu_ctx, oracle_lib):
     bv[0, 7] = (bv[0, 7] & 0xC0000000) | ((u[0, 7] & 0x3FFFFFFF) + 1)  # leaf counts do not add up
     with pytest.raises(pg.ParryGpuError):
         pg.Bvh.from_serialized(gpu_ctx, bad)
+    bad = nodes.copy()
+    bv = bad.view(np.uint32)
+    leaf = np.nonzero((u[:, 7] & 0x3FFFFFFF) == 1)[0]
+    bv[leaf[0], 3] = 0xFFFFFFFF  # leaf index above PARRYGPU_MAX_LEAF_INDEX (its row count would wrap to 0)
+    with pytest.raises(pg.ParryGpuError):
+        pg.Bvh.from_serialized(gpu_ctx, bad)
     ok = pg.Bvh.from_serialized(gpu_ctx, nodes)  # the context is still usable
     assert ok.leaf_count() == 50
+    # an insert with an out-of-range leaf index is refused and leaves the tree as it was
+    with pytest.raises(pg.ParryGpuError):
+        ok.insert(a[:2], np.array([3, 0xFFFFFFFF], np.uint32))
+    assert ok.leaf_count() == 50 and ok.id_bound() == 50
+    np.testing.assert_array_equal(ok.traverse_bvtt_single_tree(), brute_force_pairs(a))
     ok.close()
 
 

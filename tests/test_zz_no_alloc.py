@@ -57,6 +57,12 @@ def test_noalloc_matches_existing_entry_point_on_two_calls(traversal):
         st, *_ = _cast(lib.parrygpu_trimesh_cast_rays_noalloc, ctx, mesh, big, torch)
         assert st == 1
         assert b"PARRYGPU_NOALLOC_MAX_RAYS" in lib.parrygpu_last_error(ctx.handle)
+        # host rays are refused (they would need staging), and so would another GPU's memory
+        host = np.zeros((1000, 6), np.float32)
+        out = torch.empty(1000, dtype=torch.int32, device="cuda")
+        st = lib.parrygpu_trimesh_cast_rays_noalloc(ctx.handle, mesh._h, None, C.c_void_p(host.ctypes.data), 1000, C.c_float(1.0), 1,
+                                                    C.c_void_p(out.data_ptr()), C.c_void_p(out.data_ptr()), None)
+        assert st == 1 and b"device memory" in lib.parrygpu_last_error(ctx.handle)
         mesh.close()
     finally:
         ctx.close()
