@@ -272,8 +272,9 @@ typedef struct parrygpu_shapes {
  * clouds (hull h = points[first[h] .. first[h] + count[h]]), on the host with `threads` threads
  * (0 = all). The triangulation comes from this library's own hull builder (the reference's
  * quickhull numbering is not reproduced: identical triangles for points in general position, other
- * face / vertex ids); from_convex_mesh (:390-639) is restated step for step. A hull whose points span
- * less than 3-D keeps its points with no topology (ok = 0). Read the result with
+ * face / vertex ids); from_convex_mesh (:390-639) is restated step for step. As parry's
+ * convex_hull, a coplanar cloud gets a double-sided polygon (two faces); a hull whose points span
+ * less than 2-D keeps its points with no topology (ok = 0). Read the result with
  * parrygpu_polyhedra_sizes (points, faces, face entries, vertex entries, edges) and
  * parrygpu_polyhedra_copy (buffers sized from those counts; hulls: n_hulls x 8). */
 typedef struct parrygpu_polyhedra_builder parrygpu_polyhedra_builder;
@@ -283,6 +284,14 @@ parrygpu_status parrygpu_polyhedra_sizes(const parrygpu_polyhedra_builder* b, ui
 parrygpu_status parrygpu_polyhedra_copy(const parrygpu_polyhedra_builder* b, float* points, uint32_t* hulls, float* face_normals,
                                         uint32_t* face_ranges, uint32_t* face_vertices, uint32_t* face_edges, uint32_t* vertex_ranges,
                                         uint32_t* vertex_faces, uint32_t* vertex_edges, float* edge_dirs);
+/* transformation::convex_hull's triangulation of each cloud (src/transformation/convex_hull3/
+ * convex_hull.rs:13-27: closed, counter-clockwise seen from outside, the (vertices, indices) pair
+ * that check_convex_hull validates), before from_convex_mesh merges coplanar triangles: 3 hull-local
+ * vertex ids per triangle (into the hull's points as parrygpu_polyhedra_copy returns them, whose
+ * order is utils::remove_unused_points'); tri_ranges = n_hulls x (first triangle, count). Any output
+ * may be NULL; *n_triangles receives the total. */
+parrygpu_status parrygpu_polyhedra_triangles(const parrygpu_polyhedra_builder* b, uint64_t* n_triangles, uint32_t* tri_ranges,
+                                             uint32_t* triangles);
 void parrygpu_polyhedra_builder_destroy(parrygpu_polyhedra_builder* b);
 
 /* The same build on the GPU (one thread per cloud; the host builder's algorithm, the same bytes):
@@ -298,6 +307,9 @@ parrygpu_status parrygpu_polyhedra_gpu_copy(parrygpu_ctx* ctx, const parrygpu_po
                                             float* face_normals, uint32_t* face_ranges, uint32_t* face_vertices, uint32_t* face_edges,
                                             uint32_t* vertex_ranges, uint32_t* vertex_faces, uint32_t* vertex_edges, float* edge_dirs);
 parrygpu_status parrygpu_polyhedra_gpu_view(const parrygpu_polyhedra_gpu* g, const float** points, parrygpu_polyhedra* view);
+/* The GPU build's triangulations, as parrygpu_polyhedra_triangles (host or device buffers). */
+parrygpu_status parrygpu_polyhedra_gpu_triangles(parrygpu_ctx* ctx, const parrygpu_polyhedra_gpu* g, uint64_t* n_triangles,
+                                                 uint32_t* tri_ranges, uint32_t* triangles);
 void parrygpu_polyhedra_gpu_destroy(parrygpu_polyhedra_gpu* g);
 
 /* Same layout as the reference's Contact (src/query/contact/contact.rs:71-105), world space. */

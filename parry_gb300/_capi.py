@@ -61,6 +61,7 @@ SIGNATURES: dict[str, tuple] = {
     "parrygpu_polyhedra_gpu_sizes": (I32, [P, P]),
     "parrygpu_polyhedra_gpu_copy": (I32, [P, P, P, P, P, P, P, P, P, P, P, P]),
     "parrygpu_polyhedra_gpu_view": (I32, [P, P, P]),
+    "parrygpu_polyhedra_gpu_triangles": (I32, [P, P, P, P, P]),
     "parrygpu_polyhedra_gpu_destroy": (None, [P]),
     "parrygpu_trimesh_set_flags": (I32, [P, P, U32]),
     "parrygpu_trimesh_normal_constraints": (I32, [P, P, P, P]),
@@ -88,6 +89,7 @@ SIGNATURES: dict[str, tuple] = {
     "parrygpu_scene_read": (I32, [P, P, P, P, P, U64, P, P, P]),
     "parrygpu_polyhedra_sizes": (I32, [P, P]),
     "parrygpu_polyhedra_copy": (I32, [P, P, P, P, P, P, P, P, P, P, P]),
+    "parrygpu_polyhedra_triangles": (I32, [P, P, P, P]),
     "parrygpu_polyhedra_builder_destroy": (None, [P]),
     "parrygpu_mlp_create": (I32, [P, U64, C.POINTER(P)]),
     "parrygpu_mlp_destroy": (None, [P]),

@@ -32,7 +32,7 @@ struct HostWs {
 
   void reserve(uint32_t n) {
     caps = HullCaps::of(n);
-    pts.resize(n); faces.resize(caps.faces); visible.resize(caps.faces); horizon.resize(2 * caps.horizon);
+    pts.resize(n); faces.resize(caps.faces); visible.resize(caps.faces); horizon.resize(HORIZON_WORDS * caps.horizon);
     tris.resize(3 * caps.tris); used.resize(n); remap.resize(n); fpts.resize(n); edges.resize(caps.edges);
     hkeys.resize(caps.hash); hvals.resize(caps.hash); htris.resize(caps.tris); frecs.resize(caps.tris);
     face_edges.resize(caps.entries); face_vertices.resize(caps.entries); vertex_first.resize(n); vertex_count.resize(n);
@@ -49,6 +49,7 @@ struct HostHull {
   HullOut r;
   std::vector<float> points, face_normals, edge_dirs;
   std::vector<uint32_t> face_ranges, face_vertices, face_edges, vertex_ranges, vertex_faces, vertex_edges;
+  std::vector<uint32_t> triangles;
 };
 
 }  // namespace
@@ -83,8 +84,9 @@ parrygpu_status parrygpu_polyhedra_build(const float* points, const uint32_t* fi
       H.face_normals.resize(3 * (size_t)nf); H.face_ranges.resize(2 * (size_t)nf);
       H.face_vertices.resize(nfe); H.face_edges.resize(nfe); H.vertex_faces.resize(nve); H.vertex_edges.resize(nve);
       H.edge_dirs.resize(3 * (size_t)ne);
+      H.triangles.resize(3 * (size_t)H.r.ntris);
       PolyOut o{H.points.data(), nullptr, H.face_normals.data(), H.face_ranges.data(), H.face_vertices.data(), H.face_edges.data(),
-                H.vertex_ranges.data(), H.vertex_faces.data(), H.vertex_edges.data(), H.edge_dirs.data()};
+                H.vertex_ranges.data(), H.vertex_faces.data(), H.vertex_edges.data(), H.edge_dirs.data(), H.triangles.data()};
       emit(w.ws, H.r, 0, 0, 0, 0, 0, 0, o);
     }
   };
@@ -143,6 +145,21 @@ parrygpu_status parrygpu_polyhedra_copy(const parrygpu_polyhedra_builder* b, flo
     if (edge_dirs && ne) std::memcpy(edge_dirs + 3 * ep, H.edge_dirs.data(), H.edge_dirs.size() * 4);
     vp += np; fp += nf; fe += nfe; ve += nve; ep += ne;
   }
+  return PARRYGPU_OK;
+}
+
+parrygpu_status parrygpu_polyhedra_triangles(const parrygpu_polyhedra_builder* b, uint64_t* n_triangles, uint32_t* tri_ranges,
+                                             uint32_t* triangles) {
+  if (!b) return PARRYGPU_INVALID_ARG;
+  uint64_t tp = 0;
+  for (size_t h = 0; h < b->hulls.size(); ++h) {
+    const HostHull& H = b->hulls[h];
+    const uint32_t nt = (uint32_t)(H.triangles.size() / 3);
+    if (tri_ranges) { tri_ranges[2 * h] = (uint32_t)tp; tri_ranges[2 * h + 1] = nt; }
+    if (triangles && nt) std::memcpy(triangles + 3 * tp, H.triangles.data(), H.triangles.size() * 4);
+    tp += nt;
+  }
+  if (n_triangles) *n_triangles = tp;
   return PARRYGPU_OK;
 }
 

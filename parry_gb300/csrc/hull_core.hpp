@@ -7,7 +7,13 @@
 //   hull_triangles: this library's own incremental hull in double precision. It produces the same
 //     triangulation as any exact hull for points in general position, but not parry's quickhull
 //     numbering (parry orders its initial simplex by a covariance eigen-decomposition); a caller
-//     holding parry's own ConvexPolyhedron passes that topology through the C ABI instead.
+//     holding parry's own ConvexPolyhedron passes that topology through the C ABI instead. Like
+//     parry's convex_hull it always returns a closed 2-manifold that transformation::
+//     check_convex_hull accepts (src/transformation/convex_hull3/validation.rs:33-108): the faces a
+//     new point sees are grown from the face it sees best through face adjacency, a point whose
+//     seen region is not bounded by one simple cycle of edges (rounding on nearly coplanar faces) is
+//     left out as lying on the hull, and a cloud whose points are coplanar gets the double-sided
+//     polygon parry builds for it (src/transformation/convex_hull3/initial_mesh.rs).
 //   remove_unused_points and from_convex_mesh: restated step for step in f32 (src/utils/cleanup.rs:6-34,
 //     src/shape/convex_polyhedron.rs:390-639), so the faces, normals and ids follow from the
 //     triangles exactly as in the reference.
@@ -20,6 +26,7 @@
 #include <cstddef>
 #include <cstdint>
 #include <cmath>
+#include <cstring>
 
 #if defined(__CUDACC__)
 #define HC_FN __host__ __device__ inline
@@ -68,10 +75,93 @@ constexpr uint32_t NONE = 0xffffffffu;
 
 struct HFace {
   uint32_t v[3];
-  uint32_t alive;
-  D3 n;
+  uint32_t alive;   // 0 dead, 1 live, 2 live and seen from the point being inserted
+  uint32_t adj[3];  // the face across edge (v[k], v[k + 1])
+  uint32_t pad;
+  D3 n;             // unit normal and offset: the rounded plane, a filter for the exact test
   double off;
+  double tol;       // bound on the rounding of n . p - off over the cloud
 };
+
+// ---- exact orientation ----------------------------------------------------------------------
+// The hull decides visibility with the exact sign of orientation determinants (Shewchuk, "Adaptive
+// Precision Floating-Point Arithmetic and Fast Robust Geometric Predicates", 1997): a rounded
+// evaluation settles the sign when it clears an error bound, else an error-free expansion of the
+// determinant decides. Coordinates are f32 values held in doubles, so their differences are exact
+// (for coordinates within a factor 2^29 of one another, or zero) and the expansion gives the true
+// sign. With exact signs the incremental hull stays convex and manifold on coplanar and repeated
+// points, where tolerance-based tests fold faces over.
+HC_FN void two_sum(double a, double b, double* s, double* e) {
+  const double x = a + b, bv = x - a, av = x - bv;
+  *s = x;
+  *e = (a - av) + (b - bv);
+}
+HC_FN void two_prod(double a, double b, double* p, double* e) {
+  const double x = a * b;
+  *p = x;
+  *e = fma(a, b, -x);
+}
+// Sign of the exact sum of x[0..m) (m <= 24): a nonoverlapping expansion grown one term at a time
+// (Grow-Expansion), whose most significant nonzero component carries the sign.
+HC_FN int exact_sum_sign(const double* x, int m) {
+  double e[24];
+  int ne = 0;
+  for (int i = 0; i < m; ++i) {
+    double q = x[i];
+    for (int j = 0; j < ne; ++j) {
+      double sum, err;
+      two_sum(q, e[j], &sum, &err);
+      e[j] = err;
+      q = sum;
+    }
+    e[ne++] = q;
+  }
+  for (int j = ne - 1; j >= 0; --j)
+    if (e[j] != 0.0) return e[j] > 0.0 ? 1 : -1;
+  return 0;
+}
+// Sign of (x0 * y0 - x1 * y1), exactly.
+HC_FN int diff_of_products_sign(double x0, double y0, double x1, double y1) {
+  double t[4];
+  two_prod(x0, y0, &t[0], &t[1]);
+  two_prod(-x1, y1, &t[2], &t[3]);
+  return exact_sum_sign(t, 4);
+}
+// Sign of ((b - a) x (c - a)) . (p - a): positive when p lies on the side the right-handed normal of
+// triangle (a, b, c) points to.
+HC_FN int orient3d_sign(D3 a, D3 b, D3 c, D3 p) {
+  const D3 u = dsub(b, a), v = dsub(c, a), w = dsub(p, a);
+  const double m1 = v.y * w.z - v.z * w.y, m2 = v.z * w.x - v.x * w.z, m3 = v.x * w.y - v.y * w.x;
+  const double det = u.x * m1 + u.y * m2 + u.z * m3;
+  const double perm = fabs(u.x) * (fabs(v.y * w.z) + fabs(v.z * w.y)) + fabs(u.y) * (fabs(v.z * w.x) + fabs(v.x * w.z)) +
+                      fabs(u.z) * (fabs(v.x * w.y) + fabs(v.y * w.x));
+  const double bound = 1e-15 * perm;  // above the rounding of det (7.8e-16 x perm)
+  if (det > bound) return 1;
+  if (det < -bound) return -1;
+  double t[24];
+  int k = 0;
+  auto triple = [&](double x, double y, double z, bool neg) {
+    double p, pe, q0, q1, r0, r1;
+    two_prod(x, y, &p, &pe);
+    two_prod(p, z, &q0, &q1);
+    two_prod(pe, z, &r0, &r1);
+    const double sg = neg ? -1.0 : 1.0;
+    t[k++] = sg * q0; t[k++] = sg * q1; t[k++] = sg * r0; t[k++] = sg * r1;
+  };
+  triple(u.x, v.y, w.z, false); triple(u.x, v.z, w.y, true);
+  triple(u.y, v.z, w.x, false); triple(u.y, v.x, w.z, true);
+  triple(u.z, v.x, w.y, false); triple(u.z, v.y, w.x, true);
+  return exact_sum_sign(t, 24);
+}
+// True when (b - a) x (c - a) is exactly the zero vector (a, b, c collinear or repeated).
+HC_FN bool collinear_exact(D3 a, D3 b, D3 c) {
+  const D3 u = dsub(b, a), v = dsub(c, a);
+  return diff_of_products_sign(u.y, v.z, u.z, v.y) == 0 && diff_of_products_sign(u.z, v.x, u.x, v.z) == 0 &&
+         diff_of_products_sign(u.x, v.y, u.y, v.x) == 0;
+}
+
+// Words per horizon entry: edge start, edge end, the unseen face across the edge.
+constexpr uint32_t HORIZON_WORDS = 3;
 
 struct HEdge {
   uint32_t v[2];
@@ -116,7 +206,7 @@ struct HullWs {
   Span<D3> pts;              // n
   Span<HFace> faces;         // caps.faces
   Span<uint32_t> visible;    // caps.faces
-  Span<uint32_t> horizon;    // 2 x caps.horizon
+  Span<uint32_t> horizon;    // HORIZON_WORDS x caps.horizon
   Span<uint32_t> tris;       // 3 x caps.tris
   Span<uint32_t> used;       // n
   Span<uint32_t> remap;      // n
@@ -131,24 +221,113 @@ struct HullWs {
   Span<uint32_t> vertex_faces, vertex_edges;   // caps.entries
 };
 
-// Incremental convex hull of pts[0..n) (x, y, z floats). Writes the outward-oriented triangles
-// (counter-clockwise seen from outside, so (b - a) x (c - a) points out) to ws.tris and returns
-// their count; 0 when the points span less than 3-D (or, on inputs whose rounding breaks the
-// hull's manifold structure, when a capacity would overflow).
+// Double-sided polygon of a coplanar cloud (what parry's convex_hull returns for one): the 2-D hull
+// of the points on the two coordinates other than the dominant axis of the plane's normal (an exact
+// projection), by Andrew's monotone chain with exact turn signs (collinear points dropped),
+// triangulated as a fan from its first vertex on one side and a fan from its second vertex on the
+// other side, so that no diagonal is shared by the two sides. Returns the triangle count (0 when
+// fewer than 3 points are extreme).
+HC_FN uint32_t planar_triangles(uint32_t n, uint32_t i0, uint32_t i1, uint32_t i2, const HullCaps& caps, HullWs& ws) {
+  const D3 p0 = ws.pts[i0];
+  const D3 nrm = dcross(dsub(ws.pts[i1], p0), dsub(ws.pts[i2], p0));
+  const double ax = fabs(nrm.x), ay = fabs(nrm.y), az = fabs(nrm.z);
+  const int drop = (ax >= ay && ax >= az) ? 0 : (ay >= az ? 1 : 2);
+  auto X = [&](uint32_t i) { const D3 p = ws.pts[i]; return drop == 0 ? p.y : (drop == 1 ? p.z : p.x); };
+  auto Y = [&](uint32_t i) { const D3 p = ws.pts[i]; return drop == 0 ? p.z : (drop == 1 ? p.x : p.y); };
+  // point indices sorted by (X, Y) in ws.remap with a heap sort (repeated points: the first kept)
+  uint32_t m = 0;
+  for (uint32_t i = 0; i < n; ++i)
+    if (!ws.remap[i]) ws.used[m++] = i;
+  for (uint32_t i = 0; i < m; ++i) ws.remap[i] = ws.used[i];
+  auto less = [&](uint32_t a, uint32_t b) {
+    return X(a) < X(b) || (X(a) == X(b) && (Y(a) < Y(b) || (Y(a) == Y(b) && a < b)));
+  };
+  auto sift = [&](uint32_t root, uint32_t end) {
+    while (2 * root + 1 < end) {
+      uint32_t child = 2 * root + 1;
+      if (child + 1 < end && less(ws.remap[child], ws.remap[child + 1])) ++child;
+      if (!less(ws.remap[root], ws.remap[child])) return;
+      const uint32_t t = ws.remap[root]; ws.remap[root] = ws.remap[child]; ws.remap[child] = t;
+      root = child;
+    }
+  };
+  for (uint32_t i = m / 2; i-- > 0;) sift(i, m);
+  for (uint32_t end = m; end-- > 1;) {
+    const uint32_t t = ws.remap[0]; ws.remap[0] = ws.remap[end]; ws.remap[end] = t;
+    sift(0, end);
+  }
+  auto left_turn = [&](uint32_t o, uint32_t a, uint32_t b) {  // o -> a -> b counter-clockwise in (X, Y)
+    return diff_of_products_sign(X(a) - X(o), Y(b) - Y(o), Y(a) - Y(o), X(b) - X(o)) > 0;
+  };
+  // the chain, counter-clockwise in (X, Y), in ws.visible
+  uint32_t k = 0;
+  for (uint32_t i = 0; i < m; ++i) {
+    const uint32_t p = ws.remap[i];
+    while (k >= 2 && !left_turn(ws.visible[k - 2], ws.visible[k - 1], p)) --k;
+    ws.visible[k++] = p;
+  }
+  for (uint32_t i = m - 1, lower = k + 1; i-- > 0;) {
+    const uint32_t p = ws.remap[i];
+    while (k >= lower && !left_turn(ws.visible[k - 2], ws.visible[k - 1], p)) --k;
+    ws.visible[k++] = p;
+  }
+  const uint32_t h = k - 1;  // the last point repeats the first
+  if (h < 3 || 2 * (h - 2) > caps.tris) return 0;
+  uint32_t nt = 0;
+  for (uint32_t i = 1; i + 1 < h; ++i) {  // one side: fan from the first vertex
+    ws.tris[3 * nt] = ws.visible[0]; ws.tris[3 * nt + 1] = ws.visible[i]; ws.tris[3 * nt + 2] = ws.visible[i + 1];
+    ++nt;
+  }
+  for (uint32_t j = 2; j < h; ++j) {  // other side: fan from the second vertex, reversed
+    ws.tris[3 * nt] = ws.visible[1]; ws.tris[3 * nt + 1] = ws.visible[(j + 1) % h]; ws.tris[3 * nt + 2] = ws.visible[j];
+    ++nt;
+  }
+  return nt;
+}
+
+// Incremental convex hull of pts[0..n) (x, y, z floats) with exact visibility. Writes the
+// outward-oriented triangles (counter-clockwise seen from outside, so (b - a) x (c - a) points out)
+// to ws.tris and returns their count; a coplanar cloud gets its double-sided polygon; 0 when the
+// points span less than 2-D.
 HC_FN uint32_t hull_triangles(const float* in, uint32_t n, const HullCaps& caps, HullWs& ws) {
-  if (n < 4) return 0;
+  if (n < 3) return 0;
   D3 lo = {1e300, 1e300, 1e300}, hi = {-1e300, -1e300, -1e300};
+  double rmax = 0.0;
   for (uint32_t i = 0; i < n; ++i) {
     D3 p = D3{(double)in[3 * i], (double)in[3 * i + 1], (double)in[3 * i + 2]};
     ws.pts[i] = p;
     lo = D3{dmin(lo.x, p.x), dmin(lo.y, p.y), dmin(lo.z, p.z)};
     hi = D3{dmax(hi.x, p.x), dmax(hi.y, p.y), dmax(hi.z, p.z)};
+    rmax = dmax(rmax, dmax(fabs(p.x), dmax(fabs(p.y), fabs(p.z))));
   }
   D3 ext = dsub(hi, lo);
   double scale = dmax(ext.x, dmax(ext.y, ext.z));
-  if (!(scale > 0.0) || !((scale - scale) == 0.0)) return 0;  // not positive, or not finite
-  const double eps = 1e-10 * scale;  // plane-distance tolerance
+  if (!(scale > 0.0) || !((scale - scale) == 0.0)) return 0;  // all points equal, or not finite
+  // a point equal to an earlier one (f32 ==) never enters the hull: ws.remap[i] = 1 marks it, found
+  // through the open-addressing table (free until from_convex_mesh)
+  for (uint32_t h = 0; h < caps.hash; ++h) ws.hkeys[h] = ~0ull;
+  for (uint32_t i = 0; i < n; ++i) {
+    const float* q = in + 3 * i;
+    uint64_t key = 0x9E3779B97F4A7C15ull;
+    for (int k = 0; k < 3; ++k) {
+      uint32_t b;
+      const float c = q[k] == 0.0f ? 0.0f : q[k];  // -0 == +0
+      memcpy(&b, &c, 4);
+      key = (key ^ b) * 0xBF58476D1CE4E5B9ull;
+      key ^= key >> 31;
+    }
+    if (key == ~0ull) key = 0;
+    uint32_t h = (uint32_t)(key >> 40) & (caps.hash - 1);
+    ws.remap[i] = 0;
+    while (ws.hkeys[h] != ~0ull) {
+      const float* o = in + 3 * ws.hvals[h];
+      if (ws.hkeys[h] == key && o[0] == q[0] && o[1] == q[1] && o[2] == q[2]) { ws.remap[i] = 1; break; }
+      h = (h + 1) & (caps.hash - 1);
+    }
+    if (!ws.remap[i]) { ws.hkeys[h] = key; ws.hvals[h] = i; }
+  }
   // initial tetrahedron: extreme x, farthest point, farthest from the line, farthest from the plane
+  // (each an exact decision: the largest rounded measure, else the first point that is exactly off)
   uint32_t i0 = 0;
   for (uint32_t i = 1; i < n; ++i)
     if (ws.pts[i].x < ws.pts[i0].x) i0 = i;
@@ -160,7 +339,6 @@ HC_FN uint32_t hull_triangles(const float* in, uint32_t n, const HullCaps& caps,
     double l = ddot(d, d);
     if (l > best) { best = l; i1 = i; }
   }
-  if (best <= eps * eps) return 0;
   D3 e01 = dsub(ws.pts[i1], p0);
   uint32_t i2 = i0;
   best = -1.0;
@@ -169,76 +347,145 @@ HC_FN uint32_t hull_triangles(const float* in, uint32_t n, const HullCaps& caps,
     double l = ddot(c, c);
     if (l > best) { best = l; i2 = i; }
   }
-  if (best <= (eps * scale) * (eps * scale)) return 0;
+  if (collinear_exact(p0, ws.pts[i1], ws.pts[i2])) {
+    i2 = NONE;
+    for (uint32_t i = 0; i < n && i2 == NONE; ++i)
+      if (!collinear_exact(p0, ws.pts[i1], ws.pts[i])) i2 = i;
+    if (i2 == NONE) return 0;  // collinear cloud
+  }
   D3 nrm = dcross(e01, dsub(ws.pts[i2], p0));
-  double nn = sqrt(ddot(nrm, nrm));
   uint32_t i3 = i0;
   best = -1.0;
-  double side = 0.0;
   for (uint32_t i = 0; i < n; ++i) {
-    double d = ddot(nrm, dsub(ws.pts[i], p0)) / nn;
-    if (fabs(d) > best) { best = fabs(d); i3 = i; side = d; }
+    double d = fabs(ddot(nrm, dsub(ws.pts[i], p0)));
+    if (d > best) { best = d; i3 = i; }
   }
-  if (best <= eps) return 0;
+  int side = orient3d_sign(p0, ws.pts[i1], ws.pts[i2], ws.pts[i3]);
+  for (uint32_t i = 0; i < n && side == 0; ++i) {
+    side = orient3d_sign(p0, ws.pts[i1], ws.pts[i2], ws.pts[i]);
+    i3 = i;
+  }
+  if (side == 0) return planar_triangles(n, i0, i1, i2, caps, ws);
 
   uint32_t nf = 0;
-  auto add_face = [&](uint32_t a, uint32_t b, uint32_t c) {
+  auto add_face = [&](uint32_t a, uint32_t b, uint32_t c, uint32_t f0, uint32_t f1, uint32_t f2) {
     HFace f;
     f.v[0] = a; f.v[1] = b; f.v[2] = c;
-    const D3 pa = ws.pts[a];
-    D3 fn = dcross(dsub(ws.pts[b], pa), dsub(ws.pts[c], pa));
+    f.adj[0] = f0; f.adj[1] = f1; f.adj[2] = f2;
+    f.pad = 0;
+    const D3 pa = ws.pts[a], u = dsub(ws.pts[b], pa), v = dsub(ws.pts[c], pa);
+    D3 fn = dcross(u, v);
     double l = sqrt(ddot(fn, fn));
     f.n = l > 0 ? D3{fn.x / l, fn.y / l, fn.z / l} : D3{0, 0, 0};
     f.off = ddot(f.n, pa);
+    // rounding of the normal's direction (relative to how thin the face is) times the cloud's
+    // extent, plus the rounding of the two dot products
+    const double cond = l > 0 ? sqrt(ddot(u, u) * ddot(v, v)) / l : 1e300;
+    f.tol = 1e-14 * (rmax + scale * (1.0 + cond));
     f.alive = 1;
     ws.faces[nf++] = f;
   };
+  // whether face F sees p (p strictly above its plane), exactly
+  auto sees = [&](const HFace& F, const D3& p) {
+    const double d = ddot(F.n, p) - F.off;
+    if (d > F.tol) return true;
+    if (d < -F.tol) return false;
+    return orient3d_sign(ws.pts[F.v[0]], ws.pts[F.v[1]], ws.pts[F.v[2]], p) > 0;
+  };
+  // faces 0-3 with their neighbours: face k's edge j borders the face listed at [k][j]
   if (side > 0) {  // i3 above plane (i0, i1, i2): that face looks away from i3
-    add_face(i0, i2, i1); add_face(i0, i1, i3); add_face(i1, i2, i3); add_face(i2, i0, i3);
+    add_face(i0, i2, i1, 3, 2, 1); add_face(i0, i1, i3, 0, 2, 3); add_face(i1, i2, i3, 0, 3, 1); add_face(i2, i0, i3, 0, 1, 2);
   } else {
-    add_face(i0, i1, i2); add_face(i0, i3, i1); add_face(i1, i3, i2); add_face(i2, i3, i0);
+    add_face(i0, i1, i2, 1, 2, 3); add_face(i0, i3, i1, 3, 2, 0); add_face(i1, i3, i2, 1, 3, 0); add_face(i2, i3, i0, 2, 1, 0);
   }
   for (uint32_t pi = 0; pi < n; ++pi) {
-    if (pi == i0 || pi == i1 || pi == i2 || pi == i3) continue;
+    if (pi == i0 || pi == i1 || pi == i2 || pi == i3 || ws.remap[pi]) continue;
+    if (nf + caps.horizon > caps.faces) {  // drop dead faces (creation order kept), renumbering links
+      uint32_t k = 0;
+      for (uint32_t f = 0; f < nf; ++f) ws.visible[f] = ws.faces[f].alive ? k++ : NONE;
+      k = 0;
+      for (uint32_t f = 0; f < nf; ++f)
+        if (ws.faces[f].alive) {
+          HFace F = ws.faces[f];
+          for (int j = 0; j < 3; ++j) F.adj[j] = ws.visible[F.adj[j]];
+          ws.faces[k++] = F;
+        }
+      nf = k;
+      if (nf + caps.horizon > caps.faces) return 0;  // more live faces than a closed hull of n points has
+    }
     const D3 pp = ws.pts[pi];
-    uint32_t nvis = 0;
+    // the face that sees pp at the largest distance, then every face that sees pp connected to it
+    // (for a convex hull and an exact test, that is every face that sees pp)
+    uint32_t seed = NONE;
+    double bestd = -1e300;
     for (uint32_t f = 0; f < nf; ++f) {
       const HFace& F = ws.faces[f];
-      if (F.alive && ddot(F.n, pp) - F.off > eps) ws.visible[nvis++] = f;
+      if (!F.alive) continue;
+      const double d = ddot(F.n, pp) - F.off;
+      if (d > bestd && d >= -F.tol && sees(F, pp)) { bestd = d; seed = f; }
     }
-    if (nvis == 0) continue;  // inside or on the hull
-    // horizon: directed edges of visible faces whose reverse belongs to no visible face
-    uint32_t nh = 0;
+    if (seed == NONE) continue;  // inside or on the hull
+    uint32_t nvis = 0;
+    ws.visible[nvis++] = seed;
+    ws.faces[seed].alive = 2;
     for (uint32_t i = 0; i < nvis; ++i) {
-      const HFace& F = ws.faces[ws.visible[i]];
-      for (int k = 0; k < 3; ++k) {
-        const uint32_t a = F.v[k], b = F.v[(k + 1) % 3];
-        bool shared = false;
-        for (uint32_t j = 0; j < nvis && !shared; ++j) {
-          const HFace& G = ws.faces[ws.visible[j]];
-          for (int kk = 0; kk < 3; ++kk)
-            if (G.v[kk] == b && G.v[(kk + 1) % 3] == a) { shared = true; break; }
-        }
-        if (!shared) {
-          if (nh >= caps.horizon) return 0;
-          ws.horizon[2 * nh] = a;
-          ws.horizon[2 * nh + 1] = b;
-          ++nh;
+      for (int j = 0; j < 3; ++j) {
+        const uint32_t g = ws.faces[ws.visible[i]].adj[j];
+        HFace& G = ws.faces[g];
+        if (G.alive == 1 && sees(G, pp)) {
+          G.alive = 2;
+          ws.visible[nvis++] = g;
         }
       }
     }
-    for (uint32_t i = 0; i < nvis; ++i) ws.faces[ws.visible[i]].alive = 0;
-    if (nf + nh > caps.faces) {  // drop dead faces, keeping the creation order of the live ones
-      uint32_t k = 0;
-      for (uint32_t f = 0; f < nf; ++f)
-        if (ws.faces[f].alive) {
-          if (k != f) ws.faces[k] = ws.faces[f];
-          ++k;
-        }
-      nf = k;
-      if (nf + nh > caps.faces) return 0;
+    // horizon: edges of seen faces whose other face is unseen, chained into one cycle
+    uint32_t nh = 0;
+    bool simple = true;
+    for (uint32_t i = 0; i < nvis && simple; ++i) {
+      const HFace& F = ws.faces[ws.visible[i]];
+      for (int j = 0; j < 3; ++j) {
+        if (ws.faces[F.adj[j]].alive == 2) continue;
+        if (nh >= caps.horizon) { simple = false; break; }
+        ws.horizon[HORIZON_WORDS * nh] = F.v[j];
+        ws.horizon[HORIZON_WORDS * nh + 1] = F.v[(j + 1) % 3];
+        ws.horizon[HORIZON_WORDS * nh + 2] = F.adj[j];
+        ++nh;
+      }
     }
-    for (uint32_t h = 0; h < nh; ++h) add_face(ws.horizon[2 * h], ws.horizon[2 * h + 1], pi);
+    for (uint32_t h = 0; h + 1 < nh && simple; ++h) {
+      uint32_t next = NONE;
+      for (uint32_t g = h + 1; g < nh; ++g)
+        if (ws.horizon[HORIZON_WORDS * g] == ws.horizon[HORIZON_WORDS * h + 1]) { next = g; break; }
+      if (next == NONE) { simple = false; break; }
+      for (uint32_t w = 0; w < HORIZON_WORDS; ++w) {
+        const uint32_t t = ws.horizon[HORIZON_WORDS * (h + 1) + w];
+        ws.horizon[HORIZON_WORDS * (h + 1) + w] = ws.horizon[HORIZON_WORDS * next + w];
+        ws.horizon[HORIZON_WORDS * next + w] = t;
+      }
+    }
+    if (simple && (nh < 3 || ws.horizon[HORIZON_WORDS * (nh - 1) + 1] != ws.horizon[0])) simple = false;
+    if (simple) {  // one cycle through distinct vertices (no pinch)
+      for (uint32_t h = 0; h < nh; ++h) ws.used[ws.horizon[HORIZON_WORDS * h]] = 0;
+      for (uint32_t h = 0; h < nh && simple; ++h) {
+        uint32_t& mark = ws.used[ws.horizon[HORIZON_WORDS * h]];
+        if (mark) simple = false;
+        mark = 1;
+      }
+    }
+    if (!simple) {  // cannot happen with exact signs on a convex hull; kept as a guard (pp left out)
+      for (uint32_t i = 0; i < nvis; ++i) ws.faces[ws.visible[i]].alive = 1;
+      continue;
+    }
+    for (uint32_t i = 0; i < nvis; ++i) ws.faces[ws.visible[i]].alive = 0;
+    const uint32_t first = nf;
+    for (uint32_t h = 0; h < nh; ++h) {
+      const uint32_t a = ws.horizon[HORIZON_WORDS * h], b = ws.horizon[HORIZON_WORDS * h + 1];
+      const uint32_t out = ws.horizon[HORIZON_WORDS * h + 2];
+      add_face(a, b, pi, out, first + (h + 1) % nh, first + (h + nh - 1) % nh);
+      HFace& O = ws.faces[out];
+      for (int j = 0; j < 3; ++j)
+        if (O.v[j] == b && O.v[(j + 1) % 3] == a) O.adj[j] = first + h;
+    }
   }
   uint32_t nt = 0;
   for (uint32_t f = 0; f < nf; ++f) {
@@ -257,6 +504,7 @@ HC_FN uint32_t hull_triangles(const float* in, uint32_t n, const HullCaps& caps,
 // from_convex_mesh (frecs / face_edges / face_vertices, vertex_first / vertex_count / vertex_faces /
 // vertex_edges, edges).
 struct HullOut {
+  uint32_t ntris = 0;  // triangles of the hull (transformation::convex_hull's indices), in ws.tris
   uint32_t npts = 0, nfaces = 0;
   uint32_t nfentries = 0;  // face entries, those of dropped degenerate faces included
   uint32_t nventries = 0;  // vertex entries (from the kept faces)
@@ -447,6 +695,7 @@ HC_FN HullOut build_one(const float* in, uint32_t n, const HullCaps& caps, HullW
     out = HullOut();
     out.npts = m;
   }
+  out.ntris = nt;
   return out;
 }
 
@@ -457,12 +706,15 @@ struct PolyOut {
   float* face_normals;
   uint32_t *face_ranges, *face_vertices, *face_edges, *vertex_ranges, *vertex_faces, *vertex_edges;
   float* edge_dirs;
+  uint32_t* triangles;  // 3 hull-local vertex ids per triangle (may be null)
 };
 
-// Writes one hull's result (in ws, described by r) at offsets vp / fp / fe / ve / ep; null arrays
-// are skipped.
+// Writes one hull's result (in ws, described by r) at offsets vp / fp / fe / ve / ep / tp (tp in
+// triangles); null arrays are skipped.
 HC_FN void emit(const HullWs& ws, const HullOut& r, uint64_t h, uint64_t vp, uint64_t fp, uint64_t fe, uint64_t ve, uint64_t ep,
-                const PolyOut& o) {
+                const PolyOut& o, uint64_t tp = 0) {
+  if (o.triangles)
+    for (uint32_t k = 0; k < 3 * r.ntris; ++k) o.triangles[3 * tp + k] = ws.tris[k];
   if (o.hulls) {
     uint32_t* rec = o.hulls + 8 * h;
     rec[0] = (uint32_t)vp; rec[1] = r.npts;

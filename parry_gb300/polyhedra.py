@@ -15,11 +15,14 @@ TOPOLOGY_KEYS = ("face_normals", "face_ranges", "face_vertices", "face_edges", "
                  "edge_dirs")
 
 
-def build_polyhedra(pool: np.ndarray, first: np.ndarray, count: np.ndarray, threads: int = 0, ctx=None):
+def build_polyhedra(pool: np.ndarray, first: np.ndarray, count: np.ndarray, threads: int = 0, ctx=None,
+                    with_triangles: bool = False):
     """Returns (points (m, 3) f32, hulls (n, 8) u32, topology dict). hulls rows: first vertex (in
     `points`), vertex count, first face, face count, first edge, edge count, ok, 0. With a Context
     `ctx` the clouds are built on its GPU (parrygpu_polyhedra_build_gpu: the same bytes as the host
-    builder), else on `threads` host threads."""
+    builder), else on `threads` host threads. With `with_triangles` the topology dict also holds
+    transformation::convex_hull's triangulation of every cloud: "tri_ranges" (n, 2) = first
+    triangle, count and "triangles" (t, 3) of hull-local vertex ids."""
     from ._capi import lib, check
     pool = np.ascontiguousarray(pool, np.float32).reshape(-1, 3)
     first = np.ascontiguousarray(first, np.uint32)
@@ -27,7 +30,7 @@ def build_polyhedra(pool: np.ndarray, first: np.ndarray, count: np.ndarray, thre
     n = len(first)
     L = lib()
     if ctx is not None:
-        return _build_gpu(ctx, pool, first, count)
+        return _build_gpu(ctx, pool, first, count, with_triangles)
     h = C.c_void_p()
     check(L.parrygpu_polyhedra_build(pool.ctypes.data, first.ctypes.data, count.ctypes.data, n, int(threads), C.byref(h)))
     try:
@@ -43,12 +46,19 @@ def build_polyhedra(pool: np.ndarray, first: np.ndarray, count: np.ndarray, thre
             "vertex_edges": np.zeros(nve, np.uint32), "edge_dirs": np.zeros((ne, 3), np.float32),
         }
         check(L.parrygpu_polyhedra_copy(h, points.ctypes.data, hulls.ctypes.data, *[topo[k].ctypes.data for k in TOPOLOGY_KEYS]))
+        if with_triangles:
+            nt = C.c_uint64()
+            check(L.parrygpu_polyhedra_triangles(h, C.byref(nt), None, None))
+            topo["tri_ranges"] = np.zeros((n, 2), np.uint32)
+            topo["triangles"] = np.zeros((nt.value, 3), np.uint32)
+            check(L.parrygpu_polyhedra_triangles(h, None, topo["tri_ranges"].ctypes.data if n else None,
+                                                 topo["triangles"].ctypes.data if nt.value else None))
     finally:
         L.parrygpu_polyhedra_builder_destroy(h)
     return points, hulls, topo
 
 
-def _build_gpu(ctx, pool, first, count):
+def _build_gpu(ctx, pool, first, count, with_triangles=False):
     from ._capi import lib, check
     L = lib()
     n = len(first)
@@ -70,6 +80,13 @@ def _build_gpu(ctx, pool, first, count):
         }
         ptr = lambda a: C.c_void_p(a.ctypes.data) if a.size else None
         check(L.parrygpu_polyhedra_gpu_copy(ctx.handle, h, ptr(points), ptr(hulls), *[ptr(topo[k]) for k in TOPOLOGY_KEYS]), ctx.handle)
+        if with_triangles:
+            nt = C.c_uint64()
+            check(L.parrygpu_polyhedra_gpu_triangles(ctx.handle, h, C.byref(nt), None, None), ctx.handle)
+            topo["tri_ranges"] = np.zeros((n, 2), np.uint32)
+            topo["triangles"] = np.zeros((nt.value, 3), np.uint32)
+            check(L.parrygpu_polyhedra_gpu_triangles(ctx.handle, h, None, ptr(topo["tri_ranges"]), ptr(topo["triangles"])),
+                  ctx.handle)
     finally:
         L.parrygpu_polyhedra_gpu_destroy(h)
     return points, hulls, topo

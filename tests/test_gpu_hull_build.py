@@ -1,13 +1,25 @@
-"""ConvexPolyhedron::from_convex_hull on the GPU (parrygpu_polyhedra_build_gpu) against the host
-builder: the same bytes for every output array, on ellipsoid clouds of 16-64 and 8-256 points and
-on degenerate clouds (coplanar, collinear, repeated points, cube corners with coplanar faces)."""
+"""ConvexPolyhedron::from_convex_hull on the GPU (parrygpu_polyhedra_build_gpu).
+
+Pinned on the reference: the two clouds of parry's own convex-hull tests
+(crates/parry3d/tests/geometry/convex_hull.rs, fixtures in tests/golden/convex_hull_fixtures.npz)
+and a sample of the measured workload's clouds must give triangulations that the oracle's
+restatement of transformation::check_convex_hull accepts, with every hull vertex a cloud point and
+no cloud point above a hull triangle; the ConvexPolyhedron of clouds in general position passes the
+face checks (points below every face plane, convex counter-clockwise faces, V - E + F = 2). Against
+the host builder: the same bytes for every output array, on ellipsoid clouds of 16-64 and 8-256
+points and on degenerate clouds (coplanar, collinear, repeated points, cube corners with coplanar
+faces)."""
+from pathlib import Path
+
 import numpy as np
 import pytest
 
+from oracle.hull_check import check_convex_hull, check_convex_hulls, polyhedron_properties, triangulation_properties
 from parry_gb300 import workloads as W
 from parry_gb300.polyhedra import build_polyhedra
 
 pytestmark = pytest.mark.gpu
+FIXTURES = Path(__file__).resolve().parent / "golden" / "convex_hull_fixtures.npz"
 
 
 def _special_clouds():
@@ -29,8 +41,8 @@ def test_gpu_build_equals_host_build(gpu_ctx, case):
     else:
         lo, hi = (16, 64) if case == "16-64" else (8, 256)
         cloud, first, count = W.ellipsoid_hulls(20000 if lo == 16 else 3000, 50 + lo, 7, lo, hi)
-    host = build_polyhedra(cloud, first, count)
-    dev = build_polyhedra(cloud, first, count, ctx=gpu_ctx)
+    host = build_polyhedra(cloud, first, count, with_triangles=True)
+    dev = build_polyhedra(cloud, first, count, ctx=gpu_ctx, with_triangles=True)
     np.testing.assert_array_equal(dev[0].view(np.uint32), host[0].view(np.uint32))
     np.testing.assert_array_equal(dev[1], host[1])
     for k in host[2]:
@@ -46,3 +58,36 @@ def test_gpu_build_rejects_out_of_range(gpu_ctx):
     cloud = np.zeros((10, 3), np.float32)
     with pytest.raises(pg.ParryGpuError):
         build_polyhedra(cloud, np.array([5], np.uint32), np.array([8], np.uint32), ctx=gpu_ctx)
+
+
+@pytest.mark.parametrize("name", ["complex", "planar"])
+def test_reference_fixtures_pass_check_convex_hull(gpu_ctx, name):
+    cloud = np.load(FIXTURES)[name]
+    one = np.array([0], np.uint32)
+    points, hulls, topo = build_polyhedra(cloud, one, np.array([len(cloud)], np.uint32), ctx=gpu_ctx, with_triangles=True)
+    assert hulls[0, 6] == 1
+    t0, nt = topo["tri_ranges"][0]
+    tris = topo["triangles"][t0:t0 + nt]
+    check_convex_hull(points[:hulls[0, 1]], tris)
+    assert triangulation_properties(cloud, points[:hulls[0, 1]], tris) == []
+    if name == "planar":
+        assert hulls[0, 3] == 2
+        assert polyhedron_properties(cloud, one, [len(cloud)], points, hulls, topo, [0]) == []
+
+
+def test_workload_sample_passes_check_convex_hull(gpu_ctx):
+    """65,536 clouds of the hull-construction workload (16-64 points on ellipsoids, the bench's
+    generator) and 4,096 of 8-256 points: every triangulation passes check_convex_hull; a subsample
+    also passes the triangulation and ConvexPolyhedron checks."""
+    for n, lo, hi in ((65536, 16, 64), (4096, 8, 256)):
+        cloud, first, count = W.ellipsoid_hulls(n, 66, 7, lo, hi)
+        points, hulls, topo = build_polyhedra(cloud, first, count, ctx=gpu_ctx, with_triangles=True)
+        assert hulls[:, 6].all()
+        ok = check_convex_hulls(points, hulls, topo["tri_ranges"], topo["triangles"])
+        assert ok.all(), f"{int((~ok).sum())} hulls fail check_convex_hull"
+        sub = range(0, n, 257)
+        assert polyhedron_properties(cloud, first, count, points, hulls, topo, sub) == []
+        for h in sub:
+            t0, nt = topo["tri_ranges"][h]
+            p = points[hulls[h, 0]:hulls[h, 0] + hulls[h, 1]]
+            assert triangulation_properties(cloud[first[h]:first[h] + count[h]], p, topo["triangles"][t0:t0 + nt]) == []
