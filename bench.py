@@ -39,7 +39,10 @@ WORKLOAD = "terrain_trimesh_rays"
 def config(world: int, n_rays: int) -> dict:
     return {"workload": WORKLOAD, "triangles": 65536, "grid": "256x128", "rays": n_rays, "max_toi": MAX_TOI,
             "solid": True, "ray_dirs": "uniform downward hemisphere", "l2": "flushed before each step (256 MiB write)",
-            "parallelism": f"replicas{world}"}
+            "parallelism": f"shards{world}" if world > 1 else "single",
+            "sharding": "one batch of rays_per_rank x ranks rays, each rank casting its contiguous range against its "
+                        "replica of the mesh (no data exchange)" if world > 1 else None,
+            "rays_per_rank": n_rays}
 
 
 def reduce_max(x: float, world: int) -> float:
@@ -1004,7 +1007,11 @@ def run_gb300(args) -> int:
 
     n = args.n_rays
     v, i = W.terrain_mesh()
-    rays_h = W.terrain_rays(n)
+    # one batch of world x n rays; this rank casts its contiguous range (parry_gb300.sharding), the
+    # mesh and BVH replicated on every rank
+    from parry_gb300 import sharding
+    r0, r1 = sharding.ray_ranges(n * world, world)[rank]
+    rays_h = W.terrain_rays(n * world)[r0:r1] if world > 1 else W.terrain_rays(n)
     fixed = args.ray_sort is not None
     ctx = pg.Context(device=local, sort_rays=fixed and args.ray_sort >= 0, ray_sort_key=max(args.ray_sort or 0, 0))
     # One explicit stream shared by the library and the timing events (torch's default stream
