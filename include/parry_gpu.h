@@ -71,6 +71,14 @@ typedef struct parrygpu_config {
                               copies, as ray_chunks says; 0 = library default: in place when the
                               device's host link is coherent (it reads host memory through the
                               host's page tables), else staged. Other host buffers are staged. */
+  uint32_t contact_warp_cost; /* query::contact on more than 4096 pairs: pairs whose support-scan cost
+                              (vertices one support evaluation scans, summed over the two shapes, at
+                              most 1023) is at least this run one warp per pair, hulls staged in shared
+                              memory; 0 = library default; 1024 or more = never (one thread per pair) */
+  uint32_t contact_epa_inline; /* query::contact: 1 = a pair's EPA runs in the same thread right after its
+                              GJK (one workspace slot per thread of the persistent grid); 2 = through a
+                              queue, in a second persistent pass over the pairs that reach EPA; 0 =
+                              library default (2) */
 } parrygpu_config;
 
 /* ---- context ---------------------------------------------------------------------------- */
@@ -548,7 +556,9 @@ parrygpu_status parrygpu_get_config(const parrygpu_ctx* ctx, parrygpu_config* ou
 parrygpu_status parrygpu_autotune_trimesh_rays(parrygpu_ctx* ctx, const parrygpu_trimesh* mesh, const float* pose7, const float* rays,
                                                uint32_t n, float max_toi, uint32_t reps, parrygpu_config* chosen);
 /* Times parrygpu_contacts on (shapes, pairs) for each EPA residency (4, 6, 8, 12, 16 blocks per
- * SM), `reps` timed runs each (0 = 2), and keeps the fastest as for the ray tuner. */
+ * SM, one thread per pair, EPA through the queue), then at the best residency with the pairs of cost
+ * 512 or more, then 256 or more, one warp each, and with EPA right after GJK in the same thread;
+ * `reps` timed runs each (0 = 2); keeps the fastest as for the ray tuner. */
 parrygpu_status parrygpu_autotune_contacts(parrygpu_ctx* ctx, const parrygpu_shapes* shapes, const uint32_t* pairs, uint64_t n_pairs,
                                            float prediction, uint32_t reps, parrygpu_config* chosen);
 

@@ -78,7 +78,8 @@ def _alloc_like(ref, shape, dtype):
 def _config_dict(cfg) -> dict:
     return {"device": cfg.device, "ray_block": cfg.ray_block, "sort_rays": bool(cfg.sort_rays), "ray_sort_key": cfg.ray_sort_key,
             "epa_blocks_per_sm": cfg.epa_blocks_per_sm, "ray_traversal": cfg.ray_traversal, "ray_refill": cfg.ray_refill, "ray_chunks": cfg.ray_chunks,
-            "ray_host_access": cfg.ray_host_access}
+            "ray_host_access": cfg.ray_host_access, "contact_warp_cost": cfg.contact_warp_cost,
+            "contact_epa_inline": cfg.contact_epa_inline}
 
 
 class Context:
@@ -86,7 +87,7 @@ class Context:
 
     def __init__(self, device: int = 0, ray_block: int = 0, sort_rays: bool = True, ray_sort_key: int = 0,
                  epa_blocks_per_sm: int = 0, ray_traversal: int = 0, ray_refill: int = 0, ray_chunks: int = 0,
-                 ray_host_access: int = 0):
+                 ray_host_access: int = 0, contact_warp_cost: int = 0, contact_epa_inline: int = 0):
         cfg = _capi.ParryGpuConfig()
         lib().parrygpu_default_config(C.byref(cfg))
         cfg.device = device
@@ -98,6 +99,8 @@ class Context:
         cfg.ray_refill = ray_refill
         cfg.ray_chunks = ray_chunks
         cfg.ray_host_access = ray_host_access
+        cfg.contact_warp_cost = contact_warp_cost
+        cfg.contact_epa_inline = contact_epa_inline
         h = C.c_void_p()
         check(lib().parrygpu_create(C.byref(h), C.byref(cfg)))
         self._h = h
@@ -545,8 +548,9 @@ def cast_shapes(ctx: Context, shapes, pairs, velocities, max_toi: float = float(
 
 
 def autotune_contacts(ctx: Context, shapes, pairs, prediction: float = 0.0, reps: int = 2) -> dict:
-    """Times contacts(shapes, pairs, prediction) for each EPA residency and keeps the fastest in the
-    context's configuration; returns the chosen configuration."""
+    """Times contacts(shapes, pairs, prediction) for each EPA residency, then with the dearest pairs
+    one warp each and with EPA inline, and keeps the fastest in the context's configuration; returns
+    the chosen configuration."""
     st = _StagedShapes(shapes)
     kp, pp = _as_input(pairs, np.uint32)
     cfg = _capi.ParryGpuConfig()

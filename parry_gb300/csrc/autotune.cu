@@ -129,15 +129,28 @@ parrygpu_status parrygpu_autotune_contacts(parrygpu_ctx* ctx, const parrygpu_sha
   parrygpu_config best = saved;
   float best_ms = -1.0f;
   parrygpu_status s = PARRYGPU_OK;
-  for (uint32_t blocks : EPA_CANDIDATES) {
-    ctx->cfg.epa_blocks_per_sm = blocks;
+  auto trial = [&]() -> parrygpu_status {
     float ms = 0.0f;
-    s = time_runs(ctx, reps, [&]() {
+    parrygpu_status st = time_runs(ctx, reps, [&]() {
       return parrygpu_contacts(ctx, shapes, d_pairs.as<uint32_t>(), n_pairs, prediction, nullptr, d_out.as<parrygpu_contact>(),
                                d_has.as<uint8_t>(), nullptr);
     }, &ms);
-    if (s != PARRYGPU_OK) break;
-    if (best_ms < 0.0f || ms < best_ms) { best_ms = ms; best = ctx->cfg; }
+    if (st == PARRYGPU_OK && (best_ms < 0.0f || ms < best_ms)) { best_ms = ms; best = ctx->cfg; }
+    return st;
+  };
+  // one thread per pair, EPA through the queue: each EPA residency
+  ctx->cfg.contact_warp_cost = 1024;
+  ctx->cfg.contact_epa_inline = 2;
+  for (uint32_t blocks : EPA_CANDIDATES) {
+    ctx->cfg.epa_blocks_per_sm = blocks;
+    if ((s = trial()) != PARRYGPU_OK) break;
+  }
+  // then, at the best residency, the dearest pairs one warp each, and EPA right after GJK
+  for (uint32_t variant = 0; variant < 3 && s == PARRYGPU_OK; ++variant) {
+    ctx->cfg = best;
+    if (variant < 2) ctx->cfg.contact_warp_cost = variant == 0 ? 512 : 256;
+    else ctx->cfg.contact_epa_inline = 1;
+    s = trial();
   }
   cudaError_t se = cudaStreamSynchronize(ctx->stream);
   release();

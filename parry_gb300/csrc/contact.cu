@@ -2,23 +2,35 @@
 // and per-shape AABBs.
 //
 // Pipeline (one stream, no host round trip):
-//   k_contacts_main  one thread per pair: dispatch of DefaultQueryDispatcher::contact
-//                    (src/query/default_query_dispatcher.rs:302-356): ball-ball analytic, ball-convex
-//                    by point projection, otherwise GJK (gjk_device.cuh). Pairs whose GJK ends inside
-//                    the Minkowski difference append (pair, final simplex) to an EPA queue.
+//   k_pair_cost_keys + radix sort   pairs binned by support-scan cost (vertices one support
+//                    evaluation scans), ascending.
+//   k_contacts_fused one persistent launch over work items taken from an atomic counter:
+//                    - the pairs at the top of the cost order (cost >= the configured threshold), one
+//                      warp per pair, dearest first: both hulls staged into shared memory by the TMA
+//                      unit (cp.async.bulk), support points by a lane-parallel scan reduced with warp
+//                      shuffles (first index on ties), GJK and then EPA with the polytope in the warp's
+//                      shared memory (a polytope that outgrows it goes to the per-thread EPA pass);
+//                    - then the others, 32 consecutive pairs per item, one thread per pair: dispatch
+//                      of DefaultQueryDispatcher::contact (src/query/default_query_dispatcher.rs:
+//                      302-356): ball-ball analytic, ball-convex by point projection, otherwise GJK
+//                      (gjk_device.cuh). Pairs whose GJK ends inside the Minkowski difference append
+//                      (pair, final simplex) to an EPA queue.
 //   k_contacts_epa   persistent grid-stride loop over the EPA queue, one polytope workspace slot per
 //                    thread (epa_device.cuh), finishing those pairs exactly as the reference does.
-// Results are written in world space (contact_shape_shape.rs:123-138).
+// Every path runs the reference's steps in the same order on the same values, so the answers do not
+// depend on which path a pair takes. Results are written in world space (contact_shape_shape.rs:
+// 123-138).
 #include "internal.hpp"
 #include "epa_device.cuh"
 #include "contact_device.cuh"
+#include "bulk_copy.cuh"
+#include <algorithm>
 #include <cstring>
 
 using namespace pg;
 
 namespace {
 
-constexpr int CT_THREADS = 128;
 constexpr int EPA_THREADS = 64;
 
 struct ContactOut {
@@ -149,22 +161,95 @@ __global__ void k_pair_cost_keys(ShapeArrays sh, const uint32_t* __restrict__ pa
   vals[i] = i;
 }
 
-// Thread i handles pair order[i] (order = NULL: pair i).
-__global__ void __launch_bounds__(CT_THREADS) k_contacts_main(ShapeArrays sh, const uint32_t* __restrict__ pairs, uint64_t n,
-                                                              const uint32_t* __restrict__ order, float prediction,
-                                                              const float* __restrict__ init_dirs, float* __restrict__ out,
-                                                              uint8_t* __restrict__ has, uint32_t* __restrict__ queue,
-                                                              unsigned long long* __restrict__ qcount, unsigned long long* __restrict__ stats,
-                                                              uint32_t* __restrict__ err, float* __restrict__ final_dirs) {
-  uint64_t k = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
-  if (order && k < n) k = order[k];
+// EPA for pair k from GJK's final simplex s, finishing query::contact as the reference does (the
+// support-map pair's closest points, or the projection of a ball's centre onto a convex shape).
+// Returns EPA_OVERFLOW when the workspace is too small (nothing written, *iters unchanged), else
+// writes the pair's result.
+template <class WS>
+__device__ __forceinline__ int epa_pair(const WS& ws, const PairSetup& ps, uint64_t k, const Simplex& s, float prediction,
+                                        float* __restrict__ out, uint8_t* __restrict__ has, float* __restrict__ final_dirs,
+                                        uint32_t* iters) {
+  ContactOut c;
+  bool ok = false;
+  V3 p1, p2, nn;
+  uint32_t it = 0;
+  int r;
+  if (ps.path == PATH_SUPPORT) {
+    r = epa_closest_points(ws, ps.pos12, ps.s1, ps.s2, s, &p1, &p2, &nn, &it);
+    if (r == EPA_OVERFLOW) return r;
+    if (r == EPA_OK) { ok = true; finish_support_pair(ps.pos12, p1, p2, nn, &c); }
+    if (final_dirs) {
+      V3 fd = r == EPA_OK ? nn : v3(1.f, 0.f, 0.f);  // GJKResult::NoIntersection(x) when EPA fails
+      final_dirs[3 * k] = fd.x; final_dirs[3 * k + 1] = fd.y; final_dirs[3 * k + 2] = fd.z;
+    }
+  } else {
+    const ShapeDev& cs = *ps.convex;
+    V3 center = ps.cpos.t;
+    Pose m{0.f, 0.f, 0.f, 1.f, -center};
+    Pose minv = pose_inverse(m);
+    ShapeDev origin;
+    origin.type = SH_ORIGIN;
+    PointProj proj;
+    proj.face = -1;
+    proj.inside = true;
+    r = epa_closest_points(ws, minv, cs, origin, s, &p1, &p2, &nn, &it);
+    if (r == EPA_OVERFLOW) return r;
+    proj.point = r == EPA_OK ? p1 : center;
+    ok = finish_convex_ball(ps.cpos, cs, proj, ps.radius, prediction, &c);
+    if (ok && ps.path == PATH_BALL_FIRST) flip(&c);
+  }
+  *iters += it;
+  write_out(out, has, k, ok, c, ps.pa, ps.pb);
+  return r;
+}
+
+// Where a pair's EPA goes once its GJK ends inside the Minkowski difference: the queue of the
+// per-thread EPA pass (ws = NULL), or this thread's own workspace slot right away (ws set: the
+// hulls GJK just read are still in cache), a polytope outgrowing that slot going to the
+// large-slot pass through the overflow list.
+struct LaneEpa {
+  const EpaWs* ws;
+  uint32_t* ovf;
+  unsigned long long* ovf_count;
+  uint32_t iters = 0, calls = 0;
+};
+
+__device__ __forceinline__ void lane_epa(LaneEpa& le, const PairSetup& ps, uint64_t k, const Simplex& s, float prediction,
+                                         float* __restrict__ out, uint8_t* __restrict__ has, float* __restrict__ final_dirs,
+                                         uint32_t* __restrict__ queue, unsigned long long* __restrict__ qcount) {
+  if (!le.ws) { enqueue(queue, qcount, k, s); return; }
+  if (epa_pair(*le.ws, ps, k, s, prediction, out, has, final_dirs, &le.iters) == EPA_OVERFLOW) {
+    const unsigned long long e = atomicAdd(qcount, 1ull);
+    uint32_t* q = queue + (size_t)e * QUEUE_WORDS;
+    q[0] = (uint32_t)k;
+    q[QUEUE_WORDS - 1] = 0;
+    q[1] = (uint32_t)s.dim;
+    for (int i = 0; i <= s.dim; ++i) {
+      float* f = reinterpret_cast<float*>(q + 2 + 9 * i);
+      f[0] = s.v[i].p.x; f[1] = s.v[i].p.y; f[2] = s.v[i].p.z;
+      f[3] = s.v[i].o1.x; f[4] = s.v[i].o1.y; f[5] = s.v[i].o1.z;
+      f[6] = s.v[i].o2.x; f[7] = s.v[i].o2.y; f[8] = s.v[i].o2.z;
+    }
+    le.ovf[atomicAdd(le.ovf_count, 1ull)] = (uint32_t)e;
+    return;
+  }
+  le.calls++;
+}
+
+// query::contact for pair k on this thread alone (EPA as `le` says). Adds its GJK support
+// evaluations to *iters.
+__device__ __forceinline__ void contact_pair_lane(const ShapeArrays& sh, const uint32_t* __restrict__ pairs, uint64_t k, float prediction,
+                                                  const float* __restrict__ init_dirs, float* __restrict__ out, uint8_t* __restrict__ has,
+                                                  uint32_t* __restrict__ queue, unsigned long long* __restrict__ qcount,
+                                                  uint32_t* __restrict__ err, float* __restrict__ final_dirs, uint32_t* iters_out,
+                                                  LaneEpa& le) {
   uint32_t iters = 0;
-  if (k < n && !valid_pair(sh, pairs[2 * k], pairs[2 * k + 1])) {
+  if (!valid_pair(sh, pairs[2 * k], pairs[2 * k + 1])) {
     atomicOr(err, ERR_CAPACITY);
     float* o = out + 13 * k;
     for (int j = 0; j < 13; ++j) o[j] = 0.0f;
     has[k] = 0;
-  } else if (k < n) {
+  } else {
     PairSetup ps;
     setup_pair(sh, pairs[2 * k], pairs[2 * k + 1], &ps);
     ContactOut c;
@@ -194,7 +279,7 @@ __global__ void __launch_bounds__(CT_THREADS) k_contacts_main(ShapeArrays sh, co
           proj.point = g.p1;
           proj.face = -1;
         } else {
-          enqueue(queue, qcount, k, s);
+          lane_epa(le, ps, k, s, prediction, out, has, final_dirs, queue, qcount);
           done = false;
         }
       }
@@ -213,7 +298,7 @@ __global__ void __launch_bounds__(CT_THREADS) k_contacts_main(ShapeArrays sh, co
         ok = true;
         finish_support_pair(ps.pos12, g.p1, g.p2, g.dir, &c);
       } else if (g.kind == GJK_INTERSECTION) {
-        enqueue(queue, qcount, k, s);
+        lane_epa(le, ps, k, s, prediction, out, has, final_dirs, queue, qcount);
         done = false;
       }
       if (final_dirs && g.kind != GJK_INTERSECTION) {
@@ -225,9 +310,239 @@ __global__ void __launch_bounds__(CT_THREADS) k_contacts_main(ShapeArrays sh, co
     }
     if (done) write_out(out, has, k, ok, c, ps.pa, ps.pb);
   }
+  *iters_out += iters;
+}
+
+// ---- one warp per pair ----
+
+// point_cloud_support_point (src/utils/point_cloud_support_point.rs:5-19) with the warp's 32 lanes:
+// lane l scans vertices l, l + 32, ... keeping the first index of its largest dot product (NaN
+// products never count), and a shuffle reduction keeps the largest value, then the smallest index.
+// That is the sequential scan's answer (best = 0, then strict `>`), whose seed only matters when
+// vertex 0's product is NaN: then nothing replaces it. Every lane returns the same vertex.
+__device__ __forceinline__ V3 warp_convex_support(const float* pts, uint32_t n, V3 dir) {
+  const uint32_t lane = threadIdx.x & 31;
+  float bd = 0.0f;
+  uint32_t bi = 0xffffffffu;
+  bool nan0 = false;  // vertex 0's product is NaN (lane 0 scans vertex 0)
+  for (uint32_t i = lane; i < n; i += 32) {
+    const float d = dot(v3(pts[3 * i], pts[3 * i + 1], pts[3 * i + 2]), dir);
+    if (i == 0 && d != d) nan0 = true;
+    if (bi == 0xffffffffu ? !(d != d) : d > bd) { bd = d; bi = i; }
+  }
+  nan0 = __shfl_sync(0xffffffffu, nan0, 0);
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+    const float od = __shfl_xor_sync(0xffffffffu, bd, off);
+    const uint32_t oi = __shfl_xor_sync(0xffffffffu, bi, off);
+    if (oi != 0xffffffffu && (bi == 0xffffffffu || od > bd || (od == bd && oi < bi))) { bd = od; bi = oi; }
+  }
+  if (nan0 || bi == 0xffffffffu) bi = 0;
+  return v3(pts[3 * bi], pts[3 * bi + 1], pts[3 * bi + 2]);
+}
+
+__device__ __forceinline__ V3 warp_local_support(const ShapeDev& s, V3 dir) {
+  return s.type == SH_CONVEX ? warp_convex_support(s.pts, s.npts, dir) : local_support(s, dir);
+}
+
+// Polytope of one warp-per-pair EPA in shared memory: 64 vertices, 256 faces (24-byte records),
+// silhouettes of 32 edges, a walk stack of 128 (an EPA call that outgrows it finishes in the
+// per-thread pass).
+using EpaSmemLayout = EpaLayout<64, 256, 32, 128, 6>;
+using EpaWsSmem = EpaWsT<EpaSmemLayout>;
+// Hull vertices staged per shape (larger hulls are scanned where they lie in global memory); 4
+// spare floats absorb the shift that keeps the bulk-copied body 16-byte aligned.
+constexpr uint32_t STAGE_VERTS = 256;
+constexpr uint32_t STAGE_FLOATS = 3 * STAGE_VERTS + 4;
+constexpr int FUSED_WARPS = 4;
+constexpr int FUSED_THREADS = 32 * FUSED_WARPS;
+constexpr uint32_t MBAR_WAIT_POLLS = 1u << 24;
+
+struct __align__(16) WarpSmem {
+  uint32_t epa[EpaSmemLayout::WORDS];
+  float hull[2][STAGE_FLOATS];
+  uint64_t bar;
+  uint64_t pad;
+};
+static_assert(sizeof(WarpSmem) % 16 == 0 && (EpaSmemLayout::WORDS * 4) % 16 == 0 && (STAGE_FLOATS * 4) % 16 == 0,
+              "16-byte aligned shared-memory regions");
+
+// Stages shape s's vertices into `dst` (16-byte aligned) when it is a convex polyhedron of at most
+// STAGE_VERTS vertices: the 16-byte-aligned body of its byte range by one bulk copy issued by lane 0
+// (bytes added to *tx), the ragged head and tail (at most 3 floats each) by plain loads of lanes
+// 0-5. Points s.pts at the staged copy. Returns false (nothing staged) otherwise.
+__device__ __forceinline__ bool stage_hull(ShapeDev& s, float* dst, uint64_t* bar, uint32_t* tx) {
+  if (s.type != SH_CONVEX || s.npts > STAGE_VERTS || s.npts == 0) return false;
+  const uint32_t lane = threadIdx.x & 31;
+  const uintptr_t start = reinterpret_cast<uintptr_t>(s.pts), end = start + 12u * (uintptr_t)s.npts;
+  const uintptr_t base = start & ~(uintptr_t)15;         // dst[0] mirrors this address
+  const uintptr_t b0 = (start + 15) & ~(uintptr_t)15, b1 = end & ~(uintptr_t)15;
+  float* vdst = dst + (start - base) / 4;                 // where vertex 0 lands
+  if (b1 > b0) {
+    if (lane == 0) {
+      const uint32_t bytes = (uint32_t)(b1 - b0);
+      bulk_copy_g2s(dst + (b0 - base) / 4, reinterpret_cast<const void*>(b0), bytes, bar);
+      *tx += bytes;
+    }
+    const uint32_t head = (uint32_t)(b0 - start) / 4, tail = (uint32_t)(end - b1) / 4;
+    if (lane < head) vdst[lane] = s.pts[lane];
+    else if (lane >= 8 && lane < 8 + tail) {
+      const uint32_t j = (uint32_t)(b1 - start) / 4 + (lane - 8);
+      vdst[j] = s.pts[j];
+    }
+  } else {
+    for (uint32_t j = lane; j < 3 * s.npts; j += 32) vdst[j] = s.pts[j];
+  }
+  s.pts = vdst;
+  return true;
+}
+
+// query::contact for pair k (a PATH_SUPPORT pair) with the whole warp; every lane runs the
+// reference's steps on the same values (uniform control flow), the support scans lane-parallel.
+// Returns false when the staging wait timed out (the warp must stop).
+__device__ bool contact_pair_warp(const PairSetup& ps0, uint64_t k, float prediction, const float* __restrict__ init_dirs,
+                                  float* __restrict__ out, uint8_t* __restrict__ has, uint32_t* __restrict__ queue,
+                                  unsigned long long* __restrict__ qcount, uint32_t* __restrict__ err, float* __restrict__ final_dirs,
+                                  WarpSmem* w, uint32_t* phase, uint32_t* gjk_iters, uint32_t* epa_iters, uint32_t* epa_calls) {
+  const uint32_t lane = threadIdx.x & 31;
+  PairSetup ps = ps0;
+  // the previous pair's reads of the staging buffers are over before the bulk copies refill them
+  __syncwarp();
+  fence_async_shared();
+  uint32_t tx = 0;
+  stage_hull(ps.s1, w->hull[0], &w->bar, &tx);
+  stage_hull(ps.s2, w->hull[1], &w->bar, &tx);
+  // the phase's one arrival, with the bytes the copies will complete (the phase cannot complete
+  // before this arrival, so copies issued first are counted)
+  if (lane == 0) mbar_arrive_expect_tx(&w->bar, tx);
+  if (!mbar_wait_bounded(&w->bar, *phase, MBAR_WAIT_POLLS)) {
+    if (lane == 0) atomicOr(err, ERR_TIMEOUT);
+    mbar_wait_bounded(&w->bar, *phase, MBAR_WAIT_POLLS);  // the copies in flight, once more, before the warp leaves
+    return false;
+  }
+  *phase ^= 1u;
+  __syncwarp();  // the lanes' ragged stores are visible to the whole warp
+  const ShapeDev& g1 = ps.s1;
+  const ShapeDev& g2 = ps.s2;
+  const Pose pos12 = ps.pos12;
+  auto sup = [&](V3 d) {
+    const V3 sp1 = warp_local_support(g1, d);
+    const V3 sp2 = pose_point(pos12, warp_local_support(g2, pose_inv_rotate(pos12, -d)));
+    return CSO{sp1 - sp2, sp1, sp2};
+  };
+  V3 dir;
+  if (init_dirs) dir = v3(init_dirs[3 * k], init_dirs[3 * k + 1], init_dirs[3 * k + 2]);
+  else if (!try_normalize(pos12.t, EPS, &dir)) dir = v3(1.f, 0.f, 0.f);
+  Simplex s;
+  simplex_reset(s, sup(dir));
+  uint32_t gi = 0;
+  const GjkOut g = gjk_closest_points_t(sup, prediction, s, &gi);
+  ContactOut c;
+  bool ok = false, done = true;
+  V3 fd = g.dir;
+  uint32_t ei = 0, calls = 0;
+  if (g.kind == GJK_CLOSEST) {
+    ok = true;
+    finish_support_pair(pos12, g.p1, g.p2, g.dir, &c);
+  } else if (g.kind == GJK_INTERSECTION) {
+    EpaWsSmem ws{w->epa};
+    V3 p1, p2, nn;
+    const int r = epa_closest_points_t(ws, sup, s, &p1, &p2, &nn, &ei);
+    if (r == EPA_OVERFLOW) {  // the per-thread EPA pass redoes this pair from GJK's simplex
+      if (lane == 0) enqueue(queue, qcount, k, s);
+      done = false;
+      ei = 0;
+    } else {
+      calls = 1;
+      if (r == EPA_OK) { ok = true; finish_support_pair(pos12, p1, p2, nn, &c); }
+      fd = r == EPA_OK ? nn : v3(1.f, 0.f, 0.f);  // GJKResult::NoIntersection(x) when EPA fails
+    }
+  }
+  if (lane == 0) {
+    if (final_dirs && done) { final_dirs[3 * k] = fd.x; final_dirs[3 * k + 1] = fd.y; final_dirs[3 * k + 2] = fd.z; }
+    if (done) write_out(out, has, k, ok, c, ps.pa, ps.pb);
+    *gjk_iters += gi;
+    *epa_iters += ei;
+    *epa_calls += calls;
+  }
+  return true;
+}
+
+// Largest pair count n_large such that the last n_large pairs of the ascending cost order cost at
+// least `threshold` (one thread, binary search over the sorted keys).
+__global__ void k_count_costly(const uint32_t* __restrict__ sorted_keys, uint32_t n, uint32_t threshold, unsigned long long* __restrict__ out) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  uint32_t lo = 0, hi = n;
+  while (lo < hi) {
+    const uint32_t mid = lo + (hi - lo) / 2;
+    if (sorted_keys[mid] < threshold) lo = mid + 1; else hi = mid;
+  }
+  *out = n - lo;
+}
+
+// The persistent launch: item i < *n_large is the pair order[n - 1 - i] for one warp; the items after
+// it are runs of 32 pairs of order[0 ..) (order = NULL: pairs in input order), one per lane.
+// INLINE: per-thread pairs run EPA in their thread's own workspace slot of ws_pool right after GJK
+// (else through the queue).
+template <bool INLINE>
+__global__ void __launch_bounds__(FUSED_THREADS, 3) k_contacts_fused(ShapeArrays sh, const uint32_t* __restrict__ pairs, uint64_t n,
+                                                                  const uint32_t* __restrict__ order,
+                                                                  const unsigned long long* __restrict__ n_large_ptr, float prediction,
+                                                                  const float* __restrict__ init_dirs, float* __restrict__ out,
+                                                                  uint8_t* __restrict__ has, uint32_t* __restrict__ queue,
+                                                                  unsigned long long* __restrict__ qcount, unsigned long long* __restrict__ stats,
+                                                                  uint32_t* __restrict__ err, float* __restrict__ final_dirs,
+                                                                  unsigned long long* __restrict__ work, uint32_t* __restrict__ ws_pool,
+                                                                  uint32_t* __restrict__ ovf, unsigned long long* __restrict__ ovf_count) {
+  extern __shared__ __align__(16) unsigned char fused_smem[];
+  WarpSmem* w = reinterpret_cast<WarpSmem*>(fused_smem) + (threadIdx.x >> 5);
+  const uint32_t lane = threadIdx.x & 31;
+  const EpaWs slot = epa_slot(ws_pool, blockIdx.x * blockDim.x + threadIdx.x);
+  LaneEpa le{INLINE ? &slot : nullptr, ovf, ovf_count};
+  const uint64_t n_large = order ? *n_large_ptr : 0;
+  const uint64_t n_small = n - n_large;
+  if (n_large && lane == 0) mbar_init(&w->bar, 1);
+  __syncwarp();
+  uint32_t phase = 0, gjk_iters = 0, epa_iters = 0, epa_calls = 0;
+  for (;;) {
+    unsigned long long item = 0;
+    if (lane == 0) item = atomicAdd(work, 1ull);
+    item = __shfl_sync(0xffffffffu, item, 0);
+    if (item < n_large) {
+      const uint64_t k = order[n - 1 - item];
+      const uint32_t a = pairs[2 * k], b = pairs[2 * k + 1];
+      bool warp_path = valid_pair(sh, a, b);
+      PairSetup ps;
+      if (warp_path) {
+        setup_pair(sh, a, b, &ps);
+        warp_path = ps.path == PATH_SUPPORT;
+      }
+      if (!warp_path) {  // a ball pair or an invalid one: the per-thread code on lane 0
+        if (lane == 0) contact_pair_lane(sh, pairs, k, prediction, init_dirs, out, has, queue, qcount, err, final_dirs, &gjk_iters, le);
+        __syncwarp();
+        continue;
+      }
+      if (!contact_pair_warp(ps, k, prediction, init_dirs, out, has, queue, qcount, err, final_dirs, w, &phase, &gjk_iters,
+                             &epa_iters, &epa_calls))
+        break;
+      continue;
+    }
+    const unsigned long long base = (item - n_large) * 32ull;
+    if (base >= n_small) break;
+    const uint64_t idx = base + lane;
+    if (idx < n_small)
+      contact_pair_lane(sh, pairs, order ? order[idx] : idx, prediction, init_dirs, out, has, queue, qcount, err, final_dirs, &gjk_iters,
+                        le);
+  }
   if (stats) {
-    uint32_t w = __reduce_add_sync(0xffffffffu, iters);
-    if ((threadIdx.x & 31) == 0 && w) atomicAdd(&stats[0], (unsigned long long)w);
+    const uint32_t g = __reduce_add_sync(0xffffffffu, gjk_iters);
+    const uint32_t e = __reduce_add_sync(0xffffffffu, epa_iters + le.iters);
+    const uint32_t c = __reduce_add_sync(0xffffffffu, epa_calls + le.calls);
+    if (lane == 0) {
+      if (g) atomicAdd(&stats[0], (unsigned long long)g);
+      if (e) atomicAdd(&stats[1], (unsigned long long)e);
+      if (c) atomicAdd(&stats[2], (unsigned long long)c);
+    }
   }
 }
 
@@ -235,8 +550,10 @@ __global__ void __launch_bounds__(CT_THREADS) k_contacts_main(ShapeArrays sh, co
 // polytope outgrows the regular slot is appended to `ovf` (its result left to the second pass).
 // Second pass (BIG = true): the entries listed in `ovf` [0, *qcount), on large slots; a pair that
 // outgrows those raises the capacity error.
-template <bool BIG>
-__global__ void __launch_bounds__(EPA_THREADS) k_contacts_epa(ShapeArrays sh, const uint32_t* __restrict__ pairs, float prediction,
+// MINB: resident blocks per SM the registers are budgeted for (8: the compiler's choice, about 126
+// registers; 12 or 16: at most 85 or 64 registers, more warps to hide memory latency).
+template <bool BIG, int MINB = 8>
+__global__ void __launch_bounds__(EPA_THREADS, MINB) k_contacts_epa(ShapeArrays sh, const uint32_t* __restrict__ pairs, float prediction,
                                                               float* __restrict__ out, uint8_t* __restrict__ has,
                                                               const uint32_t* __restrict__ queue, const unsigned long long* __restrict__ qcount,
                                                               uint32_t* __restrict__ ws_pool, unsigned long long* __restrict__ stats,
@@ -259,44 +576,13 @@ __global__ void __launch_bounds__(EPA_THREADS) k_contacts_epa(ShapeArrays sh, co
     }
     PairSetup ps;
     setup_pair(sh, pairs[2 * k], pairs[2 * k + 1], &ps);
-    ContactOut c;
-    bool ok = false;
-    V3 p1, p2, nn;
-    const uint32_t iters0 = iters;
-    // a pair outgrowing the regular slot goes to the second pass: counted there, results written there
-    auto outgrown = [&](int r) {
-      if (r != EPA_OVERFLOW) return false;
-      if (BIG) { atomicOr(err, ERR_POLYTOPE_FULL); return false; }
-      ovf[atomicAdd(ovf_count, 1ull)] = (uint32_t)e;
-      iters = iters0;
-      return true;
-    };
-    if (ps.path == PATH_SUPPORT) {
-      int r = epa_closest_points(ws, ps.pos12, ps.s1, ps.s2, s, &p1, &p2, &nn, &iters);
-      if (outgrown(r)) continue;
-      if (r == EPA_OK) { ok = true; finish_support_pair(ps.pos12, p1, p2, nn, &c); }
-      if (final_dirs) {
-        V3 fd = r == EPA_OK ? nn : v3(1.f, 0.f, 0.f);  // GJKResult::NoIntersection(x) when EPA fails
-        final_dirs[3 * k] = fd.x; final_dirs[3 * k + 1] = fd.y; final_dirs[3 * k + 2] = fd.z;
-      }
-    } else {
-      const ShapeDev& cs = *ps.convex;
-      V3 center = ps.cpos.t;
-      Pose m{0.f, 0.f, 0.f, 1.f, -center};
-      Pose minv = pose_inverse(m);
-      ShapeDev origin;
-      origin.type = SH_ORIGIN;
-      PointProj proj;
-      proj.face = -1;
-      proj.inside = true;
-      int r = epa_closest_points(ws, minv, cs, origin, s, &p1, &p2, &nn, &iters);
-      if (outgrown(r)) continue;
-      proj.point = r == EPA_OK ? p1 : center;
-      ok = finish_convex_ball(ps.cpos, cs, proj, ps.radius, prediction, &c);
-      if (ok && ps.path == PATH_BALL_FIRST) flip(&c);
+    const int r = epa_pair(ws, ps, k, s, prediction, out, has, final_dirs, &iters);
+    if (r == EPA_OVERFLOW) {  // the second pass counts and writes this pair
+      if (BIG) atomicOr(err, ERR_POLYTOPE_FULL);
+      else ovf[atomicAdd(ovf_count, 1ull)] = (uint32_t)e;
+      continue;
     }
     calls++;
-    write_out(out, has, k, ok, c, ps.pa, ps.pb);
   }
   if (stats) {
     uint32_t w = __reduce_add_sync(0xffffffffu, iters);
@@ -327,6 +613,32 @@ __global__ void k_shape_aabbs(ShapeArrays sh, uint64_t n, float margin, float* _
   }
   float* o = out + 6 * i;
   o[0] = mn.x; o[1] = mn.y; o[2] = mn.z; o[3] = mx.x; o[4] = mx.y; o[5] = mx.z;
+}
+
+// Pairs cost at least this (vertices per support evaluation, two shapes) run one warp per pair
+// unless the context's configuration says otherwise.
+constexpr uint32_t DEFAULT_CONTACT_WARP_COST = 1024;
+
+// k_contacts_fused on a persistent grid: as many blocks as fit on every SM with `smem` bytes of
+// shared memory each.
+// With inline EPA the context's EPA workspace pool is grown to one slot per thread of the grid.
+parrygpu_status launch_fused(parrygpu_ctx* ctx, size_t smem, bool inline_epa, const ShapeArrays& sh, const uint32_t* pairs, uint64_t n,
+                             const uint32_t* order, const unsigned long long* n_large, float prediction, const float* init_dirs, float* out,
+                             uint8_t* has, uint32_t* queue, unsigned long long* qcount, unsigned long long* stats, float* final_dirs,
+                             unsigned long long* work, uint32_t* ovf, unsigned long long* ovf_count) {
+  auto kern = inline_epa ? k_contacts_fused<true> : k_contacts_fused<false>;
+  if (smem > 48 * 1024) PG_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  int per_sm = 0;
+  PG_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, FUSED_THREADS, smem));
+  if (per_sm < 1) return set_error(ctx, PARRYGPU_CUDA_ERROR, "the fused contact kernel does not fit on an SM");
+  const uint64_t sms = ctx->sm_count > 0 ? (uint64_t)ctx->sm_count : 152u;
+  const uint64_t need = div_up(n, (uint64_t)FUSED_THREADS);
+  const uint32_t blocks = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(sms * (uint64_t)per_sm, need));
+  if (inline_epa) PG_CUDA(ctx, ctx->epa_ws.reserve((size_t)blocks * FUSED_THREADS * EPA_SLOT_BYTES));
+  kern<<<blocks, FUSED_THREADS, smem, ctx->stream>>>(sh, pairs, n, order, n_large, prediction, init_dirs, out, has, queue, qcount, stats,
+                                                     ctx->d_err, final_dirs, work, ctx->epa_ws.as<uint32_t>(), ovf, ovf_count);
+  PG_LAUNCHED(ctx);
+  return PARRYGPU_OK;
 }
 
 }  // namespace
@@ -434,6 +746,7 @@ parrygpu_status parrygpu_contacts_with_dirs(parrygpu_ctx* ctx, const parrygpu_sh
   void* d_dirs = nullptr;
   bool c_dirs = false;
   if ((s = stage_output(ctx, ctx->stage_out[2], final_dirs, (size_t)n_pairs * 12, &d_dirs, &c_dirs)) != PARRYGPU_OK) return s;
+  const bool inline_epa = ctx->cfg.contact_epa_inline == 1;
   PG_CUDA(ctx, ctx->ct_queue.reserve((size_t)n_pairs * QUEUE_WORDS * 4));
   PG_CUDA(ctx, ctx->ct_counters.reserve(64));
   uint32_t epa_per_sm = ctx->cfg.epa_blocks_per_sm ? ctx->cfg.epa_blocks_per_sm : 8;
@@ -447,6 +760,7 @@ parrygpu_status parrygpu_contacts_with_dirs(parrygpu_ctx* ctx, const parrygpu_sh
   PG_CUDA(ctx, cudaMemsetAsync(ctr, 0, 64, ctx->stream));
   // pairs binned by support-scan cost (a 10-bit key, two radix passes)
   const uint32_t* order = nullptr;
+  int sorted_buf = 0;
   if (n_pairs > 4096 && n_pairs < 0xffffffffull) {
     uint32_t n = (uint32_t)n_pairs;
     if ((s = radix_sort_reserve(ctx, n)) != PARRYGPU_OK) return s;
@@ -458,21 +772,33 @@ parrygpu_status parrygpu_contacts_with_dirs(parrygpu_ctx* ctx, const parrygpu_sh
     if ((s = radix_sort_pairs(ctx, n, 10, &rb)) != PARRYGPU_OK) return s;
     kt.stop();
     order = ctx->sort_v[rb].as<uint32_t>();
+    sorted_buf = rb;
   }
   {
+    // warp-per-pair threshold: pairs of the sorted order whose cost reaches it (counted on the device)
+    const uint32_t warp_cost = ctx->cfg.contact_warp_cost ? ctx->cfg.contact_warp_cost : DEFAULT_CONTACT_WARP_COST;
+    const bool warp_path = order && warp_cost < 1024;
     KernelTimer kt(ctx, "contacts_gjk");
-    k_contacts_main<<<div_up(n_pairs, CT_THREADS), CT_THREADS, 0, ctx->stream>>>(
-        sh, (const uint32_t*)dp, n_pairs, order, prediction, (const float*)di, (float*)d_out, (uint8_t*)d_has,
-        ctx->ct_queue.as<uint32_t>(), ctr, ctr + 1, ctx->d_err, (float*)d_dirs);
+    if (warp_path) {
+      k_count_costly<<<1, 32, 0, ctx->stream>>>(ctx->sort_k[sorted_buf].as<uint32_t>(), (uint32_t)n_pairs, warp_cost, ctr + 6);
+      PG_LAUNCHED(ctx);
+    }
+    const size_t smem = warp_path ? sizeof(WarpSmem) * FUSED_WARPS : 0;
+    if ((s = launch_fused(ctx, smem, inline_epa, sh, (const uint32_t*)dp, n_pairs, order, ctr + 6, prediction, (const float*)di,
+                          (float*)d_out, (uint8_t*)d_has, ctx->ct_queue.as<uint32_t>(), ctr, ctr + 1, (float*)d_dirs, ctr + 5,
+                          ctx->ct_ovf.as<uint32_t>(), ctr + 4)) != PARRYGPU_OK)
+      return s;
     kt.stop();
-    PG_LAUNCHED(ctx);
   }
   {
     KernelTimer kt(ctx, "contacts_epa");
-    k_contacts_epa<false><<<epa_blocks, EPA_THREADS, 0, ctx->stream>>>(
-        sh, (const uint32_t*)dp, prediction, (float*)d_out, (uint8_t*)d_has, ctx->ct_queue.as<uint32_t>(), ctr,
-        ctx->epa_ws.as<uint32_t>(), ctr + 1, ctx->d_err, (float*)d_dirs, ctx->ct_ovf.as<uint32_t>(), ctr + 4);
-    PG_LAUNCHED(ctx);
+    if (!inline_epa) {
+      auto kern = epa_per_sm <= 8 ? k_contacts_epa<false, 8> : (epa_per_sm <= 12 ? k_contacts_epa<false, 12> : k_contacts_epa<false, 16>);
+      kern<<<epa_blocks, EPA_THREADS, 0, ctx->stream>>>(sh, (const uint32_t*)dp, prediction, (float*)d_out, (uint8_t*)d_has,
+                                                        ctx->ct_queue.as<uint32_t>(), ctr, ctx->epa_ws.as<uint32_t>(), ctr + 1, ctx->d_err,
+                                                        (float*)d_dirs, ctx->ct_ovf.as<uint32_t>(), ctr + 4);
+      PG_LAUNCHED(ctx);
+    }
     // pairs whose polytope outgrew the regular slots, on the large slots (an empty list exits at once)
     k_contacts_epa<true><<<EPA_BIG_SLOTS / EPA_THREADS, EPA_THREADS, 0, ctx->stream>>>(
         sh, (const uint32_t*)dp, prediction, (float*)d_out, (uint8_t*)d_has, ctx->ct_queue.as<uint32_t>(), ctr + 4,

@@ -17,18 +17,21 @@
 
 namespace pg {
 
-// Fixed capacities and word offsets of one polytope workspace.
-template <int MV, int MF, int MS, int MSTK>
+// Fixed capacities and word offsets of one polytope workspace. FW = words per face record: 8 (one
+// 32-byte sector, for per-thread workspaces in global memory) or 6 (the record without padding,
+// for workspaces in shared memory).
+template <int MV, int MF, int MS, int MSTK, int FW = 8>
 struct EpaLayout {
-  static constexpr int MAX_VERTS = MV, MAX_FACES = MF, MAX_SIL = MS, STACK = MSTK;
+  static constexpr int MAX_VERTS = MV, MAX_FACES = MF, MAX_SIL = MS, STACK = MSTK, FACE_WORDS = FW;
   static constexpr int W_VP = 0;                          // 4 words per vertex: CSO point (x, y, z, -)
   static constexpr int W_VO = W_VP + 4 * MV;              // 6 words per vertex: witness points orig1, orig2
-  static constexpr int W_FACES = W_VO + 6 * MV;           // 8 words per face
-  static constexpr int W_HEAP = W_FACES + 8 * MF;         // 2 words per heap entry
+  static constexpr int W_FACES = W_VO + 6 * MV;           // FW words per face
+  static constexpr int W_HEAP = W_FACES + FW * MF;        // 2 words per heap entry
   static constexpr int W_SIL = W_HEAP + 2 * MF;           // 1 word per silhouette edge
   static constexpr int W_STACK = W_SIL + MS;              // 1 word per stack entry
   static constexpr int WORDS = W_STACK + MSTK;            // words per workspace
-  static_assert(W_FACES % 8 == 0 && WORDS % 8 == 0, "faces and slots start on 32-byte boundaries");
+  static_assert(FW != 8 || (W_FACES % 8 == 0 && WORDS % 8 == 0), "faces and slots start on 32-byte boundaries");
+  static_assert(FW == 8 || FW == 6, "face records of 8 or 6 words");
 };
 // Per-thread workspaces in global memory.
 using EpaGlobalLayout = EpaLayout<128, 1024, 64, 256>;
@@ -59,7 +62,7 @@ struct EpaWsT {
   __device__ __forceinline__ V3 vo1(int v) const { int o = L::W_VO + 6 * v; return v3(f(o), f(o + 1), f(o + 2)); }
   __device__ __forceinline__ V3 vo2(int v) const { int o = L::W_VO + 6 * v + 3; return v3(f(o), f(o + 1), f(o + 2)); }
   // faces: word0 = pts (3 x u8) | deleted << 24; word1 = adj0 | adj1 << 16; word2 = adj2; 3-5 normal
-  __device__ __forceinline__ int fo(int fid) const { return L::W_FACES + 8 * fid; }
+  __device__ __forceinline__ int fo(int fid) const { return L::W_FACES + L::FACE_WORDS * fid; }
   __device__ __forceinline__ int pt(int fid, int k) const { return (w(fo(fid)) >> (8 * k)) & 0xff; }
   __device__ __forceinline__ bool deleted(int fid) const { return (w(fo(fid)) >> 24) != 0; }
   __device__ __forceinline__ void set_deleted(int fid) const { w(fo(fid)) |= 0x01000000u; }

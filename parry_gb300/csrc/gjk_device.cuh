@@ -425,9 +425,10 @@ __device__ __forceinline__ void gjk_result(const Simplex& s, bool prev, V3* p1, 
   *p2 = b;
 }
 
-// gjk::closest_points with exact_dist = true (gjk.rs:353-453). `iters` counts support evaluations.
-static __device__ __noinline__ GjkOut gjk_closest_points(const Pose& pos12, const ShapeDev& g1, const ShapeDev& g2, float max_dist, Simplex& s,
-                                                  uint32_t* iters) {
+// gjk::closest_points with exact_dist = true (gjk.rs:353-453). `iters` counts support evaluations;
+// `sup(dir)` is CSOPoint::from_shapes(pos12, g1, g2, dir).
+template <class Sup>
+__device__ __forceinline__ GjkOut gjk_closest_points_t(Sup sup, float max_dist, Simplex& s, uint32_t* iters) {
   const float eps_tol = GJK_EPS_TOL;
   const float eps_rel = sqrtf(eps_tol);
   GjkOut r;
@@ -449,7 +450,7 @@ static __device__ __noinline__ GjkOut gjk_closest_points(const Pose& pos12, cons
       return r;
     }
     (*iters)++;
-    CSO cso = cso_from_shapes(pos12, g1, g2, dir);
+    CSO cso = sup(dir);
     float min_bound = -dot(dir, cso.p);
     if (min_bound > max_dist) { r.kind = GJK_NO_INTERSECTION; r.dir = dir; return r; }
     if (max_bound - min_bound <= eps_rel * max_bound) {
@@ -476,6 +477,12 @@ static __device__ __noinline__ GjkOut gjk_closest_points(const Pose& pos12, cons
     niter += 1;
     if (niter == 100) { r.kind = GJK_NO_INTERSECTION; r.dir = v3(1.f, 0.f, 0.f); return r; }
   }
+}
+
+// The per-thread form.
+static __device__ __noinline__ GjkOut gjk_closest_points(const Pose& pos12, const ShapeDev& g1, const ShapeDev& g2, float max_dist, Simplex& s,
+                                                  uint32_t* iters) {
+  return gjk_closest_points_t([&](V3 d) { return cso_from_shapes(pos12, g1, g2, d); }, max_dist, s, iters);
 }
 
 }  // namespace pg

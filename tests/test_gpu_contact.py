@@ -115,6 +115,7 @@ def test_autotune_contacts_keeps_answers(oracle_lib):
     s, pairs = W.hull_pairs(8192, seed=17)
     cfg = pg.autotune_contacts(ctx, s, pairs, 0.0, reps=1)
     assert cfg["epa_blocks_per_sm"] in (4, 6, 8, 12, 16) and ctx.config == cfg
+    assert cfg["contact_warp_cost"] in (256, 512, 1024) and cfg["contact_epa_inline"] in (1, 2)
     has, out = pg.contacts(ctx, s, pairs, 0.0)
     ho, oo, _ = oracle_lib.contacts(s, pairs, 0.0)
     _compare(has, out, ho, oo, "after autotune")
@@ -140,3 +141,38 @@ def test_mixed_shapes_and_long_epa(gpu_ctx, oracle_lib):
     ho, oo, sto = oracle_lib.contacts(s2, p2, 0.0)
     assert sto["epa_max_faces"] >= 500 and st["epa_iters"] == sto["epa_iters"] == 101
     _compare(has, out, ho, oo, "capsule pair with 512 EPA faces")
+
+
+@pytest.mark.parametrize("warp_cost,epa_inline", [(2, 2), (100, 2), (300, 1), (4096, 1)])
+def test_warp_per_pair_path_vs_oracle(oracle_lib, warp_cost, epa_inline):
+    """Pairs whose support-scan cost reaches contact_warp_cost run one warp per pair (hulls staged in
+    shared memory by bulk copies, lane-parallel support scans, GJK and EPA in shared memory); the
+    others one thread per pair, with EPA right after GJK in the same thread (epa_inline 1) or through
+    the queue (2): the answers and iteration counts are the oracle's, with and without init_dir, with
+    prediction, and on mixed shapes (ball pairs in the warp bin fall back to one lane)."""
+    ctx = pg.Context(0, contact_warp_cost=warp_cost, contact_epa_inline=epa_inline)
+    try:
+        s, pairs = W.hull_pairs(40_000, seed=31)
+        has, out, st = pg.contacts(ctx, s, pairs, 0.0, want_stats=True)
+        ho, oo, sto = oracle_lib.contacts(s, pairs, 0.0)
+        _compare(has, out, ho, oo, f"hull pairs, warp cost {warp_cost}")
+        assert (st["gjk_iters"], st["epa_iters"], st["epa_calls"]) == (sto["gjk_iters"], sto["epa_iters"], sto["epa_calls"])
+        rng = np.random.default_rng(4)
+        d = rng.normal(size=(len(pairs), 3)).astype(np.float32)
+        d /= np.linalg.norm(d, axis=1, keepdims=True)
+        dirs = np.zeros((len(pairs), 3), np.float32)
+        has, out = pg.contacts(ctx, s, pairs, 0.05, init_dirs=d, final_dirs=dirs)
+        ho, oo, _ = oracle_lib.contacts(s, pairs, 0.05, init_dirs=d)
+        _compare(has, out, ho, oo, "init_dir + prediction")
+        dirs0 = np.zeros_like(dirs)
+        ctx0 = pg.Context(0, contact_warp_cost=4096)
+        pg.contacts(ctx0, s, pairs, 0.05, init_dirs=d, final_dirs=dirs0)
+        ctx0.close()
+        np.testing.assert_array_equal(dirs, dirs0)
+        s, pairs = W.mixed_contact_pairs(60_000, seed=29)
+        has, out, st = pg.contacts(ctx, s, pairs, 0.0, want_stats=True)
+        ho, oo, sto = oracle_lib.contacts(s, pairs, 0.0)
+        _compare(has, out, ho, oo, "mixed shapes")
+        assert st["epa_iters"] == sto["epa_iters"]
+    finally:
+        ctx.close()

@@ -33,11 +33,24 @@ def hull_pairs_full():
     return W.hull_pairs(FULL_PAIRS)
 
 
-def test_uneven_hull_pairs_full_size(gpu_ctx, oracle_lib, hull_pairs_full):
+@pytest.fixture(scope="module")
+def hull_pairs_oracle(oracle_lib, hull_pairs_full):
     s, pairs = hull_pairs_full
-    has, out, st = pg.contacts(gpu_ctx, s, pairs, 0.0, want_stats=True)
-    ho, oo, sto = oracle_lib.contacts(s, pairs, 0.0)
-    _compare_contacts(has, out, st, ho, oo, sto, "1,048,576 uneven hull pairs")
+    return oracle_lib.contacts(s, pairs, 0.0)
+
+
+@pytest.mark.parametrize("warp_cost,epa_inline", [(0, 0), (4096, 1), (160, 2), (2, 0)])
+def test_uneven_hull_pairs_full_size(oracle_lib, hull_pairs_full, hull_pairs_oracle, warp_cost, epa_inline):
+    """The library defaults (0, 0); one thread per pair with EPA right after GJK (4096, 1); the dearer
+    pairs one warp each (160); every pair one warp (2)."""
+    s, pairs = hull_pairs_full
+    ctx = pg.Context(0, contact_warp_cost=warp_cost, contact_epa_inline=epa_inline)
+    try:
+        has, out, st = pg.contacts(ctx, s, pairs, 0.0, want_stats=True)
+    finally:
+        ctx.close()
+    ho, oo, sto = hull_pairs_oracle
+    _compare_contacts(has, out, st, ho, oo, sto, f"1,048,576 uneven hull pairs, warp cost {warp_cost}")
     assert 0.3 < ho.mean() < 0.9
     print(f"\n{int(ho.sum())} contacts; GJK {st['gjk_iters'] / FULL_PAIRS:.3f} and EPA {st['epa_iters'] / FULL_PAIRS:.3f} "
           f"iterations per pair, {st['epa_calls']} EPA calls, identical to the oracle")
