@@ -79,6 +79,9 @@ typedef struct parrygpu_config {
                               GJK (one workspace slot per thread of the persistent grid); 2 = through a
                               queue, in a second persistent pass over the pairs that reach EPA; 0 =
                               library default (2) */
+  uint32_t mlp_infer;      /* parrygpu_mlp_predict: 1 = one fused kernel on the fifth-generation tensor
+                              cores (tcgen05.mma into TMEM, weights resident in shared memory); 2 = the
+                              training path's per-layer mma.sync GEMMs; 0 = library default (1) */
 } parrygpu_config;
 
 /* ---- context ---------------------------------------------------------------------------- */

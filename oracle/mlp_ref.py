@@ -40,6 +40,17 @@ def gelu_grad(x):
     return 0.5 * (1.0 + _erf(x / math.sqrt(2.0))) + x * np.exp(-0.5 * x * x) / math.sqrt(2.0 * math.pi)
 
 
+def forward(params: np.ndarray, feats: np.ndarray) -> np.ndarray:
+    """The network's output (n x 3, before normalisation) with the BF16 rounding of the GPU kernels
+    (inputs, weights and inter-layer activations), accumulated in float64."""
+    layers = unpack(params.astype(np.float64))
+    a = bf16(feats)
+    for li, (w, b) in enumerate(layers):
+        z = a @ bf16(w.astype(np.float32)).T + b
+        a = bf16(gelu(z).astype(np.float32)) if li < len(layers) - 1 else z
+    return a
+
+
 def loss_and_grads(params: np.ndarray, feats: np.ndarray, targets: np.ndarray, quantize: bool = True):
     """Mean (1 - cos) loss and its gradient (flat, parameter layout). quantize=False skips the BF16
     rounding (an exactly differentiable network, for finite-difference checks of this code)."""

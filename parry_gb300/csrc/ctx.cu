@@ -97,7 +97,7 @@ parrygpu_status parrygpu_create(parrygpu_ctx** out, const parrygpu_config* cfg) 
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) { cudaGetLastError(); return PARRYGPU_NO_DEVICE; }
   if (cfg && ((cfg->ray_block % 32) != 0 || cfg->ray_block > 1024 || cfg->ray_sort_key > 2 || cfg->epa_blocks_per_sm > 32 ||
               cfg->ray_traversal > 3 || cfg->ray_refill > 32 || cfg->ray_chunks > 64 || cfg->ray_host_access > 2 ||
-              (cfg->contact_warp_cost != 0 && cfg->contact_warp_cost < 2) || cfg->contact_epa_inline > 2))
+              (cfg->contact_warp_cost != 0 && cfg->contact_warp_cost < 2) || cfg->contact_epa_inline > 2 || cfg->mlp_infer > 2))
     return PARRYGPU_INVALID_ARG;
   parrygpu_ctx* ctx = new parrygpu_ctx();
   if (cfg) ctx->cfg = *cfg; else parrygpu_default_config(&ctx->cfg);

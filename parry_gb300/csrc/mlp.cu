@@ -1,5 +1,8 @@
 // Learned GJK warm start: a small MLP trained and evaluated with hand-written BF16 tensor-core
-// kernels (mma.sync m16n8k16, FP32 accumulation). No reference counterpart: its only link to the
+// kernels. Inference is one fused kernel on the fifth-generation tensor cores (k_mlp_infer_tc:
+// tcgen05.mma from shared memory into TMEM accumulators, all five layers per 128-sample tile with
+// the weights resident in shared memory); training runs per-layer mma.sync m16n8k16 GEMMs with FP32
+// accumulation and separate bias / activation / gradient kernels. No reference counterpart: its only link to the
 // reference is the init_dir parameter of contact_support_map_support_map_with_params
 // (src/query/contact/contact_support_map_support_map.rs:40-62), and the plain GJK result remains
 // the judge of the answer - a poor guess only costs iterations.
@@ -11,6 +14,7 @@
 // Layout of the parameter vector (parrygpu_mlp_get_params): per layer W [out x in] then b [out].
 #include "internal.hpp"
 #include "common.cuh"
+#include "tcgen05.cuh"
 #include <cuda_bf16.h>
 #include <vector>
 #include <cmath>
@@ -25,14 +29,16 @@ constexpr int NL = PARRYGPU_MLP_LAYERS;
 constexpr int OUT = 3;
 constexpr int DIN[NL] = {IN, HID, HID, HID, HID};
 constexpr int DOUT[NL] = {HID, HID, HID, HID, OUT};
+__host__ __device__ constexpr int din(int l) { return l == 0 ? IN : HID; }
+__host__ __device__ constexpr int dout(int l) { return l == NL - 1 ? OUT : HID; }
 constexpr int DESC = 16;
 
-constexpr uint64_t w_off(int l) {
+__host__ __device__ constexpr uint64_t w_off(int l) {
   uint64_t o = 0;
-  for (int i = 0; i < l; ++i) o += (uint64_t)DOUT[i] * DIN[i] + DOUT[i];
+  for (int i = 0; i < l; ++i) o += (uint64_t)dout(i) * din(i) + dout(i);
   return o;
 }
-constexpr uint64_t b_off(int l) { return w_off(l) + (uint64_t)DOUT[l] * DIN[l]; }
+__host__ __device__ constexpr uint64_t b_off(int l) { return w_off(l) + (uint64_t)dout(l) * din(l); }
 constexpr uint64_t N_PARAMS = w_off(NL);
 
 typedef __nv_bfloat16 bf16;
@@ -257,6 +263,194 @@ __global__ void k_normalize_dirs(const float* __restrict__ Y, const float* __res
 __global__ void k_features_to_bf16(const float* __restrict__ f, size_t n, bf16* __restrict__ x) {
   size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
   if (i < n * IN) x[i] = __float2bfloat16(f[i]);
+}
+
+// ---------------------------------------------------------------- fused inference on tcgen05
+// One CTA of 512 threads per SM, persistent over tiles of 128 samples, in two groups of 8 warps that
+// take alternate tiles, so that the tensor cores run one group's layer while the other group turns
+// its accumulator into activations. Shared memory holds every layer's BF16 weights once, as the B
+// operand (N x K, K-major, canonical core-matrix layout: 8 rows x 16 bytes per 128-byte core
+// matrix, core matrices along K 128 bytes apart, 8-row groups K/8 x 128 bytes apart), each group's
+// tile activations as the A operand in the same layout, and the biases. Per layer a group's first
+// thread issues K/16 tcgen05.mma (M = 128, N = 128, or 16 for the 3-wide output layer padded with
+// zero rows, K = 16 each) into the group's 128-column FP32 TMEM accumulator and commits them to the
+// group's mbarrier; the group's 8 warps then read the accumulator back (warp w of the group: TMEM
+// lanes 32 (w % 4) .. + 31, columns 64 (w / 4) .. + 63), add the bias, apply GELU (erf by a
+// published rational approximation, gelu_as) and write the next layer's BF16 activations into
+// shared memory. The output layer's 3 columns are normalised
+// into the init direction (the fallback of k_normalize_dirs for degenerate outputs). Activations
+// never leave the SM.
+constexpr int TC_GROUPS = 2;
+constexpr int TC_GROUP_THREADS = 256;
+constexpr int TC_THREADS = TC_GROUPS * TC_GROUP_THREADS;
+constexpr int TC_M = 128;
+constexpr int TC_NOUT = 16;  // output layer rows padded to the smallest N of an M = 128 MMA
+constexpr uint32_t TC_TMEM_COLS = 128;  // per group
+constexpr uint32_t TC_WAIT_POLLS = 1u << 24;
+__host__ __device__ constexpr int tc_rows(int l) { return l == NL - 1 ? TC_NOUT : dout(l); }
+__host__ __device__ constexpr uint32_t tc_w_bytes(int l) { return (uint32_t)tc_rows(l) * din(l) * 2; }
+__host__ __device__ constexpr uint32_t tc_w_off(int l) {
+  uint32_t o = 0;
+  for (int i = 0; i < l; ++i) o += tc_w_bytes(i);
+  return o;
+}
+constexpr uint32_t TC_ACT_BYTES = TC_M * HID * 2;
+constexpr uint32_t TC_ACT_OFF = tc_w_off(NL);                              // per group: 128 x 128 bf16
+constexpr uint32_t TC_BIAS_OFF = TC_ACT_OFF + TC_GROUPS * TC_ACT_BYTES;    // (NL - 1) x 128 + 16 floats
+constexpr uint32_t TC_BAR_OFF = TC_BIAS_OFF + ((NL - 1) * HID + TC_NOUT) * 4;
+constexpr uint32_t TC_SMEM = TC_BAR_OFF + 32;  // 2 mbarriers, the TMEM address, 2 failure flags
+static_assert(tc_w_off(1) % 1024 == 0 && TC_ACT_OFF % 1024 == 0 && TC_BAR_OFF % 8 == 0, "aligned shared-memory regions");
+
+// Byte offset of element (r, k) of an R x K K-major operand in the canonical layout.
+__device__ __forceinline__ uint32_t tc_off(uint32_t r, uint32_t k, uint32_t K) {
+  return ((r >> 3) * (K >> 3) + (k >> 3)) * 128u + (r & 7u) * 16u + (k & 7u) * 2u;
+}
+
+// GELU for the inference epilogue with erf from Abramowitz & Stegun, Handbook of Mathematical
+// Functions, 7.1.26 (|error| <= 1.5e-7, far below the BF16 rounding the activation then takes):
+// erf(z) = 1 - (a1 t + a2 t^2 + a3 t^3 + a4 t^4 + a5 t^5) exp(-z^2), t = 1 / (1 + p z), z >= 0.
+__device__ __forceinline__ float gelu_as(float x) {
+  const float z = fabsf(x) * 0.70710678118654752f;
+  const float t = __fdividef(1.0f, fmaf(0.3275911f, z, 1.0f));
+  const float poly = t * fmaf(t, fmaf(t, fmaf(t, fmaf(t, 1.061405429f, -1.453152027f), 1.421413741f), -0.284496736f), 0.254829592f);
+  const float e = 1.0f - poly * __expf(-z * z);
+  return 0.5f * x * (1.0f + copysignf(e, x));
+}
+
+__device__ __forceinline__ uint32_t pack_bf16x2(float a, float b) {
+  const __nv_bfloat162 v = __floats2bfloat162_rn(a, b);
+  return *reinterpret_cast<const uint32_t*>(&v);
+}
+
+// Barrier of one group's 256 threads (named barrier 1 + group; 0 is __syncthreads).
+__device__ __forceinline__ void group_sync(uint32_t g) { asm volatile("bar.sync %0, %1;" ::"r"(1u + g), "r"(TC_GROUP_THREADS) : "memory"); }
+
+__global__ void __launch_bounds__(TC_THREADS, 1) k_mlp_infer_tc(const float* __restrict__ feat, uint64_t n, const bf16* __restrict__ wb,
+                                                                const float* __restrict__ wf, float* __restrict__ dirs,
+                                                                uint32_t* __restrict__ err) {
+  extern __shared__ __align__(1024) uint8_t tc_smem[];
+  float* bias = reinterpret_cast<float*>(tc_smem + TC_BIAS_OFF);
+  uint64_t* bars = reinterpret_cast<uint64_t*>(tc_smem + TC_BAR_OFF);
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(tc_smem + TC_BAR_OFF + 16);
+  uint32_t* fail = tslot + 1;  // [2]
+  const uint32_t tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const uint32_t g = warp / 8, gtid = tid % TC_GROUP_THREADS, gwarp = warp % 8;
+  // weights (16-byte chunks of 8 bf16; padded rows of the output layer are zero) and biases
+#pragma unroll
+  for (int l = 0; l < NL; ++l) {
+    const uint32_t K = din(l), chunks = (uint32_t)tc_rows(l) * (K / 8);
+    for (uint32_t c = tid; c < chunks; c += TC_THREADS) {
+      const uint32_t r = c / (K / 8), kc = c % (K / 8);
+      uint4 v = make_uint4(0u, 0u, 0u, 0u);
+      if (r < (uint32_t)dout(l)) v = *reinterpret_cast<const uint4*>(wb + w_off(l) + (size_t)r * K + kc * 8);
+      *reinterpret_cast<uint4*>(tc_smem + tc_w_off(l) + tc_off(r, kc * 8, K)) = v;
+    }
+  }
+  for (uint32_t i = tid; i < (NL - 1) * HID + TC_NOUT; i += TC_THREADS) {
+    const uint32_t l = i / HID, j = i % HID;
+    bias[i] = (l < NL - 1) ? wf[b_off(l) + j] : (j < OUT ? wf[b_off(NL - 1) + j] : 0.0f);
+  }
+  if (warp == 0) tmem_alloc(tslot, TC_GROUPS * TC_TMEM_COLS);
+  if (tid == 0) {
+    mbar_init(&bars[0], 1);
+    mbar_init(&bars[1], 1);
+    fail[0] = fail[1] = 0;
+  }
+  tc_fence_before_sync();
+  __syncthreads();
+  tc_fence_after_sync();
+  uint8_t* act = tc_smem + TC_ACT_OFF + g * TC_ACT_BYTES;
+  uint64_t* bar = &bars[g];
+  const uint32_t tmem = *tslot + g * TC_TMEM_COLS;
+  const uint32_t quarter = gwarp & 3, colblk = gwarp >> 2;
+  const uint32_t row = quarter * 32 + lane;                       // this thread's TMEM lane = tile row
+  const uint32_t tl = tmem + ((quarter * 32u) << 16);             // this warp's TMEM lanes
+  uint32_t phase = 0;
+  bool failed = false;
+  const uint64_t tiles = (n + TC_M - 1) / TC_M;
+  for (uint64_t tile = (uint64_t)blockIdx.x * TC_GROUPS + g; tile < tiles && !failed; tile += (uint64_t)gridDim.x * TC_GROUPS) {
+    const uint64_t base = tile * TC_M;
+    // features -> bf16 A operand (K = 48); rows past n are zero
+    for (uint32_t c = gtid; c < TC_M * (IN / 8); c += TC_GROUP_THREADS) {
+      const uint32_t r = c / (IN / 8), kc = c % (IN / 8);
+      uint4 v = make_uint4(0u, 0u, 0u, 0u);
+      if (base + r < n) {
+        const float4* src = reinterpret_cast<const float4*>(feat + (base + r) * IN + kc * 8);
+        const float4 a = src[0], b = src[1];
+        v = make_uint4(pack_bf16x2(a.x, a.y), pack_bf16x2(a.z, a.w), pack_bf16x2(b.x, b.y), pack_bf16x2(b.z, b.w));
+      }
+      *reinterpret_cast<uint4*>(act + tc_off(r, kc * 8, IN)) = v;
+    }
+#pragma unroll
+    for (int l = 0; l < NL; ++l) {
+      const uint32_t K = din(l);
+      // the operands written by the threads become visible to the tensor cores' (async) proxy
+      fence_async_shared();
+      tc_fence_before_sync();
+      group_sync(g);
+      if (gtid == 0) {
+        tc_fence_after_sync();
+        const uint32_t sbo = (K / 8) * 128u, idesc = umma_idesc_bf16(TC_M, (uint32_t)tc_rows(l));
+        for (uint32_t ks = 0; ks < K / 16; ++ks) {
+          const uint64_t ad = umma_desc_kmajor(act + ks * 256u, 128u, sbo);
+          const uint64_t bd = umma_desc_kmajor(tc_smem + tc_w_off(l) + ks * 256u, 128u, sbo);
+          umma_bf16(tmem, ad, bd, idesc, ks > 0);
+        }
+        umma_commit(bar);
+      }
+      if (!mbar_wait_bounded(bar, phase, TC_WAIT_POLLS)) atomicOr(&fail[g], 1u);
+      group_sync(g);
+      if (fail[g]) {  // the tensor cores did not answer: report, and leave without reading TMEM
+        if (gtid == 0) atomicOr(err, ERR_TIMEOUT);
+        mbar_wait_bounded(bar, phase, TC_WAIT_POLLS);
+        failed = true;
+        break;
+      }
+      phase ^= 1u;
+      tc_fence_after_sync();
+      if (l < NL - 1) {
+        const float* bl = bias + l * HID;
+#pragma unroll 1
+        for (uint32_t c0 = colblk * 64; c0 < colblk * 64 + 64; c0 += 16) {
+          float v[16];
+          tmem_ld16(tl + c0, v);
+          uint32_t w8[8];
+#pragma unroll
+          for (int j = 0; j < 8; ++j)
+            w8[j] = pack_bf16x2(gelu_as(v[2 * j] + bl[c0 + 2 * j]), gelu_as(v[2 * j + 1] + bl[c0 + 2 * j + 1]));
+          *reinterpret_cast<uint4*>(act + tc_off(row, c0, HID)) = make_uint4(w8[0], w8[1], w8[2], w8[3]);
+          *reinterpret_cast<uint4*>(act + tc_off(row, c0 + 8, HID)) = make_uint4(w8[4], w8[5], w8[6], w8[7]);
+        }
+      } else if (colblk == 0) {
+        float v[16];
+        tmem_ld16(tl, v);
+        const uint64_t k = base + row;
+        if (k < n) {
+          const float* bl = bias + (NL - 1) * HID;
+          V3 y = v3(v[0] + bl[0], v[1] + bl[1], v[2] + bl[2]);
+          const float yy = dot(y, y);
+          V3 d;
+          if (yy > 1e-12f && isfinite(yy)) d = y / sqrtf(yy);
+          else {
+            const V3 t = v3(feat[k * IN + 4], feat[k * IN + 5], feat[k * IN + 6]);
+            const float tt = dot(t, t);
+            d = tt > 1.1920929e-7f * 1.1920929e-7f ? t / sqrtf(tt) : v3(1.f, 0.f, 0.f);
+          }
+          dirs[3 * k] = d.x;
+          dirs[3 * k + 1] = d.y;
+          dirs[3 * k + 2] = d.z;
+        }
+      }
+    }
+    // the accumulator and activations are free for the group's next tile once its threads are done
+    tc_fence_before_sync();
+    group_sync(g);
+    tc_fence_after_sync();
+  }
+  tc_fence_before_sync();
+  __syncthreads();
+  tc_fence_after_sync();
+  if (warp == 0) tmem_dealloc(*tslot, TC_GROUPS * TC_TMEM_COLS);
 }
 
 // ---------------------------------------------------------------- features
@@ -600,13 +794,25 @@ parrygpu_status parrygpu_mlp_predict(parrygpu_ctx* ctx, const parrygpu_mlp* cmlp
   bool copy;
   if ((s = stage_output(ctx, ctx->stage_out[2], dirs, n * 12, &d_dirs, &copy)) != PARRYGPU_OK) return s;
   KernelTimer kt(ctx, "mlp_predict");
-  for (uint64_t b0 = 0; b0 < n; b0 += chunk) {
-    uint64_t nb = n - b0 < chunk ? n - b0 : chunk;
-    if ((s = load_features(ctx, mlp, (const float*)d_f + b0 * IN, nb)) != PARRYGPU_OK) return s;
-    if ((s = forward(ctx, mlp, nb)) != PARRYGPU_OK) return s;
-    k_normalize_dirs<<<div_up(nb, 256), 256, 0, ctx->stream>>>(mlp->z[NL - 1].as<float>(), (const float*)d_f + b0 * IN, nb,
-                                                              (float*)d_dirs + b0 * 3);
+  if (ctx->cfg.mlp_infer != 2) {  // the fused tcgen05 kernel
+    if ((reinterpret_cast<uintptr_t>(d_f) & 15u) != 0)
+      return set_error(ctx, PARRYGPU_INVALID_ARG, "parrygpu_mlp_predict needs 16-byte aligned features");
+    PG_CUDA(ctx, cudaFuncSetAttribute(k_mlp_infer_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TC_SMEM));
+    const uint64_t tiles = (n + TC_M - 1) / TC_M;
+    const uint32_t sms = ctx->sm_count > 0 ? (uint32_t)ctx->sm_count : 152u;
+    const uint32_t grid = (uint32_t)(tiles < sms ? tiles : sms);
+    k_mlp_infer_tc<<<grid, TC_THREADS, TC_SMEM, ctx->stream>>>((const float*)d_f, n, mlp->wb.as<bf16>(), mlp->w.as<float>(),
+                                                             (float*)d_dirs, ctx->d_err);
     PG_LAUNCHED(ctx);
+  } else {  // per-layer mma.sync GEMMs (the training path's forward)
+    for (uint64_t b0 = 0; b0 < n; b0 += chunk) {
+      uint64_t nb = n - b0 < chunk ? n - b0 : chunk;
+      if ((s = load_features(ctx, mlp, (const float*)d_f + b0 * IN, nb)) != PARRYGPU_OK) return s;
+      if ((s = forward(ctx, mlp, nb)) != PARRYGPU_OK) return s;
+      k_normalize_dirs<<<div_up(nb, 256), 256, 0, ctx->stream>>>(mlp->z[NL - 1].as<float>(), (const float*)d_f + b0 * IN, nb,
+                                                                (float*)d_dirs + b0 * 3);
+      PG_LAUNCHED(ctx);
+    }
   }
   kt.stop();
   if (copy) PG_CUDA(ctx, cudaMemcpyAsync(dirs, d_dirs, n * 12, cudaMemcpyDeviceToHost, ctx->stream));

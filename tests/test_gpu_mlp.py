@@ -64,3 +64,32 @@ def test_training_and_warm_start(gpu_ctx, tmp_path):
     dd = np.abs(o0[both, 12] - o1[both, 12])
     print(f"has-contact agreement {same:.5f}, depth |diff| p99 {np.quantile(dd, 0.99):.2e} max {dd.max():.2e}")
     assert same > 0.999
+
+
+@pytest.mark.parametrize("n", [5, 128, 10_077])
+def test_tcgen05_inference_matches_oracle_and_mma_path(gpu_ctx, n):
+    """The fused tcgen05 inference kernel (weights resident in shared memory, TMEM accumulators,
+    all five layers per 128-sample tile) against the float64 forward with the same BF16 rounding,
+    and against the per-layer mma.sync forward: unit directions with cosine above 0.999 for every
+    sample (the accumulation order differs, so a BF16 activation can round the other way)."""
+    from oracle import mlp_ref
+    rng = np.random.default_rng(n)
+    mlp = pg.WarmStartMLP(gpu_ctx, seed=11)
+    x = rng.normal(size=(n, 48)).astype(np.float32)
+    x[:, 39:] = 0.0
+    d_tc = mlp.predict(x)
+    ctx2 = pg.Context(0, mlp_infer=2)
+    try:
+        mlp2 = pg.WarmStartMLP(ctx2, seed=0)
+        mlp2.set_params(mlp.get_params())
+        d_mma = mlp2.predict(x)
+    finally:
+        ctx2.close()
+    ref = _unit(mlp_ref.forward(mlp.get_params(), x))
+    for d, what in ((d_tc, "tcgen05"), (d_mma, "mma.sync")):
+        assert d.shape == (n, 3) and np.isfinite(d).all()
+        np.testing.assert_allclose(np.linalg.norm(d, axis=1), 1.0, atol=1e-5)
+        cos = np.sum(d.astype(np.float64) * ref, axis=1)
+        print(f"\n{what}: cosine to the oracle min {cos.min():.7f} median {np.median(cos):.9f}")
+        assert cos.min() > 0.999, what
+    assert np.sum(d_tc * d_mma, axis=1).min() > 0.999
