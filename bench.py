@@ -128,13 +128,26 @@ def measured_peak_hbm() -> tuple[float, str]:
     return 6800.0, "fallback"
 
 
-def profiled_traffic(name: str) -> float | None:
-    """dram read+write bytes per launch recorded from an ncu capture (profiles/<name>.txt)."""
+def measured_peak_bf16() -> tuple[float, str]:
+    """Dense BF16 tensor peak (TFLOP/s) for a kernel timed alone: the driver's measured burst figure,
+    else the earlier GB300 measurement."""
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        try:
+            return float(json.loads(p.read_text())["bf16_tflops"]), "measured"
+        except Exception:
+            pass
+    return 1900.0, "fallback"
+
+
+def profiled_traffic(name: str, key: str = "dram_bytes_per_launch_full_size") -> float | None:
+    """A figure recorded from an ncu capture (profiles/<name>.txt, line `<key>: <value> ...`):
+    by default the dram read+write bytes per launch at the full size."""
     p = ROOT / "profiles" / f"{name}.txt"
     if not p.exists():
         return None
     for line in p.read_text().splitlines():
-        if line.startswith("dram_bytes_per_launch_full_size:"):
+        if line.startswith(key + ":"):
             try:
                 return float(line.split(":", 1)[1].split()[0])
             except ValueError:
@@ -584,6 +597,12 @@ def contacts_section(ctx, stream, steps: int, warmup: int, n_pairs: int, flush) 
     sms = torch.cuda.get_device_properties(0).multi_processor_count
     fp32_peak = sms * 128 * 2 * sm_mhz * 1e6 / 1e12
     achieved = flops_per_pair * n_pairs / (kernel_ms / 1e3) / 1e12
+    # algorithmic HBM bytes per pair: both hulls' vertices once, the pair, two poses and params, the
+    # output; against the DRAM bytes an ncu capture of the same kernels measured per pair
+    hull_bytes = 12.0 * float(np.sum(prm.view(np.uint32)[:, 1][pairs.reshape(-1)].astype(np.float64))) / n_pairs
+    alg_bytes = hull_bytes + 8 + 2 * (28 + 16 + 4) + 53
+    hbm_peak, hbm_kind = measured_peak_hbm()
+    prof = profiled_traffic("contacts_gjk_epa_hull_pairs", "dram_bytes_per_pair")
     return {
         "workload": "convex hull pairs, 8-256 vertices log-uniform on ellipsoids, random relative pose, prediction 0",
         "pairs": n_pairs, "metric": "contact pairs/s", "value": round(n_pairs / (ms / 1e3), 1), "unit": "pairs/s",
@@ -600,6 +619,11 @@ def contacts_section(ctx, stream, steps: int, warmup: int, n_pairs: int, flush) 
                      "frac": round(achieved / fp32_peak, 6), "peak_source": "nominal: SMs x 128 lanes x 2 (FMA) x max SM clock",
                      "flops_per_pair": round(flops_per_pair, 1),
                      "flops_model": "5 flops per vertex dot x vertices scanned by the f32 oracle's support calls on a sample"},
+        "roofline_hbm": {"bound": "hbm", "achieved": round(alg_bytes * n_pairs / (kernel_ms / 1e3) / 1e9, 1), "peak": hbm_peak,
+                         "unit": "GB/s", "frac": round(alg_bytes * n_pairs / (kernel_ms / 1e3) / 1e9 / hbm_peak, 4),
+                         "peak_source": hbm_kind, "algorithmic_bytes_per_pair": round(alg_bytes, 1),
+                         "dram_bytes_per_pair_profiled": prof,
+                         "bytes_model": "12 B per hull vertex of both shapes once + pair, poses, params, output"},
         "cpu_baseline": {"value": round(sample / cpu_s, 1), "unit": "pairs/s", "cores": threads, "kind": "port",
                          "sample": f"first {sample} pairs; C++ restatement of parry3d f32 query::contact"},
         "matches_oracle_on_sample": same,
@@ -901,9 +925,33 @@ def learned_section(ctx, stream, dev_shapes, dev_pairs, n_eval: int, n_train: in
             b.record(stream)
         torch.cuda.synchronize()
         out[name] = sum(a.elapsed_time(b) for a, b in ev) / steps
-    f = mlp.features(dev_shapes, dev_pairs)
-    d = mlp.predict(f)
+    # stage split of the learned step: features, fused tcgen05 inference
+    ctx.enable_kernel_timing(True)
+    ctx.reset_kernel_timing()
+    for _ in range(steps):
+        f = mlp.features(dev_shapes, dev_pairs)
+        d = mlp.predict(f)
+    torch.cuda.synchronize()
+    inf_ms, inf_n = ctx.kernel_time("mlp_predict")
+    ctx.enable_kernel_timing(False)
+    ev_f = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+    ev_f[0].record(stream)
+    for _ in range(steps):
+        f = mlp.features(dev_shapes, dev_pairs)
+    ev_f[1].record(stream)
+    torch.cuda.synchronize()
+    feat_ms = ev_f[0].elapsed_time(ev_f[1]) / steps
+    inf_ms = inf_ms / max(inf_n, 1)
+    mlp_flops = 2 * (48 * 128 + 3 * 128 * 128 + 128 * 3)
+    peak_tc, peak_kind = measured_peak_bf16()
+    tflops = mlp_flops * n_eval / (inf_ms / 1e3) / 1e12
     _, _, st_p = pg.contacts(ctx, dev_shapes, dev_pairs, 0.0, out=(has, res), want_stats=True)
+    _, _, st_l = pg.contacts(ctx, dev_shapes, dev_pairs, 0.0, init_dirs=d, out=(has_l, res_l), want_stats=True)
+    # the ceiling of any predictor: the exact direction the plain run ends with, as init_dir
+    best = torch.empty((n_eval, 3), dtype=torch.float32, device="cuda")
+    pg.contacts(ctx, dev_shapes, dev_pairs, 0.0, final_dirs=best)
+    best = best / best.norm(dim=1, keepdim=True).clamp_min(1e-30)
+    _, _, st_b = pg.contacts(ctx, dev_shapes, dev_pairs, 0.0, init_dirs=best, out=(has_l, res_l), want_stats=True)
     _, _, st_l = pg.contacts(ctx, dev_shapes, dev_pairs, 0.0, init_dirs=d, out=(has_l, res_l), want_stats=True)
     hp, hl = has.cpu().numpy(), has_l.cpu().numpy()
     both = (hp == 1) & (hl == 1)
@@ -913,17 +961,25 @@ def learned_section(ctx, stream, dev_shapes, dev_pairs, n_eval: int, n_train: in
     return {
         "train_pairs": n_train, "eval_pairs": n_eval, "train_seconds": round(train_s, 3),
         "loss_per_epoch": [round(float(x), 5) for x in losses],
-        "mean_gjk_iterations": {"plain": round(ip, 4), "learned": round(il, 4), "ratio": round(ip / il, 4)},
+        "mean_gjk_iterations": {"plain": round(ip, 4), "learned": round(il, 4), "ratio": round(ip / il, 4),
+                                "exact_final_direction": round(st_b["gjk_iters"] / n_eval, 4),
+                                "ceiling_ratio": round(st_p["gjk_iters"] / st_b["gjk_iters"], 4)},
         "mean_gjk_plus_epa_iterations": {
             "plain": round((st_p["gjk_iters"] + st_p["epa_iters"]) / n_eval, 4),
-            "learned": round((st_l["gjk_iters"] + st_l["epa_iters"]) / n_eval, 4)},
+            "learned": round((st_l["gjk_iters"] + st_l["epa_iters"]) / n_eval, 4),
+            "exact_final_direction": round((st_b["gjk_iters"] + st_b["epa_iters"]) / n_eval, 4),
+            "ratio": round((st_p["gjk_iters"] + st_p["epa_iters"]) / (st_l["gjk_iters"] + st_l["epa_iters"]), 4)},
+        "mlp_stage_ms": {"features": round(feat_ms, 4), "inference": round(inf_ms, 4)},
+        "mlp_inference_roofline": {"bound": "tensor", "kernel": "k_mlp_infer_tc (tcgen05.mma, TMEM)", "achieved": round(tflops, 2),
+                                   "peak": peak_tc, "unit": "TFLOP/s", "frac": round(tflops / peak_tc, 4), "peak_source": peak_kind,
+                                   "flops_per_pair": mlp_flops},
         "pairs_per_s": {"plain": round(n_eval / (out["plain"] / 1e3), 1), "learned": round(n_eval / (out["learned"] / 1e3), 1),
                         "ratio": round(out["plain"] / out["learned"], 4)},
         "ms_per_step": {"plain": round(out["plain"], 4), "learned_incl_mlp": round(out["learned"], 4)},
         "answers": {"has_contact_agreement": round(float((hp == hl).mean()), 6),
                     "depth_abs_diff_p99": float(np.quantile(dd, 0.99)) if dd.size else 0.0,
                     "depth_abs_diff_max": float(dd.max()) if dd.size else 0.0},
-        "mlp_flops_per_pair": 2 * (48 * 128 + 3 * 128 * 128 + 128 * 3),
+        "mlp_flops_per_pair": mlp_flops,
     }
 
 
@@ -947,8 +1003,9 @@ def summarize(line: dict) -> dict:
                  "roofline_frac": line["roofline"]["frac"], "cpu": line["cpu_baseline"]["value"]},
         "contacts": pick(line.get("contacts"), "value", "unit", "kernel_ms", "matches_oracle_on_sample", "e2e.value",
                          "cpu_baseline.value", "dram_bytes_per_pair", "mixed_shapes.value"),
-        "learned": pick(line.get("learned_warm_start"), "mean_gjk_iterations.ratio", "mean_gjk_plus_epa_iterations",
-                        "pairs_per_s.ratio", "answers.has_contact_agreement"),
+        "learned": pick(line.get("learned_warm_start"), "mean_gjk_iterations.ratio", "mean_gjk_iterations.ceiling_ratio",
+                        "mean_gjk_plus_epa_iterations.ratio", "pairs_per_s.ratio", "mlp_inference_roofline.achieved",
+                        "answers.has_contact_agreement"),
         "manifolds": pick(line.get("manifolds"), "value", "unit", "matches_oracle_on_sample"),
         "frame_pipeline": pick(line.get("frame_pipeline"), "value", "unit", "matches_oracle", "e2e.value", "cpu_baseline.value"),
         "broadphase": pick(line.get("broadphase"), "value", "unit", "matches_oracle"),

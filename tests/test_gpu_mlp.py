@@ -58,7 +58,22 @@ def test_training_and_warm_start(gpu_ctx, tmp_path):
     it1 = (st1["gjk_iters"] + st1["epa_iters"]) / len(p_eval)
     print(f"GJK iterations per pair plain {st0['gjk_iters'] / len(p_eval):.3f} learned {st1['gjk_iters'] / len(p_eval):.3f}; "
           f"GJK+EPA plain {it0:.3f} learned {it1:.3f}")
-    assert st1["gjk_iters"] < st0["gjk_iters"]
+    # the ceiling of any predictor: the exact direction the plain GJK/EPA ends with, as init_dir
+    best = np.zeros((len(p_eval), 3), np.float32)
+    pg.contacts(gpu_ctx, s_eval, p_eval, 0.0, final_dirs=best)
+    best = _unit(best.astype(np.float64) + 1e-30).astype(np.float32)
+    _, _, stb = pg.contacts(gpu_ctx, s_eval, p_eval, 0.0, init_dirs=best, want_stats=True)
+    ratio = st0["gjk_iters"] / st1["gjk_iters"]
+    ceiling = st0["gjk_iters"] / stb["gjk_iters"]
+    ratio_all = (st0["gjk_iters"] + st0["epa_iters"]) / (st1["gjk_iters"] + st1["epa_iters"])
+    print(f"GJK iteration ratio plain / learned {ratio:.4f} (ceiling with the exact final direction {ceiling:.4f}); "
+          f"GJK+EPA {ratio_all:.4f}")
+    # What the network achieves on these inputs (the target of 1.5x fewer iterations is out of reach:
+    # plain GJK averages about 3.07 iterations and even the exact final direction only reaches the
+    # ceiling printed above; EPA's iterations refine the polytope around the answer whatever the
+    # start): strictly fewer GJK iterations than the default direction.
+    assert ratio > 1.0
+    assert ceiling >= ratio
     same = (h0 == h1).mean()
     both = (h0 == 1) & (h1 == 1)
     dd = np.abs(o0[both, 12] - o1[both, 12])
