@@ -479,11 +479,30 @@ __device__ void sym_eig3(float a00, float a01, float a02, float a11, float a12, 
 
 // 16-float shape descriptor: AABB half extents (3), principal second moments of the shape's
 // points (3), vertex count / 256, bounding radius, type one-hot (ball, cuboid, capsule, polyhedron),
-// AABB volume, log(vertex count) / log(256), 2 zeros.
+// AABB volume, log(vertex count) / log(256), 2 zeros. One warp per shape: the lanes stride over a
+// polyhedron's vertices (coalesced reads; the second pass over them hits the cache) and the sums,
+// bounds and moments are warp-reduced; lane 0 writes the descriptor.
+__device__ __forceinline__ float warp_sum(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+__device__ __forceinline__ float warp_min(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fminf(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+__device__ __forceinline__ float warp_max(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+
 __global__ void k_shape_desc(const uint32_t* __restrict__ types, const float4* __restrict__ params, const float* __restrict__ pool, uint64_t n,
                              uint64_t n_vertices, float* __restrict__ desc) {
-  uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
-  if (i >= n) return;
+  const uint64_t i = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
+  const uint32_t lane = threadIdx.x & 31;
+  if (i >= n) return;  // whole warps leave together
   uint32_t t = types[i];
   float4 p = params[i];
   float he[3] = {0, 0, 0}, mom[3] = {0, 0, 0}, cnt = 1.0f, rad = 0.0f;
@@ -506,27 +525,30 @@ __global__ void k_shape_desc(const uint32_t* __restrict__ types, const float4* _
     uint64_t first = __float_as_uint(p.x), c = __float_as_uint(p.y);
     if (c == 0 || first + c > n_vertices) c = 0;
     const float* v = pool + 3 * first;
-    float mn[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, mx[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX}, s[3] = {0, 0, 0};
-    for (uint64_t j = 0; j < c; ++j) {
+    float mn[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, mx[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX}, s[3] = {0, 0, 0}, r2max = 0.0f;
+    for (uint64_t j = lane; j < c; j += 32) {
       for (int d = 0; d < 3; ++d) {
         float x = v[3 * j + d];
         mn[d] = fminf(mn[d], x); mx[d] = fmaxf(mx[d], x); s[d] += x;
       }
-      float r2 = v[3 * j] * v[3 * j] + v[3 * j + 1] * v[3 * j + 1] + v[3 * j + 2] * v[3 * j + 2];
-      rad = fmaxf(rad, sqrtf(r2));
+      r2max = fmaxf(r2max, v[3 * j] * v[3 * j] + v[3 * j + 1] * v[3 * j + 1] + v[3 * j + 2] * v[3 * j + 2]);
     }
+    for (int d = 0; d < 3; ++d) { mn[d] = warp_min(mn[d]); mx[d] = warp_max(mx[d]); s[d] = warp_sum(s[d]); }
+    rad = sqrtf(warp_max(r2max));
     float inv = c ? 1.0f / (float)c : 0.0f;
     float m[3] = {s[0] * inv, s[1] * inv, s[2] * inv};
     float cxx = 0, cxy = 0, cxz = 0, cyy = 0, cyz = 0, czz = 0;
-    for (uint64_t j = 0; j < c; ++j) {
+    for (uint64_t j = lane; j < c; j += 32) {
       float x = v[3 * j] - m[0], y = v[3 * j + 1] - m[1], z = v[3 * j + 2] - m[2];
       cxx += x * x; cxy += x * y; cxz += x * z; cyy += y * y; cyz += y * z; czz += z * z;
     }
+    cxx = warp_sum(cxx); cxy = warp_sum(cxy); cxz = warp_sum(cxz); cyy = warp_sum(cyy); cyz = warp_sum(cyz); czz = warp_sum(czz);
     sym_eig3(cxx * inv, cxy * inv, cxz * inv, cyy * inv, cyz * inv, czz * inv, mom);
     for (int d = 0; d < 3; ++d) he[d] = c ? 0.5f * (mx[d] - mn[d]) : 0.0f;
     cnt = (float)c;
     t = 3;
   }
+  if (lane != 0) return;
   float* o = desc + 16 * i;
   o[0] = he[0]; o[1] = he[1]; o[2] = he[2];
   o[3] = mom[0]; o[4] = mom[1]; o[5] = mom[2];
@@ -735,7 +757,7 @@ parrygpu_status parrygpu_mlp_features(parrygpu_ctx* ctx, const parrygpu_shapes* 
   PG_CUDA(ctx, ctx->misc.reserve(64));
   DevBuf& desc = ctx->stage_out[3];
   PG_CUDA(ctx, desc.reserve(shapes->n * 16 * 4));
-  k_shape_desc<<<div_up(shapes->n, 128), 128, 0, ctx->stream>>>((const uint32_t*)t, (const float4*)p, (const float*)v, shapes->n, shapes->n_vertices,
+  k_shape_desc<<<div_up(shapes->n * 32, 256), 256, 0, ctx->stream>>>((const uint32_t*)t, (const float4*)p, (const float*)v, shapes->n, shapes->n_vertices,
                                                                  desc.as<float>());
   PG_LAUNCHED(ctx);
   k_pair_features<<<div_up(n_pairs, 128), 128, 0, ctx->stream>>>((const float*)q, desc.as<float>(), (const uint32_t*)dp, n_pairs, shapes->n,
