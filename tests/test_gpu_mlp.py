@@ -108,3 +108,49 @@ def test_tcgen05_inference_matches_oracle_and_mma_path(gpu_ctx, n):
         print(f"\n{what}: cosine to the oracle min {cos.min():.7f} median {np.median(cos):.9f}")
         assert cos.min() > 0.999, what
     assert np.sum(d_tc * d_mma, axis=1).min() > 0.999
+
+
+def _quat_rotate(q, v):
+    qv, w = q[..., :3], q[..., 3:4]
+    t = 2.0 * np.cross(qv, v)
+    return v + w * t + np.cross(qv, t)
+
+
+def test_features_match_numpy(gpu_ctx):
+    """parrygpu_mlp_features against a numpy restatement of the descriptor (AABB half extents,
+    principal second moments, vertex count / 256, bounding radius, type one-hot, AABB volume,
+    log count) and of the relative pose of b in a's frame (quaternion with w >= 0, translation)."""
+    s, pairs = W.mixed_contact_pairs(2000, seed=41)
+    t, prm, pos, pool = s.arrays()
+    f = mlp_features = pg.WarmStartMLP(gpu_ctx, seed=0).features(s, pairs)
+    desc = np.zeros((len(t), 16))
+    for i, (ty, pr) in enumerate(zip(t, prm)):
+        if ty == 0:
+            r = pr[0]; he = [r] * 3; mom = [0.2 * r * r] * 3; cnt = 1.0; rad = r
+        elif ty == 1:
+            he = pr[:3]; mom = sorted(pr[:3] ** 2 / 3.0, reverse=True); cnt = 8.0; rad = np.linalg.norm(pr[:3])
+        elif ty == 2:
+            hh, r = pr[0], pr[1]; he = [r, hh + r, r]
+            mom = sorted([0.25 * r * r, hh * hh / 3.0 + 0.25 * r * r, 0.25 * r * r], reverse=True); cnt = 2.0; rad = hh + r
+        else:
+            first, c = pr.view(np.uint32)[:2]
+            v = pool[first:first + c].astype(np.float64)
+            he = 0.5 * (v.max(0) - v.min(0))
+            mom = sorted(np.linalg.eigvalsh(np.cov(v.T, bias=True)), reverse=True)
+            cnt = float(c); rad = np.linalg.norm(v, axis=1).max()
+        d = desc[i]
+        d[0:3], d[3:6], d[6], d[7] = he, mom, cnt / 256.0, rad
+        d[8 + min(int(ty), 3)] = 1.0
+        d[12] = 8.0 * he[0] * he[1] * he[2]
+        d[13] = np.log(cnt) / np.log(256.0)
+    a, b = pairs[:, 0], pairs[:, 1]
+    qa, qb = pos[a, :4].astype(np.float64), pos[b, :4].astype(np.float64)
+    ca = np.concatenate([-qa[:, :3], qa[:, 3:]], axis=1)
+    q = np.stack([ca[:, 3] * qb[:, 0] + ca[:, 0] * qb[:, 3] + ca[:, 1] * qb[:, 2] - ca[:, 2] * qb[:, 1],
+                  ca[:, 3] * qb[:, 1] - ca[:, 0] * qb[:, 2] + ca[:, 1] * qb[:, 3] + ca[:, 2] * qb[:, 0],
+                  ca[:, 3] * qb[:, 2] + ca[:, 0] * qb[:, 1] - ca[:, 1] * qb[:, 0] + ca[:, 2] * qb[:, 3],
+                  ca[:, 3] * qb[:, 3] - ca[:, 0] * qb[:, 0] - ca[:, 1] * qb[:, 1] - ca[:, 2] * qb[:, 2]], axis=1)
+    q *= np.where(q[:, 3:4] < 0, -1.0, 1.0)
+    tr = _quat_rotate(ca, pos[b, 4:7].astype(np.float64) - pos[a, 4:7])
+    want = np.concatenate([q, tr, desc[a], desc[b], np.zeros((len(pairs), 48 - 39))], axis=1)
+    np.testing.assert_allclose(f, want, rtol=2e-4, atol=2e-5)
