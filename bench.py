@@ -517,7 +517,7 @@ def trimesh_contacts_section(ctx, stream, frames: int, warmup: int, n_shapes: in
                              "sample": f"the first {sample} shapes (one frame scaled to all {n}); C++ manifolds, numpy workspace"}}
 
 
-def contacts_section(ctx, stream, steps: int, warmup: int, n_pairs: int, flush) -> dict:
+def contacts_section(ctx, stream, steps: int, warmup: int, n_pairs: int, flush, epa_blocks: int = 0) -> dict:
     """Batched query::contact on uneven convex-hull pairs (8-256 vertices, log-uniform), the
     GJK/EPA workload: device-resident pairs/s, end-to-end pairs/s through host buffers, kernel
     split, FP32 roofline from the oracle's support-scan count, and the oracle CPU baseline."""
@@ -537,11 +537,18 @@ def contacts_section(ctx, stream, steps: int, warmup: int, n_pairs: int, flush) 
     has = torch.empty(n_pairs, dtype=torch.uint8, device="cuda")
     res = torch.empty((n_pairs, 13), dtype=torch.float32, device="cuda")
     t0 = time.perf_counter()
-    # EPA residency is tuned on the whole pair set: the best residency depends on how many pairs
-    # reach EPA at once, so a smaller sample picks for a different load
-    chosen = pg.autotune_contacts(ctx, dev, dpairs, 0.0, reps=1)
-    tune = {"chosen": {"epa_blocks_per_sm": chosen["epa_blocks_per_sm"]}, "sample_pairs": n_pairs,
-            "seconds": round(time.perf_counter() - t0, 3)}
+    if epa_blocks:
+        cfg = dict(ctx.config, epa_blocks_per_sm=epa_blocks, contact_warp_cost=4096, contact_epa_inline=2)
+        ctx_c = pg.Context(**cfg)
+        ctx_c.set_stream(stream.cuda_stream)
+        tune = {"fixed": {k: cfg[k] for k in ("epa_blocks_per_sm", "contact_warp_cost", "contact_epa_inline")}}
+        ctx = ctx_c
+    else:
+        # tuned on the whole pair set: the best EPA residency depends on how many pairs reach EPA at
+        # once, so a smaller sample picks for a different load
+        chosen = pg.autotune_contacts(ctx, dev, dpairs, 0.0, reps=1)
+        tune = {"chosen": {k: chosen[k] for k in ("epa_blocks_per_sm", "contact_warp_cost", "contact_epa_inline")},
+                "sample_pairs": n_pairs, "seconds": round(time.perf_counter() - t0, 3)}
     for _ in range(max(1, warmup)):
         pg.contacts(ctx, dev, dpairs, 0.0, out=(has, res))
     torch.cuda.synchronize()
@@ -1195,7 +1202,7 @@ def run_gb300(args) -> int:
     if args.broadphase_shapes > 0:
         broadphase = broadphase_section(ctx, stream, args.steps, args.warmup, args.broadphase_shapes, flush)
     if args.contact_pairs > 0:
-        contacts = contacts_section(ctx, stream, args.steps, args.warmup, args.contact_pairs, flush)
+        contacts = contacts_section(ctx, stream, args.steps, args.warmup, args.contact_pairs, flush, args.contact_epa_blocks)
         if args.train_pairs > 0:
             dev, dpairs = contacts_section.device_inputs
             learned = learned_section(ctx, stream, dev, dpairs, args.contact_pairs, args.train_pairs, args.steps, flush)
@@ -1273,6 +1280,8 @@ def main() -> int:
                          "default: chosen by the autotuner")
     ap.add_argument("--scene-shapes", type=int, default=262144, help="shapes of the per-frame pipeline section")
     ap.add_argument("--scene-rays", type=int, default=4194304, help="rays per frame of the per-frame pipeline section")
+    ap.add_argument("--contact-epa-blocks", type=int, default=0,
+                    help="contacts section: fixed EPA residency (one thread per pair, queued EPA) instead of the autotuner (0)")
     ap.add_argument("--train-pairs", type=int, default=1 << 21,
                     help="training pairs of the learned warm-start section (0 skips it)")
     args = ap.parse_args()
