@@ -807,6 +807,7 @@ def scene_section(ctx, stream, frames: int, warmup: int, flush, n_shapes: int = 
     graph_ms = a.elapsed_time(b) / frames
     launches = ctx.kernel_launches - l0
     frame_no, npairs = sc.info()
+    plain_stats = sc.stats()
     # stage split: one eager frame with per-stage events
     ctx.enable_kernel_timing(True)
     ctx.reset_kernel_timing()
@@ -831,6 +832,8 @@ def scene_section(ctx, stream, frames: int, warmup: int, flush, n_shapes: int = 
     d2h = out["poses"].nbytes + out["pairs"].nbytes + out["manifolds"].nbytes + out["ray_part"].nbytes + \
         out["ray_toi"].nbytes + out["ray_normal"].nbytes
     sc.close()
+    learned = scene_learned(ctx, stream, shapes, vel, rays, pred, dt, max_toi, max(1 << 16, 4 * n_shapes), frames, warmup, flush,
+                            st, graph_ms, plain_stats, stages["manifolds"])
     # the oracle frame on the host cores: the full shape set, a 262,144-ray sample scaled to 4,194,304
     threads = os.cpu_count() or 1
     sample = min(262144, len(rays))
@@ -871,6 +874,7 @@ def scene_section(ctx, stream, frames: int, warmup: int, flush, n_shapes: int = 
         "pairs_with_points": int((npts > 0).sum()), "ray_hits": hits,
         "rays_per_s_in_pipeline": round(len(rays) * 1e3 / graph_ms, 1),
         "stage_ms_eager_frame": stages,
+        "learned_seeding": learned,
         "e2e": {"value": round(1e3 / e2e_ms, 2), "unit": "frames/s", "ms_per_step": round(e2e_ms, 3), "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": int(d2h), "note": "each frame's poses, pairs, manifold records and ray hits read to the host"},
         "cpu_baseline": {"value": round(1e3 / cpu_frame_ms, 3), "unit": "frames/s", "cores": threads, "kind": "port",
@@ -879,6 +883,65 @@ def scene_section(ctx, stream, frames: int, warmup: int, flush, n_shapes: int = 
         "matches_oracle": all(same.values()),
         "matches_oracle_detail": same | {"checked": f"first frame: all {len(ww)} pairs and manifold records, the first "
                                                     f"{sample} rays, bit-exact"},
+    }
+
+
+def scene_learned(ctx, stream, shapes, vel, rays, pred, dt, max_toi, cap, frames, warmup, flush, state, plain_ms, plain_stats,
+                  plain_manifolds_ms) -> dict:
+    """The frame pipeline with the network seeding the polyhedral pairs that hold no cached normal
+    (new pairs): the network is trained on the final GJK directions of the polyhedral pairs of a
+    plain frame (`state`), then a fresh scene runs the same frames with seeding on (the features and
+    the tcgen05 inference inside each frame's graph) and is compared with the plain run at the same
+    frame: frame time, the last frame's GJK iterations and seeded pairs, the eager manifold stage."""
+    import numpy as np
+    import torch
+    import parry_gb300 as pg
+    from parry_gb300.shapes import BALL, CUBOID, CAPSULE
+
+    t = shapes.arrays()[0]
+    pairs = state["pairs"]
+    ta, tb = t[pairs[:, 0]], t[pairs[:, 1]]
+    poly = (ta != BALL) & (tb != BALL) & ~((ta == tb) & ((ta == CUBOID) | (ta == CAPSULE)))
+    p_tr = np.ascontiguousarray(pairs[poly])
+    now = shapes.with_poses(state["poses"])
+    labels = np.zeros((len(p_tr), 3), np.float32)
+    pg.contacts(ctx, now, p_tr, pred, final_dirs=labels)
+    labels /= np.maximum(np.linalg.norm(labels, axis=1, keepdims=True), 1e-12)
+    mlp = pg.WarmStartMLP(ctx, seed=7)
+    f_tr = torch.from_numpy(np.ascontiguousarray(mlp.features(now, p_tr))).cuda()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    mlp.train(f_tr, torch.from_numpy(labels).cuda(), epochs=4, batch=8192, lr=2e-3)
+    torch.cuda.synchronize()
+    train_s = time.perf_counter() - t0
+    del f_tr
+    sc = pg.Scene(ctx, shapes, vel, pred, cap)
+    sc.set_rays(torch.from_numpy(rays).cuda(), max_toi)
+    sc.set_mlp(mlp)
+    sc.step(dt, 2 * max(1, (warmup + 1) // 2), use_graph=True)
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    flush.zero_()
+    a.record(stream)
+    sc.step(dt, frames, use_graph=True)
+    b.record(stream)
+    torch.cuda.synchronize()
+    learned_ms = a.elapsed_time(b) / frames
+    st = sc.stats()
+    ctx.enable_kernel_timing(True)
+    ctx.reset_kernel_timing()
+    sc.step(dt, 1, use_graph=False)
+    ms, n = ctx.kernel_time("scene_manifolds")
+    ctx.enable_kernel_timing(False)
+    sc.close()
+    return {
+        "ms_per_frame": round(learned_ms, 4), "plain_ms_per_frame": round(plain_ms, 4),
+        "frame_time_ratio_plain_over_learned": round(plain_ms / learned_ms, 4),
+        "last_frame": {"seeded_pairs": st["seeded_pairs"], "gjk_iters": {"plain": plain_stats["gjk_iters"], "learned": st["gjk_iters"]},
+                       "epa_iters": {"plain": plain_stats["epa_iters"], "learned": st["epa_iters"]}},
+        "manifolds_stage_ms_eager": {"plain": plain_manifolds_ms, "learned": round(ms / max(n, 1), 4)},
+        "train": {"pairs": int(len(p_tr)), "epochs": 4, "seconds": round(train_s, 2),
+                  "labels": "final GJK directions of the plain frame's polyhedral pairs"},
     }
 
 
@@ -1014,7 +1077,8 @@ def summarize(line: dict) -> dict:
                         "mean_gjk_plus_epa_iterations.ratio", "pairs_per_s.ratio", "mlp_inference_roofline.achieved",
                         "answers.has_contact_agreement"),
         "manifolds": pick(line.get("manifolds"), "value", "unit", "matches_oracle_on_sample"),
-        "frame_pipeline": pick(line.get("frame_pipeline"), "value", "unit", "matches_oracle", "e2e.value", "cpu_baseline.value"),
+        "frame_pipeline": pick(line.get("frame_pipeline"), "value", "unit", "matches_oracle", "e2e.value", "cpu_baseline.value",
+                               "learned_seeding.frame_time_ratio_plain_over_learned", "learned_seeding.last_frame.seeded_pairs"),
         "broadphase": pick(line.get("broadphase"), "value", "unit", "matches_oracle"),
         "shape_cast": pick(line.get("shape_cast"), "value", "unit", "matches_oracle_on_sample"),
         "trimesh_contacts": pick(line.get("trimesh_contacts"), "value", "unit", "matches_oracle_on_sample"),

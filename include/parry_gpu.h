@@ -399,6 +399,14 @@ typedef struct parrygpu_manifold {
 #define PARRYGPU_PAIR_NONE 0xFFFFFFFFu
 parrygpu_status parrygpu_contact_manifolds(parrygpu_ctx* ctx, const parrygpu_shapes* shapes, const uint32_t* pairs, uint64_t n_pairs,
                                            float prediction, parrygpu_manifold* manifolds, parrygpu_gjk_stats* stats);
+/* parrygpu_contact_manifolds with a GJK start direction per pair for the polygonal-feature-map
+ * generator (init_dirs: n_pairs x 3 floats, host or device; NULL = none). A pair's direction is used
+ * where its record holds no cached normal (local_n1 does not normalise, e.g. a new pair);
+ * contact_manifolds_pfm_pfm.rs:67-76 otherwise starts from the relative translation. A row that does
+ * not normalise keeps that default. This is the hook the learned warm start seeds new pairs through. */
+parrygpu_status parrygpu_contact_manifolds_with_dirs(parrygpu_ctx* ctx, const parrygpu_shapes* shapes, const uint32_t* pairs,
+                                                     uint64_t n_pairs, float prediction, const float* init_dirs,
+                                                     parrygpu_manifold* manifolds, parrygpu_gjk_stats* stats);
 
 /* ---- per-frame pipeline over moving shapes ----
  * No single reference counterpart: one frame chains the parry calls a physics engine makes each step
@@ -429,6 +437,10 @@ parrygpu_status parrygpu_scene_info(parrygpu_ctx* ctx, const parrygpu_scene* sce
  * index or UINT32_MAX, toi, world normal). Synchronises. */
 parrygpu_status parrygpu_scene_read(parrygpu_ctx* ctx, const parrygpu_scene* scene, float* poses, uint32_t* pairs,
                                     parrygpu_manifold* manifolds, uint64_t cap, uint32_t* ray_part, float* ray_toi, float* ray_normal);
+/* The last frame's narrow-phase counters (synchronises): GJK and EPA iterations and EPA calls of its
+ * manifold updates, and (seeded_pairs, may be NULL) how many pairs took a learned GJK start direction
+ * (parrygpu_scene_set_mlp; 0 without a network). */
+parrygpu_status parrygpu_scene_stats(parrygpu_ctx* ctx, const parrygpu_scene* scene, parrygpu_gjk_stats* stats, uint64_t* seeded_pairs);
 
 /* ---- learned GJK warm start (no reference counterpart: parry's init_dir hook is its only tie) ----
  * A 39 -> 128 -> 128 -> 128 -> 128 -> 3 MLP (GELU, BF16 weights and activations, FP32 accumulation
@@ -462,6 +474,13 @@ uint64_t parrygpu_mlp_param_count(void);
 /* Copies the FP32 master parameters out / in (checkpoint and resume; the BF16 copies follow). */
 parrygpu_status parrygpu_mlp_get_params(parrygpu_ctx* ctx, const parrygpu_mlp* mlp, float* params);
 parrygpu_status parrygpu_mlp_set_params(parrygpu_ctx* ctx, parrygpu_mlp* mlp, const float* params);
+/* Seeds the scene's polygonal-feature-map pairs that hold no cached normal (the pairs new in a frame)
+ * with the network's GJK start direction, as parrygpu_contact_manifolds_with_dirs does; pairs that
+ * persist keep their cached normal. Each frame the pairs are listed on the device, their features
+ * computed and the network run by the fused tensor-core kernel, all inside the frame (and its graph).
+ * The scene keeps a snapshot of the weights taken by this call (later training does not reach it
+ * until the call is repeated) and computes the shape descriptors once. mlp = NULL turns seeding off. */
+parrygpu_status parrygpu_scene_set_mlp(parrygpu_ctx* ctx, parrygpu_scene* scene, const parrygpu_mlp* mlp);
 
 /* ---- contact manifolds against a TriMesh ------------------------------------------------- */
 

@@ -414,10 +414,11 @@ void oracle_compound_cast_rays_f64(void* c, const float* pose7, const float* ray
 // epa_calls, unsupported pairs, largest point count.
 // pseudo (may be null): rows of 12 floats (face, e01, e12, e20) of TrianglePseudoNormals; a triangle
 // shape of index >= pseudo_first whose params word 2 holds j > 0 has the normal constraints of row
-// j - 1.
+// j - 1. init_dirs (may be null): 3 floats per pair, the polyhedral generator's GJK start direction
+// where the record holds no cached normal.
 void oracle_manifolds_f32(const uint32_t* types, const float* params, const float* poses, const float* hullv, uint32_t nhv,
                           uint64_t nshapes, const void* poly, const uint32_t* pairs, uint64_t npairs, float prediction, int threads,
-                          uint32_t* records, uint64_t* stats, const float* pseudo, uint64_t pseudo_first) {
+                          uint32_t* records, uint64_t* stats, const float* pseudo, uint64_t pseudo_first, const float* init_dirs) {
   ShapeSet<float> set(types, params, poses, hullv, nhv, nshapes);
   set.attach(params, (const PolyIn*)poly);
   std::atomic<uint64_t> gi{0}, ei{0}, ec{0}, un{0}, mx{0};
@@ -442,7 +443,9 @@ void oracle_manifolds_f32(const uint32_t* types, const float* params, const floa
     TriPseudoNormals<float> pa, pb;
     const TriPseudoNormals<float>* ca = constraints(a, &pa);
     const TriPseudoNormals<float>* cb = constraints(b, &pb);
-    bool ok = contact_manifold_convex_convex(pos12, set.shapes[a], set.shapes[b], prediction, m, &st, ca, cb);
+    Vec3<float> learned;
+    if (init_dirs) learned = Vec3<float>(init_dirs[3 * k], init_dirs[3 * k + 1], init_dirs[3 * k + 2]);
+    bool ok = contact_manifold_convex_convex(pos12, set.shapes[a], set.shapes[b], prediction, m, &st, ca, cb, init_dirs ? &learned : nullptr);
     gi += st.gjk_iters; ei += st.epa_iters; ec += st.epa_calls;
     if (!ok) { un += 1; r[1] = 2; return; }
     r[1] = 0;

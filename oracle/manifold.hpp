@@ -761,10 +761,13 @@ inline void manifold_cuboid_triangle(const Iso<R>& pos12, const Iso<R>& pos21, c
 }
 
 // contact_manifolds_pfm_pfm.rs:44-162 for cuboids, capsules (segment + border radius), triangles and
-// hulls; c1 / c2 = normal constraints of shape 1 / 2.
+// hulls; c1 / c2 = normal constraints of shape 1 / 2. `learned` (may be null) is a caller-supplied
+// GJK start direction, used when the manifold holds no cached normal (contact_manifolds_pfm_pfm.rs:67-76
+// then falls back to the relative translation, else +x; a learned direction that does not normalise
+// keeps that fallback).
 template <class R> inline void manifold_pfm_pfm(const Iso<R>& pos12, const Shape<R>& s1, const Shape<R>& s2, R prediction, Manifold<R>& m,
                                                 GjkStats* st, const TriPseudoNormals<R>* c1 = nullptr,
-                                                const TriPseudoNormals<R>* c2 = nullptr) {
+                                                const TriPseudoNormals<R>* c2 = nullptr, const Vec3<R>* learned = nullptr) {
   if (m.try_update_contacts_eps(pos12, cos_1_degrees<R>(), R(1.0e-6))) return;
   auto pfm = [](const Shape<R>& s, R* border) {
     Shape<R> p = s;
@@ -776,6 +779,7 @@ template <class R> inline void manifold_pfm_pfm(const Iso<R>& pos12, const Shape
   Shape<R> p1 = pfm(s1, &br1), p2 = pfm(s2, &br2);
   Vec3<R> init;
   bool has_init = try_normalize(m.local_n1, eps_default<R>(), &init);
+  if (!has_init && learned) has_init = try_normalize(*learned, eps_default<R>(), &init);
   R total_prediction = (prediction + br1) + br2;
   VoronoiSimplex<R> simplex;
   GjkResult<R> r = contact_support_map_support_map_with_params(pos12, p1, p2, total_prediction, simplex, has_init ? &init : nullptr, st);
@@ -826,7 +830,7 @@ template <class R> inline void manifold_pfm_pfm(const Iso<R>& pos12, const Shape
 template <class R>
 inline bool contact_manifold_convex_convex(const Iso<R>& pos12, const Shape<R>& s1, const Shape<R>& s2, R prediction, Manifold<R>& m,
                                            GjkStats* st = nullptr, const TriPseudoNormals<R>* c1 = nullptr,
-                                           const TriPseudoNormals<R>* c2 = nullptr) {
+                                           const TriPseudoNormals<R>* c2 = nullptr, const Vec3<R>* learned = nullptr) {
   auto ok = [](const Shape<R>& s) {
     return s.type == SHAPE_BALL || s.type == SHAPE_CUBOID || s.type == SHAPE_CAPSULE || s.type == SHAPE_TRIANGLE ||
            (s.type == SHAPE_CONVEX && s.topo && s.topo->n_faces);
@@ -842,7 +846,7 @@ inline bool contact_manifold_convex_convex(const Iso<R>& pos12, const Shape<R>& 
     manifold_capsule_capsule(pos12, s1.half_height, s1.radius, s2.half_height, s2.radius, prediction, m);
   else if (s1.type == SHAPE_BALL) manifold_convex_ball(pos12.inverse(), s2, s1.radius, prediction, m, true, st, c2, c1);
   else if (s2.type == SHAPE_BALL) manifold_convex_ball(pos12, s1, s2.radius, prediction, m, false, st, c1, c2);
-  else manifold_pfm_pfm(pos12, s1, s2, prediction, m, st, c1, c2);
+  else manifold_pfm_pfm(pos12, s1, s2, prediction, m, st, c1, c2, learned);
   return true;
 }
 

@@ -47,7 +47,7 @@ _SIGS = {
     "oracle_compound_free_f64": (None, [P]),
     "oracle_compound_cast_rays_f32": (None, [P, P, P, U64, F32, I32, I32, I32, P, P, P, P]),
     "oracle_compound_cast_rays_f64": (None, [P, P, P, U64, F32, I32, I32, I32, P, P, P, P]),
-    "oracle_manifolds_f32": (None, [P, P, P, P, U32, U64, P, P, U64, F32, I32, P, P, P, U64]),
+    "oracle_manifolds_f32": (None, [P, P, P, P, U32, U64, P, P, U64, F32, I32, P, P, P, U64, P]),
     "oracle_trimesh_pseudo_normals_f32": (None, [P, U32, P, U32, P, P]),
     "oracle_project_local_normals_f32": (None, [P, P, U64, P, P]),
     "oracle_integrate_f32": (None, [P, P, U64, F32]),
@@ -272,11 +272,17 @@ def empty_manifolds(k: int) -> np.ndarray:
 
 
 def contact_manifolds(shapes, pairs: np.ndarray, prediction: float, records: np.ndarray, threads: int | None = None,
-                      pseudo: np.ndarray | None = None, pseudo_first: int = 0) -> dict:
+                      pseudo: np.ndarray | None = None, pseudo_first: int = 0, init_dirs: np.ndarray | None = None) -> dict:
     """DefaultQueryDispatcher::contact_manifold_convex_convex(pos_a^-1 pos_b, a, b, c_a, c_b, prediction,
     manifold) for every (a, b) row of `pairs`, updating `records` (k x MANIFOLD_WORDS uint32) in
     place. Normal constraints c: a triangle shape of index >= pseudo_first whose params word 2 holds
-    j > 0 uses row j - 1 of `pseudo` (rows of 12 floats: face, e01, e12, e20); else None."""
+    j > 0 uses row j - 1 of `pseudo` (rows of 12 floats: face, e01, e12, e20); else None.
+    init_dirs (k x 3 float32, optional): the polyhedral generator's GJK start direction for a pair
+    whose record holds no cached normal (contact_manifolds_pfm_pfm.rs:67-76 otherwise starts from the
+    relative translation); a row that does not normalise keeps that default."""
+    if init_dirs is not None:
+        init_dirs = np.ascontiguousarray(init_dirs, np.float32).reshape(-1, 3)
+        assert len(init_dirs) == len(pairs)
     if pseudo is not None:
         pseudo = np.ascontiguousarray(pseudo, np.float32).reshape(-1, 12)
     t, prm, pos, pool = _shape_arrays(shapes)
@@ -287,7 +293,8 @@ def contact_manifolds(shapes, pairs: np.ndarray, prediction: float, records: np.
     poly, keep = _poly_struct(shapes)
     lib().oracle_manifolds_f32(_p(t), _p(prm), _p(pos), _p(pool), len(pool), len(t), poly, _p(pairs), k, float(prediction),
                                threads if threads is not None else default_threads(), _p(records), _p(st),
-                               _p(pseudo) if pseudo is not None and len(pseudo) else None, int(pseudo_first))
+                               _p(pseudo) if pseudo is not None and len(pseudo) else None, int(pseudo_first),
+                               _p(init_dirs) if init_dirs is not None else None)
     del keep
     return {"gjk_iters": int(st[0]), "epa_iters": int(st[1]), "epa_calls": int(st[2]), "unsupported": int(st[3]),
             "max_points": int(st[4])}
@@ -463,10 +470,12 @@ def integrate(poses: np.ndarray, velocities: np.ndarray, dt: float) -> np.ndarra
 
 
 def scene_frames(shapes, velocities: np.ndarray, prediction: float, dt: float, frames: int, rays: np.ndarray | None = None,
-                 max_toi: float = 100.0, threads: int | None = None) -> dict:
+                 max_toi: float = 100.0, threads: int | None = None, dirs_fn=None) -> dict:
     """The frame pipeline restated with the oracle pieces: integrate, AABBs loosened by prediction / 2,
     binned-BVH self pairs, contact manifolds kept per pair across frames (new pairs start empty), and
     the rays cast against the final frame's shapes (Compound semantics, lowest index on ties).
+    dirs_fn(shapes, pairs) -> (k x 3) (optional) gives each frame's GJK start directions for the
+    pairs without a cached normal (the learned seeding; contact_manifolds' init_dirs).
     Returns poses, sorted pairs, their manifold words, and the ray results."""
     poses = np.ascontiguousarray(shapes.arrays()[2], np.float32).copy()
     records: dict = {}
@@ -483,7 +492,8 @@ def scene_frames(shapes, velocities: np.ndarray, prediction: float, dt: float, f
             old = records.get((int(a), int(b)))
             if old is not None:
                 recs[i] = old
-        contact_manifolds(s, pairs, prediction, recs, threads=threads)
+        dirs = dirs_fn(s, pairs) if dirs_fn is not None and len(pairs) else None
+        contact_manifolds(s, pairs, prediction, recs, threads=threads, init_dirs=dirs)
         records = {(int(a), int(b)): recs[i].copy() for i, (a, b) in enumerate(pairs)}
     out = {"poses": poses, "pairs": pairs, "manifolds": recs}
     if rays is not None:

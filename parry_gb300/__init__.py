@@ -561,21 +561,27 @@ def autotune_contacts(ctx: Context, shapes, pairs, prediction: float = 0.0, reps
     return _config_dict(cfg)
 
 
-def contact_manifolds(ctx: Context, shapes, pairs, prediction: float, manifolds, want_stats: bool = False):
+def contact_manifolds(ctx: Context, shapes, pairs, prediction: float, manifolds, want_stats: bool = False, init_dirs=None):
     """Batched DefaultQueryDispatcher::contact_manifold_convex_convex over the (a, b) rows of `pairs`,
     updating `manifolds` in place: a numpy array of parry_gb300.manifold.MANIFOLD_DTYPE records (k,),
     or a torch int32/uint32 tensor of shape (k, RECORD_WORDS) (a CUDA tensor is updated on the device).
-    Returns the stats dict when want_stats."""
+    init_dirs (k x 3, optional): the polyhedral generator's GJK start direction for pairs whose record
+    holds no cached normal (parrygpu_contact_manifolds_with_dirs). Returns the stats dict when
+    want_stats."""
     st = _StagedShapes(shapes)
     kp, pp = _as_input(pairs, np.uint32)
     k = int(kp.shape[0]) if kp is not None else 0
+    ki, pi = _as_input(init_dirs, np.float32) if init_dirs is not None else (None, None)
+    if ki is not None:
+        assert tuple(ki.shape) in ((k, 3), (k * 3,)), "init_dirs must hold 3 floats per pair"
     if _is_torch(manifolds):
         assert manifolds.is_contiguous() and tuple(manifolds.shape) == (k, RECORD_WORDS) and manifolds.element_size() == 4
     else:
         assert manifolds.dtype == MANIFOLD_DTYPE and manifolds.flags.c_contiguous and len(manifolds) == k
     stats = _capi.ParryGpuGjkStats()
-    check(lib().parrygpu_contact_manifolds(ctx.handle, C.byref(st.struct), pp, k, float(prediction), C.c_void_p(_dptr(manifolds)),
-                                           C.byref(stats) if want_stats else None), ctx.handle)
+    check(lib().parrygpu_contact_manifolds_with_dirs(ctx.handle, C.byref(st.struct), pp, k, float(prediction), pi,
+                                                     C.c_void_p(_dptr(manifolds)), C.byref(stats) if want_stats else None),
+          ctx.handle)
     if want_stats:
         return {"gjk_iters": stats.gjk_iterations, "epa_iters": stats.epa_iterations, "epa_calls": stats.epa_calls}
     return None
@@ -604,6 +610,12 @@ class Scene:
         check(lib().parrygpu_scene_set_rays(self._ctx.handle, self._h, pr, n, float(max_toi)), self._ctx.handle)
         self.n_rays = n
 
+    def set_mlp(self, mlp) -> None:
+        """Seeds the polyhedral pairs without a cached normal (new pairs) with the network's GJK start
+        direction each frame (parrygpu_scene_set_mlp); the scene keeps a snapshot of the weights.
+        None turns seeding off."""
+        check(lib().parrygpu_scene_set_mlp(self._ctx.handle, self._h, mlp._h if mlp is not None else None), self._ctx.handle)
+
     def step(self, dt: float, frames: int = 1, use_graph: bool = True) -> None:
         check(lib().parrygpu_scene_step(self._ctx.handle, self._h, float(dt), int(frames), 1 if use_graph else 0), self._ctx.handle)
 
@@ -630,6 +642,15 @@ class Scene:
                                         toi.ctypes.data if self.n_rays else None, nrm.ctypes.data if self.n_rays else None),
               self._ctx.handle)
         return {"poses": poses, "pairs": pairs, "manifolds": recs, "ray_part": part, "ray_toi": toi, "ray_normal": nrm}
+
+    def stats(self) -> dict:
+        """The last frame's narrow-phase counters: GJK / EPA iterations, EPA calls, and the pairs that
+        took a learned GJK start direction."""
+        st = _capi.ParryGpuGjkStats()
+        seeded = C.c_uint64()
+        check(lib().parrygpu_scene_stats(self._ctx.handle, self._h, C.byref(st), C.byref(seeded)), self._ctx.handle)
+        return {"gjk_iters": st.gjk_iterations, "epa_iters": st.epa_iterations, "epa_calls": st.epa_calls,
+                "seeded_pairs": seeded.value}
 
     def close(self) -> None:
         if getattr(self, "_h", None) is not None and self._h.value:

@@ -80,6 +80,7 @@ SIGNATURES: dict[str, tuple] = {
     "parrygpu_autotune_contacts": (I32, [P, P, P, U64, F32, U32, P]),
     "parrygpu_contacts_with_dirs": (I32, [P, P, P, U64, F32, P, P, P, P, P]),
     "parrygpu_contact_manifolds": (I32, [P, P, P, U64, F32, P, P]),
+    "parrygpu_contact_manifolds_with_dirs": (I32, [P, P, P, U64, F32, P, P, P]),
     "parrygpu_polyhedra_build": (I32, [P, P, P, U64, U32, C.POINTER(P)]),
     "parrygpu_scene_create": (I32, [P, P, P, F32, U64, C.POINTER(P)]),
     "parrygpu_scene_destroy": (None, [P]),
@@ -87,6 +88,8 @@ SIGNATURES: dict[str, tuple] = {
     "parrygpu_scene_step": (I32, [P, P, F32, U32, I32]),
     "parrygpu_scene_info": (I32, [P, P, P, P]),
     "parrygpu_scene_read": (I32, [P, P, P, P, P, U64, P, P, P]),
+    "parrygpu_scene_set_mlp": (I32, [P, P, P]),
+    "parrygpu_scene_stats": (I32, [P, P, P, P]),
     "parrygpu_polyhedra_sizes": (I32, [P, P]),
     "parrygpu_polyhedra_copy": (I32, [P, P, P, P, P, P, P, P, P, P, P]),
     "parrygpu_polyhedra_triangles": (I32, [P, P, P, P]),

@@ -209,8 +209,30 @@ parrygpu_status launch_shape_aabbs(parrygpu_ctx* ctx, const ShapeArrays& sh, uin
 // contact manifolds of the first min(cap, *d_count) pairs (manifold.cu) with caller-owned scratch
 // sized by manifolds_reserve(cap).
 parrygpu_status manifolds_reserve(parrygpu_ctx* ctx, uint64_t cap, MfScratch& scratch);
-// d_count may be null (then all `cap` pairs); returns after queuing the launches.
+// The frame pipeline's learned GJK start directions (mlp.cu): per-shape descriptors computed once,
+// a snapshot of the network's weights, and per-pair buffers sized for the pair capacity. The
+// manifold classification lists the polyhedral pairs whose record holds no cached normal; their
+// features and the network's directions are computed on the device before the polyhedral kernel.
+struct LearnedSeed {
+  const float* desc = nullptr;  // n_shapes x 16 descriptors
+  const void* wb = nullptr;     // BF16 weights in the network's parameter layout
+  const float* wf = nullptr;    // FP32 parameters (the biases are read from here)
+  float* feat = nullptr;        // cap x PARRYGPU_MLP_IN features, 16-byte aligned
+  uint32_t* list = nullptr;     // cap pair indices
+  float* dirs = nullptr;        // cap x 3 directions, row = pair index
+};
+// Features and tcgen05 inference of the pairs list[0 .. min(cap, *d_count)), writing their rows of
+// seed.dirs; no host synchronisation (graph-capturable).
+parrygpu_status launch_seed_dirs(parrygpu_ctx* ctx, const ShapeArrays& sh, const uint32_t* d_pairs, const LearnedSeed& seed,
+                                 const unsigned long long* d_count, uint64_t cap);
+// The shape descriptors (desc: n x 16 floats) and a snapshot of the network's BF16 weights and FP32
+// parameters into wb / wf; asynchronous on the context stream.
+parrygpu_status seed_prepare(parrygpu_ctx* ctx, const parrygpu_mlp* mlp, const ShapeArrays& sh, DevBuf& desc, DevBuf& wb, DevBuf& wf);
+// d_count may be null (then all `cap` pairs); returns after queuing the launches. init_dirs (may be
+// null): per-pair GJK start directions of the polyhedral generator where a record holds no cached
+// normal; with `seed`, the network computes them for the pairs that need one (init_dirs ignored).
 parrygpu_status launch_manifolds(parrygpu_ctx* ctx, const ShapeArrays& sh, const uint32_t* d_pairs, uint64_t cap,
-                                 const unsigned long long* d_count, float prediction, uint32_t* d_recs, MfScratch& scratch);
+                                 const unsigned long long* d_count, float prediction, uint32_t* d_recs, MfScratch& scratch,
+                                 const float* init_dirs = nullptr, const LearnedSeed* seed = nullptr);
 
 }  // namespace pg

@@ -1014,9 +1014,11 @@ enum : uint32_t {
   MK_BALL_BALL = 0, MK_CUBOID_CUBOID, MK_CAPSULE_CAPSULE, MK_CONVEX_BALL, MK_HULL_BALL,
   MK_PFM, MK_PFM_CUBOID_HULL, MK_PFM_CAPSULE_HULL, MK_PFM_HULL_HULL, MK_PFM_TRIANGLE, MK_CUBOID_TRIANGLE, MK_KINDS
 };
-// counters: [0] EPA queue length, [1..3] GJK / EPA stats, [4 + kind] bin lengths
+// counters: [0] EPA queue length, [1..3] GJK / EPA stats, [4 + kind] bin lengths, [15] learned-seed
+// list length
 constexpr int MF_CTR_BINS = 4;
-static_assert(MF_CTR_BINS + MK_KINDS <= 16, "the 128-byte counter block holds every bin length");
+constexpr int MF_CTR_SEED = 15;
+static_assert(MF_CTR_BINS + MK_KINDS <= MF_CTR_SEED, "the 128-byte counter block holds every bin length and the seed count");
 
 __device__ __forceinline__ uint32_t manifold_kind(uint32_t t1, uint32_t t2) {
   if (t1 == SH_BALL && t2 == SH_BALL) return MK_BALL_BALL;
@@ -1033,13 +1035,16 @@ __device__ __forceinline__ uint32_t manifold_kind(uint32_t t1, uint32_t t2) {
 
 // Status of each pair (invalid / unsupported records keep their content) and its bin, appended with
 // warp-aggregated atomics. A pair (PARRYGPU_PAIR_NONE, PARRYGPU_PAIR_NONE) is an empty slot: skipped. `d_n` (may be null) holds a device-side pair count: min(n, *d_n) pairs.
+// With `seed_list`, the polyhedral pairs whose record holds no cached normal (the pairs that take a
+// learned GJK start direction) are listed too, their count in ctr[MF_CTR_SEED].
 __global__ void __launch_bounds__(MF_THREADS) k_mf_classify(ShapeArrays sh, const uint32_t* __restrict__ pairs, uint64_t n,
                                                             uint32_t* __restrict__ recs, uint32_t* __restrict__ bins, uint64_t stride,
                                                             unsigned long long* __restrict__ ctr, uint32_t* __restrict__ err,
-                                                            const unsigned long long* __restrict__ d_n) {
+                                                            const unsigned long long* __restrict__ d_n, uint32_t* __restrict__ seed_list) {
   uint64_t k = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
   if (d_n && *d_n < n) n = *d_n;
   uint32_t kind = MK_KINDS;
+  bool seed = false;
   if (k < n) {
     Rec r{recs + (size_t)k * MF_WORDS};
     uint32_t a = pairs[2 * k], b = pairs[2 * k + 1];
@@ -1054,9 +1059,18 @@ __global__ void __launch_bounds__(MF_THREADS) k_mf_classify(ShapeArrays sh, cons
     } else {
       r.w[1] = PARRYGPU_OK;
       kind = manifold_kind(sh.types[a], sh.types[b]);
+      V3 n1;
+      seed = seed_list && kind >= MK_PFM && kind <= MK_PFM_TRIANGLE && !try_normalize(r.v(2), EPS, &n1);
     }
   }
   const uint32_t lane = threadIdx.x & 31;
+  if (seed_list) {
+    const uint32_t sm = __ballot_sync(0xffffffffu, seed);
+    unsigned long long sbase = 0;
+    if (sm && lane == 0) sbase = atomicAdd(&ctr[MF_CTR_SEED], (unsigned long long)__popc(sm));
+    sbase = __shfl_sync(0xffffffffu, sbase, 0);
+    if (seed) seed_list[sbase + __popc(sm & ((1u << lane) - 1))] = (uint32_t)k;
+  }
   uint32_t mask = __match_any_sync(0xffffffffu, kind);
   uint32_t leader = (uint32_t)__ffs(mask) - 1;
   unsigned long long base = 0;
@@ -1069,7 +1083,7 @@ template <uint32_t KIND>
 __global__ void __launch_bounds__(MF_THREADS) k_mf_kind(ShapeArrays sh, const uint32_t* __restrict__ pairs, float prediction,
                                                         uint32_t* __restrict__ recs, const uint32_t* __restrict__ bins, uint64_t stride,
                                                         unsigned long long* __restrict__ ctr, uint32_t* __restrict__ queue,
-                                                        uint32_t* __restrict__ err) {
+                                                        uint32_t* __restrict__ err, const float* __restrict__ init_dirs) {
   // The polyhedral kernel walks its five sub-bins as one index space: warps see one pair kind (but
   // at the bin boundaries), and one launch keeps the sub-bins' slowest pairs overlapped.
   constexpr uint32_t LAST = KIND == MK_PFM ? MK_PFM_TRIANGLE : KIND;
@@ -1126,14 +1140,18 @@ __global__ void __launch_bounds__(MF_THREADS) k_mf_kind(ShapeArrays sh, const ui
       }
     } else {
       if (!try_update_contacts(r, pos12, COS_1_DEGREES, 1.0e-6f)) {
-        // contact_manifold_pfm_pfm: GJK warm-started from the cached normal
+        // contact_manifold_pfm_pfm: GJK warm-started from the cached normal, else from the caller's
+        // (learned) direction, else the relative translation, else +x
         HullDev h1{}, h2{};
         load_hull(sh, a, &h1);
         load_hull(sh, b, &h2);
         float br1, br2;
         ShapeDev p1 = pfm_of(s1, &br1), p2 = pfm_of(s2, &br2);
         V3 dir;
-        if (!try_normalize(r.v(2), EPS, &dir) && !try_normalize(pos12.t, EPS, &dir)) dir = v3(1.f, 0.f, 0.f);
+        if (!try_normalize(r.v(2), EPS, &dir) &&
+            !(init_dirs && try_normalize(v3(init_dirs[3 * k], init_dirs[3 * k + 1], init_dirs[3 * k + 2]), EPS, &dir)) &&
+            !try_normalize(pos12.t, EPS, &dir))
+          dir = v3(1.f, 0.f, 0.f);
         float total_prediction = (prediction + br1) + br2;
         Simplex s;
         simplex_reset(s, cso_from_shapes(pos12, p1, p2, dir));
@@ -1235,15 +1253,17 @@ parrygpu_status pg::manifolds_reserve(parrygpu_ctx* ctx, uint64_t cap, MfScratch
 
 template <uint32_t KIND>
 static parrygpu_status launch_kind(parrygpu_ctx* ctx, const ShapeArrays& sh, const uint32_t* d_pairs, float prediction, uint32_t* d_recs,
-                                   MfScratch& sc, uint64_t stride, uint32_t grid) {
+                                   MfScratch& sc, uint64_t stride, uint32_t grid, const float* init_dirs = nullptr) {
   k_mf_kind<KIND><<<grid, MF_THREADS, 0, ctx->stream>>>(sh, d_pairs, prediction, d_recs, sc.bins.as<uint32_t>(), stride,
-                                                        sc.counters.as<unsigned long long>(), sc.queue.as<uint32_t>(), ctx->d_err);
+                                                        sc.counters.as<unsigned long long>(), sc.queue.as<uint32_t>(), ctx->d_err,
+                                                        init_dirs);
   PG_LAUNCHED(ctx);
   return PARRYGPU_OK;
 }
 
 parrygpu_status pg::launch_manifolds(parrygpu_ctx* ctx, const ShapeArrays& sh, const uint32_t* d_pairs, uint64_t cap,
-                                     const unsigned long long* d_count, float prediction, uint32_t* d_recs, MfScratch& sc) {
+                                     const unsigned long long* d_count, float prediction, uint32_t* d_recs, MfScratch& sc,
+                                     const float* init_dirs, const LearnedSeed* seed) {
   if (cap == 0) return PARRYGPU_OK;
   if (cap > sc.cap) return set_error(ctx, PARRYGPU_INVALID_ARG, "manifold scratch reserved for fewer pairs");
   const uint64_t stride = cap;
@@ -1254,15 +1274,19 @@ parrygpu_status pg::launch_manifolds(parrygpu_ctx* ctx, const ShapeArrays& sh, c
   unsigned long long* ctr = sc.counters.as<unsigned long long>();
   PG_CUDA(ctx, cudaMemsetAsync(ctr, 0, 128, ctx->stream));
   k_mf_classify<<<div_up(cap, MF_THREADS), MF_THREADS, 0, ctx->stream>>>(sh, d_pairs, cap, d_recs, sc.bins.as<uint32_t>(), stride, ctr,
-                                                                        ctx->d_err, d_count);
+                                                                        ctx->d_err, d_count, seed ? seed->list : nullptr);
   PG_LAUNCHED(ctx);
   parrygpu_status s;
+  if (seed) {  // the network's directions for the listed pairs, ahead of the polyhedral kernel
+    if ((s = launch_seed_dirs(ctx, sh, d_pairs, *seed, ctr + MF_CTR_SEED, cap)) != PARRYGPU_OK) return s;
+    init_dirs = seed->dirs;
+  }
   if ((s = launch_kind<MK_BALL_BALL>(ctx, sh, d_pairs, prediction, d_recs, sc, stride, grid)) != PARRYGPU_OK) return s;
   if ((s = launch_kind<MK_CUBOID_CUBOID>(ctx, sh, d_pairs, prediction, d_recs, sc, stride, grid)) != PARRYGPU_OK) return s;
   if ((s = launch_kind<MK_CAPSULE_CAPSULE>(ctx, sh, d_pairs, prediction, d_recs, sc, stride, grid)) != PARRYGPU_OK) return s;
   if ((s = launch_kind<MK_CONVEX_BALL>(ctx, sh, d_pairs, prediction, d_recs, sc, stride, grid)) != PARRYGPU_OK) return s;
   if ((s = launch_kind<MK_HULL_BALL>(ctx, sh, d_pairs, prediction, d_recs, sc, stride, grid)) != PARRYGPU_OK) return s;
-  if ((s = launch_kind<MK_PFM>(ctx, sh, d_pairs, prediction, d_recs, sc, stride, grid)) != PARRYGPU_OK) return s;
+  if ((s = launch_kind<MK_PFM>(ctx, sh, d_pairs, prediction, d_recs, sc, stride, grid, init_dirs)) != PARRYGPU_OK) return s;
   if ((s = launch_kind<MK_CUBOID_TRIANGLE>(ctx, sh, d_pairs, prediction, d_recs, sc, stride, grid)) != PARRYGPU_OK) return s;
   k_manifolds_epa<<<epa_blocks, MF_EPA_THREADS, 0, ctx->stream>>>(sh, d_pairs, prediction, d_recs, sc.queue.as<uint32_t>(), ctr,
                                                                  sc.epa_ws.as<uint32_t>(), ctr + 1, ctx->d_err);
@@ -1274,6 +1298,12 @@ extern "C" {
 
 parrygpu_status parrygpu_contact_manifolds(parrygpu_ctx* ctx, const parrygpu_shapes* shapes, const uint32_t* pairs, uint64_t n_pairs,
                                            float prediction, parrygpu_manifold* manifolds, parrygpu_gjk_stats* stats) {
+  return parrygpu_contact_manifolds_with_dirs(ctx, shapes, pairs, n_pairs, prediction, nullptr, manifolds, stats);
+}
+
+parrygpu_status parrygpu_contact_manifolds_with_dirs(parrygpu_ctx* ctx, const parrygpu_shapes* shapes, const uint32_t* pairs, uint64_t n_pairs,
+                                                     float prediction, const float* init_dirs, parrygpu_manifold* manifolds,
+                                                     parrygpu_gjk_stats* stats) {
   if (!ctx || !shapes) return PARRYGPU_INVALID_ARG;
   if (stats) std::memset(stats, 0, sizeof(*stats));
   if (n_pairs == 0) return PARRYGPU_OK;
@@ -1284,6 +1314,8 @@ parrygpu_status parrygpu_contact_manifolds(parrygpu_ctx* ctx, const parrygpu_sha
   if (s != PARRYGPU_OK) return s;
   const void* dp;
   if ((s = stage_input(ctx, ctx->stage_in[4], pairs, (size_t)n_pairs * 8, &dp)) != PARRYGPU_OK) return s;
+  const void* di = nullptr;
+  if (init_dirs && (s = stage_input(ctx, ctx->stage_in[5], init_dirs, (size_t)n_pairs * 12, &di)) != PARRYGPU_OK) return s;
   const size_t rec_bytes = (size_t)n_pairs * sizeof(parrygpu_manifold);
   // The records are read and written: host records go through a device copy and back.
   void* d_rec;
@@ -1294,7 +1326,8 @@ parrygpu_status parrygpu_contact_manifolds(parrygpu_ctx* ctx, const parrygpu_sha
   unsigned long long* ctr = ctx->mf.counters.as<unsigned long long>();  // [0] queue count, [1..3] stats
   {
     KernelTimer kt(ctx, "manifolds");
-    if ((s = launch_manifolds(ctx, sh, (const uint32_t*)dp, n_pairs, nullptr, prediction, (uint32_t*)d_rec, ctx->mf)) != PARRYGPU_OK)
+    if ((s = launch_manifolds(ctx, sh, (const uint32_t*)dp, n_pairs, nullptr, prediction, (uint32_t*)d_rec, ctx->mf, (const float*)di)) !=
+        PARRYGPU_OK)
       return s;
     kt.stop();
   }
@@ -1308,7 +1341,7 @@ parrygpu_status parrygpu_contact_manifolds(parrygpu_ctx* ctx, const parrygpu_sha
     stats->epa_calls = h[3];
   }
   bool staged_in = sh.types != shapes->types || sh.params != (const float4*)shapes->params || sh.poses != shapes->poses ||
-                   dp != pairs || (shapes->n_vertices && sh.pool != shapes->vertices);
+                   dp != pairs || (init_dirs && di != init_dirs) || (shapes->n_vertices && sh.pool != shapes->vertices);
   if (c_rec || stats || staged_in) return parrygpu_sync(ctx);
   return PARRYGPU_OK;
 }

@@ -15,6 +15,7 @@
 #include "internal.hpp"
 #include "common.cuh"
 #include "tcgen05.cuh"
+#include "contact_device.cuh"
 #include <cuda_bf16.h>
 #include <vector>
 #include <cmath>
@@ -279,7 +280,8 @@ __global__ void k_features_to_bf16(const float* __restrict__ f, size_t n, bf16* 
 // published rational approximation, gelu_as) and write the next layer's BF16 activations into
 // shared memory. The output layer's 3 columns are normalised
 // into the init direction (the fallback of k_normalize_dirs for degenerate outputs). Activations
-// never leave the SM.
+// never leave the SM. `d_count` (may be null) bounds the rows on the device (min(n, *d_count));
+// with `rows`, feature row k's direction goes to row rows[k] of `dirs`.
 constexpr int TC_GROUPS = 2;
 constexpr int TC_GROUP_THREADS = 256;
 constexpr int TC_THREADS = TC_GROUPS * TC_GROUP_THREADS;
@@ -327,8 +329,10 @@ __device__ __forceinline__ void group_sync(uint32_t g) { asm volatile("bar.sync 
 
 __global__ void __launch_bounds__(TC_THREADS, 1) k_mlp_infer_tc(const float* __restrict__ feat, uint64_t n, const bf16* __restrict__ wb,
                                                                 const float* __restrict__ wf, float* __restrict__ dirs,
-                                                                uint32_t* __restrict__ err) {
+                                                                uint32_t* __restrict__ err, const unsigned long long* __restrict__ d_count,
+                                                                const uint32_t* __restrict__ rows) {
   extern __shared__ __align__(1024) uint8_t tc_smem[];
+  if (d_count && *d_count < n) n = *d_count;
   float* bias = reinterpret_cast<float*>(tc_smem + TC_BIAS_OFF);
   uint64_t* bars = reinterpret_cast<uint64_t*>(tc_smem + TC_BAR_OFF);
   uint32_t* tslot = reinterpret_cast<uint32_t*>(tc_smem + TC_BAR_OFF + 16);
@@ -436,9 +440,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_mlp_infer_tc(const float* __r
             const float tt = dot(t, t);
             d = tt > 1.1920929e-7f * 1.1920929e-7f ? t / sqrtf(tt) : v3(1.f, 0.f, 0.f);
           }
-          dirs[3 * k] = d.x;
-          dirs[3 * k + 1] = d.y;
-          dirs[3 * k + 2] = d.z;
+          const uint64_t o = rows ? rows[k] : k;
+          dirs[3 * o] = d.x;
+          dirs[3 * o + 1] = d.y;
+          dirs[3 * o + 2] = d.z;
         }
       }
     }
@@ -562,12 +567,10 @@ __global__ void k_shape_desc(const uint32_t* __restrict__ types, const float4* _
 }
 
 // Pair features: relative pose of b in a's frame (quaternion with w >= 0, translation), desc(a), desc(b), zeros.
-__global__ void k_pair_features(const float* __restrict__ poses, const float* __restrict__ desc, const uint32_t* __restrict__ pairs, uint64_t n,
-                                uint64_t n_shapes, float* __restrict__ f) {
-  uint64_t k = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
-  if (k >= n) return;
-  uint32_t a = pairs[2 * k], b = pairs[2 * k + 1];
-  float* o = f + k * IN;
+// Row k describes pair k, or pair rows[k] when a row list is given; `d_count` (may be null) holds a
+// device-side row count: min(n, *d_count) rows.
+__device__ void pair_features(const float* __restrict__ poses, const float* __restrict__ desc, uint32_t a, uint32_t b, uint64_t n_shapes,
+                              float* __restrict__ o) {
   for (int j = 0; j < IN; ++j) o[j] = 0.0f;
   if (a >= n_shapes || b >= n_shapes) return;
   const float* pa = poses + 7 * (size_t)a;
@@ -584,6 +587,16 @@ __global__ void k_pair_features(const float* __restrict__ poses, const float* __
   o[0] = sgn * qi; o[1] = sgn * qj; o[2] = sgn * qk; o[3] = sgn * qw;
   o[4] = t.x; o[5] = t.y; o[6] = t.z;
   for (int j = 0; j < DESC; ++j) { o[7 + j] = desc[16 * (size_t)a + j]; o[7 + DESC + j] = desc[16 * (size_t)b + j]; }
+}
+
+__global__ void k_pair_features(const float* __restrict__ poses, const float* __restrict__ desc, const uint32_t* __restrict__ pairs, uint64_t n,
+                                uint64_t n_shapes, float* __restrict__ f, const uint32_t* __restrict__ rows,
+                                const unsigned long long* __restrict__ d_count) {
+  if (d_count && *d_count < n) n = *d_count;
+  for (uint64_t k = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; k < n; k += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t p = rows ? rows[k] : k;
+    pair_features(poses, desc, pairs[2 * p], pairs[2 * p + 1], n_shapes, f + k * IN);
+  }
 }
 
 uint64_t splitmix(uint64_t& s) {
@@ -698,6 +711,37 @@ parrygpu_status load_features(parrygpu_ctx* ctx, parrygpu_mlp* mlp, const float*
 
 }  // namespace
 
+// The frame pipeline's learned seeding: features of the listed pairs, then the fused tensor-core
+// inference writing each listed pair's row of the direction buffer.
+parrygpu_status pg::launch_seed_dirs(parrygpu_ctx* ctx, const ShapeArrays& sh, const uint32_t* d_pairs, const LearnedSeed& seed,
+                                     const unsigned long long* d_count, uint64_t cap) {
+  if (cap == 0) return PARRYGPU_OK;
+  const uint64_t sms = ctx->sm_count > 0 ? (uint64_t)ctx->sm_count : 152u;
+  const uint64_t fgrid = div_up(cap, 128) < sms * 16 ? div_up(cap, 128) : sms * 16;
+  k_pair_features<<<(uint32_t)fgrid, 128, 0, ctx->stream>>>(sh.poses, seed.desc, d_pairs, cap, sh.n_shapes, seed.feat, seed.list, d_count);
+  PG_LAUNCHED(ctx);
+  const uint64_t tiles = (cap + TC_M - 1) / TC_M;
+  k_mlp_infer_tc<<<(uint32_t)(tiles < sms ? tiles : sms), TC_THREADS, TC_SMEM, ctx->stream>>>(
+      seed.feat, cap, static_cast<const bf16*>(seed.wb), seed.wf, seed.dirs, ctx->d_err, d_count, seed.list);
+  PG_LAUNCHED(ctx);
+  return PARRYGPU_OK;
+}
+
+// Descriptors of the scene's shapes and a snapshot of the network's weights, once per
+// parrygpu_scene_set_mlp; also raises the inference kernel's shared-memory limit (outside any
+// graph capture).
+parrygpu_status pg::seed_prepare(parrygpu_ctx* ctx, const parrygpu_mlp* mlp, const ShapeArrays& sh, DevBuf& desc, DevBuf& wb, DevBuf& wf) {
+  PG_CUDA(ctx, cudaFuncSetAttribute(k_mlp_infer_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TC_SMEM));
+  PG_CUDA(ctx, desc.reserve(sh.n_shapes * 16 * 4));
+  PG_CUDA(ctx, wb.reserve(N_PARAMS * 2));
+  PG_CUDA(ctx, wf.reserve(N_PARAMS * 4));
+  k_shape_desc<<<div_up(sh.n_shapes * 32, 256), 256, 0, ctx->stream>>>(sh.types, sh.params, sh.pool, sh.n_shapes, sh.n_vertices, desc.as<float>());
+  PG_LAUNCHED(ctx);
+  PG_CUDA(ctx, cudaMemcpyAsync(wb.ptr, mlp->wb.ptr, N_PARAMS * 2, cudaMemcpyDeviceToDevice, ctx->stream));
+  PG_CUDA(ctx, cudaMemcpyAsync(wf.ptr, mlp->w.ptr, N_PARAMS * 4, cudaMemcpyDeviceToDevice, ctx->stream));
+  return PARRYGPU_OK;
+}
+
 extern "C" {
 
 uint64_t parrygpu_mlp_param_count(void) { return N_PARAMS; }
@@ -761,7 +805,7 @@ parrygpu_status parrygpu_mlp_features(parrygpu_ctx* ctx, const parrygpu_shapes* 
                                                                  desc.as<float>());
   PG_LAUNCHED(ctx);
   k_pair_features<<<div_up(n_pairs, 128), 128, 0, ctx->stream>>>((const float*)q, desc.as<float>(), (const uint32_t*)dp, n_pairs, shapes->n,
-                                                                 (float*)d_f);
+                                                                 (float*)d_f, nullptr, nullptr);
   PG_LAUNCHED(ctx);
   if (copy) PG_CUDA(ctx, cudaMemcpyAsync(features, d_f, n_pairs * IN * 4, cudaMemcpyDeviceToHost, ctx->stream));
   return parrygpu_sync(ctx);
@@ -824,7 +868,7 @@ parrygpu_status parrygpu_mlp_predict(parrygpu_ctx* ctx, const parrygpu_mlp* cmlp
     const uint32_t sms = ctx->sm_count > 0 ? (uint32_t)ctx->sm_count : 152u;
     const uint32_t grid = (uint32_t)(tiles < sms ? tiles : sms);
     k_mlp_infer_tc<<<grid, TC_THREADS, TC_SMEM, ctx->stream>>>((const float*)d_f, n, mlp->wb.as<bf16>(), mlp->w.as<float>(),
-                                                             (float*)d_dirs, ctx->d_err);
+                                                             (float*)d_dirs, ctx->d_err, nullptr, nullptr);
     PG_LAUNCHED(ctx);
   } else {  // per-layer mma.sync GEMMs (the training path's forward)
     for (uint64_t b0 = 0; b0 < n; b0 += chunk) {

@@ -8,7 +8,10 @@
 //   pairs               Bvh::traverse_bvtt_single_tree                      (bvh_traverse_bvtt.rs:19)
 //   k_carry_records     the narrow phase's per-pair manifold persistence: a pair found in the previous
 //                       frame keeps its ContactManifold, a new pair starts from ContactManifold::new()
-//   manifolds           contact_manifold_convex_convex per pair            (default_query_dispatcher.rs:749)
+//   manifolds           contact_manifold_convex_convex per pair            (default_query_dispatcher.rs:749);
+//                       with a network set (parrygpu_scene_set_mlp), the polyhedral pairs without a
+//                       cached normal start GJK from its predicted direction (listed, featurised and
+//                       inferred on the device inside the frame)
 //   rays                RayCast::cast_ray_and_get_normal on the shape set   (ray_composite_shape.rs:86-105)
 //
 // Everything stays on the device: the pair count lives in device memory and bounds the later kernels,
@@ -32,6 +35,8 @@ struct parrygpu_scene {
   MfScratch mf;  // narrow-phase scratch owned by the scene (stable for the graph)
   DevBuf rays, ray_order, ray_part, ray_toi, ray_nrm;  // rays stored in Morton order of their origins
   RayWaveScratch ray_wave;
+  DevBuf seed_desc, seed_wb, seed_wf, seed_feat, seed_list, seed_dirs;  // learned seeding (parrygpu_scene_set_mlp)
+  bool seeded = false;
   int cur = 0;
   uint64_t frame = 0;
   cudaGraphExec_t exec = nullptr;
@@ -205,8 +210,17 @@ static parrygpu_status scene_frame(parrygpu_ctx* ctx, parrygpu_scene* sc, float 
   }
   {
     KernelTimer kt(ctx, "scene_manifolds");
+    LearnedSeed seed;
+    if (sc->seeded) {
+      seed.desc = sc->seed_desc.as<float>();
+      seed.wb = sc->seed_wb.ptr;
+      seed.wf = sc->seed_wf.as<float>();
+      seed.feat = sc->seed_feat.as<float>();
+      seed.list = sc->seed_list.as<uint32_t>();
+      seed.dirs = sc->seed_dirs.as<float>();
+    }
     if ((s = launch_manifolds(ctx, sh, sc->pairs[nw].as<uint32_t>(), sc->cap, cnt + nw, sc->prediction, sc->recs[nw].as<uint32_t>(),
-                              sc->mf)) != PARRYGPU_OK)
+                              sc->mf, nullptr, sc->seeded ? &seed : nullptr)) != PARRYGPU_OK)
       return s;
     kt.stop();
   }
@@ -346,6 +360,7 @@ void parrygpu_scene_destroy(parrygpu_scene* sc) {
     d->release();
   for (int k = 0; k < 9; ++k) sc->poly[k].release();
   for (DevBuf* d : {&sc->ray_wave.cands, &sc->ray_wave.counter, &sc->ray_wave.keys, &sc->ray_wave.ovf}) d->release();
+  for (DevBuf* d : {&sc->seed_desc, &sc->seed_wb, &sc->seed_wf, &sc->seed_feat, &sc->seed_list, &sc->seed_dirs}) d->release();
   for (int b = 0; b < 2; ++b) {
     sc->pairs[b].release();
     sc->recs[b].release();
@@ -394,6 +409,23 @@ parrygpu_status parrygpu_scene_set_rays(parrygpu_ctx* ctx, parrygpu_scene* sc, c
   PG_CUDA(ctx, sc->ray_nrm.reserve(n_rays * 12 + 16));
   sc->n_rays = n_rays;
   sc->max_toi = max_toi;
+  return PARRYGPU_OK;
+}
+
+parrygpu_status parrygpu_scene_set_mlp(parrygpu_ctx* ctx, parrygpu_scene* sc, const parrygpu_mlp* mlp) {
+  if (!ctx || !sc) return PARRYGPU_INVALID_ARG;
+  PG_CUDA(ctx, cudaSetDevice(ctx->device));
+  PG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  drop_graph(sc);  // the captured frame bakes in whether (and with which buffers) pairs are seeded
+  sc->seeded = false;
+  if (!mlp) return PARRYGPU_OK;
+  PG_CUDA(ctx, sc->seed_feat.reserve(sc->cap * PARRYGPU_MLP_IN * 4));
+  PG_CUDA(ctx, sc->seed_list.reserve(sc->cap * 4));
+  PG_CUDA(ctx, sc->seed_dirs.reserve(sc->cap * 12));
+  parrygpu_status s = seed_prepare(ctx, mlp, scene_shapes(sc), sc->seed_desc, sc->seed_wb, sc->seed_wf);
+  if (s != PARRYGPU_OK) return s;
+  if ((s = parrygpu_sync(ctx)) != PARRYGPU_OK) return s;
+  sc->seeded = true;
   return PARRYGPU_OK;
 }
 
@@ -448,6 +480,25 @@ parrygpu_status parrygpu_scene_read(parrygpu_ctx* ctx, const parrygpu_scene* sc,
     if (ray_normal) PG_CUDA(ctx, cudaMemcpyAsync(ray_normal, sc->ray_nrm.ptr, sc->n_rays * 12, cudaMemcpyDefault, st));
   }
   return parrygpu_sync(ctx);
+}
+
+parrygpu_status parrygpu_scene_stats(parrygpu_ctx* ctx, const parrygpu_scene* sc, parrygpu_gjk_stats* stats, uint64_t* seeded_pairs) {
+  if (!ctx || !sc) return PARRYGPU_INVALID_ARG;
+  PG_CUDA(ctx, cudaSetDevice(ctx->device));
+  // the manifold counters block: [1..3] GJK iterations, EPA iterations, EPA calls; [15] seeded pairs
+  unsigned long long h[16] = {};
+  if (sc->frame > 0) {
+    PG_CUDA(ctx, cudaMemcpyAsync(h, sc->mf.counters.ptr, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream));
+  }
+  parrygpu_status s = parrygpu_sync(ctx);
+  if (stats) {
+    std::memset(stats, 0, sizeof(*stats));
+    stats->gjk_iterations = h[1];
+    stats->epa_iterations = h[2];
+    stats->epa_calls = h[3];
+  }
+  if (seeded_pairs) *seeded_pairs = sc->seeded ? h[15] : 0;
+  return s;
 }
 
 }  // extern "C"

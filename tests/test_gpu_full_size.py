@@ -6,7 +6,8 @@ restatement of parry3d on the same inputs:
 - learned warm start: the same 1,048,576 pairs started from the network's predicted directions,
   against the oracle given the same `init_dir`s (contact_support_map_support_map_with_params);
 - per-frame pipeline: 262,144 shapes and 4,194,304 rays, 3 frames: poses, pair sets, manifold
-  records and ray hits bit-exact.
+  records and ray hits bit-exact; and the same shapes with the network seeding new pairs, against
+  the oracle's frame loop given the network's directions.
 """
 import numpy as np
 import pytest
@@ -108,3 +109,34 @@ def test_frame_pipeline_full_size(gpu_ctx, oracle_lib):
     np.testing.assert_array_equal(got["ray_normal"], want["ray_normal"])
     print(f"\n{npairs} pairs, {int((n > 0).sum())} with contact points, "
           f"{int((want['ray_part'] != pg.NO_HIT).sum())} ray hits: identical to the oracle")
+
+
+def test_frame_pipeline_learned_seeding_full_size(gpu_ctx, oracle_lib):
+    """The same 262,144 shapes for 3 graph frames with the network seeding the pairs that hold no
+    cached normal: poses, pair sets and manifold records against the oracle's frame loop given the
+    network's directions for each frame's pairs (rays do not depend on the seeding and are left out)."""
+    from parry_gb300 import manifold as M
+    frames, pred, dt = 3, 0.1, 1.0 / 60.0
+    t, prm, pos, pool, poly, vel, _ = W.frame_scene(262144, 16, 400.0)
+    shapes = pg.ShapeSet.from_arrays(t, prm, pos, pool, poly)
+    mlp = pg.WarmStartMLP(gpu_ctx, seed=5)
+    sc = pg.Scene(gpu_ctx, shapes, vel, pred, 1 << 20)
+    sc.set_mlp(mlp)
+    sc.step(dt, frames, use_graph=True)
+    got = sc.read()
+    seeded = sc.stats()["seeded_pairs"]
+    sc.close()
+    want = oracle_lib.scene_frames(shapes, vel, pred, dt, frames,
+                                   dirs_fn=lambda s, p: mlp.predict(mlp.features(s, p)))
+    np.testing.assert_array_equal(got["poses"], want["poses"])
+    order = np.lexsort((got["pairs"][:, 1], got["pairs"][:, 0]))
+    np.testing.assert_array_equal(got["pairs"][order], want["pairs"])
+    gw = M.as_words(got["manifolds"])[order]
+    ww = want["manifolds"]
+    np.testing.assert_array_equal(gw[:, :8], ww[:, :8])
+    n = ww[:, 0].astype(np.int64)
+    valid = np.arange(M.MAX_POINTS)[None, :] < n[:, None]
+    np.testing.assert_array_equal(gw[:, 8:].reshape(len(gw), M.MAX_POINTS, 10)[valid],
+                                  ww[:, 8:].reshape(len(ww), M.MAX_POINTS, 10)[valid])
+    assert seeded > 0
+    print(f"\n{len(ww)} pairs, {seeded} seeded in the last frame: identical to the oracle")

@@ -207,3 +207,36 @@ def test_triangle_pairs_frames_bit_exact(gpu_ctx, oracle_lib):
         assert_records_equal(g, w)
         assert np.all(g["status"] == M.STATUS_OK)
         assert (g["n_points"] > 0).sum() > 200
+
+
+def test_with_dirs_bit_exact(gpu_ctx, oracle_lib):
+    """parrygpu_contact_manifolds_with_dirs against the oracle given the same directions, over frames
+    of a hull scene: unit directions, zero rows and NaN rows (neither normalises: the default start
+    stays). Pairs with a cached normal ignore their direction, so later frames use it only for the
+    pairs whose last update left no normal."""
+    import parry_gb300 as pg
+    from tests._contact_cases import hull_scene
+    O = oracle_lib
+    shapes0, q0 = hull_scene(1600, 5, extent=6.0)
+    pairs = brute_force_pairs(O.shape_aabbs(shapes0, 0.3))
+    rng = np.random.default_rng(5)
+    dirs = rng.normal(size=(len(pairs), 3)).astype(np.float32)
+    dirs /= np.linalg.norm(dirs, axis=1, keepdims=True)
+    dirs[::7] = 0.0
+    dirs[3::11] = np.nan
+    g, w, plain = M.new_manifolds(len(pairs)), M.new_manifolds(len(pairs)), M.new_manifolds(len(pairs))
+    for f in range(3):
+        shapes = shapes0.with_poses(moved_poses(q0, f, 305, step=0.02, angle=0.02))
+        st = pg.contact_manifolds(gpu_ctx, shapes, pairs, 0.05, g, want_stats=True, init_dirs=dirs)
+        sto = O.contact_manifolds(shapes, pairs, 0.05, M.as_words(w), init_dirs=dirs)
+        assert_records_equal(g, w)
+        assert np.all(g["status"] == M.STATUS_OK)
+        assert (st["gjk_iters"], st["epa_iters"], st["epa_calls"]) == (sto["gjk_iters"], sto["epa_iters"], sto["epa_calls"])
+        stp = pg.contact_manifolds(gpu_ctx, shapes, pairs, 0.05, plain, want_stats=True)
+        if f == 0:  # every record is new: the random starts change the GJK runs
+            assert stp["gjk_iters"] != st["gjk_iters"]
+    # zero directions everywhere are the plain call
+    z, p2 = M.new_manifolds(len(pairs)), M.new_manifolds(len(pairs))
+    pg.contact_manifolds(gpu_ctx, shapes, pairs, 0.05, z, init_dirs=np.zeros((len(pairs), 3), np.float32))
+    pg.contact_manifolds(gpu_ctx, shapes, pairs, 0.05, p2)
+    assert_records_equal(z, p2)

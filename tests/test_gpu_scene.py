@@ -109,3 +109,52 @@ def test_scene_mixed_eager_and_graph_frames(gpu_ctx):
     np.testing.assert_array_equal(pa, pb)
     _assert_records(wa, wb)
     np.testing.assert_array_equal(a["ray_part"], b["ray_part"])
+
+
+@pytest.mark.parametrize("use_graph,frames", [(False, 3), (True, 4)])
+def test_scene_learned_seeding_matches_oracle(gpu_ctx, oracle_lib, use_graph, frames):
+    """With a network set, the scene's polyhedral pairs without a cached normal start GJK from the
+    network's direction. The oracle's frame loop given the same directions (the network run on the
+    frame's pair features, as the scene runs it) reproduces every pose, pair and record bit for bit;
+    the seeded pairs are counted and change the GJK runs."""
+    import parry_gb300 as pg
+    O = oracle_lib
+    s, vel, rays = _inputs(600, 41)
+    pred, dt = 0.1, 1.0 / 60.0
+    mlp = pg.WarmStartMLP(gpu_ctx, seed=11)
+
+    def dirs_fn(shapes, pairs):
+        return mlp.predict(mlp.features(shapes, pairs))
+
+    sc = pg.Scene(gpu_ctx, s, vel, pred, 1 << 16)
+    sc.set_rays(rays, 100.0)
+    sc.set_mlp(mlp)
+    sc.step(dt, frames, use_graph=use_graph)
+    got = sc.read()
+    seeded = sc.stats()
+    sc.set_mlp(None)
+    sc.close()
+    want = O.scene_frames(s, vel, pred, dt, frames, rays=rays, max_toi=100.0, dirs_fn=dirs_fn)
+    np.testing.assert_array_equal(got["poses"], want["poses"])
+    gp, gw = _sorted_state(got)
+    assert len(want["pairs"]) > 500
+    np.testing.assert_array_equal(gp, want["pairs"])
+    _assert_records(gw, want["manifolds"])
+    np.testing.assert_array_equal(got["ray_part"], want["ray_part"])
+    assert seeded["seeded_pairs"] > 0
+    # the first frame seeds every polyhedral pair; the plain first frame differs in GJK iterations
+    runs = []
+    for with_mlp in (True, False):
+        sc = pg.Scene(gpu_ctx, s, vel, pred, 1 << 16)
+        if with_mlp:
+            sc.set_mlp(mlp)
+        sc.step(dt, 1, use_graph=False)
+        runs.append(sc.stats())
+        sc.close()
+    from parry_gb300.shapes import BALL, CUBOID, CAPSULE
+    t = s.arrays()[0]
+    pf = O.scene_frames(s, vel, pred, dt, 1)["pairs"]
+    ta, tb = t[pf[:, 0]], t[pf[:, 1]]
+    poly = (ta != BALL) & (tb != BALL) & ~((ta == tb) & ((ta == CUBOID) | (ta == CAPSULE)))
+    assert runs[0]["seeded_pairs"] == int(poly.sum()) > 0 and runs[1]["seeded_pairs"] == 0
+    assert runs[0]["gjk_iters"] != runs[1]["gjk_iters"]

@@ -313,3 +313,44 @@ def test_hull_manifolds_agree_with_contact_query(oracle_lib):
     for k in hb:
         f = rec[k]["points"]["fid1"][0] if t[pairs[k, 0]] == 3 else rec[k]["points"]["fid2"][0]
         assert (int(f) >> 30) in (1, 2, 3)
+
+
+def test_init_dirs_seed_only_records_without_a_normal(oracle_lib):
+    """init_dirs replaces the default GJK start (relative translation) only where a record holds no
+    cached normal: zero rows are the plain call; once every record has a normal, any directions give
+    the plain answer; on new records a start along the final direction shortens GJK and keeps the
+    contact decision."""
+    O = oracle_lib
+    t, p, q0 = primitive_scene(800, 3, extent=5.0)
+    shapes = ShapeSet.from_arrays(t, p, q0)
+    pairs = brute_force_pairs(O.shape_aabbs(shapes, 0.3))
+    ta, tb = t[pairs[:, 0]], t[pairs[:, 1]]
+    poly = (ta != BALL) & (tb != BALL) & ~((ta == tb) & ((ta == CUBOID) | (ta == CAPSULE)))
+    pairs = pairs[poly]
+    assert len(pairs) > 200
+    k = len(pairs)
+    plain, zero = M.new_manifolds(k), M.new_manifolds(k)
+    st_p = O.contact_manifolds(shapes, pairs, 0.05, M.as_words(plain))
+    st_z = O.contact_manifolds(shapes, pairs, 0.05, M.as_words(zero), init_dirs=np.zeros((k, 3), np.float32))
+    np.testing.assert_array_equal(M.as_words(plain), M.as_words(zero))
+    assert st_p == st_z
+    # warm records: a normal is cached for every pair with points, so random directions change nothing there
+    has_n = np.linalg.norm(plain["local_n1"], axis=1) > 1e-3
+    rng = np.random.default_rng(0)
+    rnd = rng.normal(size=(k, 3)).astype(np.float32)
+    moved = shapes.with_poses(moved_poses(q0, 1, 9, step=0.01, angle=0.01))
+    a, b = plain.copy(), plain.copy()
+    O.contact_manifolds(moved, pairs, 0.05, M.as_words(a))
+    O.contact_manifolds(moved, pairs, 0.05, M.as_words(b), init_dirs=rnd)
+    np.testing.assert_array_equal(M.as_words(a)[has_n], M.as_words(b)[has_n])
+    # new records started along the plain run's final normal: the directions are used (the GJK runs
+    # change) and the contact decisions are the plain ones
+    sub = pairs[has_n]
+    base, seeded = M.new_manifolds(len(sub)), M.new_manifolds(len(sub))
+    st_b = O.contact_manifolds(shapes, sub, 0.05, M.as_words(base))
+    st_s = O.contact_manifolds(shapes, sub, 0.05, M.as_words(seeded), init_dirs=np.ascontiguousarray(plain["local_n1"][has_n]))
+    assert st_s["gjk_iters"] != st_b["gjk_iters"]
+    np.testing.assert_array_equal(seeded["n_points"] > 0, base["n_points"] > 0)
+    touching = base["n_points"] > 0  # (a pair beyond the prediction keeps whichever separating axis GJK stopped at)
+    assert touching.sum() > 100
+    np.testing.assert_allclose(seeded["local_n1"][touching], base["local_n1"][touching], atol=2e-3)
