@@ -195,7 +195,9 @@ __device__ __forceinline__ V3 project_segment(V3 a, V3 b, V3 pt, Loc* loc) {
   return a + ab * u;
 }
 
-static __device__ __noinline__ V3 project_triangle(V3 a, V3 b, V3 c, V3 pt, Loc* loc) {
+// The triangle and tetrahedron projections have an inline body for kernels that keep their simplex
+// in registers, and an out-of-line copy that the other kernels share.
+__device__ __forceinline__ V3 project_triangle_inl(V3 a, V3 b, V3 c, V3 pt, Loc* loc) {
   V3 ab = b - a, ac = c - a, ap = pt - a;
   float ab_ap = dot(ab, ap), ac_ap = dot(ac, ap);
   if (ab_ap <= 0.0f && ac_ap <= 0.0f) { *loc = Loc{LOC_VERTEX, 0, {1.f, 0.f, 0.f}}; return a; }
@@ -236,6 +238,8 @@ static __device__ __noinline__ V3 project_triangle(V3 a, V3 b, V3 c, V3 pt, Loc*
   return pt;
 }
 
+static __device__ __noinline__ V3 project_triangle(V3 a, V3 b, V3 c, V3 pt, Loc* loc) { return project_triangle_inl(a, b, c, pt, loc); }
+
 __device__ __forceinline__ bool tet_edge(int i, V3 a, V3 nabc, V3 nabd, V3 ap, V3 ab, float ap_ab, float bp_ab, float* dabc,
                                          float* dabd, V3* res, Loc* loc) {
   float ab_ab = ap_ab - bp_ab;
@@ -273,7 +277,7 @@ __device__ __forceinline__ bool tet_face(int i, V3 a, V3 b, V3 c, V3 ap, V3 bp, 
   return false;
 }
 
-static __device__ __noinline__ V3 project_tetrahedron(V3 a, V3 b, V3 c, V3 d, V3 pt, Loc* loc) {
+__device__ __forceinline__ V3 project_tetrahedron_inl(V3 a, V3 b, V3 c, V3 d, V3 pt, Loc* loc) {
   V3 ab = b - a, ac = c - a, ad = d - a, ap = pt - a;
   float ap_ab = dot(ap, ab), ap_ac = dot(ap, ac), ap_ad = dot(ap, ad);
   if (ap_ab <= 0.0f && ap_ac <= 0.0f && ap_ad <= 0.0f) { *loc = Loc{LOC_VERTEX, 0, {1.f, 0.f, 0.f}}; return a; }
@@ -303,6 +307,10 @@ static __device__ __noinline__ V3 project_tetrahedron(V3 a, V3 b, V3 c, V3 d, V3
   if (tet_face(3, b, c, d, bp, cp, dp, bc, bd, -ab, dbcd, dcdb, dbdc, &res, loc)) return res;
   *loc = Loc{LOC_SOLID, 0, {0.f, 0.f, 0.f}};
   return pt;
+}
+
+static __device__ __noinline__ V3 project_tetrahedron(V3 a, V3 b, V3 c, V3 d, V3 pt, Loc* loc) {
+  return project_tetrahedron_inl(a, b, c, d, pt, loc);
 }
 
 // ---------------- Voronoi simplex ----------------

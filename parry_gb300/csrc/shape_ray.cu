@@ -194,6 +194,195 @@ __device__ __forceinline__ bool ray_support_map(const ShapeDev& shape, V3 o, V3 
   return true;
 }
 
+// ---- the GJK ray cast with its simplex in registers, for one support-map kind ----
+// gjk_cast_local_ray keeps its Voronoi simplex in an array indexed at run time (local memory, and
+// witness points the ray cast never reads). The candidate kernels run one shape kind per launch,
+// so the cast below is inlined with that kind's support function, and its simplex keeps only the
+// four vertex positions, moved with constant indices. Every value is computed as in
+// gjk_cast_local_ray / simplex_project_origin_and_reduce / simplex_add, so the answers are the same.
+struct RaySimplex {
+  V3 v0, v1, v2, v3;
+  int dim;
+};
+
+__device__ __forceinline__ V3 rs_vertex(const RaySimplex& s, int i) { return i == 0 ? s.v0 : (i == 1 ? s.v1 : (i == 2 ? s.v2 : s.v3)); }
+
+// VoronoiSimplex::project_origin_and_reduce: the projection of the origin; the vertices of the
+// feature that holds it move to the front (in the order the index swaps of the array form leave
+// them), and dim shrinks to that feature's.
+__device__ __forceinline__ V3 rs_project_origin_and_reduce(RaySimplex& s) {
+  const V3 o = v3(0.f, 0.f, 0.f);
+  Loc loc;
+  if (s.dim == 0) return s.v0;
+  if (s.dim == 1) {
+    V3 p = project_segment(s.v0, s.v1, o, &loc);
+    if (loc.kind == LOC_VERTEX) {
+      if (loc.id != 0) s.v0 = s.v1;
+      s.dim = 0;
+    }
+    return p;
+  }
+  if (s.dim == 2) {
+    V3 p = project_triangle_inl(s.v0, s.v1, s.v2, o, &loc);
+    if (loc.kind == LOC_VERTEX) {
+      s.v0 = rs_vertex(s, loc.id);
+      s.dim = 0;
+    } else if (loc.kind == LOC_EDGE) {
+      if (loc.id == 1) s.v0 = s.v2;       // swap(0, 2): (v2, v1)
+      else if (loc.id == 2) s.v1 = s.v2;  // swap(1, 2): (v0, v2)
+      s.dim = 1;
+    }
+    return p;
+  }
+  V3 p = project_tetrahedron_inl(s.v0, s.v1, s.v2, s.v3, o, &loc);
+  if (loc.kind == LOC_VERTEX) {
+    s.v0 = rs_vertex(s, loc.id);
+    s.dim = 0;
+  } else if (loc.kind == LOC_EDGE) {
+    const V3 a = s.v0, b = s.v1, c = s.v2, d = s.v3;
+    switch (loc.id) {
+      case 1: s.v1 = c; break;             // swap(1, 2)
+      case 2: s.v1 = d; break;             // swap(1, 3)
+      case 3: s.v0 = c; break;             // swap(0, 2)
+      case 4: s.v0 = d; break;             // swap(0, 3)
+      case 5: s.v0 = c; s.v1 = d; break;   // swap(0, 2), swap(1, 3)
+      default: s.v0 = a; s.v1 = b; break;
+    }
+    s.dim = 1;
+  } else if (loc.kind == LOC_FACE) {
+    if (loc.id == 1) s.v2 = s.v3;
+    else if (loc.id == 2) s.v1 = s.v3;
+    else if (loc.id == 3) s.v0 = s.v3;
+    s.dim = 2;
+  }
+  return p;
+}
+
+// VoronoiSimplex::add_point: refused (simplex unchanged) when the point is affinely dependent.
+__device__ __forceinline__ void rs_add(RaySimplex& s, V3 pt) {
+  if (s.dim == 0) {
+    V3 d = s.v0 - pt;
+    if (dot(d, d) < GJK_EPS_TOL) return;
+  } else if (s.dim == 1) {
+    V3 ab = s.v1 - s.v0, ac = pt - s.v0;
+    V3 c = cross(ab, ac);
+    if (dot(c, c) < GJK_EPS_TOL) return;
+  } else if (s.dim == 2) {
+    V3 ab = s.v1 - s.v0, ac = s.v2 - s.v0, ap = pt - s.v0;
+    V3 n = normalize(cross(ab, ac));
+    if (fabsf(dot(n, ap)) < GJK_EPS_TOL) return;
+  }
+  s.dim += 1;
+  if (s.dim == 1) s.v1 = pt;
+  else if (s.dim == 2) s.v2 = pt;
+  else s.v3 = pt;
+}
+
+// Support of one kind: TY = SH_CAPSULE (O(1)) or SH_CONVEX (vertex scan).
+template <uint32_t TY>
+__device__ __forceinline__ V3 kind_support(const ShapeDev& s, V3 dir) {
+  if constexpr (TY == SH_CAPSULE) {
+    V3 d;
+    if (!try_normalize(dir, 0.0f, &d)) d = v3(0.f, 1.f, 0.f);
+    V3 a = v3(0.f, -s.a, 0.f), b = v3(0.f, s.a, 0.f);
+    if (dot(d, a) > dot(d, b)) return a + d * s.b;
+    return b + d * s.b;
+  } else {
+    return convex_support(s.pts, s.npts, dir);
+  }
+}
+
+// gjk.rs:660-795 minkowski_ray_cast, as gjk_cast_local_ray, for one support kind.
+template <uint32_t TY>
+__device__ __forceinline__ bool gjk_cast_local_ray_kind(const ShapeDev& shape, V3 ro, V3 rd, float max_toi, float* toi_out, V3* n_out) {
+  const float eps_tol = GJK_EPS_TOL;
+  const float eps_rel = sqrtf(eps_tol);
+  float ray_length = norm(rd);
+  if (fabsf(ray_length) <= EPS) return false;
+  float ltoi = 0.0f;
+  V3 co = ro, cd = rd / ray_length;
+  V3 dir = -cd;
+  V3 ldir = dir;
+  RaySimplex s;
+  s.v0 = kind_support<TY>(shape, dir) - co;
+  s.dim = 0;
+  V3 proj = rs_project_origin_and_reduce(s);
+  float max_bound = FLT_MAX;
+  int niter = 0;
+  bool last_chance = false;
+  for (;;) {
+    float old_max_bound = max_bound;
+    float nb;
+    V3 u;
+    if (try_normalize(-proj, eps_tol, &u, &nb)) { dir = u; max_bound = nb; }
+    else { *toi_out = ltoi / ray_length; *n_out = ldir; return true; }
+    V3 sp;
+    if (max_bound >= old_max_bound) {
+      last_chance = true;
+      sp = proj + co;
+    } else {
+      sp = kind_support<TY>(shape, dir);
+    }
+    if (last_chance && ltoi > 0.0f) { *toi_out = ltoi / ray_length; *n_out = ldir; return true; }
+    float t;
+    if (ray_halfspace(sp, dir, co, cd, &t)) {
+      if (dot(dir, cd) < 0.0f && t > 0.0f) {
+        ldir = dir;
+        ltoi += t;
+        if (ltoi / ray_length > max_toi) return false;
+        V3 shift = cd * t;
+        co = co + shift;
+        max_bound = FLT_MAX;
+        const V3 ns = -shift;
+        s.v0 = s.v0 + ns;
+        if (s.dim >= 1) s.v1 = s.v1 + ns;
+        if (s.dim >= 2) s.v2 = s.v2 + ns;
+        if (s.dim >= 3) s.v3 = s.v3 + ns;
+        last_chance = false;
+      }
+    } else {
+      if (dot(dir, cd) > eps_tol) return false;
+    }
+    if (last_chance) return false;
+    float min_bound = -dot(dir, sp - co);
+    if (max_bound - min_bound <= eps_rel * max_bound) return false;
+    rs_add(s, sp - co);
+    proj = rs_project_origin_and_reduce(s);
+    if (s.dim == 3) {
+      if (min_bound >= eps_tol) return false;
+      *toi_out = ltoi / ray_length; *n_out = ldir; return true;
+    }
+    niter += 1;
+    if (niter == 100) return false;
+  }
+}
+
+// ray_support_map.rs:19-71 for one support kind, in the part's frame after the pose, as part_cast_ray.
+template <uint32_t TY>
+__device__ __forceinline__ bool part_cast_ray_kind(const ShapeDev& shape, const Pose& pose, V3 wo, V3 wd, float max_toi, bool solid, float* toi,
+                                                   V3* n) {
+  V3 o = pose_inv_point(pose, wo), d = pose_inv_rotate(pose, wd);
+  float t;
+  V3 nn;
+  if (!gjk_cast_local_ray_kind<TY>(shape, o, d, max_toi, &t, &nn)) return false;
+  if (!(solid || t != 0.0f)) {
+    V3 ndir = normalize(d);
+    V3 supp = kind_support<TY>(shape, ndir);
+    float eps = 0.001f;
+    float shift = dot(supp - o, ndir) + eps;
+    float t2;
+    V3 n2;
+    if (!gjk_cast_local_ray_kind<TY>(shape, o + ndir * shift, -d, shift + eps, &t2, &n2)) return false;
+    float tt = shift - t2;
+    if (!(tt <= max_toi)) return false;
+    t = tt;
+    nn = -n2;
+  }
+  *toi = t;
+  *n = pose_rotate(pose, nn);
+  return true;
+}
+
 // ray_triangle.rs:49-152 (toi <= max_toi filter), normal facing the ray origin
 __device__ __forceinline__ bool ray_triangle(V3 a, V3 b, V3 c, V3 o, V3 dir, float max_toi, float* toi, V3* nrm) {
   V3 ab = b - a, ac = c - a;
@@ -608,41 +797,42 @@ __global__ void __launch_bounds__(128) k_rays_wave(const WideNode* __restrict__ 
   }
 }
 
-// One candidate: the GJK ray cast unless its box entry lies beyond the ray's current best (a later
-// hit cannot win; an entry equal to the best may still tie with a lower index).
-__device__ __forceinline__ void run_candidate(const CompoundDev& cd, const float* rays, float max_toi, int solid, int has_pose, const Pose& cpose,
-                                              const uint32_t* order, int permuted, RayCand* e, unsigned long long* keys) {
-  RayCand c = *e;
-  if (c.part == 0xffffffffu || c.tmin > key_toi(keys[c.r])) return;
-  uint32_t r;
-  V3 o, dir;
-  ray_of(rays, order, permuted, c.k, has_pose, cpose, &r, &o, &dir);
-  ShapeDev s = load_shape(cd.types, cd.params, cd.pool, c.part);
-  Pose p = load_pose(cd.poses, c.part);
-  float t;
-  V3 nn;
-  // composite casts keep hits strictly below max_toi (CompositeShapeRef::cast_local_ray)
-  if (!part_cast_ray(s, p, o, dir, max_toi, solid != 0, &t, &nn) || !(t < max_toi)) return;
-  if (has_pose) nn = pose_rotate(cpose, nn);
-  e->hit = 1u;
-  e->t = t;
-  e->nx = nn.x;
-  e->ny = nn.y;
-  e->nz = nn.z;
-  atomicMin(&keys[r], hit_key(t, c.part));
-}
-
-// Grid-stride over the entries of a two-ended list of capacity `cap` (fail may be null).
-__global__ void __launch_bounds__(128) k_rays_cand(CompoundDev cd, const float* __restrict__ rays, float max_toi, int solid, int has_pose,
-                                                   Pose cpose, const uint32_t* __restrict__ order, int permuted, RayCand* __restrict__ list,
-                                                   unsigned long long cap, const unsigned long long* __restrict__ count,
-                                                   const unsigned long long* __restrict__ fail, unsigned long long* __restrict__ keys) {
+// One end of a two-ended list: TY = SH_CAPSULE runs the front (capsule candidates), SH_CONVEX the
+// back (the other support-map kinds; a part that is not a convex hull takes part_cast_ray).
+template <uint32_t TY>
+__global__ void __launch_bounds__(128, 4) k_rays_cand_kind(CompoundDev cd, const float* __restrict__ rays, float max_toi, int solid, int has_pose,
+                                                        Pose cpose, const uint32_t* __restrict__ order, int permuted,
+                                                        RayCand* __restrict__ list, unsigned long long cap,
+                                                        const unsigned long long* __restrict__ count,
+                                                        const unsigned long long* __restrict__ fail, unsigned long long* __restrict__ keys) {
   unsigned long long front, back;
   list_extent(count, fail, &front, &back);
-  const unsigned long long m = front + back;
+  const unsigned long long m = TY == SH_CAPSULE ? front : back;
   for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < m;
-       i += (unsigned long long)gridDim.x * blockDim.x)
-    run_candidate(cd, rays, max_toi, solid, has_pose, cpose, order, permuted, list + list_slot(i, front, cap), keys);
+       i += (unsigned long long)gridDim.x * blockDim.x) {
+    RayCand* e = list + (TY == SH_CAPSULE ? i : cap - 1ull - i);
+    RayCand c = *e;
+    if (c.part == 0xffffffffu || c.tmin > key_toi(keys[c.r])) continue;
+    uint32_t r;
+    V3 o, dir;
+    ray_of(rays, order, permuted, c.k, has_pose, cpose, &r, &o, &dir);
+    ShapeDev sh = load_shape(cd.types, cd.params, cd.pool, c.part);
+    Pose p = load_pose(cd.poses, c.part);
+    float t;
+    V3 nn;
+    bool ok;
+    if (TY == SH_CAPSULE || sh.type == SH_CONVEX) ok = part_cast_ray_kind<TY>(sh, p, o, dir, max_toi, solid != 0, &t, &nn);
+    else ok = part_cast_ray(sh, p, o, dir, max_toi, solid != 0, &t, &nn);
+    // composite casts keep hits strictly below max_toi (CompositeShapeRef::cast_local_ray)
+    if (!ok || !(t < max_toi)) continue;
+    if (has_pose) nn = pose_rotate(cpose, nn);
+    e->hit = 1u;
+    e->t = t;
+    e->nx = nn.x;
+    e->ny = nn.y;
+    e->nz = nn.z;
+    atomicMin(&keys[r], hit_key(t, c.part));
+  }
 }
 
 __global__ void __launch_bounds__(128) k_rays_finish(const RayCand* __restrict__ list, unsigned long long cap,
@@ -697,11 +887,18 @@ static parrygpu_status launch_wave(parrygpu_ctx* ctx, const WideNode* wide, Comp
   k_rays_wave<<<div_up(n, 128), 128, 0, ctx->stream>>>(wide, cd, d_rays, n, max_toi, solid, has_pose, pose, d_part, d_toi, d_nrm, ctx->d_err,
                                                        order, permuted, wb);
   PG_LAUNCHED(ctx);
-  k_rays_cand<<<grid, 128, 0, ctx->stream>>>(cd, d_rays, max_toi, solid, has_pose, pose, order, permuted, wb.a, n, cnt + 1, nullptr,
-                                             wb.keys);
+  // list A, then list B; capsules and hulls of each in their own launches
+  k_rays_cand_kind<SH_CAPSULE><<<grid, 128, 0, ctx->stream>>>(cd, d_rays, max_toi, solid, has_pose, pose, order, permuted, wb.a, n, cnt + 1,
+                                                              nullptr, wb.keys);
   PG_LAUNCHED(ctx);
-  k_rays_cand<<<grid, 128, 0, ctx->stream>>>(cd, d_rays, max_toi, solid, has_pose, pose, order, permuted, wb.b, sc.cap, cnt, cnt + 2,
-                                             wb.keys);
+  k_rays_cand_kind<SH_CONVEX><<<grid, 128, 0, ctx->stream>>>(cd, d_rays, max_toi, solid, has_pose, pose, order, permuted, wb.a, n, cnt + 1,
+                                                             nullptr, wb.keys);
+  PG_LAUNCHED(ctx);
+  k_rays_cand_kind<SH_CAPSULE><<<grid, 128, 0, ctx->stream>>>(cd, d_rays, max_toi, solid, has_pose, pose, order, permuted, wb.b, sc.cap, cnt,
+                                                              cnt + 2, wb.keys);
+  PG_LAUNCHED(ctx);
+  k_rays_cand_kind<SH_CONVEX><<<grid, 128, 0, ctx->stream>>>(cd, d_rays, max_toi, solid, has_pose, pose, order, permuted, wb.b, sc.cap, cnt,
+                                                             cnt + 2, wb.keys);
   PG_LAUNCHED(ctx);
   k_rays_finish<<<grid, 128, 0, ctx->stream>>>(wb.a, n, cnt + 1, nullptr, wb.keys, d_part, d_toi, d_nrm);
   PG_LAUNCHED(ctx);
