@@ -82,6 +82,12 @@ typedef struct parrygpu_config {
   uint32_t mlp_infer;      /* parrygpu_mlp_predict: 1 = one fused kernel on the fifth-generation tensor
                               cores (tcgen05.mma into TMEM, weights resident in shared memory); 2 = the
                               training path's per-layer mma.sync GEMMs; 0 = library default (1) */
+  uint32_t scene_ray_order; /* parrygpu_scene: the order the rays are stored and cast in (answers keep the
+                              input order): 1 = Morton code of the origin; 2 = direction octant above
+                              it; 3 = direction octant and dominant axis above it; 0 = library default */
+  uint32_t scene_ray_grid; /* parrygpu_scene rays: 1 = walk a uniform grid over the shapes, rebuilt each
+                              frame (falls back to the BVH on the device when its entries outgrow their
+                              capacity); 2 = traverse the BVH; 0 = library default (1). Same answers. */
 } parrygpu_config;
 
 /* ---- context ---------------------------------------------------------------------------- */

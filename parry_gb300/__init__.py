@@ -79,7 +79,9 @@ def _config_dict(cfg) -> dict:
     return {"device": cfg.device, "ray_block": cfg.ray_block, "sort_rays": bool(cfg.sort_rays), "ray_sort_key": cfg.ray_sort_key,
             "epa_blocks_per_sm": cfg.epa_blocks_per_sm, "ray_traversal": cfg.ray_traversal, "ray_refill": cfg.ray_refill, "ray_chunks": cfg.ray_chunks,
             "ray_host_access": cfg.ray_host_access, "contact_warp_cost": cfg.contact_warp_cost,
-            "contact_epa_inline": cfg.contact_epa_inline, "mlp_infer": cfg.mlp_infer}
+            "contact_epa_inline": cfg.contact_epa_inline, "mlp_infer": cfg.mlp_infer,
+            "scene_ray_order": cfg.scene_ray_order,
+            "scene_ray_grid": cfg.scene_ray_grid}
 
 
 class Context:
@@ -88,7 +90,8 @@ class Context:
     def __init__(self, device: int = 0, ray_block: int = 0, sort_rays: bool = True, ray_sort_key: int = 0,
                  epa_blocks_per_sm: int = 0, ray_traversal: int = 0, ray_refill: int = 0, ray_chunks: int = 0,
                  ray_host_access: int = 0, contact_warp_cost: int = 0, contact_epa_inline: int = 0,
-                 mlp_infer: int = 0):
+                 mlp_infer: int = 0, scene_ray_order: int = 0,
+                 scene_ray_grid: int = 0):
         cfg = _capi.ParryGpuConfig()
         lib().parrygpu_default_config(C.byref(cfg))
         cfg.device = device
@@ -103,6 +106,8 @@ class Context:
         cfg.contact_warp_cost = contact_warp_cost
         cfg.contact_epa_inline = contact_epa_inline
         cfg.mlp_infer = mlp_infer
+        cfg.scene_ray_order = scene_ray_order
+        cfg.scene_ray_grid = scene_ray_grid
         h = C.c_void_p()
         check(lib().parrygpu_create(C.byref(h), C.byref(cfg)))
         self._h = h

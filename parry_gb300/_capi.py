@@ -142,7 +142,9 @@ class ParryGpuConfig(C.Structure):
     _fields_ = [("device", C.c_int), ("ray_block", C.c_uint32), ("sort_rays", C.c_uint32), ("ray_sort_key", C.c_uint32),
                 ("epa_blocks_per_sm", C.c_uint32), ("ray_traversal", C.c_uint32), ("ray_refill", C.c_uint32),
                 ("ray_chunks", C.c_uint32), ("ray_host_access", C.c_uint32), ("contact_warp_cost", C.c_uint32),
-                ("contact_epa_inline", C.c_uint32), ("mlp_infer", C.c_uint32)]
+                ("contact_epa_inline", C.c_uint32), ("mlp_infer", C.c_uint32),
+                ("scene_ray_order", C.c_uint32),
+                ("scene_ray_grid", C.c_uint32)]
 
 
 _lib = None

@@ -97,7 +97,9 @@ parrygpu_status parrygpu_create(parrygpu_ctx** out, const parrygpu_config* cfg) 
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) { cudaGetLastError(); return PARRYGPU_NO_DEVICE; }
   if (cfg && ((cfg->ray_block % 32) != 0 || cfg->ray_block > 1024 || cfg->ray_sort_key > 2 || cfg->epa_blocks_per_sm > 32 ||
               cfg->ray_traversal > 3 || cfg->ray_refill > 32 || cfg->ray_chunks > 64 || cfg->ray_host_access > 2 ||
-              (cfg->contact_warp_cost != 0 && cfg->contact_warp_cost < 2) || cfg->contact_epa_inline > 2 || cfg->mlp_infer > 2))
+              (cfg->contact_warp_cost != 0 && cfg->contact_warp_cost < 2) || cfg->contact_epa_inline > 2 || cfg->mlp_infer > 2 ||
+              cfg->scene_ray_order > 3 ||
+              cfg->scene_ray_grid > 2))
     return PARRYGPU_INVALID_ARG;
   parrygpu_ctx* ctx = new parrygpu_ctx();
   if (cfg) ctx->cfg = *cfg; else parrygpu_default_config(&ctx->cfg);
@@ -134,7 +136,7 @@ void parrygpu_destroy(parrygpu_ctx* ctx) {
   ctx->epa_ws.release();
   ctx->epa_ws_big.release();
   ctx->ct_ovf.release();
-  for (DevBuf* d : {&ctx->mf.queue, &ctx->mf.counters, &ctx->mf.bins, &ctx->mf.epa_ws}) d->release();
+  for (DevBuf* d : {&ctx->mf.queue, &ctx->mf.counters, &ctx->mf.bins, &ctx->mf.epa_ws, &ctx->mf.redo}) d->release();
   for (DevBuf* d : {&ctx->ray_wave.cands, &ctx->ray_wave.counter, &ctx->ray_wave.keys, &ctx->ray_wave.ovf}) d->release();
   if (ctx->d_err) cudaFree(ctx->d_err);
   if (ctx->h_err) cudaFreeHost(ctx->h_err);

@@ -41,10 +41,19 @@ struct RayWaveScratch {
   uint64_t cap = 0;
 };
 
+// A uniform grid over a shape set's AABBs, rebuilt on the device each frame (shape_ray.cu): cell
+// ranges into the entry array (shape indices), the grid's placement (from the BVH root box), its
+// resolution (fixed when the scratch is reserved) and the entry capacity.
+struct RayGridScratch {
+  DevBuf dev, starts, cursor, entries, sums;
+  uint32_t res[3] = {0, 0, 0};
+  uint64_t cells = 0, cap = 0;
+};
+
 // Scratch of the contact-manifold kernels (manifold.cu): EPA queue, counters (queue length, stats,
 // bin lengths), per-kind pair bins, per-slot EPA polytope workspaces.
 struct MfScratch {
-  DevBuf queue, counters, bins, epa_ws;
+  DevBuf queue, counters, bins, epa_ws, redo;
   uint64_t cap = 0;
 };
 
@@ -166,6 +175,10 @@ parrygpu_status radix_sort_pairs_in(parrygpu_ctx* ctx, uint32_t n, int key_bits,
 uint32_t radix_sort_hist_entries(uint32_t n);
 // In-place exclusive prefix sum of m words (buffer padded to a multiple of 4 words with zeros).
 parrygpu_status exclusive_scan_u32(parrygpu_ctx* ctx, uint32_t* data, uint32_t m);
+// The same over many blocks for long arrays (tile sums, one-block scan of the sums, tile scans);
+// `sums` holds exclusive_scan_u32_sums(m) words. No allocation, no host synchronisation.
+uint32_t exclusive_scan_u32_sums(uint32_t m);
+parrygpu_status exclusive_scan_u32_wide(parrygpu_ctx* ctx, uint32_t* data, uint32_t m, uint32_t* sums);
 
 // ---- ray casts (ray.cu): launch helpers on caller-provided device buffers (no allocation) ----
 // Key width (bits) of the ray ordering for the context's ray_sort_key mode.
@@ -198,7 +211,11 @@ parrygpu_status launch_hull_boxes(parrygpu_ctx* ctx, const uint32_t* types, cons
                                   uint64_t n_vertices, float* box);
 parrygpu_status launch_shape_rays(parrygpu_ctx* ctx, const parrygpu_bvh* bvh, const uint32_t* types, const float* params,
                                   const float* poses, const float* pool, const float* hull_box, const float* d_rays, const uint32_t* order,
-                                  uint32_t n, float max_toi, uint32_t* d_part, float* d_toi, float* d_nrm, RayWaveScratch& scratch);
+                                  uint32_t n, float max_toi, uint32_t* d_part, float* d_toi, float* d_nrm, RayWaveScratch& scratch,
+                                  RayGridScratch* grid = nullptr, const float* d_aabbs = nullptr);
+// Grid resolution for n shapes in the box root[6] (about 4 cells per shape, at most 1024 a side and
+// 2^22 cells) and the entry capacity; no allocation happens in the frame afterwards.
+parrygpu_status shape_ray_grid_reserve(parrygpu_ctx* ctx, RayGridScratch& grid, uint64_t n_shapes, const float* root);
 
 // ---- shapes (contact.cu) ----
 // World AABBs of a compound's parts (Shape::compute_aabb(pos)) into d_out (n x 6 floats).

@@ -413,6 +413,13 @@ __global__ void k_ray_keys(const float* __restrict__ rays, uint32_t n, const uin
     key = (oct << 27) | (key >> 3);
   } else if (key_mode == 2) {
     key >>= 14;  // the top 16 bits of the Morton code: a two-pass sort
+  } else if (key_mode == 3) {
+    // direction class: octant and dominant axis (5 bits) above the top 25 bits of the Morton code
+    const float* d = rays + 6 * (size_t)i + 3;
+    const uint32_t oct = (d[0] < 0.0f ? 4u : 0u) | (d[1] < 0.0f ? 2u : 0u) | (d[2] < 0.0f ? 1u : 0u);
+    const float ax = fabsf(d[0]), ay = fabsf(d[1]), az = fabsf(d[2]);
+    const uint32_t dom = (ax >= ay && ax >= az) ? 0u : (ay >= az ? 1u : 2u);
+    key = ((oct * 3u + dom) << 25) | (key >> 5);
   }
   keys[i] = key;
   vals[i] = i;

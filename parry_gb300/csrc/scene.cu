@@ -12,7 +12,9 @@
 //                       with a network set (parrygpu_scene_set_mlp), the polyhedral pairs without a
 //                       cached normal start GJK from its predicted direction (listed, featurised and
 //                       inferred on the device inside the frame)
-//   rays                RayCast::cast_ray_and_get_normal on the shape set   (ray_composite_shape.rs:86-105)
+//   rays                RayCast::cast_ray_and_get_normal on the shape set   (ray_composite_shape.rs:86-105),
+//                       walking a uniform grid over the shapes rebuilt each frame (the BVH traversal's
+//                       answers; the BVH kernel takes over on the device when the grid overflows)
 //
 // Everything stays on the device: the pair count lives in device memory and bounds the later kernels,
 // buffers are sized at creation (pair capacity), so a frame is a fixed sequence of kernel launches and
@@ -35,6 +37,7 @@ struct parrygpu_scene {
   MfScratch mf;  // narrow-phase scratch owned by the scene (stable for the graph)
   DevBuf rays, ray_order, ray_part, ray_toi, ray_nrm;  // rays stored in Morton order of their origins
   RayWaveScratch ray_wave;
+  RayGridScratch ray_grid;  // the rays' uniform grid (cells == 0: the BVH is traversed)
   DevBuf seed_desc, seed_wb, seed_wf, seed_feat, seed_list, seed_dirs;  // learned seeding (parrygpu_scene_set_mlp)
   bool seeded = false;
   int cur = 0;
@@ -48,6 +51,7 @@ struct parrygpu_scene {
 namespace {
 
 constexpr int SC_THREADS = 256;
+constexpr uint32_t DEFAULT_SCENE_RAY_ORDER = 1;  // the origins' Morton order
 constexpr int REC_WORDS = 8 + 10 * PARRYGPU_MANIFOLD_MAX_POINTS;
 constexpr unsigned long long EMPTY_KEY = ~0ull;
 
@@ -228,8 +232,8 @@ static parrygpu_status scene_frame(parrygpu_ctx* ctx, parrygpu_scene* sc, float 
     KernelTimer kt(ctx, "scene_rays");
     if ((s = launch_shape_rays(ctx, &sc->bvh, sc->types.as<uint32_t>(), sc->params.as<float>(), sc->poses.as<float>(), sc->pool.as<float>(),
                                sc->hull_box.as<float>(), sc->rays.as<float>(), sc->ray_order.as<uint32_t>(), (uint32_t)sc->n_rays, sc->max_toi,
-                               sc->ray_part.as<uint32_t>(), sc->ray_toi.as<float>(), sc->ray_nrm.as<float>(), sc->ray_wave)) !=
-        PARRYGPU_OK)
+                               sc->ray_part.as<uint32_t>(), sc->ray_toi.as<float>(), sc->ray_nrm.as<float>(), sc->ray_wave,
+                               sc->ray_grid.cells ? &sc->ray_grid : nullptr, sc->aabbs.as<float>())) != PARRYGPU_OK)
       return s;
     kt.stop();
   }
@@ -354,13 +358,14 @@ void parrygpu_scene_destroy(parrygpu_scene* sc) {
   cudaDeviceSynchronize();  // frames in flight still read the scene's buffers
   drop_graph(sc);
   for (DevBuf* d : {&sc->types, &sc->params, &sc->poses, &sc->vel, &sc->pool, &sc->aabbs, &sc->hull_box, &sc->counts, &sc->mf.queue, &sc->mf.counters,
-                    &sc->mf.epa_ws, &sc->mf.bins, &sc->rays, &sc->ray_order, &sc->ray_part,
+                    &sc->mf.epa_ws, &sc->mf.bins, &sc->mf.redo, &sc->rays, &sc->ray_order, &sc->ray_part,
                     &sc->ray_toi, &sc->ray_nrm, &sc->bvh.wide, &sc->bvh.leaf_parent, &sc->bvh.node_parent, &sc->bvh.leaf_index,
                     &sc->bvh.flags, &sc->bvh.root_aabb, &sc->bvh.info})
     d->release();
   for (int k = 0; k < 9; ++k) sc->poly[k].release();
   for (DevBuf* d : {&sc->ray_wave.cands, &sc->ray_wave.counter, &sc->ray_wave.keys, &sc->ray_wave.ovf}) d->release();
   for (DevBuf* d : {&sc->seed_desc, &sc->seed_wb, &sc->seed_wf, &sc->seed_feat, &sc->seed_list, &sc->seed_dirs}) d->release();
+  for (DevBuf* d : {&sc->ray_grid.dev, &sc->ray_grid.starts, &sc->ray_grid.cursor, &sc->ray_grid.entries, &sc->ray_grid.sums}) d->release();
   for (int b = 0; b < 2; ++b) {
     sc->pairs[b].release();
     sc->recs[b].release();
@@ -388,7 +393,10 @@ parrygpu_status parrygpu_scene_set_rays(parrygpu_ctx* ctx, parrygpu_scene* sc, c
     if ((s = radix_sort_reserve(ctx, n)) != PARRYGPU_OK) { tmp.release(); return s; }
     PG_CUDA(ctx, ctx->misc.reserve(64));
     uint32_t* bounds = ctx->misc.as<uint32_t>() + 8;
-    if ((s = launch_ray_keys(ctx, tmp.as<float>(), n, bounds, ctx->sort_k[0].as<uint32_t>(), ctx->sort_v[0].as<uint32_t>(), 0u)) !=
+    // scene_ray_order 1 / 2 / 3 -> ray key 0 (origin) / 1 (octant, origin) / 3 (octant and dominant axis, origin)
+    const uint32_t order_mode = ctx->cfg.scene_ray_order ? ctx->cfg.scene_ray_order : DEFAULT_SCENE_RAY_ORDER;
+    const uint32_t key_mode = order_mode == 1 ? 0u : (order_mode == 2 ? 1u : 3u);
+    if ((s = launch_ray_keys(ctx, tmp.as<float>(), n, bounds, ctx->sort_k[0].as<uint32_t>(), ctx->sort_v[0].as<uint32_t>(), key_mode)) !=
         PARRYGPU_OK) {
       tmp.release();
       return s;
@@ -404,6 +412,15 @@ parrygpu_status parrygpu_scene_set_rays(parrygpu_ctx* ctx, parrygpu_scene* sc, c
     if (e != cudaSuccess) return check_cuda(ctx, e, "scene ray ordering");
   }
   if ((s = shape_rays_reserve(ctx, sc->ray_wave, n)) != PARRYGPU_OK) return s;
+  if (ctx->cfg.scene_ray_grid != 2 && n > 0) {
+    // the grid's resolution from the shapes' current bounds (its placement follows them each frame)
+    float root[6];
+    PG_CUDA(ctx, cudaMemcpyAsync(root, sc->bvh.root_aabb.ptr, sizeof(root), cudaMemcpyDeviceToHost, ctx->stream));
+    PG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    if ((s = shape_ray_grid_reserve(ctx, sc->ray_grid, sc->n, root)) != PARRYGPU_OK) return s;
+  } else {
+    sc->ray_grid.cells = 0;
+  }
   PG_CUDA(ctx, sc->ray_part.reserve(n_rays * 4 + 16));
   PG_CUDA(ctx, sc->ray_toi.reserve(n_rays * 4 + 16));
   PG_CUDA(ctx, sc->ray_nrm.reserve(n_rays * 12 + 16));

@@ -13,6 +13,7 @@
 #include "internal.hpp"
 #include "epa_device.cuh"
 #include "contact_device.cuh"
+#include "gjk_reg.cuh"
 
 #include <cstring>
 
@@ -64,9 +65,10 @@ __device__ __forceinline__ bool ray_toi_with_halfspace(V3 center, V3 normal, V3 
 }
 
 // gjk.rs:660-795 minkowski_ray_cast of the ray (origin, rd) with max_toi = f32::MAX on
-// g1 - pos12 * g2; leaves the simplex as the reference does (directional_distance reads it).
-__device__ __noinline__ bool minkowski_ray_cast(const Pose& pos12, const ShapeDev& g1, bool round, float border, const ShapeDev& g2, V3 rd,
-                                                Simplex& s, float* toi_out, V3* n_out) {
+// g1 - pos12 * g2; leaves the simplex as the reference does (directional_distance reads it). The
+// simplex is a RegSimplex (gjk_reg.cuh) kept in registers: the loop is inlined into the kernel.
+__device__ __forceinline__ bool minkowski_ray_cast(const Pose& pos12, const ShapeDev& g1, bool round, float border, const ShapeDev& g2,
+                                                   V3 rd, RegSimplex<true>& s, float* toi_out, V3* n_out) {
   const float eps_tol = GJK_EPS_TOL;
   const float eps_rel = sqrtf(eps_tol);
   float ray_length = norm(rd);
@@ -76,8 +78,8 @@ __device__ __noinline__ bool minkowski_ray_cast(const Pose& pos12, const ShapeDe
   V3 dir = -cd;
   V3 ldir = dir;
   CSO sp = cast_cso(pos12, g1, round, border, g2, dir);
-  simplex_reset(s, CSO{sp.p - co, sp.o1, sp.o2});
-  V3 proj = simplex_project_origin_and_reduce(s);
+  rs_reset(s, CSO{sp.p - co, sp.o1, sp.o2});
+  V3 proj = rs_project_origin_and_reduce(s);
   float max_bound = FLT_MAX;
   int niter = 0;
   bool last_chance = false;
@@ -105,7 +107,7 @@ __device__ __noinline__ bool minkowski_ray_cast(const Pose& pos12, const ShapeDe
         V3 shift = cd * t;
         co = co + shift;
         max_bound = FLT_MAX;
-        for (int i = 0; i <= s.dim; ++i) s.v[i].p = s.v[i].p + (-shift);
+        rs_translate(s, -shift);
         last_chance = false;
       }
     } else {
@@ -114,8 +116,8 @@ __device__ __noinline__ bool minkowski_ray_cast(const Pose& pos12, const ShapeDe
     if (last_chance) return false;
     float min_bound = -dot(dir, support.p - co);
     if (max_bound - min_bound <= eps_rel * max_bound) return false;
-    simplex_add(s, CSO{support.p - co, support.o1, support.o2});
-    proj = simplex_project_origin_and_reduce(s);
+    rs_add(s, CSO{support.p - co, support.o1, support.o2});
+    proj = rs_project_origin_and_reduce(s);
     if (s.dim == 3) {
       if (min_bound >= eps_tol) return false;
       *toi_out = ltoi / ray_length; *n_out = ldir; return true;
@@ -178,12 +180,12 @@ __device__ __forceinline__ bool cast_ball_ball(const Pose& pos12, V3 vel12, floa
 __device__ __forceinline__ bool cast_support_maps(const EpaWs& ws, const Pose& pos12, V3 vel12, const ShapeDev& g1, const ShapeDev& g2,
                                                   const CastOptions& opt, CastHit* h, uint32_t* gjk_iters, uint32_t* epa_iters,
                                                   uint32_t* epa_calls, bool* epa_overflow) {
-  Simplex s;
+  RegSimplex<true> s;
   float toi;
   V3 normal1;
   if (!minkowski_ray_cast(pos12, g1, opt.target > 0.0f, opt.target, g2, vel12, s, &toi, &normal1)) return false;
   V3 w1 = v3(0.f, 0.f, 0.f), w2 = v3(0.f, 0.f, 0.f);
-  if (toi != 0.0f) gjk_result(s, s.dim == 3, &w1, &w2);
+  if (toi != 0.0f) rs_witness(s, s.dim == 3, &w1, &w2);
   if (toi > opt.max_toi) return false;
   if ((opt.geometry_on_penetration || !opt.stop_at_penetration) && toi < 1.0e-5f) {
     // contact_support_map_support_map(pos12, g1, g2, f32::MAX)
@@ -218,7 +220,10 @@ __device__ __forceinline__ bool cast_support_maps(const EpaWs& ws, const Pose& p
   return true;
 }
 
-__global__ void __launch_bounds__(SC_THREADS) k_cast_shapes(ShapeArrays sh, const uint32_t* __restrict__ pairs, uint64_t n,
+// MINB = resident blocks of SC_THREADS per SM the register budget is cut for: 4 leaves the inlined
+// ray cast all the registers it wants, 6 caps it at 168 (a few spills, more warps per SM).
+template <int MINB>
+__global__ void __launch_bounds__(SC_THREADS, MINB) k_cast_shapes(ShapeArrays sh, const uint32_t* __restrict__ pairs, uint64_t n,
                                                             const float* __restrict__ vels, CastOptions opt, float* __restrict__ out,
                                                             uint8_t* __restrict__ status, uint32_t* __restrict__ ws_pool,
                                                             unsigned long long* __restrict__ stats, uint32_t* __restrict__ err) {
@@ -303,8 +308,13 @@ extern "C" parrygpu_status parrygpu_cast_shapes(parrygpu_ctx* ctx, const parrygp
                   options->compute_impact_geometry_on_penetration != 0};
   {
     KernelTimer kt(ctx, "cast_shapes");
-    k_cast_shapes<<<blocks, SC_THREADS, 0, ctx->stream>>>(sh, (const uint32_t*)dp, n_pairs, (const float*)dv, opt, (float*)d_out,
-                                                          (uint8_t*)d_status, ctx->epa_ws.as<uint32_t>(), ctr, ctx->d_err);
+    // the persistent grid's residency decides the register budget
+    if (per_sm <= 4)
+      k_cast_shapes<4><<<blocks, SC_THREADS, 0, ctx->stream>>>(sh, (const uint32_t*)dp, n_pairs, (const float*)dv, opt, (float*)d_out,
+                                                               (uint8_t*)d_status, ctx->epa_ws.as<uint32_t>(), ctr, ctx->d_err);
+    else
+      k_cast_shapes<6><<<blocks, SC_THREADS, 0, ctx->stream>>>(sh, (const uint32_t*)dp, n_pairs, (const float*)dv, opt, (float*)d_out,
+                                                               (uint8_t*)d_status, ctx->epa_ws.as<uint32_t>(), ctr, ctx->d_err);
     kt.stop();
     PG_LAUNCHED(ctx);
   }

@@ -13,8 +13,11 @@
 #include "internal.hpp"
 #include "gjk_device.cuh"
 #include "lbvh_device.cuh"
+#include "gjk_reg.cuh"
 
 #include <cooperative_groups.h>
+#include <algorithm>
+#include <cmath>
 
 using namespace pg;
 
@@ -197,87 +200,9 @@ __device__ __forceinline__ bool ray_support_map(const ShapeDev& shape, V3 o, V3 
 // ---- the GJK ray cast with its simplex in registers, for one support-map kind ----
 // gjk_cast_local_ray keeps its Voronoi simplex in an array indexed at run time (local memory, and
 // witness points the ray cast never reads). The candidate kernels run one shape kind per launch,
-// so the cast below is inlined with that kind's support function, and its simplex keeps only the
-// four vertex positions, moved with constant indices. Every value is computed as in
-// gjk_cast_local_ray / simplex_project_origin_and_reduce / simplex_add, so the answers are the same.
-struct RaySimplex {
-  V3 v0, v1, v2, v3;
-  int dim;
-};
-
-__device__ __forceinline__ V3 rs_vertex(const RaySimplex& s, int i) { return i == 0 ? s.v0 : (i == 1 ? s.v1 : (i == 2 ? s.v2 : s.v3)); }
-
-// VoronoiSimplex::project_origin_and_reduce: the projection of the origin; the vertices of the
-// feature that holds it move to the front (in the order the index swaps of the array form leave
-// them), and dim shrinks to that feature's.
-__device__ __forceinline__ V3 rs_project_origin_and_reduce(RaySimplex& s) {
-  const V3 o = v3(0.f, 0.f, 0.f);
-  Loc loc;
-  if (s.dim == 0) return s.v0;
-  if (s.dim == 1) {
-    V3 p = project_segment(s.v0, s.v1, o, &loc);
-    if (loc.kind == LOC_VERTEX) {
-      if (loc.id != 0) s.v0 = s.v1;
-      s.dim = 0;
-    }
-    return p;
-  }
-  if (s.dim == 2) {
-    V3 p = project_triangle_inl(s.v0, s.v1, s.v2, o, &loc);
-    if (loc.kind == LOC_VERTEX) {
-      s.v0 = rs_vertex(s, loc.id);
-      s.dim = 0;
-    } else if (loc.kind == LOC_EDGE) {
-      if (loc.id == 1) s.v0 = s.v2;       // swap(0, 2): (v2, v1)
-      else if (loc.id == 2) s.v1 = s.v2;  // swap(1, 2): (v0, v2)
-      s.dim = 1;
-    }
-    return p;
-  }
-  V3 p = project_tetrahedron_inl(s.v0, s.v1, s.v2, s.v3, o, &loc);
-  if (loc.kind == LOC_VERTEX) {
-    s.v0 = rs_vertex(s, loc.id);
-    s.dim = 0;
-  } else if (loc.kind == LOC_EDGE) {
-    const V3 a = s.v0, b = s.v1, c = s.v2, d = s.v3;
-    switch (loc.id) {
-      case 1: s.v1 = c; break;             // swap(1, 2)
-      case 2: s.v1 = d; break;             // swap(1, 3)
-      case 3: s.v0 = c; break;             // swap(0, 2)
-      case 4: s.v0 = d; break;             // swap(0, 3)
-      case 5: s.v0 = c; s.v1 = d; break;   // swap(0, 2), swap(1, 3)
-      default: s.v0 = a; s.v1 = b; break;
-    }
-    s.dim = 1;
-  } else if (loc.kind == LOC_FACE) {
-    if (loc.id == 1) s.v2 = s.v3;
-    else if (loc.id == 2) s.v1 = s.v3;
-    else if (loc.id == 3) s.v0 = s.v3;
-    s.dim = 2;
-  }
-  return p;
-}
-
-// VoronoiSimplex::add_point: refused (simplex unchanged) when the point is affinely dependent.
-__device__ __forceinline__ void rs_add(RaySimplex& s, V3 pt) {
-  if (s.dim == 0) {
-    V3 d = s.v0 - pt;
-    if (dot(d, d) < GJK_EPS_TOL) return;
-  } else if (s.dim == 1) {
-    V3 ab = s.v1 - s.v0, ac = pt - s.v0;
-    V3 c = cross(ab, ac);
-    if (dot(c, c) < GJK_EPS_TOL) return;
-  } else if (s.dim == 2) {
-    V3 ab = s.v1 - s.v0, ac = s.v2 - s.v0, ap = pt - s.v0;
-    V3 n = normalize(cross(ab, ac));
-    if (fabsf(dot(n, ap)) < GJK_EPS_TOL) return;
-  }
-  s.dim += 1;
-  if (s.dim == 1) s.v1 = pt;
-  else if (s.dim == 2) s.v2 = pt;
-  else s.v3 = pt;
-}
-
+// so the cast below is inlined with that kind's support function over a positions-only
+// RegSimplex (gjk_reg.cuh); every value is computed as in gjk_cast_local_ray, so the answers are
+// the same.
 // Support of one kind: TY = SH_CAPSULE (O(1)) or SH_CONVEX (vertex scan).
 template <uint32_t TY>
 __device__ __forceinline__ V3 kind_support(const ShapeDev& s, V3 dir) {
@@ -303,9 +228,11 @@ __device__ __forceinline__ bool gjk_cast_local_ray_kind(const ShapeDev& shape, V
   V3 co = ro, cd = rd / ray_length;
   V3 dir = -cd;
   V3 ldir = dir;
-  RaySimplex s;
-  s.v0 = kind_support<TY>(shape, dir) - co;
-  s.dim = 0;
+  RegSimplex<false> s;
+  {
+    const V3 sp = kind_support<TY>(shape, dir) - co;
+    rs_reset(s, CSO{sp, sp, sp});
+  }
   V3 proj = rs_project_origin_and_reduce(s);
   float max_bound = FLT_MAX;
   int niter = 0;
@@ -333,11 +260,7 @@ __device__ __forceinline__ bool gjk_cast_local_ray_kind(const ShapeDev& shape, V
         V3 shift = cd * t;
         co = co + shift;
         max_bound = FLT_MAX;
-        const V3 ns = -shift;
-        s.v0 = s.v0 + ns;
-        if (s.dim >= 1) s.v1 = s.v1 + ns;
-        if (s.dim >= 2) s.v2 = s.v2 + ns;
-        if (s.dim >= 3) s.v3 = s.v3 + ns;
+        rs_translate(s, -shift);
         last_chance = false;
       }
     } else {
@@ -346,7 +269,10 @@ __device__ __forceinline__ bool gjk_cast_local_ray_kind(const ShapeDev& shape, V
     if (last_chance) return false;
     float min_bound = -dot(dir, sp - co);
     if (max_bound - min_bound <= eps_rel * max_bound) return false;
-    rs_add(s, sp - co);
+    {
+      const V3 q = sp - co;
+      rs_add(s, CSO{q, q, q});
+    }
     proj = rs_project_origin_and_reduce(s);
     if (s.dim == 3) {
       if (min_bound >= eps_tol) return false;
@@ -486,11 +412,19 @@ __global__ void k_hull_local_boxes(const uint32_t* __restrict__ types, const flo
   box[2 * (size_t)i + 1] = hi;
 }
 
+// How far outside a shape the GJK ray cast (gjk.rs:660-795) may report a hit, as a margin for the
+// pre-tests below: the cast stops when its distance bounds agree within sqrt(eps) relative, and on a
+// rounded shape it was measured reporting hits for rays passing up to 0.41 % of a capsule's radius
+// outside it (800,000 grazing rays against the f32 oracle); 3 % of the shape's extent keeps a wide
+// safety factor. Plus 1e-4 of the coordinates' magnitude for the rounding of the transform.
+__device__ __forceinline__ float gjk_ray_margin(float ext, V3 ol) {
+  return 0.03f * ext + 1e-4f * (1.0f + ext + fmaxf(fmaxf(fabsf(ol.x), fabsf(ol.y)), fabsf(ol.z)));
+}
+
 // Conservative pre-test of a capsule / hull candidate: can the ray (world o, dir) reach the shape's
-// local box (capsule: its exact bounds; hull: its vertex bounds), inflated by a margin far above
-// the rounding of the transform and of the GJK ray cast, before `tlim`? A false answer proves the
-// GJK ray cast cannot return a hit at toi <= tlim, so the candidate is dropped without changing any
-// answer. *t_in receives a lower bound of the entry time.
+// local box (capsule: its exact bounds; hull: its vertex bounds), inflated by gjk_ray_margin, before
+// `tlim`? A false answer proves the GJK ray cast cannot return a hit at toi <= tlim, so the
+// candidate is dropped without changing any answer. *t_in receives a lower bound of the entry time.
 __device__ __forceinline__ bool local_box_may_hit(const CompoundDev& cd, uint32_t part, uint32_t ty, V3 o, V3 dir, float tlim, float* t_in) {
   float3 lo, hi;
   float4 prm = cd.params[part];
@@ -508,8 +442,8 @@ __device__ __forceinline__ bool local_box_may_hit(const CompoundDev& cd, uint32_
   Pose p = load_pose(cd.poses, part);
   V3 ol = pose_inv_point(p, o), dl = pose_inv_rotate(p, dir);
   float ext = fmaxf(fmaxf(fmaxf(fabsf(lo.x), fabsf(hi.x)), fmaxf(fabsf(lo.y), fabsf(hi.y))), fmaxf(fabsf(lo.z), fabsf(hi.z)));
-  float m = 1e-4f * (1.0f + ext + fmaxf(fmaxf(fabsf(ol.x), fabsf(ol.y)), fabsf(ol.z)));
   if (!(ext < 1e30f)) { *t_in = 0.0f; return true; }  // unbounded box: no filter
+  const float m = gjk_ray_margin(ext, ol);
   float tmin = 0.0f, tmax = tlim + fabsf(tlim) * 1e-5f;
   const float oo[3] = {ol.x, ol.y, ol.z}, dd[3] = {dl.x, dl.y, dl.z};
   const float lov[3] = {lo.x - m, lo.y - m, lo.z - m}, hiv[3] = {hi.x + m, hi.y + m, hi.z + m};
@@ -526,6 +460,24 @@ __device__ __forceinline__ bool local_box_may_hit(const CompoundDev& cd, uint32_
   }
   *t_in = tmin;
   return tmin <= tmax;
+}
+
+// Conservative pre-test of a capsule candidate after the box test: can the ray's line come within
+// radius + margin of the capsule's axis line? The line-to-line distance is a lower bound of the
+// distance from the ray to the capsule's axis segment, so a ray farther than that misses the
+// capsule. Computed in double precision in the capsule's frame (axis = y) with the box test's
+// margin (gjk_ray_margin). A false answer proves the GJK ray cast returns no hit.
+__device__ __forceinline__ bool capsule_may_hit(const CompoundDev& cd, uint32_t part, V3 o, V3 dir) {
+  const float4 prm = cd.params[part];
+  const Pose p = load_pose(cd.poses, part);
+  const V3 ol = pose_inv_point(p, o), dl = pose_inv_rotate(p, dir);
+  const double h = prm.x, rad = prm.y;
+  const double lim = rad + (double)gjk_ray_margin(prm.x + prm.y, ol);
+  const double ex = dl.x, ez = dl.z, px = ol.x, pz = ol.z;
+  const double den2 = ex * ex + ez * ez;
+  if (den2 == 0.0) return px * px + pz * pz <= lim * lim;  // along the axis: a constant distance
+  const double num = px * ez - pz * ex;                      // |P x E| in the x-z plane
+  return num * num <= lim * lim * den2;
 }
 
 // Thread k handles ray r = order[k] (order may be null: r = k), read from slot k when the rays were
@@ -661,9 +613,12 @@ struct WaveBufs {
   RayCand* a;            // nearest candidate of each ray that has one (capacity n)
   RayCand* b;            // the other candidates (capacity cap)
   unsigned long long cap;
-  unsigned long long* count;    // [0] list B counter, [1] list A counter, [2] list B first-failure snapshot
+  unsigned long long* count;    // [0] list B counter, [1] list A counter, [2] list B first-failure snapshot,
+                                // [8] list C counter, [9] list C snapshot
   unsigned long long* keys;  // per ray (index r)
   uint8_t* ovf;              // per ray (index r)
+  RayCand* c;                // the grid walk's analytic candidates: balls at the front, the others at the back
+                             // (capacity cap)
 };
 
 // Appends one slot per calling thread to a two-ended list of `cap` entries (kind 0 at the front,
@@ -701,12 +656,123 @@ __device__ __forceinline__ unsigned long long list_slot(unsigned long long i, un
   return i < front ? i : cap - 1ull - (i - front);
 }
 
+// ---- uniform grid over the shapes (the frame pipeline's rays) ----
+// Each frame the grid is placed on the BVH root box (which holds every shape's loosened AABB),
+// widened by `delta`; its resolution is fixed. A shape is entered in every cell its AABB, widened by
+// delta, overlaps. A ray clipped to the grid box walks its cells in order (3-D DDA) and tests the
+// entries' AABBs as the BVH traversal tests its leaf boxes. A point of the ray lies within delta of
+// a cell the walk visits (delta is far above the walk's rounding), so every shape the ray reaches
+// is met; the walk stops once the next cell starts beyond the best hit (with a margin). The leaves
+// met are those the BVH traversal meets (possibly more, and some twice), and the answer - the
+// minimum (toi, index) - is the same. When the entries outgrow their capacity the grid reports
+// itself unusable (ok = 0) and the BVH kernel casts the rays of that frame instead.
+struct GridDev {
+  float lo[3], cell[3], inv[3], delta;
+  uint32_t res[3], ok;
+  unsigned long long total;  // entries counted this frame
+};
+
+// One entry of a cell: the shape's AABB with its index and type (two 16-byte loads, no second
+// lookup).
+struct __align__(16) GridEntry {
+  float mn[3];
+  uint32_t part;
+  float mx[3];
+  uint32_t type;
+};
+
+__global__ void k_grid_setup(const float* __restrict__ root, GridDev* __restrict__ g, uint32_t rx, uint32_t ry, uint32_t rz) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  float m = 0.0f;
+  for (int i = 0; i < 6; ++i) m = fmaxf(m, fabsf(root[i]));
+  const float delta = 1e-3f + 4e-6f * m;
+  const uint32_t res[3] = {rx, ry, rz};
+  for (int i = 0; i < 3; ++i) {
+    const float lo = root[i] - delta, hi = root[3 + i] + delta;
+    float c = (hi - lo) / (float)res[i];
+    if (!(c > 0.0f) || !isfinite(c)) c = 1.0f;
+    g->lo[i] = lo;
+    g->cell[i] = c;
+    g->inv[i] = 1.0f / c;
+    g->res[i] = res[i];
+  }
+  g->delta = delta;
+  g->ok = isfinite(m) ? 1u : 0u;
+  g->total = 0ull;
+}
+
+__device__ __forceinline__ uint32_t grid_coord(const GridDev& g, int axis, float x) {
+  const float f = floorf((x - g.lo[axis]) * g.inv[axis]);
+  if (!(f > 0.0f)) return 0u;  // (NaN too)
+  const float top = (float)(g.res[axis] - 1u);
+  return f >= top ? g.res[axis] - 1u : (uint32_t)f;
+}
+
+// Cell range of shape i's AABB widened by delta; false for an empty range.
+__device__ __forceinline__ void grid_range(const GridDev& g, const float* __restrict__ aabbs, uint32_t i, uint32_t* a, uint32_t* b) {
+  const float* bx = aabbs + 6 * (size_t)i;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    a[k] = grid_coord(g, k, bx[k] - g.delta);
+    b[k] = grid_coord(g, k, bx[3 + k] + g.delta);
+  }
+}
+
+__global__ void k_grid_count(const float* __restrict__ aabbs, uint32_t n, GridDev* __restrict__ g, uint32_t* __restrict__ counts) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  const GridDev gd = *g;
+  unsigned long long mine = 0;
+  if (i < n && gd.ok) {
+    uint32_t a[3], b[3];
+    grid_range(gd, aabbs, i, a, b);
+    mine = (unsigned long long)(b[0] - a[0] + 1) * (b[1] - a[1] + 1) * (b[2] - a[2] + 1);
+    if (mine <= 4096ull) {
+      for (uint32_t z = a[2]; z <= b[2]; ++z)
+        for (uint32_t y = a[1]; y <= b[1]; ++y)
+          for (uint32_t x = a[0]; x <= b[0]; ++x) atomicAdd(&counts[((size_t)z * gd.res[1] + y) * gd.res[0] + x], 1u);
+    }
+  }
+  // a shape over more than 4096 cells is not entered, and the grid is not used this frame
+  if (mine > 4096ull) {
+    g->ok = 0u;
+    mine = 0;
+  }
+  const uint32_t w = __reduce_add_sync(0xffffffffu, (uint32_t)mine);
+  if ((threadIdx.x & 31) == 0 && w) atomicAdd(&g->total, (unsigned long long)w);
+}
+
+__global__ void k_grid_check(GridDev* __restrict__ g, unsigned long long cap) {
+  if (threadIdx.x == 0 && blockIdx.x == 0 && g->total > cap) g->ok = 0u;
+}
+
+__global__ void k_grid_fill(const float* __restrict__ aabbs, const uint32_t* __restrict__ types, uint32_t n, const GridDev* __restrict__ g,
+                            const uint32_t* __restrict__ starts, uint32_t* __restrict__ cursor, GridEntry* __restrict__ entries,
+                            unsigned long long cap) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  const GridDev gd = *g;
+  if (i >= n || !gd.ok) return;
+  uint32_t a[3], b[3];
+  grid_range(gd, aabbs, i, a, b);
+  const float* bx = aabbs + 6 * (size_t)i;
+  const GridEntry e{{bx[0], bx[1], bx[2]}, i, {bx[3], bx[4], bx[5]}, types[i]};
+  for (uint32_t z = a[2]; z <= b[2]; ++z)
+    for (uint32_t y = a[1]; y <= b[1]; ++y)
+      for (uint32_t x = a[0]; x <= b[0]; ++x) {
+        const size_t c = ((size_t)z * gd.res[1] + y) * gd.res[0] + x;
+        const unsigned long long slot = (unsigned long long)starts[c] + atomicAdd(&cursor[c], 1u);
+        if (slot < cap) entries[slot] = e;
+      }
+}
+
 __global__ void __launch_bounds__(128) k_rays_wave(const WideNode* __restrict__ wide, CompoundDev cd, const float* __restrict__ rays, uint32_t n,
                                                    float max_toi, int solid, int has_pose, Pose cpose, uint32_t* __restrict__ part_out,
                                                    float* __restrict__ toi_out, float* __restrict__ normal_out, uint32_t* __restrict__ err,
-                                                   const uint32_t* __restrict__ order, int permuted, WaveBufs wb) {
+                                                   const uint32_t* __restrict__ order, int permuted, WaveBufs wb,
+                                                   const GridDev* __restrict__ grid) {
   uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= n) return;
+  // with a usable grid the walk (k_rays_walk) casts the rays instead
+  if (grid && grid->ok != 0u) return;
   uint32_t r;
   V3 o, dir;
   ray_of(rays, order, permuted, k, has_pose, cpose, &r, &o, &dir);
@@ -746,6 +812,7 @@ __global__ void __launch_bounds__(128) k_rays_wave(const WideNode* __restrict__ 
     if (!part_cast_ray_analytic(s, p, o, dir, best, solid != 0, &t, &nn)) return;
     if (t < best || (have && t == best && part < best_part)) { best = t; best_part = part; best_n = nn; have = true; }
   };
+  {
   WideNode w;
   load_wide(wide, 0, &w);
   if ((w.r.data & 0x3fffffffu) == 0u) {
@@ -780,6 +847,7 @@ __global__ void __launch_bounds__(128) k_rays_wave(const WideNode* __restrict__ 
       load_wide(wide, next, &w);
     }
   }
+  }  // BVH traversal
   if (near_part != 0xffffffffu) {
     // at most one entry per ray: list A (n entries) never fills
     unsigned long long slot = append_slot2(wb.count + 1, n, cd.types[near_part] == SH_CAPSULE ? 0u : 1u, nullptr);
@@ -794,6 +862,154 @@ __global__ void __launch_bounds__(128) k_rays_wave(const WideNode* __restrict__ 
     normal_out[3 * (size_t)r] = best_n.x;
     normal_out[3 * (size_t)r + 1] = best_n.y;
     normal_out[3 * (size_t)r + 2] = best_n.z;
+  }
+}
+
+// The grid walk alone (frame pipeline rays): every shape whose AABB the ray enters below max_toi
+// becomes a candidate - an analytic shape in list C (balls at the front), a capsule / hull that
+// passes the local-box pre-test in list A (the ray's nearest) or B - and the leaf tests run in their
+// own kernels afterwards, each over one shape kind. Walking without a best hit costs the walk the
+// cells behind a ray's first hit, but keeps the warp's lanes on one code path: walking leaf tests
+// inline left fewer than 5 of 32 lanes active. The ray's outputs start as "no hit"; the candidate
+// kernels publish hits through the per-ray key and k_rays_finish writes the winners. A ray whose
+// candidates overflow a list is marked for the single-kernel cast. Does nothing when the grid is
+// unusable (the BVH wave kernel casts the rays then).
+__global__ void __launch_bounds__(128) k_rays_walk(CompoundDev cd, const float* __restrict__ rays, uint32_t n, float max_toi, int has_pose,
+                                                   Pose cpose, uint32_t* __restrict__ part_out, float* __restrict__ toi_out,
+                                                   float* __restrict__ normal_out, const uint32_t* __restrict__ order, int permuted,
+                                                   WaveBufs wb, const GridDev* __restrict__ grid, const uint32_t* __restrict__ starts,
+                                                   const GridEntry* __restrict__ entries) {
+  const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n || grid->ok == 0u) return;
+  uint32_t r;
+  V3 o, dir;
+  ray_of(rays, order, permuted, k, has_pose, cpose, &r, &o, &dir);
+  const uint32_t zmask = (dir.x == 0.0f ? 1u : 0u) | (dir.y == 0.0f ? 2u : 0u) | (dir.z == 0.0f ? 4u : 0u);
+  const V3 inv = v3(dir.x != 0.0f ? 1.0f / dir.x : 0.0f, dir.y != 0.0f ? 1.0f / dir.y : 0.0f, dir.z != 0.0f ? 1.0f / dir.z : 0.0f);
+  bool overflow = false;
+  uint32_t near_part = 0xffffffffu, near_ty = 0u;
+  float near_tmin = FLT_MAX;
+  const GridDev g = *grid;
+  const float3 glo = make_float3(g.lo[0], g.lo[1], g.lo[2]);
+  const float3 ghi = make_float3(g.lo[0] + g.cell[0] * (float)g.res[0], g.lo[1] + g.cell[1] * (float)g.res[1], g.lo[2] + g.cell[2] * (float)g.res[2]);
+  const float t0 = slab(glo, ghi, o, inv, zmask, max_toi);
+  if (t0 != FLT_MAX) {
+    uint32_t cx = grid_coord(g, 0, o.x + dir.x * t0), cy = grid_coord(g, 1, o.y + dir.y * t0), cz = grid_coord(g, 2, o.z + dir.z * t0);
+    uint32_t s0 = 0xffffffffu, s1 = 0xffffffffu, s2 = 0xffffffffu, s3 = 0xffffffffu;  // the last parts met
+    auto cross_t = [&](int a, uint32_t ci, float oa, float da, float ia) {
+      if (zmask & (1u << a)) return FLT_MAX;
+      const float b = g.lo[a] + g.cell[a] * (float)(da > 0.0f ? ci + 1u : ci);
+      return (b - oa) * ia;
+    };
+    size_t cell = ((size_t)cz * g.res[1] + cy) * g.res[0] + cx;
+    uint32_t j = starts[cell], e1 = starts[cell + 1];
+    // One loop turn tests one entry of the current cell, or steps to the next cell: lanes whose
+    // cells hold different numbers of entries stay in step.
+    for (;;) {
+      if (j < e1) {
+        const float4 ea = __ldg(reinterpret_cast<const float4*>(entries + j));
+        const float4 eb = __ldg(reinterpret_cast<const float4*>(entries + j) + 1);
+        ++j;
+        const uint32_t part = __float_as_uint(ea.w);
+        if (part == s0 || part == s1 || part == s2 || part == s3) continue;  // met in an earlier cell
+        s3 = s2;
+        s2 = s1;
+        s1 = s0;
+        s0 = part;
+        float ts = slab(make_float3(ea.x, ea.y, ea.z), make_float3(eb.x, eb.y, eb.z), o, inv, zmask, max_toi);
+        if (ts == FLT_MAX || !(ts < max_toi) || overflow) continue;
+        const uint32_t ty = __float_as_uint(eb.w);
+        if (analytic_type(ty)) {
+          const unsigned long long slot = append_slot2(wb.count + 8, wb.cap, ty == SH_BALL ? 0u : 1u, wb.count + 9);
+          if (slot != ~0ull) wb.c[slot] = RayCand{k, r, part, 0u, ts, 0.f, 0.f, 0.f, 0.f, 0.f};
+          else overflow = true;
+          continue;
+        }
+        float t_box;
+        if (!local_box_may_hit(cd, part, ty, o, dir, max_toi, &t_box)) continue;
+        ts = fmaxf(ts, t_box);
+        uint32_t dpart = part, dty = ty;
+        float dt = ts;
+        if (ts < near_tmin) {
+          dpart = near_part;
+          dty = near_ty;
+          dt = near_tmin;
+          near_part = part;
+          near_ty = ty;
+          near_tmin = ts;
+        }
+        if (dpart != 0xffffffffu) {
+          const unsigned long long slot = append_slot2(wb.count, wb.cap, dty == SH_CAPSULE ? 0u : 1u, wb.count + 2);
+          if (slot != ~0ull) wb.b[slot] = RayCand{k, r, dpart, 0u, dt, 0.f, 0.f, 0.f, 0.f, 0.f};
+          else overflow = true;
+        }
+        continue;
+      }
+      const float tx = cross_t(0, cx, o.x, dir.x, inv.x), ty = cross_t(1, cy, o.y, dir.y, inv.y), tz = cross_t(2, cz, o.z, dir.z, inv.z);
+      const float tn = fminf(tx, fminf(ty, tz));
+      if (tn >= FLT_MAX || !(tn <= max_toi)) break;
+      if (tn == tx) {
+        if (dir.x > 0.0f) { if (++cx >= g.res[0]) break; }
+        else { if (cx == 0u) break; --cx; }
+      } else if (tn == ty) {
+        if (dir.y > 0.0f) { if (++cy >= g.res[1]) break; }
+        else { if (cy == 0u) break; --cy; }
+      } else {
+        if (dir.z > 0.0f) { if (++cz >= g.res[2]) break; }
+        else { if (cz == 0u) break; --cz; }
+      }
+      cell = ((size_t)cz * g.res[1] + cy) * g.res[0] + cx;
+      j = starts[cell];
+      e1 = starts[cell + 1];
+    }
+  }
+  if (near_part != 0xffffffffu && !overflow) {
+    const unsigned long long slot = append_slot2(wb.count + 1, n, near_ty == SH_CAPSULE ? 0u : 1u, nullptr);
+    wb.a[slot] = RayCand{k, r, near_part, 0u, near_tmin, 0.f, 0.f, 0.f, 0.f, 0.f};
+  }
+  wb.keys[r] = ~0ull;
+  wb.ovf[r] = overflow ? 1 : 0;
+  part_out[r] = 0xffffffffu;
+  toi_out[r] = 0.0f;
+  if (normal_out) {
+    normal_out[3 * (size_t)r] = 0.0f;
+    normal_out[3 * (size_t)r + 1] = 0.0f;
+    normal_out[3 * (size_t)r + 2] = 0.0f;
+  }
+}
+
+// The analytic candidates of list C: FRONT = the balls, else the cuboids and triangles. A candidate
+// whose box entry lies beyond the ray's current best is skipped.
+template <bool FRONT>
+__global__ void __launch_bounds__(128) k_rays_cand_analytic(CompoundDev cd, const float* __restrict__ rays, float max_toi, int solid,
+                                                            int has_pose, Pose cpose, const uint32_t* __restrict__ order, int permuted,
+                                                            RayCand* __restrict__ list, unsigned long long cap,
+                                                            const unsigned long long* __restrict__ count,
+                                                            const unsigned long long* __restrict__ fail, unsigned long long* __restrict__ keys) {
+  unsigned long long front, back;
+  list_extent(count, fail, &front, &back);
+  const unsigned long long m = FRONT ? front : back;
+  for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < m;
+       i += (unsigned long long)gridDim.x * blockDim.x) {
+    RayCand* e = list + (FRONT ? i : cap - 1ull - i);
+    const RayCand c = *e;
+    if (c.tmin > key_toi(keys[c.r])) continue;
+    uint32_t r;
+    V3 o, dir;
+    ray_of(rays, order, permuted, c.k, has_pose, cpose, &r, &o, &dir);
+    const ShapeDev sh = load_shape(cd.types, cd.params, cd.pool, c.part);
+    const Pose p = load_pose(cd.poses, c.part);
+    float t;
+    V3 nn;
+    // composite casts keep hits strictly below max_toi (CompositeShapeRef::cast_local_ray)
+    if (!part_cast_ray_analytic(sh, p, o, dir, max_toi, solid != 0, &t, &nn) || !(t < max_toi)) continue;
+    if (has_pose) nn = pose_rotate(cpose, nn);
+    e->hit = 1u;
+    e->t = t;
+    e->nx = nn.x;
+    e->ny = nn.y;
+    e->nz = nn.z;
+    atomicMin(&keys[r], hit_key(t, c.part));
   }
 }
 
@@ -812,10 +1028,14 @@ __global__ void __launch_bounds__(128, 4) k_rays_cand_kind(CompoundDev cd, const
        i += (unsigned long long)gridDim.x * blockDim.x) {
     RayCand* e = list + (TY == SH_CAPSULE ? i : cap - 1ull - i);
     RayCand c = *e;
-    if (c.part == 0xffffffffu || c.tmin > key_toi(keys[c.r])) continue;
+    if (c.part == 0xffffffffu) continue;
+    const float best = key_toi(keys[c.r]);
+    if (c.tmin > best) continue;
     uint32_t r;
     V3 o, dir;
     ray_of(rays, order, permuted, c.k, has_pose, cpose, &r, &o, &dir);
+    // (the candidate passed the local-box pre-test when it was listed); a capsule's axis distance
+    if (TY == SH_CAPSULE && !capsule_may_hit(cd, c.part, o, dir)) continue;
     ShapeDev sh = load_shape(cd.types, cd.params, cd.pool, c.part);
     Pose p = load_pose(cd.poses, c.part);
     float t;
@@ -867,26 +1087,101 @@ static parrygpu_status compound_copy_in(parrygpu_ctx* ctx, DevBuf& dst, const vo
 parrygpu_status shape_rays_reserve(parrygpu_ctx* ctx, RayWaveScratch& sc, uint32_t n) {
   if (n > (1u << 30)) return set_error(ctx, PARRYGPU_INVALID_ARG, "shape-set ray casts take at most 2^30 rays per call");
   uint64_t cap = 4ull * n + 1024;  // below 2^32: the list counters pack two 32-bit counts
-  PG_CUDA(ctx, sc.cands.reserve((cap + n) * sizeof(RayCand)));  // list A (n slots) then list B (cap)
-  PG_CUDA(ctx, sc.counter.reserve(32));
+  PG_CUDA(ctx, sc.cands.reserve((2 * cap + n) * sizeof(RayCand)));  // list A (n slots), list B (cap), list C (cap)
+  PG_CUDA(ctx, sc.counter.reserve(96));  // [0..2] lists A / B, [8..9] list C
   PG_CUDA(ctx, sc.keys.reserve((size_t)n * 8 + 16));
   PG_CUDA(ctx, sc.ovf.reserve((size_t)n + 16));
   sc.cap = cap;
   return PARRYGPU_OK;
 }
 
-// The wavefront cast of n rays (see k_rays_wave). No allocation, no host synchronisation.
+parrygpu_status shape_ray_grid_reserve(parrygpu_ctx* ctx, RayGridScratch& g, uint64_t n_shapes, const float* root) {
+  double ext[3], vol = 1.0;
+  for (int i = 0; i < 3; ++i) {
+    ext[i] = (double)root[3 + i] - (double)root[i];
+    if (!(ext[i] > 0.0) || !std::isfinite(ext[i])) ext[i] = 0.0;
+    vol *= ext[i] > 0.0 ? ext[i] : 1.0;
+  }
+  double c = std::cbrt(vol / (4.0 * (double)(n_shapes ? n_shapes : 1)));
+  uint64_t cells = 0;
+  for (int it = 0; it < 64; ++it) {
+    cells = 1;
+    for (int i = 0; i < 3; ++i) {
+      double r = ext[i] > 0.0 && c > 0.0 ? std::ceil(ext[i] / c) : 1.0;
+      g.res[i] = (uint32_t)std::min(1024.0, std::max(1.0, r));
+      cells *= g.res[i];
+    }
+    if (cells <= (1ull << 22)) break;
+    c *= 1.25;
+  }
+  g.cells = cells;
+  g.cap = 16ull * n_shapes + 4096ull;
+  PG_CUDA(ctx, g.dev.reserve(sizeof(GridDev)));
+  PG_CUDA(ctx, g.starts.reserve(((cells + 1 + 3) & ~3ull) * 4 + 16));
+  PG_CUDA(ctx, g.cursor.reserve(cells * 4 + 16));
+  PG_CUDA(ctx, g.entries.reserve(g.cap * sizeof(GridEntry)));
+  PG_CUDA(ctx, g.sums.reserve((size_t)exclusive_scan_u32_sums((uint32_t)(cells + 1)) * 4 + 16));
+  return PARRYGPU_OK;
+}
+
+// The grid of this frame from the shapes' AABBs and the BVH root box: placement, counts, starts
+// (exclusive scan), capacity check, fill.
+static parrygpu_status build_grid(parrygpu_ctx* ctx, RayGridScratch& g, const float* root, const float* aabbs, const uint32_t* types,
+                                  uint32_t n_shapes) {
+  GridDev* gd = g.dev.as<GridDev>();
+  const uint32_t m = (uint32_t)((g.cells + 1 + 3) & ~3ull);
+  k_grid_setup<<<1, 32, 0, ctx->stream>>>(root, gd, g.res[0], g.res[1], g.res[2]);
+  PG_LAUNCHED(ctx);
+  PG_CUDA(ctx, cudaMemsetAsync(g.starts.ptr, 0, (size_t)m * 4, ctx->stream));
+  PG_CUDA(ctx, cudaMemsetAsync(g.cursor.ptr, 0, g.cells * 4, ctx->stream));
+  k_grid_count<<<div_up(n_shapes, 256), 256, 0, ctx->stream>>>(aabbs, n_shapes, gd, g.starts.as<uint32_t>());
+  PG_LAUNCHED(ctx);
+  k_grid_check<<<1, 32, 0, ctx->stream>>>(gd, g.cap);
+  PG_LAUNCHED(ctx);
+  parrygpu_status s = exclusive_scan_u32_wide(ctx, g.starts.as<uint32_t>(), m, g.sums.as<uint32_t>());
+  if (s != PARRYGPU_OK) return s;
+  k_grid_fill<<<div_up(n_shapes, 256), 256, 0, ctx->stream>>>(aabbs, types, n_shapes, gd, g.starts.as<uint32_t>(), g.cursor.as<uint32_t>(),
+                                                              g.entries.as<GridEntry>(), g.cap);
+  PG_LAUNCHED(ctx);
+  return PARRYGPU_OK;
+}
+
+// The wavefront cast of n rays (see k_rays_wave). No allocation, no host synchronisation. With a
+// grid (and the shapes' AABBs and the BVH root box), the grid is rebuilt and walked; the BVH kernel
+// still launches and casts the rays itself only if the grid reports itself unusable.
 static parrygpu_status launch_wave(parrygpu_ctx* ctx, const WideNode* wide, CompoundDev cd, const float* d_rays, const uint32_t* order,
                                    int permuted, uint32_t n, float max_toi, int solid, int has_pose, Pose pose, uint32_t* d_part,
-                                   float* d_toi, float* d_nrm, RayWaveScratch& sc) {
+                                   float* d_toi, float* d_nrm, RayWaveScratch& sc, RayGridScratch* rg = nullptr, const float* aabbs = nullptr,
+                                   const float* root = nullptr, uint32_t n_shapes = 0) {
   unsigned long long* cnt = sc.counter.as<unsigned long long>();
-  WaveBufs wb{sc.cands.as<RayCand>(), sc.cands.as<RayCand>() + n, sc.cap, cnt, sc.keys.as<unsigned long long>(), sc.ovf.as<uint8_t>()};
+  WaveBufs wb{sc.cands.as<RayCand>(), sc.cands.as<RayCand>() + n, sc.cap, cnt, sc.keys.as<unsigned long long>(), sc.ovf.as<uint8_t>(),
+              sc.cands.as<RayCand>() + n + sc.cap};
   uint32_t grid = (uint32_t)(ctx->sm_count > 0 ? ctx->sm_count : 152) * 16;
   PG_CUDA(ctx, cudaMemsetAsync(cnt, 0, 16, ctx->stream));
   PG_CUDA(ctx, cudaMemsetAsync(cnt + 2, 0xff, 8, ctx->stream));
-  k_rays_wave<<<div_up(n, 128), 128, 0, ctx->stream>>>(wide, cd, d_rays, n, max_toi, solid, has_pose, pose, d_part, d_toi, d_nrm, ctx->d_err,
-                                                       order, permuted, wb);
+  PG_CUDA(ctx, cudaMemsetAsync(cnt + 8, 0, 8, ctx->stream));
+  PG_CUDA(ctx, cudaMemsetAsync(cnt + 9, 0xff, 8, ctx->stream));
+  const bool use_grid = rg && rg->cells && aabbs && root;
+  const GridDev* gd = nullptr;
+  if (use_grid) {
+    parrygpu_status s = build_grid(ctx, *rg, root, aabbs, cd.types, n_shapes);
+    if (s != PARRYGPU_OK) return s;
+    gd = rg->dev.as<GridDev>();
+    k_rays_walk<<<div_up(n, 128), 128, 0, ctx->stream>>>(cd, d_rays, n, max_toi, has_pose, pose, d_part, d_toi, d_nrm, order, permuted, wb, gd,
+                                                         rg->starts.as<uint32_t>(), rg->entries.as<GridEntry>());
+    PG_LAUNCHED(ctx);
+  }
+  k_rays_wave<<<div_up(n, 128), 128, 0, ctx->stream>>>(wide, cd, d_rays, n, max_toi, solid, has_pose, pose, d_part, d_toi, d_nrm,
+                                                       ctx->d_err, order, permuted, wb, gd);
   PG_LAUNCHED(ctx);
+  if (use_grid) {  // the walk's analytic candidates first: their hits prune the GJK candidates
+    k_rays_cand_analytic<true><<<grid, 128, 0, ctx->stream>>>(cd, d_rays, max_toi, solid, has_pose, pose, order, permuted, wb.c, sc.cap,
+                                                              cnt + 8, cnt + 9, wb.keys);
+    PG_LAUNCHED(ctx);
+    k_rays_cand_analytic<false><<<grid, 128, 0, ctx->stream>>>(cd, d_rays, max_toi, solid, has_pose, pose, order, permuted, wb.c, sc.cap,
+                                                               cnt + 8, cnt + 9, wb.keys);
+    PG_LAUNCHED(ctx);
+  }
   // list A, then list B; capsules and hulls of each in their own launches
   k_rays_cand_kind<SH_CAPSULE><<<grid, 128, 0, ctx->stream>>>(cd, d_rays, max_toi, solid, has_pose, pose, order, permuted, wb.a, n, cnt + 1,
                                                               nullptr, wb.keys);
@@ -904,6 +1199,10 @@ static parrygpu_status launch_wave(parrygpu_ctx* ctx, const WideNode* wide, Comp
   PG_LAUNCHED(ctx);
   k_rays_finish<<<grid, 128, 0, ctx->stream>>>(wb.b, sc.cap, cnt, cnt + 2, wb.keys, d_part, d_toi, d_nrm);
   PG_LAUNCHED(ctx);
+  if (use_grid) {
+    k_rays_finish<<<grid, 128, 0, ctx->stream>>>(wb.c, sc.cap, cnt + 8, cnt + 9, wb.keys, d_part, d_toi, d_nrm);
+    PG_LAUNCHED(ctx);
+  }
   // rays whose candidates overflowed list B: the single-kernel cast, for them only
   k_compound_rays<<<div_up(n, 128), 128, 0, ctx->stream>>>(wide, cd, d_rays, n, max_toi, solid, has_pose, pose, d_part, d_toi, d_nrm,
                                                            ctx->d_err, order, permuted, sc.ovf.as<uint8_t>());
@@ -921,11 +1220,13 @@ parrygpu_status launch_hull_boxes(parrygpu_ctx* ctx, const uint32_t* types, cons
 
 parrygpu_status launch_shape_rays(parrygpu_ctx* ctx, const parrygpu_bvh* bvh, const uint32_t* types, const float* params,
                                   const float* poses, const float* pool, const float* hull_box, const float* d_rays, const uint32_t* order,
-                                  uint32_t n, float max_toi, uint32_t* d_part, float* d_toi, float* d_nrm, RayWaveScratch& scratch) {
+                                  uint32_t n, float max_toi, uint32_t* d_part, float* d_toi, float* d_nrm, RayWaveScratch& scratch,
+                                  RayGridScratch* grid, const float* d_aabbs) {
   if (n == 0 || bvh->n_leaves == 0) return PARRYGPU_OK;
   CompoundDev cd{types, (const float4*)params, poses, pool, (const float4*)hull_box};
   Pose pose{0.f, 0.f, 0.f, 1.f, v3(0.f, 0.f, 0.f)};
-  return launch_wave(ctx, bvh->wide.as<WideNode>(), cd, d_rays, order, order ? 1 : 0, n, max_toi, 1, 0, pose, d_part, d_toi, d_nrm, scratch);
+  return launch_wave(ctx, bvh->wide.as<WideNode>(), cd, d_rays, order, order ? 1 : 0, n, max_toi, 1, 0, pose, d_part, d_toi, d_nrm, scratch,
+                     grid, d_aabbs, grid ? bvh->root_aabb.as<float>() : nullptr, bvh->n_leaves);
 }
 
 extern "C" {

@@ -191,6 +191,98 @@ uint32_t radix_sort_hist_entries(uint32_t n) { return div_up(n ? n : 1, RS_TILE)
 
 // In-place exclusive prefix sum of `m` words in one block (the buffer holds m rounded up to a
 // multiple of 4 words, the padding zeroed).
+namespace {
+
+constexpr uint32_t MSCAN_THREADS = 256;
+constexpr uint32_t MSCAN_TILE = MSCAN_THREADS * 16;  // words per block
+
+// Sum of each tile of `data` (m words, a multiple of 4) into sums[tile].
+__global__ void __launch_bounds__(MSCAN_THREADS) k_mscan_reduce(const uint32_t* __restrict__ data, uint32_t m, uint32_t* __restrict__ sums) {
+  __shared__ uint32_t ws[MSCAN_THREADS / 32];
+  const uint32_t base = blockIdx.x * MSCAN_TILE, tid = threadIdx.x;
+  uint32_t t = 0;
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    const uint32_t idx = base + (j * MSCAN_THREADS + tid) * 4;
+    if (idx < m) {
+      const uint4 v = *reinterpret_cast<const uint4*>(data + idx);
+      t += v.x + v.y + v.z + v.w;
+    }
+  }
+  t = __reduce_add_sync(0xffffffffu, t);
+  if ((tid & 31) == 0) ws[tid >> 5] = t;
+  __syncthreads();
+  if (tid < 32) {
+    uint32_t v = tid < MSCAN_THREADS / 32 ? ws[tid] : 0u;
+    v = __reduce_add_sync(0xffffffffu, v);
+    if (tid == 0) sums[blockIdx.x] = v;
+  }
+}
+
+// Exclusive scan of each tile in place, offset by the tile's scanned sum: 4 consecutive words per
+// thread per step, warp-shuffle scans, a running carry over the tile's 4 steps.
+__global__ void __launch_bounds__(MSCAN_THREADS) k_mscan_tiles(uint32_t* __restrict__ data, uint32_t m, const uint32_t* __restrict__ offs) {
+  __shared__ uint32_t ws[MSCAN_THREADS / 32];
+  __shared__ uint32_t carry;
+  const uint32_t tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+  if (tid == 0) carry = offs[blockIdx.x];
+  __syncthreads();
+  for (int j = 0; j < 4; ++j) {
+    const uint32_t idx = blockIdx.x * MSCAN_TILE + (j * MSCAN_THREADS + tid) * 4;
+    uint4 v = make_uint4(0u, 0u, 0u, 0u);
+    if (idx < m) v = *reinterpret_cast<const uint4*>(data + idx);
+    const uint32_t t = v.x + v.y + v.z + v.w;
+    uint32_t incl = t;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= (uint32_t)o) incl += y;
+    }
+    if (lane == 31) ws[w] = incl;
+    __syncthreads();
+    if (w == 0) {
+      uint32_t x = lane < MSCAN_THREADS / 32 ? ws[lane] : 0u;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= (uint32_t)o) x += y;
+      }
+      if (lane < MSCAN_THREADS / 32) ws[lane] = x;
+    }
+    __syncthreads();
+    const uint32_t excl = carry + (w ? ws[w - 1] : 0u) + (incl - t);
+    if (idx < m) {
+      uint4 o;
+      o.x = excl;
+      o.y = excl + v.x;
+      o.z = o.y + v.y;
+      o.w = o.z + v.z;
+      *reinterpret_cast<uint4*>(data + idx) = o;
+    }
+    __syncthreads();
+    if (tid == 0) carry += ws[MSCAN_THREADS / 32 - 1];
+    __syncthreads();
+  }
+}
+
+}  // namespace
+
+uint32_t exclusive_scan_u32_sums(uint32_t m) { return (m + MSCAN_TILE - 1) / MSCAN_TILE + 4; }
+
+parrygpu_status exclusive_scan_u32_wide(parrygpu_ctx* ctx, uint32_t* data, uint32_t m, uint32_t* sums) {
+  if (m == 0) return PARRYGPU_OK;
+  m = (m + 3u) & ~3u;
+  const uint32_t tiles = (m + MSCAN_TILE - 1) / MSCAN_TILE;
+  k_mscan_reduce<<<tiles, MSCAN_THREADS, 0, ctx->stream>>>(data, m, sums);
+  PG_LAUNCHED(ctx);
+  PG_CUDA(ctx, cudaMemsetAsync(sums + tiles, 0, ((tiles + 3u) & ~3u) * 4 - tiles * 4 + 4, ctx->stream));
+  k_rs_scan<<<1, SCAN_THREADS, 0, ctx->stream>>>(sums, (tiles + 3u) & ~3u);
+  PG_LAUNCHED(ctx);
+  k_mscan_tiles<<<tiles, MSCAN_THREADS, 0, ctx->stream>>>(data, m, sums);
+  PG_LAUNCHED(ctx);
+  return PARRYGPU_OK;
+}
+
 parrygpu_status exclusive_scan_u32(parrygpu_ctx* ctx, uint32_t* data, uint32_t m) {
   if (m == 0) return PARRYGPU_OK;
   k_rs_scan<<<1, SCAN_THREADS, 0, ctx->stream>>>(data, (m + 3u) & ~3u);

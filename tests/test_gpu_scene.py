@@ -158,3 +158,55 @@ def test_scene_learned_seeding_matches_oracle(gpu_ctx, oracle_lib, use_graph, fr
     poly = (ta != BALL) & (tb != BALL) & ~((ta == tb) & ((ta == CUBOID) | (ta == CAPSULE)))
     assert runs[0]["seeded_pairs"] == int(poly.sum()) > 0 and runs[1]["seeded_pairs"] == 0
     assert runs[0]["gjk_iters"] != runs[1]["gjk_iters"]
+
+
+def _grid_rays(n, extent, seed):
+    """Random rays plus axis-aligned ones (zero direction components), rays from outside the shapes'
+    bounds, and a zero-direction ray."""
+    rng = np.random.default_rng(seed)
+    o = rng.uniform(-extent - 5, extent + 5, (n, 3))
+    d = rng.normal(size=(n, 3))
+    d[: n // 8] = np.eye(3)[rng.integers(0, 3, n // 8)] * rng.choice([-1.0, 1.0], (n // 8, 1))
+    d[n // 8: n // 4, rng.integers(0, 3)] = 0.0
+    d[-1] = 0.0
+    o[n // 4: n // 4 + n // 16] *= 4.0
+    nz = np.linalg.norm(d, axis=1, keepdims=True)
+    d = np.where(nz > 0, d / np.maximum(nz, 1e-30), d)
+    return np.concatenate([o, d], axis=1).astype(np.float32)
+
+
+@pytest.mark.parametrize("giant", [False, True])
+def test_scene_ray_grid_matches_bvh_and_oracle(oracle_lib, giant):
+    """The frame pipeline's rays through the per-frame uniform grid and through the BVH give the same
+    answers, equal to the oracle's, for random, axis-aligned, outside-origin and zero-direction rays.
+    With every cuboid 3 times larger the entries outgrow the grid's capacity, the grid reports
+    itself unusable and the BVH kernel casts the rays: same answers again."""
+    import parry_gb300 as pg
+    O = oracle_lib
+    s, vel, _ = _inputs(900, 53, extent=7.0)
+    if giant:
+        t, prm, pos, pool = s.arrays()
+        poly = s.polyhedra()
+        from parry_gb300.shapes import CUBOID
+        t = t.copy()
+        prm = prm.copy()
+        prm[t == CUBOID, :3] *= 3.0
+        s = pg.ShapeSet.from_arrays(t, prm, pos, pool, poly)
+    rays = _grid_rays(6000, 7.0, 5)
+    out = []
+    for mode in (1, 2):
+        ctx = pg.Context(0, scene_ray_grid=mode)
+        sc = pg.Scene(ctx, s, vel, 0.1, 1 << 20)
+        sc.set_rays(rays, 40.0)
+        sc.step(1.0 / 60.0, 3, use_graph=True)
+        out.append(sc.read())
+        sc.close()
+        ctx.close()
+    a, b = out
+    for key in ("ray_part", "ray_toi", "ray_normal"):
+        np.testing.assert_array_equal(a[key], b[key])
+    want = O.scene_frames(s, vel, 0.1, 1.0 / 60.0, 3, rays=rays, max_toi=40.0)
+    np.testing.assert_array_equal(a["ray_part"], want["ray_part"])
+    np.testing.assert_array_equal(a["ray_toi"], want["ray_toi"])
+    np.testing.assert_array_equal(a["ray_normal"], want["ray_normal"])
+    assert int((a["ray_part"] != pg.NO_HIT).sum()) > 300

@@ -85,3 +85,69 @@ def test_candidate_overflow_falls_back_exactly(gpu_ctx, oracle_lib):
         po, to, no = O.Compound(s).cast_rays_and_get_normal(rays, 1000.0, solid=solid)
         _compare(p, t, nn, po, to, no, f"solid={solid}")
         assert np.all(p != pg.NO_HIT)
+
+
+def _grazing_rays(rng, n, centre, radial, along, offset, dist):
+    """Rays passing the point centre + radial * offset (radial a unit vector) with a direction
+    perpendicular to `radial` (tilted by `along`), starting `dist` before that point."""
+    side = np.cross(radial, along)
+    side /= np.linalg.norm(side, axis=1, keepdims=True)
+    tilt = rng.uniform(-0.5, 0.5, (n, 1))
+    d = side + tilt * along
+    d -= radial * np.sum(d * radial, axis=1, keepdims=True)
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    p = centre + radial * offset[:, None]
+    return np.concatenate([p - d * dist[:, None], d], 1).astype(np.float32)
+
+
+@pytest.mark.parametrize("solid", [True, False])
+def test_grazing_rays_match_oracle(gpu_ctx, oracle_lib, solid):
+    """Rays grazing capsules and hulls, from just inside to 5 % outside their surfaces. On rounded
+    shapes parry's GJK ray cast reports hits a little outside the surface; the pre-tests that drop
+    candidates before the GJK ray cast (local box, capsule axis distance) must not drop any of them,
+    so every answer equals the oracle's."""
+    from parry_gb300.shapes import CAPSULE, CONVEX
+    rng = np.random.default_rng(21 + solid)
+    s = CC.mixed_scene(400, seed=23, extent=40.0)
+    t, prm, pos, pool = s.arrays()
+    rays = []
+    for i in np.nonzero((t == CAPSULE) | (t == CONVEX))[0][:120]:
+        m = 4000
+        q, c = pos[i, :4].astype(np.float64), pos[i, 4:7].astype(np.float64)
+        u = np.stack([q[:3]] * m)
+        w = q[3]
+
+        def rot(v):  # world <- local
+            tt = 2 * np.cross(u, v)
+            return v + w * tt + np.cross(u, tt)
+        if t[i] == CAPSULE:
+            h, r = float(prm[i, 0]), float(prm[i, 1])
+            phi = rng.uniform(0, 2 * np.pi, m)
+            radial_l = np.stack([np.cos(phi), np.zeros(m), np.sin(phi)], 1)
+            y = rng.uniform(-h, h, m)
+            base_l = np.stack([np.zeros(m), y, np.zeros(m)], 1)
+            offset = r * (1.0 + rng.uniform(-0.01, 0.05, m))
+            along = rot(np.tile([0.0, 1.0, 0.0], (m, 1)))
+        else:
+            first, count = int(prm[i].view(np.uint32)[0]), int(prm[i].view(np.uint32)[1])
+            v = pool[first:first + count].astype(np.float64)
+            radial_l = rng.normal(size=(m, 3))
+            radial_l /= np.linalg.norm(radial_l, axis=1, keepdims=True)
+            supp = np.max(radial_l @ v.T, axis=1)  # support distance along each radial direction
+            ext = np.max(np.abs(v))
+            base_l = np.zeros((m, 3))
+            offset = supp + ext * rng.uniform(-0.01, 0.05, m)
+            along = rot(np.cross(radial_l, rng.normal(size=(m, 3))))
+            along /= np.linalg.norm(along, axis=1, keepdims=True)
+        radial = rot(radial_l)
+        centre = rot(base_l) + c
+        rays.append(_grazing_rays(rng, m, centre, radial, along, offset, rng.uniform(1, 60, m)))
+    rays = np.concatenate(rays)
+    comp = pg.Compound(gpu_ctx, s)
+    p, tt, n = comp.cast_rays_and_get_normal(rays, 100.0, solid=solid)
+    po, to, no = oracle_lib.Compound(s).cast_rays_and_get_normal(rays, 100.0, solid=solid)
+    np.testing.assert_array_equal(p, po)
+    hit = po != pg.NO_HIT
+    np.testing.assert_array_equal(tt[hit], to[hit])
+    np.testing.assert_array_equal(n[hit], no[hit])
+    assert 0.1 < hit.mean() < 0.95
