@@ -136,7 +136,7 @@ void parrygpu_destroy(parrygpu_ctx* ctx) {
   ctx->epa_ws.release();
   ctx->epa_ws_big.release();
   ctx->ct_ovf.release();
-  for (DevBuf* d : {&ctx->mf.queue, &ctx->mf.counters, &ctx->mf.bins, &ctx->mf.epa_ws, &ctx->mf.redo}) d->release();
+  for (DevBuf* d : {&ctx->mf.queue, &ctx->mf.counters, &ctx->mf.bins, &ctx->mf.epa_ws}) d->release();
   for (DevBuf* d : {&ctx->ray_wave.cands, &ctx->ray_wave.counter, &ctx->ray_wave.keys, &ctx->ray_wave.ovf}) d->release();
   if (ctx->d_err) cudaFree(ctx->d_err);
   if (ctx->h_err) cudaFreeHost(ctx->h_err);

@@ -53,7 +53,7 @@ struct RayGridScratch {
 // Scratch of the contact-manifold kernels (manifold.cu): EPA queue, counters (queue length, stats,
 // bin lengths), per-kind pair bins, per-slot EPA polytope workspaces.
 struct MfScratch {
-  DevBuf queue, counters, bins, epa_ws, redo;
+  DevBuf queue, counters, bins, epa_ws;
   uint64_t cap = 0;
 };
 

@@ -1015,11 +1015,10 @@ enum : uint32_t {
   MK_PFM, MK_PFM_CUBOID_HULL, MK_PFM_CAPSULE_HULL, MK_PFM_HULL_HULL, MK_PFM_TRIANGLE, MK_CUBOID_TRIANGLE, MK_KINDS
 };
 // counters: [0] EPA queue length, [1..3] GJK / EPA stats, [4 + kind] bin lengths, [15] learned-seed
-// list length, [16] EPAs redone on global workspaces
+// list length
 constexpr int MF_CTR_BINS = 4;
 constexpr int MF_CTR_SEED = 15;
-constexpr int MF_CTR_REDO = 16;
-constexpr size_t MF_CTR_BYTES = 256;
+constexpr size_t MF_CTR_BYTES = 128;
 static_assert(MF_CTR_BINS + MK_KINDS <= MF_CTR_SEED, "the 128-byte counter block holds every bin length and the seed count");
 
 __device__ __forceinline__ uint32_t manifold_kind(uint32_t t1, uint32_t t2) {
@@ -1173,9 +1172,9 @@ __global__ void __launch_bounds__(MF_THREADS) k_mf_kind(ShapeArrays sh, const ui
 }
 
 // One queued EPA (the ball projections or the polyhedral pair's contact) and its feature clipping,
-// on workspace `ws`. False when the polytope outgrew the workspace (nothing written).
+// on workspace `ws`.
 template <class WS>
-__device__ __forceinline__ bool manifold_epa_entry(const WS& ws, bool last_resort, ShapeArrays& sh, const uint32_t* __restrict__ pairs,
+__device__ __forceinline__ void manifold_epa_entry(const WS& ws, ShapeArrays& sh, const uint32_t* __restrict__ pairs,
                                                    float prediction, uint32_t* __restrict__ recs, const uint32_t* __restrict__ q,
                                                    uint32_t* __restrict__ err, uint32_t* iters) {
   uint64_t k;
@@ -1196,10 +1195,7 @@ __device__ __forceinline__ bool manifold_epa_entry(const WS& ws, bool last_resor
     float br1, br2;
     ShapeDev p1 = pfm_of(s1, &br1), p2 = pfm_of(s2, &br2);
     int res = epa_closest_points(ws, pos12, p1, p2, s, &q1, &q2, &nn, iters);
-    if (res == EPA_OVERFLOW) {
-      if (!last_resort) return false;
-      atomicOr(err, ERR_POLYTOPE_FULL);
-    }
+    if (res == EPA_OVERFLOW) atomicOr(err, ERR_POLYTOPE_FULL);
     // EPA failure: contact_support_map_support_map_with_params returns NoIntersection(x axis)
     const uint32_t j1 = constraint_row(sh, a), j2 = constraint_row(sh, b);
     if (res == EPA_OK) finish_pfm(r, pos12, s1, h1, s2, h2, GJK_CLOSEST, q1, q2, nn, &overflow, &bad, sh.pseudo, j1, j2);
@@ -1217,66 +1213,26 @@ __device__ __forceinline__ bool manifold_epa_entry(const WS& ws, bool last_resor
     ShapeDev origin;
     origin.type = SH_ORIGIN;
     int res = epa_closest_points(ws, minv, cs, origin, s, &q1, &q2, &nn, iters);
-    if (res == EPA_OVERFLOW) {
-      if (!last_resort) return false;
-      atomicOr(err, ERR_POLYTOPE_FULL);
-    }
+    if (res == EPA_OVERFLOW) atomicOr(err, ERR_POLYTOPE_FULL);
     V3 proj = res == EPA_OK ? q1 : center;
     uint32_t fid = hull_projection_feature(cs, ch, center, proj, true, &bad);
     finish_convex_ball(r, cpos, proj, true, fid, radius, prediction, ball_first);
   }
   if (overflow) atomicOr(err, ERR_CAPACITY);
   if (bad) atomicOr(err, ERR_BAD_INDEX);
-  return true;
 }
 
-// The queued EPAs with the polytope in shared memory: MF_SMEM_SLOTS threads per block, each with
-// its own slot (an access costs the shared-memory latency instead of an L2 round trip, and the
-// queue of a frame is a few thousand entries at most). An EPA whose polytope outgrows the slot is
-// listed (its iterations are not counted) for k_manifolds_epa, which redoes it on a global slot.
-using EpaMfLayout = EpaLayout<32, 96, 32, 64, 6>;
-constexpr int MF_SMEM_SLOTS = 32;
-constexpr size_t MF_SMEM_BYTES = (size_t)MF_SMEM_SLOTS * EpaMfLayout::WORDS * 4;
-static_assert((EpaMfLayout::WORDS * 4) % 16 == 0, "16-byte aligned slots");
-
-__global__ void __launch_bounds__(MF_SMEM_SLOTS) k_manifolds_epa_smem(ShapeArrays sh, const uint32_t* __restrict__ pairs, float prediction,
-                                                                      uint32_t* __restrict__ recs, const uint32_t* __restrict__ queue,
-                                                                      const unsigned long long* __restrict__ qcount,
-                                                                      uint32_t* __restrict__ redo, unsigned long long* __restrict__ redo_count,
-                                                                      unsigned long long* __restrict__ stats, uint32_t* __restrict__ err) {
-  extern __shared__ __align__(16) uint32_t mf_epa_smem[];
-  const EpaWsT<EpaMfLayout> ws{mf_epa_smem + (size_t)threadIdx.x * EpaMfLayout::WORDS};
-  const unsigned long long total = *qcount;
-  uint32_t iters = 0, calls = 0;
-  for (unsigned long long e = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; e < total;
-       e += (unsigned long long)gridDim.x * blockDim.x) {
-    uint32_t it = 0;
-    if (manifold_epa_entry(ws, false, sh, pairs, prediction, recs, queue + (size_t)e * QUEUE_WORDS, err, &it)) {
-      iters += it;
-      calls++;
-    } else {
-      redo[atomicAdd(redo_count, 1ull)] = (uint32_t)e;
-    }
-  }
-  if (stats) {
-    if (iters) atomicAdd(&stats[1], (unsigned long long)iters);
-    if (calls) atomicAdd(&stats[2], (unsigned long long)calls);
-  }
-}
-
-// The queued EPAs on global workspace slots: all of them, or (redo) the listed ones.
+// The queued EPAs, one per thread of a persistent grid, each thread on its own global workspace slot.
 __global__ void __launch_bounds__(MF_EPA_THREADS) k_manifolds_epa(ShapeArrays sh, const uint32_t* __restrict__ pairs, float prediction,
                                                                   uint32_t* __restrict__ recs, const uint32_t* __restrict__ queue,
                                                                   const unsigned long long* __restrict__ qcount, uint32_t* __restrict__ ws_pool,
-                                                                  unsigned long long* __restrict__ stats, uint32_t* __restrict__ err,
-                                                                  const uint32_t* __restrict__ redo) {
+                                                                  unsigned long long* __restrict__ stats, uint32_t* __restrict__ err) {
   const uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x;
   EpaWs ws = epa_slot(ws_pool, slot);
   const unsigned long long total = *qcount;
   uint32_t iters = 0, calls = 0;
-  for (unsigned long long i = slot; i < total; i += (unsigned long long)gridDim.x * blockDim.x) {
-    const unsigned long long e = redo ? redo[i] : i;
-    manifold_epa_entry(ws, true, sh, pairs, prediction, recs, queue + (size_t)e * QUEUE_WORDS, err, &iters);
+  for (unsigned long long e = slot; e < total; e += (unsigned long long)gridDim.x * blockDim.x) {
+    manifold_epa_entry(ws, sh, pairs, prediction, recs, queue + (size_t)e * QUEUE_WORDS, err, &iters);
     calls++;
   }
   if (stats) {
@@ -1298,8 +1254,6 @@ __global__ void __launch_bounds__(MF_EPA_THREADS) k_manifolds_epa(ShapeArrays sh
 parrygpu_status pg::manifolds_reserve(parrygpu_ctx* ctx, uint64_t cap, MfScratch& sc) {
   PG_CUDA(ctx, sc.queue.reserve((size_t)cap * QUEUE_WORDS * 4));
   PG_CUDA(ctx, sc.counters.reserve(MF_CTR_BYTES));
-  PG_CUDA(ctx, sc.redo.reserve((size_t)cap * 4 + 16));
-  PG_CUDA(ctx, cudaFuncSetAttribute(k_manifolds_epa_smem, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)MF_SMEM_BYTES));
   PG_CUDA(ctx, sc.bins.reserve((size_t)cap * MK_KINDS * 4));
   uint32_t epa_blocks = (uint32_t)(ctx->sm_count > 0 ? ctx->sm_count : 152) * 8;
   PG_CUDA(ctx, sc.epa_ws.reserve((size_t)epa_blocks * MF_EPA_THREADS * EPA_SLOT_BYTES));
@@ -1344,13 +1298,8 @@ parrygpu_status pg::launch_manifolds(parrygpu_ctx* ctx, const ShapeArrays& sh, c
   if ((s = launch_kind<MK_HULL_BALL>(ctx, sh, d_pairs, prediction, d_recs, sc, stride, grid)) != PARRYGPU_OK) return s;
   if ((s = launch_kind<MK_PFM>(ctx, sh, d_pairs, prediction, d_recs, sc, stride, grid, init_dirs)) != PARRYGPU_OK) return s;
   if ((s = launch_kind<MK_CUBOID_TRIANGLE>(ctx, sh, d_pairs, prediction, d_recs, sc, stride, grid)) != PARRYGPU_OK) return s;
-  // the queued EPAs on shared-memory slots, then on global slots those that outgrew them
-  k_manifolds_epa_smem<<<sms, MF_SMEM_SLOTS, MF_SMEM_BYTES, ctx->stream>>>(sh, d_pairs, prediction, d_recs, sc.queue.as<uint32_t>(), ctr,
-                                                                          sc.redo.as<uint32_t>(), ctr + MF_CTR_REDO, ctr + 1, ctx->d_err);
-  PG_LAUNCHED(ctx);
-  k_manifolds_epa<<<epa_blocks, MF_EPA_THREADS, 0, ctx->stream>>>(sh, d_pairs, prediction, d_recs, sc.queue.as<uint32_t>(),
-                                                                 ctr + MF_CTR_REDO, sc.epa_ws.as<uint32_t>(), ctr + 1, ctx->d_err,
-                                                                 sc.redo.as<uint32_t>());
+  k_manifolds_epa<<<epa_blocks, MF_EPA_THREADS, 0, ctx->stream>>>(sh, d_pairs, prediction, d_recs, sc.queue.as<uint32_t>(), ctr,
+                                                                 sc.epa_ws.as<uint32_t>(), ctr + 1, ctx->d_err);
   PG_LAUNCHED(ctx);
   return PARRYGPU_OK;
 }

@@ -358,7 +358,7 @@ void parrygpu_scene_destroy(parrygpu_scene* sc) {
   cudaDeviceSynchronize();  // frames in flight still read the scene's buffers
   drop_graph(sc);
   for (DevBuf* d : {&sc->types, &sc->params, &sc->poses, &sc->vel, &sc->pool, &sc->aabbs, &sc->hull_box, &sc->counts, &sc->mf.queue, &sc->mf.counters,
-                    &sc->mf.epa_ws, &sc->mf.bins, &sc->mf.redo, &sc->rays, &sc->ray_order, &sc->ray_part,
+                    &sc->mf.epa_ws, &sc->mf.bins, &sc->rays, &sc->ray_order, &sc->ray_part,
                     &sc->ray_toi, &sc->ray_nrm, &sc->bvh.wide, &sc->bvh.leaf_parent, &sc->bvh.node_parent, &sc->bvh.leaf_index,
                     &sc->bvh.flags, &sc->bvh.root_aabb, &sc->bvh.info})
     d->release();

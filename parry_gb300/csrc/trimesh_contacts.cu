@@ -240,7 +240,7 @@ void parrygpu_trimesh_contacts_destroy(parrygpu_trimesh_contacts* tc) {
   cudaDeviceSynchronize();
   for (DevBuf* d : {&tc->tri_pool, &tc->aabb, &tc->inter[0], &tc->inter[1], &tc->count[0], &tc->count[1], &tc->recs[0], &tc->recs[1],
                     &tc->map, &tc->pairs, &tc->types, &tc->params, &tc->poses, &tc->pool, &tc->mf.queue, &tc->mf.counters, &tc->mf.bins,
-                    &tc->mf.epa_ws, &tc->mf.redo})
+                    &tc->mf.epa_ws})
     d->release();
   delete tc;
 }
