@@ -630,23 +630,38 @@ class Scene:
         check(lib().parrygpu_scene_info(self._ctx.handle, self._h, C.byref(f), C.byref(n)), self._ctx.handle)
         return f.value, n.value
 
-    def read(self) -> dict:
+    def read(self, out: dict | None = None) -> dict:
         """Host copies of the current poses, pairs (unsorted) with their manifold records, and the
-        last frame's ray results."""
+        last frame's ray results. `out` (optional) holds preallocated destinations under the same
+        keys - numpy arrays or (pinned) CPU torch tensors: poses (n, 7) f32, pairs (capacity, 2) u32,
+        manifolds (capacity, RECORD_WORDS) u32 words, ray_part (n_rays,) u32, ray_toi (n_rays,) f32,
+        ray_normal (n_rays, 3) f32 - so a frame loop reads into pinned memory without allocating;
+        the returned dict then views their first n_pairs rows."""
         from .manifold import new_manifolds
         _, npairs = self.info()
         npairs = min(npairs, self.capacity)
-        poses = np.empty((self.n, 7), np.float32)
-        pairs = np.empty((npairs, 2), np.uint32)
-        recs = new_manifolds(npairs)
-        part = np.empty(self.n_rays, np.uint32)
-        toi = np.empty(self.n_rays, np.float32)
-        nrm = np.empty((self.n_rays, 3), np.float32)
-        check(lib().parrygpu_scene_read(self._ctx.handle, self._h, poses.ctypes.data, pairs.ctypes.data if npairs else None,
-                                        recs.ctypes.data if npairs else None, npairs, part.ctypes.data if self.n_rays else None,
-                                        toi.ctypes.data if self.n_rays else None, nrm.ctypes.data if self.n_rays else None),
+        if out is None:
+            dst = {"poses": np.empty((self.n, 7), np.float32), "pairs": np.empty((npairs, 2), np.uint32),
+                   "manifolds": new_manifolds(npairs), "ray_part": np.empty(self.n_rays, np.uint32),
+                   "ray_toi": np.empty(self.n_rays, np.float32), "ray_normal": np.empty((self.n_rays, 3), np.float32)}
+        else:
+            dst = out
+            assert tuple(dst["poses"].shape) == (self.n, 7) and len(dst["pairs"]) >= npairs and len(dst["manifolds"]) >= npairs
+            assert len(dst["ray_part"]) == self.n_rays and len(dst["ray_toi"]) == self.n_rays and len(dst["ray_normal"]) == self.n_rays
+
+        def ptr(a):
+            return a.data_ptr() if _is_torch(a) else a.ctypes.data
+        has_rays = self.n_rays > 0
+        check(lib().parrygpu_scene_read(self._ctx.handle, self._h, ptr(dst["poses"]), ptr(dst["pairs"]) if npairs else None,
+                                        ptr(dst["manifolds"]) if npairs else None, npairs, ptr(dst["ray_part"]) if has_rays else None,
+                                        ptr(dst["ray_toi"]) if has_rays else None, ptr(dst["ray_normal"]) if has_rays else None),
               self._ctx.handle)
-        return {"poses": poses, "pairs": pairs, "manifolds": recs, "ray_part": part, "ray_toi": toi, "ray_normal": nrm}
+        if out is None:
+            return dst
+        res = dict(dst)
+        res["pairs"] = dst["pairs"][:npairs]
+        res["manifolds"] = dst["manifolds"][:npairs]
+        return res
 
     def stats(self) -> dict:
         """The last frame's narrow-phase counters: GJK / EPA iterations, EPA calls, and the pairs that

@@ -210,3 +210,28 @@ def test_scene_ray_grid_matches_bvh_and_oracle(oracle_lib, giant):
     np.testing.assert_array_equal(a["ray_toi"], want["ray_toi"])
     np.testing.assert_array_equal(a["ray_normal"], want["ray_normal"])
     assert int((a["ray_part"] != pg.NO_HIT).sum()) > 300
+
+
+def test_scene_read_into_pinned_buffers(gpu_ctx):
+    """Scene.read into caller-provided (pinned) buffers gives the same state as a fresh read."""
+    import torch
+    import parry_gb300 as pg
+    s, vel, rays = _inputs(700, 61, n_rays=2000)
+    sc = pg.Scene(gpu_ctx, s, vel, 0.1, 1 << 15)
+    sc.set_rays(rays, 100.0)
+    sc.step(1.0 / 60.0, 2, use_graph=True)
+    a = sc.read()
+    pin = {"poses": torch.empty((700, 7), dtype=torch.float32, pin_memory=True),
+           "pairs": torch.empty((1 << 15, 2), dtype=torch.int32, pin_memory=True),
+           "manifolds": torch.empty((1 << 15, M.RECORD_WORDS), dtype=torch.int32, pin_memory=True),
+           "ray_part": torch.empty(2000, dtype=torch.int32, pin_memory=True),
+           "ray_toi": torch.empty(2000, dtype=torch.float32, pin_memory=True),
+           "ray_normal": torch.empty((2000, 3), dtype=torch.float32, pin_memory=True)}
+    b = sc.read(out=pin)
+    sc.close()
+    np.testing.assert_array_equal(a["poses"], b["poses"].numpy())
+    np.testing.assert_array_equal(a["pairs"], b["pairs"].numpy().view(np.uint32))
+    np.testing.assert_array_equal(M.as_words(a["manifolds"]), b["manifolds"].numpy().view(np.uint32))
+    np.testing.assert_array_equal(a["ray_part"], b["ray_part"].numpy().view(np.uint32))
+    np.testing.assert_array_equal(a["ray_toi"], b["ray_toi"].numpy())
+    np.testing.assert_array_equal(a["ray_normal"], b["ray_normal"].numpy())
