@@ -562,12 +562,15 @@ __global__ void __launch_bounds__(128) k_compound_rays(const WideNode* __restric
 //                   candidate goes to list A, the others to list B (both compacted by
 //                   warp-aggregated appends, so the GJK kernels run on dense lists).
 //                   The ray's best hit so far is published as the 64-bit key (toi bits, index).
-//   k_rays_cand     GJK ray casts (their toi does not depend on the max_toi bound, which only
-//                   accepts or rejects) for list A, then for list B skipping candidates whose box
-//                   entry lies beyond the ray's current best; atomicMin of (toi, index).
+//   k_rays_cand_kind<capsule | hull>  GJK ray casts (their toi does not depend on the max_toi
+//                   bound, which only accepts or rejects) for list A, then for list B skipping
+//                   candidates whose box entry lies beyond the ray's current best; atomicMin of
+//                   (toi, index).
 //   k_rays_finish   the candidate holding its ray's minimum key writes the ray's result.
+// The frame pipeline replaces k_rays_wave by the grid walk k_rays_walk (below), which lists the
+// analytic leaves too (list C, tested by k_rays_cand_analytic before the GJK candidates).
 // The minimum of (toi, index) over every hit with toi < max_toi is the single-kernel answer (nearest
-// hit, lowest index on exact ties). Rays whose candidates did not fit list B are redone by the
+// hit, lowest index on exact ties). Rays whose candidates did not fit a list are redone by the
 // single kernel (mask `only`).
 struct RayCand {
   uint32_t k, r, part, hit;
