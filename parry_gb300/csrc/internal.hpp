@@ -79,6 +79,11 @@ struct parrygpu_ctx {
   // with the fork / join events that order it after and before the context stream's work.
   cudaStream_t aux_stream = nullptr;
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  // Copy streams and per-chunk events of the pipelined host-record manifold update (uploads on one,
+  // downloads on the other, compute on `stream`).
+  cudaStream_t up_stream = nullptr, down_stream = nullptr;
+  static constexpr int PIPE_EVENTS = 16;
+  cudaEvent_t pipe_ev[PIPE_EVENTS] = {};
   // Optional per-kernel event timing (parrygpu_enable_kernel_timing).
   bool timing = false;
   std::map<std::string, std::vector<std::pair<cudaEvent_t, cudaEvent_t>>> pending;

@@ -1304,6 +1304,56 @@ parrygpu_status pg::launch_manifolds(parrygpu_ctx* ctx, const ShapeArrays& sh, c
   return PARRYGPU_OK;
 }
 
+// Host records on a large batch: the records go up, get updated and come down in chunks, uploads on
+// one copy stream, the manifold kernels on the context stream and downloads on another, so that the
+// copies of one chunk overlap the kernels of the next (the records are most of the bytes; shapes,
+// pairs and directions are already staged). Each chunk is an independent batch of pairs, so the
+// records are those of the single-shot call.
+constexpr uint64_t MF_PIPE_CHUNKS = 8;
+constexpr uint64_t MF_PIPE_MIN = 262144;  // pairs per chunk at least
+
+static parrygpu_status manifolds_pipelined(parrygpu_ctx* ctx, const ShapeArrays& sh, const uint32_t* dp, const float* di, uint64_t n_pairs,
+                                           float prediction, parrygpu_manifold* host, uint32_t* d_rec) {
+  if (!ctx->up_stream) {
+    PG_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->up_stream, cudaStreamNonBlocking));
+    PG_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->down_stream, cudaStreamNonBlocking));
+    for (cudaEvent_t& e : ctx->pipe_ev) PG_CUDA(ctx, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    if (!ctx->ev_fork) {
+      PG_CUDA(ctx, cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming));
+      PG_CUDA(ctx, cudaEventCreateWithFlags(&ctx->ev_join, cudaEventDisableTiming));
+    }
+  }
+  uint64_t chunks = MF_PIPE_CHUNKS;
+  while (chunks > 2 && n_pairs / chunks < MF_PIPE_MIN) --chunks;
+  const uint64_t chunk = (n_pairs + chunks - 1) / chunks;
+  parrygpu_status s;
+  if ((s = manifolds_reserve(ctx, chunk, ctx->mf)) != PARRYGPU_OK) return s;
+  cudaStream_t main = ctx->stream;
+  // the copy streams start after the staging already queued on the context stream
+  PG_CUDA(ctx, cudaEventRecord(ctx->ev_fork, main));
+  PG_CUDA(ctx, cudaStreamWaitEvent(ctx->up_stream, ctx->ev_fork, 0));
+  PG_CUDA(ctx, cudaStreamWaitEvent(ctx->down_stream, ctx->ev_fork, 0));
+  const size_t rb = sizeof(parrygpu_manifold);
+  uint64_t c = 0;
+  for (uint64_t off = 0; off < n_pairs; off += chunk, ++c) {
+    const uint64_t m = n_pairs - off < chunk ? n_pairs - off : chunk;
+    cudaEvent_t up_done = ctx->pipe_ev[(2 * c) % parrygpu_ctx::PIPE_EVENTS];
+    cudaEvent_t comp_done = ctx->pipe_ev[(2 * c + 1) % parrygpu_ctx::PIPE_EVENTS];
+    PG_CUDA(ctx, cudaMemcpyAsync(d_rec + off * MF_WORDS, host + off, m * rb, cudaMemcpyHostToDevice, ctx->up_stream));
+    PG_CUDA(ctx, cudaEventRecord(up_done, ctx->up_stream));
+    PG_CUDA(ctx, cudaStreamWaitEvent(main, up_done, 0));
+    if ((s = launch_manifolds(ctx, sh, dp + 2 * off, m, nullptr, prediction, d_rec + off * MF_WORDS, ctx->mf, di ? di + 3 * off : nullptr)) !=
+        PARRYGPU_OK)
+      return s;
+    PG_CUDA(ctx, cudaEventRecord(comp_done, main));
+    PG_CUDA(ctx, cudaStreamWaitEvent(ctx->down_stream, comp_done, 0));
+    PG_CUDA(ctx, cudaMemcpyAsync(host + off, d_rec + off * MF_WORDS, m * rb, cudaMemcpyDeviceToHost, ctx->down_stream));
+  }
+  PG_CUDA(ctx, cudaEventRecord(ctx->ev_join, ctx->down_stream));
+  PG_CUDA(ctx, cudaStreamWaitEvent(main, ctx->ev_join, 0));
+  return parrygpu_sync(ctx);
+}
+
 extern "C" {
 
 parrygpu_status parrygpu_contact_manifolds(parrygpu_ctx* ctx, const parrygpu_shapes* shapes, const uint32_t* pairs, uint64_t n_pairs,
@@ -1331,6 +1381,8 @@ parrygpu_status parrygpu_contact_manifolds_with_dirs(parrygpu_ctx* ctx, const pa
   void* d_rec;
   bool c_rec;
   if ((s = stage_output(ctx, ctx->stage_out[0], manifolds, rec_bytes, &d_rec, &c_rec)) != PARRYGPU_OK) return s;
+  if (c_rec && !stats && !ctx->timing && n_pairs >= 2 * MF_PIPE_MIN)
+    return manifolds_pipelined(ctx, sh, (const uint32_t*)dp, (const float*)di, n_pairs, prediction, manifolds, (uint32_t*)d_rec);
   if (c_rec) PG_CUDA(ctx, cudaMemcpyAsync(d_rec, manifolds, rec_bytes, cudaMemcpyHostToDevice, ctx->stream));
   if ((s = manifolds_reserve(ctx, n_pairs, ctx->mf)) != PARRYGPU_OK) return s;
   unsigned long long* ctr = ctx->mf.counters.as<unsigned long long>();  // [0] queue count, [1..3] stats

@@ -240,3 +240,22 @@ def test_with_dirs_bit_exact(gpu_ctx, oracle_lib):
     pg.contact_manifolds(gpu_ctx, shapes, pairs, 0.05, z, init_dirs=np.zeros((len(pairs), 3), np.float32))
     pg.contact_manifolds(gpu_ctx, shapes, pairs, 0.05, p2)
     assert_records_equal(z, p2)
+
+
+def test_pipelined_host_records_match_device_records(gpu_ctx):
+    """A large batch with host records runs in chunks (uploads, kernels and downloads overlapped on
+    three streams): its records equal those of the same update on device records, frame after frame."""
+    import torch
+    import parry_gb300 as pg
+    from parry_gb300 import workloads as W
+    t, prm, pos0, pool, poly, pairs = W.primitive_pairs(600_000)
+    k = len(pairs)
+    host = M.new_manifolds(k)
+    dev = torch.zeros((k, M.RECORD_WORDS), dtype=torch.int32, device="cuda")
+    for f in range(3):
+        shapes = ShapeSet.from_arrays(t, prm, W.drifted_poses(pos0, f), pool, poly)
+        pg.contact_manifolds(gpu_ctx, shapes, pairs, 0.05, host)
+        pg.contact_manifolds(gpu_ctx, shapes, pairs, 0.05, dev)
+        torch.cuda.synchronize()
+        np.testing.assert_array_equal(M.as_words(host), dev.cpu().numpy().view(np.uint32))
+    assert int((host["n_points"] > 0).sum()) > k // 10
