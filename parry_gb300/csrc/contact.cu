@@ -145,11 +145,13 @@ __device__ __forceinline__ void flip(ContactOut* c) {
 // Binning key of a pair: the vertices one support evaluation of the pair scans (vertex count of
 // a convex / triangle shape, 1 for the others, summed over the two shapes; capped at 1023).
 // Threads of a warp then run pairs of similar cost, and so do the EPA queue entries they append.
-__global__ void k_pair_cost_keys(ShapeArrays sh, const uint32_t* __restrict__ pairs, uint32_t n, uint32_t* __restrict__ keys,
+// Keys of pairs base .. base + n - 1, values their indices.
+__global__ void k_pair_cost_keys(ShapeArrays sh, const uint32_t* __restrict__ pairs, uint32_t base, uint32_t n, uint32_t* __restrict__ keys,
                                  uint32_t* __restrict__ vals) {
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  uint32_t a = pairs[2 * (size_t)i], b = pairs[2 * (size_t)i + 1];
+  const size_t k = (size_t)base + i;
+  uint32_t a = pairs[2 * k], b = pairs[2 * k + 1];
   uint32_t c = 2;
   if (a < sh.n_shapes && b < sh.n_shapes) {
     uint32_t ta = sh.types[a], tb = sh.types[b];
@@ -158,7 +160,33 @@ __global__ void k_pair_cost_keys(ShapeArrays sh, const uint32_t* __restrict__ pa
     c = (ca > 1023u ? 1023u : ca) + (cb > 1023u ? 1023u : cb);
   }
   keys[i] = c > 1023u ? 1023u : c;
-  vals[i] = i;
+  vals[i] = (uint32_t)k;
+}
+
+// For chunk c of `chunk` consecutive pairs (a multiple of 32): the end (exclusive) of the
+// vertex-pool range that the chunk's shapes reference, maximised into ends[c] (zeroed by the
+// caller). Invalid shape indices are skipped (the contact kernels report them).
+__global__ void k_chunk_vertex_ends(ShapeArrays sh, const uint32_t* __restrict__ pairs, uint64_t n, uint64_t chunk,
+                                    unsigned long long* __restrict__ ends) {
+  const uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+  unsigned long long e = 0;
+  if (i < n) {
+    for (int j = 0; j < 2; ++j) {
+      const uint32_t s = pairs[2 * i + j];
+      if (s >= sh.n_shapes) continue;
+      const uint32_t t = sh.types[s];
+      if (t == SH_CONVEX || t == SH_TRIANGLE) {
+        const float4 p = sh.params[s];
+        const unsigned long long end = (unsigned long long)__float_as_uint(p.x) + __float_as_uint(p.y);
+        e = end > e ? end : e;
+      }
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned long long x = __shfl_xor_sync(0xffffffffu, e, o);
+    e = x > e ? x : e;
+  }
+  if ((threadIdx.x & 31) == 0 && e && i < n) atomicMax(&ends[i / chunk], e);
 }
 
 // EPA for pair k from GJK's final simplex s, finishing query::contact as the reference does (the
@@ -546,8 +574,9 @@ __global__ void __launch_bounds__(FUSED_THREADS, 3) k_contacts_fused(ShapeArrays
   }
 }
 
-// EPA of the queued pairs. Regular pass (BIG = false): queue entries [0, *qcount); a pair whose
-// polytope outgrows the regular slot is appended to `ovf` (its result left to the second pass).
+// EPA of the queued pairs. Regular pass (BIG = false): queue entries [*qstart, *qcount) (qstart
+// NULL: from 0); a pair whose polytope outgrows the regular slot is appended to `ovf` (its result
+// left to the second pass).
 // Second pass (BIG = true): the entries listed in `ovf` [0, *qcount), on large slots; a pair that
 // outgrows those raises the capacity error.
 // MINB: resident blocks per SM the registers are budgeted for (8: the compiler's choice, about 126
@@ -558,12 +587,13 @@ __global__ void __launch_bounds__(EPA_THREADS, MINB) k_contacts_epa(ShapeArrays 
                                                               const uint32_t* __restrict__ queue, const unsigned long long* __restrict__ qcount,
                                                               uint32_t* __restrict__ ws_pool, unsigned long long* __restrict__ stats,
                                                               uint32_t* __restrict__ err, float* __restrict__ final_dirs,
-                                                              uint32_t* __restrict__ ovf, unsigned long long* __restrict__ ovf_count) {
+                                                              uint32_t* __restrict__ ovf, unsigned long long* __restrict__ ovf_count,
+                                                              const unsigned long long* __restrict__ qstart) {
   const uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x;
   auto ws = [&]() { if constexpr (BIG) return epa_slot_big(ws_pool, slot); else return epa_slot(ws_pool, slot); }();
-  const unsigned long long total = *qcount;
+  const unsigned long long total = *qcount, start = qstart ? *qstart : 0ull;
   uint32_t iters = 0, calls = 0;
-  for (unsigned long long i = slot; i < total; i += (unsigned long long)gridDim.x * blockDim.x) {
+  for (unsigned long long i = start + slot; i < total; i += (unsigned long long)gridDim.x * blockDim.x) {
     const unsigned long long e = BIG ? ovf[i] : i;
     const uint32_t* q = queue + (size_t)e * QUEUE_WORDS;
     uint64_t k = q[0];
@@ -643,14 +673,21 @@ parrygpu_status launch_fused(parrygpu_ctx* ctx, size_t smem, bool inline_epa, co
 
 }  // namespace
 
-parrygpu_status pg::stage_shapes(parrygpu_ctx* ctx, const parrygpu_shapes* s, ShapeArrays* out) {
+parrygpu_status pg::stage_shapes(parrygpu_ctx* ctx, const parrygpu_shapes* s, ShapeArrays* out, bool defer_pool) {
   if (!s) return set_error(ctx, PARRYGPU_INVALID_ARG, "shapes is null");
   const void *t, *p, *q, *v;
   parrygpu_status st;
   if ((st = stage_input(ctx, ctx->stage_in[0], s->types, (size_t)s->n * 4, &t)) != PARRYGPU_OK) return st;
   if ((st = stage_input(ctx, ctx->stage_in[1], s->params, (size_t)s->n * 16, &p)) != PARRYGPU_OK) return st;
   if ((st = stage_input(ctx, ctx->stage_in[2], s->poses, (size_t)s->n * 28, &q)) != PARRYGPU_OK) return st;
-  if ((st = stage_input(ctx, ctx->stage_in[3], s->vertices, (size_t)s->n_vertices * 12, &v)) != PARRYGPU_OK) return st;
+  if (defer_pool && s->n_vertices && s->vertices && !is_device_ptr(s->vertices)) {
+    if (on_other_device(s->vertices, ctx->device))
+      return set_error(ctx, PARRYGPU_INVALID_ARG, "an input buffer lives on another GPU than the context's device %d", ctx->device);
+    PG_CUDA(ctx, ctx->stage_in[3].reserve((size_t)s->n_vertices * 12));
+    v = ctx->stage_in[3].ptr;
+  } else if ((st = stage_input(ctx, ctx->stage_in[3], s->vertices, (size_t)s->n_vertices * 12, &v)) != PARRYGPU_OK) {
+    return st;
+  }
   if (((uintptr_t)p & 15) != 0) return set_error(ctx, PARRYGPU_INVALID_ARG, "shape params must be 16-byte aligned");
   *out = ShapeArrays{(const uint32_t*)t, (const float4*)p, (const float*)q, (const float*)v, s->n, s->n_vertices, PolyArrays{}};
   if (const parrygpu_polyhedra* ph = s->polyhedra) {
@@ -695,6 +732,121 @@ parrygpu_status compound_part_aabbs(parrygpu_ctx* ctx, const parrygpu_compound* 
   return PARRYGPU_OK;
 }
 
+// Host shapes, pairs and outputs on a large batch: the vertex pool (most of the bytes) goes up in
+// pieces on a copy stream while the context stream runs the pairs in chunks. A chunk's cost sort
+// and GJK launch wait for the piece that completes the pool range its pairs reference (read back
+// from a small kernel over the staged pairs before the chunks are queued). The EPA pass runs over
+// the queue entries appended since the previous pass after the first chunk, after the third and
+// after the last: the stream then alternates GJK chunks, whose pieces arrive about one chunk's
+// GJK time apart, with EPA passes long enough to cover the next pieces' uploads, and each pass
+// pays one tail (its last long polytopes). The large-slot pass and the output copies run once at
+// the end. Every pair runs the kernels of the single-shot call on the same values, so the
+// answers are the same.
+constexpr uint64_t CT_PIPE_CHUNKS = 8;
+constexpr uint64_t CT_PIPE_MIN = 131072;  // pairs per chunk at least
+constexpr uint64_t CT_PIPE_PIECES = 16;
+
+static parrygpu_status contacts_pipelined(parrygpu_ctx* ctx, const parrygpu_shapes* shapes, const ShapeArrays& sh, const uint32_t* dp,
+                                   const float* di, uint64_t n_pairs, float prediction, float* d_out, uint8_t* d_has, float* d_dirs) {
+  if (!ctx->up_stream) {
+    PG_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->up_stream, cudaStreamNonBlocking));
+    PG_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->down_stream, cudaStreamNonBlocking));
+    for (cudaEvent_t& e : ctx->pipe_ev) PG_CUDA(ctx, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    if (!ctx->ev_fork) {
+      PG_CUDA(ctx, cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming));
+      PG_CUDA(ctx, cudaEventCreateWithFlags(&ctx->ev_join, cudaEventDisableTiming));
+    }
+  }
+  if (!ctx->h_pipe) PG_CUDA(ctx, cudaMallocHost(&ctx->h_pipe, parrygpu_ctx::PIPE_EVENTS * sizeof(unsigned long long)));
+  static_assert(CT_PIPE_CHUNKS <= parrygpu_ctx::PIPE_EVENTS && CT_PIPE_PIECES <= parrygpu_ctx::PIPE_EVENTS, "one event per piece");
+  cudaStream_t main = ctx->stream;
+  // the pool pieces, after the work already queued on the context stream (the staging buffer's last readers)
+  const uint64_t nv = sh.n_vertices;
+  const char* host_pool = static_cast<const char*>(static_cast<const void*>(shapes->vertices));
+  char* dev_pool = ctx->stage_in[3].as<char>();
+  uint64_t piece_end[CT_PIPE_PIECES];
+  PG_CUDA(ctx, cudaEventRecord(ctx->ev_fork, main));
+  PG_CUDA(ctx, cudaStreamWaitEvent(ctx->up_stream, ctx->ev_fork, 0));
+  uint64_t prev = 0;
+  for (uint64_t p = 0; p < CT_PIPE_PIECES; ++p) {
+    const uint64_t end = nv * (p + 1) / CT_PIPE_PIECES;
+    piece_end[p] = end;
+    if (end > prev)
+      PG_CUDA(ctx, cudaMemcpyAsync(dev_pool + 12 * prev, host_pool + 12 * prev, 12 * (end - prev), cudaMemcpyHostToDevice, ctx->up_stream));
+    PG_CUDA(ctx, cudaEventRecord(ctx->pipe_ev[p], ctx->up_stream));
+    prev = end;
+  }
+  // chunk sizes (multiples of 256) and the pool range each chunk references
+  uint64_t chunks = CT_PIPE_CHUNKS;
+  while (chunks > 2 && n_pairs / chunks < CT_PIPE_MIN) --chunks;
+  const uint64_t chunk = div_up(div_up(n_pairs, chunks), (uint64_t)256) * 256;
+  chunks = div_up(n_pairs, chunk);
+  PG_CUDA(ctx, ctx->misc.reserve(parrygpu_ctx::PIPE_EVENTS * sizeof(unsigned long long)));
+  unsigned long long* d_ends = ctx->misc.as<unsigned long long>();
+  PG_CUDA(ctx, cudaMemsetAsync(d_ends, 0, chunks * sizeof(unsigned long long), main));
+  k_chunk_vertex_ends<<<div_up(n_pairs, 256), 256, 0, main>>>(sh, dp, n_pairs, chunk, d_ends);
+  PG_LAUNCHED(ctx);
+  PG_CUDA(ctx, cudaMemcpyAsync(ctx->h_pipe, d_ends, chunks * sizeof(unsigned long long), cudaMemcpyDeviceToHost, main));
+  PG_CUDA(ctx, cudaStreamSynchronize(main));
+  // scratch: the EPA queue and overflow list hold the whole batch, the sort one chunk
+  parrygpu_status s;
+  PG_CUDA(ctx, ctx->ct_queue.reserve((size_t)n_pairs * QUEUE_WORDS * 4));
+  PG_CUDA(ctx, ctx->ct_counters.reserve(128));
+  PG_CUDA(ctx, ctx->ct_ovf.reserve((size_t)n_pairs * 4));
+  uint32_t epa_per_sm = ctx->cfg.epa_blocks_per_sm ? ctx->cfg.epa_blocks_per_sm : 8;
+  if (epa_per_sm > 32) epa_per_sm = 32;
+  const uint32_t epa_blocks = (uint32_t)(ctx->sm_count > 0 ? ctx->sm_count : 152) * epa_per_sm;
+  PG_CUDA(ctx, ctx->epa_ws.reserve((size_t)epa_blocks * EPA_THREADS * EPA_SLOT_BYTES));
+  PG_CUDA(ctx, ctx->epa_ws_big.reserve((size_t)EPA_BIG_SLOTS * EPA_BIG_SLOT_BYTES));
+  if ((s = radix_sort_reserve(ctx, (uint32_t)chunk)) != PARRYGPU_OK) return s;
+  // [0] queue count, [1..3] stats, [4] overflow count, [5] work counter, [6] costly pairs, [8] EPA pass start
+  unsigned long long* ctr = ctx->ct_counters.as<unsigned long long>();
+  PG_CUDA(ctx, cudaMemsetAsync(ctr, 0, 128, main));
+  const uint32_t warp_cost = ctx->cfg.contact_warp_cost ? ctx->cfg.contact_warp_cost : DEFAULT_CONTACT_WARP_COST;
+  const bool warp_path = warp_cost < 1024;
+  const size_t smem = warp_path ? sizeof(WarpSmem) * FUSED_WARPS : 0;
+  auto epa = epa_per_sm <= 8 ? k_contacts_epa<false, 8> : (epa_per_sm <= 12 ? k_contacts_epa<false, 12> : k_contacts_epa<false, 16>);
+  unsigned long long need = 0;
+  for (uint64_t c = 0; c < chunks; ++c) {
+    const uint64_t off = c * chunk, m = n_pairs - off < chunk ? n_pairs - off : chunk;
+    need = ctx->h_pipe[c] > need ? ctx->h_pipe[c] : need;
+    const uint64_t need_v = need < nv ? need : nv;
+    if (need_v) {
+      uint64_t p = 0;
+      while (piece_end[p] < need_v) ++p;
+      PG_CUDA(ctx, cudaStreamWaitEvent(main, ctx->pipe_ev[p], 0));
+    }
+    PG_CUDA(ctx, cudaMemsetAsync(ctr + 5, 0, 16, main));
+    k_pair_cost_keys<<<div_up(m, (uint64_t)256), 256, 0, main>>>(sh, dp, (uint32_t)off, (uint32_t)m, ctx->sort_k[0].as<uint32_t>(),
+                                                                 ctx->sort_v[0].as<uint32_t>());
+    PG_LAUNCHED(ctx);
+    int rb;
+    if ((s = radix_sort_pairs(ctx, (uint32_t)m, 10, &rb)) != PARRYGPU_OK) return s;
+    if (warp_path) {
+      k_count_costly<<<1, 32, 0, main>>>(ctx->sort_k[rb].as<uint32_t>(), (uint32_t)m, warp_cost, ctr + 6);
+      PG_LAUNCHED(ctx);
+    }
+    if ((s = launch_fused(ctx, smem, false, sh, dp, m, ctx->sort_v[rb].as<uint32_t>(), ctr + 6, prediction, di, d_out, d_has,
+                          ctx->ct_queue.as<uint32_t>(), ctr, nullptr, d_dirs, ctr + 5, ctx->ct_ovf.as<uint32_t>(), ctr + 4)) != PARRYGPU_OK)
+      return s;
+    if (c == 0 || c == 2 || c + 1 == chunks) {
+      epa<<<epa_blocks, EPA_THREADS, 0, main>>>(sh, dp, prediction, d_out, d_has, ctx->ct_queue.as<uint32_t>(), ctr,
+                                                ctx->epa_ws.as<uint32_t>(), nullptr, ctx->d_err, d_dirs, ctx->ct_ovf.as<uint32_t>(), ctr + 4,
+                                                ctr + 8);
+      PG_LAUNCHED(ctx);
+      PG_CUDA(ctx, cudaMemcpyAsync(ctr + 8, ctr, sizeof(unsigned long long), cudaMemcpyDeviceToDevice, main));
+    }
+  }
+  k_contacts_epa<true><<<EPA_BIG_SLOTS / EPA_THREADS, EPA_THREADS, 0, main>>>(
+      sh, dp, prediction, d_out, d_has, ctx->ct_queue.as<uint32_t>(), ctr + 4, ctx->epa_ws_big.as<uint32_t>(), nullptr, ctx->d_err, d_dirs,
+      ctx->ct_ovf.as<uint32_t>(), nullptr, nullptr);
+  PG_LAUNCHED(ctx);
+  // every piece is in before the call returns (a tail of the pool that no pair references included)
+  PG_CUDA(ctx, cudaEventRecord(ctx->ev_join, ctx->up_stream));
+  PG_CUDA(ctx, cudaStreamWaitEvent(main, ctx->ev_join, 0));
+  return PARRYGPU_OK;
+}
+
 extern "C" {
 
 parrygpu_status parrygpu_shapes_aabbs(parrygpu_ctx* ctx, const parrygpu_shapes* shapes, float margin, float* aabbs) {
@@ -733,8 +885,11 @@ parrygpu_status parrygpu_contacts_with_dirs(parrygpu_ctx* ctx, const parrygpu_sh
   if (n_pairs == 0) return PARRYGPU_OK;
   if (!pairs || !out || !has_contact) return set_error(ctx, PARRYGPU_INVALID_ARG, "pairs, out and has_contact are required");
   PG_CUDA(ctx, cudaSetDevice(ctx->device));
+  // a host vertex pool on a large batch: its upload overlapped with the kernels (no statistics or timing asked)
+  const bool pipe = !stats && !ctx->timing && ctx->cfg.contact_epa_inline != 1 && n_pairs >= 2 * CT_PIPE_MIN && n_pairs < 0xffffffffull &&
+                    shapes->n_vertices && shapes->vertices && !is_device_ptr(shapes->vertices);
   ShapeArrays sh;
-  parrygpu_status s = stage_shapes(ctx, shapes, &sh);
+  parrygpu_status s = stage_shapes(ctx, shapes, &sh, pipe);
   if (s != PARRYGPU_OK) return s;
   const void *dp, *di = nullptr;
   if ((s = stage_input(ctx, ctx->stage_in[4], pairs, (size_t)n_pairs * 8, &dp)) != PARRYGPU_OK) return s;
@@ -746,6 +901,15 @@ parrygpu_status parrygpu_contacts_with_dirs(parrygpu_ctx* ctx, const parrygpu_sh
   void* d_dirs = nullptr;
   bool c_dirs = false;
   if ((s = stage_output(ctx, ctx->stage_out[2], final_dirs, (size_t)n_pairs * 12, &d_dirs, &c_dirs)) != PARRYGPU_OK) return s;
+  if (pipe) {
+    if ((s = contacts_pipelined(ctx, shapes, sh, (const uint32_t*)dp, (const float*)di, n_pairs, prediction, (float*)d_out, (uint8_t*)d_has,
+                                (float*)d_dirs)) != PARRYGPU_OK)
+      return s;
+    if (c_out) PG_CUDA(ctx, cudaMemcpyAsync(out, d_out, (size_t)n_pairs * 52, cudaMemcpyDeviceToHost, ctx->stream));
+    if (c_has) PG_CUDA(ctx, cudaMemcpyAsync(has_contact, d_has, (size_t)n_pairs, cudaMemcpyDeviceToHost, ctx->stream));
+    if (c_dirs) PG_CUDA(ctx, cudaMemcpyAsync(final_dirs, d_dirs, (size_t)n_pairs * 12, cudaMemcpyDeviceToHost, ctx->stream));
+    return parrygpu_sync(ctx);
+  }
   const bool inline_epa = ctx->cfg.contact_epa_inline == 1;
   PG_CUDA(ctx, ctx->ct_queue.reserve((size_t)n_pairs * QUEUE_WORDS * 4));
   PG_CUDA(ctx, ctx->ct_counters.reserve(64));
@@ -765,7 +929,7 @@ parrygpu_status parrygpu_contacts_with_dirs(parrygpu_ctx* ctx, const parrygpu_sh
     uint32_t n = (uint32_t)n_pairs;
     if ((s = radix_sort_reserve(ctx, n)) != PARRYGPU_OK) return s;
     KernelTimer kt(ctx, "contacts_bin");
-    k_pair_cost_keys<<<div_up(n, 256), 256, 0, ctx->stream>>>(sh, (const uint32_t*)dp, n, ctx->sort_k[0].as<uint32_t>(),
+    k_pair_cost_keys<<<div_up(n, 256), 256, 0, ctx->stream>>>(sh, (const uint32_t*)dp, 0u, n, ctx->sort_k[0].as<uint32_t>(),
                                                                 ctx->sort_v[0].as<uint32_t>());
     PG_LAUNCHED(ctx);
     int rb;
@@ -796,13 +960,13 @@ parrygpu_status parrygpu_contacts_with_dirs(parrygpu_ctx* ctx, const parrygpu_sh
       auto kern = epa_per_sm <= 8 ? k_contacts_epa<false, 8> : (epa_per_sm <= 12 ? k_contacts_epa<false, 12> : k_contacts_epa<false, 16>);
       kern<<<epa_blocks, EPA_THREADS, 0, ctx->stream>>>(sh, (const uint32_t*)dp, prediction, (float*)d_out, (uint8_t*)d_has,
                                                         ctx->ct_queue.as<uint32_t>(), ctr, ctx->epa_ws.as<uint32_t>(), ctr + 1, ctx->d_err,
-                                                        (float*)d_dirs, ctx->ct_ovf.as<uint32_t>(), ctr + 4);
+                                                        (float*)d_dirs, ctx->ct_ovf.as<uint32_t>(), ctr + 4, nullptr);
       PG_LAUNCHED(ctx);
     }
     // pairs whose polytope outgrew the regular slots, on the large slots (an empty list exits at once)
     k_contacts_epa<true><<<EPA_BIG_SLOTS / EPA_THREADS, EPA_THREADS, 0, ctx->stream>>>(
         sh, (const uint32_t*)dp, prediction, (float*)d_out, (uint8_t*)d_has, ctx->ct_queue.as<uint32_t>(), ctr + 4,
-        ctx->epa_ws_big.as<uint32_t>(), ctr + 1, ctx->d_err, (float*)d_dirs, ctx->ct_ovf.as<uint32_t>(), nullptr);
+        ctx->epa_ws_big.as<uint32_t>(), ctr + 1, ctx->d_err, (float*)d_dirs, ctx->ct_ovf.as<uint32_t>(), nullptr, nullptr);
     kt.stop();
     PG_LAUNCHED(ctx);
   }

@@ -168,7 +168,8 @@ __device__ __forceinline__ void dequeue(const uint32_t* __restrict__ e, uint64_t
 }
 
 // Stages a parrygpu_shapes description on the device (host arrays are copied, device arrays used in place).
-parrygpu_status stage_shapes(parrygpu_ctx* ctx, const parrygpu_shapes* s, ShapeArrays* out);
+// defer_pool: a host vertex pool only gets its device buffer (out->pool), the caller copies it.
+parrygpu_status stage_shapes(parrygpu_ctx* ctx, const parrygpu_shapes* s, ShapeArrays* out, bool defer_pool = false);
 
 // Launchers on device buffers, no allocation and no host synchronisation (graph-capturable):
 // Shape::compute_aabb(pos).loosened(margin) for n shapes (contact.cu);

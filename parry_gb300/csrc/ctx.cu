@@ -140,6 +140,7 @@ void parrygpu_destroy(parrygpu_ctx* ctx) {
   for (DevBuf* d : {&ctx->ray_wave.cands, &ctx->ray_wave.counter, &ctx->ray_wave.keys, &ctx->ray_wave.ovf}) d->release();
   if (ctx->d_err) cudaFree(ctx->d_err);
   if (ctx->h_err) cudaFreeHost(ctx->h_err);
+  if (ctx->h_pipe) cudaFreeHost(ctx->h_pipe);
   drop_pending(ctx);
   if (ctx->aux_stream) { cudaStreamSynchronize(ctx->aux_stream); cudaStreamDestroy(ctx->aux_stream); }
   if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);

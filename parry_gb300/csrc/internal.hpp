@@ -84,6 +84,7 @@ struct parrygpu_ctx {
   cudaStream_t up_stream = nullptr, down_stream = nullptr;
   static constexpr int PIPE_EVENTS = 16;
   cudaEvent_t pipe_ev[PIPE_EVENTS] = {};
+  unsigned long long* h_pipe = nullptr;  // pinned, PIPE_EVENTS words: per-chunk figures read back by a pipelined call
   // Optional per-kernel event timing (parrygpu_enable_kernel_timing).
   bool timing = false;
   std::map<std::string, std::vector<std::pair<cudaEvent_t, cudaEvent_t>>> pending;

@@ -176,3 +176,44 @@ def test_warp_per_pair_path_vs_oracle(oracle_lib, warp_cost, epa_inline):
         assert st["epa_iters"] == sto["epa_iters"]
     finally:
         ctx.close()
+
+
+@pytest.mark.parametrize("shuffle", [False, True])
+def test_pipelined_host_buffers_match_device_buffers(gpu_ctx, shuffle):
+    """A large batch from host shapes runs in chunks while the vertex pool goes up in pieces (pairs
+    in shape order, and shuffled so that the first chunk needs the whole pool): has_contact, the
+    contacts and the final directions equal those of the same call on device buffers, bit for bit,
+    from pageable and from pinned host memory."""
+    import torch
+    s, pairs = W.hull_pairs(300_000, seed=21)
+    if shuffle:
+        pairs = np.ascontiguousarray(pairs[np.random.default_rng(3).permutation(len(pairs))])
+    k = len(pairs)
+    dirs = np.random.default_rng(4).normal(size=(k, 3)).astype(np.float32)
+    arrays = [np.ascontiguousarray(a) for a in s.arrays()]
+    arrays[0] = arrays[0].view(np.int32)
+    dev = tuple(torch.from_numpy(a).cuda() for a in arrays)
+    dpairs = torch.from_numpy(pairs.view(np.int32)).cuda()
+    ddirs = torch.from_numpy(dirs).cuda()
+    dfin = torch.empty((k, 3), dtype=torch.float32, device="cuda")
+    dh, dr = pg.contacts(gpu_ctx, dev, dpairs, 0.0, init_dirs=ddirs, final_dirs=dfin)
+    torch.cuda.synchronize()
+    dh, dr, dfin = dh.cpu().numpy(), dr.cpu().numpy(), dfin.cpu().numpy()
+    assert 0.3 < dh.mean() < 0.95
+    # pageable host memory
+    fin = np.empty((k, 3), np.float32)
+    hh, hr = pg.contacts(gpu_ctx, s, pairs, 0.0, init_dirs=dirs, final_dirs=fin)
+    np.testing.assert_array_equal(hh, dh)
+    np.testing.assert_array_equal(hr.view(np.uint32), dr.view(np.uint32))
+    np.testing.assert_array_equal(fin.view(np.uint32), dfin.view(np.uint32))
+    # pinned host memory, outputs into caller buffers
+    host = tuple(torch.from_numpy(a).pin_memory() for a in arrays)
+    hp = torch.from_numpy(pairs.view(np.int32)).pin_memory()
+    hd = torch.from_numpy(dirs).pin_memory()
+    ph = torch.empty(k, dtype=torch.uint8, pin_memory=True)
+    pr = torch.empty((k, 13), dtype=torch.float32, pin_memory=True)
+    pf = torch.empty((k, 3), dtype=torch.float32, pin_memory=True)
+    pg.contacts(gpu_ctx, host, hp, 0.0, init_dirs=hd, out=(ph, pr), final_dirs=pf)
+    np.testing.assert_array_equal(ph.numpy(), dh)
+    np.testing.assert_array_equal(pr.numpy().view(np.uint32), dr.view(np.uint32))
+    np.testing.assert_array_equal(pf.numpy().view(np.uint32), dfin.view(np.uint32))
