@@ -20,6 +20,8 @@
 // Every path runs the reference's steps in the same order on the same values, so the answers do not
 // depend on which path a pair takes. Results are written in world space (contact_shape_shape.rs:
 // 123-138).
+// the support scan's loop unrolled as the compiler chooses (faster here than any explicit factor)
+#define PG_SCAN_UNROLL 0
 #include "internal.hpp"
 #include "epa_device.cuh"
 #include "contact_device.cuh"
