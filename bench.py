@@ -208,6 +208,29 @@ def contacts_f64_error(s, pairs, has, res, sample: int = 16384) -> dict:
             "point_err_max": float(perr.max(initial=0.0)), "point_err_p99": q(perr)}
 
 
+def host_link_rates(stream, mb: int = 512, reps: int = 3) -> dict:
+    """Pinned host <-> device copy rates of this process (one buffer of `mb` MB each way, best of
+    `reps`): the ceiling the end-to-end figures' copies run against."""
+    import torch
+    h = torch.empty(mb << 20, dtype=torch.uint8, pin_memory=True)
+    d = torch.empty(mb << 20, dtype=torch.uint8, device="cuda")
+    out = {}
+    for name, dst, src in (("h2d_gbs", d, h), ("d2h_gbs", h, d)):
+        best = float("inf")
+        for _ in range(reps + 1):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            a.record(stream)
+            dst.copy_(src, non_blocking=True)
+            b.record(stream)
+            torch.cuda.synchronize()
+            best = min(best, a.elapsed_time(b))
+        out[name] = round((mb << 20) / (best / 1e3) / 1e9, 1)
+    out["bytes"] = mb << 20
+    del h, d
+    return out
+
+
 def broadphase_section(ctx, stream, steps: int, warmup: int, n_shapes: int, flush) -> dict:
     """Broadphase + narrow phase on 131,072 balls and cuboids (50/50) in a cube of side 400: shape
     AABBs loosened by prediction/2, LBVH build, all overlapping pairs (traverse_bvtt_single_tree),
@@ -1084,13 +1107,14 @@ def summarize(line: dict) -> dict:
         "learned": pick(line.get("learned_warm_start"), "mean_gjk_iterations.ratio", "mean_gjk_iterations.ceiling_ratio",
                         "mean_gjk_plus_epa_iterations.ratio", "pairs_per_s.ratio", "mlp_inference_roofline.achieved",
                         "answers.has_contact_agreement"),
-        "manifolds": pick(line.get("manifolds"), "value", "unit", "matches_oracle_on_sample"),
+        "manifolds": pick(line.get("manifolds"), "value", "unit", "matches_oracle_on_sample", "e2e.value"),
         "frame_pipeline": pick(line.get("frame_pipeline"), "value", "unit", "matches_oracle", "e2e.value", "cpu_baseline.value",
                                "learned_seeding.frame_time_ratio_plain_over_learned", "learned_seeding.last_frame.seeded_pairs"),
         "broadphase": pick(line.get("broadphase"), "value", "unit", "matches_oracle"),
         "shape_cast": pick(line.get("shape_cast"), "value", "unit", "matches_oracle_on_sample"),
         "trimesh_contacts": pick(line.get("trimesh_contacts"), "value", "unit", "matches_oracle_on_sample"),
         "hull_build": pick(line.get("hull_build"), "value", "unit", "matches_host_builder_on_sample"),
+        "host_link": line.get("host_link"),
     }
 
 
@@ -1251,6 +1275,7 @@ def run_gb300(args) -> int:
                          "(ray_host_access=2)"}
     mesh_ip.close()
     ctx_ip.close()
+    link_before = host_link_rates(stream)
     contacts = None
     learned = None
     manifolds = None
@@ -1320,6 +1345,7 @@ def run_gb300(args) -> int:
             "shape_cast": shape_cast,
             "trimesh_contacts": trimesh_contacts,
             "hull_build": hull_build,
+            "host_link": {"before_sections": link_before, "after_sections": host_link_rates(stream)},
         }
         line["summary"] = summarize(line)
         print(json.dumps(line), flush=True)
