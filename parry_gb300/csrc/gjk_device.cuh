@@ -211,40 +211,49 @@ __device__ __forceinline__ V3 project_segment(V3 a, V3 b, V3 pt, Loc* loc) {
 
 // The triangle and tetrahedron projections have an inline body for kernels that keep their simplex
 // in registers, and an out-of-line copy that the other kernels share.
+// The region tests are evaluated in full and the answer selected, instead of returning at the
+// first region that holds: lanes of a warp that project onto different regions then stay on one
+// path. Every value is the expression the early-return form computes for its region (same
+// operands, same operations), so the answer is the same bits.
 __device__ __forceinline__ V3 project_triangle_inl(V3 a, V3 b, V3 c, V3 pt, Loc* loc) {
-  V3 ab = b - a, ac = c - a, ap = pt - a;
-  float ab_ap = dot(ab, ap), ac_ap = dot(ac, ap);
-  if (ab_ap <= 0.0f && ac_ap <= 0.0f) { *loc = Loc{LOC_VERTEX, 0, {1.f, 0.f, 0.f}}; return a; }
-  V3 bp = pt - b;
-  float ab_bp = dot(ab, bp), ac_bp = dot(ac, bp);
-  if (ab_bp >= 0.0f && ac_bp <= ab_bp) { *loc = Loc{LOC_VERTEX, 1, {0.f, 1.f, 0.f}}; return b; }
-  V3 cp = pt - c;
-  float ab_cp = dot(ab, cp), ac_cp = dot(ac, cp);
-  if (ac_cp >= 0.0f && ab_cp <= ac_cp) { *loc = Loc{LOC_VERTEX, 2, {0.f, 0.f, 1.f}}; return c; }
-  V3 bc = c - b;
-  V3 n = cross(ab, ac);
-  float vc = dot(n, cross(ab, ap));
-  if (vc < 0.0f && ab_ap >= 0.0f && ab_bp <= 0.0f) {
-    float v = ab_ap / dot(ab, ab);
-    *loc = Loc{LOC_EDGE, 0, {1.0f - v, v, 0.f}};
-    return a + ab * v;
+  const V3 ab = b - a, ac = c - a, ap = pt - a;
+  const float ab_ap = dot(ab, ap), ac_ap = dot(ac, ap);
+  const V3 bp = pt - b;
+  const float ab_bp = dot(ab, bp), ac_bp = dot(ac, bp);
+  const V3 cp = pt - c;
+  const float ab_cp = dot(ab, cp), ac_cp = dot(ac, cp);
+  const V3 bc = c - b;
+  const V3 n = cross(ab, ac);
+  const float vc = dot(n, cross(ab, ap));
+  const float vb = -dot(n, cross(ac, cp));
+  const float va = dot(n, cross(bc, bp));
+  // the first region that holds, in the early-return form's order
+  int region;  // 0-2 vertex a / b / c, 3 edge ab, 4 edge ac, 5 edge bc, 6 face, 7 solid
+  if (ab_ap <= 0.0f && ac_ap <= 0.0f) region = 0;
+  else if (ab_bp >= 0.0f && ac_bp <= ab_bp) region = 1;
+  else if (ac_cp >= 0.0f && ab_cp <= ac_cp) region = 2;
+  else if (vc < 0.0f && ab_ap >= 0.0f && ab_bp <= 0.0f) region = 3;
+  else if (vb < 0.0f && ac_ap >= 0.0f && ac_cp <= 0.0f) region = 4;
+  else if (va < 0.0f && ac_bp - ab_bp >= 0.0f && ab_cp - ac_cp >= 0.0f) region = 5;
+  else if (va + vb + vc != 0.0f) region = 6;
+  else region = 7;
+  if (region < 3) {
+    *loc = Loc{LOC_VERTEX, region, {region == 0 ? 1.f : 0.f, region == 1 ? 1.f : 0.f, region == 2 ? 1.f : 0.f}};
+    return region == 0 ? a : (region == 1 ? b : c);
   }
-  float vb = -dot(n, cross(ac, cp));
-  if (vb < 0.0f && ac_ap >= 0.0f && ac_cp <= 0.0f) {
-    float w = ac_ap / dot(ac, ac);
-    *loc = Loc{LOC_EDGE, 2, {1.0f - w, w, 0.f}};
-    return a + ac * w;
+  if (region < 6) {
+    // edge: base + dir * (num / den)
+    const V3 base = region == 5 ? b : a;
+    const V3 dir = region == 3 ? ab : (region == 4 ? ac : bc);
+    const float num = region == 3 ? ab_ap : (region == 4 ? ac_ap : dot(bc, bp));
+    const float t = num / dot(dir, dir);
+    *loc = Loc{LOC_EDGE, region == 3 ? 0 : (region == 4 ? 2 : 1), {1.0f - t, t, 0.f}};
+    return base + dir * t;
   }
-  float va = dot(n, cross(bc, bp));
-  if (va < 0.0f && ac_bp - ab_bp >= 0.0f && ab_cp - ac_cp >= 0.0f) {
-    float w = dot(bc, bp) / dot(bc, bc);
-    *loc = Loc{LOC_EDGE, 1, {1.0f - w, w, 0.f}};
-    return b + bc * w;
-  }
-  int side = dot(n, ap) >= 0.0f ? 0 : 1;
-  if (va + vb + vc != 0.0f) {
-    float denom = 1.0f / (va + vb + vc);
-    float v = vb * denom, w = vc * denom;
+  if (region == 6) {
+    const int side = dot(n, ap) >= 0.0f ? 0 : 1;
+    const float denom = 1.0f / (va + vb + vc);
+    const float v = vb * denom, w = vc * denom;
     *loc = Loc{LOC_FACE, side, {(1.0f - v) - w, v, w}};
     return (a + ab * v) + ac * w;
   }
