@@ -443,6 +443,17 @@ parrygpu_status parrygpu_scene_info(parrygpu_ctx* ctx, const parrygpu_scene* sce
  * index or UINT32_MAX, toi, world normal). Synchronises. */
 parrygpu_status parrygpu_scene_read(parrygpu_ctx* ctx, const parrygpu_scene* scene, float* poses, uint32_t* pairs,
                                     parrygpu_manifold* manifolds, uint64_t cap, uint32_t* ray_part, float* ray_toi, float* ray_normal);
+/* parrygpu_scene_read without waiting for the copies: returns once the current frame has finished
+ * and its outputs' copies are queued on a copy stream (*n_pairs = the pair rows copied), so the next
+ * frames (parrygpu_scene_step, eager) run while the copies proceed; their kernels that overwrite what
+ * the copies read wait for them on the device. The host buffers hold the frame's outputs once
+ * parrygpu_scene_read_wait returns; they must be page-locked for the copies to overlap. A further
+ * read waits for this one first. */
+parrygpu_status parrygpu_scene_read_async(parrygpu_ctx* ctx, parrygpu_scene* scene, float* poses, uint32_t* pairs,
+                                          parrygpu_manifold* manifolds, uint64_t cap, uint32_t* ray_part, float* ray_toi, float* ray_normal,
+                                          uint64_t* n_pairs);
+/* Waits for the copies of the last parrygpu_scene_read_async (returns at once when none is in flight). */
+parrygpu_status parrygpu_scene_read_wait(parrygpu_ctx* ctx, parrygpu_scene* scene);
 /* The last frame's narrow-phase counters (synchronises): GJK and EPA iterations and EPA calls of its
  * manifold updates, and (seeded_pairs, may be NULL) how many pairs took a learned GJK start direction
  * (parrygpu_scene_set_mlp; 0 without a network). */

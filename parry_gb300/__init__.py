@@ -630,14 +630,20 @@ class Scene:
         check(lib().parrygpu_scene_info(self._ctx.handle, self._h, C.byref(f), C.byref(n)), self._ctx.handle)
         return f.value, n.value
 
-    def read(self, out: dict | None = None) -> dict:
+    def read(self, out: dict | None = None, wait: bool = True) -> dict:
         """Host copies of the current poses, pairs (unsorted) with their manifold records, and the
         last frame's ray results. `out` (optional) holds preallocated destinations under the same
         keys - numpy arrays or (pinned) CPU torch tensors: poses (n, 7) f32, pairs (capacity, 2) u32,
         manifolds (capacity, RECORD_WORDS) u32 words, ray_part (n_rays,) u32, ray_toi (n_rays,) f32,
         ray_normal (n_rays, 3) f32 - so a frame loop reads into pinned memory without allocating;
-        the returned dict then views their first n_pairs rows."""
+        the returned dict then views their first n_pairs rows. wait=False (with `out`) returns once
+        the frame has finished and its copies are queued (parrygpu_scene_read_async): the next
+        step() runs while they proceed, and the buffers hold this frame's outputs after read_wait()."""
         from .manifold import new_manifolds
+        if not wait:
+            if out is None:
+                raise ValueError("an asynchronous read needs its destination buffers (out=)")
+            return self._read_async(out)
         _, npairs = self.info()
         npairs = min(npairs, self.capacity)
         if out is None:
@@ -662,6 +668,29 @@ class Scene:
         res["pairs"] = dst["pairs"][:npairs]
         res["manifolds"] = dst["manifolds"][:npairs]
         return res
+
+    def _read_async(self, dst: dict) -> dict:
+        assert tuple(dst["poses"].shape) == (self.n, 7) and len(dst["pairs"]) == len(dst["manifolds"])
+        assert len(dst["ray_part"]) == self.n_rays and len(dst["ray_toi"]) == self.n_rays and len(dst["ray_normal"]) == self.n_rays
+
+        def ptr(a):
+            return a.data_ptr() if _is_torch(a) else a.ctypes.data
+        has_rays = self.n_rays > 0
+        npairs = C.c_uint64()
+        check(lib().parrygpu_scene_read_async(self._ctx.handle, self._h, ptr(dst["poses"]), ptr(dst["pairs"]), ptr(dst["manifolds"]),
+                                              len(dst["pairs"]), ptr(dst["ray_part"]) if has_rays else None,
+                                              ptr(dst["ray_toi"]) if has_rays else None, ptr(dst["ray_normal"]) if has_rays else None,
+                                              C.byref(npairs)), self._ctx.handle)
+        self._pending = dst  # the buffers the copies write stay referenced until read_wait
+        res = dict(dst)
+        res["pairs"] = dst["pairs"][:npairs.value]
+        res["manifolds"] = dst["manifolds"][:npairs.value]
+        return res
+
+    def read_wait(self) -> None:
+        """Waits for the copies of the last read(wait=False)."""
+        check(lib().parrygpu_scene_read_wait(self._ctx.handle, self._h), self._ctx.handle)
+        self._pending = None
 
     def stats(self) -> dict:
         """The last frame's narrow-phase counters: GJK / EPA iterations, EPA calls, and the pairs that

@@ -88,6 +88,8 @@ SIGNATURES: dict[str, tuple] = {
     "parrygpu_scene_step": (I32, [P, P, F32, U32, I32]),
     "parrygpu_scene_info": (I32, [P, P, P, P]),
     "parrygpu_scene_read": (I32, [P, P, P, P, P, U64, P, P, P]),
+    "parrygpu_scene_read_async": (I32, [P, P, P, P, P, U64, P, P, P, P]),
+    "parrygpu_scene_read_wait": (I32, [P, P]),
     "parrygpu_scene_set_mlp": (I32, [P, P, P]),
     "parrygpu_scene_stats": (I32, [P, P, P, P]),
     "parrygpu_polyhedra_sizes": (I32, [P, P]),

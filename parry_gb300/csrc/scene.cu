@@ -42,6 +42,15 @@ struct parrygpu_scene {
   bool seeded = false;
   int cur = 0;
   uint64_t frame = 0;
+  // An asynchronous read (parrygpu_scene_read_async): its copies run on the context's download
+  // stream between read_start and read_done, the poses from a snapshot, the pairs and records from
+  // buffer parity read_cur, the ray results in place. read_order: the context stream has not yet been
+  // ordered after read_done (a frame does so before it overwrites the ray results or that buffer);
+  // read_inflight: the host has not yet waited for it.
+  DevBuf pose_snap;
+  cudaEvent_t read_start = nullptr, read_done = nullptr;
+  bool read_order = false, read_inflight = false;
+  int read_cur = 0;
   cudaGraphExec_t exec = nullptr;
   float graph_dt = 0.0f;
   int graph_cur = 0;  // the buffer parity the graph was captured at
@@ -171,6 +180,16 @@ static ShapeArrays scene_shapes(const parrygpu_scene* sc) {
 
 // One frame: integrate, AABBs, refit, pairs into the other buffer, carry the records, manifolds, rays.
 // With kernel timing on (and outside graph capture) each stage is bracketed as "scene_<stage>".
+// The context stream waits for an asynchronous read's copies (before a kernel that overwrites what
+// they read).
+static parrygpu_status order_after_read(parrygpu_ctx* ctx, parrygpu_scene* sc) {
+  if (sc->read_order) {
+    PG_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, sc->read_done, 0));
+    sc->read_order = false;
+  }
+  return PARRYGPU_OK;
+}
+
 static parrygpu_status scene_frame(parrygpu_ctx* ctx, parrygpu_scene* sc, float dt) {
   int old = sc->cur, nw = 1 - sc->cur;
   cudaStream_t st = ctx->stream;
@@ -194,6 +213,8 @@ static parrygpu_status scene_frame(parrygpu_ctx* ctx, parrygpu_scene* sc, float 
   }
   unsigned long long* cnt = sc->counts.as<unsigned long long>();
   {
+    // the pairs and records of buffer nw are an asynchronous read's source two frames after it
+    if (nw == sc->read_cur && (s = order_after_read(ctx, sc)) != PARRYGPU_OK) return s;
     KernelTimer kt(ctx, "scene_pairs");
     PG_CUDA(ctx, cudaMemsetAsync(cnt + nw, 0, 8, st));
     if ((s = launch_self_pairs(ctx, &sc->bvh, sc->pairs[nw].as<uint32_t>(), sc->cap, cnt + nw)) != PARRYGPU_OK) return s;
@@ -229,6 +250,7 @@ static parrygpu_status scene_frame(parrygpu_ctx* ctx, parrygpu_scene* sc, float 
     kt.stop();
   }
   if (sc->n_rays) {
+    if ((s = order_after_read(ctx, sc)) != PARRYGPU_OK) return s;  // the ray results are a read's source
     KernelTimer kt(ctx, "scene_rays");
     if ((s = launch_shape_rays(ctx, &sc->bvh, sc->types.as<uint32_t>(), sc->params.as<float>(), sc->poses.as<float>(), sc->pool.as<float>(),
                                sc->hull_box.as<float>(), sc->rays.as<float>(), sc->ray_order.as<uint32_t>(), (uint32_t)sc->n_rays, sc->max_toi,
@@ -251,6 +273,8 @@ static void drop_graph(parrygpu_scene* sc) {
 // since nothing ran.
 static parrygpu_status capture_two_frames(parrygpu_ctx* ctx, parrygpu_scene* sc, float dt) {
   PG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));  // no replay of the old graph in flight
+  parrygpu_status so = order_after_read(ctx, sc);  // no wait on a read's event inside the graph
+  if (so != PARRYGPU_OK) return so;
   drop_graph(sc);
   int cur0 = sc->cur;
   uint64_t frame0 = sc->frame, launches0 = ctx->launches;
@@ -355,8 +379,11 @@ parrygpu_status parrygpu_scene_create(parrygpu_ctx* ctx, const parrygpu_shapes* 
 
 void parrygpu_scene_destroy(parrygpu_scene* sc) {
   if (!sc) return;
-  cudaDeviceSynchronize();  // frames in flight still read the scene's buffers
+  cudaDeviceSynchronize();  // frames and reads in flight still use the scene's buffers
   drop_graph(sc);
+  sc->pose_snap.release();
+  if (sc->read_start) cudaEventDestroy(sc->read_start);
+  if (sc->read_done) cudaEventDestroy(sc->read_done);
   for (DevBuf* d : {&sc->types, &sc->params, &sc->poses, &sc->vel, &sc->pool, &sc->aabbs, &sc->hull_box, &sc->counts, &sc->mf.queue, &sc->mf.counters,
                     &sc->mf.epa_ws, &sc->mf.bins, &sc->rays, &sc->ray_order, &sc->ray_part,
                     &sc->ray_toi, &sc->ray_nrm, &sc->bvh.wide, &sc->bvh.leaf_parent, &sc->bvh.node_parent, &sc->bvh.leaf_index,
@@ -379,6 +406,8 @@ parrygpu_status parrygpu_scene_set_rays(parrygpu_ctx* ctx, parrygpu_scene* sc, c
   if (!ctx || !sc) return PARRYGPU_INVALID_ARG;
   if (n_rays > 0xffffffffull) return set_error(ctx, PARRYGPU_INVALID_ARG, "too many rays");
   PG_CUDA(ctx, cudaSetDevice(ctx->device));
+  parrygpu_status sw = parrygpu_scene_read_wait(ctx, sc);  // the ray buffers may be reallocated
+  if (sw != PARRYGPU_OK) return sw;
   PG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   drop_graph(sc);  // the captured frame bakes in the ray buffers
   parrygpu_status s;
@@ -454,6 +483,7 @@ parrygpu_status parrygpu_scene_step(parrygpu_ctx* ctx, parrygpu_scene* sc, float
     if (!sc->exec || sc->graph_dt != dt || sc->graph_cur != sc->cur) {
       if ((s = capture_two_frames(ctx, sc, dt)) != PARRYGPU_OK) return s;
     }
+    if ((s = order_after_read(ctx, sc)) != PARRYGPU_OK) return s;  // replays start after a read's copies
     for (uint32_t k = 0; k + 2 <= frames; k += 2) {
       PG_CUDA(ctx, cudaGraphLaunch(sc->exec, ctx->stream));
       ctx->launches += sc->graph_launches;
@@ -482,6 +512,7 @@ parrygpu_status parrygpu_scene_read(parrygpu_ctx* ctx, const parrygpu_scene* sc,
                                     uint64_t cap, uint32_t* ray_part, float* ray_toi, float* ray_normal) {
   if (!ctx || !sc) return PARRYGPU_INVALID_ARG;
   PG_CUDA(ctx, cudaSetDevice(ctx->device));
+  if (sc->read_inflight) PG_CUDA(ctx, cudaEventSynchronize(sc->read_done));  // its host buffers may be these
   unsigned long long c = 0;
   PG_CUDA(ctx, cudaMemcpyAsync(&c, sc->counts.as<unsigned long long>() + sc->cur, 8, cudaMemcpyDeviceToHost, ctx->stream));
   PG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
@@ -497,6 +528,56 @@ parrygpu_status parrygpu_scene_read(parrygpu_ctx* ctx, const parrygpu_scene* sc,
     if (ray_normal) PG_CUDA(ctx, cudaMemcpyAsync(ray_normal, sc->ray_nrm.ptr, sc->n_rays * 12, cudaMemcpyDefault, st));
   }
   return parrygpu_sync(ctx);
+}
+
+parrygpu_status parrygpu_scene_read_async(parrygpu_ctx* ctx, parrygpu_scene* sc, float* poses, uint32_t* pairs, parrygpu_manifold* manifolds,
+                                          uint64_t cap, uint32_t* ray_part, float* ray_toi, float* ray_normal, uint64_t* n_pairs) {
+  if (!ctx || !sc) return PARRYGPU_INVALID_ARG;
+  PG_CUDA(ctx, cudaSetDevice(ctx->device));
+  parrygpu_status s = parrygpu_scene_read_wait(ctx, sc);  // one read in flight at a time
+  if (s != PARRYGPU_OK) return s;
+  if (!ctx->down_stream) PG_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->down_stream, cudaStreamNonBlocking));
+  if (!sc->read_start) {
+    PG_CUDA(ctx, cudaEventCreateWithFlags(&sc->read_start, cudaEventDisableTiming));
+    PG_CUDA(ctx, cudaEventCreateWithFlags(&sc->read_done, cudaEventDisableTiming));
+  }
+  // the frame's pair count (this waits for the frame)
+  unsigned long long c = 0;
+  PG_CUDA(ctx, cudaMemcpyAsync(&c, sc->counts.as<unsigned long long>() + sc->cur, 8, cudaMemcpyDeviceToHost, ctx->stream));
+  if ((s = parrygpu_sync(ctx)) != PARRYGPU_OK) return s;
+  uint64_t np = c < sc->cap ? c : sc->cap;
+  if (np > cap) np = cap;
+  if (n_pairs) *n_pairs = pairs || manifolds ? np : 0;
+  cudaStream_t st = ctx->stream, dn = ctx->down_stream;
+  // the poses change at the next frame's first kernel: copied from a snapshot
+  if (poses) {
+    PG_CUDA(ctx, sc->pose_snap.reserve(sc->n * 28));
+    PG_CUDA(ctx, cudaMemcpyAsync(sc->pose_snap.ptr, sc->poses.ptr, sc->n * 28, cudaMemcpyDeviceToDevice, st));
+  }
+  PG_CUDA(ctx, cudaEventRecord(sc->read_start, st));
+  PG_CUDA(ctx, cudaStreamWaitEvent(dn, sc->read_start, 0));
+  if (poses) PG_CUDA(ctx, cudaMemcpyAsync(poses, sc->pose_snap.ptr, sc->n * 28, cudaMemcpyDefault, dn));
+  if (pairs && np) PG_CUDA(ctx, cudaMemcpyAsync(pairs, sc->pairs[sc->cur].ptr, np * 8, cudaMemcpyDefault, dn));
+  if (manifolds && np) PG_CUDA(ctx, cudaMemcpyAsync(manifolds, sc->recs[sc->cur].ptr, np * sizeof(parrygpu_manifold), cudaMemcpyDefault, dn));
+  if (sc->n_rays) {
+    if (ray_part) PG_CUDA(ctx, cudaMemcpyAsync(ray_part, sc->ray_part.ptr, sc->n_rays * 4, cudaMemcpyDefault, dn));
+    if (ray_toi) PG_CUDA(ctx, cudaMemcpyAsync(ray_toi, sc->ray_toi.ptr, sc->n_rays * 4, cudaMemcpyDefault, dn));
+    if (ray_normal) PG_CUDA(ctx, cudaMemcpyAsync(ray_normal, sc->ray_nrm.ptr, sc->n_rays * 12, cudaMemcpyDefault, dn));
+  }
+  PG_CUDA(ctx, cudaEventRecord(sc->read_done, dn));
+  sc->read_cur = sc->cur;
+  sc->read_order = true;
+  sc->read_inflight = true;
+  return PARRYGPU_OK;
+}
+
+parrygpu_status parrygpu_scene_read_wait(parrygpu_ctx* ctx, parrygpu_scene* sc) {
+  if (!ctx || !sc) return PARRYGPU_INVALID_ARG;
+  if (!sc->read_inflight) return PARRYGPU_OK;
+  PG_CUDA(ctx, cudaSetDevice(ctx->device));
+  sc->read_inflight = false;
+  PG_CUDA(ctx, cudaEventSynchronize(sc->read_done));
+  return PARRYGPU_OK;
 }
 
 parrygpu_status parrygpu_scene_stats(parrygpu_ctx* ctx, const parrygpu_scene* sc, parrygpu_gjk_stats* stats, uint64_t* seeded_pairs) {

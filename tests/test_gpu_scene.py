@@ -235,3 +235,63 @@ def test_scene_read_into_pinned_buffers(gpu_ctx):
     np.testing.assert_array_equal(a["ray_part"], b["ray_part"].numpy().view(np.uint32))
     np.testing.assert_array_equal(a["ray_toi"], b["ray_toi"].numpy())
     np.testing.assert_array_equal(a["ray_normal"], b["ray_normal"].numpy())
+
+
+def _pinned(n, cap, n_rays):
+    import torch
+    return {"poses": torch.empty((n, 7), dtype=torch.float32, pin_memory=True),
+            "pairs": torch.empty((cap, 2), dtype=torch.int32, pin_memory=True),
+            "manifolds": torch.empty((cap, M.RECORD_WORDS), dtype=torch.int32, pin_memory=True),
+            "ray_part": torch.empty(n_rays, dtype=torch.int32, pin_memory=True),
+            "ray_toi": torch.empty(n_rays, dtype=torch.float32, pin_memory=True),
+            "ray_normal": torch.empty((n_rays, 3), dtype=torch.float32, pin_memory=True)}
+
+
+def _assert_same_read(a, b):
+    """A read of one scene (numpy) against a read of its twin into pinned buffers: pairs come in
+    append order, so they are compared as sets, each with its record."""
+    np.testing.assert_array_equal(a["poses"], b["poses"].numpy())
+    pa, ra = _sorted_state(a)
+    pb, rb = _sorted_state({"pairs": b["pairs"].numpy().view(np.uint32), "manifolds": b["manifolds"].numpy().view(np.uint32)})
+    np.testing.assert_array_equal(pa, pb)
+    _assert_records(rb, ra)
+    np.testing.assert_array_equal(a["ray_part"], b["ray_part"].numpy().view(np.uint32))
+    np.testing.assert_array_equal(a["ray_toi"], b["ray_toi"].numpy())
+    np.testing.assert_array_equal(a["ray_normal"], b["ray_normal"].numpy())
+
+
+def test_scene_async_read_overlaps_next_frames(gpu_ctx):
+    """Scene.read(wait=False) copies a frame's outputs while the next frames run: after read_wait the
+    buffers hold that frame's outputs (a twin scene read synchronously gives the same), the frames
+    after it are unchanged by the read, and graph replays after a read stay correct."""
+    import parry_gb300 as pg
+    s, vel, rays = _inputs(700, 71, n_rays=2000)
+    dt, cap = 1.0 / 60.0, 1 << 15
+    a = pg.Scene(gpu_ctx, s, vel, 0.1, cap)
+    b = pg.Scene(gpu_ctx, s, vel, 0.1, cap)
+    for sc in (a, b):
+        sc.set_rays(rays, 100.0)
+    pin = _pinned(700, cap, 2000)
+    for frame in range(4):
+        a.step(dt, 1, use_graph=False)
+        b.step(dt, 1, use_graph=False)
+        want = b.read()
+        got = a.read(out=pin, wait=False)
+        a.step(dt, 1, use_graph=False)  # runs while the copies proceed
+        a.read_wait()
+        _assert_same_read(want, got)
+        b.step(dt, 1, use_graph=False)
+        _assert_same_read(b.read(), a.read(out=_pinned(700, cap, 2000)))
+    # a read followed by graph replays, then an eager frame
+    got = a.read(out=pin, wait=False)
+    want = b.read()
+    a.step(dt, 4, use_graph=True)
+    b.step(dt, 4, use_graph=True)
+    a.read_wait()
+    _assert_same_read(want, got)
+    a.step(dt, 1, use_graph=False)
+    b.step(dt, 1, use_graph=False)
+    _assert_same_read(b.read(), a.read(out=_pinned(700, cap, 2000)))
+    assert len(want["pairs"]) > 100 and int((want["ray_part"] != pg.NO_HIT).sum()) > 100
+    a.close()
+    b.close()
