@@ -387,10 +387,33 @@ def hull_build_section(ctx, steps: int, n_hulls: int) -> dict:
         run()
         times.append(time.perf_counter() - t0)
     ms = 1e3 * statistics.median(times)
-    # end to end: host clouds in, host arrays out
+    # end to end: host clouds in, host arrays out - pinned buffers allocated once (the sizes of the
+    # device run), and for comparison freshly allocated pageable arrays
+    npts, nf, nfe, nve, ne = (int(x) for x in sizes)
+
+    def pinned(shape, dt):
+        return torch.empty(shape, dtype=dt, pin_memory=True).numpy()
+    p_in = (pinned(cloud.shape, torch.float32), pinned(first.shape, torch.int32).view(np.uint32),
+            pinned(count.shape, torch.int32).view(np.uint32))
+    for dst, src in zip(p_in, (cloud, first, count)):
+        dst[...] = src
+    p_out = {"points": pinned((npts, 3), torch.float32), "hulls": pinned((n_hulls, 8), torch.int32).view(np.uint32),
+             "face_normals": pinned((nf, 3), torch.float32), "face_ranges": pinned((nf, 2), torch.int32).view(np.uint32),
+             "face_vertices": pinned(nfe, torch.int32).view(np.uint32), "face_edges": pinned(nfe, torch.int32).view(np.uint32),
+             "vertex_ranges": pinned((npts, 2), torch.int32).view(np.uint32), "vertex_faces": pinned(nve, torch.int32).view(np.uint32),
+             "vertex_edges": pinned(nve, torch.int32).view(np.uint32), "edge_dirs": pinned((ne, 3), torch.float32)}
+    out_bytes = sum(a.nbytes for a in p_out.values())
+    build_polyhedra(*p_in, ctx=ctx, out=p_out)
+    e2e_times = []
+    for _ in range(3):
+        t0 = time.perf_counter()
+        build_polyhedra(*p_in, ctx=ctx, out=p_out)
+        e2e_times.append(time.perf_counter() - t0)
+    e2e_ms = 1e3 * statistics.median(e2e_times)
     t0 = time.perf_counter()
     build_polyhedra(cloud, first, count, ctx=ctx)
-    e2e_ms = 1e3 * (time.perf_counter() - t0)
+    e2e_pageable_ms = 1e3 * (time.perf_counter() - t0)
+    del p_out, p_in
     sample = min(n_hulls, 65536)
     sc = cloud[: int(first[sample - 1] + count[sample - 1])]
     threads = os.cpu_count() or 1
@@ -404,7 +427,10 @@ def hull_build_section(ctx, steps: int, n_hulls: int) -> dict:
             "value": round(n_hulls / (ms / 1e3), 1), "unit": "hulls/s", "ms_per_step": round(ms, 3),
             "faces": int(sizes[1]), "edges": int(sizes[4]),
             "e2e": {"value": round(n_hulls / (e2e_ms / 1e3), 1), "unit": "hulls/s", "ms": round(e2e_ms, 2),
-                    "h2d_bytes": int(cloud.nbytes + first.nbytes + count.nbytes)},
+                    "h2d_bytes": int(cloud.nbytes + first.nbytes + count.nbytes), "d2h_bytes": int(out_bytes),
+                    "note": "pinned host clouds in, pinned host arrays out (allocated once), median of 3",
+                    "pageable": {"value": round(n_hulls / (e2e_pageable_ms / 1e3), 1), "unit": "hulls/s",
+                                 "ms": round(e2e_pageable_ms, 2), "note": "numpy clouds in, freshly allocated numpy arrays out"}},
             "matches_host_builder_on_sample": same,
             "cpu_baseline": {"value": round(sample / cpu_s, 1), "unit": "hulls/s", "cores": threads, "kind": "port",
                              "sample": f"first {sample} clouds; the same hull + from_convex_mesh code on host threads"}}

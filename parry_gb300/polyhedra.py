@@ -16,13 +16,16 @@ TOPOLOGY_KEYS = ("face_normals", "face_ranges", "face_vertices", "face_edges", "
 
 
 def build_polyhedra(pool: np.ndarray, first: np.ndarray, count: np.ndarray, threads: int = 0, ctx=None,
-                    with_triangles: bool = False):
+                    with_triangles: bool = False, out: dict | None = None):
     """Returns (points (m, 3) f32, hulls (n, 8) u32, topology dict). hulls rows: first vertex (in
     `points`), vertex count, first face, face count, first edge, edge count, ok, 0. With a Context
     `ctx` the clouds are built on its GPU (parrygpu_polyhedra_build_gpu: the same bytes as the host
     builder), else on `threads` host threads. With `with_triangles` the topology dict also holds
     transformation::convex_hull's triangulation of every cloud: "tri_ranges" (n, 2) = first
-    triangle, count and "triangles" (t, 3) of hull-local vertex ids."""
+    triangle, count and "triangles" (t, 3) of hull-local vertex ids. `out` (GPU builds, optional):
+    destination arrays under the keys "points", "hulls" and the topology keys, at least as long as
+    the build's (numpy arrays, or numpy views of pinned memory so that the copies run at the host
+    link's speed); the returned arrays are then views of their leading rows."""
     from ._capi import lib, check
     pool = np.ascontiguousarray(pool, np.float32).reshape(-1, 3)
     first = np.ascontiguousarray(first, np.uint32)
@@ -30,7 +33,7 @@ def build_polyhedra(pool: np.ndarray, first: np.ndarray, count: np.ndarray, thre
     n = len(first)
     L = lib()
     if ctx is not None:
-        return _build_gpu(ctx, pool, first, count, with_triangles)
+        return _build_gpu(ctx, pool, first, count, with_triangles, out)
     h = C.c_void_p()
     check(L.parrygpu_polyhedra_build(pool.ctypes.data, first.ctypes.data, count.ctypes.data, n, int(threads), C.byref(h)))
     try:
@@ -58,7 +61,7 @@ def build_polyhedra(pool: np.ndarray, first: np.ndarray, count: np.ndarray, thre
     return points, hulls, topo
 
 
-def _build_gpu(ctx, pool, first, count, with_triangles=False):
+def _build_gpu(ctx, pool, first, count, with_triangles=False, out=None):
     from ._capi import lib, check
     L = lib()
     n = len(first)
@@ -70,14 +73,23 @@ def _build_gpu(ctx, pool, first, count, with_triangles=False):
         sizes = np.zeros(5, np.uint64)
         check(L.parrygpu_polyhedra_gpu_sizes(h, C.c_void_p(sizes.ctypes.data)))
         npts, nf, nfe, nve, ne = (int(x) for x in sizes)
-        points = np.zeros((npts, 3), np.float32)
-        hulls = np.zeros((n, 8), np.uint32)
-        topo = {
-            "face_normals": np.zeros((nf, 3), np.float32), "face_ranges": np.zeros((nf, 2), np.uint32),
-            "face_vertices": np.zeros(nfe, np.uint32), "face_edges": np.zeros(nfe, np.uint32),
-            "vertex_ranges": np.zeros((npts, 2), np.uint32), "vertex_faces": np.zeros(nve, np.uint32),
-            "vertex_edges": np.zeros(nve, np.uint32), "edge_dirs": np.zeros((ne, 3), np.float32),
-        }
+        rows = {"points": npts, "hulls": n, "face_normals": nf, "face_ranges": nf, "face_vertices": nfe, "face_edges": nfe,
+                "vertex_ranges": npts, "vertex_faces": nve, "vertex_edges": nve, "edge_dirs": ne}
+        if out is not None:
+            for k, m in rows.items():
+                if len(out[k]) < m:
+                    raise ValueError(f"out[{k!r}] holds {len(out[k])} rows, the build needs {m}")
+            points, hulls = out["points"][:npts], out["hulls"][:n]
+            topo = {k: out[k][:rows[k]] for k in TOPOLOGY_KEYS}
+        else:
+            points = np.empty((npts, 3), np.float32)
+            hulls = np.empty((n, 8), np.uint32)
+            topo = {
+                "face_normals": np.empty((nf, 3), np.float32), "face_ranges": np.empty((nf, 2), np.uint32),
+                "face_vertices": np.empty(nfe, np.uint32), "face_edges": np.empty(nfe, np.uint32),
+                "vertex_ranges": np.empty((npts, 2), np.uint32), "vertex_faces": np.empty(nve, np.uint32),
+                "vertex_edges": np.empty(nve, np.uint32), "edge_dirs": np.empty((ne, 3), np.float32),
+            }
         ptr = lambda a: C.c_void_p(a.ctypes.data) if a.size else None
         check(L.parrygpu_polyhedra_gpu_copy(ctx.handle, h, ptr(points), ptr(hulls), *[ptr(topo[k]) for k in TOPOLOGY_KEYS]), ctx.handle)
         if with_triangles:

@@ -91,3 +91,30 @@ def test_workload_sample_passes_check_convex_hull(gpu_ctx):
             t0, nt = topo["tri_ranges"][h]
             p = points[hulls[h, 0]:hulls[h, 0] + hulls[h, 1]]
             assert triangulation_properties(cloud[first[h]:first[h] + count[h]], p, topo["triangles"][t0:t0 + nt]) == []
+
+
+def test_gpu_build_into_caller_buffers(gpu_ctx):
+    """build_polyhedra(out=...) into larger pinned buffers returns views of their leading rows that
+    equal the arrays of a plain build, byte for byte; a buffer too short is refused."""
+    import torch
+    cloud, first, count = W.ellipsoid_hulls(3000, 66, 7, 16, 64)
+    pts, hulls, topo = build_polyhedra(cloud, first, count, ctx=gpu_ctx)
+
+    def pinned(rows, cols, dt):
+        shape = (rows + 17, cols) if cols else (rows + 17,)
+        return torch.zeros(shape, dtype=dt, pin_memory=True).numpy()
+    out = {"points": pinned(len(pts), 3, torch.float32), "hulls": pinned(len(hulls), 8, torch.int32).view(np.uint32)}
+    for k, a in topo.items():
+        out[k] = pinned(len(a), a.shape[1] if a.ndim == 2 else 0, torch.float32 if a.dtype == np.float32 else torch.int32)
+        if a.dtype == np.uint32:
+            out[k] = out[k].view(np.uint32)
+    p2, h2, t2 = build_polyhedra(cloud, first, count, ctx=gpu_ctx, out=out)
+    np.testing.assert_array_equal(p2.view(np.uint32), pts.view(np.uint32))
+    np.testing.assert_array_equal(h2, hulls)
+    for k in topo:
+        np.testing.assert_array_equal(t2[k].view(np.uint32), topo[k].view(np.uint32))
+        assert np.shares_memory(t2[k], out[k])
+    short = dict(out)
+    short["face_vertices"] = out["face_vertices"][: len(topo["face_vertices"]) - 1]
+    with pytest.raises(ValueError):
+        build_polyhedra(cloud, first, count, ctx=gpu_ctx, out=short)
