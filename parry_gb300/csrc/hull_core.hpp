@@ -77,10 +77,9 @@ struct HFace {
   uint32_t v[3];
   uint32_t alive;   // 0 dead, 1 live, 2 live and seen from the point being inserted
   uint32_t adj[3];  // the face across edge (v[k], v[k + 1])
-  uint32_t pad;
-  D3 n;             // unit normal and offset: the rounded plane, a filter for the exact test
-  double off;
-  double tol;       // bound on the rounding of n . p - off over the cloud
+  float off;        // unit normal and offset rounded to f32: a filter for the exact test
+  float n[3];
+  float tol;        // bound on the error of n . p - off (evaluated in f32) over the cloud
 };
 
 // ---- exact orientation ----------------------------------------------------------------------
@@ -372,22 +371,25 @@ HC_FN uint32_t hull_triangles(const float* in, uint32_t n, const HullCaps& caps,
     HFace f;
     f.v[0] = a; f.v[1] = b; f.v[2] = c;
     f.adj[0] = f0; f.adj[1] = f1; f.adj[2] = f2;
-    f.pad = 0;
     const D3 pa = ws.pts[a], u = dsub(ws.pts[b], pa), v = dsub(ws.pts[c], pa);
     D3 fn = dcross(u, v);
     double l = sqrt(ddot(fn, fn));
-    f.n = l > 0 ? D3{fn.x / l, fn.y / l, fn.z / l} : D3{0, 0, 0};
-    f.off = ddot(f.n, pa);
-    // rounding of the normal's direction (relative to how thin the face is) times the cloud's
-    // extent, plus the rounding of the two dot products
+    const D3 nd = l > 0 ? D3{fn.x / l, fn.y / l, fn.z / l} : D3{0, 0, 0};
+    f.n[0] = (float)nd.x; f.n[1] = (float)nd.y; f.n[2] = (float)nd.z;
+    f.off = (float)ddot(nd, pa);
+    // the f32 evaluation (products, sums, and the rounding of the normal and offset to f32: about
+    // 9 f32 epsilons of the cloud's radius) plus the normal's direction error in double (relative to
+    // how thin the face is) times the cloud's extent, with margin; infinite for a degenerate face
     const double cond = l > 0 ? sqrt(ddot(u, u) * ddot(v, v)) / l : 1e300;
-    f.tol = 1e-14 * (rmax + scale * (1.0 + cond));
+    f.tol = (float)(1e-6 * (rmax + scale * (1.0 + cond)));
     f.alive = 1;
     ws.faces[nf++] = f;
   };
-  // whether face F sees p (p strictly above its plane), exactly
-  auto sees = [&](const HFace& F, const D3& p) {
-    const double d = ddot(F.n, p) - F.off;
+  // the f32 filter's signed distance of point pf from face F's plane
+  auto dist = [](const HFace& F, const F3& pf) { return ((F.n[0] * pf.x + F.n[1] * pf.y) + F.n[2] * pf.z) - F.off; };
+  // whether face F sees p (p strictly above its plane), exactly (pf: p's f32 coordinates)
+  auto sees = [&](const HFace& F, const F3& pf, const D3& p) {
+    const float d = dist(F, pf);
     if (d > F.tol) return true;
     if (d < -F.tol) return false;
     return orient3d_sign(ws.pts[F.v[0]], ws.pts[F.v[1]], ws.pts[F.v[2]], p) > 0;
@@ -414,15 +416,16 @@ HC_FN uint32_t hull_triangles(const float* in, uint32_t n, const HullCaps& caps,
       if (nf + caps.horizon > caps.faces) return 0;  // more live faces than a closed hull of n points has
     }
     const D3 pp = ws.pts[pi];
-    // the face that sees pp at the largest distance, then every face that sees pp connected to it
-    // (for a convex hull and an exact test, that is every face that sees pp)
+    const F3 pf = F3{in[3 * pi], in[3 * pi + 1], in[3 * pi + 2]};
+    // the face that sees pp at the largest (filter) distance, then every face that sees pp connected
+    // to it (for a convex hull and an exact test, that is every face that sees pp)
     uint32_t seed = NONE;
-    double bestd = -1e300;
+    float bestd = 0.0f;
     for (uint32_t f = 0; f < nf; ++f) {
       const HFace& F = ws.faces[f];
       if (!F.alive) continue;
-      const double d = ddot(F.n, pp) - F.off;
-      if (d > bestd && d >= -F.tol && sees(F, pp)) { bestd = d; seed = f; }
+      const float d = dist(F, pf);  // NaN (overflowing coordinates): left to the exact test
+      if (!(d < -F.tol) && (seed == NONE || d > bestd) && sees(F, pf, pp)) { bestd = d; seed = f; }
     }
     if (seed == NONE) continue;  // inside or on the hull
     uint32_t nvis = 0;
@@ -432,7 +435,7 @@ HC_FN uint32_t hull_triangles(const float* in, uint32_t n, const HullCaps& caps,
       for (int j = 0; j < 3; ++j) {
         const uint32_t g = ws.faces[ws.visible[i]].adj[j];
         HFace& G = ws.faces[g];
-        if (G.alive == 1 && sees(G, pp)) {
+        if (G.alive == 1 && sees(G, pf, pp)) {
           G.alive = 2;
           ws.visible[nvis++] = g;
         }
