@@ -218,3 +218,49 @@ def test_in_place_host_access(oracle_lib, traversal):
     m.cast_rays_and_get_normal(rp.cuda(), 100.0, out=(fp, tp, npn))
     _compare(fp.numpy().view(np.uint32), tp.numpy(), npn.numpy(), fo, to, no)
     ctx.close()
+
+
+def _grid_mesh(nx=8, nz=8, tilt=False):
+    """A height field on integer grid points (heights 0..3, exact in f32), two triangles per cell
+    (one diagonal), or a tilted plane: shared edges and vertices where hits tie exactly."""
+    xs, zs = np.meshgrid(np.arange(nx + 1, dtype=np.float32), np.arange(nz + 1, dtype=np.float32), indexing="ij")
+    h = (xs * 0.5 + zs * 0.25) if tilt else ((xs.astype(np.int64) * 7 + zs.astype(np.int64) * 3) % 4).astype(np.float32)
+    v = np.stack([xs.ravel(), h.ravel().astype(np.float32), zs.ravel()], axis=1).astype(np.float32)
+    idx = []
+    for i in range(nx):
+        for j in range(nz):
+            a, b, c, d = i * (nz + 1) + j, (i + 1) * (nz + 1) + j, (i + 1) * (nz + 1) + j + 1, i * (nz + 1) + j + 1
+            idx += [[a, d, b], [b, d, c]]
+    return v, np.array(idx, np.uint32)
+
+
+@pytest.mark.parametrize("tilt", [False, True])
+def test_degenerate_rays_vs_oracle(gpu_ctx, oracle_lib, tilt):
+    """Rays the reference's arithmetic treats specially, against the f32 oracle: straight down onto
+    grid vertices and edges (exact toi ties between triangles: the lowest index wins), axis-aligned
+    and two-zero-component directions (the slab test's zero-direction branch), horizontal rays along
+    the grid lines (parallel to faces), origins on the surface (toi 0), hits at exactly max_toi
+    (rejected) and the zero direction."""
+    v, i = _grid_mesh(tilt=tilt)
+    rays = []
+    for x in np.arange(0.0, 8.01, 0.5):
+        for z in np.arange(0.0, 8.01, 0.5):
+            rays.append([x, 10.0, z, 0.0, -1.0, 0.0])           # vertical: vertices, edges, cell centres
+            rays.append([x, 10.0, z, 0.0, -1.0, 1e-30])          # nearly vertical, denormal-free tiny component
+    for y in np.arange(0.0, 3.01, 0.5):
+        for k in np.arange(0.0, 8.01, 1.0):
+            rays.append([-1.0, y, k, 1.0, 0.0, 0.0])             # along grid lines, one axis only
+            rays.append([k, y, -1.0, 0.0, 0.0, 1.0])
+            rays.append([-1.0, y, -1.0, 1.0, 0.0, 1.0])          # diagonal, zero y component
+    for x in np.arange(0.25, 8.0, 1.0):
+        rays.append([x, float(v[int(x) * 9, 1]) if not tilt else x * 0.5, 0.0, 0.0, -1.0, 0.0])  # on or at the surface
+    rays.append([4.0, 10.0, 4.0, 0.0, 0.0, 0.0])                 # zero direction
+    rays = np.array(rays, np.float32)
+    m = pg.TriMesh(gpu_ctx, v, i)
+    O = oracle_lib.TriMesh(v, i)
+    for max_toi in (100.0, 7.0, 10.0 - 1.0):
+        f, t, n = m.cast_rays_and_get_normal(rays, max_toi)
+        fo, to, no = O.cast_rays_and_get_normal(rays, max_toi)
+        _compare(f, t, n, fo, to, no)
+        np.testing.assert_array_equal(t[fo != pg.NO_HIT].view(np.uint32), to[fo != pg.NO_HIT].view(np.uint32))
+    assert int((fo != pg.NO_HIT).sum()) > len(rays) // 3
