@@ -217,3 +217,40 @@ def test_pipelined_host_buffers_match_device_buffers(gpu_ctx, shuffle):
     np.testing.assert_array_equal(ph.numpy(), dh)
     np.testing.assert_array_equal(pr.numpy().view(np.uint32), dr.view(np.uint32))
     np.testing.assert_array_equal(pf.numpy().view(np.uint32), dfin.view(np.uint32))
+
+
+def test_degenerate_contacts_vs_oracle(gpu_ctx, oracle_lib):
+    """Configurations the reference's branches single out, against the f32 oracle: coincident
+    shapes (same pose), cuboids face to face at distance exactly 0 and at exactly the prediction,
+    a ball centred inside a cuboid and at a cuboid's corner, balls touching, capsules whose axes
+    cross, a flat (coplanar) hull and one with repeated points, coplanar triangles, and every pair
+    the other way round (ball first / ball second paths)."""
+    I = pg.shapes.pose7([0, 0, 0], [0, 0, 0, 1])
+
+    def at(x, y=0.0, z=0.0, q=(0, 0, 0, 1)):
+        return pg.shapes.pose7([x, y, z], q)
+    s = pg.ShapeSet()
+    s.add_cuboid([1, 1, 1], I)                                   # 0
+    s.add_cuboid([1, 1, 1], I)                                   # 1 coincident with 0
+    s.add_cuboid([1, 1, 1], at(2.0))                             # 2 face to face with 0, distance 0
+    s.add_cuboid([1, 1, 1], at(2.25))                            # 3 distance 0.25 from 0
+    s.add_ball(0.5, I)                                           # 4 centred inside 0
+    s.add_ball(0.5, at(1.0, 1.0, 1.0))                           # 5 centred on a corner of 0
+    s.add_ball(1.0, at(3.0))                                     # 6
+    s.add_ball(1.0, at(5.0))                                     # 7 touching 6
+    s.add_capsule(1.0, 0.5, I)                                   # 8 along y
+    s.add_capsule(1.0, 0.5, at(0.0, 0.0, 0.0, (0.0, 0.0, np.sqrt(0.5), np.sqrt(0.5))))  # 9 along x, axes cross
+    sq = np.array([[-1, 0, -1], [1, 0, -1], [1, 0, 1], [-1, 0, 1], [0, 0, 0]], np.float32)
+    s.add_convex(sq, at(0.0, 1.0))                               # 10 flat hull on top of 0
+    rep = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0], [0, 0, 1], [1, 0, 0], [0, 1, 0]], np.float32)
+    s.add_convex(rep, at(0.5, 0.5, 0.5))                         # 11 repeated points, inside 0
+    s.add_triangle([-1, 0, -1], [1, 0, -1], [0, 0, 1], I)        # 12
+    s.add_triangle([-1, 0, -1], [1, 0, -1], [0, 0, 1], I)        # 13 coplanar with 12
+    s.add_triangle([-1, 0, 1], [1, 0, 1], [0, 0, -1], at(0.0, 1.0))  # 14 on the top face of 0
+    n = 15
+    pairs = np.array([(a, b) for a in range(n) for b in range(n) if a != b], np.uint32)
+    for pred in (0.0, 0.25, 1.0):
+        has, out = pg.contacts(gpu_ctx, s, pairs, pred)
+        ho, oo, _ = oracle_lib.contacts(s, pairs, pred)
+        _compare(has, out, ho, oo, f"degenerate configurations, prediction {pred}")
+    assert ho.sum() > len(pairs) // 3
