@@ -452,7 +452,8 @@ __device__ __forceinline__ bool local_box_may_hit(const CompoundDev& cd, uint32_
     if (fabsf(dd[i]) < 1e-30f) {
       if (oo[i] < lov[i] || oo[i] > hiv[i]) return false;
     } else {
-      float a = (lov[i] - oo[i]) / dd[i], b = (hiv[i] - oo[i]) / dd[i];
+      // fast division (within 2 ulp): the inflated box and the padded tmax absorb it
+      float a = __fdividef(lov[i] - oo[i], dd[i]), b = __fdividef(hiv[i] - oo[i], dd[i]);
       if (a > b) { float t = a; a = b; b = t; }
       tmin = fmaxf(tmin, a);
       tmax = fminf(tmax, b);
