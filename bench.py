@@ -140,6 +140,31 @@ def measured_peak_bf16() -> tuple[float, str]:
     return 1900.0, "fallback"
 
 
+def measured_fp32_peak(n: int = 8192, reps: int = 3) -> float:
+    """FP32 (FFMA) throughput measured in this process: cuBLAS SGEMM with TF32 off, n x n x n, best
+    of `reps` (TFLOP/s). The denominator of the FP32-bound kernels' roofline."""
+    import torch
+    prev = torch.backends.cuda.matmul.allow_tf32
+    torch.backends.cuda.matmul.allow_tf32 = False
+    try:
+        a = torch.randn((n, n), device="cuda", dtype=torch.float32)
+        b = torch.randn((n, n), device="cuda", dtype=torch.float32)
+        c = a @ b
+        best = float("inf")
+        for _ in range(reps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            e0.record()
+            torch.matmul(a, b, out=c)
+            e1.record()
+            torch.cuda.synchronize()
+            best = min(best, e0.elapsed_time(e1))
+        del a, b, c
+        return 2.0 * n ** 3 / (best / 1e3) / 1e12
+    finally:
+        torch.backends.cuda.matmul.allow_tf32 = prev
+
+
 def profiled_traffic(name: str, key: str = "dram_bytes_per_launch_full_size") -> float | None:
     """A figure recorded from an ncu capture (profiles/<name>.txt, line `<key>: <value> ...`):
     by default the dram read+write bytes per launch at the full size."""
@@ -651,7 +676,8 @@ def contacts_section(ctx, stream, steps: int, warmup: int, n_pairs: int, flush, 
     except Exception:
         pass
     sms = torch.cuda.get_device_properties(0).multi_processor_count
-    fp32_peak = sms * 128 * 2 * sm_mhz * 1e6 / 1e12
+    fp32_nominal = sms * 128 * 2 * sm_mhz * 1e6 / 1e12
+    fp32_peak = measured_fp32_peak()
     achieved = flops_per_pair * n_pairs / (kernel_ms / 1e3) / 1e12
     # algorithmic HBM bytes per pair: both hulls' vertices once, the pair, two poses and params, the
     # output; against the DRAM bytes an ncu capture of the same kernels measured per pair
@@ -672,7 +698,8 @@ def contacts_section(ctx, stream, steps: int, warmup: int, n_pairs: int, flush, 
                             "epa_calls": gst["epa_calls"]},
         "contact_fraction": round(float(has.float().mean().item()), 4),
         "roofline": {"bound": "fp32", "achieved": round(achieved, 4), "peak": round(fp32_peak, 1), "unit": "TFLOP/s",
-                     "frac": round(achieved / fp32_peak, 6), "peak_source": "nominal: SMs x 128 lanes x 2 (FMA) x max SM clock",
+                     "frac": round(achieved / fp32_peak, 6), "peak_source": "measured: cuBLAS SGEMM 8192^3, TF32 off, in this process",
+                     "nominal_peak": round(fp32_nominal, 1), "nominal_source": "SMs x 128 lanes x 2 (FMA) x max SM clock",
                      "flops_per_pair": round(flops_per_pair, 1),
                      "flops_model": "5 flops per vertex dot x vertices scanned by the f32 oracle's support calls on a sample"},
         "roofline_hbm": {"bound": "hbm", "achieved": round(alg_bytes * n_pairs / (kernel_ms / 1e3) / 1e9, 1), "peak": hbm_peak,
