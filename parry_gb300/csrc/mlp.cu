@@ -4,8 +4,8 @@
 // the weights resident in shared memory); training runs per-layer mma.sync m16n8k16 GEMMs with FP32
 // accumulation and separate bias / activation / gradient kernels. No reference counterpart: its only link to the
 // reference is the init_dir parameter of contact_support_map_support_map_with_params
-// (src/query/contact/contact_support_map_support_map.rs:40-62), and the plain GJK result remains
-// the judge of the answer - a poor guess only costs iterations.
+// (src/query/contact/contact_support_map_support_map.rs:40-62), and GJK from that start still
+// decides the answer - a poor guess only costs iterations.
 //
 // Network: 48 (39 features + zero padding) -> 128 -> 128 -> 128 -> 128 -> 3, GELU (erf form) after
 // each hidden layer, output normalised to a unit direction in the first shape's frame.
