@@ -472,7 +472,8 @@ typedef struct parrygpu_mlp parrygpu_mlp;
 /* Xavier-uniform initialisation from `seed`. */
 parrygpu_status parrygpu_mlp_create(parrygpu_ctx* ctx, uint64_t seed, parrygpu_mlp** out);
 void parrygpu_mlp_destroy(parrygpu_mlp* mlp);
-/* Pair features (n_pairs x 48 floats: relative pose of b in a's frame, descriptors of a and b). */
+/* Pair features (n_pairs x 48 floats: relative pose of b in a's frame, descriptors of a and b) into a
+ * 16-byte aligned buffer. Asynchronous when every buffer is on the device; synchronises otherwise. */
 parrygpu_status parrygpu_mlp_features(parrygpu_ctx* ctx, const parrygpu_shapes* shapes, const uint32_t* pairs, uint64_t n_pairs,
                                       float* features);
 /* Trains on (features, unit target directions) with Adam for `epochs` passes in minibatches of

@@ -589,13 +589,27 @@ __device__ void pair_features(const float* __restrict__ poses, const float* __re
   for (int j = 0; j < DESC; ++j) { o[7 + j] = desc[16 * (size_t)a + j]; o[7 + DESC + j] = desc[16 * (size_t)b + j]; }
 }
 
-__global__ void k_pair_features(const float* __restrict__ poses, const float* __restrict__ desc, const uint32_t* __restrict__ pairs, uint64_t n,
-                                uint64_t n_shapes, float* __restrict__ f, const uint32_t* __restrict__ rows,
-                                const unsigned long long* __restrict__ d_count) {
+// 128 rows per block turn: each thread builds its row in shared memory, then the block stores the
+// rows' contiguous span with 16-byte stores (f must be 16-byte aligned).
+constexpr int PF_THREADS = 128;
+__global__ void __launch_bounds__(PF_THREADS) k_pair_features(const float* __restrict__ poses, const float* __restrict__ desc,
+                                                              const uint32_t* __restrict__ pairs, uint64_t n, uint64_t n_shapes,
+                                                              float* __restrict__ f, const uint32_t* __restrict__ rows,
+                                                              const unsigned long long* __restrict__ d_count) {
+  __shared__ __align__(16) float tile[PF_THREADS * IN];
   if (d_count && *d_count < n) n = *d_count;
-  for (uint64_t k = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; k < n; k += (uint64_t)gridDim.x * blockDim.x) {
-    const uint64_t p = rows ? rows[k] : k;
-    pair_features(poses, desc, pairs[2 * p], pairs[2 * p + 1], n_shapes, f + k * IN);
+  for (uint64_t base = blockIdx.x * (uint64_t)PF_THREADS; base < n; base += (uint64_t)gridDim.x * PF_THREADS) {
+    const uint64_t k = base + threadIdx.x;
+    if (k < n) {
+      const uint64_t p = rows ? rows[k] : k;
+      pair_features(poses, desc, pairs[2 * p], pairs[2 * p + 1], n_shapes, tile + threadIdx.x * IN);
+    }
+    __syncthreads();
+    const uint64_t m = n - base < (uint64_t)PF_THREADS ? n - base : (uint64_t)PF_THREADS;
+    const float4* src = reinterpret_cast<const float4*>(tile);
+    float4* dst = reinterpret_cast<float4*>(f + base * IN);
+    for (uint32_t i = threadIdx.x; i < (uint32_t)m * (IN / 4); i += PF_THREADS) dst[i] = src[i];
+    __syncthreads();
   }
 }
 
@@ -717,8 +731,8 @@ parrygpu_status pg::launch_seed_dirs(parrygpu_ctx* ctx, const ShapeArrays& sh, c
                                      const unsigned long long* d_count, uint64_t cap) {
   if (cap == 0) return PARRYGPU_OK;
   const uint64_t sms = ctx->sm_count > 0 ? (uint64_t)ctx->sm_count : 152u;
-  const uint64_t fgrid = div_up(cap, 128) < sms * 16 ? div_up(cap, 128) : sms * 16;
-  k_pair_features<<<(uint32_t)fgrid, 128, 0, ctx->stream>>>(sh.poses, seed.desc, d_pairs, cap, sh.n_shapes, seed.feat, seed.list, d_count);
+  const uint64_t fgrid = div_up(cap, PF_THREADS) < sms * 16 ? div_up(cap, PF_THREADS) : sms * 16;
+  k_pair_features<<<(uint32_t)fgrid, PF_THREADS, 0, ctx->stream>>>(sh.poses, seed.desc, d_pairs, cap, sh.n_shapes, seed.feat, seed.list, d_count);
   PG_LAUNCHED(ctx);
   const uint64_t tiles = (cap + TC_M - 1) / TC_M;
   k_mlp_infer_tc<<<(uint32_t)(tiles < sms ? tiles : sms), TC_THREADS, TC_SMEM, ctx->stream>>>(
@@ -798,17 +812,21 @@ parrygpu_status parrygpu_mlp_features(parrygpu_ctx* ctx, const parrygpu_shapes* 
   void* d_f;
   bool copy;
   if ((s = stage_output(ctx, ctx->stage_out[0], features, n_pairs * IN * 4, &d_f, &copy)) != PARRYGPU_OK) return s;
-  PG_CUDA(ctx, ctx->misc.reserve(64));
+  if (((uintptr_t)d_f & 15) != 0) return set_error(ctx, PARRYGPU_INVALID_ARG, "parrygpu_mlp_features needs a 16-byte aligned output");
   DevBuf& desc = ctx->stage_out[3];
   PG_CUDA(ctx, desc.reserve(shapes->n * 16 * 4));
   k_shape_desc<<<div_up(shapes->n * 32, 256), 256, 0, ctx->stream>>>((const uint32_t*)t, (const float4*)p, (const float*)v, shapes->n, shapes->n_vertices,
                                                                  desc.as<float>());
   PG_LAUNCHED(ctx);
-  k_pair_features<<<div_up(n_pairs, 128), 128, 0, ctx->stream>>>((const float*)q, desc.as<float>(), (const uint32_t*)dp, n_pairs, shapes->n,
-                                                                 (float*)d_f, nullptr, nullptr);
+  k_pair_features<<<div_up(n_pairs, PF_THREADS), PF_THREADS, 0, ctx->stream>>>((const float*)q, desc.as<float>(), (const uint32_t*)dp, n_pairs,
+                                                                               shapes->n, (float*)d_f, nullptr, nullptr);
   PG_LAUNCHED(ctx);
   if (copy) PG_CUDA(ctx, cudaMemcpyAsync(features, d_f, n_pairs * IN * 4, cudaMemcpyDeviceToHost, ctx->stream));
-  return parrygpu_sync(ctx);
+  // host inputs or outputs: wait for their copies; all on the device: return at once, as the other calls do
+  const bool staged = t != shapes->types || p != shapes->params || q != shapes->poses || dp != pairs ||
+                      (shapes->n_vertices && v != shapes->vertices);
+  if (copy || staged) return parrygpu_sync(ctx);
+  return PARRYGPU_OK;
 }
 
 parrygpu_status parrygpu_mlp_train(parrygpu_ctx* ctx, parrygpu_mlp* mlp, const float* features, const float* targets, uint64_t n, uint32_t epochs,
