@@ -85,8 +85,13 @@ def test_training_and_warm_start(gpu_ctx, tmp_path):
 def test_tcgen05_inference_matches_oracle_and_mma_path(gpu_ctx, n):
     """The fused tcgen05 inference kernel (weights resident in shared memory, TMEM accumulators,
     all five layers per 128-sample tile) against the float64 forward with the same BF16 rounding,
-    and against the per-layer mma.sync forward: unit directions with cosine above 0.999 for every
-    sample (the accumulation order differs, so a BF16 activation can round the other way)."""
+    and against the per-layer mma.sync forward. The mma.sync forward (erf GELU) gives unit
+    directions with cosine above 0.999 for every sample (the accumulation order differs, so a BF16
+    activation can round the other way). The tcgen05 epilogue evaluates GELU in tanh form with the
+    tanh.approx instruction (2.6e-5 from the erf form, 2^-11 relative), below the BF16 rounding of
+    each activation; on these random, untrained weights a rare sample whose output vector is short
+    turns those last bits into a direction a few degrees off, so the bound there is statistical:
+    median cosine above 0.99999, 99.9 % of the samples above 0.999, every sample above 0.99."""
     from oracle import mlp_ref
     rng = np.random.default_rng(n)
     mlp = pg.WarmStartMLP(gpu_ctx, seed=11)
@@ -105,9 +110,14 @@ def test_tcgen05_inference_matches_oracle_and_mma_path(gpu_ctx, n):
         assert d.shape == (n, 3) and np.isfinite(d).all()
         np.testing.assert_allclose(np.linalg.norm(d, axis=1), 1.0, atol=1e-5)
         cos = np.sum(d.astype(np.float64) * ref, axis=1)
-        print(f"\n{what}: cosine to the oracle min {cos.min():.7f} median {np.median(cos):.9f}")
-        assert cos.min() > 0.999, what
-    assert np.sum(d_tc * d_mma, axis=1).min() > 0.999
+        q = np.quantile(cos, 0.001)
+        print(f"\n{what}: cosine to the oracle min {cos.min():.7f} 0.1 % {q:.7f} median {np.median(cos):.9f}")
+        if what == "mma.sync":
+            assert cos.min() > 0.999, what
+        else:
+            assert cos.min() > 0.99 and q > 0.999 and np.median(cos) > 0.99999, what
+    cross = np.sum(d_tc * d_mma, axis=1)
+    assert cross.min() > 0.99 and np.quantile(cross, 0.001) > 0.999
 
 
 def _quat_rotate(q, v):
