@@ -276,8 +276,8 @@ __global__ void k_features_to_bf16(const float* __restrict__ f, size_t n, bf16* 
 // thread issues K/16 tcgen05.mma (M = 128, N = 128, or 16 for the 3-wide output layer padded with
 // zero rows, K = 16 each) into the group's 128-column FP32 TMEM accumulator and commits them to the
 // group's mbarrier; the group's 8 warps then read the accumulator back (warp w of the group: TMEM
-// lanes 32 (w % 4) .. + 31, columns 64 (w / 4) .. + 63), add the bias, apply GELU (erf by a
-// published rational approximation, gelu_as) and write the next layer's BF16 activations into
+// lanes 32 (w % 4) .. + 31, columns 64 (w / 4) .. + 63), add the bias, apply GELU (tanh form with
+// one special-function operation, gelu_th) and write the next layer's BF16 activations into
 // shared memory. The output layer's 3 columns are normalised
 // into the init direction (the fallback of k_normalize_dirs for degenerate outputs). Activations
 // never leave the SM. `d_count` (may be null) bounds the rows on the device (min(n, *d_count));
@@ -306,17 +306,6 @@ static_assert(tc_w_off(1) % 1024 == 0 && TC_ACT_OFF % 1024 == 0 && TC_BAR_OFF % 
 // Byte offset of element (r, k) of an R x K K-major operand in the canonical layout.
 __device__ __forceinline__ uint32_t tc_off(uint32_t r, uint32_t k, uint32_t K) {
   return ((r >> 3) * (K >> 3) + (k >> 3)) * 128u + (r & 7u) * 16u + (k & 7u) * 2u;
-}
-
-// GELU for the inference epilogue with erf from Abramowitz & Stegun, Handbook of Mathematical
-// Functions, 7.1.26 (|error| <= 1.5e-7, far below the BF16 rounding the activation then takes):
-// erf(z) = 1 - (a1 t + a2 t^2 + a3 t^3 + a4 t^4 + a5 t^5) exp(-z^2), t = 1 / (1 + p z), z >= 0.
-__device__ __forceinline__ float gelu_as(float x) {
-  const float z = fabsf(x) * 0.70710678118654752f;
-  const float t = __fdividef(1.0f, fmaf(0.3275911f, z, 1.0f));
-  const float poly = t * fmaf(t, fmaf(t, fmaf(t, fmaf(t, 1.061405429f, -1.453152027f), 1.421413741f), -0.284496736f), 0.254829592f);
-  const float e = 1.0f - poly * __expf(-z * z);
-  return 0.5f * x * (1.0f + copysignf(e, x));
 }
 
 // GELU for the inference epilogue in the tanh form of Hendrycks and Gimpel ("Gaussian Error Linear
