@@ -181,12 +181,28 @@ static __device__ __noinline__ bool epa_face_bcoords(V3 A, V3 B, V3 C, float bc[
   return false;
 }
 
+// The `inside` answer of epa_face_bcoords alone: the face region needs neither its barycentric
+// coordinates nor their division, and a vertex or edge region only its projected point.
+static __device__ __noinline__ bool epa_face_inside(V3 A, V3 B, V3 C) {
+  const TriRegion r = tri_region(A, B, C, v3(0.f, 0.f, 0.f));
+  if (r.region >= 6) return r.region == 6;
+  V3 proj;
+  if (r.region < 3) {
+    proj = r.region == 0 ? A : (r.region == 1 ? B : C);
+  } else {
+    float t;
+    proj = tri_edge_point(r, A, B, &t);
+  }
+  bool is_inside = fabsf(proj.x) <= EPS && fabsf(proj.y) <= EPS && fabsf(proj.z) <= EPS;
+  float tol = EPS * 100.0f;
+  return is_inside || dot(proj, proj) < tol * tol;
+}
+
 // Face::new (epa3.rs:90-118): writes face `fid`, returns whether the origin projects inside it.
 template <class WS>
 static __device__ __noinline__ bool epa_new_face(const WS& ws, int fid, int p0, int p1, int p2, int a0, int a1, int a2) {
   V3 A = ws.vp(p0), B = ws.vp(p1), C = ws.vp(p2);
-  float bc[3];
-  bool inside = epa_face_bcoords(A, B, C, bc);
+  bool inside = epa_face_inside(A, B, C);
   V3 n;
   if (!try_normalize(cross(B - A, C - A), EPS, &n)) n = v3(0.f, 0.f, 0.f);
   int o = ws.fo(fid);

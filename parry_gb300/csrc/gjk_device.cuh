@@ -211,51 +211,70 @@ __device__ __forceinline__ V3 project_segment(V3 a, V3 b, V3 pt, Loc* loc) {
 
 // The triangle and tetrahedron projections have an inline body for kernels that keep their simplex
 // in registers, and an out-of-line copy that the other kernels share.
-// The region tests are evaluated in full and the answer selected, instead of returning at the
-// first region that holds: lanes of a warp that project onto different regions then stay on one
-// path. Every value is the expression the early-return form computes for its region (same
-// operands, same operations), so the answer is the same bits.
-__device__ __forceinline__ V3 project_triangle_inl(V3 a, V3 b, V3 c, V3 pt, Loc* loc) {
-  const V3 ab = b - a, ac = c - a, ap = pt - a;
-  const float ab_ap = dot(ab, ap), ac_ap = dot(ac, ap);
-  const V3 bp = pt - b;
-  const float ab_bp = dot(ab, bp), ac_bp = dot(ac, bp);
-  const V3 cp = pt - c;
-  const float ab_cp = dot(ab, cp), ac_cp = dot(ac, cp);
-  const V3 bc = c - b;
-  const V3 n = cross(ab, ac);
-  const float vc = dot(n, cross(ab, ap));
-  const float vb = -dot(n, cross(ac, cp));
-  const float va = dot(n, cross(bc, bp));
-  // the first region that holds, in the early-return form's order
+// The Voronoi region of pt against triangle (a, b, c), with the quantities its projection needs.
+// The region tests are evaluated in full and the first that holds selected, instead of returning
+// at the first region that holds: lanes of a warp that project onto different regions then stay on
+// one path. Every value is the expression the early-return form computes (same operands, same
+// operations), so the answer is the same bits.
+struct TriRegion {
+  V3 ab, ac, bc, ap, bp, n;
+  float ab_ap, ac_ap, va, vb, vc;
   int region;  // 0-2 vertex a / b / c, 3 edge ab, 4 edge ac, 5 edge bc, 6 face, 7 solid
-  if (ab_ap <= 0.0f && ac_ap <= 0.0f) region = 0;
-  else if (ab_bp >= 0.0f && ac_bp <= ab_bp) region = 1;
-  else if (ac_cp >= 0.0f && ab_cp <= ac_cp) region = 2;
-  else if (vc < 0.0f && ab_ap >= 0.0f && ab_bp <= 0.0f) region = 3;
-  else if (vb < 0.0f && ac_ap >= 0.0f && ac_cp <= 0.0f) region = 4;
-  else if (va < 0.0f && ac_bp - ab_bp >= 0.0f && ab_cp - ac_cp >= 0.0f) region = 5;
-  else if (va + vb + vc != 0.0f) region = 6;
-  else region = 7;
+};
+
+__device__ __forceinline__ TriRegion tri_region(V3 a, V3 b, V3 c, V3 pt) {
+  TriRegion r;
+  r.ab = b - a; r.ac = c - a; r.ap = pt - a;
+  r.ab_ap = dot(r.ab, r.ap); r.ac_ap = dot(r.ac, r.ap);
+  r.bp = pt - b;
+  const float ab_bp = dot(r.ab, r.bp), ac_bp = dot(r.ac, r.bp);
+  const V3 cp = pt - c;
+  const float ab_cp = dot(r.ab, cp), ac_cp = dot(r.ac, cp);
+  r.bc = c - b;
+  r.n = cross(r.ab, r.ac);
+  r.vc = dot(r.n, cross(r.ab, r.ap));
+  r.vb = -dot(r.n, cross(r.ac, cp));
+  r.va = dot(r.n, cross(r.bc, r.bp));
+  if (r.ab_ap <= 0.0f && r.ac_ap <= 0.0f) r.region = 0;
+  else if (ab_bp >= 0.0f && ac_bp <= ab_bp) r.region = 1;
+  else if (ac_cp >= 0.0f && ab_cp <= ac_cp) r.region = 2;
+  else if (r.vc < 0.0f && r.ab_ap >= 0.0f && ab_bp <= 0.0f) r.region = 3;
+  else if (r.vb < 0.0f && r.ac_ap >= 0.0f && ac_cp <= 0.0f) r.region = 4;
+  else if (r.va < 0.0f && ac_bp - ab_bp >= 0.0f && ab_cp - ac_cp >= 0.0f) r.region = 5;
+  else if (r.va + r.vb + r.vc != 0.0f) r.region = 6;
+  else r.region = 7;
+  return r;
+}
+
+// The edge projection of a region 3-5: base + dir * t, t = num / |dir|^2.
+__device__ __forceinline__ V3 tri_edge_point(const TriRegion& r, V3 a, V3 b, float* t_out) {
+  const V3 base = r.region == 5 ? b : a;
+  const V3 dir = r.region == 3 ? r.ab : (r.region == 4 ? r.ac : r.bc);
+  const float num = r.region == 3 ? r.ab_ap : (r.region == 4 ? r.ac_ap : dot(r.bc, r.bp));
+  const float t = num / dot(dir, dir);
+  *t_out = t;
+  return base + dir * t;
+}
+
+__device__ __forceinline__ V3 project_triangle_inl(V3 a, V3 b, V3 c, V3 pt, Loc* loc) {
+  const TriRegion r = tri_region(a, b, c, pt);
+  const int region = r.region;
   if (region < 3) {
     *loc = Loc{LOC_VERTEX, region, {region == 0 ? 1.f : 0.f, region == 1 ? 1.f : 0.f, region == 2 ? 1.f : 0.f}};
     return region == 0 ? a : (region == 1 ? b : c);
   }
   if (region < 6) {
-    // edge: base + dir * (num / den)
-    const V3 base = region == 5 ? b : a;
-    const V3 dir = region == 3 ? ab : (region == 4 ? ac : bc);
-    const float num = region == 3 ? ab_ap : (region == 4 ? ac_ap : dot(bc, bp));
-    const float t = num / dot(dir, dir);
+    float t;
+    const V3 p = tri_edge_point(r, a, b, &t);
     *loc = Loc{LOC_EDGE, region == 3 ? 0 : (region == 4 ? 2 : 1), {1.0f - t, t, 0.f}};
-    return base + dir * t;
+    return p;
   }
   if (region == 6) {
-    const int side = dot(n, ap) >= 0.0f ? 0 : 1;
-    const float denom = 1.0f / (va + vb + vc);
-    const float v = vb * denom, w = vc * denom;
+    const int side = dot(r.n, r.ap) >= 0.0f ? 0 : 1;
+    const float denom = 1.0f / ((r.va + r.vb) + r.vc);
+    const float v = r.vb * denom, w = r.vc * denom;
     *loc = Loc{LOC_FACE, side, {(1.0f - v) - w, v, w}};
-    return (a + ab * v) + ac * w;
+    return (a + r.ab * v) + r.ac * w;
   }
   *loc = Loc{LOC_SOLID, 0, {0.f, 0.f, 0.f}};
   return pt;
