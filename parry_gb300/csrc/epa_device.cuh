@@ -198,9 +198,15 @@ static __device__ __noinline__ bool epa_face_inside(V3 A, V3 B, V3 C) {
   return is_inside || dot(proj, proj) < tol * tol;
 }
 
-// Face::new (epa3.rs:90-118): writes face `fid`, returns whether the origin projects inside it.
+// Face::new (epa3.rs:90-118): writes face `fid`; returns whether the origin projects inside it and
+// the face's distance from the origin along its normal, measured at its first vertex (the value the
+// expansion loop pushes on the heap).
+struct NewFace {
+  float dist;
+  bool inside;
+};
 template <class WS>
-static __device__ __noinline__ bool epa_new_face(const WS& ws, int fid, int p0, int p1, int p2, int a0, int a1, int a2) {
+static __device__ __noinline__ NewFace epa_new_face(const WS& ws, int fid, int p0, int p1, int p2, int a0, int a1, int a2) {
   V3 A = ws.vp(p0), B = ws.vp(p1), C = ws.vp(p2);
   bool inside = epa_face_inside(A, B, C);
   V3 n;
@@ -210,7 +216,7 @@ static __device__ __noinline__ bool epa_new_face(const WS& ws, int fid, int p0, 
   ws.w(o + 1) = (uint32_t)a0 | ((uint32_t)a1 << 16);
   ws.w(o + 2) = (uint32_t)a2;
   ws.f(o + 3) = n.x; ws.f(o + 4) = n.y; ws.f(o + 5) = n.z;
-  return inside;
+  return NewFace{dot(n, A), inside};
 }
 
 // Face::closest_points (epa3.rs:120-129) for the face with vertices (a, b, c).
@@ -269,10 +275,10 @@ __device__ __forceinline__ int epa_closest_points_t(const WS& ws, Sup sup, const
       ws.set_vert(1, t2);
       ws.set_vert(2, t1);
     }
-    bool in0 = epa_new_face(ws, 0, 0, 1, 2, 3, 1, 2);
-    bool in1 = epa_new_face(ws, 1, 1, 3, 2, 3, 2, 0);
-    bool in2 = epa_new_face(ws, 2, 0, 2, 3, 0, 1, 3);
-    bool in3 = epa_new_face(ws, 3, 0, 3, 1, 2, 1, 0);
+    bool in0 = epa_new_face(ws, 0, 0, 1, 2, 3, 1, 2).inside;
+    bool in1 = epa_new_face(ws, 1, 1, 3, 2, 3, 2, 0).inside;
+    bool in2 = epa_new_face(ws, 2, 0, 2, 3, 0, 1, 3).inside;
+    bool in3 = epa_new_face(ws, 3, 0, 3, 1, 2, 1, 0).inside;
     nfaces = 4;
     bool ins[4] = {in0, in1, in2, in3};
     for (int k = 0; k < 4; ++k) {
@@ -361,11 +367,11 @@ __device__ __forceinline__ int epa_closest_points_t(const WS& ws, Sup sup, const
       int new_id = nfaces;
       int pt1 = ws.pt(sfid, (opp + 2) % 3);
       int pt2 = ws.pt(sfid, (opp + 1) % 3);
-      bool inside = epa_new_face(ws, new_id, pt1, pt2, support_id, sfid, new_id + 1, new_id - 1);
+      const NewFace nf = epa_new_face(ws, new_id, pt1, pt2, support_id, sfid, new_id + 1, new_id - 1);
       ws.set_adj(sfid, (opp + 1) % 3, new_id);
       nfaces++;
-      if (inside) {
-        float dist = dot(ws.normal(new_id), ws.vp(ws.pt(new_id, 0)));
+      if (nf.inside) {
+        const float dist = nf.dist;  // dot(normal, first vertex), as Face::new's caller computes it
         if (dist < curr_dist) {
           epa_closest_points_of(ws, fpts[0], fpts[1], fpts[2], p1, p2);
           *n = fnormal;
