@@ -241,12 +241,16 @@ __device__ __forceinline__ int epa_next_ccw(const WS& ws, int fid, int id) {
 }
 
 template <class WS>
-__device__ __forceinline__ bool epa_can_be_seen_by(const WS& ws, int fid, int point, int opp) {
-  V3 p0 = ws.vp(ws.pt(fid, opp));
-  V3 p1 = ws.vp(ws.pt(fid, (opp + 1) % 3));
-  V3 p2 = ws.vp(ws.pt(fid, (opp + 2) % 3));
-  V3 pt = ws.vp(point);
+// `pt` is the point's position (the expansion's support point, in registers); the edge's two
+// vertices are read only when the plane test does not settle it.
+__device__ __forceinline__ bool epa_can_be_seen_by(const WS& ws, int fid, V3 pt, int opp) {
+  const uint32_t w0 = ws.w(ws.fo(fid));
+  const int i0 = (int)((w0 >> (8 * opp)) & 0xff);
+  V3 p0 = ws.vp(i0);
   if (dot(pt - p0, ws.normal(fid)) >= -GJK_EPS_TOL) return true;
+  const int o1 = (opp + 1) % 3, o2 = (opp + 2) % 3;
+  V3 p1 = ws.vp((int)((w0 >> (8 * o1)) & 0xff));
+  V3 p2 = ws.vp((int)((w0 >> (8 * o2)) & 0xff));
   float e = EPS * 100.0f;
   V3 c = cross(p2 - p1, pt - p1);
   return fabsf(dot(c, c)) <= e * e;
@@ -343,7 +347,7 @@ __device__ __forceinline__ int epa_closest_points_t(const WS& ws, Sup sup, const
       uint32_t e = ws.w(L::W_STACK + --sp);
       int id = (int)(e & 0xffff), opp = (int)(e >> 16);
       if (ws.deleted(id)) continue;
-      if (!epa_can_be_seen_by(ws, id, support_id, opp)) {
+      if (!epa_can_be_seen_by(ws, id, cso.p, opp)) {
         if (nsil >= L::MAX_SIL) return EPA_OVERFLOW;
         ws.w(L::W_SIL + nsil++) = (uint32_t)id | ((uint32_t)opp << 16);
       } else {
