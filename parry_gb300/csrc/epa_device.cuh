@@ -95,62 +95,61 @@ struct EpaHeap {
   const WS* ws;
   int len;
   static constexpr int H = WS::Layout::W_HEAP;
+  // an entry is (face id, distance bits), read and written as one 8-byte word pair
   __device__ __forceinline__ uint32_t id(int i) const { return ws->w(H + 2 * i); }
-  __device__ __forceinline__ float nd(int i) const { return ws->f(H + 2 * i + 1); }
-  __device__ __forceinline__ void put(int i, uint32_t fid, float d) const { ws->w(H + 2 * i) = fid; ws->f(H + 2 * i + 1) = d; }
+  __device__ __forceinline__ uint2 ent(int i) const { return *reinterpret_cast<const uint2*>(&ws->w(H + 2 * i)); }
+  __device__ __forceinline__ void put(int i, uint2 e) const { *reinterpret_cast<uint2*>(&ws->w(H + 2 * i)) = e; }
+  static __device__ __forceinline__ float dist_of(uint2 e) { return __uint_as_float(e.y); }
   // FaceId::cmp: -1 / 0 / 1 (NaN -> 0)
   static __device__ __forceinline__ int cmp(float a, float b) { return a < b ? -1 : (a > b ? 1 : 0); }
-  __device__ int sift_up(int start, int pos) {
-    uint32_t eid = id(pos);
-    float ed = nd(pos);
+  // BinaryHeap::sift_up of entry e, held in registers, from slot pos
+  __device__ int sift_up(int start, int pos, uint2 e) {
+    const float ed = dist_of(e);
     while (pos > start) {
       int parent = (pos - 1) / 2;
-      if (cmp(ed, nd(parent)) <= 0) break;
-      put(pos, id(parent), nd(parent));
+      const uint2 pe = ent(parent);
+      if (cmp(ed, dist_of(pe)) <= 0) break;
+      put(pos, pe);
       pos = parent;
     }
-    put(pos, eid, ed);
+    put(pos, e);
     return pos;
   }
   __device__ void push(uint32_t fid, float d) {
-    put(len, fid, d);
     int old = len;
     len += 1;
-    sift_up(0, old);
+    sift_up(0, old, make_uint2(fid, __float_as_uint(d)));
   }
-  __device__ void sift_down_to_bottom(int pos) {
+  // BinaryHeap::sift_down_to_bottom of entry e from slot pos
+  __device__ void sift_down_to_bottom(int pos, uint2 e) {
     int end = len, start = pos;
-    uint32_t eid = id(pos);
-    float ed = nd(pos);
     int child = 2 * pos + 1;
     while (end >= 2 && child <= end - 2) {
-      child += (cmp(nd(child), nd(child + 1)) <= 0) ? 1 : 0;
-      put(pos, id(child), nd(child));
+      const uint2 c0 = ent(child), c1 = ent(child + 1);
+      const bool right = cmp(dist_of(c0), dist_of(c1)) <= 0;
+      child += right ? 1 : 0;
+      put(pos, right ? c1 : c0);
       pos = child;
       child = 2 * pos + 1;
     }
     if (child == end - 1) {
-      put(pos, id(child), nd(child));
+      put(pos, ent(child));
       pos = child;
     }
-    put(pos, eid, ed);
-    sift_up(start, pos);
+    sift_up(start, pos, e);
   }
+  // BinaryHeap::pop: the last entry moves to the root and sinks
   __device__ bool pop(uint32_t* fid, float* d) {
     if (len == 0) return false;
     len -= 1;
-    uint32_t iid = id(len);
-    float idd = nd(len);
+    uint2 out = ent(len);
     if (len > 0) {
-      uint32_t rid = id(0);
-      float rd = nd(0);
-      put(0, iid, idd);
-      iid = rid;
-      idd = rd;
-      sift_down_to_bottom(0);
+      const uint2 root = ent(0);
+      sift_down_to_bottom(0, out);
+      out = root;
     }
-    *fid = iid;
-    *d = idd;
+    *fid = out.x;
+    *d = dist_of(out);
     return true;
   }
 };
