@@ -75,6 +75,24 @@ struct EpaWsT {
     else w(fo(fid) + 2) = (uint32_t)v;
   }
   __device__ __forceinline__ V3 normal(int fid) const { int o = fo(fid) + 3; return v3(f(o), f(o + 1), f(o + 2)); }
+  // words 0-5 of a face record (pts | deleted flag, adj0 | adj1, adj2, normal) in vector loads
+  struct Rec {
+    uint32_t w0, w1, w2;
+    V3 n;
+  };
+  __device__ __forceinline__ Rec rec(int fid) const {
+    if constexpr (L::FACE_WORDS == 8) {
+      const uint4 a = *reinterpret_cast<const uint4*>(base + fo(fid));
+      const uint2 b = *reinterpret_cast<const uint2*>(base + fo(fid) + 4);
+      return Rec{a.x, a.y, a.z, v3(__uint_as_float(a.w), __uint_as_float(b.x), __uint_as_float(b.y))};
+    } else {
+      const uint2* q = reinterpret_cast<const uint2*>(base + fo(fid));
+      const uint2 a = q[0], b = q[1], c = q[2];
+      return Rec{a.x, a.y, b.x, v3(__uint_as_float(b.y), __uint_as_float(c.x), __uint_as_float(c.y))};
+    }
+  }
+  // set_deleted for a face whose word 0 the caller already holds
+  __device__ __forceinline__ void set_deleted_word(int fid, uint32_t w0) const { w(fo(fid)) = w0 | 0x01000000u; }
 };
 using EpaWs = EpaWsT<EpaGlobalLayout>;
 // The workspace of slot `slot` in a pool of EPA_WORDS-word slots.
@@ -242,8 +260,7 @@ __device__ __forceinline__ int epa_next_ccw(const WS& ws, int fid, int id) {
 template <class WS>
 // `pt` is the point's position (the expansion's support point, in registers); the edge's two
 // vertices are read only when the plane test does not settle it.
-__device__ __forceinline__ bool epa_can_be_seen_by(const WS& ws, int fid, V3 pt, int opp) {
-  const uint32_t w0 = ws.w(ws.fo(fid));
+__device__ __forceinline__ bool epa_can_be_seen_by(const WS& ws, int fid, uint32_t w0, V3 pt, int opp) {
   const int i0 = (int)((w0 >> (8 * opp)) & 0xff);
   V3 p0 = ws.vp(i0);
   if (dot(pt - p0, ws.normal(fid)) >= -GJK_EPS_TOL) return true;
@@ -314,12 +331,12 @@ __device__ __forceinline__ int epa_closest_points_t(const WS& ws, Sup sup, const
   float neg;
   while (heap.pop(&fid_u, &neg)) {
     int fid = (int)fid_u;
-    if (ws.deleted(fid)) continue;
+    const auto F = ws.rec(fid);  // copy of the popped face (its fields are modified below)
+    if (F.w0 >> 24) continue;     // deleted
     (*iters)++;
-    // copy of the popped face (its fields are modified below)
-    int fpts[3] = {ws.pt(fid, 0), ws.pt(fid, 1), ws.pt(fid, 2)};
-    int fadj[3] = {ws.adj(fid, 0), ws.adj(fid, 1), ws.adj(fid, 2)};
-    V3 fnormal = ws.normal(fid);
+    int fpts[3] = {(int)(F.w0 & 0xff), (int)((F.w0 >> 8) & 0xff), (int)((F.w0 >> 16) & 0xff)};
+    int fadj[3] = {(int)(F.w1 & 0xffff), (int)(F.w1 >> 16), (int)F.w2};
+    V3 fnormal = F.n;
     if (nverts >= L::MAX_VERTS) return EPA_OVERFLOW;
     CSO cso = sup(fnormal);
     int support_id = nverts;
@@ -333,7 +350,7 @@ __device__ __forceinline__ int epa_closest_points_t(const WS& ws, Sup sup, const
       return EPA_OK;
     }
     old_dist = curr_dist;
-    ws.set_deleted(fid);
+    ws.set_deleted_word(fid, F.w0);
     // silhouette: depth-first walk restated with an explicit stack (same visiting order)
     int nsil = 0;
     int sp = 0;
@@ -345,16 +362,17 @@ __device__ __forceinline__ int epa_closest_points_t(const WS& ws, Sup sup, const
     while (sp > 0) {
       uint32_t e = ws.w(L::W_STACK + --sp);
       int id = (int)(e & 0xffff), opp = (int)(e >> 16);
-      if (ws.deleted(id)) continue;
-      if (!epa_can_be_seen_by(ws, id, cso.p, opp)) {
+      const uint32_t w0 = ws.w(ws.fo(id));
+      if (w0 >> 24) continue;  // deleted
+      if (!epa_can_be_seen_by(ws, id, w0, cso.p, opp)) {
         if (nsil >= L::MAX_SIL) return EPA_OVERFLOW;
         ws.w(L::W_SIL + nsil++) = (uint32_t)id | ((uint32_t)opp << 16);
       } else {
-        ws.set_deleted(id);
+        ws.set_deleted_word(id, w0);
         int a1 = (opp + 2) % 3, a2 = opp;
         int adj1 = ws.adj(id, a1), adj2 = ws.adj(id, a2);
-        int o1 = epa_next_ccw(ws, adj1, ws.pt(id, a1));
-        int o2 = epa_next_ccw(ws, adj2, ws.pt(id, a2));
+        int o1 = epa_next_ccw(ws, adj1, (int)((w0 >> (8 * a1)) & 0xff));
+        int o2 = epa_next_ccw(ws, adj2, (int)((w0 >> (8 * a2)) & 0xff));
         if (sp + 2 > L::STACK) return EPA_OVERFLOW;
         ws.w(L::W_STACK + sp++) = (uint32_t)adj2 | ((uint32_t)o2 << 16);
         ws.w(L::W_STACK + sp++) = (uint32_t)adj1 | ((uint32_t)o1 << 16);
