@@ -93,6 +93,12 @@ struct EpaWsT {
   }
   // set_deleted for a face whose word 0 the caller already holds
   __device__ __forceinline__ void set_deleted_word(int fid, uint32_t w0) const { w(fo(fid)) = w0 | 0x01000000u; }
+  // set_adj for a face whose word 1 the caller already holds
+  __device__ __forceinline__ void set_adj_held(int fid, int k, int v, uint32_t w1) const {
+    if (k == 0) w(fo(fid) + 1) = (w1 & 0xffff0000u) | (uint32_t)v;
+    else if (k == 1) w(fo(fid) + 1) = (w1 & 0xffffu) | ((uint32_t)v << 16);
+    else w(fo(fid) + 2) = (uint32_t)v;
+  }
 };
 using EpaWs = EpaWsT<EpaGlobalLayout>;
 // The workspace of slot `slot` in a pool of EPA_WORDS-word slots.
@@ -260,10 +266,10 @@ __device__ __forceinline__ int epa_next_ccw(const WS& ws, int fid, int id) {
 template <class WS>
 // `pt` is the point's position (the expansion's support point, in registers); the edge's two
 // vertices are read only when the plane test does not settle it.
-__device__ __forceinline__ bool epa_can_be_seen_by(const WS& ws, int fid, uint32_t w0, V3 pt, int opp) {
+__device__ __forceinline__ bool epa_can_be_seen_by(const WS& ws, uint32_t w0, V3 fn, V3 pt, int opp) {
   const int i0 = (int)((w0 >> (8 * opp)) & 0xff);
   V3 p0 = ws.vp(i0);
-  if (dot(pt - p0, ws.normal(fid)) >= -GJK_EPS_TOL) return true;
+  if (dot(pt - p0, fn) >= -GJK_EPS_TOL) return true;
   const int o1 = (opp + 1) % 3, o2 = (opp + 2) % 3;
   V3 p1 = ws.vp((int)((w0 >> (8 * o1)) & 0xff));
   V3 p2 = ws.vp((int)((w0 >> (8 * o2)) & 0xff));
@@ -362,17 +368,18 @@ __device__ __forceinline__ int epa_closest_points_t(const WS& ws, Sup sup, const
     while (sp > 0) {
       uint32_t e = ws.w(L::W_STACK + --sp);
       int id = (int)(e & 0xffff), opp = (int)(e >> 16);
-      const uint32_t w0 = ws.w(ws.fo(id));
-      if (w0 >> 24) continue;  // deleted
-      if (!epa_can_be_seen_by(ws, id, w0, cso.p, opp)) {
+      const auto R = ws.rec(id);
+      if (R.w0 >> 24) continue;  // deleted
+      if (!epa_can_be_seen_by(ws, R.w0, R.n, cso.p, opp)) {
         if (nsil >= L::MAX_SIL) return EPA_OVERFLOW;
         ws.w(L::W_SIL + nsil++) = (uint32_t)id | ((uint32_t)opp << 16);
       } else {
-        ws.set_deleted_word(id, w0);
+        ws.set_deleted_word(id, R.w0);
         int a1 = (opp + 2) % 3, a2 = opp;
-        int adj1 = ws.adj(id, a1), adj2 = ws.adj(id, a2);
-        int o1 = epa_next_ccw(ws, adj1, (int)((w0 >> (8 * a1)) & 0xff));
-        int o2 = epa_next_ccw(ws, adj2, (int)((w0 >> (8 * a2)) & 0xff));
+        auto adj_of = [&](int k) { return k == 0 ? (int)(R.w1 & 0xffff) : (k == 1 ? (int)(R.w1 >> 16) : (int)R.w2); };
+        int adj1 = adj_of(a1), adj2 = adj_of(a2);
+        int o1 = epa_next_ccw(ws, adj1, (int)((R.w0 >> (8 * a1)) & 0xff));
+        int o2 = epa_next_ccw(ws, adj2, (int)((R.w0 >> (8 * a2)) & 0xff));
         if (sp + 2 > L::STACK) return EPA_OVERFLOW;
         ws.w(L::W_STACK + sp++) = (uint32_t)adj2 | ((uint32_t)o2 << 16);
         ws.w(L::W_STACK + sp++) = (uint32_t)adj1 | ((uint32_t)o1 << 16);
@@ -383,13 +390,14 @@ __device__ __forceinline__ int epa_closest_points_t(const WS& ws, Sup sup, const
     for (int s = 0; s < nsil; ++s) {
       uint32_t e = ws.w(L::W_SIL + s);
       int sfid = (int)(e & 0xffff), opp = (int)(e >> 16);
-      if (ws.deleted(sfid)) continue;
+      const uint2 w01 = *reinterpret_cast<const uint2*>(&ws.w(ws.fo(sfid)));  // pts | deleted, adj0 | adj1
+      if (w01.x >> 24) continue;  // deleted
       if (nfaces >= L::MAX_FACES || heap.len >= L::MAX_FACES) return EPA_OVERFLOW;
       int new_id = nfaces;
-      int pt1 = ws.pt(sfid, (opp + 2) % 3);
-      int pt2 = ws.pt(sfid, (opp + 1) % 3);
+      int pt1 = (int)((w01.x >> (8 * ((opp + 2) % 3))) & 0xff);
+      int pt2 = (int)((w01.x >> (8 * ((opp + 1) % 3))) & 0xff);
       const NewFace nf = epa_new_face(ws, new_id, pt1, pt2, support_id, sfid, new_id + 1, new_id - 1);
-      ws.set_adj(sfid, (opp + 1) % 3, new_id);
+      ws.set_adj_held(sfid, (opp + 1) % 3, new_id, w01.y);
       nfaces++;
       if (nf.inside) {
         const float dist = nf.dist;  // dot(normal, first vertex), as Face::new's caller computes it
