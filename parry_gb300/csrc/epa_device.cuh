@@ -51,9 +51,10 @@ struct EpaWsT {
   // vertices
   __device__ __forceinline__ void set_vert(int v, const CSO& c) const {
     *reinterpret_cast<float4*>(base + L::W_VP + 4 * v) = make_float4(c.p.x, c.p.y, c.p.z, 0.0f);
-    int o = L::W_VO + 6 * v;
-    f(o) = c.o1.x; f(o + 1) = c.o1.y; f(o + 2) = c.o1.z;
-    f(o + 3) = c.o2.x; f(o + 4) = c.o2.y; f(o + 5) = c.o2.z;
+    float2* o = reinterpret_cast<float2*>(base + L::W_VO + 6 * v);  // 8-byte aligned: W_VO and 6 v are even
+    o[0] = make_float2(c.o1.x, c.o1.y);
+    o[1] = make_float2(c.o1.z, c.o2.x);
+    o[2] = make_float2(c.o2.y, c.o2.z);
   }
   __device__ __forceinline__ V3 vp(int v) const {
     float4 q = *reinterpret_cast<const float4*>(base + L::W_VP + 4 * v);
@@ -89,6 +90,18 @@ struct EpaWsT {
       const uint2* q = reinterpret_cast<const uint2*>(base + fo(fid));
       const uint2 a = q[0], b = q[1], c = q[2];
       return Rec{a.x, a.y, b.x, v3(__uint_as_float(b.y), __uint_as_float(c.x), __uint_as_float(c.y))};
+    }
+  }
+  // writes words 0-5 of a face record in vector stores
+  __device__ __forceinline__ void put_rec(int fid, uint32_t w0, uint32_t w1, uint32_t w2, V3 n) const {
+    if constexpr (L::FACE_WORDS == 8) {
+      *reinterpret_cast<uint4*>(base + fo(fid)) = make_uint4(w0, w1, w2, __float_as_uint(n.x));
+      *reinterpret_cast<uint2*>(base + fo(fid) + 4) = make_uint2(__float_as_uint(n.y), __float_as_uint(n.z));
+    } else {
+      uint2* q = reinterpret_cast<uint2*>(base + fo(fid));
+      q[0] = make_uint2(w0, w1);
+      q[1] = make_uint2(w2, __float_as_uint(n.x));
+      q[2] = make_uint2(__float_as_uint(n.y), __float_as_uint(n.z));
     }
   }
   // set_deleted for a face whose word 0 the caller already holds
@@ -234,11 +247,7 @@ static __device__ __noinline__ NewFace epa_new_face(const WS& ws, int fid, int p
   bool inside = epa_face_inside(A, B, C);
   V3 n;
   if (!try_normalize(cross(B - A, C - A), EPS, &n)) n = v3(0.f, 0.f, 0.f);
-  int o = ws.fo(fid);
-  ws.w(o) = (uint32_t)p0 | ((uint32_t)p1 << 8) | ((uint32_t)p2 << 16);
-  ws.w(o + 1) = (uint32_t)a0 | ((uint32_t)a1 << 16);
-  ws.w(o + 2) = (uint32_t)a2;
-  ws.f(o + 3) = n.x; ws.f(o + 4) = n.y; ws.f(o + 5) = n.z;
+  ws.put_rec(fid, (uint32_t)p0 | ((uint32_t)p1 << 8) | ((uint32_t)p2 << 16), (uint32_t)a0 | ((uint32_t)a1 << 16), (uint32_t)a2, n);
   return NewFace{dot(n, A), inside};
 }
 
