@@ -266,13 +266,6 @@ __device__ __forceinline__ void epa_face_closest_points(const WS& ws, int fid, V
 }
 
 template <class WS>
-__device__ __forceinline__ int epa_next_ccw(const WS& ws, int fid, int id) {
-  if (ws.pt(fid, 0) == id) return 1;
-  if (ws.pt(fid, 1) == id) return 2;
-  return 0;
-}
-
-template <class WS>
 // `pt` is the point's position (the expansion's support point, in registers); the edge's two
 // vertices are read only when the plane test does not settle it.
 __device__ __forceinline__ bool epa_can_be_seen_by(const WS& ws, uint32_t w0, V3 fn, V3 pt, int opp) {
@@ -366,19 +359,23 @@ __device__ __forceinline__ int epa_closest_points_t(const WS& ws, Sup sup, const
     }
     old_dist = curr_dist;
     ws.set_deleted_word(fid, F.w0);
-    // silhouette: depth-first walk restated with an explicit stack (same visiting order)
+    // silhouette: depth-first walk restated with an explicit stack (same visiting order). An entry
+    // holds the face and the vertex whose next_ccw gives the opposite corner, resolved when the entry
+    // is popped and the face's record read anyway (a face's corners never change).
     int nsil = 0;
     int sp = 0;
-    for (int k = 2; k >= 0; --k) {
-      int a = fadj[k];
-      int o = epa_next_ccw(ws, a, fpts[k]);
-      ws.w(L::W_STACK + sp++) = (uint32_t)a | ((uint32_t)o << 16);
-    }
+    auto next_ccw_of = [](uint32_t w0, int vid) {
+      if ((int)(w0 & 0xff) == vid) return 1;
+      if ((int)((w0 >> 8) & 0xff) == vid) return 2;
+      return 0;
+    };
+    for (int k = 2; k >= 0; --k) ws.w(L::W_STACK + sp++) = (uint32_t)fadj[k] | ((uint32_t)fpts[k] << 16);
     while (sp > 0) {
       uint32_t e = ws.w(L::W_STACK + --sp);
-      int id = (int)(e & 0xffff), opp = (int)(e >> 16);
+      int id = (int)(e & 0xffff);
       const auto R = ws.rec(id);
       if (R.w0 >> 24) continue;  // deleted
+      const int opp = next_ccw_of(R.w0, (int)(e >> 16));
       if (!epa_can_be_seen_by(ws, R.w0, R.n, cso.p, opp)) {
         if (nsil >= L::MAX_SIL) return EPA_OVERFLOW;
         ws.w(L::W_SIL + nsil++) = (uint32_t)id | ((uint32_t)opp << 16);
@@ -387,11 +384,9 @@ __device__ __forceinline__ int epa_closest_points_t(const WS& ws, Sup sup, const
         int a1 = (opp + 2) % 3, a2 = opp;
         auto adj_of = [&](int k) { return k == 0 ? (int)(R.w1 & 0xffff) : (k == 1 ? (int)(R.w1 >> 16) : (int)R.w2); };
         int adj1 = adj_of(a1), adj2 = adj_of(a2);
-        int o1 = epa_next_ccw(ws, adj1, (int)((R.w0 >> (8 * a1)) & 0xff));
-        int o2 = epa_next_ccw(ws, adj2, (int)((R.w0 >> (8 * a2)) & 0xff));
         if (sp + 2 > L::STACK) return EPA_OVERFLOW;
-        ws.w(L::W_STACK + sp++) = (uint32_t)adj2 | ((uint32_t)o2 << 16);
-        ws.w(L::W_STACK + sp++) = (uint32_t)adj1 | ((uint32_t)o1 << 16);
+        ws.w(L::W_STACK + sp++) = (uint32_t)adj2 | (((R.w0 >> (8 * a2)) & 0xffu) << 16);
+        ws.w(L::W_STACK + sp++) = (uint32_t)adj1 | (((R.w0 >> (8 * a1)) & 0xffu) << 16);
       }
     }
     int first_new = nfaces;
