@@ -27,9 +27,9 @@ struct EpaLayout {
   static constexpr int W_VO = W_VP + 4 * MV;              // 6 words per vertex: witness points orig1, orig2
   static constexpr int W_FACES = W_VO + 6 * MV;           // FW words per face
   static constexpr int W_HEAP = W_FACES + FW * MF;        // 2 words per heap entry
-  static constexpr int W_SIL = W_HEAP + 2 * MF;           // 1 word per silhouette edge
-  static constexpr int W_STACK = W_SIL + MS;              // 1 word per stack entry
-  static constexpr int WORDS = W_STACK + MSTK;            // words per workspace
+  static constexpr int WORDS = W_HEAP + 2 * MF;           // words per workspace (the silhouette walk's
+                                                          // stack and edge list live in the thread's
+                                                          // local memory: MS and MSTK entries)
   static_assert(FW != 8 || (W_FACES % 8 == 0 && WORDS % 8 == 0), "faces and slots start on 32-byte boundaries");
   static_assert(FW == 8 || FW == 6, "face records of 8 or 6 words");
 };
@@ -364,35 +364,36 @@ __device__ __forceinline__ int epa_closest_points_t(const WS& ws, Sup sup, const
     // is popped and the face's record read anyway (a face's corners never change).
     int nsil = 0;
     int sp = 0;
+    uint32_t stk[L::STACK], sil[L::MAX_SIL];  // local memory: a warp's lanes touch the same few slots
     auto next_ccw_of = [](uint32_t w0, int vid) {
       if ((int)(w0 & 0xff) == vid) return 1;
       if ((int)((w0 >> 8) & 0xff) == vid) return 2;
       return 0;
     };
-    for (int k = 2; k >= 0; --k) ws.w(L::W_STACK + sp++) = (uint32_t)fadj[k] | ((uint32_t)fpts[k] << 16);
+    for (int k = 2; k >= 0; --k) stk[sp++] = (uint32_t)fadj[k] | ((uint32_t)fpts[k] << 16);
     while (sp > 0) {
-      uint32_t e = ws.w(L::W_STACK + --sp);
+      uint32_t e = stk[--sp];
       int id = (int)(e & 0xffff);
       const auto R = ws.rec(id);
       if (R.w0 >> 24) continue;  // deleted
       const int opp = next_ccw_of(R.w0, (int)(e >> 16));
       if (!epa_can_be_seen_by(ws, R.w0, R.n, cso.p, opp)) {
         if (nsil >= L::MAX_SIL) return EPA_OVERFLOW;
-        ws.w(L::W_SIL + nsil++) = (uint32_t)id | ((uint32_t)opp << 16);
+        sil[nsil++] = (uint32_t)id | ((uint32_t)opp << 16);
       } else {
         ws.set_deleted_word(id, R.w0);
         int a1 = (opp + 2) % 3, a2 = opp;
         auto adj_of = [&](int k) { return k == 0 ? (int)(R.w1 & 0xffff) : (k == 1 ? (int)(R.w1 >> 16) : (int)R.w2); };
         int adj1 = adj_of(a1), adj2 = adj_of(a2);
         if (sp + 2 > L::STACK) return EPA_OVERFLOW;
-        ws.w(L::W_STACK + sp++) = (uint32_t)adj2 | (((R.w0 >> (8 * a2)) & 0xffu) << 16);
-        ws.w(L::W_STACK + sp++) = (uint32_t)adj1 | (((R.w0 >> (8 * a1)) & 0xffu) << 16);
+        stk[sp++] = (uint32_t)adj2 | (((R.w0 >> (8 * a2)) & 0xffu) << 16);
+        stk[sp++] = (uint32_t)adj1 | (((R.w0 >> (8 * a1)) & 0xffu) << 16);
       }
     }
     int first_new = nfaces;
     if (nsil == 0) return EPA_NONE;
     for (int s = 0; s < nsil; ++s) {
-      uint32_t e = ws.w(L::W_SIL + s);
+      uint32_t e = sil[s];
       int sfid = (int)(e & 0xffff), opp = (int)(e >> 16);
       const uint2 w01 = *reinterpret_cast<const uint2*>(&ws.w(ws.fo(sfid)));  // pts | deleted, adj0 | adj1
       if (w01.x >> 24) continue;  // deleted
