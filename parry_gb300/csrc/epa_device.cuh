@@ -26,10 +26,11 @@ struct EpaLayout {
   static constexpr int W_VP = 0;                          // 4 words per vertex: CSO point (x, y, z, -)
   static constexpr int W_VO = W_VP + 4 * MV;              // 6 words per vertex: witness points orig1, orig2
   static constexpr int W_FACES = W_VO + 6 * MV;           // FW words per face
-  static constexpr int W_HEAP = W_FACES + FW * MF;        // 2 words per heap entry
-  static constexpr int WORDS = W_HEAP + 2 * MF;           // words per workspace (the silhouette walk's
-                                                          // stack and edge list live in the thread's
-                                                          // local memory: MS and MSTK entries)
+  // the heap (MF entries of 2 words) lives in the thread's local memory up to 1,024 entries, else at
+  // the end of the workspace; the silhouette walk's stack and edge list (MSTK, MS) in local memory
+  static constexpr bool HEAP_LOCAL = MF <= 1024;
+  static constexpr int W_HEAP = W_FACES + FW * MF;
+  static constexpr int WORDS = W_HEAP + (HEAP_LOCAL ? 0 : 2 * MF);  // words per workspace
   static_assert(FW != 8 || (W_FACES % 8 == 0 && WORDS % 8 == 0), "faces and slots start on 32-byte boundaries");
   static_assert(FW == 8 || FW == 6, "face records of 8 or 6 words");
 };
@@ -129,13 +130,11 @@ __device__ __forceinline__ EpaWsBig epa_slot_big(uint32_t* pool, uint32_t slot) 
 
 template <class WS>
 struct EpaHeap {
-  const WS* ws;
+  uint2* h;  // (face id, distance bits) per entry, in the thread's local memory
   int len;
-  static constexpr int H = WS::Layout::W_HEAP;
-  // an entry is (face id, distance bits), read and written as one 8-byte word pair
-  __device__ __forceinline__ uint32_t id(int i) const { return ws->w(H + 2 * i); }
-  __device__ __forceinline__ uint2 ent(int i) const { return *reinterpret_cast<const uint2*>(&ws->w(H + 2 * i)); }
-  __device__ __forceinline__ void put(int i, uint2 e) const { *reinterpret_cast<uint2*>(&ws->w(H + 2 * i)) = e; }
+  __device__ __forceinline__ uint32_t id(int i) const { return h[i].x; }
+  __device__ __forceinline__ uint2 ent(int i) const { return h[i]; }
+  __device__ __forceinline__ void put(int i, uint2 e) const { h[i] = e; }
   static __device__ __forceinline__ float dist_of(uint2 e) { return __uint_as_float(e.y); }
   // FaceId::cmp: -1 / 0 / 1 (NaN -> 0)
   static __device__ __forceinline__ int cmp(float a, float b) { return a < b ? -1 : (a > b ? 1 : 0); }
@@ -292,7 +291,10 @@ __device__ __forceinline__ int epa_closest_points_t(const WS& ws, Sup sup, const
   int nverts = simplex.dim + 1;
   for (int i = 0; i < nverts; ++i) ws.set_vert(i, simplex.v[i]);
   int nfaces = 0;
-  EpaHeap<WS> heap{&ws, 0};
+  // the heap in local memory (interleaved across a warp's lanes, whose sifts touch the same top
+  // slots), or for large capacities in the workspace
+  uint2 heap_local[L::HEAP_LOCAL ? L::MAX_FACES : 1];
+  EpaHeap<WS> heap{L::HEAP_LOCAL ? heap_local : reinterpret_cast<uint2*>(&ws.w(L::W_HEAP)), 0};
   if (simplex.dim == 0) {
     *p1 = v3(0.f, 0.f, 0.f); *p2 = v3(0.f, 0.f, 0.f); *n = v3(0.f, 1.f, 0.f);
     return EPA_OK;
