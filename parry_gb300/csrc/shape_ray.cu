@@ -878,95 +878,188 @@ __global__ void __launch_bounds__(128) k_rays_wave(const WideNode* __restrict__ 
 // kernels publish hits through the per-ray key and k_rays_finish writes the winners. A ray whose
 // candidates overflow a list is marked for the single-kernel cast. Does nothing when the grid is
 // unusable (the BVH wave kernel casts the rays then).
+// Per-warp staging of the grid walk's appends to a two-ended list: a warp's entries gather in shared
+// memory (front kind from slot 0 up, back kind from the last slot down) and reach the global list in
+// batches of up to WALK_STAGE, one counter update per batch. The lanes of a walk rarely append in
+// the same loop turn, so appending one group of lanes at a time cost one contended atomic on the
+// list's counter per 1-5 entries. Every live lane of the warp takes part in each put and flush, so
+// the held counts (n0, n1) and the overflow bits are the same in all of them.
+constexpr uint32_t WALK_STAGE = 32;
+struct WalkStage {
+  RayCand* e;      // this warp's WALK_STAGE shared-memory slots
+  uint32_t n0, n1;  // front / back entries held
+};
+
+// Writes the held entries to the list and empties the stage. A batch that does not fit is not
+// written: its first-failure snapshot is kept (as by append_slot2) and the owners of its entries
+// (lane = k mod 32) are returned as overflow bits.
+__device__ __forceinline__ uint32_t walk_stage_flush(WalkStage& st, unsigned live, unsigned long long* counter, unsigned long long cap,
+                                                     unsigned long long* fail, RayCand* __restrict__ list) {
+  const uint32_t n0 = st.n0, n1 = st.n1;
+  if (n0 + n1 == 0u) return 0u;
+  const uint32_t lane = threadIdx.x & 31u, leader = (uint32_t)__ffs(live) - 1u;
+  const uint32_t rank = (uint32_t)__popc(live & ((1u << lane) - 1u)), size = (uint32_t)__popc(live);
+  unsigned long long base = 0;
+  if (lane == leader) base = atomicAdd(counter, (unsigned long long)n0 | ((unsigned long long)n1 << 32));
+  base = __shfl_sync(live, base, leader);
+  const unsigned long long lo = base & 0xffffffffull, hi = base >> 32;
+  uint32_t bits = 0u;
+  if (lo + hi + n0 + n1 > cap) {
+    if (lane == leader) atomicMin(fail, base);
+    for (uint32_t i = rank; i < n0; i += size) bits |= 1u << (st.e[i].k & 31u);
+    for (uint32_t i = rank; i < n1; i += size) bits |= 1u << (st.e[WALK_STAGE - 1u - i].k & 31u);
+  } else {
+    for (uint32_t i = rank; i < n0; i += size) list[lo + i] = st.e[i];
+    for (uint32_t i = rank; i < n1; i += size) list[cap - 1ull - (hi + i)] = st.e[WALK_STAGE - 1u - i];
+  }
+  __syncwarp(live);  // the slots are read before they are refilled
+  st.n0 = 0u;
+  st.n1 = 0u;
+  return __reduce_or_sync(live, bits);
+}
+
+// Adds the entry of each lane with `add` (kind 0 front, 1 back); flushes first if they do not fit.
+__device__ __forceinline__ uint32_t walk_stage_put(WalkStage& st, unsigned live, bool add, uint32_t kind, const RayCand& c,
+                                                   unsigned long long* counter, unsigned long long cap, unsigned long long* fail,
+                                                   RayCand* __restrict__ list) {
+  const unsigned want = __ballot_sync(live, add), back = __ballot_sync(live, add && kind != 0u);
+  const uint32_t m1 = (uint32_t)__popc(back), m0 = (uint32_t)__popc(want) - m1;
+  uint32_t bits = 0u;
+  if (st.n0 + st.n1 + m0 + m1 > WALK_STAGE) bits = walk_stage_flush(st, live, counter, cap, fail, list);
+  if (add) {
+    const unsigned lt = (1u << (threadIdx.x & 31u)) - 1u;
+    const uint32_t idx = kind ? WALK_STAGE - 1u - (st.n1 + (uint32_t)__popc(back & lt)) : st.n0 + (uint32_t)__popc(want & ~back & lt);
+    st.e[idx] = c;
+  }
+  __syncwarp(live);  // the entries are in place before any lane flushes them
+  st.n0 += m0;
+  st.n1 += m1;
+  return bits;
+}
+
 __global__ void __launch_bounds__(128) k_rays_walk(CompoundDev cd, const float* __restrict__ rays, uint32_t n, float max_toi, int has_pose,
                                                    Pose cpose, uint32_t* __restrict__ part_out, float* __restrict__ toi_out,
                                                    float* __restrict__ normal_out, const uint32_t* __restrict__ order, int permuted,
                                                    WaveBufs wb, const GridDev* __restrict__ grid, const uint32_t* __restrict__ starts,
                                                    const GridEntry* __restrict__ entries) {
+  __shared__ RayCand stage_mem[2][4][WALK_STAGE];  // lists B and C, per warp of the 128-thread block
   const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= n || grid->ok == 0u) return;
+  const bool mine = k < n && grid->ok != 0u;
+  const unsigned live = __ballot_sync(0xffffffffu, mine);
+  if (!mine) return;
+  const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
+  WalkStage st_b{stage_mem[0][warp], 0u, 0u}, st_c{stage_mem[1][warp], 0u, 0u};
+  uint32_t ovf_bits = 0u;
   uint32_t r;
   V3 o, dir;
   ray_of(rays, order, permuted, k, has_pose, cpose, &r, &o, &dir);
   const uint32_t zmask = (dir.x == 0.0f ? 1u : 0u) | (dir.y == 0.0f ? 2u : 0u) | (dir.z == 0.0f ? 4u : 0u);
   const V3 inv = v3(dir.x != 0.0f ? 1.0f / dir.x : 0.0f, dir.y != 0.0f ? 1.0f / dir.y : 0.0f, dir.z != 0.0f ? 1.0f / dir.z : 0.0f);
-  bool overflow = false;
   uint32_t near_part = 0xffffffffu, near_ty = 0u;
   float near_tmin = FLT_MAX;
   const GridDev g = *grid;
   const float3 glo = make_float3(g.lo[0], g.lo[1], g.lo[2]);
   const float3 ghi = make_float3(g.lo[0] + g.cell[0] * (float)g.res[0], g.lo[1] + g.cell[1] * (float)g.res[1], g.lo[2] + g.cell[2] * (float)g.res[2]);
   const float t0 = slab(glo, ghi, o, inv, zmask, max_toi);
-  if (t0 != FLT_MAX) {
-    uint32_t cx = grid_coord(g, 0, o.x + dir.x * t0), cy = grid_coord(g, 1, o.y + dir.y * t0), cz = grid_coord(g, 2, o.z + dir.z * t0);
-    uint32_t s0 = 0xffffffffu, s1 = 0xffffffffu, s2 = 0xffffffffu, s3 = 0xffffffffu;  // the last parts met
-    auto cross_t = [&](int a, uint32_t ci, float oa, float da, float ia) {
-      if (zmask & (1u << a)) return FLT_MAX;
-      const float b = g.lo[a] + g.cell[a] * (float)(da > 0.0f ? ci + 1u : ci);
-      return (b - oa) * ia;
-    };
-    size_t cell = ((size_t)cz * g.res[1] + cy) * g.res[0] + cx;
-    uint32_t j = starts[cell], e1 = starts[cell + 1];
-    // One loop turn tests one entry of the current cell, or steps to the next cell: lanes whose
-    // cells hold different numbers of entries stay in step.
-    for (;;) {
-      if (j < e1) {
-        const float4 ea = __ldg(reinterpret_cast<const float4*>(entries + j));
-        const float4 eb = __ldg(reinterpret_cast<const float4*>(entries + j) + 1);
-        ++j;
-        const uint32_t part = __float_as_uint(ea.w);
-        if (part == s0 || part == s1 || part == s2 || part == s3) continue;  // met in an earlier cell
-        s3 = s2;
-        s2 = s1;
-        s1 = s0;
-        s0 = part;
-        float ts = slab(make_float3(ea.x, ea.y, ea.z), make_float3(eb.x, eb.y, eb.z), o, inv, zmask, max_toi);
-        if (ts == FLT_MAX || !(ts < max_toi) || overflow) continue;
-        const uint32_t ty = __float_as_uint(eb.w);
-        if (analytic_type(ty)) {
-          const unsigned long long slot = append_slot2(wb.count + 8, wb.cap, ty == SH_BALL ? 0u : 1u, wb.count + 9);
-          if (slot != ~0ull) wb.c[slot] = RayCand{k, r, part, 0u, ts, 0.f, 0.f, 0.f, 0.f, 0.f};
-          else overflow = true;
-          continue;
-        }
-        float t_box;
-        if (!local_box_may_hit(cd, part, ty, o, dir, max_toi, &t_box)) continue;
-        ts = fmaxf(ts, t_box);
-        uint32_t dpart = part, dty = ty;
-        float dt = ts;
-        if (ts < near_tmin) {
-          dpart = near_part;
-          dty = near_ty;
-          dt = near_tmin;
-          near_part = part;
-          near_ty = ty;
-          near_tmin = ts;
-        }
-        if (dpart != 0xffffffffu) {
-          const unsigned long long slot = append_slot2(wb.count, wb.cap, dty == SH_CAPSULE ? 0u : 1u, wb.count + 2);
-          if (slot != ~0ull) wb.b[slot] = RayCand{k, r, dpart, 0u, dt, 0.f, 0.f, 0.f, 0.f, 0.f};
-          else overflow = true;
-        }
-        continue;
-      }
-      const float tx = cross_t(0, cx, o.x, dir.x, inv.x), ty = cross_t(1, cy, o.y, dir.y, inv.y), tz = cross_t(2, cz, o.z, dir.z, inv.z);
-      const float tn = fminf(tx, fminf(ty, tz));
-      if (tn >= FLT_MAX || !(tn <= max_toi)) break;
-      if (tn == tx) {
-        if (dir.x > 0.0f) { if (++cx >= g.res[0]) break; }
-        else { if (cx == 0u) break; --cx; }
-      } else if (tn == ty) {
-        if (dir.y > 0.0f) { if (++cy >= g.res[1]) break; }
-        else { if (cy == 0u) break; --cy; }
-      } else {
-        if (dir.z > 0.0f) { if (++cz >= g.res[2]) break; }
-        else { if (cz == 0u) break; --cz; }
-      }
-      cell = ((size_t)cz * g.res[1] + cy) * g.res[0] + cx;
-      j = starts[cell];
-      e1 = starts[cell + 1];
-    }
+  bool walking = t0 != FLT_MAX;
+  uint32_t cx = 0u, cy = 0u, cz = 0u, j = 0u, e1 = 0u;
+  uint32_t s0 = 0xffffffffu, s1 = 0xffffffffu, s2 = 0xffffffffu, s3 = 0xffffffffu;  // the last parts met
+  auto cross_t = [&](int a, uint32_t ci, float oa, float da, float ia) {
+    if (zmask & (1u << a)) return FLT_MAX;
+    const float b = g.lo[a] + g.cell[a] * (float)(da > 0.0f ? ci + 1u : ci);
+    return (b - oa) * ia;
+  };
+  if (walking) {
+    cx = grid_coord(g, 0, o.x + dir.x * t0);
+    cy = grid_coord(g, 1, o.y + dir.y * t0);
+    cz = grid_coord(g, 2, o.z + dir.z * t0);
+    const size_t cell = ((size_t)cz * g.res[1] + cy) * g.res[0] + cx;
+    j = starts[cell];
+    e1 = starts[cell + 1];
   }
+  // One loop turn tests one entry of the current cell, or steps to the next cell: lanes whose cells
+  // hold different numbers of entries stay in step. Each turn ends at a point all live lanes reach,
+  // where the entries chosen in the turn go to the warp's stages.
+  for (;;) {
+    bool add_b = false, add_c = false;
+    uint32_t kind = 0u;
+    RayCand cand;
+    const bool overflow = (ovf_bits >> lane) & 1u;
+    if (walking) {
+      if (j < e1) {
+        do {
+          const float4 ea = __ldg(reinterpret_cast<const float4*>(entries + j));
+          const float4 eb = __ldg(reinterpret_cast<const float4*>(entries + j) + 1);
+          ++j;
+          const uint32_t part = __float_as_uint(ea.w);
+          if (part == s0 || part == s1 || part == s2 || part == s3) break;  // met in an earlier cell
+          s3 = s2;
+          s2 = s1;
+          s1 = s0;
+          s0 = part;
+          float ts = slab(make_float3(ea.x, ea.y, ea.z), make_float3(eb.x, eb.y, eb.z), o, inv, zmask, max_toi);
+          if (ts == FLT_MAX || !(ts < max_toi) || overflow) break;
+          const uint32_t ty = __float_as_uint(eb.w);
+          if (analytic_type(ty)) {
+            add_c = true;
+            kind = ty == SH_BALL ? 0u : 1u;
+            cand = RayCand{k, r, part, 0u, ts, 0.f, 0.f, 0.f, 0.f, 0.f};
+            break;
+          }
+          float t_box;
+          if (!local_box_may_hit(cd, part, ty, o, dir, max_toi, &t_box)) break;
+          ts = fmaxf(ts, t_box);
+          uint32_t dpart = part, dty = ty;
+          float dt = ts;
+          if (ts < near_tmin) {
+            dpart = near_part;
+            dty = near_ty;
+            dt = near_tmin;
+            near_part = part;
+            near_ty = ty;
+            near_tmin = ts;
+          }
+          if (dpart != 0xffffffffu) {
+            add_b = true;
+            kind = dty == SH_CAPSULE ? 0u : 1u;
+            cand = RayCand{k, r, dpart, 0u, dt, 0.f, 0.f, 0.f, 0.f, 0.f};
+          }
+        } while (false);
+      } else {
+        const float tx = cross_t(0, cx, o.x, dir.x, inv.x), ty = cross_t(1, cy, o.y, dir.y, inv.y), tz = cross_t(2, cz, o.z, dir.z, inv.z);
+        const float tn = fminf(tx, fminf(ty, tz));
+        bool out = tn >= FLT_MAX || !(tn <= max_toi);
+        if (!out) {
+          if (tn == tx) {
+            if (dir.x > 0.0f) out = ++cx >= g.res[0];
+            else if (cx == 0u) out = true;
+            else --cx;
+          } else if (tn == ty) {
+            if (dir.y > 0.0f) out = ++cy >= g.res[1];
+            else if (cy == 0u) out = true;
+            else --cy;
+          } else {
+            if (dir.z > 0.0f) out = ++cz >= g.res[2];
+            else if (cz == 0u) out = true;
+            else --cz;
+          }
+        }
+        if (out) {
+          walking = false;
+        } else {
+          const size_t cell = ((size_t)cz * g.res[1] + cy) * g.res[0] + cx;
+          j = starts[cell];
+          e1 = starts[cell + 1];
+        }
+      }
+    }
+    if (__any_sync(live, add_c)) ovf_bits |= walk_stage_put(st_c, live, add_c, kind, cand, wb.count + 8, wb.cap, wb.count + 9, wb.c);
+    if (__any_sync(live, add_b)) ovf_bits |= walk_stage_put(st_b, live, add_b, kind, cand, wb.count, wb.cap, wb.count + 2, wb.b);
+    if (!__any_sync(live, walking)) break;
+  }
+  ovf_bits |= walk_stage_flush(st_c, live, wb.count + 8, wb.cap, wb.count + 9, wb.c);
+  ovf_bits |= walk_stage_flush(st_b, live, wb.count, wb.cap, wb.count + 2, wb.b);
+  const bool overflow = (ovf_bits >> lane) & 1u;
   if (near_part != 0xffffffffu && !overflow) {
     const unsigned long long slot = append_slot2(wb.count + 1, n, near_ty == SH_CAPSULE ? 0u : 1u, nullptr);
     wb.a[slot] = RayCand{k, r, near_part, 0u, near_tmin, 0.f, 0.f, 0.f, 0.f, 0.f};

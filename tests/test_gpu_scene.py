@@ -212,6 +212,50 @@ def test_scene_ray_grid_matches_bvh_and_oracle(oracle_lib, giant):
     assert int((a["ray_part"] != pg.NO_HIT).sum()) > 300
 
 
+def test_scene_ray_grid_candidate_overflow(oracle_lib):
+    """A row of 800 balls, cuboids, capsules and hulls along every ray: the grid walk's candidate
+    lists (4 per ray + 1024 entries) overflow in its staged batches, and the affected rays are recast
+    by the single-kernel path. Same answers as the BVH path and the oracle."""
+    import parry_gb300 as pg
+    O = oracle_lib
+    s = pg.ShapeSet()
+    rng = np.random.default_rng(9)
+    pts = rng.normal(size=(24, 3))
+    pts /= np.linalg.norm(pts, axis=1, keepdims=True)
+    for i in range(800):
+        pose = (0.0, 0.0, 0.0, 1.0, 2.0 * i, 0.0, 0.0)
+        kind = i % 4
+        if kind == 0:
+            s.add_ball(0.45, pose)
+        elif kind == 1:
+            s.add_cuboid((0.3, 0.4, 0.35), pose)
+        elif kind == 2:
+            s.add_capsule(0.4, 0.3, pose)
+        else:
+            s.add_convex(pts * 0.5, pose)
+    n = 64
+    o = np.stack([np.full(n, -5.0), rng.uniform(-0.2, 0.2, n), rng.uniform(-0.2, 0.2, n)], 1)
+    d = np.tile([1.0, 0.0, 0.0], (n, 1)) + rng.normal(scale=1e-3, size=(n, 3))
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    rays = np.concatenate([o, d], 1).astype(np.float32)
+    vel = np.zeros((800, 6), np.float32)
+    out = []
+    for mode in (1, 2):
+        ctx = pg.Context(0, scene_ray_grid=mode)
+        sc = pg.Scene(ctx, s, vel, 0.1, 1 << 16)
+        sc.set_rays(rays, 2000.0)
+        sc.step(1.0 / 60.0, 2, use_graph=False)
+        out.append(sc.read())
+        sc.close()
+        ctx.close()
+    a, b = out
+    want = O.scene_frames(s, vel, 0.1, 1.0 / 60.0, 2, rays=rays, max_toi=2000.0)
+    for key in ("ray_part", "ray_toi", "ray_normal"):
+        np.testing.assert_array_equal(a[key], b[key])
+        np.testing.assert_array_equal(a[key], want[key])
+    assert np.all(a["ray_part"] != pg.NO_HIT)
+
+
 def test_scene_read_into_pinned_buffers(gpu_ctx):
     """Scene.read into caller-provided (pinned) buffers gives the same state as a fresh read."""
     import torch
