@@ -472,7 +472,7 @@ __device__ __forceinline__ bool capsule_may_hit(const CompoundDev& cd, uint32_t 
   const float4 prm = cd.params[part];
   const Pose p = load_pose(cd.poses, part);
   const V3 ol = pose_inv_point(p, o), dl = pose_inv_rotate(p, dir);
-  const double h = prm.x, rad = prm.y;
+  const double rad = prm.y;
   const double lim = rad + (double)gjk_ray_margin(prm.x + prm.y, ol);
   const double ex = dl.x, ez = dl.z, px = ol.x, pz = ol.z;
   const double den2 = ex * ex + ez * ez;
